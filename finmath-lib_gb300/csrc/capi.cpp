@@ -1,0 +1,794 @@
+// capi.cpp -- the C ABI: handles, device memory, validation and the call sequence of
+// finmath-lib's BrownianMotion / MonteCarloProcess / product API on the GPU.
+//
+// Device memory comes from the stream-ordered allocator with the default pool's release
+// threshold raised, so repeated create/destroy cycles (one per valuation in a service)
+// reuse HBM instead of returning it to the driver.
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "lmm_internal.h"
+
+namespace lmm {
+
+// ------------------------------------------------------------------ errors
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+int fail(int code, const std::string& msg)
+{
+    g_last_error = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what)
+{
+    g_last_error = std::string("CUDA error in ") + what + ": " + cudaGetErrorString(e);
+    if (e == cudaErrorMemoryAllocation) return LMM_ERR_NOMEM;
+    return LMM_ERR_CUDA;
+}
+
+// ------------------------------------------------------------------ stats
+static const char* kKernelNames[K_COUNT] = {
+    "mt19937_jump_generate", "lmm_paths_fp64", "lmm_paths_fp32", "numeraire_adjust_reduce", "swaption_value",
+    "bermudan_regress_step", "bermudan_solve6", "value_mean_stderr", "lmm_adjoint", "portfolio_persistent", "misc"};
+
+const char* kernel_name(int id) { return (id >= 0 && id < K_COUNT) ? kKernelNames[id] : "?"; }
+
+static std::atomic<int64_t> g_launches[K_COUNT];
+static std::atomic<bool> g_timing{false};
+struct PendingTiming {
+    int id;
+    cudaEvent_t start, stop;
+};
+static std::mutex g_timing_mu;
+static std::vector<PendingTiming> g_pending;
+static double g_total_ms[K_COUNT];
+
+bool timing_enabled() { return g_timing.load(); }
+
+KernelTimer::KernelTimer(int id_, cudaStream_t s, int launches) : id(id_), stream(s)
+{
+    g_launches[id] += launches;
+    if (g_timing.load()) {
+        if (cudaEventCreate(&start) == cudaSuccess) cudaEventRecord(start, stream);
+        else start = nullptr;
+    }
+}
+
+KernelTimer::~KernelTimer()
+{
+    if (!start) return;
+    cudaEvent_t stop = nullptr;
+    if (cudaEventCreate(&stop) != cudaSuccess) return;
+    cudaEventRecord(stop, stream);
+    std::lock_guard<std::mutex> lock(g_timing_mu);
+    g_pending.push_back({id, start, stop});
+}
+
+static void collect_timings()
+{
+    std::lock_guard<std::mutex> lock(g_timing_mu);
+    for (auto& t : g_pending) {
+        float ms = 0.0f;
+        if (cudaEventSynchronize(t.stop) == cudaSuccess && cudaEventElapsedTime(&ms, t.start, t.stop) == cudaSuccess)
+            g_total_ms[t.id] += ms;
+        cudaEventDestroy(t.start);
+        cudaEventDestroy(t.stop);
+    }
+    g_pending.clear();
+}
+
+// ------------------------------------------------------------------ device memory
+static int ensure_pool()
+{
+    static std::once_flag once;
+    static int rc = LMM_OK;
+    std::call_once(once, [] {
+        int dev = 0;
+        cudaMemPool_t pool;
+        if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetDefaultMemPool(&pool, dev) != cudaSuccess) {
+            rc = fail(LMM_ERR_CUDA, "no CUDA device / memory pool available");
+            return;
+        }
+        uint64_t thr = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    });
+    return rc;
+}
+
+template <typename T>
+static int dalloc(T** p, size_t count, cudaStream_t s)
+{
+    *p = nullptr;
+    if (count == 0) return LMM_OK;
+    void* v = nullptr;
+    cudaError_t e = cudaMallocAsync(&v, count * sizeof(T), s);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMallocAsync");
+    *p = static_cast<T*>(v);
+    return LMM_OK;
+}
+
+template <typename T>
+static void dfree(T*& p, cudaStream_t s)
+{
+    if (p) cudaFreeAsync((void*)p, s);
+    p = nullptr;
+}
+
+template <typename T>
+static int upload(T** d, const T* h, size_t count, cudaStream_t s)
+{
+    int rc = dalloc(d, count, s);
+    if (rc) return rc;
+    if (count) LMM_CUDA(cudaMemcpyAsync(*d, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+    return LMM_OK;
+}
+
+static int binary_search(const double* a, int n, double key)
+{
+    int lo = 0, hi = n - 1;
+    while (lo <= hi) {
+        const int mid = (int)(((unsigned)lo + (unsigned)hi) >> 1);
+        if (a[mid] < key) lo = mid + 1;
+        else if (a[mid] > key) hi = mid - 1;
+        else return mid;
+    }
+    return -(lo + 1);
+}
+
+static double round_to_tick(double t) { return std::rint(t / (1.0 / (365.0 * 24.0))) * (1.0 / (365.0 * 24.0)); }
+
+// TimeDiscretizationFromArray.getTimeIndex (:272-274)
+static int time_index(const std::vector<double>& grid, double t)
+{
+    return binary_search(grid.data(), (int)grid.size(), round_to_tick(t));
+}
+
+}  // namespace lmm
+
+using namespace lmm;
+
+// ------------------------------------------------------------------ handles
+struct lmm_brownian {
+    int T = 0, F = 0, P = 0, seed = 0, precision = 0;
+    std::vector<double> times;
+    cudaStream_t stream = nullptr;
+    RngPlan plan;
+    uint32_t* d_seeded = nullptr;
+    uint64_t* d_jumps = nullptr;
+    double* d_sqrt_dt = nullptr;
+    void* d_dw = nullptr;
+    bool generated = false;
+};
+
+struct lmm_process {
+    lmm_brownian* bm = nullptr;
+    int T = 0, N = 0, F = 0, P = 0, scheme = 1, precision = 0;
+    double cap = 1e5;
+    std::vector<double> times, tenor, discount;
+    bool has_discount = false;
+    std::vector<int> first, tenor_tidx, obs_slot;
+    std::vector<uint8_t> num_det;
+    int num_det_prefix = 0, nobs = 0;
+    cudaStream_t stream = nullptr;
+    // device tables
+    double *d_loadings = nullptr, *d_variance = nullptr, *d_dt = nullptr, *d_delta = nullptr, *d_init = nullptr;
+    float *d_lam32 = nullptr, *d_var32 = nullptr;
+    int *d_first = nullptr, *d_obs_slot = nullptr;
+    uint8_t* d_det = nullptr;
+    // results
+    void* d_states = nullptr;
+    double *d_numeraire = nullptr, *d_partials = nullptr, *d_num_adj = nullptr;
+    int path_blocks = 0;
+    bool simulated = false;
+    // product scratch
+    double* d_values = nullptr;
+    double* d_reduce = nullptr;
+    size_t reduce_bytes = 0;
+    double *d_under = nullptr, *d_ex = nullptr, *d_basis = nullptr, *d_gram = nullptr, *d_beta = nullptr;
+    double *d_period_length = nullptr, *d_tenor_delta = nullptr;
+    int* d_period_index = nullptr;
+    int berm_capacity = 0;
+};
+
+extern "C" {
+
+const char* lmm_last_error(void) { return g_last_error.c_str(); }
+
+int lmm_version(void) { return 1; }
+
+// ------------------------------------------------------------------ Brownian motion
+int lmm_brownian_create(const double* times, int num_times, int F, int P, int seed, int precision, lmm_brownian** out)
+{
+    if (!out) return fail(LMM_ERR_INVALID, "lmm_brownian_create: out is NULL");
+    *out = nullptr;
+    if (!times || num_times < 2 || F <= 0 || P <= 0) return fail(LMM_ERR_INVALID, "lmm_brownian_create: need >= 2 times, F > 0, P > 0");
+    if (precision != LMM_PRECISION_FP64 && precision != LMM_PRECISION_MIXED) return fail(LMM_ERR_INVALID, "unknown precision");
+    for (int i = 1; i < num_times; i++)
+        if (!(times[i] > times[i - 1])) return fail(LMM_ERR_INVALID, "time discretization must be strictly increasing");
+    const int64_t values = (int64_t)(num_times - 1) * F * (int64_t)P;
+    if ((int64_t)(num_times - 1) * F > (1 << 30) || values > ((int64_t)1 << 40)) return fail(LMM_ERR_INVALID, "Brownian motion too large");
+    int rc = ensure_pool();
+    if (rc) return rc;
+    lmm_brownian* b = new lmm_brownian();
+    b->T = num_times - 1;
+    b->F = F;
+    b->P = P;
+    b->seed = seed;
+    b->precision = precision;
+    b->times.assign(times, times + num_times);
+    cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { delete b; return cuda_fail(e, "cudaStreamCreate"); }
+    *out = b;
+    return LMM_OK;
+}
+
+static int brownian_ensure(lmm_brownian* b)
+{
+    if (b->generated) return LMM_OK;
+    const int64_t values = (int64_t)b->T * b->F * (int64_t)b->P;
+    int rc = plan_mt_generate(values, &b->plan);
+    if (rc) return rc;
+    uint32_t seeded[kMtN];
+    mt_seeded_state((int64_t)b->seed, seeded);  // int seed widened to long (BrownianMotionFromMersenneRandomNumbers.java:147)
+    std::vector<double> sq(b->T);
+    for (int t = 0; t < b->T; t++) sq[t] = std::sqrt(b->times[t + 1] - b->times[t]);
+    if ((rc = upload(&b->d_seeded, seeded, kMtN, b->stream))) return rc;
+    if ((rc = upload(&b->d_jumps, b->plan.polys.data(), b->plan.polys.size(), b->stream))) return rc;
+    if ((rc = upload(&b->d_sqrt_dt, sq.data(), sq.size(), b->stream))) return rc;
+    const size_t esz = b->precision == LMM_PRECISION_FP64 ? sizeof(double) : sizeof(float);
+    if ((rc = dalloc((unsigned char**)&b->d_dw, (size_t)values * esz, b->stream))) return rc;
+    RngLaunch a;
+    a.plan = &b->plan;
+    a.d_seeded = b->d_seeded;
+    a.d_jumps = b->d_jumps;
+    a.num_values = values;
+    a.values_per_path = b->T * b->F;
+    a.num_paths = b->P;
+    a.num_factors = b->F;
+    a.mode = b->precision == LMM_PRECISION_FP64 ? 1 : 2;
+    a.d_sqrt_dt = b->d_sqrt_dt;
+    a.d_out = b->d_dw;
+    rc = launch_mt_generate(a, b->stream, nullptr);
+    if (rc) return rc;
+    b->generated = true;
+    return LMM_OK;
+}
+
+int lmm_brownian_generate(lmm_brownian* b)
+{
+    if (!b) return fail(LMM_ERR_INVALID, "null handle");
+    int rc = brownian_ensure(b);
+    if (rc) return rc;
+    LMM_CUDA(cudaStreamSynchronize(b->stream));
+    return LMM_OK;
+}
+
+int lmm_brownian_get_increment(lmm_brownian* b, int t, int k, double* out)
+{
+    if (!b || !out) return fail(LMM_ERR_INVALID, "null argument");
+    if (t < 0 || t >= b->T || k < 0 || k >= b->F) return fail(LMM_ERR_INVALID, "time index or factor out of range");
+    int rc = brownian_ensure(b);
+    if (rc) return rc;
+    const size_t off = ((size_t)t * b->F + k) * (size_t)b->P;
+    if (b->precision == LMM_PRECISION_FP64) {
+        LMM_CUDA(cudaMemcpyAsync(out, static_cast<double*>(b->d_dw) + off, sizeof(double) * b->P, cudaMemcpyDeviceToHost, b->stream));
+        LMM_CUDA(cudaStreamSynchronize(b->stream));
+    } else {
+        std::vector<float> tmp(b->P);
+        LMM_CUDA(cudaMemcpyAsync(tmp.data(), static_cast<float*>(b->d_dw) + off, sizeof(float) * b->P, cudaMemcpyDeviceToHost, b->stream));
+        LMM_CUDA(cudaStreamSynchronize(b->stream));
+        for (int p = 0; p < b->P; p++) out[p] = tmp[p];
+    }
+    return LMM_OK;
+}
+
+int lmm_brownian_destroy(lmm_brownian* b)
+{
+    if (!b) return LMM_OK;
+    dfree(b->d_seeded, b->stream);
+    dfree(b->d_jumps, b->stream);
+    dfree(b->d_sqrt_dt, b->stream);
+    dfree(b->d_dw, b->stream);
+    cudaStreamSynchronize(b->stream);
+    cudaStreamDestroy(b->stream);
+    delete b;
+    return LMM_OK;
+}
+
+int lmm_mt19937_uniforms(int64_t seed, int64_t offset, int64_t count, double* out)
+{
+    if (!out || offset < 0 || count <= 0) return fail(LMM_ERR_INVALID, "lmm_mt19937_uniforms: bad arguments");
+    if (offset + count > ((int64_t)1 << 32)) return fail(LMM_ERR_INVALID, "lmm_mt19937_uniforms: range too large");
+    int rc = ensure_pool();
+    if (rc) return rc;
+    cudaStream_t s;
+    LMM_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    RngPlan plan;
+    const int64_t n = offset + count;
+    uint32_t seeded[kMtN];
+    mt_seeded_state(seed, seeded);
+    uint32_t* d_seeded = nullptr;
+    uint64_t* d_jumps = nullptr;
+    double* d_out = nullptr;
+    rc = plan_mt_generate(n, &plan);
+    if (!rc) rc = upload(&d_seeded, seeded, kMtN, s);
+    if (!rc) rc = upload(&d_jumps, plan.polys.data(), plan.polys.size(), s);
+    if (!rc) rc = dalloc(&d_out, (size_t)n, s);
+    if (!rc) {
+        RngLaunch a;
+        a.plan = &plan;
+        a.d_seeded = d_seeded;
+        a.d_jumps = d_jumps;
+        a.num_values = n;
+        a.values_per_path = 1;
+        a.num_paths = 1;
+        a.num_factors = 1;
+        a.mode = 0;
+        a.d_sqrt_dt = nullptr;
+        a.d_out = d_out;
+        rc = launch_mt_generate(a, s, nullptr);
+    }
+    if (!rc) {
+        cudaError_t e = cudaMemcpyAsync(out, d_out + offset, sizeof(double) * (size_t)count, cudaMemcpyDeviceToHost, s);
+        if (e != cudaSuccess) rc = cuda_fail(e, "cudaMemcpyAsync");
+    }
+    dfree(d_seeded, s);
+    dfree(d_jumps, s);
+    dfree(d_out, s);
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (!rc && e != cudaSuccess) rc = cuda_fail(e, "cudaStreamSynchronize");
+    cudaStreamDestroy(s);
+    return rc;
+}
+
+// ------------------------------------------------------------------ process
+int lmm_process_create(const lmm_model_desc* m, lmm_brownian* bm, lmm_process** out)
+{
+    if (!out) return fail(LMM_ERR_INVALID, "lmm_process_create: out is NULL");
+    *out = nullptr;
+    if (!m || !bm) return fail(LMM_ERR_INVALID, "lmm_process_create: null model or Brownian motion");
+    const int T = m->num_steps, N = m->num_periods, F = m->num_factors;
+    if (T != bm->T || !m->times) return fail(LMM_ERR_INVALID, "model time discretization must be the Brownian motion's");
+    for (int i = 0; i <= T; i++)
+        if (m->times[i] != bm->times[i]) return fail(LMM_ERR_INVALID, "model time discretization must be the Brownian motion's");
+    if (F != bm->F) return fail(LMM_ERR_INVALID, "number of factors differs from the Brownian motion's");
+    if (N <= 0 || N > 64 || F > 16) return fail(LMM_ERR_INVALID, "supported sizes: 1 <= forward rates <= 64, factors <= 16");
+    if (!m->tenor || !m->factor_loadings || !m->variance || !m->initial_forwards) return fail(LMM_ERR_INVALID, "model tables missing");
+    if (m->measure != 0) return fail(LMM_ERR_INVALID, "only the SPOT measure is implemented on this path");
+    if (m->state_space != 0) return fail(LMM_ERR_INVALID, "only the LOGNORMAL state space is implemented on this path");
+    if (m->scheme != LMM_SCHEME_EULER && m->scheme != LMM_SCHEME_EULER_FUNCTIONAL) return fail(LMM_ERR_INVALID, "unknown scheme");
+    for (int j = 1; j <= N; j++)
+        if (!(m->tenor[j] > m->tenor[j - 1])) return fail(LMM_ERR_INVALID, "tenor must be strictly increasing");
+    if (m->tenor[N - 1] > m->times[T]) return fail(LMM_ERR_INVALID, "every forward rate must fix within the simulation horizon");
+    lmm_process* pr = new lmm_process();
+    pr->bm = bm;
+    pr->T = T;
+    pr->N = N;
+    pr->F = F;
+    pr->P = bm->P;
+    pr->scheme = m->scheme;
+    pr->precision = bm->precision;
+    pr->cap = m->libor_cap;
+    pr->times.assign(m->times, m->times + T + 1);
+    pr->tenor.assign(m->tenor, m->tenor + N + 1);
+    pr->has_discount = m->discount_chain != nullptr;
+    if (pr->has_discount) pr->discount.assign(m->discount_chain, m->discount_chain + N + 1);
+    pr->stream = bm->stream;
+    // first alive component m(t_i)+1 (LIBORMarketModelFromCovarianceModel.getDrift :1127-1130)
+    pr->first.resize(T);
+    for (int i = 0; i < T; i++) {
+        int f = time_index(pr->tenor, pr->times[i]) + 1;
+        if (f < 0) f = -f - 1 + 1;
+        pr->first[i] = f;
+    }
+    // process index of each fixing (getNumerairetUnAdjustedAtLIBORIndex :1054-1057) and numeraire determinism
+    pr->tenor_tidx.resize(N + 1);
+    for (int l = 0; l <= N; l++) {
+        int ti = time_index(pr->times, pr->tenor[l]);
+        if (ti < 0) ti = -ti - 1;
+        pr->tenor_tidx[l] = ti;
+    }
+    pr->num_det.assign(N + 1, 0);
+    pr->num_det[0] = 1;
+    for (int l = 0; l < N; l++) pr->num_det[l + 1] = (uint8_t)(pr->num_det[l] && pr->tenor_tidx[l] == 0);
+    pr->num_det_prefix = 0;
+    while (pr->num_det_prefix < N && pr->num_det[pr->num_det_prefix]) pr->num_det_prefix++;
+    pr->obs_slot.resize(T + 1);
+    for (int t = 0; t <= T; t++) pr->obs_slot[t] = t;
+    pr->nobs = T + 1;
+
+    std::vector<double> dt(T), delta(N);
+    for (int i = 0; i < T; i++) dt[i] = pr->times[i + 1] - pr->times[i];
+    for (int j = 0; j < N; j++) delta[j] = pr->tenor[j + 1] - pr->tenor[j];
+    cudaStream_t s = pr->stream;
+    int rc = 0;
+    if (!rc) rc = upload(&pr->d_loadings, m->factor_loadings, (size_t)T * N * F, s);
+    if (!rc) rc = upload(&pr->d_variance, m->variance, (size_t)T * N, s);
+    if (!rc) rc = upload(&pr->d_dt, dt.data(), dt.size(), s);
+    if (!rc) rc = upload(&pr->d_delta, delta.data(), delta.size(), s);
+    if (!rc) rc = upload(&pr->d_init, m->initial_forwards, (size_t)N, s);
+    if (!rc) rc = upload(&pr->d_first, pr->first.data(), pr->first.size(), s);
+    if (!rc) rc = upload(&pr->d_det, pr->num_det.data(), pr->num_det.size(), s);
+    if (!rc && pr->precision == LMM_PRECISION_MIXED) {
+        std::vector<float> l32((size_t)T * N * F), v32((size_t)T * N);
+        for (size_t i = 0; i < l32.size(); i++) l32[i] = (float)m->factor_loadings[i];
+        for (size_t i = 0; i < v32.size(); i++) v32[i] = (float)m->variance[i];
+        rc = upload(&pr->d_lam32, l32.data(), l32.size(), s);
+        if (!rc) rc = upload(&pr->d_var32, v32.data(), v32.size(), s);
+        if (!rc) rc = cudaStreamSynchronize(s) == cudaSuccess ? 0 : fail(LMM_ERR_CUDA, "stream sync");
+    }
+    if (!rc) rc = cudaStreamSynchronize(s) == cudaSuccess ? 0 : fail(LMM_ERR_CUDA, "stream sync");
+    if (rc) {
+        lmm_process_destroy(pr);
+        return rc;
+    }
+    *out = pr;
+    return LMM_OK;
+}
+
+static void process_free_results(lmm_process* pr)
+{
+    dfree(pr->d_states, pr->stream);
+    dfree(pr->d_numeraire, pr->stream);
+    dfree(pr->d_partials, pr->stream);
+    dfree(pr->d_num_adj, pr->stream);
+    dfree(pr->d_obs_slot, pr->stream);
+    pr->simulated = false;
+}
+
+int lmm_process_set_observed_times(lmm_process* pr, const uint8_t* mask)
+{
+    if (!pr || !mask) return fail(LMM_ERR_INVALID, "null argument");
+    process_free_results(pr);
+    pr->nobs = 0;
+    for (int t = 0; t <= pr->T; t++) pr->obs_slot[t] = mask[t] ? pr->nobs++ : -1;
+    return LMM_OK;
+}
+
+static int process_ensure(lmm_process* pr)
+{
+    if (pr->simulated) return LMM_OK;
+    int rc = brownian_ensure(pr->bm);
+    if (rc) return rc;
+    cudaStream_t s = pr->stream;
+    const size_t esz = pr->precision == LMM_PRECISION_FP64 ? sizeof(double) : sizeof(float);
+    pr->path_blocks = path_blocks(pr->P);
+    if (!rc) rc = upload(&pr->d_obs_slot, pr->obs_slot.data(), pr->obs_slot.size(), s);
+    if (!rc) rc = dalloc((unsigned char**)&pr->d_states, (size_t)pr->nobs * pr->N * (size_t)pr->P * esz, s);
+    if (!rc) rc = dalloc(&pr->d_numeraire, (size_t)(pr->N + 1) * pr->P, s);
+    if (!rc) rc = dalloc(&pr->d_partials, (size_t)pr->path_blocks * pr->N * 2, s);
+    if (!rc) rc = dalloc(&pr->d_num_adj, (size_t)(pr->N + 1), s);
+    if (rc) return rc;
+    PathLaunch a;
+    a.T = pr->T;
+    a.N = pr->N;
+    a.F = pr->F;
+    a.P = pr->P;
+    a.scheme = pr->scheme;
+    a.libor_cap = pr->cap;
+    a.d_loadings = pr->d_loadings;
+    a.d_variance = pr->d_variance;
+    a.d_dt = pr->d_dt;
+    a.d_first = pr->d_first;
+    a.d_delta = pr->d_delta;
+    a.d_init = pr->d_init;
+    a.d_obs_slot = pr->d_obs_slot;
+    a.d_dw = pr->bm->d_dw;
+    a.d_states = pr->d_states;
+    a.d_numeraire = pr->d_numeraire;
+    a.d_inv_num_partials = pr->d_partials;
+    a.num_det_prefix = pr->num_det_prefix;
+    int blocks = 0;
+    rc = pr->precision == LMM_PRECISION_FP64 ? launch_paths_fp64(a, s, &blocks)
+                                              : launch_paths_fp32(a, pr->d_lam32, pr->d_var32, s, &blocks);
+    if (rc) return rc;
+    rc = launch_numeraire_finish(pr->d_partials, blocks, pr->N, pr->P, pr->d_numeraire, pr->d_det, pr->d_num_adj, s);
+    if (rc) return rc;
+    pr->simulated = true;
+    return LMM_OK;
+}
+
+int lmm_process_simulate(lmm_process* pr)
+{
+    if (!pr) return fail(LMM_ERR_INVALID, "null handle");
+    int rc = process_ensure(pr);
+    if (rc) return rc;
+    LMM_CUDA(cudaStreamSynchronize(pr->stream));
+    return LMM_OK;
+}
+
+int lmm_process_get_value(lmm_process* pr, int t, int j, double* out)
+{
+    if (!pr || !out) return fail(LMM_ERR_INVALID, "null argument");
+    if (t < 0 || t > pr->T || j < 0 || j >= pr->N) return fail(LMM_ERR_INVALID, "time index or component out of range");
+    if (pr->obs_slot[t] < 0) return fail(LMM_ERR_STATE, "time index not among the observed times of this process");
+    int rc = process_ensure(pr);
+    if (rc) return rc;
+    const size_t off = ((size_t)pr->obs_slot[t] * pr->N + j) * (size_t)pr->P;
+    if (pr->precision == LMM_PRECISION_FP64) {
+        LMM_CUDA(cudaMemcpyAsync(out, static_cast<double*>(pr->d_states) + off, sizeof(double) * pr->P, cudaMemcpyDeviceToHost, pr->stream));
+        LMM_CUDA(cudaStreamSynchronize(pr->stream));
+    } else {
+        std::vector<float> tmp(pr->P);
+        LMM_CUDA(cudaMemcpyAsync(tmp.data(), static_cast<float*>(pr->d_states) + off, sizeof(float) * pr->P, cudaMemcpyDeviceToHost, pr->stream));
+        LMM_CUDA(cudaStreamSynchronize(pr->stream));
+        for (int p = 0; p < pr->P; p++) out[p] = tmp[p];
+    }
+    return LMM_OK;
+}
+
+int lmm_process_get_numeraire(lmm_process* pr, double time, double* out)
+{
+    if (!pr || !out) return fail(LMM_ERR_INVALID, "null argument");
+    const int l = time_index(pr->tenor, time);
+    if (l < 0) return fail(LMM_ERR_INVALID, "numeraire requested off the tenor grid");
+    int rc = process_ensure(pr);
+    if (rc) return rc;
+    double adj = 0.0;
+    LMM_CUDA(cudaMemcpyAsync(out, pr->d_numeraire + (size_t)l * pr->P, sizeof(double) * pr->P, cudaMemcpyDeviceToHost, pr->stream));
+    LMM_CUDA(cudaMemcpyAsync(&adj, pr->d_num_adj + l, sizeof(double), cudaMemcpyDeviceToHost, pr->stream));
+    LMM_CUDA(cudaStreamSynchronize(pr->stream));
+    if (!pr->has_discount) return LMM_OK;
+    const double pd = pr->discount[l];
+    for (int p = 0; p < pr->P; p++)
+        out[p] = pr->num_det[l] ? (1.0 / pd) * (out[p] * adj) : (out[p] * adj) / pd;
+    return LMM_OK;
+}
+
+int lmm_process_destroy(lmm_process* pr)
+{
+    if (!pr) return LMM_OK;
+    cudaStream_t s = pr->stream;
+    process_free_results(pr);
+    dfree(pr->d_loadings, s);
+    dfree(pr->d_variance, s);
+    dfree(pr->d_dt, s);
+    dfree(pr->d_delta, s);
+    dfree(pr->d_init, s);
+    dfree(pr->d_lam32, s);
+    dfree(pr->d_var32, s);
+    dfree(pr->d_first, s);
+    dfree(pr->d_det, s);
+    dfree(pr->d_values, s);
+    dfree(pr->d_reduce, s);
+    dfree(pr->d_under, s);
+    dfree(pr->d_ex, s);
+    dfree(pr->d_basis, s);
+    dfree(pr->d_gram, s);
+    dfree(pr->d_beta, s);
+    dfree(pr->d_period_length, s);
+    dfree(pr->d_tenor_delta, s);
+    dfree(pr->d_period_index, s);
+    cudaStreamSynchronize(s);
+    delete pr;
+    return LMM_OK;
+}
+
+int lmm_process_stream(lmm_process* pr, void** out)
+{
+    if (!pr || !out) return fail(LMM_ERR_INVALID, "null argument");
+    *out = (void*)pr->stream;
+    return LMM_OK;
+}
+
+// ------------------------------------------------------------------ products
+static ProductView product_view(lmm_process* pr)
+{
+    ProductView v;
+    v.P = pr->P;
+    v.N = pr->N;
+    v.T = pr->T;
+    v.state_fp32 = pr->precision == LMM_PRECISION_MIXED;
+    v.d_states = pr->d_states;
+    v.h_obs_slot = pr->obs_slot.data();
+    v.d_numeraire = pr->d_numeraire;
+    v.d_num_adj = pr->d_num_adj;
+    v.h_discount = pr->has_discount ? pr->discount.data() : nullptr;
+    v.h_num_det = pr->num_det.data();
+    return v;
+}
+
+// process time index of a time with ROUND_NEAREST (LIBORMarketModelFromCovarianceModel.getForwardRate :1243-1252)
+static int process_index_nearest(const lmm_process* pr, double t)
+{
+    int ti = time_index(pr->times, t);
+    if (ti < 0) {
+        ti = -ti - 2;
+        if (ti < 0) return -1;
+        if (ti + 1 <= pr->T && t - pr->times[ti] > pr->times[ti + 1] - t) ti++;
+    }
+    return ti;
+}
+
+static int ensure_values(lmm_process* pr)
+{
+    int rc = LMM_OK;
+    if (!pr->d_values) rc = dalloc(&pr->d_values, (size_t)pr->P, pr->stream);
+    if (!rc && !pr->d_reduce) {
+        pr->reduce_bytes = (2 * 1024 + 2) * sizeof(double);
+        rc = dalloc((unsigned char**)&pr->d_reduce, pr->reduce_bytes, pr->stream);
+    }
+    return rc;
+}
+
+int lmm_swaption_get_value(lmm_process* pr, const lmm_swaption_desc* d, double* value, double* error)
+{
+    if (!pr || !d || !value) return fail(LMM_ERR_INVALID, "null argument");
+    if (d->num_periods <= 0 || d->num_periods > 64 || !d->fixing_dates || !d->payment_dates || !d->swaprates)
+        return fail(LMM_ERR_INVALID, "swaption needs 1..64 periods with fixing, payment dates and swap rates");
+    SwaptionLaunch a;
+    std::memset(&a, 0, sizeof(a));
+    a.notional = d->notional;
+    a.num_index = time_index(pr->tenor, d->exercise_date);
+    if (a.num_index < 0) return fail(LMM_ERR_INVALID, "exercise date must be a tenor time (numeraire on the tenor grid)");
+    if (pr->num_det[a.num_index]) return fail(LMM_ERR_INVALID, "exercise at a deterministic numeraire time is not supported");
+    int n = 0;
+    // Swaption.getValue loops backward and stops at the first period paid at or before time 0.
+    int start = 0;
+    for (int per = d->num_periods - 1; per >= 0; per--)
+        if (d->payment_dates[per] <= 0.0) { start = per + 1; break; }
+    for (int per = start; per < d->num_periods; per++) {
+        const double fix = d->fixing_dates[per], pay = d->payment_dates[per];
+        const int si = time_index(pr->tenor, fix), ei = time_index(pr->tenor, pay);
+        if (si < 0 || ei != si + 1) return fail(LMM_ERR_INVALID, "swaption periods must be single tenor periods");
+        const int ti = process_index_nearest(pr, std::min(d->exercise_date, fix));
+        if (ti <= 0) return fail(LMM_ERR_INVALID, "swaption forwards must be read after the first simulation time");
+        if (pr->obs_slot[ti] < 0) return fail(LMM_ERR_STATE, "swaption needs an unobserved process time");
+        a.period_slot[n] = pr->obs_slot[ti];
+        a.period_index[n] = si;
+        a.period_length[n] = d->period_lengths ? d->period_lengths[per] : pay - fix;
+        a.disc_dt[n] = pay - std::max(fix, d->exercise_date);
+        a.strike[n] = d->swaprates[per];
+        n++;
+    }
+    a.nper = n;
+    int rc = process_ensure(pr);
+    if (!rc) rc = ensure_values(pr);
+    if (rc) return rc;
+    ProductView v = product_view(pr);
+    rc = launch_swaption(v, a, pr->d_values, pr->stream);
+    if (rc) return rc;
+    return reduce_mean_stderr(pr->d_values, pr->P, pr->d_reduce, pr->reduce_bytes, value, error, pr->stream);
+}
+
+int lmm_bermudan_get_value(lmm_process* pr, const lmm_bermudan_desc* d, double* value, double* error, double* values_host)
+{
+    if (!pr || !d || !value) return fail(LMM_ERR_INVALID, "null argument");
+    const int n = d->num_periods;
+    if (n <= 0 || n > 64 || !d->is_exercise_date || !d->fixing_dates || !d->period_lengths || !d->payment_dates ||
+        !d->notionals || !d->swaprates)
+        return fail(LMM_ERR_INVALID, "Bermudan needs 1..64 periods and all per-period arrays");
+    if (d->basis != LMM_BASIS_REFERENCE && d->basis != LMM_BASIS_SWAPRATE) return fail(LMM_ERR_INVALID, "unknown regression basis");
+    BermudanLaunch a;
+    a.nper = n;
+    a.callable = d->is_callable ? 1 : 0;
+    a.basis = d->basis;
+    a.per.resize(n);
+    std::vector<int> pidx(n);
+    std::vector<double> plen(n), tdelta(pr->N);
+    for (int j = 0; j < pr->N; j++) tdelta[j] = pr->tenor[j + 1] - pr->tenor[j];
+    for (int q = 0; q < n; q++) {
+        const double fix = d->fixing_dates[q];
+        const int si = time_index(pr->tenor, fix), ei = time_index(pr->tenor, fix + d->period_lengths[q]);
+        if (si < 0 || ei != si + 1) return fail(LMM_ERR_INVALID, "Bermudan periods must be single tenor periods");
+        if (q > 0 && !(fix > d->fixing_dates[q - 1])) return fail(LMM_ERR_INVALID, "fixing dates must be increasing");
+        pidx[q] = si;
+        plen[q] = d->period_lengths[q];
+    }
+    for (int q = 0; q < n; q++) {
+        BermudanPeriod& c = a.per[q];
+        std::memset(&c, 0, sizeof(c));
+        const double fix = d->fixing_dates[q];
+        const int ti = process_index_nearest(pr, fix);
+        if (ti <= 0) return fail(LMM_ERR_INVALID, "Bermudan periods must fix after the first simulation time");
+        if (pr->obs_slot[ti] < 0) return fail(LMM_ERR_STATE, "Bermudan needs an unobserved process time");
+        c.libor_slot = pr->obs_slot[ti];
+        c.libor_index = pidx[q];
+        c.pay_num_index = time_index(pr->tenor, d->payment_dates[q]);
+        if (c.pay_num_index < 0) return fail(LMM_ERR_INVALID, "payment dates must be tenor times");
+        c.exercisable = d->is_exercise_date[q] ? 1 : 0;
+        c.period_length = d->period_lengths[q];
+        c.strike = d->swaprates[q];
+        c.notional = d->notionals[q];
+        c.fixing = fix;
+        c.ex_slot = c.libor_slot;
+        c.ex_num_index = pidx[q];
+        if (c.exercisable && pr->num_det[c.ex_num_index])
+            return fail(LMM_ERR_INVALID, "exercise at a deterministic numeraire time is not supported");
+        // reference basis (BermudanSwaption.getBasisFunctions :215-252)
+        int fi = binary_search(d->fixing_dates, n, fix);
+        if (fi < 0) fi = -fi;
+        if (fi >= n) fi = n - 1;
+        const double pay_fi = d->payment_dates[fi];
+        const int sh = time_index(pr->tenor, pay_fi);
+        if (sh != pidx[fi] + 1 || pidx[fi] != c.libor_index) return fail(LMM_ERR_INVALID, "short forward must be a tenor period");
+        c.short_index = pidx[fi];
+        c.short_dt = pay_fi - fix;
+        const double t_last = d->payment_dates[n - 1];
+        c.long_first = time_index(pr->tenor, d->fixing_dates[fi]);
+        c.long_last = time_index(pr->tenor, t_last);
+        if (c.long_first < 0 || c.long_last <= c.long_first) return fail(LMM_ERR_INVALID, "long forward must span tenor periods");
+        c.long_dt = t_last - d->fixing_dates[fi];
+        c.swap_first = q;
+        c.swap_last = n;
+    }
+    int rc = process_ensure(pr);
+    if (!rc) rc = ensure_values(pr);
+    if (rc) return rc;
+    cudaStream_t s = pr->stream;
+    const int blocks = bermudan_blocks(pr->P);
+    if (pr->berm_capacity == 0) {
+        if (!rc) rc = dalloc(&pr->d_under, (size_t)pr->P, s);
+        if (!rc) rc = dalloc(&pr->d_ex, (size_t)pr->P, s);
+        if (!rc) rc = dalloc(&pr->d_basis, (size_t)5 * pr->P, s);
+        if (!rc) rc = dalloc(&pr->d_gram, (size_t)blocks * 26 * 2, s);
+        if (!rc) rc = dalloc(&pr->d_beta, (size_t)64 * 6, s);
+        if (!rc) rc = dalloc(&pr->d_period_length, (size_t)64, s);
+        if (!rc) rc = dalloc(&pr->d_period_index, (size_t)64, s);
+        if (!rc) rc = dalloc(&pr->d_tenor_delta, (size_t)64, s);
+        if (rc) return rc;
+        pr->berm_capacity = 64;
+    }
+    LMM_CUDA(cudaMemcpyAsync(pr->d_period_length, plen.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    LMM_CUDA(cudaMemcpyAsync(pr->d_period_index, pidx.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+    LMM_CUDA(cudaMemcpyAsync(pr->d_tenor_delta, tdelta.data(), sizeof(double) * pr->N, cudaMemcpyHostToDevice, s));
+    BermudanScratch sc;
+    sc.d_values = pr->d_values;
+    sc.d_under = pr->d_under;
+    sc.d_ex = pr->d_ex;
+    sc.d_basis = pr->d_basis;
+    sc.d_partials = pr->d_gram;
+    sc.d_beta = pr->d_beta;
+    sc.d_tenor_delta = pr->d_tenor_delta;
+    sc.d_period_index = pr->d_period_index;
+    sc.d_period_length = pr->d_period_length;
+    ProductView v = product_view(pr);
+    rc = launch_bermudan(v, a, sc, s, nullptr);
+    if (rc) return rc;
+    rc = reduce_mean_stderr(pr->d_values, pr->P, pr->d_reduce, pr->reduce_bytes, value, error, s);
+    if (rc) return rc;
+    if (values_host) {
+        LMM_CUDA(cudaMemcpyAsync(values_host, pr->d_values, sizeof(double) * pr->P, cudaMemcpyDeviceToHost, s));
+        LMM_CUDA(cudaStreamSynchronize(s));
+    }
+    return LMM_OK;
+}
+
+// ------------------------------------------------------------------ instrumentation
+int lmm_stats_enable_timing(int enable)
+{
+    g_timing.store(enable != 0);
+    return LMM_OK;
+}
+
+int lmm_stats_reset(void)
+{
+    collect_timings();
+    for (int i = 0; i < K_COUNT; i++) {
+        g_launches[i] = 0;
+        g_total_ms[i] = 0.0;
+    }
+    return LMM_OK;
+}
+
+int lmm_stats_get(int max, const char** names, int64_t* launches, double* total_ms)
+{
+    collect_timings();
+    const int n = max < K_COUNT ? max : K_COUNT;
+    for (int i = 0; i < n; i++) {
+        if (names) names[i] = kKernelNames[i];
+        if (launches) launches[i] = g_launches[i].load();
+        if (total_ms) total_ms[i] = g_total_ms[i];
+    }
+    return n;
+}
+
+}  // extern "C"

@@ -1,0 +1,175 @@
+// lmm_internal.h -- shared declarations of the GB300 LMM library (host + device).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "lmm_gb300.h"
+
+namespace lmm {
+
+// ---------------------------------------------------------------- errors
+void set_error(const std::string& msg);
+int fail(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+
+#define LMM_CUDA(call)                                                   \
+    do {                                                                 \
+        cudaError_t e_ = (call);                                         \
+        if (e_ != cudaSuccess) return ::lmm::cuda_fail(e_, #call);       \
+    } while (0)
+
+// Kernel-launch bookkeeping: every launch of a library kernel bumps a counter and,
+// when timing is enabled, is bracketed by CUDA events on the launching stream.
+enum KernelId : int {
+    K_MT_JUMP_GENERATE = 0,
+    K_PATHS_FP64,
+    K_PATHS_FP32,
+    K_NUMERAIRE_FINISH,
+    K_SWAPTION,
+    K_BERMUDAN_STEP,
+    K_BERMUDAN_SOLVE,
+    K_VALUE_REDUCE,
+    K_ADJOINT,
+    K_PORTFOLIO,
+    K_MISC,
+    K_COUNT
+};
+const char* kernel_name(int id);
+struct KernelTimer {
+    KernelTimer(int id, cudaStream_t s, int launches = 1);
+    ~KernelTimer();
+    int id;
+    cudaStream_t stream;
+    cudaEvent_t start = nullptr;
+};
+bool timing_enabled();
+
+// ---------------------------------------------------------------- MT19937 (host side)
+constexpr int kMtN = 624;
+constexpr int kMtM = 397;
+constexpr int kPolyWords = 312;            // 19937-bit GF(2) polynomials, 64-bit words
+constexpr int kMtDegree = 19937;
+constexpr int kJumpWindow = kMtDegree + kMtN - 1;  // raw words needed by one jump (20560)
+
+// Seeded 624-word array of commons-math3 MersenneTwister(long seed).
+void mt_seeded_state(int64_t seed, uint32_t out[kMtN]);
+// Jump polynomials x^(2^j * stride) mod phi for j = 0..count-1 (cached per stride).
+const std::vector<uint64_t>& mt_jump_polynomials(uint64_t stride_words, int count);
+
+// ---------------------------------------------------------------- device launchers
+struct RngPlan {
+    int64_t chunks = 0;
+    int64_t chunk_values = 0;
+    int njumps = 0;
+    std::vector<uint64_t> polys;   // [njumps][312]
+};
+// Chunking of a stream of num_values values (2 words each) over the resident CTAs.
+int plan_mt_generate(int64_t num_values, RngPlan* plan);
+
+struct RngLaunch {
+    const RngPlan* plan;
+    const uint32_t* d_seeded;  // [624] seeded state
+    const uint64_t* d_jumps;   // plan->polys on the device
+    int64_t num_values;        // values in the stream (normals or uniforms)
+    int values_per_path;       // T*F for Brownian increments (1 for plain uniforms)
+    int num_paths;             // P (row stride of the [T*F][P] layout)
+    int num_factors;           // F
+    int mode;                  // 0 uniforms (double), 1 increments fp64, 2 increments fp32
+    const double* d_sqrt_dt;   // [T] (modes 1,2)
+    void* d_out;
+};
+int launch_mt_generate(const RngLaunch& a, cudaStream_t s, int* num_launches);
+
+struct PathLaunch {
+    int T, N, F, P;
+    int scheme;                // 0 EULER, 1 EULER_FUNCTIONAL
+    double libor_cap;          // +inf: no cap
+    const double* d_loadings;  // [T][N][F]
+    const double* d_variance;  // [T][N]
+    const double* d_dt;        // [T]
+    const int* d_first;        // [T] first alive component at t_i
+    const double* d_delta;     // [N] period lengths
+    const double* d_init;      // [N] initial forwards
+    const int* d_obs_slot;     // [T+1] observation slot or -1
+    const void* d_dw;          // [T][F][P] fp64 or fp32
+    void* d_states;            // [nobs][N][P] fp64 or fp32
+    double* d_numeraire;       // [N+1][P] unadjusted spot numeraire
+    double* d_inv_num_partials;// [blocks][N][2] double-double partial sums of 1/N(T_{l+1})
+    int num_det_prefix;        // numeraire deterministic for l < num_det_prefix
+};
+int launch_paths_fp64(const PathLaunch& a, cudaStream_t s, int* blocks_out);
+int launch_paths_fp32(const PathLaunch& a, const float* lam32, const float* var32, cudaStream_t s, int* blocks_out);
+int path_blocks(int P);
+
+// numeraire adjustment: adj[l] = mean over paths of 1/N_l (or the deterministic value)
+int launch_numeraire_finish(const double* d_partials, int blocks, int N, int P, const double* d_numeraire,
+                            const uint8_t* d_det, double* d_adj, cudaStream_t s);
+
+struct ProductView {
+    int P, N, T;
+    int state_fp32;              // states stored as float
+    const void* d_states;        // [nobs][N][P]
+    const int* h_obs_slot;       // host copy [T+1]
+    const double* d_numeraire;   // [N+1][P]
+    const double* d_num_adj;     // [N+1] mean of 1/N (or deterministic value)
+    const double* h_discount;    // [N+1] P^d chain (nullptr = none)
+    const uint8_t* h_num_det;    // [N+1]
+};
+
+struct SwaptionLaunch {
+    int nper;
+    int period_slot[64];         // observation slot of min(exercise, fixing) per period
+    int num_index;               // tenor index of the exercise date
+    int period_index[64];        // tenor index of each period
+    double period_length[64];
+    double disc_dt[64];          // payment - max(fixing, exercise)
+    double strike[64];
+    double notional;
+};
+int launch_swaption(const ProductView& v, const SwaptionLaunch& a, double* d_values, cudaStream_t s);
+
+// mean and standard error of d_values[P] (Kahan-equivalent compensated sums)
+int reduce_mean_stderr(const double* d_values, int P, double* d_scratch, size_t scratch_bytes, double* h_mean,
+                       double* h_stderr, cudaStream_t s);
+
+struct BermudanPeriod {
+    int libor_slot;      // observation slot of the fixing index
+    int libor_index;     // tenor index of the period
+    int pay_num_index;   // tenor index of the payment date (numeraire)
+    int ex_slot;         // observation slot of the exercise index (exercisable periods)
+    int ex_num_index;    // tenor index of the exercise date
+    int exercisable;
+    double period_length, strike, notional, fixing;
+    // basis 0 (reference built-in)
+    int short_index;     // tenor index of the short forward
+    double short_dt;     // payment[fi] - fixing
+    int long_first, long_last;  // tenor indices [first, last) of the long rate
+    double long_dt;      // last payment - fixing[fi]
+    // basis 1 (swap rate + numeraire)
+    int swap_first, swap_last;  // product periods [first, last) of the remaining swap
+};
+struct BermudanLaunch {
+    int nper, callable, basis;
+    std::vector<BermudanPeriod> per;
+};
+struct BermudanScratch {
+    double* d_values;     // [P]
+    double* d_under;      // [P]
+    double* d_ex;         // [P]
+    double* d_basis;      // [5][P]
+    double* d_partials;   // [blocks][27][2]
+    double* d_beta;       // [nper][6]
+    const double* d_tenor_delta;    // [N]
+    const int* d_period_index;      // [nper]
+    const double* d_period_length;  // [nper]
+};
+int bermudan_blocks(int P);
+int launch_bermudan(const ProductView& v, const BermudanLaunch& a, const BermudanScratch& sc, cudaStream_t s,
+                    int* launches);
+
+}  // namespace lmm

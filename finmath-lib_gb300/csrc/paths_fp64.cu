@@ -1,0 +1,156 @@
+// paths_fp64.cu -- K2 (plain FP64 form): fused Euler-log path kernel.
+//
+// Reference: EulerSchemeFromProcessModel.doPrecalculateProcess
+// (montecarlo/process/EulerSchemeFromProcessModel.java:170-326) with the drift of
+// LIBORMarketModelFromCovarianceModel.getDrift (…/models/LIBORMarketModelFromCovarianceModel.java:1125-1191),
+// the state-space transforms (:1200-1223) and the spot numeraire (:1017-1074).
+//
+// One thread owns one path.  Its forward vector lives in registers across all T
+// steps; the spot-measure drift is the running sum S_k += L_j/(L_j + 1/delta_j) * lambda_jk
+// over alive components j, so a step costs O(N*F) instead of O(N^2*F).  Only the time
+// indices that products observe are written, as [slot][component][path] rows (coalesced
+// across the warp).  The spot numeraire N(T_l) = prod (1 + L_i(T_i) delta_i) is formed
+// at the end from the frozen fixings, and each block writes compensated partial sums
+// of 1/N(T_l) for the numeraire adjustment.
+//
+// Compiled with -fmad=false: every + and * rounds separately, as in the reference's
+// Java; exp/log/division are CUDA's (division correctly rounded, exp/log within 1 ulp).
+#include "lmm_internal.h"
+#include "reduce.cuh"
+
+namespace lmm {
+namespace {
+
+constexpr int kPathThreads = 128;
+
+template <int NMAX, int FMAX, bool FUNCTIONAL>
+__global__ void __launch_bounds__(kPathThreads) paths_fp64_kernel(const PathLaunch a)
+{
+    const int p = blockIdx.x * kPathThreads + threadIdx.x;
+    const bool active = p < a.P;
+    const int N = a.N, F = a.F, P = a.P;
+    const bool capped = !isinf(a.libor_cap);
+    const double* dW = static_cast<const double*>(a.d_dw);
+    double* states = static_cast<double*>(a.d_states);
+
+    double L[NMAX];
+    double Y[FUNCTIONAL ? 1 : NMAX];
+#pragma unroll
+    for (int j = 0; j < NMAX; j++) {
+        if (j < N) {
+            // getInitialState (:1081-1093): log(max(f,0)); applyStateSpaceTransform (:1200-1212)
+            const double f = __ldg(a.d_init + j);
+            const double y0 = log(f > 0.0 ? f : 0.0);
+            double v = exp(y0);
+            if (capped && v > a.libor_cap) v = a.libor_cap;
+            L[j] = v;
+            if (!FUNCTIONAL) Y[FUNCTIONAL ? 0 : j] = y0;
+        } else {
+            L[j] = 0.0;
+        }
+    }
+    {
+        const int slot = __ldg(a.d_obs_slot + 0);
+        if (slot >= 0 && active) {
+#pragma unroll
+            for (int j = 0; j < NMAX; j++)
+                if (j < N) states[((size_t)slot * N + j) * P + p] = L[j];
+        }
+    }
+
+    for (int i = 0; i < a.T; i++) {
+        const int first = __ldg(a.d_first + i);
+        const double dt = __ldg(a.d_dt + i);
+        const double* lam = a.d_loadings + (size_t)i * N * F;
+        const double* var = a.d_variance + (size_t)i * N;
+        double dw[FMAX];
+#pragma unroll
+        for (int k = 0; k < FMAX; k++) dw[k] = (k < F && active) ? dW[((size_t)i * F + k) * P + p] : 0.0;
+        double S[FMAX];
+#pragma unroll
+        for (int k = 0; k < FMAX; k++) S[k] = 0.0;
+#pragma unroll
+        for (int j = 0; j < NMAX; j++) {
+            if (j < N && j >= first) {
+                const double Lj = L[j];
+                const double delta = __ldg(a.d_delta + j);
+                // Scalar(delta).discount(L, delta) (stochastic/Scalar.java:321-328), times L (:1149-1153)
+                const double os = (1.0 / (Lj * (delta / delta) + 1.0 / delta)) * Lj;
+                double mu = 0.0;
+                double lj[FMAX];
+#pragma unroll
+                for (int k = 0; k < FMAX; k++) {
+                    if (k < F) {
+                        lj[k] = __ldg(lam + j * F + k);
+                        S[k] = S[k] + os * lj[k];  // :1156-1158
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < FMAX; k++)
+                    if (k < F) mu = mu + S[k] * lj[k];  // :1159 (addSumProduct, left to right)
+                mu = mu + __ldg(var + j) * -0.5;         // :1183-1189
+                // Euler step (EulerSchemeFromProcessModel.java:235-255)
+                double y = FUNCTIONAL ? log(Lj) : Y[FUNCTIONAL ? 0 : j];
+                y = y + mu * dt;
+#pragma unroll
+                for (int k = 0; k < FMAX; k++)
+                    if (k < F) y = y + dw[k] * lj[k];
+                if (!FUNCTIONAL) Y[FUNCTIONAL ? 0 : j] = y;
+                double v = exp(y);
+                if (capped && v > a.libor_cap) v = a.libor_cap;
+                L[j] = v;
+            }
+        }
+        const int slot = __ldg(a.d_obs_slot + i + 1);
+        if (slot >= 0 && active) {
+#pragma unroll
+            for (int j = 0; j < NMAX; j++)
+                if (j < N) states[((size_t)slot * N + j) * P + p] = L[j];
+        }
+    }
+
+    // Spot numeraire from the frozen fixings L_l(T_l) (:1050-1066): Scalar.accrue while
+    // the numeraire is deterministic, RandomVariableFromDoubleArray.accrue afterwards.
+    double Nv = 1.0;
+    if (active) a.d_numeraire[p] = 1.0;
+#pragma unroll
+    for (int l = 0; l < NMAX; l++) {
+        if (l < N) {
+            const double delta = __ldg(a.d_delta + l);
+            if (l < a.num_det_prefix) Nv = L[l] * (delta * Nv) + Nv;
+            else Nv = Nv * (1.0 + L[l] * delta);
+            if (active) a.d_numeraire[(size_t)(l + 1) * P + p] = Nv;
+            // numeraire adjustment input: mean of N(T)^-1 * N(0) (:869-874)
+            const double inv = (1.0 / Nv) * 1.0;
+            block_dd_partial(active ? inv : 0.0, a.d_inv_num_partials + ((size_t)blockIdx.x * N + l) * 2);
+        }
+    }
+}
+
+template <int NMAX, int FMAX>
+int launch_t(const PathLaunch& a, cudaStream_t s, int blocks)
+{
+    if (a.scheme == 1)
+        paths_fp64_kernel<NMAX, FMAX, true><<<blocks, kPathThreads, 0, s>>>(a);
+    else
+        paths_fp64_kernel<NMAX, FMAX, false><<<blocks, kPathThreads, 0, s>>>(a);
+    LMM_CUDA(cudaGetLastError());
+    return LMM_OK;
+}
+
+}  // namespace
+
+int path_blocks(int P) { return (P + kPathThreads - 1) / kPathThreads; }
+
+int launch_paths_fp64(const PathLaunch& a, cudaStream_t s, int* blocks_out)
+{
+    const int blocks = path_blocks(a.P);
+    if (blocks_out) *blocks_out = blocks;
+    KernelTimer kt(K_PATHS_FP64, s);
+    if (a.N <= 24 && a.F <= 4) return launch_t<24, 4>(a, s, blocks);
+    if (a.N <= 40 && a.F <= 10) return launch_t<40, 10>(a, s, blocks);
+    if (a.N <= 64 && a.F <= 16) return launch_t<64, 16>(a, s, blocks);
+    return fail(LMM_ERR_INVALID, "FP64 path kernel supports at most 64 forward rates and 16 factors");
+}
+
+}  // namespace lmm

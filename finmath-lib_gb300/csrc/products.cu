@@ -1,0 +1,497 @@
+// products.cu -- numeraire adjustment (K3), European swaption, Bermudan backward induction
+// with regression (K4/K5) and the compensated mean / standard error of per-path values.
+//
+// References (finmath-lib, src/main/java/net/finmath/):
+//   LIBORMarketModelFromCovarianceModel.getNumeraire            …/models/LIBORMarketModelFromCovarianceModel.java:860-876
+//   Swaption.getValue                                           montecarlo/interestrate/products/Swaption.java:137-199
+//   BermudanSwaption.getValues / getBasisFunctions              montecarlo/interestrate/products/BermudanSwaption.java:91-157, 215-252
+//   MonteCarloConditionalExpectationRegression                  montecarlo/conditionalexpectation/MonteCarloConditionalExpectationRegression.java:98-150
+//   RandomVariableFromDoubleArray.getAverage / getStandardError montecarlo/RandomVariableFromDoubleArray.java:287-308, 332-354, 419-428
+//
+// Compiled with -fmad=false (unfused FP64, as the reference's Java).
+#include "lmm_internal.h"
+#include "reduce.cuh"
+
+#include <math_constants.h>
+#include <cstring>
+
+namespace lmm {
+namespace {
+
+constexpr int kProdThreads = 256;
+constexpr int kMaxN = 64;
+
+struct NumeraireInfo {
+    int P;
+    int has_discount;
+    const double* numeraire;   // [N+1][P] unadjusted
+    const double* adj;         // [N+1] mean of 1/N (device)
+    double pd[kMaxN + 1];      // P^d(T_l)
+    unsigned char det[kMaxN + 1];
+};
+
+// getNumeraire(T_l) including the discount-curve adjustment (:869-874).
+__device__ __forceinline__ double numeraire_adj(const NumeraireInfo& n, int l, int p)
+{
+    const double Nu = n.numeraire[(size_t)l * n.P + p];
+    if (!n.has_discount) return Nu;
+    const double a = n.adj[l];
+    if (n.det[l]) return (1.0 / n.pd[l]) * (Nu * a);  // Scalar.div: invert, then mult
+    return (Nu * a) / n.pd[l];
+}
+
+template <typename TS>
+__device__ __forceinline__ double state_at(const void* states, int slot, int N, int P, int j, int p)
+{
+    return (double)static_cast<const TS*>(states)[((size_t)slot * N + j) * P + p];
+}
+
+// ------------------------------------------------------------------ numeraire adjustment
+__global__ void numeraire_finish_kernel(const double* partials, int blocks, int N, int P, const double* numeraire,
+                                        const uint8_t* det, double* adj)
+{
+    const int l = blockIdx.x;  // numeraire index 0..N
+    if (l > N) return;
+    if (det[l]) {
+        if (threadIdx.x == 0) adj[l] = 1.0 * (1.0 / numeraire[(size_t)l * P]);
+        return;
+    }
+    dd acc{0.0, 0.0};
+    for (int b = threadIdx.x; b < blocks; b += blockDim.x) {
+        const double* q = partials + ((size_t)b * N + (l - 1)) * 2;
+        acc = dd_add(acc, dd{q[0], q[1]});
+    }
+    acc = block_dd_sum(acc);
+    if (threadIdx.x == 0) adj[l] = (acc.hi + acc.lo) / (double)P;
+}
+
+// ------------------------------------------------------------------ mean / standard error
+__global__ void sum_partials_kernel(const double* x, int P, const double* center, double* partials)
+{
+    dd acc{0.0, 0.0};
+    const double m = center ? *center : 0.0;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x) {
+        const double v = center ? (x[p] - m) * (x[p] - m) : x[p];
+        acc = dd_add_d(acc, v);
+    }
+    acc = block_dd_sum(acc);
+    if (threadIdx.x == 0) {
+        partials[2 * blockIdx.x] = acc.hi;
+        partials[2 * blockIdx.x + 1] = acc.lo;
+    }
+}
+
+__global__ void finish_partials_kernel(const double* partials, int blocks, int P, double* out)
+{
+    dd acc{0.0, 0.0};
+    for (int b = threadIdx.x; b < blocks; b += blockDim.x) acc = dd_add(acc, dd{partials[2 * b], partials[2 * b + 1]});
+    acc = block_dd_sum(acc);
+    if (threadIdx.x == 0) *out = (acc.hi + acc.lo) / (double)P;
+}
+
+// ------------------------------------------------------------------ swaption
+struct SwaptionParams {
+    SwaptionLaunch s;
+    NumeraireInfo num;
+    const void* states;
+    int N, P, fp32;
+    double* values;
+};
+
+template <typename TS>
+__global__ void __launch_bounds__(kProdThreads) swaption_kernel(const SwaptionParams a)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= a.P) return;
+    const double w = 1.0 / (double)a.P;
+    double v = 0.0;
+    for (int per = a.s.nper - 1; per >= 0; per--) {
+        const double L = state_at<TS>(a.states, a.s.period_slot[per], a.N, a.P, a.s.period_index[per], p);
+        const double payoff = ((L - a.s.strike[per]) * a.s.period_length[per]) * a.s.notional;
+        v = v + payoff;
+        v = v / (1.0 + L * a.s.disc_dt[per]);
+        v = v * 1.0;
+    }
+    double x = isnan(v) ? v : (v > 0.0 ? v : 0.0);
+    x = x / numeraire_adj(a.num, a.s.num_index, p);
+    x = x * w;
+    x = x * 1.0;
+    x = x / w;
+    a.values[p] = x;
+}
+
+// ------------------------------------------------------------------ Bermudan
+constexpr int kGramEntries = 26;  // G[0][1..5], G[1..5][1..5] (i<=j), rhs[0..5]
+
+struct BermStepParams {
+    BermudanPeriod cur;        // period processed by this launch
+    int has_cur;
+    int apply_choose;          // apply the pending choose of the previous exercise
+    double choose_fixing;
+    const double* beta;        // [6] of the pending choose
+    int basis, callable;
+    NumeraireInfo num;
+    const void* states;
+    int N, P, fp32;
+    double* values;
+    double* under;
+    double* ex;
+    double* basis_buf;         // [5][P]
+    double* partials;          // [blocks][26][2]
+    const double* tenor_delta;     // [N] tenor period lengths (device)
+    const int* period_index;       // [nper] tenor index of each product period (device)
+    const double* period_length;   // [nper] product period lengths (device)
+    int init;                      // first launch: values = underlying = 0, exercise time = +inf
+    int final_pass;
+};
+
+template <typename TS>
+__device__ void bermudan_basis(const BermStepParams& a, int p, double B[5])
+{
+    const BermudanPeriod& c = a.cur;
+    if (a.basis == 1) {
+        // {S, S^2, N, N^2, S*N}: S = par rate of the remaining periods from L_j(T_ex)
+        double df = 1.0, ann = 0.0;
+        for (int q = c.swap_first; q < c.swap_last; q++) {
+            const double Lq = state_at<TS>(a.states, c.ex_slot, a.N, a.P, a.period_index[q], p);
+            const double dq = a.period_length[q];
+            df = (q == c.swap_first) ? 1.0 / (1.0 + Lq * dq) : df / (1.0 + Lq * dq);
+            ann = (q == c.swap_first) ? dq * df : ann + dq * df;
+        }
+        const double S = (1.0 - df) / ann;
+        const double Nn = numeraire_adj(a.num, c.ex_num_index, p);
+        B[0] = S;
+        B[1] = S * S;
+        B[2] = Nn;
+        B[3] = Nn * Nn;
+        B[4] = S * Nn;
+    } else {
+        // reference basis {P_short, P_short^2, P_long, P_long^2, 1/N} (BermudanSwaption.java:215-252)
+        const double rs = state_at<TS>(a.states, c.ex_slot, a.N, a.P, c.short_index, p);
+        const double ds = 1.0 / (rs * c.short_dt + 1.0);
+        double rl;
+        if (c.long_last == c.long_first + 1) {
+            rl = state_at<TS>(a.states, c.ex_slot, a.N, a.P, c.long_first, p);
+        } else {
+            double acc = 0.0;
+            for (int q = c.long_first; q < c.long_last; q++) {
+                const double Lq = state_at<TS>(a.states, c.ex_slot, a.N, a.P, q, p);
+                const double sub = a.tenor_delta[q];
+                acc = (q == c.long_first) ? Lq * sub + 1.0 : acc * (1.0 + Lq * sub);
+            }
+            rl = (acc - 1.0) / c.long_dt;
+        }
+        const double dl = 1.0 / (rl * c.long_dt + 1.0);
+        B[0] = ds;
+        B[1] = ds * ds;
+        B[2] = dl;
+        B[3] = dl * dl;
+        B[4] = 1.0 / numeraire_adj(a.num, c.ex_num_index, p);
+    }
+}
+
+template <typename TS>
+__global__ void __launch_bounds__(kProdThreads) bermudan_step_kernel(const BermStepParams a)
+{
+    const double w = 1.0 / (double)a.P;
+    dd acc[kGramEntries];
+#pragma unroll
+    for (int e = 0; e < kGramEntries; e++) acc[e] = dd{0.0, 0.0};
+    const bool gram = a.has_cur && a.cur.exercisable;
+    double beta[6];
+    if (a.apply_choose) {
+#pragma unroll
+        for (int i = 0; i < 6; i++) beta[i] = a.beta[i];
+    }
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.P; p += gridDim.x * blockDim.x) {
+        double v, u;
+        if (a.init) {
+            v = 0.0;
+            u = 0.0;
+            a.ex[p] = CUDART_INF;
+        } else {
+            v = a.values[p];
+            u = a.under[p];
+        }
+        if (a.apply_choose) {
+            // conditional expectation X beta (:104-107), then choose (:139, :141)
+            double ce = 1.0 * beta[0];
+#pragma unroll
+            for (int i = 1; i < 6; i++) ce = ce + a.basis_buf[(size_t)(i - 1) * a.P + p] * beta[i];
+            const bool cont = ce >= 0.0;
+            v = cont ? v : u;
+            if (!cont) a.ex[p] = a.choose_fixing;
+        }
+        if (a.has_cur) {
+            const BermudanPeriod& c = a.cur;
+            const double L = state_at<TS>(a.states, c.libor_slot, a.N, a.P, c.libor_index, p);
+            double payoff = ((L - c.strike) * c.period_length) * c.notional;
+            payoff = payoff / numeraire_adj(a.num, c.pay_num_index, p);
+            payoff = payoff * w;
+            if (a.callable) u = u + payoff;
+            else v = v + payoff;
+            if (gram) {
+                const double y = v - u;
+                double B[5];
+                bermudan_basis<TS>(a, p, B);
+#pragma unroll
+                for (int i = 0; i < 5; i++) a.basis_buf[(size_t)i * a.P + p] = B[i];
+                int e = 0;
+#pragma unroll
+                for (int i = 0; i < 5; i++) acc[e + i] = dd_add_d(acc[e + i], B[i]);  // G[0][1..5]
+                e += 5;
+#pragma unroll
+                for (int i = 0; i < 5; i++)
+#pragma unroll
+                    for (int j = i; j < 5; j++) {
+                        acc[e] = dd_add_d(acc[e], B[i] * B[j]);
+                        e++;
+                    }
+                acc[e] = dd_add_d(acc[e], y * 1.0);  // rhs[0] = mean(y * 1)
+                e++;
+#pragma unroll
+                for (int i = 0; i < 5; i++) acc[e + i] = dd_add_d(acc[e + i], y * B[i]);
+            }
+        }
+        if (a.final_pass) v = (v * 1.0) / w;
+        a.values[p] = v;
+        a.under[p] = u;
+    }
+    if (gram) {
+#pragma unroll
+        for (int e = 0; e < kGramEntries; e++) {
+            const dd s = block_dd_sum(acc[e]);
+            if (threadIdx.x == 0) {
+                a.partials[((size_t)blockIdx.x * kGramEntries + e) * 2] = s.hi;
+                a.partials[((size_t)blockIdx.x * kGramEntries + e) * 2 + 1] = s.lo;
+            }
+        }
+    }
+}
+
+// One-sided Jacobi SVD pseudo-inverse solve of the 6x6 normal equations.  The same
+// algorithm and cutoff as the oracle: singular values <= max(6 * s_max * 2^-52,
+// sqrt(2^-1022)) are dropped (SVD-based least squares, MonteCarloConditionalExpectationRegression.java:136,147).
+__device__ void solve_pinv6(const double Gin[36], const double b[6], double x[6])
+{
+    double U[36], V[36], s[6];
+    for (int i = 0; i < 36; i++) U[i] = Gin[i];
+    for (int i = 0; i < 6; i++)
+        for (int j = 0; j < 6; j++) V[i * 6 + j] = (i == j) ? 1.0 : 0.0;
+    for (int sweep = 0; sweep < 60; sweep++) {
+        int rotated = 0;
+        for (int p = 0; p < 5; p++)
+            for (int q = p + 1; q < 6; q++) {
+                double alpha = 0.0, beta = 0.0, gamma = 0.0;
+                for (int k = 0; k < 6; k++) {
+                    const double up = U[k * 6 + p], uq = U[k * 6 + q];
+                    alpha += up * up;
+                    beta += uq * uq;
+                    gamma += up * uq;
+                }
+                if (gamma == 0.0 || fabs(gamma) <= 1e-17 * sqrt(alpha * beta)) continue;
+                rotated = 1;
+                const double zeta = (beta - alpha) / (2.0 * gamma);
+                const double t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+                const double c = 1.0 / sqrt(1.0 + t * t), sn = c * t;
+                for (int k = 0; k < 6; k++) {
+                    const double up = U[k * 6 + p], uq = U[k * 6 + q];
+                    U[k * 6 + p] = c * up - sn * uq;
+                    U[k * 6 + q] = sn * up + c * uq;
+                }
+                for (int k = 0; k < 6; k++) {
+                    const double vp = V[k * 6 + p], vq = V[k * 6 + q];
+                    V[k * 6 + p] = c * vp - sn * vq;
+                    V[k * 6 + q] = sn * vp + c * vq;
+                }
+            }
+        if (!rotated) break;
+    }
+    double smax = 0.0;
+    for (int j = 0; j < 6; j++) {
+        double nn = 0.0;
+        for (int k = 0; k < 6; k++) nn += U[k * 6 + j] * U[k * 6 + j];
+        s[j] = sqrt(nn);
+        if (s[j] > 0.0)
+            for (int k = 0; k < 6; k++) U[k * 6 + j] = U[k * 6 + j] / s[j];
+        smax = s[j] > smax ? s[j] : smax;
+    }
+    double tol = 6.0 * smax * 0x1.0p-52;
+    const double tmin = sqrt(0x1.0p-1022);
+    if (tol < tmin) tol = tmin;
+    for (int i = 0; i < 6; i++) {
+        double acc = 0.0;
+        for (int j = 0; j < 6; j++) {
+            if (!(s[j] > tol)) continue;
+            double utb = 0.0;
+            for (int r = 0; r < 6; r++) utb += U[r * 6 + j] * b[r];
+            acc += V[i * 6 + j] * (utb / s[j]);
+        }
+        x[i] = acc;
+    }
+}
+
+__global__ void __launch_bounds__(256) bermudan_solve_kernel(const double* partials, int blocks, int P, double* beta_out)
+{
+    __shared__ double tot[kGramEntries];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nwarps = blockDim.x >> 5;
+    for (int e = warp; e < kGramEntries; e += nwarps) {
+        dd acc{0.0, 0.0};
+        for (int b = lane; b < blocks; b += 32) {
+            const double* q = partials + ((size_t)b * kGramEntries + e) * 2;
+            acc = dd_add(acc, dd{q[0], q[1]});
+        }
+        acc = warp_dd_sum(acc);
+        if (lane == 0) tot[e] = (acc.hi + acc.lo) / (double)P;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double G[36], rhs[6], x[6];
+        G[0] = 1.0 * 1.0;
+        int e = 0;
+        for (int j = 1; j < 6; j++) { G[j] = tot[e]; G[j * 6] = tot[e]; e++; }
+        for (int i = 1; i < 6; i++)
+            for (int j = i; j < 6; j++) { G[i * 6 + j] = tot[e]; G[j * 6 + i] = tot[e]; e++; }
+        for (int i = 0; i < 6; i++) rhs[i] = tot[e++];
+        solve_pinv6(G, rhs, x);
+        for (int i = 0; i < 6; i++) beta_out[i] = x[i];
+    }
+}
+
+NumeraireInfo make_numeraire_info(const ProductView& v)
+{
+    NumeraireInfo n;
+    n.P = v.P;
+    n.has_discount = v.h_discount != nullptr;
+    n.numeraire = v.d_numeraire;
+    n.adj = v.d_num_adj;
+    for (int l = 0; l <= kMaxN; l++) {
+        n.pd[l] = (v.h_discount && l <= v.N) ? v.h_discount[l] : 1.0;
+        n.det[l] = (l <= v.N) ? v.h_num_det[l] : 0;
+    }
+    return n;
+}
+
+int grid_for(int P, int threads, int max_blocks)
+{
+    int b = (P + threads - 1) / threads;
+    return b < max_blocks ? b : max_blocks;
+}
+
+}  // namespace
+
+int launch_numeraire_finish(const double* d_partials, int blocks, int N, int P, const double* d_numeraire,
+                            const uint8_t* d_det, double* d_adj, cudaStream_t s)
+{
+    KernelTimer kt(K_NUMERAIRE_FINISH, s);
+    numeraire_finish_kernel<<<N + 1, 256, 0, s>>>(d_partials, blocks, N, P, d_numeraire, d_det, d_adj);
+    LMM_CUDA(cudaGetLastError());
+    return LMM_OK;
+}
+
+int reduce_mean_stderr(const double* d_values, int P, double* d_scratch, size_t scratch_bytes, double* h_mean,
+                       double* h_stderr, cudaStream_t s)
+{
+    const int blocks = grid_for(P, 256, 1024);
+    if (scratch_bytes < (size_t)(2 * blocks + 2) * sizeof(double)) return fail(LMM_ERR_INVALID, "reduction scratch too small");
+    double* partials = d_scratch;
+    double* res = d_scratch + 2 * blocks;
+    {
+        KernelTimer kt(K_VALUE_REDUCE, s, 4);
+        sum_partials_kernel<<<blocks, 256, 0, s>>>(d_values, P, nullptr, partials);
+        finish_partials_kernel<<<1, 256, 0, s>>>(partials, blocks, P, res);
+        sum_partials_kernel<<<blocks, 256, 0, s>>>(d_values, P, res, partials);
+        finish_partials_kernel<<<1, 256, 0, s>>>(partials, blocks, P, res + 1);
+        LMM_CUDA(cudaGetLastError());
+    }
+    double h[2];
+    LMM_CUDA(cudaMemcpyAsync(h, res, sizeof(h), cudaMemcpyDeviceToHost, s));
+    LMM_CUDA(cudaStreamSynchronize(s));
+    *h_mean = h[0];
+    if (h_stderr) *h_stderr = P > 1 ? sqrt(h[1]) / sqrt((double)P) : 0.0;
+    return LMM_OK;
+}
+
+int launch_swaption(const ProductView& v, const SwaptionLaunch& a, double* d_values, cudaStream_t s)
+{
+    SwaptionParams prm;
+    prm.s = a;
+    prm.num = make_numeraire_info(v);
+    prm.states = v.d_states;
+    prm.N = v.N;
+    prm.P = v.P;
+    prm.fp32 = v.state_fp32;
+    prm.values = d_values;
+    const int blocks = (v.P + kProdThreads - 1) / kProdThreads;
+    KernelTimer kt(K_SWAPTION, s);
+    if (v.state_fp32) swaption_kernel<float><<<blocks, kProdThreads, 0, s>>>(prm);
+    else swaption_kernel<double><<<blocks, kProdThreads, 0, s>>>(prm);
+    LMM_CUDA(cudaGetLastError());
+    return LMM_OK;
+}
+
+int bermudan_blocks(int P)
+{
+    static int cap = 0;
+    if (!cap) {
+        int dev = 0, sms = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            sms = 152;
+        cap = sms * 4;
+    }
+    return grid_for(P, kProdThreads, cap);
+}
+
+int launch_bermudan(const ProductView& v, const BermudanLaunch& a, const BermudanScratch& sc, cudaStream_t s,
+                    int* launches)
+{
+    const int blocks = bermudan_blocks(v.P);
+    BermStepParams prm;
+    std::memset(&prm, 0, sizeof(prm));
+    prm.basis = a.basis;
+    prm.callable = a.callable;
+    prm.num = make_numeraire_info(v);
+    prm.states = v.d_states;
+    prm.N = v.N;
+    prm.P = v.P;
+    prm.fp32 = v.state_fp32;
+    prm.values = sc.d_values;
+    prm.under = sc.d_under;
+    prm.ex = sc.d_ex;
+    prm.basis_buf = sc.d_basis;
+    prm.partials = sc.d_partials;
+    prm.tenor_delta = sc.d_tenor_delta;
+    prm.period_index = sc.d_period_index;
+    prm.period_length = sc.d_period_length;
+    int pending = -1;  // exercise period whose choose is pending
+    for (int per = a.nper - 1; per >= -1; per--) {
+        prm.has_cur = per >= 0;
+        if (per >= 0) prm.cur = a.per[per];
+        prm.apply_choose = pending >= 0;
+        if (pending >= 0) {
+            prm.beta = sc.d_beta + (size_t)pending * 6;
+            prm.choose_fixing = a.per[pending].fixing;
+        }
+        prm.final_pass = per < 0;
+        prm.init = per == a.nper - 1;
+        {
+            KernelTimer kt(K_BERMUDAN_STEP, s);
+            if (v.state_fp32) bermudan_step_kernel<float><<<blocks, kProdThreads, 0, s>>>(prm);
+            else bermudan_step_kernel<double><<<blocks, kProdThreads, 0, s>>>(prm);
+            LMM_CUDA(cudaGetLastError());
+        }
+        if (launches) (*launches)++;
+        pending = -1;
+        if (per >= 0 && a.per[per].exercisable) {
+            KernelTimer kt(K_BERMUDAN_SOLVE, s);
+            bermudan_solve_kernel<<<1, 256, 0, s>>>(sc.d_partials, blocks, v.P, sc.d_beta + (size_t)per * 6);
+            LMM_CUDA(cudaGetLastError());
+            if (launches) (*launches)++;
+            pending = per;
+        }
+    }
+    return LMM_OK;
+}
+
+}  // namespace lmm

@@ -1,0 +1,82 @@
+// reduce.cuh -- deterministic compensated (double-double) reductions.
+//
+// The reference averages with Kahan summation in path order
+// (montecarlo/RandomVariableFromDoubleArray.java:287-308).  On the GPU every partial
+// sum is an unevaluated pair hi + lo built from error-free TwoSum steps, combined in a
+// fixed tree (lane order, warp order, block order), so results are reproducible run to
+// run and agree with the sequential Kahan sum to within one rounding.  TwoSum has no
+// products, so FMA contraction cannot change it.
+#pragma once
+
+namespace lmm {
+
+struct dd {
+    double hi, lo;
+};
+
+__device__ __forceinline__ void two_sum(double a, double b, double& s, double& e)
+{
+    s = a + b;
+    const double bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+__device__ __forceinline__ dd dd_add(dd x, dd y)
+{
+    double s, e;
+    two_sum(x.hi, y.hi, s, e);
+    e = e + (x.lo + y.lo);
+    const double hi = s + e;
+    return dd{hi, e - (hi - s)};
+}
+
+__device__ __forceinline__ dd dd_add_d(dd x, double y)
+{
+    double s, e;
+    two_sum(x.hi, y, s, e);
+    e = e + x.lo;
+    const double hi = s + e;
+    return dd{hi, e - (hi - s)};
+}
+
+__device__ __forceinline__ dd warp_dd_sum(dd v)
+{
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        dd o;
+        o.hi = __shfl_down_sync(0xffffffffu, v.hi, off);
+        o.lo = __shfl_down_sync(0xffffffffu, v.lo, off);
+        v = dd_add(v, o);
+    }
+    return v;
+}
+
+// Block-wide sum; the full result is valid in thread 0.  All threads must call it.
+__device__ __forceinline__ dd block_dd_sum(dd v)
+{
+    __shared__ dd warp_part[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nwarps = (blockDim.x + 31) >> 5;
+    v = warp_dd_sum(v);
+    if (lane == 0) warp_part[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        dd w = (lane < nwarps) ? warp_part[lane] : dd{0.0, 0.0};
+        w = warp_dd_sum(w);
+        if (lane == 0) v = w;
+    }
+    __syncthreads();
+    return v;
+}
+
+// Block-wide sum of one double per thread written as (hi, lo) to out[0..1] by thread 0.
+__device__ __forceinline__ void block_dd_partial(double x, double* out)
+{
+    const dd s = block_dd_sum(dd{x, 0.0});
+    if (threadIdx.x == 0) {
+        out[0] = s.hi;
+        out[1] = s.lo;
+    }
+}
+
+}  // namespace lmm

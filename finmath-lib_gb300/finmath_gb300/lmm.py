@@ -1,0 +1,430 @@
+"""Host-side mirror of finmath-lib's API for the LIBOR Market Model Monte Carlo path.
+
+Class and method names follow finmath-lib (src/main/java/net/finmath/...), so code and
+tests read like the reference's: build a TimeDiscretizationFromArray, a covariance model,
+LIBORMarketModelFromCovarianceModel.of(...), a BrownianMotionFromMersenneRandomNumbers,
+an EulerSchemeFromProcessModel, wrap it in LIBORMonteCarloSimulationFromLIBORModel and
+ask products for getValue(model).  Every numeric step runs in liblmm_gb300.so: host
+setup in its C++ part, simulation and valuation in its CUDA kernels.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from ._lib import check
+
+_D = ctypes.POINTER(ctypes.c_double)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(_D)
+
+
+# --------------------------------------------------------------------------- time
+class TimeDiscretizationFromArray:
+    """net.finmath.time.TimeDiscretizationFromArray (tick-rounded, sorted)."""
+
+    def __init__(self, initial_or_times, numberOfTimeSteps: int | None = None, deltaT: float | None = None):
+        L = _lib.load()
+        if numberOfTimeSteps is None:
+            t = np.unique(np.asarray([np.rint(x / (1.0 / (365.0 * 24.0))) * (1.0 / (365.0 * 24.0))
+                                      for x in initial_or_times], dtype=np.float64))
+            self._t = t
+        else:
+            out = np.empty(numberOfTimeSteps + 1)
+            check(L.lmm_time_discretization(float(initial_or_times), int(numberOfTimeSteps), float(deltaT), _p(out)),
+                  "TimeDiscretizationFromArray")
+            self._t = out
+
+    def getNumberOfTimes(self):
+        return len(self._t)
+
+    def getNumberOfTimeSteps(self):
+        return len(self._t) - 1
+
+    def getTime(self, i):
+        return float(self._t[i])
+
+    def getTimeStep(self, i):
+        return float(self._t[i + 1] - self._t[i])
+
+    def getTimeIndex(self, time: float) -> int:
+        key = np.rint(time / (1.0 / (365.0 * 24.0))) * (1.0 / (365.0 * 24.0))
+        i = int(np.searchsorted(self._t, key))
+        if i < len(self._t) and self._t[i] == key:
+            return i
+        return -(i + 1)
+
+    def getAsDoubleArray(self):
+        return self._t.copy()
+
+
+# --------------------------------------------------------------------------- curves
+class ForwardCurveInterpolation:
+    """ForwardCurveInterpolation with LINEAR interpolation on values, CONSTANT extrapolation."""
+
+    def __init__(self, name, times, forwards, paymentOffset):
+        self.name = name
+        self.times = _f64(times)
+        self.forwards = _f64(forwards)
+        self.paymentOffset = float(paymentOffset)
+
+    @staticmethod
+    def createForwardCurveFromForwards(name, times, givenForwards, paymentOffset):
+        return ForwardCurveInterpolation(name, times, givenForwards, paymentOffset)
+
+    def getPaymentOffset(self, fixingTime=None):
+        return self.paymentOffset
+
+    def getForward(self, model, fixingTime, paymentOffset=None):
+        out = ctypes.c_double()
+        check(_lib.load().lmm_forward_curve_value(_p(self.times), _p(self.forwards), len(self.times), float(fixingTime),
+                                                  ctypes.byref(out)), "getForward")
+        f = out.value
+        if paymentOffset is not None and paymentOffset != self.paymentOffset:
+            po = self.paymentOffset
+            f = (np.exp(np.log(1 + f * po) * paymentOffset / po) - 1.0) / paymentOffset
+        return f
+
+
+class DiscountCurveFromForwardCurve:
+    def __init__(self, forwardCurve: ForwardCurveInterpolation):
+        self.forwardCurve = forwardCurve
+
+    def getDiscountFactor(self, model, maturity=None):
+        if maturity is None:
+            maturity = model
+        c = self.forwardCurve
+        out = ctypes.c_double()
+        check(_lib.load().lmm_discount_factor_from_forward_curve(_p(c.times), _p(c.forwards), len(c.times),
+                                                                  c.paymentOffset, float(maturity), ctypes.byref(out)),
+              "getDiscountFactor")
+        return out.value
+
+
+# --------------------------------------------------------------------------- covariance
+class LIBORCorrelationModelExponentialDecay:
+    def __init__(self, timeDiscretization, liborPeriodDiscretization, numberOfFactors, a, isCalibrateable=False):
+        tenor = liborPeriodDiscretization.getAsDoubleArray()
+        N = len(tenor) - 1
+        self.factorMatrix = np.empty((N, numberOfFactors))
+        self.correlationMatrix = np.empty((N, N))
+        check(_lib.load().lmm_correlation_exponential_decay(_p(_f64(tenor)), N, int(numberOfFactors), float(a),
+                                                           _p(self.factorMatrix), _p(self.correlationMatrix)),
+              "LIBORCorrelationModelExponentialDecay")
+
+    def getNumberOfFactors(self):
+        return self.factorMatrix.shape[1]
+
+    def getFactorLoading(self, timeIndex, factor, component):
+        return float(self.factorMatrix[component, factor])
+
+    def getCorrelation(self, timeIndex, component1, component2):
+        return float(self.correlationMatrix[component1, component2])
+
+
+class LIBORVolatilityModelFourParameterExponentialForm:
+    def __init__(self, timeDiscretization, liborPeriodDiscretization, a, b, c, d, isCalibrateable=False):
+        t = _f64(timeDiscretization.getAsDoubleArray())
+        tn = _f64(liborPeriodDiscretization.getAsDoubleArray())
+        T, N = len(t) - 1, len(tn) - 1
+        self.volatility = np.empty((T, N))
+        check(_lib.load().lmm_volatility_four_parameter(_p(t), T, _p(tn), N, float(a), float(b), float(c), float(d),
+                                                       _p(self.volatility)), "LIBORVolatilityModelFourParameterExponentialForm")
+
+    def getVolatility(self, timeIndex, liborIndex):
+        return float(self.volatility[timeIndex, liborIndex])
+
+
+class LIBORVolatilityModelFromGivenMatrix:
+    def __init__(self, timeDiscretization, liborPeriodDiscretization, volatility):
+        self.volatility = _f64(volatility)
+
+    def getVolatility(self, timeIndex, liborIndex):
+        return float(self.volatility[timeIndex, liborIndex])
+
+
+class LIBORCovarianceModelFromVolatilityAndCorrelation:
+    def __init__(self, timeDiscretization, liborPeriodDiscretization, volatilityModel, correlationModel):
+        vol = _f64(volatilityModel.volatility)
+        fm = _f64(correlationModel.factorMatrix)
+        corr = _f64(correlationModel.correlationMatrix)
+        T, N = vol.shape
+        F = fm.shape[1]
+        self.factorLoadings = np.empty((T, N, F))
+        self.variance = np.empty((T, N))
+        check(_lib.load().lmm_covariance_tables(T, N, F, _p(vol), _p(fm), _p(corr), _p(self.factorLoadings),
+                                               _p(self.variance)), "LIBORCovarianceModelFromVolatilityAndCorrelation")
+        self.timeDiscretization = timeDiscretization
+        self.liborPeriodDiscretization = liborPeriodDiscretization
+
+    def getNumberOfFactors(self):
+        return self.factorLoadings.shape[2]
+
+    def getFactorLoading(self, timeIndex, component):
+        return self.factorLoadings[timeIndex, component].copy()
+
+    def getCovariance(self, timeIndex, component1, component2):
+        if component1 != component2:
+            return float(np.dot(self.factorLoadings[timeIndex, component1], self.factorLoadings[timeIndex, component2]))
+        return float(self.variance[timeIndex, component1])
+
+
+# --------------------------------------------------------------------------- model
+class LIBORMarketModelFromCovarianceModel:
+    """The model's tables as finmath-lib evaluates them (LIBORMarketModelFromCovarianceModel.java:388-444)."""
+
+    MEASURE_SPOT = "SPOT"
+    STATE_LOGNORMAL = "LOGNORMAL"
+
+    def __init__(self, liborPeriodDiscretization, analyticModel, forwardRateCurve, discountCurve, randomVariableFactory,
+                 covarianceModel, calibrationItems=None, properties=None):
+        props = dict(properties or {})
+        if str(props.get("measure", "SPOT")).upper() != "SPOT":
+            raise ValueError("only the SPOT measure is implemented on this path")
+        if str(props.get("stateSpace", "LOGNORMAL")).upper() != "LOGNORMAL":
+            raise ValueError("only the LOGNORMAL state space is implemented on this path")
+        if calibrationItems:
+            raise ValueError("calibration is not part of this path")
+        self.liborPeriodDiscretization = liborPeriodDiscretization
+        self.forwardRateCurve = forwardRateCurve
+        self.discountCurve = discountCurve
+        self.covarianceModel = covarianceModel
+        self.liborCap = float(props.get("liborCap", 1e5))
+        tenor = liborPeriodDiscretization.getAsDoubleArray()
+        N = len(tenor) - 1
+        # getInitialState (:1081-1093): forward over [T_j, T_j + delta_j]
+        self.initialForwards = np.array([forwardRateCurve.getForward(None, tenor[j], tenor[j + 1] - tenor[j])
+                                         for j in range(N)])
+        self.discountChain = None
+        if discountCurve is not None:
+            df = _f64([discountCurve.getDiscountFactor(None, t) for t in tenor])
+            self.discountChain = np.empty(N + 1)
+            check(_lib.load().lmm_numeraire_discount_chain(_p(_f64(tenor)), N, _p(df), _p(self.discountChain)),
+                  "numeraire adjustment")
+
+    @staticmethod
+    def of(liborPeriodDiscretization, analyticModel, forwardRateCurve, discountCurve, randomVariableFactory,
+           covarianceModel, calibrationItems=None, properties=None):
+        return LIBORMarketModelFromCovarianceModel(liborPeriodDiscretization, analyticModel, forwardRateCurve,
+                                                   discountCurve, randomVariableFactory, covarianceModel,
+                                                   calibrationItems, properties)
+
+    def getNumberOfComponents(self):
+        return self.liborPeriodDiscretization.getNumberOfTimeSteps()
+
+
+# --------------------------------------------------------------------------- Brownian motion
+class BrownianMotionFromMersenneRandomNumbers:
+    """GPU-resident BrownianMotionFromMersenneRandomNumbers (bit-exact MT19937 uniforms)."""
+
+    def __init__(self, timeDiscretization, numberOfFactors, numberOfPaths, seed, precision=_lib.PRECISION_FP64):
+        self._L = _lib.load()
+        self.timeDiscretization = timeDiscretization
+        self.numberOfFactors = int(numberOfFactors)
+        self.numberOfPaths = int(numberOfPaths)
+        self.seed = int(seed)
+        self.precision = precision
+        self._times = _f64(timeDiscretization.getAsDoubleArray())
+        h = ctypes.c_void_p()
+        check(self._L.lmm_brownian_create(_p(self._times), len(self._times), self.numberOfFactors, self.numberOfPaths,
+                                          self.seed, int(precision), ctypes.byref(h)), "BrownianMotionFromMersenneRandomNumbers")
+        self._h = h
+
+    def getBrownianIncrement(self, timeIndex, factor) -> np.ndarray:
+        out = np.empty(self.numberOfPaths)
+        check(self._L.lmm_brownian_get_increment(self._h, int(timeIndex), int(factor), _p(out)), "getBrownianIncrement")
+        return out
+
+    getIncrement = getBrownianIncrement
+
+    def getTimeDiscretization(self):
+        return self.timeDiscretization
+
+    def getNumberOfFactors(self):
+        return self.numberOfFactors
+
+    def getNumberOfPaths(self):
+        return self.numberOfPaths
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.lmm_brownian_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def mersenne_twister_uniforms(seed: int, count: int, offset: int = 0) -> np.ndarray:
+    """The first values of MersenneTwister(seed).nextDouble(), generated on the GPU."""
+    out = np.empty(count)
+    check(_lib.load().lmm_mt19937_uniforms(int(seed), int(offset), int(count), _p(out)), "lmm_mt19937_uniforms")
+    return out
+
+
+# --------------------------------------------------------------------------- process
+class EulerSchemeFromProcessModel:
+    EULER = _lib.SCHEME_EULER
+    EULER_FUNCTIONAL = _lib.SCHEME_EULER_FUNCTIONAL
+
+    def __init__(self, model: LIBORMarketModelFromCovarianceModel, brownianMotion: BrownianMotionFromMersenneRandomNumbers,
+                 scheme=None, observedTimeIndices=None):
+        self._L = _lib.load()
+        self.model = model
+        self.brownianMotion = brownianMotion
+        self.scheme = _lib.SCHEME_EULER_FUNCTIONAL if scheme is None else scheme
+        cov = model.covarianceModel
+        self._keep = dict(times=_f64(brownianMotion._times), tenor=_f64(model.liborPeriodDiscretization.getAsDoubleArray()),
+                          lam=_f64(cov.factorLoadings), var=_f64(cov.variance), init=_f64(model.initialForwards),
+                          chain=None if model.discountChain is None else _f64(model.discountChain))
+        k = self._keep
+        T = len(k["times"]) - 1
+        N = len(k["tenor"]) - 1
+        desc = _lib.LmmModelDesc(T, _p(k["times"]), N, _p(k["tenor"]), cov.getNumberOfFactors(), _p(k["lam"]),
+                                 _p(k["var"]), _p(k["init"]), _p(k["chain"]), model.liborCap, int(self.scheme), 0, 0)
+        h = ctypes.c_void_p()
+        check(self._L.lmm_process_create(ctypes.byref(desc), brownianMotion._h, ctypes.byref(h)), "EulerSchemeFromProcessModel")
+        self._h = h
+        self.numberOfPaths = brownianMotion.numberOfPaths
+        if observedTimeIndices is not None:
+            mask = np.zeros(T + 1, dtype=np.uint8)
+            mask[np.asarray(list(observedTimeIndices), dtype=np.int64)] = 1
+            check(self._L.lmm_process_set_observed_times(self._h, mask.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))),
+                  "observed times")
+
+    def getProcessValue(self, timeIndex, componentIndex) -> np.ndarray:
+        out = np.empty(self.numberOfPaths)
+        check(self._L.lmm_process_get_value(self._h, int(timeIndex), int(componentIndex), _p(out)), "getProcessValue")
+        return out
+
+    def simulate(self):
+        check(self._L.lmm_process_simulate(self._h), "doPrecalculateProcess")
+
+    def getNumeraire(self, time) -> np.ndarray:
+        out = np.empty(self.numberOfPaths)
+        check(self._L.lmm_process_get_numeraire(self._h, float(time), _p(out)), "getNumeraire")
+        return out
+
+    def getTimeDiscretization(self):
+        return self.brownianMotion.timeDiscretization
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.lmm_process_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class LIBORMonteCarloSimulationFromLIBORModel:
+    def __init__(self, process: EulerSchemeFromProcessModel):
+        self.process = process
+        self.model = process.model
+
+    def getLIBOR(self, timeIndex, liborIndex):
+        return self.process.getProcessValue(timeIndex, liborIndex)
+
+    def getNumeraire(self, time):
+        return self.process.getNumeraire(time)
+
+    def getNumberOfPaths(self):
+        return self.process.numberOfPaths
+
+    def getTimeDiscretization(self):
+        return self.process.getTimeDiscretization()
+
+    def getLiborPeriodDiscretization(self):
+        return self.model.liborPeriodDiscretization
+
+
+# --------------------------------------------------------------------------- products
+class Swaption:
+    """net.finmath.montecarlo.interestrate.products.Swaption."""
+
+    def __init__(self, exerciseDate, fixingDates, paymentDates, swaprates, periodLengths=None, notional=1.0):
+        self.exerciseDate = float(exerciseDate)
+        self.fixingDates = _f64(fixingDates)
+        self.paymentDates = _f64(paymentDates)
+        self.swaprates = _f64(np.broadcast_to(swaprates, self.fixingDates.shape))
+        self.periodLengths = None if periodLengths is None else _f64(periodLengths)
+        self.notional = float(notional)
+
+    def getValues(self, model: LIBORMonteCarloSimulationFromLIBORModel):
+        d = _lib.LmmSwaptionDesc(self.exerciseDate, len(self.fixingDates), _p(self.fixingDates), _p(self.paymentDates),
+                                 _p(self.periodLengths), _p(self.swaprates), self.notional)
+        v, e = ctypes.c_double(), ctypes.c_double()
+        check(_lib.load().lmm_swaption_get_value(model.process._h, ctypes.byref(d), ctypes.byref(v), ctypes.byref(e)),
+              "Swaption.getValue")
+        return {"value": v.value, "error": e.value}
+
+    def getValue(self, model):
+        return self.getValues(model)["value"]
+
+
+class BermudanSwaption:
+    """net.finmath.montecarlo.interestrate.products.BermudanSwaption.
+
+    regressionBasisFunctionsProvider: None for the reference's built-in basis, or
+    "swaprate" for the {1, S, S^2, N, N^2, S*N} provider.
+    """
+
+    def __init__(self, isPeriodStartDateExerciseDate, fixingDates, periodLength, paymentDates, periodNotionals, swaprates,
+                 isCallable=True, regressionBasisFunctionsProvider=None):
+        self.isPeriodStartDateExerciseDate = np.ascontiguousarray(isPeriodStartDateExerciseDate, dtype=np.uint8)
+        n = len(self.isPeriodStartDateExerciseDate)
+        self.fixingDates = _f64(fixingDates)
+        self.periodLengths = _f64(np.broadcast_to(periodLength, (n,)))
+        self.paymentDates = _f64(paymentDates)
+        self.periodNotionals = _f64(np.broadcast_to(periodNotionals, (n,)))
+        self.swaprates = _f64(np.broadcast_to(swaprates, (n,)))
+        self.isCallable = bool(isCallable)
+        if regressionBasisFunctionsProvider in (None, "reference"):
+            self.basis = _lib.BASIS_REFERENCE
+        elif regressionBasisFunctionsProvider == "swaprate":
+            self.basis = _lib.BASIS_SWAPRATE
+        else:
+            raise ValueError("unknown regression basis provider")
+
+    def getValues(self, model: LIBORMonteCarloSimulationFromLIBORModel, per_path: bool = False):
+        d = _lib.LmmBermudanDesc(len(self.fixingDates),
+                                 self.isPeriodStartDateExerciseDate.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)),
+                                 _p(self.fixingDates), _p(self.periodLengths), _p(self.paymentDates),
+                                 _p(self.periodNotionals), _p(self.swaprates), int(self.isCallable), self.basis)
+        v, e = ctypes.c_double(), ctypes.c_double()
+        pp = np.empty(model.getNumberOfPaths()) if per_path else None
+        check(_lib.load().lmm_bermudan_get_value(model.process._h, ctypes.byref(d), ctypes.byref(v), ctypes.byref(e),
+                                                 _p(pp)), "BermudanSwaption.getValues")
+        out = {"value": v.value, "error": e.value}
+        if per_path:
+            out["values"] = pp
+        return out
+
+    def getValue(self, model):
+        return self.getValues(model)["value"]
+
+
+# --------------------------------------------------------------------------- instrumentation
+def kernel_stats():
+    L = _lib.load()
+    n = 16
+    names = (ctypes.c_char_p * n)()
+    launches = (ctypes.c_int64 * n)()
+    ms = (ctypes.c_double * n)()
+    k = L.lmm_stats_get(n, names, launches, ms)
+    return {names[i].decode(): (int(launches[i]), float(ms[i])) for i in range(k)}

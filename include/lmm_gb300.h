@@ -1,0 +1,206 @@
+/*
+ * lmm_gb300.h -- C ABI of the GB300-native LIBOR Market Model Monte Carlo library.
+ *
+ * This is the drop-in boundary a finmath-lib host binds (JNI / Panama FFM / ctypes):
+ * plain C types, host pointers and sizes, no CUDA or torch types.  Every entry point
+ * names the finmath-lib interface it replaces (file:line in finmath-lib's
+ * src/main/java/net/finmath/ tree).
+ *
+ * Conventions
+ *   - Every function returns an int status: LMM_OK (0) or a negative LMM_ERR_* code;
+ *     lmm_last_error() returns a thread-local message for the last failure.  A finmath
+ *     shim maps these to CalculationException (valuation path) or
+ *     IllegalArgumentException (invalid arguments).
+ *   - Host arrays are caller-owned and copied on input; device memory is owned by the
+ *     handle and released by the matching *_destroy.
+ *   - A handle is used by one thread at a time (the Java shim serialises per handle,
+ *     as finmath's lazy initialisation is synchronized); different handles may be used
+ *     concurrently.  Each handle enqueues its work on its own CUDA stream.
+ *   - Arrays of random variables are [index][path] row-major: one contiguous path
+ *     vector per (time, component), i.e. RandomVariable.getRealizations() layout.
+ */
+#ifndef LMM_GB300_H
+#define LMM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LMM_OK 0
+#define LMM_ERR_INVALID (-1)   /* invalid argument or unsupported configuration */
+#define LMM_ERR_NOMEM (-2)     /* device or host allocation failed */
+#define LMM_ERR_CUDA (-3)      /* CUDA runtime error (message holds the CUDA error string) */
+#define LMM_ERR_TIMEOUT (-4)   /* a bounded device-side wait gave up */
+#define LMM_ERR_STATE (-5)     /* call out of order (e.g. value requested before simulation) */
+
+/* Precision forms of the path. */
+#define LMM_PRECISION_FP64 0   /* plain FP64: the parity form */
+#define LMM_PRECISION_MIXED 1  /* FP32 log-space paths, FP64 numeraire / regression / sums */
+
+/* Discretisation schemes: EulerSchemeFromProcessModel.Scheme (montecarlo/process/EulerSchemeFromProcessModel.java:68-73). */
+#define LMM_SCHEME_EULER 0
+#define LMM_SCHEME_EULER_FUNCTIONAL 1
+
+/* Regression bases of the Bermudan swaption. */
+#define LMM_BASIS_REFERENCE 0  /* BermudanSwaption.getBasisFunctions: {1, P_short, P_short^2, P_long, P_long^2, 1/N} (…/products/BermudanSwaption.java:215-252) */
+#define LMM_BASIS_SWAPRATE 1   /* a RegressionBasisFunctionsProvider giving {1, S, S^2, N, N^2, S*N} (conditionalexpectation/RegressionBasisFunctionsProvider.java:28) */
+
+const char* lmm_last_error(void);
+int lmm_version(void);
+
+/* ---------------------------------------------------------------- host-side model setup
+ * Tables a finmath shim can equally take from its own Java objects. */
+
+/* TimeDiscretizationFromArray(initial, numberOfTimeSteps, deltaT) with tick rounding
+ * (time/TimeDiscretizationFromArray.java:210-217, 387-389).  out has num_steps+1 entries. */
+int lmm_time_discretization(double initial, int num_steps, double dt, double* out_times);
+
+/* LinearAlgebra.factorReduction (functions/LinearAlgebra.java:380-482): n x n
+ * correlation -> n x num_factors factor matrix (row-major). */
+int lmm_factor_reduction(const double* correlation, int n, int num_factors, double* out_factors);
+
+/* LIBORCorrelationModelExponentialDecay (…/covariance/LIBORCorrelationModelExponentialDecay.java:102-134):
+ * rho_ij = exp(-a |T_i - T_j|) reduced to num_factors; outputs the factor matrix
+ * [num_periods][num_factors] and the reduced correlation [num_periods][num_periods]. */
+int lmm_correlation_exponential_decay(const double* tenor, int num_periods, int num_factors, double a,
+                                      double* out_factor_matrix, double* out_correlation);
+
+/* LIBORVolatilityModelFourParameterExponentialForm.getVolatility
+ * (…/covariance/LIBORVolatilityModelFourParameterExponentialForm.java:168-194): out [num_steps][num_periods]. */
+int lmm_volatility_four_parameter(const double* times, int num_steps, const double* tenor, int num_periods,
+                                  double a, double b, double c, double d, double* out_volatility);
+
+/* LIBORCovarianceModelFromVolatilityAndCorrelation.getFactorLoading / getCovariance
+ * (…/covariance/LIBORCovarianceModelFromVolatilityAndCorrelation.java:48-57, 83-93):
+ * loadings [num_steps][num_periods][num_factors], variance [num_steps][num_periods]. */
+int lmm_covariance_tables(int num_steps, int num_periods, int num_factors, const double* volatility,
+                          const double* factor_matrix, const double* correlation, double* out_loadings,
+                          double* out_variance);
+
+/* ForwardCurveInterpolation (LINEAR on values, CONSTANT extrapolation) value at t
+ * (marketdata/model/curves/ForwardCurveInterpolation.java:224-233, 298-346). */
+int lmm_forward_curve_value(const double* nodes, const double* values, int num_nodes, double t, double* out);
+
+/* DiscountCurveFromForwardCurve.getDiscountFactor (marketdata/model/curves/DiscountCurveFromForwardCurve.java:115-140). */
+int lmm_discount_factor_from_forward_curve(const double* nodes, const double* values, int num_nodes,
+                                           double payment_offset, double maturity, double* out);
+
+/* The deterministic numeraire adjustment P^d(T_i) chain of
+ * LIBORMarketModelFromCovarianceModel.getNumeraireDefaultableZeroBondAsOfTimeZero
+ * (…/models/LIBORMarketModelFromCovarianceModel.java:915-944); df has num_periods+1 entries. */
+int lmm_numeraire_discount_chain(const double* tenor, int num_periods, const double* discount_factors,
+                                 double* out_chain);
+
+/* ---------------------------------------------------------------- Brownian motion */
+typedef struct lmm_brownian lmm_brownian;
+
+/* new BrownianMotionFromMersenneRandomNumbers(timeDiscretization, numberOfFactors, numberOfPaths, seed)
+ * (montecarlo/BrownianMotionFromMersenneRandomNumbers.java:69-103).  Generation is lazy,
+ * as in the reference (:123-131): it runs at the first increment request or simulation. */
+int lmm_brownian_create(const double* times, int num_times, int num_factors, int num_paths, int seed,
+                        int precision, lmm_brownian** out);
+/* getBrownianIncrement(timeIndex, factor) (:123-136): num_paths doubles. */
+int lmm_brownian_get_increment(lmm_brownian* bm, int time_index, int factor, double* out_host);
+/* doGenerateBrownianMotion (:141-191), explicit trigger. */
+int lmm_brownian_generate(lmm_brownian* bm);
+int lmm_brownian_destroy(lmm_brownian* bm);
+
+/* The MT19937 stream of commons-math3 MersenneTwister(seed).nextDouble() as used by
+ * randomnumbers/MersenneTwister.java:42-51, values [offset, offset+count) generated on
+ * the GPU by the same partitioned generator. */
+int lmm_mt19937_uniforms(int64_t seed, int64_t offset, int64_t count, double* out_host);
+
+/* The same stream computed on the host by one GF(2) jump of `skip` words followed by
+ * sequential generation: tempered 32-bit words [skip, skip+count).  A check of the jump
+ * polynomials that needs no GPU; not a production path. */
+int lmm_mt19937_words_host(int64_t seed, uint64_t skip, uint64_t count, uint32_t* out);
+
+/* ---------------------------------------------------------------- LMM process */
+typedef struct {
+    int num_steps;                  /* T: simulation time steps */
+    const double* times;            /* T+1 simulation times (the Brownian motion's grid) */
+    int num_periods;                /* N: forward rates */
+    const double* tenor;            /* N+1 tenor times */
+    int num_factors;                /* F */
+    const double* factor_loadings;  /* [T][N][F]  lambda_{i,j,k} = sigma_{i,j} f_{j,k} */
+    const double* variance;         /* [T][N]     getCovariance(t_i, j, j) */
+    const double* initial_forwards; /* [N]        forward curve at T_j over the period */
+    const double* discount_chain;   /* [N+1]      P^d(T_l), or NULL for no discount curve */
+    double libor_cap;               /* liborCap property (default 1e5); +inf disables */
+    int scheme;                     /* LMM_SCHEME_* */
+    int measure;                    /* 0 = SPOT (the only measure of this path) */
+    int state_space;                /* 0 = LOGNORMAL (the only state space of this path) */
+} lmm_model_desc;
+
+typedef struct lmm_process lmm_process;
+
+/* LIBORMarketModelFromCovarianceModel.of(...) (…/models/LIBORMarketModelFromCovarianceModel.java:283, 388-444)
+ * + new EulerSchemeFromProcessModel(model, brownianMotion) (montecarlo/process/EulerSchemeFromProcessModel.java:101-123)
+ * + new LIBORMonteCarloSimulationFromLIBORModel(process) (montecarlo/interestrate/LIBORMonteCarloSimulationFromLIBORModel.java:32-37).
+ * The process keeps a reference to bm (which must outlive it) and uses bm's precision. */
+int lmm_process_create(const lmm_model_desc* model, lmm_brownian* bm, lmm_process** out);
+/* Restrict storage to the time indices in mask[T+1] (non-zero = keep).  The default is
+ * every time index (the reference materialises all).  Products need the tenor times. */
+int lmm_process_set_observed_times(lmm_process* proc, const uint8_t* mask);
+/* doPrecalculateProcess (EulerSchemeFromProcessModel.java:170-326), explicit trigger;
+ * the getters below trigger it lazily. */
+int lmm_process_simulate(lmm_process* proc);
+/* getProcessValue(timeIndex, component) (:132-146) == getLIBOR(timeIndex, liborIndex)
+ * (LIBORMarketModelFromCovarianceModel.java:1308-1312): num_paths doubles. */
+int lmm_process_get_value(lmm_process* proc, int time_index, int component, double* out_host);
+/* LIBORMonteCarloSimulationFromLIBORModel.getNumeraire(time) (:153-155) at a tenor time: num_paths doubles. */
+int lmm_process_get_numeraire(lmm_process* proc, double time, double* out_host);
+int lmm_process_destroy(lmm_process* proc);
+
+/* ---------------------------------------------------------------- products */
+typedef struct {
+    double exercise_date;
+    int num_periods;
+    const double* fixing_dates;     /* [n] */
+    const double* payment_dates;    /* [n] */
+    const double* period_lengths;   /* [n] or NULL (payment - fixing) */
+    const double* swaprates;        /* [n] */
+    double notional;
+} lmm_swaption_desc;
+
+/* Swaption.getValue(evaluationTime 0, model) (montecarlo/interestrate/products/Swaption.java:137-199),
+ * then getAverage / getStandardError (montecarlo/AbstractMonteCarloProduct.java:82-104). */
+int lmm_swaption_get_value(lmm_process* proc, const lmm_swaption_desc* product, double* out_value,
+                           double* out_error);
+
+typedef struct {
+    int num_periods;
+    const uint8_t* is_exercise_date;  /* [n] isPeriodStartDateExerciseDate */
+    const double* fixing_dates;       /* [n] */
+    const double* period_lengths;     /* [n] */
+    const double* payment_dates;      /* [n] */
+    const double* notionals;          /* [n] periodNotionals */
+    const double* swaprates;          /* [n] */
+    int is_callable;                  /* isCallable */
+    int basis;                        /* LMM_BASIS_* */
+} lmm_bermudan_desc;
+
+/* BermudanSwaption.getValues(evaluationTime 0, model) (montecarlo/interestrate/products/BermudanSwaption.java:91-157):
+ * value and error (standard error).  out_values_host (optional, num_paths doubles)
+ * receives the per-path values (the "value" random variable). */
+int lmm_bermudan_get_value(lmm_process* proc, const lmm_bermudan_desc* product, double* out_value,
+                           double* out_error, double* out_values_host);
+
+/* ---------------------------------------------------------------- instrumentation */
+/* Per-kernel launch counts and (when enabled) CUDA-event times of this library's kernels. */
+int lmm_stats_enable_timing(int enable);
+int lmm_stats_reset(void);
+/* Fills names[i] (static strings), launches[i], total_ms[i] for up to max entries; returns the count. */
+int lmm_stats_get(int max, const char** names, int64_t* launches, double* total_ms);
+/* The CUDA stream (as an opaque pointer) on which a process enqueues its work. */
+int lmm_process_stream(lmm_process* proc, void** out_stream);
+/* A FP64 fused-multiply-add throughput probe (DFMA/s), used to report the FP64 roofline. */
+int lmm_probe_fp64_fma_rate(double* out_fma_per_second);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LMM_GB300_H */
