@@ -1,0 +1,345 @@
+#!/usr/bin/env python3
+"""Benchmark: LMM path-steps/s of the LIBOR Market Model Monte Carlo path on one GB300.
+
+Workload (one "step" = one full valuation pass): the lmm40 configuration -- 40
+semi-annual forwards (0-20y), 80 Euler-log steps of 0.25y, 10 factors, 2^20 paths,
+MT19937 seed 7 -- generating the Brownian increments, simulating the paths with the
+spot-measure drift and numeraire, and valuing the 1y-19.5y payer Bermudan swaption by
+regression ({1,S,S^2,N,N^2,S*N}) and the 10y-into-10y payer swaption.  Metric = paths *
+time steps / seconds.  Synthetic inputs as the workload defines them; the Brownian
+increments (6.7 GB) are larger than L2, so no separate flush is needed.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU restatement of the reference's algorithm (the oracle,
+C, all host threads) on a bounded sample of the same workload; under torchrun only
+rank 0 runs it.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+for _p in (HERE, os.path.join(HERE, "finmath-lib_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "LMM path-steps/s"
+UNIT = "path-steps/s"
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(paths: int, threads: int):
+    """The oracle (C restatement of the reference's path) on a bounded sample of the workload."""
+    from oracle import pyoracle as po
+    from finmath_gb300 import workloads as W
+    cfg = W.LMM40
+    m = po.build_model(**{k: cfg[k] for k in ("dt", "T_end", "period", "tenor_end", "F", "corr_decay", "abcd",
+                                              "curve_nodes", "curve_values")})
+    obs = np.zeros(m.T + 1, np.uint8)
+    obs[W.tenor_time_indices(cfg)] = 1
+    fix, plen, pay, K = W.bermudan_schedule(cfg)
+    ex, sfix, spay, sK = W.swaption_schedule(cfg)
+    t0 = time.perf_counter()
+    dW = po.brownian_increments(m.times, m.F, paths, cfg["seed"])
+    sim = po.Simulation(m, dW, observe=obs, threads=threads)
+    berm = sim.bermudan(fix, plen, pay, K, basis_id=1)
+    swpt = sim.swaption(ex, sfix, spay, sK)
+    dt = time.perf_counter() - t0
+    return paths * m.T / dt, dt, berm, swpt
+
+
+def run_reference(args):
+    ws, rank, local = _dist()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    paths = args.cpu_paths
+    for _ in range(args.warmup):
+        cpu_baseline(paths, threads)
+    times = []
+    for _ in range(args.steps):
+        v, dt, _, _ = cpu_baseline(paths, threads)
+        times.append(dt)
+    value = paths * 80 * args.steps / sum(times)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "lmm40 (40 forwards, 80 steps, 10 factors, seed 7)", "paths_per_step": paths,
+                       "note": "finmath-lib is Java and no JDK exists on this box; the timed CPU path is the "
+                               "oracle, a C restatement of the reference's algorithm (sequential MT19937 + ICDF, "
+                               "OpenMP Euler over paths, Bermudan regression)"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{paths} paths of lmm40 per step (full workload: 1,048,576)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def _traffic_from_profile():
+    """DRAM bytes per launch of the path kernel from the committed ncu summary, if present."""
+    path = os.path.join(HERE, "profiles", "lmm_paths_fp64_lmm40.md")
+    try:
+        for ln in open(path):
+            if ln.startswith("traffic_bytes_per_launch:"):
+                return float(ln.split(":", 1)[1].strip())
+    except OSError:
+        pass
+    return None
+
+
+def run_ours(args):
+    import torch
+    import finmath_gb300 as F
+    from finmath_gb300 import workloads as W
+
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    L = F.load()
+    cfg = W.LMM40
+    P = args.paths
+    prec = F.PRECISION_MIXED if args.precision == "mixed" else F.PRECISION_FP64
+    fix, plen, pay, K = W.bermudan_schedule(cfg)
+    ex, sfix, spay, sK = W.swaption_schedule(cfg)
+    berm = F.BermudanSwaption(np.ones(len(fix)), fix, plen, pay, 1.0, K, True, "swaprate")
+    swpt = F.Swaption(ex, sfix, spay, sK)
+    T = int(round(cfg["T_end"] / cfg["dt"]))
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    # ---------------- device-resident throughput: model tables uploaded once, increments,
+    # paths and products recomputed every step (the seed is re-set to force regeneration)
+    sim = W.build(cfg, paths=P, precision=prec)
+    stream = ctypes.c_void_p()
+    L.lmm_process_stream(sim.process._h, ctypes.byref(stream))
+    ts = torch.cuda.ExternalStream(stream.value)
+    bm = sim.process.brownianMotion
+
+    def step():
+        bm.setSeed(cfg["seed"])
+        b = berm.getValues(sim)
+        s = swpt.getValues(sim)
+        return b, s
+
+    for _ in range(args.warmup):
+        res = step()
+    barrier()
+    L.lmm_stats_reset()
+    L.lmm_stats_enable_timing(1)
+    clocks = ClockSampler(local)
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    e0.record(ts)
+    for _ in range(args.steps):
+        res = step()
+    e1.record(ts)
+    barrier()
+    clk = clocks.stop()
+    L.lmm_stats_enable_timing(0)
+    ms = e0.elapsed_time(e1) / args.steps
+    stats = F.kernel_stats()
+    launches = sum(v[0] for v in stats.values())
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = ws * P * T / (ms * 1e-3)
+
+    # ---------------- roofline of the dominant kernel (the path kernel)
+    kname = "lmm_paths_fp32" if prec == F.PRECISION_MIXED else "lmm_paths_fp64"
+    k_launch, k_ms = stats[kname]
+    k_avg_s = k_ms / max(k_launch, 1) * 1e-3
+    td = F.TimeDiscretizationFromArray(0.0, T, cfg["dt"]).getAsDoubleArray()
+    tenor = np.arange(0.0, cfg["tenor_end"] + 1e-9, cfg["period"])
+    N, Fk = len(tenor) - 1, cfg["F"]
+    comp_steps = sum(N - (int(np.searchsorted(tenor, t, side="right"))) for t in td[:-1])
+    flops = P * comp_steps * (6 * Fk + 8 + 3)   # add/mul of drift+diffusion, plus div, exp, log
+    fma = ctypes.c_double()
+    L.lmm_probe_fp64_fma_rate(ctypes.byref(fma))
+    peak = 2.0 * fma.value / 1e12
+    achieved = flops / k_avg_s / 1e12
+    traffic = _traffic_from_profile() if prec == F.PRECISION_FP64 and P == (1 << 20) else None
+    roofline = {"bound": "fp64" if prec == F.PRECISION_FP64 else "fp32", "kernel": kname,
+                "achieved": achieved, "peak": peak if prec == F.PRECISION_FP64 else None, "unit": "TFLOP/s",
+                "frac": achieved / peak if prec == F.PRECISION_FP64 else None, "traffic": traffic,
+                "algorithmic_flops_per_launch": flops, "avg_launch_ms": k_avg_s * 1e3,
+                "peak_source": "FP64 FMA rate measured live by the library's DFMA probe (x2 flops); "
+                               "MEASURED_PEAKS.json holds no FP64 figure",
+                "component_steps_per_path": comp_steps}
+
+    # ---------------- end to end through the C ABI with host buffers (tables in, prices out)
+    e2e_times = []
+    h2d = d2h = 0
+    for i in range(args.steps + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s2 = W.build(cfg, paths=P, precision=prec)
+        b2 = berm.getValues(s2)
+        w2 = swpt.getValues(s2)
+        s2.process.close()
+        s2.process.brownianMotion.close()
+        torch.cuda.synchronize()
+        if i > 0:
+            e2e_times.append(time.perf_counter() - t0)
+        if i == 0:
+            cov = s2.process.model.covarianceModel
+            h2d = (cov.factorLoadings.nbytes + cov.variance.nbytes + 8 * (2 * (T + 1) + 4 * (N + 1))
+                   + 624 * 4 + 9 * 312 * 8 + 3 * 64 * 8)
+            d2h = 4 * 16
+    e2e_ms = 1e3 * statistics.mean(e2e_times)
+    if dist is not None:
+        t = torch.tensor([e2e_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e = {"value": ws * P * T / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+           "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms,
+           "note": "C-ABI valuation from host tables: Brownian motion + process creation, lazy "
+                   "generation/simulation, Bermudan + swaption values read back, handles destroyed"}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if prec == F.PRECISION_FP64 else "f32/f64 mixed", "data": "synthetic",
+            "config": {"workload": "lmm40: 40 forwards (0-20y), 80 Euler-log steps, 10 factors, seed 7",
+                       "paths": P, "products": "payer Bermudan 1y-19.5y K=4% (basis {1,S,S^2,N,N^2,SN}) + 10y10y payer swaption",
+                       "parallelism": f"replicas x{ws}", "l2": "inputs larger than L2 (Brownian increments 6.7 GB)"},
+            "prices": {"bermudan": res[0], "swaption": res[1]},
+            "e2e": e2e, "roofline": roofline, "clocks": clk, "gpu_launches": int(launches),
+            "kernels_ms": {k: v[1] / max(args.steps, 1) for k, v in stats.items() if v[0]}}
+
+    if rank == 0 and args.precision == "fp64" and not args.no_forms:
+        line["forms"] = {"mixed": mixed_form(args, F, W, cfg, P, T, berm, swpt, res)}
+    if rank == 0 and not args.no_cpu_baseline:
+        v, dt, _, _ = cpu_baseline(args.cpu_paths, os.cpu_count() or 1)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                                "sample": f"{args.cpu_paths} paths of lmm40, one pass ({dt:.1f} s)"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def mixed_form(args, F, W, cfg, P, T, berm, swpt, res64):
+    """The mixed-precision form on the same workload: throughput and price error vs FP64."""
+    import torch
+    L = F.load()
+    sim = W.build(cfg, paths=P, precision=F.PRECISION_MIXED)
+    bm = sim.process.brownianMotion
+    for _ in range(2):
+        bm.setSeed(cfg["seed"])
+        b = berm.getValues(sim)
+        s = swpt.getValues(sim)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        bm.setSeed(cfg["seed"])
+        b = berm.getValues(sim)
+        s = swpt.getValues(sim)
+    torch.cuda.synchronize()
+    ms = 1e3 * (time.perf_counter() - t0) / args.steps
+    out = {"value": P * T / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms,
+           "bermudan": b, "swaption": s,
+           "bermudan_error_bp": 1e4 * (b["value"] - res64[0]["value"]),
+           "bermudan_error_in_se": (b["value"] - res64[0]["value"]) / res64[0]["error"],
+           "swaption_error_bp": 1e4 * (s["value"] - res64[1]["value"])}
+    sim.process.close()
+    bm.close()
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--paths", type=int, default=1 << 20)
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    ap.add_argument("--cpu-paths", type=int, default=32768)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-forms", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -166,6 +166,7 @@ struct lmm_brownian {
     double* d_sqrt_dt = nullptr;
     void* d_dw = nullptr;
     bool generated = false;
+    uint64_t generation = 0;   // bumped whenever the increments change
 };
 
 struct lmm_process {
@@ -188,6 +189,7 @@ struct lmm_process {
     double *d_numeraire = nullptr, *d_partials = nullptr, *d_num_adj = nullptr;
     int path_blocks = 0;
     bool simulated = false;
+    uint64_t bm_generation = 0;  // Brownian generation the results were simulated from
     // product scratch
     double* d_values = nullptr;
     double* d_reduce = nullptr;
@@ -234,17 +236,18 @@ static int brownian_ensure(lmm_brownian* b)
 {
     if (b->generated) return LMM_OK;
     const int64_t values = (int64_t)b->T * b->F * (int64_t)b->P;
-    int rc = plan_mt_generate(values, &b->plan);
-    if (rc) return rc;
+    int rc = LMM_OK;
+    if (b->plan.chunks == 0 && (rc = plan_mt_generate(values, &b->plan))) return rc;
     uint32_t seeded[kMtN];
     mt_seeded_state((int64_t)b->seed, seeded);  // int seed widened to long (BrownianMotionFromMersenneRandomNumbers.java:147)
     std::vector<double> sq(b->T);
     for (int t = 0; t < b->T; t++) sq[t] = std::sqrt(b->times[t + 1] - b->times[t]);
-    if ((rc = upload(&b->d_seeded, seeded, kMtN, b->stream))) return rc;
-    if ((rc = upload(&b->d_jumps, b->plan.polys.data(), b->plan.polys.size(), b->stream))) return rc;
-    if ((rc = upload(&b->d_sqrt_dt, sq.data(), sq.size(), b->stream))) return rc;
+    if (!b->d_seeded && (rc = dalloc(&b->d_seeded, kMtN, b->stream))) return rc;
+    LMM_CUDA(cudaMemcpyAsync(b->d_seeded, seeded, sizeof(seeded), cudaMemcpyHostToDevice, b->stream));
+    if (!b->d_jumps && (rc = upload(&b->d_jumps, b->plan.polys.data(), b->plan.polys.size(), b->stream))) return rc;
+    if (!b->d_sqrt_dt && (rc = upload(&b->d_sqrt_dt, sq.data(), sq.size(), b->stream))) return rc;
     const size_t esz = b->precision == LMM_PRECISION_FP64 ? sizeof(double) : sizeof(float);
-    if ((rc = dalloc((unsigned char**)&b->d_dw, (size_t)values * esz, b->stream))) return rc;
+    if (!b->d_dw && (rc = dalloc((unsigned char**)&b->d_dw, (size_t)values * esz, b->stream))) return rc;
     RngLaunch a;
     a.plan = &b->plan;
     a.d_seeded = b->d_seeded;
@@ -259,6 +262,15 @@ static int brownian_ensure(lmm_brownian* b)
     rc = launch_mt_generate(a, b->stream, nullptr);
     if (rc) return rc;
     b->generated = true;
+    b->generation++;
+    return LMM_OK;
+}
+
+int lmm_brownian_set_seed(lmm_brownian* b, int seed)
+{
+    if (!b) return fail(LMM_ERR_INVALID, "null handle");
+    b->seed = seed;
+    b->generated = false;  // regenerated lazily; processes re-simulate on next use
     return LMM_OK;
 }
 
@@ -455,18 +467,20 @@ int lmm_process_set_observed_times(lmm_process* pr, const uint8_t* mask)
 
 static int process_ensure(lmm_process* pr)
 {
-    if (pr->simulated) return LMM_OK;
+    if (pr->simulated && pr->bm->generated && pr->bm_generation == pr->bm->generation) return LMM_OK;
     int rc = brownian_ensure(pr->bm);
     if (rc) return rc;
     cudaStream_t s = pr->stream;
     const size_t esz = pr->precision == LMM_PRECISION_FP64 ? sizeof(double) : sizeof(float);
     pr->path_blocks = path_blocks(pr->P);
-    if (!rc) rc = upload(&pr->d_obs_slot, pr->obs_slot.data(), pr->obs_slot.size(), s);
-    if (!rc) rc = dalloc((unsigned char**)&pr->d_states, (size_t)pr->nobs * pr->N * (size_t)pr->P * esz, s);
-    if (!rc) rc = dalloc(&pr->d_numeraire, (size_t)(pr->N + 1) * pr->P, s);
-    if (!rc) rc = dalloc(&pr->d_partials, (size_t)pr->path_blocks * pr->N * 2, s);
-    if (!rc) rc = dalloc(&pr->d_num_adj, (size_t)(pr->N + 1), s);
-    if (rc) return rc;
+    if (!pr->d_obs_slot) {
+        if (!rc) rc = upload(&pr->d_obs_slot, pr->obs_slot.data(), pr->obs_slot.size(), s);
+        if (!rc) rc = dalloc((unsigned char**)&pr->d_states, (size_t)pr->nobs * pr->N * (size_t)pr->P * esz, s);
+        if (!rc) rc = dalloc(&pr->d_numeraire, (size_t)(pr->N + 1) * pr->P, s);
+        if (!rc) rc = dalloc(&pr->d_partials, (size_t)pr->path_blocks * pr->N * 2, s);
+        if (!rc) rc = dalloc(&pr->d_num_adj, (size_t)(pr->N + 1), s);
+        if (rc) return rc;
+    }
     PathLaunch a;
     a.T = pr->T;
     a.N = pr->N;
@@ -493,6 +507,7 @@ static int process_ensure(lmm_process* pr)
     rc = launch_numeraire_finish(pr->d_partials, blocks, pr->N, pr->P, pr->d_numeraire, pr->d_det, pr->d_num_adj, s);
     if (rc) return rc;
     pr->simulated = true;
+    pr->bm_generation = pr->bm->generation;
     return LMM_OK;
 }
 

@@ -150,15 +150,23 @@ __device__ void bermudan_basis(const BermStepParams& a, int p, double B[5])
 {
     const BermudanPeriod& c = a.cur;
     if (a.basis == 1) {
-        // {S, S^2, N, N^2, S*N}: S = par rate of the remaining periods from L_j(T_ex)
-        double df = 1.0, ann = 0.0;
+        // {S, S^2, N, N^2, S*N}: S = par rate of the remaining periods from L_j(T_ex),
+        // S = (prod g_q - 1) / sum_s d_s prod_{r>s} g_r with g_q = 1 + L_q d_q, both by a
+        // forward recursion (one division per path instead of one per period)
+        double H = 0.0, prod = 1.0;
         for (int q = c.swap_first; q < c.swap_last; q++) {
             const double Lq = state_at<TS>(a.states, c.ex_slot, a.N, a.P, a.period_index[q], p);
             const double dq = a.period_length[q];
-            df = (q == c.swap_first) ? 1.0 / (1.0 + Lq * dq) : df / (1.0 + Lq * dq);
-            ann = (q == c.swap_first) ? dq * df : ann + dq * df;
+            const double g = 1.0 + Lq * dq;
+            if (q == c.swap_first) {
+                prod = g;
+                H = dq;
+            } else {
+                prod = prod * g;
+                H = H * g + dq;
+            }
         }
-        const double S = (1.0 - df) / ann;
+        const double S = (prod - 1.0) / H;
         const double Nn = numeraire_adj(a.num, c.ex_num_index, p);
         B[0] = S;
         B[1] = S * S;
@@ -194,9 +202,10 @@ template <typename TS>
 __global__ void __launch_bounds__(kProdThreads) bermudan_step_kernel(const BermStepParams a)
 {
     const double w = 1.0 / (double)a.P;
-    dd acc[kGramEntries];
+    // per-thread plain sums over this thread's few paths; compensated across threads
+    double acc[kGramEntries];
 #pragma unroll
-    for (int e = 0; e < kGramEntries; e++) acc[e] = dd{0.0, 0.0};
+    for (int e = 0; e < kGramEntries; e++) acc[e] = 0.0;
     const bool gram = a.has_cur && a.cur.exercisable;
     double beta[6];
     if (a.apply_choose) {
@@ -238,19 +247,19 @@ __global__ void __launch_bounds__(kProdThreads) bermudan_step_kernel(const BermS
                 for (int i = 0; i < 5; i++) a.basis_buf[(size_t)i * a.P + p] = B[i];
                 int e = 0;
 #pragma unroll
-                for (int i = 0; i < 5; i++) acc[e + i] = dd_add_d(acc[e + i], B[i]);  // G[0][1..5]
+                for (int i = 0; i < 5; i++) acc[e + i] = acc[e + i] + B[i];  // G[0][1..5]
                 e += 5;
 #pragma unroll
                 for (int i = 0; i < 5; i++)
 #pragma unroll
                     for (int j = i; j < 5; j++) {
-                        acc[e] = dd_add_d(acc[e], B[i] * B[j]);
+                        acc[e] = acc[e] + B[i] * B[j];
                         e++;
                     }
-                acc[e] = dd_add_d(acc[e], y * 1.0);  // rhs[0] = mean(y * 1)
+                acc[e] = acc[e] + y * 1.0;  // rhs[0] = mean(y * 1)
                 e++;
 #pragma unroll
-                for (int i = 0; i < 5; i++) acc[e + i] = dd_add_d(acc[e + i], y * B[i]);
+                for (int i = 0; i < 5; i++) acc[e + i] = acc[e + i] + y * B[i];
             }
         }
         if (a.final_pass) v = (v * 1.0) / w;
@@ -260,7 +269,7 @@ __global__ void __launch_bounds__(kProdThreads) bermudan_step_kernel(const BermS
     if (gram) {
 #pragma unroll
         for (int e = 0; e < kGramEntries; e++) {
-            const dd s = block_dd_sum(acc[e]);
+            const dd s = block_dd_sum(dd{acc[e], 0.0});
             if (threadIdx.x == 0) {
                 a.partials[((size_t)blockIdx.x * kGramEntries + e) * 2] = s.hi;
                 a.partials[((size_t)blockIdx.x * kGramEntries + e) * 2 + 1] = s.lo;
@@ -289,7 +298,7 @@ __device__ void solve_pinv6(const double Gin[36], const double b[6], double x[6]
                     beta += uq * uq;
                     gamma += up * uq;
                 }
-                if (gamma == 0.0 || fabs(gamma) <= 1e-17 * sqrt(alpha * beta)) continue;
+                if (gamma == 0.0 || fabs(gamma) <= 0x1.0p-52 * sqrt(alpha * beta)) continue;
                 rotated = 1;
                 const double zeta = (beta - alpha) / (2.0 * gamma);
                 const double t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));

@@ -63,6 +63,7 @@ SIGNATURES = {
                                            ctypes.POINTER(_VP)]),
     "lmm_brownian_get_increment": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, _D]),
     "lmm_brownian_generate": (ctypes.c_int, [_VP]),
+    "lmm_brownian_set_seed": (ctypes.c_int, [_VP, ctypes.c_int]),
     "lmm_brownian_destroy": (ctypes.c_int, [_VP]),
     "lmm_mt19937_uniforms": (ctypes.c_int, [ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, _D]),
     "lmm_mt19937_words_host": (ctypes.c_int, [ctypes.c_int64, ctypes.c_uint64, ctypes.c_uint64,

@@ -246,6 +246,11 @@ class BrownianMotionFromMersenneRandomNumbers:
 
     getIncrement = getBrownianIncrement
 
+    def setSeed(self, seed):
+        """getCloneWithModifiedSeed, in place (keeps the device allocation)."""
+        self.seed = int(seed)
+        check(self._L.lmm_brownian_set_seed(self._h, self.seed), "setSeed")
+
     def getTimeDiscretization(self):
         return self.timeDiscretization
 

@@ -104,6 +104,10 @@ int lmm_brownian_create(const double* times, int num_times, int num_factors, int
                         int precision, lmm_brownian** out);
 /* getBrownianIncrement(timeIndex, factor) (:123-136): num_paths doubles. */
 int lmm_brownian_get_increment(lmm_brownian* bm, int time_index, int factor, double* out_host);
+/* getCloneWithModifiedSeed(seed) (:106-109) in place: the increments are regenerated
+ * lazily with the new seed, reusing the device allocation; processes built on this
+ * Brownian motion re-simulate on their next use. */
+int lmm_brownian_set_seed(lmm_brownian* bm, int seed);
 /* doGenerateBrownianMotion (:141-191), explicit trigger. */
 int lmm_brownian_generate(lmm_brownian* bm);
 int lmm_brownian_destroy(lmm_brownian* bm);

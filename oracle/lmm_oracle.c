@@ -349,7 +349,7 @@ static void svd_one_sided_jacobi(int m, int n, const double* A, double* U, doubl
                     beta += uq * uq;
                     gamma += up * uq;
                 }
-                if (gamma == 0.0 || fabs(gamma) <= 1e-17 * sqrt(alpha * beta)) continue;
+                if (gamma == 0.0 || fabs(gamma) <= 0x1.0p-52 * sqrt(alpha * beta)) continue;
                 rotated = 1;
                 double zeta = (beta - alpha) / (2.0 * gamma);
                 double t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
@@ -886,21 +886,21 @@ int orc_bermudan(const orc_sim* s, int nper, const uint8_t* exercisable, const d
             }
             basis[1] = b[0]; basis[2] = b[1]; basis[3] = b[2]; basis[4] = b[3]; basis[5] = b[4];
         } else {
-            /* {1, S, S^2, N, N^2, S*N}: S = par rate of the remaining periods from L_j(T_ex). */
-            for (int p = 0; p < P; p++) { b[0][p] = 0.0; b[5][p] = 0.0; }
+            /* {1, S, S^2, N, N^2, S*N}: S = par rate of the remaining periods from L_j(T_ex),
+             * S = (prod g_q - 1) / sum_s d_s prod_{r>s} g_r, g_q = 1 + L_q d_q, by the forward
+             * recursion B = B g, H = H g + d (b[0] = B, b[5] = H). */
             for (int q = per; q < nper; q++) {
                 const double* lq = sim_forward(s, fix, fixing[q], payment[q]);
                 if (!lq) { rc = -6; goto done; }
                 const double dq = period_length[q];
                 for (int p = 0; p < P; p++) {
-                    /* b[0] = discount factor, b[5] = annuity */
-                    double df = (q == per) ? 1.0 / (1.0 + lq[p] * dq) : b[0][p] / (1.0 + lq[p] * dq);
-                    b[0][p] = df;
-                    b[5][p] = (q == per) ? dq * df : b[5][p] + dq * df;
+                    double g = 1.0 + lq[p] * dq;
+                    if (q == per) { b[0][p] = g; b[5][p] = dq; }
+                    else { b[0][p] = b[0][p] * g; b[5][p] = b[5][p] * g + dq; }
                 }
             }
             for (int p = 0; p < P; p++) {
-                double S = (1.0 - b[0][p]) / b[5][p];
+                double S = (b[0][p] - 1.0) / b[5][p];
                 double Nn = num[p];
                 b[0][p] = S;
                 b[1][p] = S * S;

@@ -1,0 +1,49 @@
+"""GPU MT19937 + inverse normal against the oracle (bit-exact uniforms)."""
+import numpy as np
+import pytest
+
+import finmath_gb300 as F
+from finmath_gb300 import workloads as W
+from oracle import pyoracle as po
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("seed", [3141, 7, 1352, -5])
+@pytest.mark.parametrize("offset,count", [(0, 4096), (311, 1000), (123457, 3000), (2_500_001, 777)])
+def test_uniforms_bit_exact(seed, offset, count):
+    g = F.mersenne_twister_uniforms(seed, count, offset)
+    o = po.mt_doubles(seed, count, skip=offset)
+    assert np.array_equal(g, o)
+
+
+def test_uniforms_across_many_chunks():
+    # 3e6 values: the generator splits the stream into one chunk per resident CTA
+    n = 3_000_000
+    g = F.mersenne_twister_uniforms(7, n)
+    o = po.mt_doubles(7, n)
+    assert np.array_equal(g, o)
+
+
+@pytest.mark.parametrize("P,T,Fk", [(5000, 20, 3), (1, 7, 2), (33, 5, 1), (1000, 13, 10)])
+def test_brownian_increments_fp64(P, T, Fk):
+    td = F.TimeDiscretizationFromArray(0.0, T, 0.5)
+    bm = F.BrownianMotionFromMersenneRandomNumbers(td, Fk, P, 3141)
+    ref = po.brownian_increments(td.getAsDoubleArray(), Fk, P, 3141)
+    worst = 0.0
+    for t in range(T):
+        for k in range(Fk):
+            g = bm.getBrownianIncrement(t, k)
+            r = ref[t, k]
+            worst = max(worst, float(np.max(np.abs(g - r) / np.maximum(np.abs(r), 1e-300))))
+    # central branch is unfused +,*,/ (bit-identical); tails go through log (CUDA vs libm, <= a few ulp)
+    assert worst <= 4e-15
+
+
+def test_brownian_increments_mixed_precision():
+    td = F.TimeDiscretizationFromArray(0.0, 20, 0.5)
+    bm = F.BrownianMotionFromMersenneRandomNumbers(td, 3, 5000, 3141, F.PRECISION_MIXED)
+    ref = po.brownian_increments(td.getAsDoubleArray(), 3, 5000, 3141)
+    for t in (0, 7, 19):
+        g = bm.getBrownianIncrement(t, 2)
+        assert np.max(np.abs(g - ref[t, 2])) < 2e-6 * np.max(np.abs(ref[t, 2]))

@@ -1,0 +1,107 @@
+"""The C ABI library on the CPU: loads, exports every declared symbol, host-side model
+setup is identical to the oracle's, the MT19937 jump polynomials are right, and GPU
+entry points fail loudly (no CPU fallback) when no GPU is present."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import finmath_gb300 as F
+from finmath_gb300 import _lib, workloads as W
+from oracle import pyoracle as po
+from conftest import oracle_model
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "lmm_gb300.h")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\**\s+\**(lmm_\w+)\s*\(", src, re.M)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = F.load()
+    names = declared_functions()
+    assert len(names) >= 25
+    for n in names:
+        assert hasattr(lib, n), n
+    assert set(names) <= set(_lib.SIGNATURES), "every declared entry point has a ctypes signature"
+
+
+def test_time_discretization_matches_oracle():
+    for n, dt in ((20, 0.5), (80, 0.25), (7, 1.0 / 3.0)):
+        assert np.array_equal(F.TimeDiscretizationFromArray(0.0, n, dt).getAsDoubleArray(), po.time_discretization(0.0, n, dt))
+
+
+@pytest.mark.parametrize("name", ["lmm20", "lmm40"])
+def test_model_tables_match_oracle_bitwise(name):
+    cfg = W.WORKLOADS[name]
+    m = oracle_model(cfg)
+    td = F.TimeDiscretizationFromArray(0.0, m.T, cfg["dt"])
+    tn = F.TimeDiscretizationFromArray(0.0, m.N, cfg["period"])
+    corr = F.LIBORCorrelationModelExponentialDecay(td, tn, cfg["F"], cfg["corr_decay"])
+    vol = F.LIBORVolatilityModelFourParameterExponentialForm(td, tn, *cfg["abcd"])
+    cov = F.LIBORCovarianceModelFromVolatilityAndCorrelation(td, tn, vol, corr)
+    curve = F.ForwardCurveInterpolation.createForwardCurveFromForwards("f", cfg["curve_nodes"], cfg["curve_values"], cfg["period"])
+    model = F.LIBORMarketModelFromCovarianceModel.of(tn, None, curve, F.DiscountCurveFromForwardCurve(curve), None, cov)
+    assert np.array_equal(corr.factorMatrix, m.factor)
+    assert np.array_equal(corr.correlationMatrix, m.corr)
+    assert np.array_equal(vol.volatility, m.vol)
+    assert np.array_equal(cov.factorLoadings, m.loadings)
+    assert np.array_equal(cov.variance, m.variance)
+    assert np.array_equal(model.initialForwards, m.initial_forwards)
+    assert np.array_equal(model.discountChain, m.discount_chain)
+
+
+def test_factor_reduction_reproduces_pca_of_numpy():
+    tn = np.arange(0, 20.5, 0.5)[:-1]
+    corr = np.exp(-0.03 * np.abs(tn[:, None] - tn[None, :]))
+    out = np.empty((40, 10))
+    _lib.check(F.load().lmm_factor_reduction(corr.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), 40, 10,
+                                             out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+    # rows have unit length after the reduction; F F^T is the best rank-10 correlation
+    assert np.allclose(np.sum(out * out, axis=1), 1.0, atol=1e-12)
+    ev, V = np.linalg.eigh(corr)
+    top = V[:, -10:] * np.sqrt(ev[-10:])
+    top = top / np.linalg.norm(top, axis=1, keepdims=True)
+    assert np.allclose(out @ out.T, top @ top.T, atol=1e-10)
+
+
+@pytest.mark.parametrize("seed,skip", [(3141, 0), (3141, 1), (3141, 623), (3141, 624), (7, 99991), (7, 5_000_001),
+                                       (1352, 1 << 21)])
+def test_mt19937_jump_polynomials_host(seed, skip):
+    out = np.empty(40, dtype=np.uint32)
+    rc = F.load().lmm_mt19937_words_host(seed, skip, 40, out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)))
+    assert rc == 0
+    assert np.array_equal(out, po.mt_words(seed, 40, skip=skip))
+
+
+def test_invalid_arguments_are_rejected_with_messages():
+    lib = F.load()
+    out = np.empty(4)
+    rc = lib.lmm_factor_reduction(out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), 2, 3,
+                                  out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+    assert rc == _lib.LMM_ERR_INVALID
+    assert b"F <= n" in lib.lmm_last_error()
+    h = ctypes.c_void_p()
+    t = np.array([0.0, 0.5, 0.5])
+    rc = lib.lmm_brownian_create(t.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), 3, 1, 10, 1, 0, ctypes.byref(h))
+    assert rc == _lib.LMM_ERR_INVALID and b"increasing" in lib.lmm_last_error()
+
+
+def _have_gpu():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+@pytest.mark.skipif(_have_gpu(), reason="checks the behaviour without a GPU")
+def test_gpu_entry_points_fail_loudly_without_gpu():
+    with pytest.raises(F.CalculationException):
+        F.mersenne_twister_uniforms(3141, 10)

@@ -1,0 +1,103 @@
+"""The oracle's LMM valuation: snapshot, structural properties and statistical checks (CPU)."""
+import json
+import os
+
+import numpy as np
+import pytest
+from scipy.stats import norm
+
+from finmath_gb300 import workloads as W
+from oracle import pyoracle as po
+from conftest import oracle_model
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+@pytest.fixture(scope="module")
+def lmm20():
+    cfg = W.LMM20
+    m = oracle_model(cfg)
+    dW = po.brownian_increments(m.times, m.F, cfg["paths"], cfg["seed"])
+    return cfg, m, dW, po.Simulation(m, dW)
+
+
+def test_snapshot(lmm20):
+    cfg, m, dW, sim = lmm20
+    g = json.load(open(os.path.join(GOLD, "oracle_lmm20.json")))
+    ex, fix, pay, K = W.swaption_schedule(cfg)
+    assert sim.swaption(ex, fix, pay, K) == pytest.approx(tuple(g["swaption"]), rel=1e-12)
+    bf, bl, bp, bK = W.bermudan_schedule(cfg)
+    assert sim.bermudan(bf, bl, bp, bK, basis_id=0) == pytest.approx(tuple(g["bermudan_reference_basis"]), rel=1e-12)
+    assert sim.bermudan(bf, bl, bp, bK, basis_id=1) == pytest.approx(tuple(g["bermudan_swaprate_basis"]), rel=1e-12)
+    assert np.allclose(sim.process_value(10, 19)[:8], g["L_10_19_first8"], rtol=1e-13, atol=0)
+    assert np.allclose(dW[3, 1, :8], g["dW_t3_f1_first8"], rtol=1e-14, atol=0)
+
+
+def test_numeraire_adjustment_reprices_discount_bonds(lmm20):
+    # getNumeraire rescales so that E[N(0)/N(T)] equals the discount curve P^d(T) (:869-874)
+    cfg, m, dW, sim = lmm20
+    for i in (1, 2, 7, 20):
+        T = m.tenor[i]
+        assert po.kahan_average(1.0 / sim.numeraire(T)) == pytest.approx(m.discount_chain[i], rel=1e-13)
+
+
+def test_frozen_forwards_after_fixing(lmm20):
+    cfg, m, dW, sim = lmm20
+    # L_j stops evolving at T_j (EulerSchemeFromProcessModel copies components whose drift is null)
+    for j in (2, 9):
+        tj = int(round(m.tenor[j] / cfg["dt"]))
+        assert np.array_equal(sim.process_value(tj, j), sim.process_value(m.T, j))
+
+
+def black_swaption_rebonato(m, ex, fix, pay, K):
+    """Black price of a payer swaption with Rebonato's frozen-weight swap-rate volatility."""
+    tenor = m.tenor
+    idx = [int(np.searchsorted(tenor, f)) for f in fix]
+    L0 = m.initial_forwards
+    df = np.cumprod(1.0 / (1.0 + L0 * np.diff(tenor)))
+    df = np.concatenate([[1.0], df])
+    ann = sum((pay[q] - fix[q]) * df[idx[q] + 1] for q in range(len(fix)))
+    S0 = (df[idx[0]] - df[idx[-1] + 1]) / ann
+    w = np.array([(pay[q] - fix[q]) * df[idx[q] + 1] / ann for q in range(len(fix))])
+    var = 0.0
+    for i in range(len(m.times) - 1):
+        if m.times[i] >= ex:
+            break
+        dt = m.times[i + 1] - m.times[i]
+        lam = m.loadings[i][idx]
+        cov = lam @ lam.T
+        wl = w * L0[idx]
+        var += wl @ cov @ wl * dt
+    sig = np.sqrt(var) / S0
+    d1 = (np.log(S0 / K) + 0.5 * sig * sig) / sig
+    return df[0] * ann * (S0 * norm.cdf(d1) - K * norm.cdf(d1 - sig))
+
+
+def test_swaption_close_to_rebonato_approximation(lmm20):
+    cfg, m, dW, sim = lmm20
+    ex, fix, pay, K = W.swaption_schedule(cfg)
+    v, se = sim.swaption(ex, fix, pay, K)
+    approx = black_swaption_rebonato(m, ex, fix, pay, np.full(len(fix), K)[0])
+    # same tolerance idea as LIBORMarketModelValuationTest.testSwaption (:366-428): statistical + approximation error
+    assert abs(v - approx) < 3 * se + 0.03 * approx
+
+
+def test_bermudan_dominates_european_swaptions(lmm20):
+    cfg, m, dW, sim = lmm20
+    bf, bl, bp, K = W.bermudan_schedule(cfg)
+    berm, se = sim.bermudan(bf, bl, bp, K, basis_id=1)
+    for ex in (2.0, 5.0):
+        fix = bf[bf >= ex]
+        v, _ = sim.swaption(ex, fix, fix + 0.5, K)
+        assert berm > v - 3 * se
+
+
+def test_euler_and_functional_schemes_agree_to_rounding():
+    cfg = W.LMM20
+    P = 500
+    mf = oracle_model(cfg, scheme=1)
+    me = oracle_model(cfg, scheme=0)
+    dW = po.brownian_increments(mf.times, mf.F, P, cfg["seed"])
+    a = po.Simulation(mf, dW).process_value(20, 19)
+    b = po.Simulation(me, dW).process_value(20, 19)
+    assert np.allclose(a, b, rtol=1e-12, atol=0)
