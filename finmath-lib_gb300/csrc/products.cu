@@ -14,6 +14,7 @@
 
 #include <math_constants.h>
 #include <cstring>
+#include <mutex>
 
 namespace lmm {
 namespace {
@@ -503,4 +504,67 @@ int launch_bermudan(const ProductView& v, const BermudanLaunch& a, const Bermuda
     return LMM_OK;
 }
 
+// ------------------------------------------------------------------ allocation-free mean / standard error
+// The allocation-free variant of reduce_mean_stderr keeps its scratch (the block partials
+// of the two compensated sums and the two results) in this file-scope array instead of
+// memory from the pool.  Every GPU that loads the library holds these 8,208 bytes until
+// the process exits.
+namespace {
+constexpr int kNoAllocBlocks = 512;
+constexpr int64_t kNoAllocMaxValues = (int64_t)1 << 30;
+std::mutex g_noalloc_mu;
+double* g_noalloc_addr[256] = {};
+}  // namespace
+
+static __device__ __align__(256) double g_noalloc_scratch[2 * kNoAllocBlocks + 2];
+
+// Device address of the scratch on the current device, looked up once per device with
+// that device current.  Host code must not pass g_noalloc_scratch itself to a kernel:
+// on the host that name is only a stand-in for the device symbol.
+static int noalloc_scratch_address(double** out)
+{
+    int dev = 0;
+    LMM_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 256) return fail(LMM_ERR_INVALID, "device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+        g_noalloc_addr[dev] = static_cast<double*>(p);
+    }
+    *out = g_noalloc_addr[dev];
+    return LMM_OK;
+}
+
 }  // namespace lmm
+
+extern "C" int lmm_values_mean_stderr_noalloc(const double* d_values, int64_t num_values, void* stream,
+                                              double* out_mean, double* out_error)
+{
+    using namespace lmm;
+    if (!d_values || !out_mean) return fail(LMM_ERR_INVALID, "lmm_values_mean_stderr_noalloc: null argument");
+    if (num_values < 1 || num_values > kNoAllocMaxValues)
+        return fail(LMM_ERR_INVALID, "lmm_values_mean_stderr_noalloc: num_values must be in [1, 2^30]");
+    double* scratch = nullptr;
+    int rc = noalloc_scratch_address(&scratch);
+    if (rc) return rc;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int P = (int)num_values;
+    const int blocks = grid_for(P, 256, kNoAllocBlocks);
+    // Each block overwrites its own partial and the finishing kernels overwrite the
+    // results, so nothing left by an earlier call is read and nothing needs clearing.
+    double* partials = scratch;
+    double* res = scratch + 2 * kNoAllocBlocks;
+    sum_partials_kernel<<<blocks, 256, 0, s>>>(d_values, P, nullptr, partials);
+    finish_partials_kernel<<<1, 256, 0, s>>>(partials, blocks, P, res);
+    sum_partials_kernel<<<blocks, 256, 0, s>>>(d_values, P, res, partials);
+    finish_partials_kernel<<<1, 256, 0, s>>>(partials, blocks, P, res + 1);
+    LMM_CUDA(cudaGetLastError());
+    double h[2];
+    LMM_CUDA(cudaMemcpyAsync(h, res, sizeof(h), cudaMemcpyDeviceToHost, s));
+    LMM_CUDA(cudaStreamSynchronize(s));
+    *out_mean = h[0];
+    if (out_error) *out_error = P > 1 ? sqrt(h[1]) / sqrt((double)P) : 0.0;
+    return LMM_OK;
+}

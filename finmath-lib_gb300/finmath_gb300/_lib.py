@@ -76,6 +76,7 @@ SIGNATURES = {
     "lmm_process_destroy": (ctypes.c_int, [_VP]),
     "lmm_swaption_get_value": (ctypes.c_int, [_VP, ctypes.POINTER(LmmSwaptionDesc), _D, _D]),
     "lmm_bermudan_get_value": (ctypes.c_int, [_VP, ctypes.POINTER(LmmBermudanDesc), _D, _D, _D]),
+    "lmm_values_mean_stderr_noalloc": (ctypes.c_int, [_VP, ctypes.c_int64, _VP, _D, _D]),
     "lmm_stats_enable_timing": (ctypes.c_int, [ctypes.c_int]),
     "lmm_stats_reset": (ctypes.c_int, []),
     "lmm_stats_get": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_char_p), _I64, _D]),

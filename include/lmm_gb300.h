@@ -193,6 +193,24 @@ typedef struct {
 int lmm_bermudan_get_value(lmm_process* proc, const lmm_bermudan_desc* product, double* out_value,
                            double* out_error, double* out_values_host);
 
+/* Mean and standard error of num_values doubles already in device memory (d_values),
+ * computed with the same compensated reduction as the product entry points, without
+ * allocating anything.  No counterpart in finmath-lib: it exists for callers that must
+ * not allocate device memory on their valuation path -- a service that reserves its
+ * whole device budget at start-up and forbids allocator calls afterwards, or code that
+ * records its work into a CUDA graph, where an allocation would become part of the
+ * graph.  Its scratch is one fixed 8,208-byte array per GPU inside the library (held
+ * until the process exits), so:
+ *   - num_values must be in [1, 2^30]; larger inputs are rejected with LMM_ERR_INVALID;
+ *   - every call shares that array: calls that overlap on the GPU (different streams, or
+ *     different host threads on one device) race and must be serialised by the caller;
+ *   - the first call on a device looks up the array's device address (which may load the
+ *     library's GPU code on that device); make that first call before any stream capture.
+ * stream is a cudaStream_t (NULL = the legacy default stream); d_values must be ready in
+ * stream order.  The call waits for the two results and writes them to host memory. */
+int lmm_values_mean_stderr_noalloc(const double* d_values, int64_t num_values, void* stream, double* out_mean,
+                                   double* out_error);
+
 /* ---------------------------------------------------------------- instrumentation */
 /* Per-kernel launch counts and (when enabled) CUDA-event times of this library's kernels. */
 int lmm_stats_enable_timing(int enable);
