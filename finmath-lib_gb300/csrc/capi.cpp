@@ -181,6 +181,7 @@ struct lmm_process {
     cudaStream_t stream = nullptr;
     // device tables
     double *d_loadings = nullptr, *d_variance = nullptr, *d_dt = nullptr, *d_delta = nullptr, *d_init = nullptr;
+    double *d_inv_delta = nullptr, *d_var_half = nullptr;
     float *d_lam32 = nullptr, *d_var32 = nullptr;
     int *d_first = nullptr, *d_obs_slot = nullptr;
     uint8_t* d_det = nullptr;
@@ -195,9 +196,11 @@ struct lmm_process {
     double* d_reduce = nullptr;
     size_t reduce_bytes = 0;
     double *d_under = nullptr, *d_ex = nullptr, *d_basis = nullptr, *d_gram = nullptr, *d_beta = nullptr;
+    double *d_svd = nullptr, *d_rhs = nullptr;
     double *d_period_length = nullptr, *d_tenor_delta = nullptr;
-    int* d_period_index = nullptr;
-    int berm_capacity = 0;
+    int *d_period_index = nullptr, *d_ex_period = nullptr;
+    BermudanPeriod* d_per = nullptr;
+    int berm_capacity = 0;   // exercise dates the basis / Gram buffers hold
 };
 
 extern "C" {
@@ -417,15 +420,25 @@ int lmm_process_create(const lmm_model_desc* m, lmm_brownian* bm, lmm_process** 
     for (int t = 0; t <= T; t++) pr->obs_slot[t] = t;
     pr->nobs = T + 1;
 
-    std::vector<double> dt(T), delta(N);
+    std::vector<double> dt(T), delta(N), inv_delta(N), var_half((size_t)T * N);
     for (int i = 0; i < T; i++) dt[i] = pr->times[i + 1] - pr->times[i];
-    for (int j = 0; j < N; j++) delta[j] = pr->tenor[j + 1] - pr->tenor[j];
+    for (int j = 0; j < N; j++) {
+        delta[j] = pr->tenor[j + 1] - pr->tenor[j];
+        inv_delta[j] = 1.0 / delta[j];
+        if (delta[j] / delta[j] != 1.0) {
+            delete pr;
+            return fail(LMM_ERR_INVALID, "tenor periods must be finite and positive");
+        }
+    }
+    for (size_t i = 0; i < var_half.size(); i++) var_half[i] = m->variance[i] * -0.5;
     cudaStream_t s = pr->stream;
     int rc = 0;
     if (!rc) rc = upload(&pr->d_loadings, m->factor_loadings, (size_t)T * N * F, s);
     if (!rc) rc = upload(&pr->d_variance, m->variance, (size_t)T * N, s);
     if (!rc) rc = upload(&pr->d_dt, dt.data(), dt.size(), s);
     if (!rc) rc = upload(&pr->d_delta, delta.data(), delta.size(), s);
+    if (!rc) rc = upload(&pr->d_inv_delta, inv_delta.data(), inv_delta.size(), s);
+    if (!rc) rc = upload(&pr->d_var_half, var_half.data(), var_half.size(), s);
     if (!rc) rc = upload(&pr->d_init, m->initial_forwards, (size_t)N, s);
     if (!rc) rc = upload(&pr->d_first, pr->first.data(), pr->first.size(), s);
     if (!rc) rc = upload(&pr->d_det, pr->num_det.data(), pr->num_det.size(), s);
@@ -493,6 +506,8 @@ static int process_ensure(lmm_process* pr)
     a.d_dt = pr->d_dt;
     a.d_first = pr->d_first;
     a.d_delta = pr->d_delta;
+    a.d_inv_delta = pr->d_inv_delta;
+    a.d_var_half = pr->d_var_half;
     a.d_init = pr->d_init;
     a.d_obs_slot = pr->d_obs_slot;
     a.d_dw = pr->bm->d_dw;
@@ -567,6 +582,8 @@ int lmm_process_destroy(lmm_process* pr)
     dfree(pr->d_variance, s);
     dfree(pr->d_dt, s);
     dfree(pr->d_delta, s);
+    dfree(pr->d_inv_delta, s);
+    dfree(pr->d_var_half, s);
     dfree(pr->d_init, s);
     dfree(pr->d_lam32, s);
     dfree(pr->d_var32, s);
@@ -582,6 +599,10 @@ int lmm_process_destroy(lmm_process* pr)
     dfree(pr->d_period_length, s);
     dfree(pr->d_tenor_delta, s);
     dfree(pr->d_period_index, s);
+    dfree(pr->d_svd, s);
+    dfree(pr->d_rhs, s);
+    dfree(pr->d_ex_period, s);
+    dfree(pr->d_per, s);
     cudaStreamSynchronize(s);
     delete pr;
     return LMM_OK;
@@ -740,17 +761,29 @@ int lmm_bermudan_get_value(lmm_process* pr, const lmm_bermudan_desc* d, double* 
     if (rc) return rc;
     cudaStream_t s = pr->stream;
     const int blocks = bermudan_blocks(pr->P);
-    if (pr->berm_capacity == 0) {
+    int ne = 0;
+    for (int q = 0; q < n; q++) ne += a.per[q].exercisable ? 1 : 0;
+    if (!pr->d_under) {
         if (!rc) rc = dalloc(&pr->d_under, (size_t)pr->P, s);
         if (!rc) rc = dalloc(&pr->d_ex, (size_t)pr->P, s);
-        if (!rc) rc = dalloc(&pr->d_basis, (size_t)5 * pr->P, s);
-        if (!rc) rc = dalloc(&pr->d_gram, (size_t)blocks * 26 * 2, s);
+        if (!rc) rc = dalloc(&pr->d_rhs, (size_t)blocks * 6 * 2, s);
         if (!rc) rc = dalloc(&pr->d_beta, (size_t)64 * 6, s);
+        if (!rc) rc = dalloc(&pr->d_svd, (size_t)64 * 80, s);
         if (!rc) rc = dalloc(&pr->d_period_length, (size_t)64, s);
         if (!rc) rc = dalloc(&pr->d_period_index, (size_t)64, s);
+        if (!rc) rc = dalloc(&pr->d_ex_period, (size_t)64, s);
         if (!rc) rc = dalloc(&pr->d_tenor_delta, (size_t)64, s);
+        if (!rc) rc = dalloc(&pr->d_per, (size_t)64, s);
         if (rc) return rc;
-        pr->berm_capacity = 64;
+    }
+    if (ne > pr->berm_capacity) {
+        dfree(pr->d_basis, s);
+        dfree(pr->d_gram, s);
+        const int bx = bermudan_gram_blocks(pr->P, ne);
+        if (!rc) rc = dalloc(&pr->d_basis, (size_t)ne * 5 * pr->P, s);
+        if (!rc) rc = dalloc(&pr->d_gram, (size_t)ne * bx * 20 * 2, s);
+        if (rc) return rc;
+        pr->berm_capacity = ne;
     }
     LMM_CUDA(cudaMemcpyAsync(pr->d_period_length, plen.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
     LMM_CUDA(cudaMemcpyAsync(pr->d_period_index, pidx.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
@@ -760,8 +793,12 @@ int lmm_bermudan_get_value(lmm_process* pr, const lmm_bermudan_desc* d, double* 
     sc.d_under = pr->d_under;
     sc.d_ex = pr->d_ex;
     sc.d_basis = pr->d_basis;
-    sc.d_partials = pr->d_gram;
+    sc.d_gram = pr->d_gram;
+    sc.d_svd = pr->d_svd;
+    sc.d_partials = pr->d_rhs;
     sc.d_beta = pr->d_beta;
+    sc.d_per = pr->d_per;
+    sc.d_ex_period = pr->d_ex_period;
     sc.d_tenor_delta = pr->d_tenor_delta;
     sc.d_period_index = pr->d_period_index;
     sc.d_period_length = pr->d_period_length;

@@ -94,6 +94,8 @@ struct PathLaunch {
     const double* d_dt;        // [T]
     const int* d_first;        // [T] first alive component at t_i
     const double* d_delta;     // [N] period lengths
+    const double* d_inv_delta; // [N] 1.0 / delta (delta/delta == 1.0 exactly for the validated tenor)
+    const double* d_var_half;  // [T][N] variance * -0.5 (exact scaling)
     const double* d_init;      // [N] initial forwards
     const int* d_obs_slot;     // [T+1] observation slot or -1
     const void* d_dw;          // [T][F][P] fp64 or fp32
@@ -161,14 +163,19 @@ struct BermudanScratch {
     double* d_values;     // [P]
     double* d_under;      // [P]
     double* d_ex;         // [P]
-    double* d_basis;      // [5][P]
-    double* d_partials;   // [blocks][27][2]
-    double* d_beta;       // [nper][6]
+    double* d_basis;      // [ne][5][P] basis functions of every exercise date
+    double* d_gram;       // [ne][gram blocks][20][2] Gram partial sums
+    double* d_svd;        // [ne][80] U, s, V and cutoff of every exercise date
+    double* d_partials;   // [blocks][6][2] X^T y partial sums of one date
+    double* d_beta;       // [ne][6]
+    BermudanPeriod* d_per;          // [nper]
+    int* d_ex_period;               // [ne]
     const double* d_tenor_delta;    // [N]
     const int* d_period_index;      // [nper]
     const double* d_period_length;  // [nper]
 };
 int bermudan_blocks(int P);
+int bermudan_gram_blocks(int P, int ne);
 int launch_bermudan(const ProductView& v, const BermudanLaunch& a, const BermudanScratch& sc, cudaStream_t s,
                     int* launches);
 

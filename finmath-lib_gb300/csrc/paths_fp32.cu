@@ -63,7 +63,7 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp32_kernel(const PathLaun
 #pragma unroll
         for (int j = 0; j < NMAX; j++) {
             if (j < N && j >= first) {
-                const float invd = (float)(1.0 / __ldg(a.d_delta + j));
+                const float invd = (float)__ldg(a.d_inv_delta + j);
                 const float os = __fdividef(L[j], L[j] + invd);
                 float mu = -0.5f * __ldg(var + j);
                 float diff = 0.0f;

@@ -62,7 +62,7 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp64_kernel(const PathLaun
         const int first = __ldg(a.d_first + i);
         const double dt = __ldg(a.d_dt + i);
         const double* lam = a.d_loadings + (size_t)i * N * F;
-        const double* var = a.d_variance + (size_t)i * N;
+        const double* var_half = a.d_var_half + (size_t)i * N;
         double dw[FMAX];
 #pragma unroll
         for (int k = 0; k < FMAX; k++) dw[k] = (k < F && active) ? dW[((size_t)i * F + k) * P + p] : 0.0;
@@ -73,9 +73,9 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp64_kernel(const PathLaun
         for (int j = 0; j < NMAX; j++) {
             if (j < N && j >= first) {
                 const double Lj = L[j];
-                const double delta = __ldg(a.d_delta + j);
-                // Scalar(delta).discount(L, delta) (stochastic/Scalar.java:321-328), times L (:1149-1153)
-                const double os = (1.0 / (Lj * (delta / delta) + 1.0 / delta)) * Lj;
+                // Scalar(delta).discount(L, delta) = 1/(L*(delta/delta) + 1/delta) (stochastic/Scalar.java:321-328),
+                // times L (:1149-1153); delta/delta is exactly 1.0 and 1/delta is precomputed.
+                const double os = (1.0 / (Lj + __ldg(a.d_inv_delta + j))) * Lj;
                 double mu = 0.0;
                 double lj[FMAX];
 #pragma unroll
@@ -88,7 +88,7 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp64_kernel(const PathLaun
 #pragma unroll
                 for (int k = 0; k < FMAX; k++)
                     if (k < F) mu = mu + S[k] * lj[k];  // :1159 (addSumProduct, left to right)
-                mu = mu + __ldg(var + j) * -0.5;         // :1183-1189
+                mu = mu + __ldg(var_half + j);           // :1183-1189, variance * -0.5
                 // Euler step (EulerSchemeFromProcessModel.java:235-255)
                 double y = FUNCTIONAL ? log(Lj) : Y[FUNCTIONAL ? 0 : j];
                 y = y + mu * dt;

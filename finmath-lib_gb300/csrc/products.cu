@@ -122,34 +122,30 @@ __global__ void __launch_bounds__(kProdThreads) swaption_kernel(const SwaptionPa
 }
 
 // ------------------------------------------------------------------ Bermudan
-constexpr int kGramEntries = 26;  // G[0][1..5], G[1..5][1..5] (i<=j), rhs[0..5]
+// The regression's Gram matrix X^T X at an exercise date depends only on the basis
+// functions, not on the backward induction, so (as the reference caches its solver,
+// MonteCarloConditionalExpectationRegression.java:125-137) all exercise dates' Gram
+// matrices are accumulated in one pass and their SVDs computed in parallel.  The
+// backward induction then needs, per date, only the six sums of X^T y and a 6x6 apply.
+constexpr int kGram = 20;  // G[0][1..5] and G[1..5][1..5] (i<=j); G[0][0] = 1 exactly
+constexpr int kRhs = 6;
+constexpr int kSvdStride = 80;  // U[36], s[6], V[36], tol, pad
 
-struct BermStepParams {
-    BermudanPeriod cur;        // period processed by this launch
-    int has_cur;
-    int apply_choose;          // apply the pending choose of the previous exercise
-    double choose_fixing;
-    const double* beta;        // [6] of the pending choose
-    int basis, callable;
+struct BermShared {
+    int basis, callable, N, P, ne;
     NumeraireInfo num;
     const void* states;
-    int N, P, fp32;
-    double* values;
-    double* under;
-    double* ex;
-    double* basis_buf;         // [5][P]
-    double* partials;          // [blocks][26][2]
-    const double* tenor_delta;     // [N] tenor period lengths (device)
-    const int* period_index;       // [nper] tenor index of each product period (device)
-    const double* period_length;   // [nper] product period lengths (device)
-    int init;                      // first launch: values = underlying = 0, exercise time = +inf
-    int final_pass;
+    const BermudanPeriod* per;     // [nper] (device)
+    const int* ex_period;          // [ne] period index of each exercise date (device)
+    const double* tenor_delta;     // [N]
+    const int* period_index;       // [nper]
+    const double* period_length;   // [nper]
+    double* basis_buf;             // [ne][5][P]
 };
 
 template <typename TS>
-__device__ void bermudan_basis(const BermStepParams& a, int p, double B[5])
+__device__ void bermudan_basis(const BermShared& a, const BermudanPeriod& c, int p, double B[5])
 {
-    const BermudanPeriod& c = a.cur;
     if (a.basis == 1) {
         // {S, S^2, N, N^2, S*N}: S = par rate of the remaining periods from L_j(T_ex),
         // S = (prod g_q - 1) / sum_s d_s prod_{r>s} g_r with g_q = 1 + L_q d_q, both by a
@@ -199,93 +195,48 @@ __device__ void bermudan_basis(const BermStepParams& a, int p, double B[5])
     }
 }
 
+// grid (bx, ne): basis functions of exercise date blockIdx.y and their Gram partial sums
 template <typename TS>
-__global__ void __launch_bounds__(kProdThreads) bermudan_step_kernel(const BermStepParams a)
+__global__ void __launch_bounds__(kProdThreads) bermudan_gram_kernel(const BermShared a, double* partials)
 {
-    const double w = 1.0 / (double)a.P;
-    // per-thread plain sums over this thread's few paths; compensated across threads
-    double acc[kGramEntries];
+    const int e = blockIdx.y;
+    const BermudanPeriod c = a.per[a.ex_period[e]];
+    double acc[kGram];
 #pragma unroll
-    for (int e = 0; e < kGramEntries; e++) acc[e] = 0.0;
-    const bool gram = a.has_cur && a.cur.exercisable;
-    double beta[6];
-    if (a.apply_choose) {
-#pragma unroll
-        for (int i = 0; i < 6; i++) beta[i] = a.beta[i];
-    }
+    for (int k = 0; k < kGram; k++) acc[k] = 0.0;
+    double* bb = a.basis_buf + (size_t)e * 5 * a.P;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.P; p += gridDim.x * blockDim.x) {
-        double v, u;
-        if (a.init) {
-            v = 0.0;
-            u = 0.0;
-            a.ex[p] = CUDART_INF;
-        } else {
-            v = a.values[p];
-            u = a.under[p];
-        }
-        if (a.apply_choose) {
-            // conditional expectation X beta (:104-107), then choose (:139, :141)
-            double ce = 1.0 * beta[0];
+        double B[5];
+        bermudan_basis<TS>(a, c, p, B);
 #pragma unroll
-            for (int i = 1; i < 6; i++) ce = ce + a.basis_buf[(size_t)(i - 1) * a.P + p] * beta[i];
-            const bool cont = ce >= 0.0;
-            v = cont ? v : u;
-            if (!cont) a.ex[p] = a.choose_fixing;
-        }
-        if (a.has_cur) {
-            const BermudanPeriod& c = a.cur;
-            const double L = state_at<TS>(a.states, c.libor_slot, a.N, a.P, c.libor_index, p);
-            double payoff = ((L - c.strike) * c.period_length) * c.notional;
-            payoff = payoff / numeraire_adj(a.num, c.pay_num_index, p);
-            payoff = payoff * w;
-            if (a.callable) u = u + payoff;
-            else v = v + payoff;
-            if (gram) {
-                const double y = v - u;
-                double B[5];
-                bermudan_basis<TS>(a, p, B);
+        for (int i = 0; i < 5; i++) bb[(size_t)i * a.P + p] = B[i];
+        int k = 0;
 #pragma unroll
-                for (int i = 0; i < 5; i++) a.basis_buf[(size_t)i * a.P + p] = B[i];
-                int e = 0;
+        for (int i = 0; i < 5; i++) acc[k + i] = acc[k + i] + B[i];  // mean(1 * B_i)
+        k += 5;
 #pragma unroll
-                for (int i = 0; i < 5; i++) acc[e + i] = acc[e + i] + B[i];  // G[0][1..5]
-                e += 5;
+        for (int i = 0; i < 5; i++)
 #pragma unroll
-                for (int i = 0; i < 5; i++)
-#pragma unroll
-                    for (int j = i; j < 5; j++) {
-                        acc[e] = acc[e] + B[i] * B[j];
-                        e++;
-                    }
-                acc[e] = acc[e] + y * 1.0;  // rhs[0] = mean(y * 1)
-                e++;
-#pragma unroll
-                for (int i = 0; i < 5; i++) acc[e + i] = acc[e + i] + y * B[i];
+            for (int j = i; j < 5; j++) {
+                acc[k] = acc[k] + B[i] * B[j];
+                k++;
             }
-        }
-        if (a.final_pass) v = (v * 1.0) / w;
-        a.values[p] = v;
-        a.under[p] = u;
     }
-    if (gram) {
 #pragma unroll
-        for (int e = 0; e < kGramEntries; e++) {
-            const dd s = block_dd_sum(dd{acc[e], 0.0});
-            if (threadIdx.x == 0) {
-                a.partials[((size_t)blockIdx.x * kGramEntries + e) * 2] = s.hi;
-                a.partials[((size_t)blockIdx.x * kGramEntries + e) * 2 + 1] = s.lo;
-            }
+    for (int k = 0; k < kGram; k++) {
+        const dd s = block_dd_sum(dd{acc[k], 0.0});
+        if (threadIdx.x == 0) {
+            double* q = partials + (((size_t)e * gridDim.x + blockIdx.x) * kGram + k) * 2;
+            q[0] = s.hi;
+            q[1] = s.lo;
         }
     }
 }
 
-// One-sided Jacobi SVD pseudo-inverse solve of the 6x6 normal equations.  The same
-// algorithm and cutoff as the oracle: singular values <= max(6 * s_max * 2^-52,
-// sqrt(2^-1022)) are dropped (SVD-based least squares, MonteCarloConditionalExpectationRegression.java:136,147).
-__device__ void solve_pinv6(const double Gin[36], const double b[6], double x[6])
+// One-sided Jacobi SVD G V = U diag(s) of the 6x6 Gram matrix (the oracle's algorithm).
+__device__ void svd6(const double G[36], double U[36], double s[6], double V[36])
 {
-    double U[36], V[36], s[6];
-    for (int i = 0; i < 36; i++) U[i] = Gin[i];
+    for (int i = 0; i < 36; i++) U[i] = G[i];
     for (int i = 0; i < 6; i++)
         for (int j = 0; j < 6; j++) V[i * 6 + j] = (i == j) ? 1.0 : 0.0;
     for (int sweep = 0; sweep < 60; sweep++) {
@@ -303,33 +254,170 @@ __device__ void solve_pinv6(const double Gin[36], const double b[6], double x[6]
                 rotated = 1;
                 const double zeta = (beta - alpha) / (2.0 * gamma);
                 const double t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-                const double c = 1.0 / sqrt(1.0 + t * t), sn = c * t;
+                const double cs = 1.0 / sqrt(1.0 + t * t), sn = cs * t;
                 for (int k = 0; k < 6; k++) {
                     const double up = U[k * 6 + p], uq = U[k * 6 + q];
-                    U[k * 6 + p] = c * up - sn * uq;
-                    U[k * 6 + q] = sn * up + c * uq;
+                    U[k * 6 + p] = cs * up - sn * uq;
+                    U[k * 6 + q] = sn * up + cs * uq;
                 }
                 for (int k = 0; k < 6; k++) {
                     const double vp = V[k * 6 + p], vq = V[k * 6 + q];
-                    V[k * 6 + p] = c * vp - sn * vq;
-                    V[k * 6 + q] = sn * vp + c * vq;
+                    V[k * 6 + p] = cs * vp - sn * vq;
+                    V[k * 6 + q] = sn * vp + cs * vq;
                 }
             }
         if (!rotated) break;
     }
-    double smax = 0.0;
     for (int j = 0; j < 6; j++) {
         double nn = 0.0;
         for (int k = 0; k < 6; k++) nn += U[k * 6 + j] * U[k * 6 + j];
         s[j] = sqrt(nn);
         if (s[j] > 0.0)
             for (int k = 0; k < 6; k++) U[k * 6 + j] = U[k * 6 + j] / s[j];
-        smax = s[j] > smax ? s[j] : smax;
     }
-    double tol = 6.0 * smax * 0x1.0p-52;
-    const double tmin = sqrt(0x1.0p-1022);
-    if (tol < tmin) tol = tmin;
-    for (int i = 0; i < 6; i++) {
+}
+
+// grid ne x 32: reduce the Gram partials of date blockIdx.x, SVD, store U, s, V, cutoff
+__global__ void __launch_bounds__(32) bermudan_svd_kernel(const double* partials, int bx, int P, double* svd)
+{
+    __shared__ double tot[kGram];
+    const int e = blockIdx.x, lane = threadIdx.x;
+    for (int k = 0; k < kGram; k++) {
+        dd acc{0.0, 0.0};
+        for (int b = lane; b < bx; b += 32) {
+            const double* q = partials + (((size_t)e * bx + b) * kGram + k) * 2;
+            acc = dd_add(acc, dd{q[0], q[1]});
+        }
+        acc = warp_dd_sum(acc);
+        if (lane == 0) tot[k] = (acc.hi + acc.lo) / (double)P;
+    }
+    __syncwarp();
+    if (lane == 0) {
+        double G[36], U[36], s[6], V[36];
+        G[0] = 1.0 * 1.0;
+        int k = 0;
+        for (int j = 1; j < 6; j++) { G[j] = tot[k]; G[j * 6] = tot[k]; k++; }
+        for (int i = 1; i < 6; i++)
+            for (int j = i; j < 6; j++) { G[i * 6 + j] = tot[k]; G[j * 6 + i] = tot[k]; k++; }
+        svd6(G, U, s, V);
+        double smax = 0.0;
+        for (int j = 0; j < 6; j++) smax = s[j] > smax ? s[j] : smax;
+        double tol = 6.0 * smax * 0x1.0p-52;
+        const double tmin = sqrt(0x1.0p-1022);
+        if (tol < tmin) tol = tmin;
+        double* o = svd + (size_t)e * kSvdStride;
+        for (int i = 0; i < 36; i++) o[i] = U[i];
+        for (int i = 0; i < 6; i++) o[36 + i] = s[i];
+        for (int i = 0; i < 36; i++) o[42 + i] = V[i];
+        o[78] = tol;
+    }
+}
+
+struct BermStepParams {
+    BermShared sh;
+    int cur;                   // period processed by this launch (-1: final pass)
+    int cur_ex;                // exercise index of cur (or -1)
+    int pending_ex;            // exercise index whose choose is pending (or -1)
+    double pending_fixing;
+    const double* beta;        // [ne][6]
+    double* values;
+    double* under;
+    double* ex;
+    double* partials;          // [blocks][6][2]
+    int init;
+};
+
+template <typename TS>
+__global__ void __launch_bounds__(kProdThreads) bermudan_step_kernel(const BermStepParams a)
+{
+    const BermShared& sh = a.sh;
+    const double w = 1.0 / (double)sh.P;
+    double acc[kRhs];
+#pragma unroll
+    for (int i = 0; i < kRhs; i++) acc[i] = 0.0;
+    double beta[6];
+    const double* bprev = nullptr;
+    if (a.pending_ex >= 0) {
+#pragma unroll
+        for (int i = 0; i < 6; i++) beta[i] = a.beta[a.pending_ex * 6 + i];
+        bprev = sh.basis_buf + (size_t)a.pending_ex * 5 * sh.P;
+    }
+    const double* bcur = a.cur_ex >= 0 ? sh.basis_buf + (size_t)a.cur_ex * 5 * sh.P : nullptr;
+    BermudanPeriod c;
+    if (a.cur >= 0) c = sh.per[a.cur];
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < sh.P; p += gridDim.x * blockDim.x) {
+        double v, u;
+        if (a.init) {
+            v = 0.0;
+            u = 0.0;
+            a.ex[p] = CUDART_INF;
+        } else {
+            v = a.values[p];
+            u = a.under[p];
+        }
+        if (bprev) {
+            // conditional expectation X beta (:104-107), then choose (:139, :141)
+            double ce = 1.0 * beta[0];
+#pragma unroll
+            for (int i = 1; i < 6; i++) ce = ce + bprev[(size_t)(i - 1) * sh.P + p] * beta[i];
+            const bool cont = ce >= 0.0;
+            v = cont ? v : u;
+            if (!cont) a.ex[p] = a.pending_fixing;
+        }
+        if (a.cur >= 0) {
+            const double L = state_at<TS>(sh.states, c.libor_slot, sh.N, sh.P, c.libor_index, p);
+            double payoff = ((L - c.strike) * c.period_length) * c.notional;
+            payoff = payoff / numeraire_adj(sh.num, c.pay_num_index, p);
+            payoff = payoff * w;
+            if (sh.callable) u = u + payoff;
+            else v = v + payoff;
+            if (bcur) {
+                const double y = v - u;
+                acc[0] = acc[0] + y * 1.0;
+#pragma unroll
+                for (int i = 0; i < 5; i++) acc[1 + i] = acc[1 + i] + y * bcur[(size_t)i * sh.P + p];
+            }
+        } else {
+            v = (v * 1.0) / w;
+        }
+        a.values[p] = v;
+        a.under[p] = u;
+    }
+    if (bcur) {
+#pragma unroll
+        for (int i = 0; i < kRhs; i++) {
+            const dd s = block_dd_sum(dd{acc[i], 0.0});
+            if (threadIdx.x == 0) {
+                a.partials[((size_t)blockIdx.x * kRhs + i) * 2] = s.hi;
+                a.partials[((size_t)blockIdx.x * kRhs + i) * 2 + 1] = s.lo;
+            }
+        }
+    }
+}
+
+// X^T y sums of one date and beta = V diag(1/s) U^T (X^T y) with the SVD's cutoff,
+// in the oracle's order (MonteCarloConditionalExpectationRegression.java:141-147).
+__global__ void __launch_bounds__(192) bermudan_apply_kernel(const double* partials, int blocks, int P, const double* svd,
+                                                             double* beta_out)
+{
+    __shared__ double b[kRhs];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (warp < kRhs) {
+        dd acc{0.0, 0.0};
+        for (int k = lane; k < blocks; k += 32) {
+            const double* q = partials + ((size_t)k * kRhs + warp) * 2;
+            acc = dd_add(acc, dd{q[0], q[1]});
+        }
+        acc = warp_dd_sum(acc);
+        if (lane == 0) b[warp] = (acc.hi + acc.lo) / (double)P;
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        const double* U = svd;
+        const double* s = svd + 36;
+        const double* V = svd + 42;
+        const double tol = svd[78];
+        const int i = threadIdx.x;
         double acc = 0.0;
         for (int j = 0; j < 6; j++) {
             if (!(s[j] > tol)) continue;
@@ -337,35 +425,7 @@ __device__ void solve_pinv6(const double Gin[36], const double b[6], double x[6]
             for (int r = 0; r < 6; r++) utb += U[r * 6 + j] * b[r];
             acc += V[i * 6 + j] * (utb / s[j]);
         }
-        x[i] = acc;
-    }
-}
-
-__global__ void __launch_bounds__(256) bermudan_solve_kernel(const double* partials, int blocks, int P, double* beta_out)
-{
-    __shared__ double tot[kGramEntries];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int nwarps = blockDim.x >> 5;
-    for (int e = warp; e < kGramEntries; e += nwarps) {
-        dd acc{0.0, 0.0};
-        for (int b = lane; b < blocks; b += 32) {
-            const double* q = partials + ((size_t)b * kGramEntries + e) * 2;
-            acc = dd_add(acc, dd{q[0], q[1]});
-        }
-        acc = warp_dd_sum(acc);
-        if (lane == 0) tot[e] = (acc.hi + acc.lo) / (double)P;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double G[36], rhs[6], x[6];
-        G[0] = 1.0 * 1.0;
-        int e = 0;
-        for (int j = 1; j < 6; j++) { G[j] = tot[e]; G[j * 6] = tot[e]; e++; }
-        for (int i = 1; i < 6; i++)
-            for (int j = i; j < 6; j++) { G[i * 6 + j] = tot[e]; G[j * 6 + i] = tot[e]; e++; }
-        for (int i = 0; i < 6; i++) rhs[i] = tot[e++];
-        solve_pinv6(G, rhs, x);
-        for (int i = 0; i < 6; i++) beta_out[i] = x[i];
+        beta_out[i] = acc;
     }
 }
 
@@ -453,37 +513,73 @@ int bermudan_blocks(int P)
     return grid_for(P, kProdThreads, cap);
 }
 
+int bermudan_gram_blocks(int P, int ne)
+{
+    const int total = bermudan_blocks(P);
+    int bx = (total + ne - 1) / (ne > 0 ? ne : 1);
+    const int need = (P + kProdThreads - 1) / kProdThreads;
+    if (bx > need) bx = need;
+    return bx < 1 ? 1 : bx;
+}
+
 int launch_bermudan(const ProductView& v, const BermudanLaunch& a, const BermudanScratch& sc, cudaStream_t s,
                     int* launches)
 {
     const int blocks = bermudan_blocks(v.P);
+    std::vector<int> ex_period, ex_of_period(a.nper, -1);
+    for (int q = 0; q < a.nper; q++)
+        if (a.per[q].exercisable) {
+            ex_of_period[q] = (int)ex_period.size();
+            ex_period.push_back(q);
+        }
+    const int ne = (int)ex_period.size();
+    LMM_CUDA(cudaMemcpyAsync(sc.d_per, a.per.data(), sizeof(BermudanPeriod) * a.nper, cudaMemcpyHostToDevice, s));
+    if (ne) LMM_CUDA(cudaMemcpyAsync(sc.d_ex_period, ex_period.data(), sizeof(int) * ne, cudaMemcpyHostToDevice, s));
+    BermShared sh;
+    std::memset(&sh, 0, sizeof(sh));
+    sh.basis = a.basis;
+    sh.callable = a.callable;
+    sh.N = v.N;
+    sh.P = v.P;
+    sh.ne = ne;
+    sh.num = make_numeraire_info(v);
+    sh.states = v.d_states;
+    sh.per = sc.d_per;
+    sh.ex_period = sc.d_ex_period;
+    sh.tenor_delta = sc.d_tenor_delta;
+    sh.period_index = sc.d_period_index;
+    sh.period_length = sc.d_period_length;
+    sh.basis_buf = sc.d_basis;
+    if (ne > 0) {
+        const int bx = bermudan_gram_blocks(v.P, ne);
+        {
+            KernelTimer kt(K_BERMUDAN_STEP, s);
+            const dim3 grid(bx, ne);
+            if (v.state_fp32) bermudan_gram_kernel<float><<<grid, kProdThreads, 0, s>>>(sh, sc.d_gram);
+            else bermudan_gram_kernel<double><<<grid, kProdThreads, 0, s>>>(sh, sc.d_gram);
+            LMM_CUDA(cudaGetLastError());
+        }
+        {
+            KernelTimer kt(K_BERMUDAN_SOLVE, s);
+            bermudan_svd_kernel<<<ne, 32, 0, s>>>(sc.d_gram, bx, v.P, sc.d_svd);
+            LMM_CUDA(cudaGetLastError());
+        }
+        if (launches) (*launches) += 2;
+    }
     BermStepParams prm;
     std::memset(&prm, 0, sizeof(prm));
-    prm.basis = a.basis;
-    prm.callable = a.callable;
-    prm.num = make_numeraire_info(v);
-    prm.states = v.d_states;
-    prm.N = v.N;
-    prm.P = v.P;
-    prm.fp32 = v.state_fp32;
+    prm.sh = sh;
+    prm.beta = sc.d_beta;
     prm.values = sc.d_values;
     prm.under = sc.d_under;
     prm.ex = sc.d_ex;
-    prm.basis_buf = sc.d_basis;
     prm.partials = sc.d_partials;
-    prm.tenor_delta = sc.d_tenor_delta;
-    prm.period_index = sc.d_period_index;
-    prm.period_length = sc.d_period_length;
-    int pending = -1;  // exercise period whose choose is pending
+    int pending = -1;  // exercise index whose choose is pending
     for (int per = a.nper - 1; per >= -1; per--) {
-        prm.has_cur = per >= 0;
-        if (per >= 0) prm.cur = a.per[per];
-        prm.apply_choose = pending >= 0;
-        if (pending >= 0) {
-            prm.beta = sc.d_beta + (size_t)pending * 6;
-            prm.choose_fixing = a.per[pending].fixing;
-        }
-        prm.final_pass = per < 0;
+        prm.cur = per;
+        prm.cur_ex = per >= 0 ? ex_of_period[per] : -1;
+        prm.pending_ex = pending;
+        prm.pending_fixing = pending >= 0 ? a.per[ex_period[pending]].fixing : 0.0;
         prm.init = per == a.nper - 1;
         {
             KernelTimer kt(K_BERMUDAN_STEP, s);
@@ -493,12 +589,13 @@ int launch_bermudan(const ProductView& v, const BermudanLaunch& a, const Bermuda
         }
         if (launches) (*launches)++;
         pending = -1;
-        if (per >= 0 && a.per[per].exercisable) {
+        if (per >= 0 && prm.cur_ex >= 0) {
             KernelTimer kt(K_BERMUDAN_SOLVE, s);
-            bermudan_solve_kernel<<<1, 256, 0, s>>>(sc.d_partials, blocks, v.P, sc.d_beta + (size_t)per * 6);
+            bermudan_apply_kernel<<<1, 192, 0, s>>>(sc.d_partials, blocks, v.P, sc.d_svd + (size_t)prm.cur_ex * kSvdStride,
+                                                    sc.d_beta + (size_t)prm.cur_ex * 6);
             LMM_CUDA(cudaGetLastError());
             if (launches) (*launches)++;
-            pending = per;
+            pending = prm.cur_ex;
         }
     }
     return LMM_OK;

@@ -52,7 +52,23 @@ __device__ __forceinline__ uint32_t mt_next(uint32_t x_m, uint32_t x_0, uint32_t
 }
 
 // NormalDistribution.inverseCumulativeNormalDistributionWichura (functions/NormalDistribution.java:67-162),
-// AS241 (Wichura 1988) with the reference's evaluation order.
+// AS241 (Wichura 1988) with the reference's evaluation order.  The central branch
+// (|p - 0.5| <= 0.425, ~85 % of draws) and the tails are separate functions so that the
+// generator can run each on a compacted set of lanes.
+__device__ __forceinline__ double icdf_central(double q)
+{
+    const double r = 0.180625 - q * q;
+    const double num = (((((((2.5090809287301226727e+03 * r + 3.3430575583588128105e+04) * r +
+                             6.7265770927008700853e+04) * r + 4.5921953931549871457e+04) * r +
+                           1.3731693765509461125e+04) * r + 1.9715909503065514427e+03) * r +
+                         1.3314166789178437745e+02) * r + 3.3871328727963666080e+00);
+    const double den = (((((((5.2264952788528545610e+03 * r + 2.8729085735721942674e+04) * r +
+                             3.9307895800092710610e+04) * r + 2.1213794301586595867e+04) * r +
+                           5.3941960214247511077e+03) * r + 6.8718700749205790830e+02) * r +
+                         4.2313330701600911252e+01) * r + 1.0);
+    return q * num / den;
+}
+
 __device__ double icdf_wichura(double p)
 {
     const double q = p - 0.5;
@@ -184,6 +200,10 @@ __global__ void __launch_bounds__(kRngThreads, 2) mt_generate_kernel(const RngPa
     // ---- generate: 624 words -> 312 values per round
     uint32_t* cur = x;
     uint32_t* nxt = x + kMtN;
+    // tail draws of a round, processed by consecutive lanes after the central ones
+    __shared__ double tail_u[kMtN / 2];
+    __shared__ short tail_i[kMtN / 2];
+    __shared__ int tail_n;
     const int TF = prm.values_per_path;
     const int F = prm.num_factors;
     const int P = prm.num_paths;
@@ -194,12 +214,15 @@ __global__ void __launch_bounds__(kRngThreads, 2) mt_generate_kernel(const RngPa
             const int k = 227 + tid;
             nxt[k] = mt_next(nxt[k - 227], cur[k], cur[k + 1]);
         }
+        if (tid == 0) tail_n = 0;  // every lane finished the previous round's tails before the barrier above
         __syncthreads();
         if (tid < 170) {
             const int k = 454 + tid;
             nxt[k] = mt_next(nxt[k - 227], cur[k], (k == kMtN - 1) ? nxt[0] : cur[k + 1]);
         }
         __syncthreads();
+        const int64_t path0 = v / TF;          // first path of this round (uniform)
+        const int tf0 = (int)(v - path0 * TF);
         if (tid < kMtN / 2) {
             const int64_t vv = v + tid;
             if (vv < v1) {
@@ -209,16 +232,33 @@ __global__ void __launch_bounds__(kRngThreads, 2) mt_generate_kernel(const RngPa
                 if (prm.mode == 0) {
                     static_cast<double*>(prm.out)[vv] = u;
                 } else {
-                    const int64_t path = vv / TF;
-                    const int tf = (int)(vv - path * TF);
-                    const int t = tf / F;
-                    const size_t o = (size_t)tf * (size_t)P + (size_t)path;
-                    if (prm.mode == 1) {
-                        static_cast<double*>(prm.out)[o] = icdf_wichura(u) * __ldg(prm.sqrt_dt + t);
+                    const double q = u - 0.5;
+                    if (fabs(q) <= 0.425) {
+                        const int loc = tf0 + tid;
+                        const int tf = loc % TF;
+                        const size_t o = (size_t)tf * (size_t)P + (size_t)(path0 + loc / TF);
+                        const double sq = __ldg(prm.sqrt_dt + tf / F);
+                        if (prm.mode == 1) static_cast<double*>(prm.out)[o] = icdf_central(q) * sq;
+                        else static_cast<float*>(prm.out)[o] = icdf_wichura_f32(u) * (float)sq;
                     } else {
-                        static_cast<float*>(prm.out)[o] = icdf_wichura_f32(u) * (float)__ldg(prm.sqrt_dt + t);
+                        const int slot = atomicAdd(&tail_n, 1);
+                        tail_u[slot] = u;
+                        tail_i[slot] = (short)tid;
                     }
                 }
+            }
+        }
+        if (prm.mode != 0) {
+            __syncthreads();
+            const int n_tail = tail_n;
+            for (int k = tid; k < n_tail; k += kRngThreads) {
+                const double u = tail_u[k];
+                const int loc = tf0 + tail_i[k];
+                const int tf = loc % TF;
+                const size_t o = (size_t)tf * (size_t)P + (size_t)(path0 + loc / TF);
+                const double sq = __ldg(prm.sqrt_dt + tf / F);
+                if (prm.mode == 1) static_cast<double*>(prm.out)[o] = icdf_wichura(u) * sq;
+                else static_cast<float*>(prm.out)[o] = icdf_wichura_f32(u) * (float)sq;
             }
         }
         uint32_t* tmp = cur;
