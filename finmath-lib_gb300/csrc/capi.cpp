@@ -201,6 +201,15 @@ struct lmm_process {
     int *d_period_index = nullptr, *d_ex_period = nullptr;
     BermudanPeriod* d_per = nullptr;
     int berm_capacity = 0;   // exercise dates the basis / Gram buffers hold
+    // adjoint
+    std::vector<double> h_loadings, h_variance, h_vol;
+    int ckpt_stride = 0, want_ckpt = 0;
+    void* d_ckpt = nullptr;
+    void *d_adj_lam = nullptr, *d_adj_f = nullptr, *d_adj_sigma = nullptr, *d_adj_var_half = nullptr,
+         *d_adj_inv_delta = nullptr, *d_adj_dt = nullptr;
+    double *d_abar = nullptr, *d_abar_partials = nullptr, *d_seeds = nullptr, *d_value_partials = nullptr,
+           *d_value_out = nullptr, *d_vega_partials = nullptr, *d_delta_partials = nullptr, *d_vegas = nullptr,
+           *d_deltas = nullptr;
 };
 
 extern "C" {
@@ -396,6 +405,9 @@ int lmm_process_create(const lmm_model_desc* m, lmm_brownian* bm, lmm_process** 
     pr->tenor.assign(m->tenor, m->tenor + N + 1);
     pr->has_discount = m->discount_chain != nullptr;
     if (pr->has_discount) pr->discount.assign(m->discount_chain, m->discount_chain + N + 1);
+    pr->h_loadings.assign(m->factor_loadings, m->factor_loadings + (size_t)T * N * F);
+    pr->h_variance.assign(m->variance, m->variance + (size_t)T * N);
+    if (m->volatility) pr->h_vol.assign(m->volatility, m->volatility + (size_t)T * N);
     pr->stream = bm->stream;
     // first alive component m(t_i)+1 (LIBORMarketModelFromCovarianceModel.getDrift :1127-1130)
     pr->first.resize(T);
@@ -480,7 +492,9 @@ int lmm_process_set_observed_times(lmm_process* pr, const uint8_t* mask)
 
 static int process_ensure(lmm_process* pr)
 {
-    if (pr->simulated && pr->bm->generated && pr->bm_generation == pr->bm->generation) return LMM_OK;
+    if (pr->simulated && pr->bm->generated && pr->bm_generation == pr->bm->generation &&
+        pr->ckpt_stride == pr->want_ckpt)
+        return LMM_OK;
     int rc = brownian_ensure(pr->bm);
     if (rc) return rc;
     cudaStream_t s = pr->stream;
@@ -515,6 +529,19 @@ static int process_ensure(lmm_process* pr)
     a.d_numeraire = pr->d_numeraire;
     a.d_inv_num_partials = pr->d_partials;
     a.num_det_prefix = pr->num_det_prefix;
+    a.d_ckpt = nullptr;
+    a.ckpt_stride = 0;
+    if (pr->want_ckpt > 0) {
+        if (pr->ckpt_stride != pr->want_ckpt) {
+            dfree(pr->d_ckpt, s);
+            const size_t slots = (size_t)(pr->T / pr->want_ckpt + 1);
+            const size_t esz = pr->precision == LMM_PRECISION_FP64 ? sizeof(double) : sizeof(float);
+            rc = dalloc((unsigned char**)&pr->d_ckpt, slots * pr->N * (size_t)pr->P * esz, s);
+            if (rc) return rc;
+        }
+        a.d_ckpt = pr->d_ckpt;
+        a.ckpt_stride = pr->want_ckpt;
+    }
     int blocks = 0;
     rc = pr->precision == LMM_PRECISION_FP64 ? launch_paths_fp64(a, s, &blocks)
                                               : launch_paths_fp32(a, pr->d_lam32, pr->d_var32, s, &blocks);
@@ -523,6 +550,7 @@ static int process_ensure(lmm_process* pr)
     if (rc) return rc;
     pr->simulated = true;
     pr->bm_generation = pr->bm->generation;
+    pr->ckpt_stride = pr->want_ckpt;
     return LMM_OK;
 }
 
@@ -603,6 +631,14 @@ int lmm_process_destroy(lmm_process* pr)
     dfree(pr->d_rhs, s);
     dfree(pr->d_ex_period, s);
     dfree(pr->d_per, s);
+    dfree(pr->d_ckpt, s);
+    void* adj_tables[] = {pr->d_adj_lam, pr->d_adj_f, pr->d_adj_sigma, pr->d_adj_var_half, pr->d_adj_inv_delta, pr->d_adj_dt};
+    for (void* q : adj_tables)
+        if (q) cudaFreeAsync(q, s);
+    double* adj_bufs[] = {pr->d_abar, pr->d_abar_partials, pr->d_seeds, pr->d_value_partials, pr->d_value_out,
+                          pr->d_vega_partials, pr->d_delta_partials, pr->d_vegas, pr->d_deltas};
+    for (double* q : adj_bufs)
+        if (q) cudaFreeAsync(q, s);
     cudaStreamSynchronize(s);
     delete pr;
     return LMM_OK;
@@ -695,7 +731,8 @@ int lmm_swaption_get_value(lmm_process* pr, const lmm_swaption_desc* d, double* 
     return reduce_mean_stderr(pr->d_values, pr->P, pr->d_reduce, pr->reduce_bytes, value, error, pr->stream);
 }
 
-int lmm_bermudan_get_value(lmm_process* pr, const lmm_bermudan_desc* d, double* value, double* error, double* values_host)
+static int bermudan_run(lmm_process* pr, const lmm_bermudan_desc* d, double* value, double* error, double* values_host,
+                        BermudanLaunch* launch_out)
 {
     if (!pr || !d || !value) return fail(LMM_ERR_INVALID, "null argument");
     const int n = d->num_periods;
@@ -811,6 +848,144 @@ int lmm_bermudan_get_value(lmm_process* pr, const lmm_bermudan_desc* d, double* 
         LMM_CUDA(cudaMemcpyAsync(values_host, pr->d_values, sizeof(double) * pr->P, cudaMemcpyDeviceToHost, s));
         LMM_CUDA(cudaStreamSynchronize(s));
     }
+    if (launch_out) *launch_out = a;
+    return LMM_OK;
+}
+
+int lmm_bermudan_get_value(lmm_process* pr, const lmm_bermudan_desc* d, double* value, double* error, double* values_host)
+{
+    return bermudan_run(pr, d, value, error, values_host, nullptr);
+}
+
+}  // extern "C"
+
+template <typename R>
+static int upload_as(void** d, const std::vector<double>& h, cudaStream_t s)
+{
+    std::vector<R> t(h.begin(), h.end());
+    R* p = nullptr;
+    int rc = upload(&p, t.data(), t.size(), s);
+    *d = p;
+    return rc;
+}
+
+static int adjoint_tables(lmm_process* pr)
+{
+    if (pr->d_adj_f) return LMM_OK;
+    const int T = pr->T, N = pr->N, F = pr->F;
+    std::vector<double> sigma((size_t)T * N), f((size_t)T * N * F, 0.0), vh((size_t)T * N), invd(N), dt(T);
+    for (size_t q = 0; q < sigma.size(); q++) {
+        sigma[q] = pr->h_vol.empty() ? std::sqrt(pr->h_variance[q]) : pr->h_vol[q];
+        vh[q] = pr->h_variance[q] * -0.5;
+    }
+    for (int i = 0; i < T; i++)
+        for (int j = 0; j < N; j++) {
+            const double sg = sigma[(size_t)i * N + j];
+            for (int k = 0; k < F; k++)
+                f[((size_t)i * N + j) * F + k] = sg != 0.0 ? pr->h_loadings[((size_t)i * N + j) * F + k] / sg : 0.0;
+        }
+    for (int j = 0; j < N; j++) invd[j] = 1.0 / (pr->tenor[j + 1] - pr->tenor[j]);
+    for (int i = 0; i < T; i++) dt[i] = pr->times[i + 1] - pr->times[i];
+    cudaStream_t s = pr->stream;
+    int rc = LMM_OK;
+    if (pr->precision == LMM_PRECISION_MIXED) {
+        if (!rc) rc = upload_as<float>(&pr->d_adj_lam, pr->h_loadings, s);
+        if (!rc) rc = upload_as<float>(&pr->d_adj_f, f, s);
+        if (!rc) rc = upload_as<float>(&pr->d_adj_sigma, sigma, s);
+        if (!rc) rc = upload_as<float>(&pr->d_adj_var_half, vh, s);
+        if (!rc) rc = upload_as<float>(&pr->d_adj_inv_delta, invd, s);
+        if (!rc) rc = upload_as<float>(&pr->d_adj_dt, dt, s);
+    } else {
+        if (!rc) rc = upload_as<double>(&pr->d_adj_lam, pr->h_loadings, s);
+        if (!rc) rc = upload_as<double>(&pr->d_adj_f, f, s);
+        if (!rc) rc = upload_as<double>(&pr->d_adj_sigma, sigma, s);
+        if (!rc) rc = upload_as<double>(&pr->d_adj_var_half, vh, s);
+        if (!rc) rc = upload_as<double>(&pr->d_adj_inv_delta, invd, s);
+        if (!rc) rc = upload_as<double>(&pr->d_adj_dt, dt, s);
+    }
+    if (!rc) LMM_CUDA(cudaStreamSynchronize(s));  // host staging vectors go out of scope
+    return rc;
+}
+
+extern "C" {
+
+int lmm_bermudan_get_gradient(lmm_process* pr, const lmm_bermudan_desc* d, int stride, int freeze, double* value,
+                              double* error, double* deltas, double* vegas)
+{
+    if (!pr || !d || !value || !deltas || !vegas) return fail(LMM_ERR_INVALID, "null argument");
+    if (stride < 1 || stride > 16) return fail(LMM_ERR_INVALID, "checkpoint stride must be in [1, 16]");
+    if (pr->N > 40 || pr->F > 10) return fail(LMM_ERR_INVALID, "the adjoint supports at most 40 forward rates and 10 factors");
+    if (pr->obs_slot[pr->T] < 0) return fail(LMM_ERR_STATE, "the adjoint needs the last simulation time observed");
+    pr->want_ckpt = stride;
+    BermudanLaunch bl;
+    int rc = bermudan_run(pr, d, value, error, nullptr, &bl);
+    if (rc) return rc;
+    if ((rc = adjoint_tables(pr))) return rc;
+    cudaStream_t s = pr->stream;
+    const int T = pr->T, N = pr->N, P = pr->P;
+    const int sb = (P + 255) / 256;
+    const int blocks = adjoint_blocks(P);
+    if (!pr->d_seeds) {
+        if (!rc) rc = dalloc(&pr->d_abar, (size_t)N + 1, s);
+        if (!rc) rc = dalloc(&pr->d_abar_partials, (size_t)sb * (N + 1), s);
+        if (!rc) rc = dalloc(&pr->d_seeds, (size_t)N * P, s);
+        if (!rc) rc = dalloc(&pr->d_value_partials, (size_t)sb, s);
+        if (!rc) rc = dalloc(&pr->d_value_out, (size_t)1, s);
+        if (!rc) rc = dalloc(&pr->d_vega_partials, (size_t)blocks * T * N, s);
+        if (!rc) rc = dalloc(&pr->d_delta_partials, (size_t)blocks * N, s);
+        if (!rc) rc = dalloc(&pr->d_vegas, (size_t)T * N, s);
+        if (!rc) rc = dalloc(&pr->d_deltas, (size_t)N, s);
+        if (rc) return rc;
+    }
+    LMM_CUDA(cudaMemsetAsync(pr->d_abar_partials, 0, sizeof(double) * (size_t)sb * (N + 1), s));
+    std::vector<double> delta(N);
+    for (int j = 0; j < N; j++) delta[j] = pr->tenor[j + 1] - pr->tenor[j];
+    AdjointLaunch L;
+    std::memset(&L, 0, sizeof(L));
+    L.T = T;
+    L.N = N;
+    L.F = pr->F;
+    L.P = P;
+    L.nper = bl.nper;
+    L.stride = stride;
+    L.ckpt_is_L = (pr->precision == LMM_PRECISION_FP64 && pr->scheme == LMM_SCHEME_EULER_FUNCTIONAL) ? 1 : 0;
+    L.callable = bl.callable;
+    L.freeze_adjustment = freeze ? 1 : 0;
+    L.fp32 = pr->precision == LMM_PRECISION_MIXED;
+    L.T_slot = pr->obs_slot[T];
+    L.blocks = blocks;
+    L.cap = pr->cap;
+    L.h_discount = pr->has_discount ? pr->discount.data() : nullptr;
+    L.h_num_det = pr->num_det.data();
+    L.h_delta = delta.data();
+    L.d_per = pr->d_per;
+    L.d_states = pr->d_states;
+    L.d_numeraire = pr->d_numeraire;
+    L.d_num_adj = pr->d_num_adj;
+    L.d_ex = pr->d_ex;
+    L.d_first = pr->d_first;
+    L.d_init = pr->d_init;
+    L.d_dw = pr->bm->d_dw;
+    L.d_ckpt = pr->d_ckpt;
+    L.d_lam = pr->d_adj_lam;
+    L.d_f = pr->d_adj_f;
+    L.d_sigma = pr->d_adj_sigma;
+    L.d_var_half = pr->d_adj_var_half;
+    L.d_inv_delta = pr->d_adj_inv_delta;
+    L.d_dt = pr->d_adj_dt;
+    L.d_abar = pr->d_abar;
+    L.d_abar_partials = pr->d_abar_partials;
+    L.d_seeds = pr->d_seeds;
+    L.d_value_partials = pr->d_value_partials;
+    L.d_value_out = pr->d_value_out;
+    L.d_vega_partials = pr->d_vega_partials;
+    L.d_delta_partials = pr->d_delta_partials;
+    L.d_vegas = pr->d_vegas;
+    L.d_deltas = pr->d_deltas;
+    if ((rc = launch_adjoint(L, s))) return rc;
+    LMM_CUDA(cudaMemcpyAsync(deltas, pr->d_deltas, sizeof(double) * N, cudaMemcpyDeviceToHost, s));
+    LMM_CUDA(cudaMemcpyAsync(vegas, pr->d_vegas, sizeof(double) * (size_t)T * N, cudaMemcpyDeviceToHost, s));
+    LMM_CUDA(cudaStreamSynchronize(s));
     return LMM_OK;
 }
 

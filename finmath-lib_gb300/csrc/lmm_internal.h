@@ -1,7 +1,9 @@
 // lmm_internal.h -- shared declarations of the GB300 LMM library (host + device).
 #pragma once
 
+#include <cmath>
 #include <cstddef>
+#include <cstring>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -103,6 +105,8 @@ struct PathLaunch {
     double* d_numeraire;       // [N+1][P] unadjusted spot numeraire
     double* d_inv_num_partials;// [blocks][N][2] double-double partial sums of 1/N(T_{l+1})
     int num_det_prefix;        // numeraire deterministic for l < num_det_prefix
+    void* d_ckpt;              // [T/stride+1][N][P] path state every ckpt_stride steps (nullptr: none)
+    int ckpt_stride;           // state = L (FP64 EULER_FUNCTIONAL) or log L (EULER, mixed)
 };
 int launch_paths_fp64(const PathLaunch& a, cudaStream_t s, int* blocks_out);
 int launch_paths_fp32(const PathLaunch& a, const float* lam32, const float* var32, cudaStream_t s, int* blocks_out);
@@ -176,6 +180,28 @@ struct BermudanScratch {
 };
 int bermudan_blocks(int P);
 int bermudan_gram_blocks(int P, int ne);
+
+struct AdjointLaunch {
+    int T, N, F, P, nper, stride, ckpt_is_L, callable, freeze_adjustment, fp32, T_slot, blocks;
+    double cap;
+    const double* h_discount;      // [N+1] or nullptr
+    const uint8_t* h_num_det;      // [N+1]
+    const double* h_delta;         // [N]
+    const BermudanPeriod* d_per;   // [nper]
+    const void* d_states;          // [nobs][N][P]
+    const double* d_numeraire;     // [N+1][P]
+    const double* d_num_adj;       // [N+1]
+    const double* d_ex;            // [P] exercise time of the forward valuation
+    const int* d_first;            // [T]
+    const double* d_init;          // [N]
+    const void* d_dw;              // [T][F][P]
+    const void* d_ckpt;            // [T/stride+1][N][P]
+    const void *d_lam, *d_f, *d_sigma, *d_var_half, *d_inv_delta, *d_dt;  // tables in the path precision
+    double *d_abar, *d_abar_partials, *d_seeds, *d_value_partials, *d_value_out;
+    double *d_vega_partials, *d_delta_partials, *d_vegas, *d_deltas;
+};
+int adjoint_blocks(int P);
+int launch_adjoint(const AdjointLaunch& a, cudaStream_t s);
 int launch_bermudan(const ProductView& v, const BermudanLaunch& a, const BermudanScratch& sc, cudaStream_t s,
                     int* launches);
 

@@ -48,6 +48,12 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp32_kernel(const PathLaun
             for (int j = 0; j < NMAX; j++)
                 if (j < N) states[((size_t)slot * N + j) * P + p] = L[j];
         }
+        if (a.d_ckpt && active) {
+            float* ck = static_cast<float*>(a.d_ckpt);
+#pragma unroll
+            for (int j = 0; j < NMAX; j++)
+                if (j < N) ck[(size_t)j * P + p] = Y[j];
+        }
     }
     for (int i = 0; i < a.T; i++) {
         const int first = __ldg(a.d_first + i);
@@ -87,6 +93,12 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp32_kernel(const PathLaun
 #pragma unroll
             for (int j = 0; j < NMAX; j++)
                 if (j < N) states[((size_t)slot * N + j) * P + p] = L[j];
+        }
+        if (a.d_ckpt && active && (i + 1) % a.ckpt_stride == 0) {
+            float* ck = static_cast<float*>(a.d_ckpt) + (size_t)((i + 1) / a.ckpt_stride) * N * P;
+#pragma unroll
+            for (int j = 0; j < NMAX; j++)
+                if (j < N) ck[(size_t)j * P + p] = Y[j];
         }
     }
     // FP64 spot numeraire from the frozen fixings (as paths_fp64.cu)

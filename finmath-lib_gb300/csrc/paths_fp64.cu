@@ -56,6 +56,12 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp64_kernel(const PathLaun
             for (int j = 0; j < NMAX; j++)
                 if (j < N) states[((size_t)slot * N + j) * P + p] = L[j];
         }
+        if (a.d_ckpt && active) {
+            double* ck = static_cast<double*>(a.d_ckpt);
+#pragma unroll
+            for (int j = 0; j < NMAX; j++)
+                if (j < N) ck[(size_t)j * P + p] = FUNCTIONAL ? L[j] : Y[FUNCTIONAL ? 0 : j];
+        }
     }
 
     for (int i = 0; i < a.T; i++) {
@@ -106,6 +112,12 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp64_kernel(const PathLaun
 #pragma unroll
             for (int j = 0; j < NMAX; j++)
                 if (j < N) states[((size_t)slot * N + j) * P + p] = L[j];
+        }
+        if (a.d_ckpt && active && (i + 1) % a.ckpt_stride == 0) {
+            double* ck = static_cast<double*>(a.d_ckpt) + (size_t)((i + 1) / a.ckpt_stride) * N * P;
+#pragma unroll
+            for (int j = 0; j < NMAX; j++)
+                if (j < N) ck[(size_t)j * P + p] = FUNCTIONAL ? L[j] : Y[FUNCTIONAL ? 0 : j];
         }
     }
 

@@ -33,7 +33,8 @@ class LmmModelDesc(ctypes.Structure):
     _fields_ = [("num_steps", ctypes.c_int), ("times", _D), ("num_periods", ctypes.c_int), ("tenor", _D),
                 ("num_factors", ctypes.c_int), ("factor_loadings", _D), ("variance", _D),
                 ("initial_forwards", _D), ("discount_chain", _D), ("libor_cap", ctypes.c_double),
-                ("scheme", ctypes.c_int), ("measure", ctypes.c_int), ("state_space", ctypes.c_int)]
+                ("scheme", ctypes.c_int), ("measure", ctypes.c_int), ("state_space", ctypes.c_int),
+                ("volatility", _D)]
 
 
 class LmmSwaptionDesc(ctypes.Structure):
@@ -76,6 +77,8 @@ SIGNATURES = {
     "lmm_process_destroy": (ctypes.c_int, [_VP]),
     "lmm_swaption_get_value": (ctypes.c_int, [_VP, ctypes.POINTER(LmmSwaptionDesc), _D, _D]),
     "lmm_bermudan_get_value": (ctypes.c_int, [_VP, ctypes.POINTER(LmmBermudanDesc), _D, _D, _D]),
+    "lmm_bermudan_get_gradient": (ctypes.c_int, [_VP, ctypes.POINTER(LmmBermudanDesc), ctypes.c_int, ctypes.c_int,
+                                                 _D, _D, _D, _D]),
     "lmm_values_mean_stderr_noalloc": (ctypes.c_int, [_VP, ctypes.c_int64, _VP, _D, _D]),
     "lmm_stats_enable_timing": (ctypes.c_int, [ctypes.c_int]),
     "lmm_stats_reset": (ctypes.c_int, []),

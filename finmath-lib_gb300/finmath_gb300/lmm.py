@@ -165,6 +165,7 @@ class LIBORCovarianceModelFromVolatilityAndCorrelation:
                                                _p(self.variance)), "LIBORCovarianceModelFromVolatilityAndCorrelation")
         self.timeDiscretization = timeDiscretization
         self.liborPeriodDiscretization = liborPeriodDiscretization
+        self.volatility = vol
 
     def getNumberOfFactors(self):
         return self.factorLoadings.shape[2]
@@ -297,8 +298,11 @@ class EulerSchemeFromProcessModel:
         k = self._keep
         T = len(k["times"]) - 1
         N = len(k["tenor"]) - 1
+        vol = getattr(cov, "volatility", None)
+        k["vol"] = None if vol is None else _f64(vol)
         desc = _lib.LmmModelDesc(T, _p(k["times"]), N, _p(k["tenor"]), cov.getNumberOfFactors(), _p(k["lam"]),
-                                 _p(k["var"]), _p(k["init"]), _p(k["chain"]), model.liborCap, int(self.scheme), 0, 0)
+                                 _p(k["var"]), _p(k["init"]), _p(k["chain"]), model.liborCap, int(self.scheme), 0, 0,
+                                 _p(k["vol"]))
         h = ctypes.c_void_p()
         check(self._L.lmm_process_create(ctypes.byref(desc), brownianMotion._h, ctypes.byref(h)), "EulerSchemeFromProcessModel")
         self._h = h
@@ -422,6 +426,27 @@ class BermudanSwaption:
 
     def getValue(self, model):
         return self.getValues(model)["value"]
+
+    def _desc(self):
+        return _lib.LmmBermudanDesc(len(self.fixingDates),
+                                    self.isPeriodStartDateExerciseDate.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)),
+                                    _p(self.fixingDates), _p(self.periodLengths), _p(self.paymentDates),
+                                    _p(self.periodNotionals), _p(self.swaprates), int(self.isCallable), self.basis)
+
+    def getGradient(self, model: LIBORMonteCarloSimulationFromLIBORModel, checkpointStride: int = 8,
+                    freezeNumeraireAdjustment: bool = False):
+        """Value, deltas d V / d L_j(0) and vegas d V / d sigma_{i,j} by the adjoint kernel
+        (the role of RandomVariableDifferentiable.getGradient with these leaves)."""
+        proc = model.process
+        T = len(proc._keep["times"]) - 1
+        N = len(proc._keep["tenor"]) - 1
+        d = self._desc()
+        v, e = ctypes.c_double(), ctypes.c_double()
+        deltas, vegas = np.empty(N), np.empty((T, N))
+        check(_lib.load().lmm_bermudan_get_gradient(proc._h, ctypes.byref(d), int(checkpointStride),
+                                                    int(freezeNumeraireAdjustment), ctypes.byref(v), ctypes.byref(e),
+                                                    _p(deltas), _p(vegas)), "BermudanSwaption.getGradient")
+        return {"value": v.value, "error": e.value, "deltas": deltas, "vegas": vegas}
 
 
 # --------------------------------------------------------------------------- instrumentation

@@ -137,6 +137,8 @@ typedef struct {
     int scheme;                     /* LMM_SCHEME_* */
     int measure;                    /* 0 = SPOT (the only measure of this path) */
     int state_space;                /* 0 = LOGNORMAL (the only state space of this path) */
+    const double* volatility;       /* [T][N] sigma_{i,j}, optional: the leaves of the vegas
+                                       (NULL: sqrt(variance), i.e. rho_jj = 1) */
 } lmm_model_desc;
 
 typedef struct lmm_process lmm_process;
@@ -210,6 +212,22 @@ int lmm_bermudan_get_value(lmm_process* proc, const lmm_bermudan_desc* product, 
  * stream order.  The call waits for the two results and writes them to host memory. */
 int lmm_values_mean_stderr_noalloc(const double* d_values, int64_t num_values, void* stream, double* out_mean,
                                    double* out_error);
+
+/* BermudanSwaption value and its gradient, as RandomVariableDifferentiable.getGradient()
+ * (montecarlo/automaticdifferentiation/RandomVariableDifferentiable.java:56-75) gives it for
+ * the initial forwards and the volatility-matrix entries as leaves
+ * (LIBORMarketModelNormalAADSensitivitiesTest.java:343-355, 431-434).  A hand-written adjoint
+ * of the Euler-log step replays each path backward from checkpoints written every
+ * checkpoint_stride steps (1..16); exercise decisions are frozen from the forward
+ * valuation.  freeze_numeraire_adjustment = 1 treats the numeraire adjustment's path
+ * average as a constant, as the reference's AAD does (RandomVariableDifferentiableAAD
+ * getAverage returns a double); 0 differentiates through it (the derivative that central
+ * finite differences of the value measure).
+ * out_deltas[N] = d value / d initial forward j; out_vegas[T][N] = d value / d sigma_{i,j}
+ * (zero where sigma_{i,j} does not enter: t_i >= T_j). */
+int lmm_bermudan_get_gradient(lmm_process* proc, const lmm_bermudan_desc* product, int checkpoint_stride,
+                              int freeze_numeraire_adjustment, double* out_value, double* out_error,
+                              double* out_deltas, double* out_vegas);
 
 /* ---------------------------------------------------------------- instrumentation */
 /* Per-kernel launch counts and (when enabled) CUDA-event times of this library's kernels. */

@@ -927,3 +927,30 @@ done:
     for (int i = 0; i < MAXB; i++) free(b[i]);
     return rc;
 }
+
+/* Value of the Bermudan with the exercise time of every path given (decisions frozen):
+ * the mean over paths of the realised, numeraire-discounted cash flows.  Central finite
+ * differences of this function with common random numbers are the exact pathwise
+ * derivative with frozen exercise decisions -- the quantity an adjoint computes. */
+int orc_bermudan_frozen(const orc_sim* s, int nper, const double* fixing, const double* period_length,
+                        const double* payment, const double* notional, const double* strike, int callable,
+                        const double* exercise_time, double* value)
+{
+    const int P = s->P;
+    double* x = (double*)calloc((size_t)P, sizeof(double));
+    double* num = (double*)malloc(sizeof(double) * (size_t)P);
+    int rc = 0;
+    for (int per = 0; per < nper; per++) {
+        const double fix = fixing[per];
+        const double* L = sim_forward(s, fix, fix, fix + period_length[per]);
+        if (!L || orc_sim_numeraire(s, payment[per], num) < 0) { rc = -1; break; }
+        for (int p = 0; p < P; p++) {
+            const int paid = callable ? (fix >= exercise_time[p]) : (fix < exercise_time[p]);
+            if (paid) x[p] += ((L[p] - strike[per]) * period_length[per]) * notional[per] / num[p];
+        }
+    }
+    if (!rc) *value = orc_kahan_average(x, P);
+    free(x);
+    free(num);
+    return rc;
+}

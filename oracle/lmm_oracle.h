@@ -125,6 +125,12 @@ int orc_bermudan(const orc_sim* s, int nper, const uint8_t* exercisable, const d
                  double* value, double* stderr_out, double* per_path /* or NULL */,
                  double* exercise_time /* or NULL */);
 
+/* Bermudan value with frozen per-path exercise times (for finite differences of the
+ * pathwise derivative). */
+int orc_bermudan_frozen(const orc_sim* s, int nper, const double* fixing, const double* period_length,
+                        const double* payment, const double* notional, const double* strike, int callable,
+                        const double* exercise_time, double* value);
+
 #ifdef __cplusplus
 }
 #endif

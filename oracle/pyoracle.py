@@ -86,6 +86,7 @@ def lib():
                                    ctypes.c_double, _D, _D, _D]
         L.orc_bermudan.argtypes = [ctypes.c_void_p, ctypes.c_int, _U8, _D, _D, _D, _D, _D, ctypes.c_int,
                                    ctypes.c_int, _D, _D, _D, _D]
+        L.orc_bermudan_frozen.argtypes = [ctypes.c_void_p, ctypes.c_int, _D, _D, _D, _D, _D, ctypes.c_int, _D, _D]
         _lib = L
     return _lib
 
@@ -279,6 +280,23 @@ class Simulation:
         if rc != 0:
             raise ValueError(f"bermudan failed rc={rc}")
         return (v.value, e.value, pp, et) if per_path else (v.value, e.value)
+
+
+def _bermudan_frozen(self, fixing, period_length, payment, strike, exercise_time, notional=None, callable_=True):
+    fixing, period_length, payment = f64(fixing), f64(period_length), f64(payment)
+    n = len(fixing)
+    strike = f64(np.broadcast_to(strike, (n,)))
+    notional = f64(np.ones(n) if notional is None else np.broadcast_to(notional, (n,)))
+    ex = f64(exercise_time)
+    v = ctypes.c_double()
+    rc = lib().orc_bermudan_frozen(self._h, n, _p(fixing), _p(period_length), _p(payment), _p(notional), _p(strike),
+                                   int(callable_), _p(ex), ctypes.byref(v))
+    if rc != 0:
+        raise ValueError(f"frozen bermudan failed rc={rc}")
+    return v.value
+
+
+Simulation.bermudan_frozen = _bermudan_frozen
 
 
 def kahan_average(x) -> float:
