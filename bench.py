@@ -282,7 +282,11 @@ def run_ours(args):
             "kernels_ms": {k: v[1] / max(args.steps, 1) for k, v in stats.items() if v[0]}}
 
     if rank == 0 and args.precision == "fp64" and not args.no_forms:
-        line["forms"] = {"mixed": mixed_form(args, F, W, cfg, P, T, berm, swpt, res)}
+        line["forms"] = {"mixed": mixed_form(args, F, W, cfg, P, T, berm, swpt, res),
+                         "greeks": greeks_form(args, F, W, cfg, P, T, berm,
+                                               ms - stats["mt19937_jump_generate"][1] / max(args.steps, 1))}
+        if not args.no_portfolio:
+            line["forms"]["portfolio"] = portfolio_form(args, F, W, cfg, P)
     if rank == 0 and not args.no_cpu_baseline:
         v, dt, _, _ = cpu_baseline(args.cpu_paths, os.cpu_count() or 1)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
@@ -321,6 +325,83 @@ def mixed_form(args, F, W, cfg, P, T, berm, swpt, res64):
     return out
 
 
+def greeks_form(args, F, W, cfg, P, T, berm, fp64_valuation_ms):
+    """Differentiation form: Bermudan value + 40 deltas + every vega by the checkpointed adjoint,
+    from scratch (increments regenerated), mixed precision and FP64, against FP64 bump-and-revalue."""
+    import torch
+    out = {}
+    grads = {}
+    for name, prec in (("mixed", F.PRECISION_MIXED), ("fp64", F.PRECISION_FP64)):
+        sim = W.build(cfg, paths=P, precision=prec)
+        bm = sim.process.brownianMotion
+        g = berm.getGradient(sim, checkpointStride=8)
+        reps = max(1, min(args.steps, 3))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            bm.setSeed(cfg["seed"])
+            g = berm.getGradient(sim, checkpointStride=8)
+        torch.cuda.synchronize()
+        ms = 1e3 * (time.perf_counter() - t0) / reps
+        grads[name] = g
+        out[name] = {"ms_price_and_greeks": ms, "value": g["value"], "error": g["error"],
+                     "num_deltas": int(g["deltas"].size), "num_vegas": int(np.count_nonzero(g["vegas"]))}
+        sim.process.close()
+        bm.close()
+    g32, g64 = grads["mixed"], grads["fp64"]
+    nv = int(np.count_nonzero(g64["vegas"]))
+    # central differences of every delta and vega with common random numbers: 2 revaluations each,
+    # the Brownian increments reused (the measured FP64 valuation minus increment generation)
+    reval_ms = fp64_valuation_ms
+    bump_ms = (2 * (g64["deltas"].size + nv) + 1) * reval_ms
+    out["fp64_bump_and_revalue_ms_estimate"] = bump_ms
+    out["speedup_mixed_adjoint_vs_fp64_bump_and_revalue"] = bump_ms / out["mixed"]["ms_price_and_greeks"]
+    out["mixed_vs_fp64"] = {
+        "value_bp": 1e4 * (g32["value"] - g64["value"]),
+        "max_abs_delta_diff_bp_per_bp": float(np.max(np.abs(g32["deltas"] - g64["deltas"]))),
+        "max_abs_vega_diff_bp_per_vol_pt": float(1e4 * 1e-2 * np.max(np.abs(g32["vegas"] - g64["vegas"]))),
+        "max_rel_delta_diff": float(np.max(np.abs(g32["deltas"] - g64["deltas"])) / np.max(np.abs(g64["deltas"]))),
+        "max_rel_vega_diff": float(np.max(np.abs(g32["vegas"] - g64["vegas"])) / np.max(np.abs(g64["vegas"]))),
+    }
+    out["note"] = ("bump-and-revalue estimate = (2 x (deltas + nonzero vegas) + 1) x the measured FP64 valuation; "
+                   "delta differences are price bp per 1 bp of forward, vega differences price bp per 1 vol point")
+    return out
+
+
+def portfolio_form(args, F, W, cfg, P):
+    """Batching form: 256 Bermudan swaptions (seeded schedules, strikes, payer/receiver) with
+    values, deltas and vegas on the shared 2^20-path mixed-precision simulation, one graph
+    launch; knobs from the autotuner (cached per GPU and problem shape)."""
+    import torch
+    prods = W.portfolio_products(cfg, n=256, seed=20261203)
+    sim = W.build(cfg, paths=P, precision=F.PRECISION_MIXED)
+    name = torch.cuda.get_device_name()
+    T = int(round(cfg["T_end"] / cfg["dt"]))
+    key = F.autotune.key(name, P, T, 40, cfg["F"], F.PRECISION_MIXED)
+    t0 = time.perf_counter()
+    knobs = F.autotune.tune(sim, prods, key, subset=16)
+    tune_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    pf = F.Portfolio(sim, prods, True, knobs["checkpointStride"], knobs["concurrency"], knobs["adjointThreads"],
+                     knobs["gramBlocks"])
+    create_s = time.perf_counter() - t0
+    pf.run()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    out = pf.run()
+    wall_ms = 1e3 * (time.perf_counter() - t0)
+    lat = np.sort(out["latency_ms"])
+    res = {"products": len(prods), "paths": P, "precision": "mixed", "knobs": knobs,
+           "device_ms": out["total_ms"], "wall_ms": wall_ms, "latency_p50_ms": float(np.percentile(lat, 50)),
+           "latency_p99_ms": float(np.percentile(lat, 99)), "per_product_ms": out["total_ms"] / len(prods),
+           "greeks_per_product": 40 + 1560, "graph_record_s": create_s, "autotune_s": tune_s,
+           "value_sum": float(np.sum(out["values"]))}
+    pf.close()
+    sim.process.close()
+    sim.process.brownianMotion.close()
+    return res
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -329,12 +410,15 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--paths", type=int, default=1 << 20)
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
-    ap.add_argument("--cpu-paths", type=int, default=32768)
+    ap.add_argument("--cpu-paths", type=int, default=0, help="CPU sample paths (default 2^19 for the baseline leg, 2^18 per reference step)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true")
+    ap.add_argument("--no-portfolio", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
+    if args.cpu_paths <= 0:
+        args.cpu_paths = (1 << 18) if args.impl == "reference" else (1 << 19)
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -29,7 +29,6 @@
 namespace lmm {
 namespace {
 
-constexpr int kAdjThreads = 128;
 constexpr int kMaxStride = 16;
 
 template <typename R>
@@ -59,6 +58,8 @@ struct AdjTables {
 
 struct AdjParams {
     int T, N, F, P, stride, ckpt_is_L;
+    int t_end;   // last time index the product reads (reverse sweep starts there)
+    int n_eff;   // components 0..n_eff-1 influence the product (spot drift of j uses l <= j only)
     int capped;
     double cap;
     const int* first;        // [T]
@@ -85,7 +86,7 @@ __device__ __forceinline__ void forward_step(const AdjParams& a, const AdjTables
     }
 #pragma unroll
     for (int j = 0; j < NMAX; j++) {
-        if (j >= N) continue;
+        if (j >= a.n_eff) continue;
         if (j < first) {
             Yn[j] = Y[j];
             continue;
@@ -107,19 +108,19 @@ __device__ __forceinline__ void forward_step(const AdjParams& a, const AdjTables
     }
 }
 
-template <typename R, int NMAX, int FMAX>
+template <typename R, int NMAX, int FMAX, int kAdjThreads>
 __global__ void __launch_bounds__(kAdjThreads) adjoint_kernel(const AdjParams a, const AdjTables<R> tb)
 {
     extern __shared__ double smem_adj[];
     double* acc = smem_adj;                                      // [T][N] block vega accumulator
-    R* wpart = reinterpret_cast<R*>(smem_adj + (size_t)a.T * a.N);  // [4 warps][NMAX]
-    const int N = a.N, F = a.F, T = a.T;
+    R* wpart = reinterpret_cast<R*>(smem_adj + (size_t)a.T * a.N);  // [warps][NMAX]
+    const int N = a.N, F = a.F, T = a.T, NE = a.n_eff, TE = a.t_end;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     for (int q = tid; q < T * N; q += kAdjThreads) acc[q] = 0.0;
     double dsum[NMAX];
 #pragma unroll
     for (int j = 0; j < NMAX; j++) dsum[j] = 0.0;
-    const int nseg = (T + a.stride - 1) / a.stride;
+    const int nseg = (TE + a.stride - 1) / a.stride;
     __syncthreads();
 
     for (int base = blockIdx.x * kAdjThreads; base < a.P; base += gridDim.x * kAdjThreads) {
@@ -128,12 +129,12 @@ __global__ void __launch_bounds__(kAdjThreads) adjoint_kernel(const AdjParams a,
         R Ybar[NMAX];
         R seg[kMaxStride + 1][NMAX];
         for (int s = nseg - 1; s >= 0; s--) {
-            const int n0 = s * a.stride, n1 = min(n0 + a.stride, T);
+            const int n0 = s * a.stride, n1 = min(n0 + a.stride, TE);
             // state at the checkpoint
 #pragma unroll
             for (int j = 0; j < NMAX; j++) {
                 R y = R(0);
-                if (j < N && active) {
+                if (j < NE && active) {
                     const size_t o = ((size_t)s * N + j) * a.P + p;
                     if (a.ckpt_is_L) y = (R)log(static_cast<const double*>(tb.ckpt)[o]);
                     else y = static_cast<const R*>(tb.ckpt)[o];
@@ -146,7 +147,7 @@ __global__ void __launch_bounds__(kAdjThreads) adjoint_kernel(const AdjParams a,
 #pragma unroll
                 for (int j = 0; j < NMAX; j++) {
                     R yb = R(0);
-                    if (j < N && active) {
+                    if (j < NE && active) {
                         const R y = seg[n1 - n0][j];
                         const R L = fexp<R>(y);
                         if (!(a.capped && L > (R)a.cap)) yb = (R)a.seeds[(size_t)j * a.P + p] * L;
@@ -175,7 +176,7 @@ __global__ void __launch_bounds__(kAdjThreads) adjoint_kernel(const AdjParams a,
                 for (int j = 0; j < NMAX; j++) {
                     os[j] = R(0);
                     Lv[j] = R(0);
-                    if (j < N && j >= first) {
+                    if (j < NE && j >= first) {
                         R L = fexp<R>(Y[j]);
                         const bool c = a.capped && L > (R)a.cap;
                         if (c) L = (R)a.cap;
@@ -192,7 +193,7 @@ __global__ void __launch_bounds__(kAdjThreads) adjoint_kernel(const AdjParams a,
                 for (int jj = NMAX - 1; jj >= 0; jj--) {
                     const int j = jj;
                     contrib[j] = R(0);
-                    if (j < N && j >= first) {
+                    if (j < NE && j >= first) {
                         const R yb = Ybar[j];
                         const R mub = yb * dt;
                         R osb = R(0), sg = R(0);
@@ -219,7 +220,7 @@ __global__ void __launch_bounds__(kAdjThreads) adjoint_kernel(const AdjParams a,
                 // block-sum the vega contributions of step i (deterministic order)
 #pragma unroll
                 for (int j = 0; j < NMAX; j++) {
-                    if (j < N && j >= first) {
+                    if (j < NE && j >= first) {
                         R v = active ? contrib[j] : R(0);
 #pragma unroll
                         for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
@@ -227,7 +228,7 @@ __global__ void __launch_bounds__(kAdjThreads) adjoint_kernel(const AdjParams a,
                     }
                 }
                 __syncthreads();
-                if (tid < N && tid >= first) {
+                if (tid < NE && tid >= first) {
                     double t = 0.0;
                     for (int w = 0; w < kAdjThreads / 32; w++) t += (double)wpart[w * NMAX + tid];
                     acc[(size_t)i * N + tid] += t;
@@ -238,7 +239,7 @@ __global__ void __launch_bounds__(kAdjThreads) adjoint_kernel(const AdjParams a,
         // deltas: Y_0 = log(L_0(0)) -> d value / d L_0 = Ybar / L_0
 #pragma unroll
         for (int j = 0; j < NMAX; j++)
-            if (j < N && active) dsum[j] += (double)Ybar[j] / a.init[j];
+            if (j < NE && active) dsum[j] += (double)Ybar[j] / a.init[j];
     }
     // write block partials
     for (int q = tid; q < T * N; q += kAdjThreads) a.vega_partials[(size_t)blockIdx.x * T * N + q] = acc[q];
@@ -359,33 +360,46 @@ __global__ void __launch_bounds__(256) column_sum_kernel(const double* in, int r
     }
 }
 
-template <typename R, int NMAX, int FMAX>
+template <typename R, int NMAX, int FMAX, int TH>
 int launch_adj(const AdjParams& a, const AdjTables<R>& tb, int blocks, cudaStream_t s)
 {
-    const size_t smem = (size_t)a.T * a.N * sizeof(double) + 4 * NMAX * sizeof(R);
+    const size_t smem = (size_t)a.T * a.N * sizeof(double) + (TH / 32) * NMAX * sizeof(R);
     if (smem > 200 * 1024) return fail(LMM_ERR_INVALID, "adjoint: time steps x forward rates too large");
-    LMM_CUDA(cudaFuncSetAttribute(adjoint_kernel<R, NMAX, FMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    adjoint_kernel<R, NMAX, FMAX><<<blocks, kAdjThreads, smem, s>>>(a, tb);
+    static bool attr_set = false;  // set once, before any stream capture
+    if (!attr_set) {
+        LMM_CUDA(cudaFuncSetAttribute(adjoint_kernel<R, NMAX, FMAX, TH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      200 * 1024));
+        attr_set = true;
+    }
+    adjoint_kernel<R, NMAX, FMAX, TH><<<blocks, TH, smem, s>>>(a, tb);
     LMM_CUDA(cudaGetLastError());
     return LMM_OK;
 }
 
-template <typename R>
-int launch_adj_dispatch(const AdjParams& a, const AdjTables<R>& tb, int blocks, cudaStream_t s)
+template <typename R, int NMAX, int FMAX>
+int launch_adj_threads(const AdjParams& a, const AdjTables<R>& tb, int threads, int blocks, cudaStream_t s)
 {
-    if (a.N <= 24 && a.F <= 4) return launch_adj<R, 24, 4>(a, tb, blocks, s);
-    if (a.N <= 40 && a.F <= 10) return launch_adj<R, 40, 10>(a, tb, blocks, s);
+    if (threads == 64) return launch_adj<R, NMAX, FMAX, 64>(a, tb, blocks, s);
+    if (threads == 256) return launch_adj<R, NMAX, FMAX, 256>(a, tb, blocks, s);
+    return launch_adj<R, NMAX, FMAX, 128>(a, tb, blocks, s);
+}
+
+template <typename R>
+int launch_adj_dispatch(const AdjParams& a, const AdjTables<R>& tb, int threads, int blocks, cudaStream_t s)
+{
+    if (a.N <= 24 && a.F <= 4) return launch_adj_threads<R, 24, 4>(a, tb, threads, blocks, s);
+    if (a.N <= 40 && a.F <= 10) return launch_adj_threads<R, 40, 10>(a, tb, threads, blocks, s);
     return fail(LMM_ERR_INVALID, "adjoint supports at most 40 forward rates and 10 factors");
 }
 
 }  // namespace
 
-int adjoint_blocks(int P)
+int adjoint_blocks(int P, int threads)
 {
     int dev = 0, sms = 152;
     if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int want = sms * 4;
-    const int need = (P + kAdjThreads - 1) / kAdjThreads;
+    const int want = sms * (512 / threads);
+    const int need = (P + threads - 1) / threads;
     return need < want ? need : want;
 }
 
@@ -439,6 +453,8 @@ int launch_adjoint(const AdjointLaunch& L, cudaStream_t s)
     ap.stride = L.stride;
     ap.ckpt_is_L = L.ckpt_is_L;
     ap.capped = !std::isinf(L.cap);
+    ap.t_end = L.t_end;
+    ap.n_eff = L.n_eff;
     ap.cap = L.cap;
     ap.first = L.d_first;
     ap.init = L.d_init;
@@ -453,12 +469,12 @@ int launch_adjoint(const AdjointLaunch& L, cudaStream_t s)
             AdjTables<float> tb{static_cast<const float*>(L.d_lam), static_cast<const float*>(L.d_f),
                                 static_cast<const float*>(L.d_sigma), static_cast<const float*>(L.d_var_half),
                                 static_cast<const float*>(L.d_inv_delta), static_cast<const float*>(L.d_dt), L.d_dw, L.d_ckpt};
-            rc = launch_adj_dispatch<float>(ap, tb, blocks, s);
+            rc = launch_adj_dispatch<float>(ap, tb, L.threads, blocks, s);
         } else {
             AdjTables<double> tb{static_cast<const double*>(L.d_lam), static_cast<const double*>(L.d_f),
                                  static_cast<const double*>(L.d_sigma), static_cast<const double*>(L.d_var_half),
                                  static_cast<const double*>(L.d_inv_delta), static_cast<const double*>(L.d_dt), L.d_dw, L.d_ckpt};
-            rc = launch_adj_dispatch<double>(ap, tb, blocks, s);
+            rc = launch_adj_dispatch<double>(ap, tb, L.threads, blocks, s);
         }
     }
     if (rc) return rc;

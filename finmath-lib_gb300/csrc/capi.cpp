@@ -4,6 +4,7 @@
 // Device memory comes from the stream-ordered allocator with the default pool's release
 // threshold raised, so repeated create/destroy cycles (one per valuation in a service)
 // reuse HBM instead of returning it to the driver.
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -731,23 +732,25 @@ int lmm_swaption_get_value(lmm_process* pr, const lmm_swaption_desc* d, double* 
     return reduce_mean_stderr(pr->d_values, pr->P, pr->d_reduce, pr->reduce_bytes, value, error, pr->stream);
 }
 
-static int bermudan_run(lmm_process* pr, const lmm_bermudan_desc* d, double* value, double* error, double* values_host,
-                        BermudanLaunch* launch_out)
+// Validate a BermudanSwaption description against the process and build its launch tables.
+static int build_bermudan(lmm_process* pr, const lmm_bermudan_desc* d, BermudanLaunch* out, std::vector<int>* out_pidx,
+                          std::vector<double>* out_plen)
 {
-    if (!pr || !d || !value) return fail(LMM_ERR_INVALID, "null argument");
+    if (!pr || !d) return fail(LMM_ERR_INVALID, "null argument");
     const int n = d->num_periods;
     if (n <= 0 || n > 64 || !d->is_exercise_date || !d->fixing_dates || !d->period_lengths || !d->payment_dates ||
         !d->notionals || !d->swaprates)
         return fail(LMM_ERR_INVALID, "Bermudan needs 1..64 periods and all per-period arrays");
     if (d->basis != LMM_BASIS_REFERENCE && d->basis != LMM_BASIS_SWAPRATE) return fail(LMM_ERR_INVALID, "unknown regression basis");
-    BermudanLaunch a;
+    BermudanLaunch& a = *out;
     a.nper = n;
     a.callable = d->is_callable ? 1 : 0;
     a.basis = d->basis;
     a.per.resize(n);
-    std::vector<int> pidx(n);
-    std::vector<double> plen(n), tdelta(pr->N);
-    for (int j = 0; j < pr->N; j++) tdelta[j] = pr->tenor[j + 1] - pr->tenor[j];
+    std::vector<int>& pidx = *out_pidx;
+    std::vector<double>& plen = *out_plen;
+    pidx.assign(n, 0);
+    plen.assign(n, 0.0);
     for (int q = 0; q < n; q++) {
         const double fix = d->fixing_dates[q];
         const int si = time_index(pr->tenor, fix), ei = time_index(pr->tenor, fix + d->period_lengths[q]);
@@ -793,6 +796,22 @@ static int bermudan_run(lmm_process* pr, const lmm_bermudan_desc* d, double* val
         c.swap_first = q;
         c.swap_last = n;
     }
+    return LMM_OK;
+}
+
+static int bermudan_run(lmm_process* pr, const lmm_bermudan_desc* d, double* value, double* error, double* values_host,
+                        BermudanLaunch* launch_out)
+{
+    if (!pr || !d || !value) return fail(LMM_ERR_INVALID, "null argument");
+    BermudanLaunch a;
+    std::vector<int> pidx;
+    std::vector<double> plen, tdelta(pr->N);
+    for (int j = 0; j < pr->N; j++) tdelta[j] = pr->tenor[j + 1] - pr->tenor[j];
+    {
+        const int rcb = build_bermudan(pr, d, &a, &pidx, &plen);
+        if (rcb) return rcb;
+    }
+    const int n = a.nper;
     int rc = process_ensure(pr);
     if (!rc) rc = ensure_values(pr);
     if (rc) return rc;
@@ -813,12 +832,13 @@ static int bermudan_run(lmm_process* pr, const lmm_bermudan_desc* d, double* val
         if (!rc) rc = dalloc(&pr->d_per, (size_t)64, s);
         if (rc) return rc;
     }
+    if (!pr->d_gram) {
+        // Gram partials: at most bermudan_blocks(P) + 64 blocks over all exercise dates
+        if ((rc = dalloc(&pr->d_gram, (size_t)(blocks + 64) * 20 * 2, s))) return rc;
+    }
     if (ne > pr->berm_capacity) {
         dfree(pr->d_basis, s);
-        dfree(pr->d_gram, s);
-        const int bx = bermudan_gram_blocks(pr->P, ne);
         if (!rc) rc = dalloc(&pr->d_basis, (size_t)ne * 5 * pr->P, s);
-        if (!rc) rc = dalloc(&pr->d_gram, (size_t)ne * bx * 20 * 2, s);
         if (rc) return rc;
         pr->berm_capacity = ne;
     }
@@ -924,7 +944,8 @@ int lmm_bermudan_get_gradient(lmm_process* pr, const lmm_bermudan_desc* d, int s
     cudaStream_t s = pr->stream;
     const int T = pr->T, N = pr->N, P = pr->P;
     const int sb = (P + 255) / 256;
-    const int blocks = adjoint_blocks(P);
+    const int threads = 128;
+    const int blocks = adjoint_blocks(P, threads);
     if (!pr->d_seeds) {
         if (!rc) rc = dalloc(&pr->d_abar, (size_t)N + 1, s);
         if (!rc) rc = dalloc(&pr->d_abar_partials, (size_t)sb * (N + 1), s);
@@ -954,6 +975,12 @@ int lmm_bermudan_get_gradient(lmm_process* pr, const lmm_bermudan_desc* d, int s
     L.fp32 = pr->precision == LMM_PRECISION_MIXED;
     L.T_slot = pr->obs_slot[T];
     L.blocks = blocks;
+    L.threads = threads;
+    // the product reads forwards up to its last period: reverse from that fixing over components <= it
+    int m_end = 0;
+    for (int q = 0; q < bl.nper; q++) m_end = std::max(m_end, bl.per[q].libor_index);
+    L.n_eff = m_end + 1;
+    L.t_end = std::max(1, pr->tenor_tidx[m_end]);
     L.cap = pr->cap;
     L.h_discount = pr->has_discount ? pr->discount.data() : nullptr;
     L.h_num_det = pr->num_det.data();
@@ -1017,5 +1044,358 @@ int lmm_stats_get(int max, const char** names, int64_t* launches, double* total_
     }
     return n;
 }
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ portfolio batch
+struct PortfolioBranch {
+    double *values = nullptr, *under = nullptr, *ex = nullptr, *basis = nullptr, *gram = nullptr, *svd = nullptr,
+           *rhs = nullptr, *beta = nullptr, *reduce = nullptr;
+    double *seeds = nullptr, *abar = nullptr, *abar_partials = nullptr, *value_partials = nullptr,
+           *value_out = nullptr, *vega_partials = nullptr, *delta_partials = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+};
+
+struct lmm_portfolio {
+    lmm_process* pr = nullptr;
+    int n = 0, greeks = 0, stride = 8, conc = 4, threads = 128, gram_blocks = 0;
+    std::vector<BermudanLaunch> launch;
+    std::vector<std::vector<int>> pidx;
+    std::vector<std::vector<double>> plen;
+    std::vector<size_t> per_off, ex_off, idx_off, len_off;   // offsets into the device tables
+    unsigned char* d_tables = nullptr;
+    double *d_tenor_delta = nullptr, *d_meanvar = nullptr, *d_vegas = nullptr, *d_deltas = nullptr;
+    unsigned long long* d_ts = nullptr;
+    std::vector<PortfolioBranch> br;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t fork = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int max_ne = 0;
+    const void* captured[5] = {};  // process buffers the graph reads (re-recorded if any moves)
+};
+
+static void portfolio_fingerprint(const lmm_portfolio* pf, const void* out[5])
+{
+    out[0] = pf->pr->d_states;
+    out[1] = pf->pr->d_numeraire;
+    out[2] = pf->pr->d_num_adj;
+    out[3] = pf->pr->d_ckpt;
+    out[4] = pf->pr->bm->d_dw;
+}
+
+static int portfolio_free(lmm_portfolio* pf)
+{
+    if (!pf) return LMM_OK;
+    cudaStream_t s = pf->stream ? pf->stream : pf->pr->stream;
+    if (pf->exec) cudaGraphExecDestroy(pf->exec);
+    if (pf->graph) cudaGraphDestroy(pf->graph);
+    for (auto& b : pf->br) {
+        double* bufs[] = {b.values, b.under, b.ex, b.basis, b.gram, b.svd, b.rhs, b.beta, b.reduce, b.seeds, b.abar,
+                          b.abar_partials, b.value_partials, b.value_out, b.vega_partials, b.delta_partials};
+        for (double* q : bufs)
+            if (q) cudaFreeAsync(q, s);
+        if (b.done) cudaEventDestroy(b.done);
+        if (b.stream) cudaStreamDestroy(b.stream);
+    }
+    double* bufs[] = {pf->d_tenor_delta, pf->d_meanvar, pf->d_vegas, pf->d_deltas};
+    for (double* q : bufs)
+        if (q) cudaFreeAsync(q, s);
+    if (pf->d_tables) cudaFreeAsync(pf->d_tables, s);
+    if (pf->d_ts) cudaFreeAsync(pf->d_ts, s);
+    cudaStreamSynchronize(s);
+    if (pf->fork) cudaEventDestroy(pf->fork);
+    if (pf->stream) cudaStreamDestroy(pf->stream);
+    delete pf;
+    return LMM_OK;
+}
+
+// enqueue one product's regression, backward induction, reduction and adjoint on a branch
+static int portfolio_enqueue(lmm_portfolio* pf, int q, PortfolioBranch& b)
+{
+    lmm_process* pr = pf->pr;
+    const BermudanLaunch& a = pf->launch[q];
+    cudaStream_t s = b.stream;
+    BermudanScratch sc;
+    sc.d_values = b.values;
+    sc.d_under = b.under;
+    sc.d_ex = b.ex;
+    sc.d_basis = b.basis;
+    sc.d_gram = b.gram;
+    sc.d_svd = b.svd;
+    sc.d_partials = b.rhs;
+    sc.d_beta = b.beta;
+    sc.d_per = reinterpret_cast<BermudanPeriod*>(pf->d_tables + pf->per_off[q]);
+    sc.d_ex_period = reinterpret_cast<int*>(pf->d_tables + pf->ex_off[q]);
+    sc.d_tenor_delta = pf->d_tenor_delta;
+    sc.d_period_index = reinterpret_cast<const int*>(pf->d_tables + pf->idx_off[q]);
+    sc.d_period_length = reinterpret_cast<const double*>(pf->d_tables + pf->len_off[q]);
+    sc.tables_on_device = 1;
+    sc.gram_blocks = pf->gram_blocks;
+    ProductView v = product_view(pr);
+    int rc = launch_bermudan(v, a, sc, s, nullptr);
+    if (!rc) rc = reduce_mean_var_device(b.values, pr->P, b.reduce, pf->d_meanvar + 2 * (size_t)q, s);
+    if (rc) return rc;
+    if (pf->greeks) {
+        const int T = pr->T, N = pr->N, P = pr->P;
+        const int sb = (P + 255) / 256;
+        LMM_CUDA(cudaMemsetAsync(b.abar_partials, 0, sizeof(double) * (size_t)sb * (N + 1), s));
+        std::vector<double> delta(N);
+        for (int j = 0; j < N; j++) delta[j] = pr->tenor[j + 1] - pr->tenor[j];
+        AdjointLaunch L;
+        std::memset(&L, 0, sizeof(L));
+        L.T = T;
+        L.N = N;
+        L.F = pr->F;
+        L.P = P;
+        L.nper = a.nper;
+        L.stride = pf->stride;
+        L.ckpt_is_L = (pr->precision == LMM_PRECISION_FP64 && pr->scheme == LMM_SCHEME_EULER_FUNCTIONAL) ? 1 : 0;
+        L.callable = a.callable;
+        L.fp32 = pr->precision == LMM_PRECISION_MIXED;
+        L.T_slot = pr->obs_slot[T];
+        L.threads = pf->threads;
+        L.blocks = adjoint_blocks(P, pf->threads);
+        int m_end = 0;
+        for (int k = 0; k < a.nper; k++) m_end = std::max(m_end, a.per[k].libor_index);
+        L.n_eff = m_end + 1;
+        L.t_end = std::max(1, pr->tenor_tidx[m_end]);
+        L.cap = pr->cap;
+        L.h_discount = pr->has_discount ? pr->discount.data() : nullptr;
+        L.h_num_det = pr->num_det.data();
+        L.h_delta = delta.data();
+        L.d_per = sc.d_per;
+        L.d_states = pr->d_states;
+        L.d_numeraire = pr->d_numeraire;
+        L.d_num_adj = pr->d_num_adj;
+        L.d_ex = b.ex;
+        L.d_first = pr->d_first;
+        L.d_init = pr->d_init;
+        L.d_dw = pr->bm->d_dw;
+        L.d_ckpt = pr->d_ckpt;
+        L.d_lam = pr->d_adj_lam;
+        L.d_f = pr->d_adj_f;
+        L.d_sigma = pr->d_adj_sigma;
+        L.d_var_half = pr->d_adj_var_half;
+        L.d_inv_delta = pr->d_adj_inv_delta;
+        L.d_dt = pr->d_adj_dt;
+        L.d_abar = b.abar;
+        L.d_abar_partials = b.abar_partials;
+        L.d_seeds = b.seeds;
+        L.d_value_partials = b.value_partials;
+        L.d_value_out = b.value_out;
+        L.d_vega_partials = b.vega_partials;
+        L.d_delta_partials = b.delta_partials;
+        L.d_vegas = pf->d_vegas + (size_t)q * T * N;
+        L.d_deltas = pf->d_deltas + (size_t)q * N;
+        if ((rc = launch_adjoint(L, s))) return rc;
+    }
+    return launch_timestamp(pf->d_ts + 1 + q, s);
+}
+
+static int portfolio_record(lmm_portfolio* pf)
+{
+    int rc = LMM_OK;
+    cudaError_t e;
+    cudaStream_t s = pf->stream;
+    if (pf->exec) {
+        cudaGraphExecDestroy(pf->exec);
+        pf->exec = nullptr;
+    }
+    if (pf->graph) {
+        cudaGraphDestroy(pf->graph);
+        pf->graph = nullptr;
+    }
+    // fork the branches off one stream, join them back
+    const bool timing = g_timing.exchange(false);
+    if (!rc) {
+        e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) rc = cuda_fail(e, "cudaStreamBeginCapture");
+    }
+    if (!rc) {
+        int rc2 = launch_timestamp(pf->d_ts, s);
+        if (!rc2 && cudaEventRecord(pf->fork, s) != cudaSuccess) rc2 = fail(LMM_ERR_CUDA, "fork");
+        for (auto& b : pf->br)
+            if (!rc2 && cudaStreamWaitEvent(b.stream, pf->fork, 0) != cudaSuccess) rc2 = fail(LMM_ERR_CUDA, "fork wait");
+        for (int q = 0; q < pf->n && !rc2; q++) rc2 = portfolio_enqueue(pf, q, pf->br[q % pf->conc]);
+        for (auto& b : pf->br) {
+            if (!rc2 && cudaEventRecord(b.done, b.stream) != cudaSuccess) rc2 = fail(LMM_ERR_CUDA, "join");
+            if (!rc2 && cudaStreamWaitEvent(s, b.done, 0) != cudaSuccess) rc2 = fail(LMM_ERR_CUDA, "join wait");
+        }
+        e = cudaStreamEndCapture(s, &pf->graph);
+        if (rc2) rc = rc2;
+        else if (e != cudaSuccess) rc = cuda_fail(e, "cudaStreamEndCapture");
+    }
+    g_timing.store(timing);
+    if (!rc) {
+        e = cudaGraphInstantiate(&pf->exec, pf->graph, 0);
+        if (e != cudaSuccess) rc = cuda_fail(e, "cudaGraphInstantiate");
+    }
+    if (!rc) portfolio_fingerprint(pf, pf->captured);
+    return rc;
+}
+
+extern "C" {
+
+int lmm_portfolio_create(lmm_process* pr, const lmm_portfolio_desc* desc, lmm_portfolio** out)
+{
+    if (!out) return fail(LMM_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    if (!pr || !desc || desc->num_products <= 0 || !desc->products) return fail(LMM_ERR_INVALID, "empty portfolio");
+    if (desc->with_greeks && (desc->checkpoint_stride < 1 || desc->checkpoint_stride > 16))
+        return fail(LMM_ERR_INVALID, "checkpoint stride must be in [1, 16]");
+    if (desc->concurrency < 1 || desc->concurrency > 16) return fail(LMM_ERR_INVALID, "concurrency must be in [1, 16]");
+    if (desc->adjoint_threads != 64 && desc->adjoint_threads != 128 && desc->adjoint_threads != 256)
+        return fail(LMM_ERR_INVALID, "adjoint threads must be 64, 128 or 256");
+    if (desc->with_greeks && (pr->N > 40 || pr->F > 10))
+        return fail(LMM_ERR_INVALID, "the adjoint supports at most 40 forward rates and 10 factors");
+    if (pr->obs_slot[pr->T] < 0) return fail(LMM_ERR_STATE, "the portfolio needs the last simulation time observed");
+    lmm_portfolio* pf = new lmm_portfolio();
+    pf->pr = pr;
+    pf->n = desc->num_products;
+    pf->greeks = desc->with_greeks ? 1 : 0;
+    pf->stride = desc->with_greeks ? desc->checkpoint_stride : 0;
+    pf->conc = std::min(desc->concurrency, pf->n);
+    pf->threads = desc->adjoint_threads;
+    pf->gram_blocks = desc->gram_blocks;
+    int rc = LMM_OK;
+    // ---- validate and lay out the product tables
+    pf->launch.resize(pf->n);
+    pf->pidx.resize(pf->n);
+    pf->plen.resize(pf->n);
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        size_t o = (off + 255) & ~(size_t)255;
+        off = o + bytes;
+        return o;
+    };
+    std::vector<std::vector<int>> ex_period(pf->n);
+    for (int q = 0; q < pf->n && !rc; q++) {
+        rc = build_bermudan(pr, &desc->products[q], &pf->launch[q], &pf->pidx[q], &pf->plen[q]);
+        if (rc) break;
+        for (int k = 0; k < pf->launch[q].nper; k++)
+            if (pf->launch[q].per[k].exercisable) ex_period[q].push_back(k);
+        pf->max_ne = std::max(pf->max_ne, (int)ex_period[q].size());
+        pf->per_off.push_back(take(sizeof(BermudanPeriod) * pf->launch[q].nper));
+        pf->ex_off.push_back(take(sizeof(int) * std::max<size_t>(1, ex_period[q].size())));
+        pf->idx_off.push_back(take(sizeof(int) * pf->launch[q].nper));
+        pf->len_off.push_back(take(sizeof(double) * pf->launch[q].nper));
+    }
+    if (rc) {
+        delete pf;
+        return rc;
+    }
+    // ---- simulate (with checkpoints for the adjoint) before recording the graph
+    if (pf->greeks) pr->want_ckpt = pf->stride;
+    rc = process_ensure(pr);
+    if (!rc && pf->greeks) rc = adjoint_tables(pr);
+    if (rc) {
+        delete pf;
+        return rc;
+    }
+    cudaError_t e = cudaStreamCreateWithFlags(&pf->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete pf;
+        return cuda_fail(e, "cudaStreamCreate");
+    }
+    cudaStream_t s = pf->stream;
+    const int T = pr->T, N = pr->N, P = pr->P;
+    std::vector<unsigned char> host(off);
+    for (int q = 0; q < pf->n; q++) {
+        std::memcpy(host.data() + pf->per_off[q], pf->launch[q].per.data(), sizeof(BermudanPeriod) * pf->launch[q].nper);
+        if (!ex_period[q].empty())
+            std::memcpy(host.data() + pf->ex_off[q], ex_period[q].data(), sizeof(int) * ex_period[q].size());
+        std::memcpy(host.data() + pf->idx_off[q], pf->pidx[q].data(), sizeof(int) * pf->launch[q].nper);
+        std::memcpy(host.data() + pf->len_off[q], pf->plen[q].data(), sizeof(double) * pf->launch[q].nper);
+    }
+    std::vector<double> tdelta(N);
+    for (int j = 0; j < N; j++) tdelta[j] = pr->tenor[j + 1] - pr->tenor[j];
+    if (!rc) rc = upload(&pf->d_tables, host.data(), host.size(), s);
+    if (!rc) rc = upload(&pf->d_tenor_delta, tdelta.data(), tdelta.size(), s);
+    if (!rc) rc = dalloc(&pf->d_meanvar, (size_t)2 * pf->n, s);
+    if (!rc) rc = dalloc(&pf->d_ts, (size_t)pf->n + 1, s);
+    if (!rc && pf->greeks) rc = dalloc(&pf->d_vegas, (size_t)pf->n * T * N, s);
+    if (!rc && pf->greeks) rc = dalloc(&pf->d_deltas, (size_t)pf->n * N, s);
+    // ---- per-branch scratch
+    const int blocks = bermudan_blocks(P);
+    const int sb = (P + 255) / 256;
+    const int ablocks = adjoint_blocks(P, pf->threads);
+    pf->br.resize(pf->conc);
+    for (auto& b : pf->br) {
+        if (!rc) rc = cudaStreamCreateWithFlags(&b.stream, cudaStreamNonBlocking) == cudaSuccess ? 0 : fail(LMM_ERR_CUDA, "stream");
+        if (!rc) rc = cudaEventCreateWithFlags(&b.done, cudaEventDisableTiming) == cudaSuccess ? 0 : fail(LMM_ERR_CUDA, "event");
+        if (!rc) rc = dalloc(&b.values, (size_t)P, s);
+        if (!rc) rc = dalloc(&b.under, (size_t)P, s);
+        if (!rc) rc = dalloc(&b.ex, (size_t)P, s);
+        if (!rc) rc = dalloc(&b.basis, (size_t)std::max(1, pf->max_ne) * 5 * P, s);
+        if (!rc) rc = dalloc(&b.gram, (size_t)(blocks + 64 + (pf->gram_blocks > 0 ? pf->gram_blocks * 64 : 0)) * 40, s);
+        if (!rc) rc = dalloc(&b.svd, (size_t)64 * 80, s);
+        if (!rc) rc = dalloc(&b.rhs, (size_t)blocks * 12, s);
+        if (!rc) rc = dalloc(&b.beta, (size_t)64 * 6, s);
+        if (!rc) rc = dalloc(&b.reduce, (size_t)2 * 1024 + 2, s);
+        if (pf->greeks) {
+            if (!rc) rc = dalloc(&b.seeds, (size_t)N * P, s);
+            if (!rc) rc = dalloc(&b.abar, (size_t)N + 1, s);
+            if (!rc) rc = dalloc(&b.abar_partials, (size_t)sb * (N + 1), s);
+            if (!rc) rc = dalloc(&b.value_partials, (size_t)sb, s);
+            if (!rc) rc = dalloc(&b.value_out, (size_t)1, s);
+            if (!rc) rc = dalloc(&b.vega_partials, (size_t)ablocks * T * N, s);
+            if (!rc) rc = dalloc(&b.delta_partials, (size_t)ablocks * N, s);
+        }
+    }
+    if (!rc) rc = cudaEventCreateWithFlags(&pf->fork, cudaEventDisableTiming) == cudaSuccess ? 0 : fail(LMM_ERR_CUDA, "event");
+    if (!rc) rc = cudaStreamSynchronize(s) == cudaSuccess ? 0 : fail(LMM_ERR_CUDA, "stream sync");
+    // one eager run first: sets kernel attributes and checks every launch outside the capture
+    for (int q = 0; q < pf->n && !rc; q++) rc = portfolio_enqueue(pf, q, pf->br[q % pf->conc]);
+    for (auto& b : pf->br)
+        if (!rc) rc = cudaStreamSynchronize(b.stream) == cudaSuccess ? 0 : fail(LMM_ERR_CUDA, "portfolio warm-up");
+    if (!rc) rc = portfolio_record(pf);
+    if (rc) {
+        portfolio_free(pf);
+        return rc;
+    }
+    *out = pf;
+    return LMM_OK;
+}
+
+int lmm_portfolio_run(lmm_portfolio* pf, double* values, double* errors, double* deltas, double* vegas, double* latency_ms,
+                      double* total_ms)
+{
+    if (!pf || !values) return fail(LMM_ERR_INVALID, "null argument");
+    lmm_process* pr = pf->pr;
+    // the simulation the graph reads must be current (same checkpoint stride, current increments)
+    if (pf->greeks) pr->want_ckpt = pf->stride;
+    const bool stale = !(pr->simulated && pr->bm->generated && pr->bm_generation == pr->bm->generation &&
+                         pr->ckpt_stride == pr->want_ckpt);
+    int rc = process_ensure(pr);
+    if (rc) return rc;
+    if (stale) LMM_CUDA(cudaStreamSynchronize(pr->stream));
+    const void* now[5];
+    portfolio_fingerprint(pf, now);
+    if (std::memcmp(now, pf->captured, sizeof(now)) != 0 && (rc = portfolio_record(pf))) return rc;
+    cudaStream_t s = pf->stream;
+    LMM_CUDA(cudaGraphLaunch(pf->exec, s));
+    const int n = pf->n, T = pr->T, N = pr->N, P = pr->P;
+    std::vector<double> mv(2 * (size_t)n);
+    std::vector<unsigned long long> ts(n + 1);
+    LMM_CUDA(cudaMemcpyAsync(mv.data(), pf->d_meanvar, sizeof(double) * mv.size(), cudaMemcpyDeviceToHost, s));
+    LMM_CUDA(cudaMemcpyAsync(ts.data(), pf->d_ts, sizeof(unsigned long long) * ts.size(), cudaMemcpyDeviceToHost, s));
+    if (pf->greeks && deltas) LMM_CUDA(cudaMemcpyAsync(deltas, pf->d_deltas, sizeof(double) * (size_t)n * N, cudaMemcpyDeviceToHost, s));
+    if (pf->greeks && vegas)
+        LMM_CUDA(cudaMemcpyAsync(vegas, pf->d_vegas, sizeof(double) * (size_t)n * T * N, cudaMemcpyDeviceToHost, s));
+    LMM_CUDA(cudaStreamSynchronize(s));
+    unsigned long long last = ts[0];
+    for (int q = 0; q < n; q++) {
+        values[q] = mv[2 * q];
+        if (errors) errors[q] = P > 1 ? std::sqrt(mv[2 * q + 1]) / std::sqrt((double)P) : 0.0;
+        if (latency_ms) latency_ms[q] = (double)(ts[1 + q] - ts[0]) * 1e-6;
+        last = std::max(last, ts[1 + q]);
+    }
+    if (total_ms) *total_ms = (double)(last - ts[0]) * 1e-6;
+    return LMM_OK;
+}
+
+int lmm_portfolio_destroy(lmm_portfolio* pf) { return portfolio_free(pf); }
 
 }  // extern "C"

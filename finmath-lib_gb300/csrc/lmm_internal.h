@@ -177,12 +177,18 @@ struct BermudanScratch {
     const double* d_tenor_delta;    // [N]
     const int* d_period_index;      // [nper]
     const double* d_period_length;  // [nper]
+    int tables_on_device = 0;       // d_per / d_ex_period already hold this product's tables
+    int gram_blocks = 0;            // Gram blocks per exercise date (0: automatic)
 };
+int reduce_mean_var_device(const double* d_values, int P, double* d_scratch, double* d_out2, cudaStream_t s);
+int launch_timestamp(unsigned long long* d_out, cudaStream_t s);
 int bermudan_blocks(int P);
 int bermudan_gram_blocks(int P, int ne);
 
 struct AdjointLaunch {
     int T, N, F, P, nper, stride, ckpt_is_L, callable, freeze_adjustment, fp32, T_slot, blocks;
+    int threads;        // adjoint threads per block (64, 128, 256)
+    int t_end, n_eff;   // reverse sweep from time index t_end over components 0..n_eff-1
     double cap;
     const double* h_discount;      // [N+1] or nullptr
     const uint8_t* h_num_det;      // [N+1]
@@ -200,7 +206,7 @@ struct AdjointLaunch {
     double *d_abar, *d_abar_partials, *d_seeds, *d_value_partials, *d_value_out;
     double *d_vega_partials, *d_delta_partials, *d_vegas, *d_deltas;
 };
-int adjoint_blocks(int P);
+int adjoint_blocks(int P, int threads);
 int launch_adjoint(const AdjointLaunch& a, cudaStream_t s);
 int launch_bermudan(const ProductView& v, const BermudanLaunch& a, const BermudanScratch& sc, cudaStream_t s,
                     int* launches);

@@ -522,6 +522,34 @@ int bermudan_gram_blocks(int P, int ne)
     return bx < 1 ? 1 : bx;
 }
 
+int reduce_mean_var_device(const double* d_values, int P, double* d_scratch, double* d_out2, cudaStream_t s)
+{
+    const int blocks = grid_for(P, 256, 1024);
+    KernelTimer kt(K_VALUE_REDUCE, s, 4);
+    sum_partials_kernel<<<blocks, 256, 0, s>>>(d_values, P, nullptr, d_scratch);
+    finish_partials_kernel<<<1, 256, 0, s>>>(d_scratch, blocks, P, d_out2);
+    sum_partials_kernel<<<blocks, 256, 0, s>>>(d_values, P, d_out2, d_scratch);
+    finish_partials_kernel<<<1, 256, 0, s>>>(d_scratch, blocks, P, d_out2 + 1);
+    LMM_CUDA(cudaGetLastError());
+    return LMM_OK;
+}
+
+namespace {
+__global__ void timestamp_kernel(unsigned long long* out)
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    *out = t;
+}
+}  // namespace
+
+int launch_timestamp(unsigned long long* d_out, cudaStream_t s)
+{
+    timestamp_kernel<<<1, 1, 0, s>>>(d_out);
+    LMM_CUDA(cudaGetLastError());
+    return LMM_OK;
+}
+
 int launch_bermudan(const ProductView& v, const BermudanLaunch& a, const BermudanScratch& sc, cudaStream_t s,
                     int* launches)
 {
@@ -533,8 +561,10 @@ int launch_bermudan(const ProductView& v, const BermudanLaunch& a, const Bermuda
             ex_period.push_back(q);
         }
     const int ne = (int)ex_period.size();
-    LMM_CUDA(cudaMemcpyAsync(sc.d_per, a.per.data(), sizeof(BermudanPeriod) * a.nper, cudaMemcpyHostToDevice, s));
-    if (ne) LMM_CUDA(cudaMemcpyAsync(sc.d_ex_period, ex_period.data(), sizeof(int) * ne, cudaMemcpyHostToDevice, s));
+    if (!sc.tables_on_device) {
+        LMM_CUDA(cudaMemcpyAsync(sc.d_per, a.per.data(), sizeof(BermudanPeriod) * a.nper, cudaMemcpyHostToDevice, s));
+        if (ne) LMM_CUDA(cudaMemcpyAsync(sc.d_ex_period, ex_period.data(), sizeof(int) * ne, cudaMemcpyHostToDevice, s));
+    }
     BermShared sh;
     std::memset(&sh, 0, sizeof(sh));
     sh.basis = a.basis;
@@ -551,7 +581,7 @@ int launch_bermudan(const ProductView& v, const BermudanLaunch& a, const Bermuda
     sh.period_length = sc.d_period_length;
     sh.basis_buf = sc.d_basis;
     if (ne > 0) {
-        const int bx = bermudan_gram_blocks(v.P, ne);
+        const int bx = sc.gram_blocks > 0 ? sc.gram_blocks : bermudan_gram_blocks(v.P, ne);
         {
             KernelTimer kt(K_BERMUDAN_STEP, s);
             const dim3 grid(bx, ne);

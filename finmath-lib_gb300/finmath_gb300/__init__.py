@@ -10,8 +10,8 @@ from .lmm import (TimeDiscretizationFromArray, ForwardCurveInterpolation, Discou
                   LIBORCorrelationModelExponentialDecay, LIBORVolatilityModelFourParameterExponentialForm,
                   LIBORVolatilityModelFromGivenMatrix, LIBORCovarianceModelFromVolatilityAndCorrelation,
                   LIBORMarketModelFromCovarianceModel, BrownianMotionFromMersenneRandomNumbers,
-                  EulerSchemeFromProcessModel, LIBORMonteCarloSimulationFromLIBORModel, Swaption, BermudanSwaption,
+                  EulerSchemeFromProcessModel, LIBORMonteCarloSimulationFromLIBORModel, Swaption, BermudanSwaption, Portfolio,
                   mersenne_twister_uniforms, kernel_stats)
-from . import workloads
+from . import workloads, autotune
 
 __all__ = [n for n in dir() if not n.startswith("_")]

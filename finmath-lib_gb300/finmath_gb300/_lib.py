@@ -48,6 +48,12 @@ class LmmBermudanDesc(ctypes.Structure):
                 ("is_callable", ctypes.c_int), ("basis", ctypes.c_int)]
 
 
+class LmmPortfolioDesc(ctypes.Structure):
+    _fields_ = [("num_products", ctypes.c_int), ("products", ctypes.c_void_p), ("with_greeks", ctypes.c_int),
+                ("checkpoint_stride", ctypes.c_int), ("concurrency", ctypes.c_int), ("adjoint_threads", ctypes.c_int),
+                ("gram_blocks", ctypes.c_int)]
+
+
 # name -> (restype, argtypes); every exported symbol of include/lmm_gb300.h
 SIGNATURES = {
     "lmm_last_error": (ctypes.c_char_p, []),
@@ -79,6 +85,9 @@ SIGNATURES = {
     "lmm_bermudan_get_value": (ctypes.c_int, [_VP, ctypes.POINTER(LmmBermudanDesc), _D, _D, _D]),
     "lmm_bermudan_get_gradient": (ctypes.c_int, [_VP, ctypes.POINTER(LmmBermudanDesc), ctypes.c_int, ctypes.c_int,
                                                  _D, _D, _D, _D]),
+    "lmm_portfolio_create": (ctypes.c_int, [_VP, ctypes.POINTER(LmmPortfolioDesc), ctypes.POINTER(_VP)]),
+    "lmm_portfolio_run": (ctypes.c_int, [_VP, _D, _D, _D, _D, _D, _D]),
+    "lmm_portfolio_destroy": (ctypes.c_int, [_VP]),
     "lmm_values_mean_stderr_noalloc": (ctypes.c_int, [_VP, ctypes.c_int64, _VP, _D, _D]),
     "lmm_stats_enable_timing": (ctypes.c_int, [ctypes.c_int]),
     "lmm_stats_reset": (ctypes.c_int, []),

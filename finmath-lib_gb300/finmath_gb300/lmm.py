@@ -449,6 +449,47 @@ class BermudanSwaption:
         return {"value": v.value, "error": e.value, "deltas": deltas, "vegas": vegas}
 
 
+class Portfolio:
+    """Bermudan swaptions valued together (with deltas and vegas) on one shared simulation:
+    the per-product kernels are recorded once into a CUDA graph; run() launches it."""
+
+    def __init__(self, model: LIBORMonteCarloSimulationFromLIBORModel, products, withGreeks=True, checkpointStride=8,
+                 concurrency=4, adjointThreads=128, gramBlocks=0):
+        self._L = _lib.load()
+        self.model = model
+        self.products = list(products)
+        self._descs = (_lib.LmmBermudanDesc * len(self.products))(*[b._desc() for b in self.products])
+        d = _lib.LmmPortfolioDesc(len(self.products), ctypes.cast(self._descs, ctypes.c_void_p), int(withGreeks),
+                                  int(checkpointStride), int(concurrency), int(adjointThreads), int(gramBlocks))
+        h = ctypes.c_void_p()
+        check(self._L.lmm_portfolio_create(model.process._h, ctypes.byref(d), ctypes.byref(h)), "Portfolio")
+        self._h = h
+        self.withGreeks = bool(withGreeks)
+        proc = model.process
+        self.T = len(proc._keep["times"]) - 1
+        self.N = len(proc._keep["tenor"]) - 1
+
+    def run(self):
+        n = len(self.products)
+        v, e, lat, tot = np.empty(n), np.empty(n), np.empty(n), ctypes.c_double()
+        dl = np.empty((n, self.N)) if self.withGreeks else None
+        vg = np.empty((n, self.T, self.N)) if self.withGreeks else None
+        check(self._L.lmm_portfolio_run(self._h, _p(v), _p(e), _p(dl), _p(vg), _p(lat), ctypes.byref(tot)),
+              "Portfolio.run")
+        return {"values": v, "errors": e, "deltas": dl, "vegas": vg, "latency_ms": lat, "total_ms": tot.value}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.lmm_portfolio_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 # --------------------------------------------------------------------------- instrumentation
 def kernel_stats():
     L = _lib.load()

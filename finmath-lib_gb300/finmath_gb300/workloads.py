@@ -70,3 +70,34 @@ def build(cfg, paths=None, precision=0, observe_tenor_only=True, seed=None):
     obs = tenor_time_indices(cfg) if observe_tenor_only else None
     process = F.EulerSchemeFromProcessModel(model, bm, observedTimeIndices=obs)
     return F.LIBORMonteCarloSimulationFromLIBORModel(process)
+
+
+def portfolio_products(cfg=LMM40, n=256, seed=20261203, basis="swaprate"):
+    """The batching workload: n Bermudan swaptions on the shared model, drawn from a seed.
+
+    First exercise: uniform integer 1-10y; swap end: first exercise plus a uniform integer
+    tenor of 1-10y; strike: the ATM par swap rate of the initial curve plus a uniform
+    -100..+100 bp; payer or receiver (notional +1 / -1) with probability 1/2; exercisable
+    on every semi-annual period start.  Generator: numpy.random.default_rng(seed).
+    """
+    from .lmm import BermudanSwaption, ForwardCurveInterpolation
+    rng = np.random.default_rng(seed)
+    period = cfg["period"]
+    tenor = np.arange(0.0, cfg["tenor_end"] + 1e-9, period)
+    curve = ForwardCurveInterpolation.createForwardCurveFromForwards("f", cfg["curve_nodes"], cfg["curve_values"], period)
+    L0 = np.array([curve.getForward(None, t, period) for t in tenor[:-1]])
+    df = np.concatenate([[1.0], np.cumprod(1.0 / (1.0 + L0 * period))])
+    out = []
+    horizon = cfg["tenor_end"]
+    for _ in range(n):
+        first = int(rng.integers(1, min(10, int(horizon) - 1) + 1))
+        end = min(first + int(rng.integers(1, 11)), int(horizon))
+        i0, i1 = int(round(first / period)), int(round(end / period))
+        ann = sum(period * df[k + 1] for k in range(i0, i1))
+        atm = (df[i0] - df[i1]) / ann
+        strike = atm + rng.uniform(-0.01, 0.01)
+        notional = 1.0 if rng.random() < 0.5 else -1.0
+        fix = tenor[i0:i1]
+        out.append(BermudanSwaption(np.ones(len(fix)), fix, np.full(len(fix), period), fix + period, notional, strike,
+                                    True, basis))
+    return out

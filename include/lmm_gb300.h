@@ -229,6 +229,35 @@ int lmm_bermudan_get_gradient(lmm_process* proc, const lmm_bermudan_desc* produc
                               int freeze_numeraire_adjustment, double* out_value, double* out_error,
                               double* out_deltas, double* out_vegas);
 
+/* ---------------------------------------------------------------- portfolio batch
+ * A portfolio of Bermudan swaptions valued, with their deltas and vegas, on one shared
+ * simulation: the per-product work (regression, backward induction, adjoint) is recorded
+ * once into a CUDA graph whose launch values the whole portfolio.  finmath-lib values a
+ * portfolio product by product on a shared LIBORMonteCarloSimulationFromLIBORModel
+ * (AbstractMonteCarloProduct.getValues, montecarlo/AbstractMonteCarloProduct.java:87-104);
+ * this is that loop, batched. */
+typedef struct {
+    int num_products;
+    const lmm_bermudan_desc* products;  /* [num_products] */
+    int with_greeks;                     /* 0: values and errors only */
+    int checkpoint_stride;               /* adjoint checkpoint stride, 1..16 */
+    int concurrency;                     /* products in flight (independent branches of the graph), 1..16 */
+    int adjoint_threads;                 /* paths per adjoint block: 64, 128 or 256 */
+    int gram_blocks;                     /* blocks per exercise date in the Gram pass (0: automatic) */
+} lmm_portfolio_desc;
+
+typedef struct lmm_portfolio lmm_portfolio;
+
+/* Validates every product, allocates per-branch scratch, and records the graph. */
+int lmm_portfolio_create(lmm_process* proc, const lmm_portfolio_desc* desc, lmm_portfolio** out);
+/* One graph launch: out_values/out_errors [n]; out_deltas [n][N] and out_vegas [n][T][N] (with
+ * greeks, else may be NULL); out_latency_ms [n] = completion time of each product measured on
+ * the device from the start of the launch (may be NULL); out_total_ms the device time of the
+ * whole launch (may be NULL). */
+int lmm_portfolio_run(lmm_portfolio* pf, double* out_values, double* out_errors, double* out_deltas, double* out_vegas,
+                      double* out_latency_ms, double* out_total_ms);
+int lmm_portfolio_destroy(lmm_portfolio* pf);
+
 /* ---------------------------------------------------------------- instrumentation */
 /* Per-kernel launch counts and (when enabled) CUDA-event times of this library's kernels. */
 int lmm_stats_enable_timing(int enable);
