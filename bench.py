@@ -334,13 +334,13 @@ def greeks_form(args, F, W, cfg, P, T, berm, fp64_valuation_ms):
     for name, prec in (("mixed", F.PRECISION_MIXED), ("fp64", F.PRECISION_FP64)):
         sim = W.build(cfg, paths=P, precision=prec)
         bm = sim.process.brownianMotion
-        g = berm.getGradient(sim, checkpointStride=8)
+        g = berm.getGradient(sim, checkpointStride=1)
         reps = max(1, min(args.steps, 3))
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(reps):
             bm.setSeed(cfg["seed"])
-            g = berm.getGradient(sim, checkpointStride=8)
+            g = berm.getGradient(sim, checkpointStride=1)
         torch.cuda.synchronize()
         ms = 1e3 * (time.perf_counter() - t0) / reps
         grads[name] = g

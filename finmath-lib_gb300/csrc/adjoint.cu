@@ -23,6 +23,10 @@
 // their cross-path adjustment a_l = mean(1/N_l) (:869-874) and the numeraire chain.
 #include <math_constants.h>
 
+#include <algorithm>
+#include <cstring>
+#include <cmath>
+
 #include "lmm_internal.h"
 #include "reduce.cuh"
 
@@ -38,217 +42,294 @@ __device__ __forceinline__ float fexp<float>(float x) { return __expf(x); }
 template <>
 __device__ __forceinline__ double fexp<double>(double x) { return exp(x); }
 template <typename R>
+__device__ __forceinline__ R flog(R x);
+template <>
+__device__ __forceinline__ float flog<float>(float x) { return __logf(x); }
+template <>
+__device__ __forceinline__ double flog<double>(double x) { return log(x); }
+template <typename R>
 __device__ __forceinline__ R fdiv(R a, R b);
 template <>
 __device__ __forceinline__ float fdiv<float>(float a, float b) { return __fdividef(a, b); }
 template <>
 __device__ __forceinline__ double fdiv<double>(double a, double b) { return a / b; }
 
+// vector unit of the factor-matrix rows (one 16-byte load)
+template <typename R>
+struct Vec;
+template <>
+struct Vec<float> {
+    using T = float4;
+    static constexpr int W = 4;
+    static __device__ __forceinline__ void unpack(const T& v, float* o) { o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w; }
+};
+template <>
+struct Vec<double> {
+    using T = double2;
+    static constexpr int W = 2;
+    static __device__ __forceinline__ void unpack(const T& v, double* o) { o[0] = v.x; o[1] = v.y; }
+};
+
+// row pitch of the factor table f[T][N][pitch]: FMAX rounded up to whole 16-byte vectors
+template <typename R, int FMAX>
+__host__ __device__ constexpr int f_pitch() { return (FMAX + Vec<R>::W - 1) / Vec<R>::W * Vec<R>::W; }
+
+// row pitch (elements) of a warp's transpose buffer: 16-byte rows, conflict-free vector reads
+template <typename R>
+__host__ __device__ constexpr int red_pitch() { return sizeof(R) == 4 ? 36 : 34; }
+
 template <typename R>
 struct AdjTables {
-    const R* lam;       // [T][N][F]
-    const R* f;         // [T][N][F] lam / sigma
+    const R* lam;       // [T][N][F] factor loadings (replay)
+    const R* var_half;  // [T][N] -variance/2 (replay)
+    const R* f;         // [T][N][pitch] factor matrix rows f_jk = lam_jk / sigma_j, zero padded
     const R* sigma;     // [T][N]
-    const R* var_half;  // [T][N]
     const R* inv_delta; // [N]
     const R* dt;        // [T]
     const void* dw;     // [T][F][P] of type R
-    const void* ckpt;   // [T/stride+1][N][P]
 };
 
-struct AdjParams {
-    int T, N, F, P, stride, ckpt_is_L;
-    int t_end;   // last time index the product reads (reverse sweep starts there)
-    int n_eff;   // components 0..n_eff-1 influence the product (spot drift of j uses l <= j only)
+struct RevParams {
+    int T, N, F, P;
+    int n_lo, n_hi;      // steps [n_lo, n_hi) of this sweep, in reverse
+    int t_end, n_eff;    // product horizon: states t_end, components 0..n_eff-1
+    int base_step;       // states[] holds the steps base_step, base_step+1, ...
+    int seed;            // 1: start from the seeds at t_end, else from ybar
     int capped;
     double cap;
-    const int* first;        // [T]
-    const double* init;      // [N]
-    const double* seeds;     // [N][P]  d value / d L_m(T_m), already divided by P
-    double* vega_partials;   // [blocks][T][N]
-    double* delta_partials;  // [blocks][N]
+    const int* first;     // [T]
+    const double* init;   // [N]
+    const double* seeds;  // [N][P]  d value / d L_m(T_m), already divided by P
+    const void* states;   // [slots][N][P] forward rates L (type R)
+    void* ybar;           // [N][P] (type R): adjoint of log L carried between sweeps
+    double* vega_partials;   // [warps][T][N]
+    double* delta_partials;  // [warps][N]
 };
 
-template <typename R, int NMAX, int FMAX>
-__device__ __forceinline__ void forward_step(const AdjParams& a, const AdjTables<R>& tb, int i, int p, bool active,
-                                             const R* Y, R* Yn)
+// sum of row r of a warp's transpose buffer over the 32 lanes, in fixed order
+template <typename R>
+__device__ __forceinline__ double row_sum(const R* red, int r)
 {
-    const int N = a.N, F = a.F;
-    const int first = __ldg(a.first + i);
-    const R dt = tb.dt[i];
-    const R* lam = tb.lam + (size_t)i * N * F;
-    const R* dW = static_cast<const R*>(tb.dw);
-    R dw[FMAX], S[FMAX];
+    using V = Vec<R>;
+    const typename V::T* row = reinterpret_cast<const typename V::T*>(red + r * red_pitch<R>());
+    R acc = R(0);
 #pragma unroll
-    for (int k = 0; k < FMAX; k++) {
-        dw[k] = (k < F && active) ? dW[((size_t)i * F + k) * a.P + p] : R(0);
-        S[k] = R(0);
+    for (int q = 0; q < 32 / V::W; q++) {
+        R e[V::W];
+        V::unpack(row[q], e);
+#pragma unroll
+        for (int w = 0; w < V::W; w++) acc += e[w];
     }
-#pragma unroll
-    for (int j = 0; j < NMAX; j++) {
-        if (j >= a.n_eff) continue;
-        if (j < first) {
-            Yn[j] = Y[j];
-            continue;
-        }
-        R L = fexp<R>(Y[j]);
-        if (a.capped && L > (R)a.cap) L = (R)a.cap;
-        const R os = fdiv<R>(L, L + tb.inv_delta[j]);
-        R mu = tb.var_half[(size_t)i * N + j], diff = R(0);
-#pragma unroll
-        for (int k = 0; k < FMAX; k++) {
-            if (k < F) {
-                const R l = lam[j * F + k];
-                S[k] = S[k] + os * l;
-                mu = mu + S[k] * l;
-                diff = diff + dw[k] * l;
-            }
-        }
-        Yn[j] = Y[j] + (mu * dt + diff);
-    }
+    return (double)acc;
 }
 
-template <typename R, int NMAX, int FMAX, int kAdjThreads>
-__global__ void __launch_bounds__(kAdjThreads) adjoint_kernel(const AdjParams a, const AdjTables<R> tb)
-{
-    extern __shared__ double smem_adj[];
-    double* acc = smem_adj;                                      // [T][N] block vega accumulator
-    R* wpart = reinterpret_cast<R*>(smem_adj + (size_t)a.T * a.N);  // [warps][NMAX]
-    const int N = a.N, F = a.F, T = a.T, NE = a.n_eff, TE = a.t_end;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    for (int q = tid; q < T * N; q += kAdjThreads) acc[q] = 0.0;
-    double dsum[NMAX];
-#pragma unroll
-    for (int j = 0; j < NMAX; j++) dsum[j] = 0.0;
-    const int nseg = (TE + a.stride - 1) / a.stride;
-    __syncthreads();
+// Reverse sweep over the steps [n_lo, n_hi) of every path, from stored forward rates.
+// One thread per path (grid-stride over path batches; the partition is fixed by the grid, so
+// the per-warp partial sums and their order do not depend on the checkpoint stride).
+// resident warps per SM the register budget is sized for: 12 in FP32, 8 in FP64 (whose
+// arrays are twice as wide and whose FP64 pipe, not latency, bounds the sweep)
+template <typename R, int TH>
+__host__ __device__ constexpr int rev_min_blocks() { return (sizeof(R) == 4 ? 384 : 256) / TH > 0 ? (sizeof(R) == 4 ? 384 : 256) / TH : 1; }
 
-    for (int base = blockIdx.x * kAdjThreads; base < a.P; base += gridDim.x * kAdjThreads) {
+template <typename R, int NMAX, int FMAX, int TH>
+__global__ void __launch_bounds__(TH, rev_min_blocks<R, TH>()) reverse_kernel(const RevParams a, const AdjTables<R> tb)
+{
+    constexpr int FP = f_pitch<R, FMAX>();
+    constexpr int RS = red_pitch<R>();
+    constexpr bool kKeepOs = sizeof(R) == 4;  // FP64 recomputes os_j in the reverse pass (registers)
+    using V = Vec<R>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    R* red = reinterpret_cast<R*>(smem_raw) + (size_t)warp * NMAX * RS;  // [NMAX][RS] of this warp
+    const int N = a.N, F = a.F, NE = a.n_eff;
+    const size_t gw = (size_t)blockIdx.x * (TH / 32) + warp;
+    double* vp = a.vega_partials + gw * a.T * N;
+    const R* states = static_cast<const R*>(a.states);
+    const R* dW = static_cast<const R*>(tb.dw);
+    const R cap = (R)a.cap;
+
+    for (int base = blockIdx.x * TH; base < a.P; base += gridDim.x * TH) {
         const int p = base + tid;
         const bool active = p < a.P;
         R Ybar[NMAX];
-        R seg[kMaxStride + 1][NMAX];
-        for (int s = nseg - 1; s >= 0; s--) {
-            const int n0 = s * a.stride, n1 = min(n0 + a.stride, TE);
-            // state at the checkpoint
+        if (a.seed) {
+            const R* Ls = states + (size_t)(a.t_end - a.base_step) * N * a.P;
 #pragma unroll
             for (int j = 0; j < NMAX; j++) {
-                R y = R(0);
+                R yb = R(0);
                 if (j < NE && active) {
-                    const size_t o = ((size_t)s * N + j) * a.P + p;
-                    if (a.ckpt_is_L) y = (R)log(static_cast<const double*>(tb.ckpt)[o]);
-                    else y = static_cast<const R*>(tb.ckpt)[o];
+                    const R L = Ls[(size_t)j * a.P + p];
+                    if (!(a.capped && L >= cap)) yb = (R)a.seeds[(size_t)j * a.P + p] * L;
                 }
-                seg[0][j] = y;
+                Ybar[j] = yb;
             }
-            for (int n = n0; n < n1; n++) forward_step<R, NMAX, FMAX>(a, tb, n, p, active, seg[n - n0], seg[n - n0 + 1]);
-            if (s == nseg - 1) {
-                // seed: d value / d Y_m(T) = d value / d L_m(T_m) * L_m (components are frozen after fixing)
+        } else {
+            const R* yb = static_cast<const R*>(a.ybar);
 #pragma unroll
-                for (int j = 0; j < NMAX; j++) {
-                    R yb = R(0);
-                    if (j < NE && active) {
-                        const R y = seg[n1 - n0][j];
-                        const R L = fexp<R>(y);
-                        if (!(a.capped && L > (R)a.cap)) yb = (R)a.seeds[(size_t)j * a.P + p] * L;
-                    }
-                    Ybar[j] = yb;
-                }
-            }
-            for (int n = n1 - 1; n >= n0; n--) {
-                const int i = n;
-                const R* Y = seg[n - n0];
-                const int first = __ldg(a.first + i);
-                const R dt = tb.dt[i];
-                const R* lam = tb.lam + (size_t)i * N * F;
-                const R* fj = tb.f + (size_t)i * N * F;
-                const R* dW = static_cast<const R*>(tb.dw);
-                R dw[FMAX], S[FMAX], Rk[FMAX];
-#pragma unroll
-                for (int k = 0; k < FMAX; k++) {
-                    dw[k] = (k < F && active) ? dW[((size_t)i * F + k) * a.P + p] : R(0);
-                    S[k] = R(0);
-                    Rk[k] = R(0);
-                }
-                // forward pass of the step: running sums S^(N-1) and the measure-change ratios
-                R os[NMAX], Lv[NMAX];
-#pragma unroll
-                for (int j = 0; j < NMAX; j++) {
-                    os[j] = R(0);
-                    Lv[j] = R(0);
-                    if (j < NE && j >= first) {
-                        R L = fexp<R>(Y[j]);
-                        const bool c = a.capped && L > (R)a.cap;
-                        if (c) L = (R)a.cap;
-                        Lv[j] = c ? R(-1) : L;  // -1 marks a capped component (no derivative)
-                        os[j] = fdiv<R>(L, L + tb.inv_delta[j]);
-#pragma unroll
-                        for (int k = 0; k < FMAX; k++)
-                            if (k < F) S[k] = S[k] + os[j] * lam[j * F + k];
-                    }
-                }
-                // reverse pass
-                R contrib[NMAX];
-#pragma unroll
-                for (int jj = NMAX - 1; jj >= 0; jj--) {
-                    const int j = jj;
-                    contrib[j] = R(0);
-                    if (j < NE && j >= first) {
-                        const R yb = Ybar[j];
-                        const R mub = yb * dt;
-                        R osb = R(0), sg = R(0);
-#pragma unroll
-                        for (int k = 0; k < FMAX; k++) {
-                            if (k < F) {
-                                const R l = lam[j * F + k];
-                                Rk[k] = Rk[k] + mub * l;
-                                osb = osb + l * Rk[k];
-                                const R lb = mub * S[k] + os[j] * Rk[k] + yb * dw[k];
-                                sg = sg + lb * fj[j * F + k];
-                                S[k] = S[k] - os[j] * l;  // S^(j-1)
-                            }
-                        }
-                        sg = sg - mub * tb.sigma[(size_t)i * N + j];
-                        contrib[j] = sg;
-                        if (Lv[j] > R(0)) {
-                            const R c = tb.inv_delta[j];
-                            const R den = Lv[j] + c;
-                            Ybar[j] = yb + fdiv<R>(osb * c, den * den) * Lv[j];
-                        }
-                    }
-                }
-                // block-sum the vega contributions of step i (deterministic order)
-#pragma unroll
-                for (int j = 0; j < NMAX; j++) {
-                    if (j < NE && j >= first) {
-                        R v = active ? contrib[j] : R(0);
-#pragma unroll
-                        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-                        if (lane == 0) wpart[warp * NMAX + j] = v;
-                    }
-                }
-                __syncthreads();
-                if (tid < NE && tid >= first) {
-                    double t = 0.0;
-                    for (int w = 0; w < kAdjThreads / 32; w++) t += (double)wpart[w * NMAX + tid];
-                    acc[(size_t)i * N + tid] += t;
-                }
-                __syncthreads();
-            }
+            for (int j = 0; j < NMAX; j++) Ybar[j] = (j < NE && active) ? yb[(size_t)j * a.P + p] : R(0);
         }
-        // deltas: Y_0 = log(L_0(0)) -> d value / d L_0 = Ybar / L_0
+
+        for (int n = a.n_hi - 1; n >= a.n_lo; n--) {
+            const int first = __ldg(a.first + n);
+            const R dt = tb.dt[n];
+            const R* Ls = states + (size_t)(n - a.base_step) * N * a.P;
+            const R* sig = tb.sigma + (size_t)n * N;
+            const R* frow = tb.f + (size_t)n * N * FP;
+            R dw[FMAX], S[FMAX], Rk[FMAX];
 #pragma unroll
-        for (int j = 0; j < NMAX; j++)
-            if (j < NE && active) dsum[j] += (double)Ybar[j] / a.init[j];
+            for (int k = 0; k < FMAX; k++) {
+                dw[k] = (k < F && active) ? dW[((size_t)n * F + k) * a.P + p] : R(0);
+                S[k] = R(0);
+                Rk[k] = R(0);
+            }
+            // forward pass of the step: S_k = sum_j os_j sigma_j f_jk
+            R os[kKeepOs ? NMAX : 1];
+            unsigned long long capmask = 0ull;
+#pragma unroll
+            for (int j = 0; j < NMAX; j++) {
+                if (j < NE && j >= first) {
+                    const R L = active ? Ls[(size_t)j * a.P + p] : R(0);
+                    if (a.capped && L >= cap) capmask |= 1ull << j;
+                    const R o = fdiv<R>(L, L + tb.inv_delta[j]);
+                    if (kKeepOs) os[kKeepOs ? j : 0] = o;
+                    const R oss = o * sig[j];
+                    R fr[FP];
+#pragma unroll
+                    for (int q = 0; q < FP / V::W; q++) V::unpack(__ldg(reinterpret_cast<const typename V::T*>(frow + j * FP) + q), fr + q * V::W);
+#pragma unroll
+                    for (int k = 0; k < FMAX; k++)
+                        if (k < F) S[k] = S[k] + oss * fr[k];
+                }
+            }
+            // reverse pass over the components
+#pragma unroll
+            for (int jj = NMAX - 1; jj >= 0; jj--) {
+                const int j = jj;
+                if (j < NE && j >= first) {
+                    R o;
+                    if (kKeepOs) {
+                        o = os[kKeepOs ? j : 0];
+                    } else {
+                        const R L = active ? Ls[(size_t)j * a.P + p] : R(0);
+                        o = fdiv<R>(L, L + tb.inv_delta[j]);
+                    }
+                    const R sg = sig[j];
+                    const R yb = Ybar[j];
+                    const R mub = yb * dt;
+                    const R mubs = mub * sg;
+                    const R oss = o * sg;
+                    R fr[FP];
+#pragma unroll
+                    for (int q = 0; q < FP / V::W; q++) V::unpack(__ldg(reinterpret_cast<const typename V::T*>(frow + j * FP) + q), fr + q * V::W);
+                    R A = R(0), B = R(0), D = R(0);
+#pragma unroll
+                    for (int k = 0; k < FMAX; k++) {
+                        if (k < F) {
+                            Rk[k] = Rk[k] + mubs * fr[k];  // R_k = sum_{l>=j} mubar_l lam_lk
+                            A = A + Rk[k] * fr[k];
+                            B = B + S[k] * fr[k];          // S^(j)
+                            D = D + dw[k] * fr[k];
+                            S[k] = S[k] - oss * fr[k];     // S^(j-1)
+                        }
+                    }
+                    // sigmabar_ij = sum_k lambar_jk f_jk - mubar_j sigma_ij with
+                    // lambar_jk = mubar_j S_k + os_j R_k + Ybar'_j dW_k
+                    red[j * RS + lane] = active ? (mub * B + o * A + yb * D - mubs) : R(0);
+                    // osbar_j = sigma_j A;  d os_j / d Y_j = os_j (1 - os_j) (zero where capped)
+                    if (!((capmask >> j) & 1ull)) Ybar[j] = yb + (sg * A) * (o * (R(1) - o));
+                }
+            }
+            __syncwarp();
+#pragma unroll
+            for (int h = 0; h < (NMAX + 31) / 32; h++) {
+                const int r = lane + 32 * h;
+                if (r < NE && r >= first) vp[(size_t)n * N + r] += row_sum<R>(red, r);
+            }
+            __syncwarp();
+        }
+
+        if (a.n_lo > 0) {
+            R* yb = static_cast<R*>(a.ybar);
+#pragma unroll
+            for (int j = 0; j < NMAX; j++)
+                if (j < NE && active) yb[(size_t)j * a.P + p] = Ybar[j];
+        } else {
+            // deltas: Y_0 = log(L_0(0)) -> d value / d L_0 = Ybar / L_0
+#pragma unroll
+            for (int j = 0; j < NMAX; j++)
+                if (j < NE) red[j * RS + lane] = active ? (R)((double)Ybar[j] / a.init[j]) : R(0);
+            __syncwarp();
+#pragma unroll
+            for (int h = 0; h < (NMAX + 31) / 32; h++) {
+                const int r = lane + 32 * h;
+                if (r < NE) a.delta_partials[gw * N + r] += row_sum<R>(red, r);
+            }
+            __syncwarp();
+        }
     }
-    // write block partials
-    for (int q = tid; q < T * N; q += kAdjThreads) a.vega_partials[(size_t)blockIdx.x * T * N + q] = acc[q];
+}
+
+// Replays the Euler-log steps [n0, n_stop) of every path from the checkpoint at n0 (forward
+// rates) and stores the forward rates of the steps n0..n_stop in seg[0..n_stop-n0].
+struct ReplayParams {
+    int T, N, F, P, n0, n_stop, n_eff, capped;
+    double cap;
+    const int* first;
+    const void* ckpt_slot;  // [N][P] forward rates at n0
+    void* seg;              // [n_stop-n0+1][N][P]
+};
+
+template <typename R, int NMAX, int FMAX>
+__global__ void __launch_bounds__(128) replay_kernel(const ReplayParams a, const AdjTables<R> tb)
+{
+    const int p = blockIdx.x * 128 + threadIdx.x;
+    if (p >= a.P) return;
+    const int N = a.N, F = a.F, NE = a.n_eff, P = a.P;
+    const R* ck = static_cast<const R*>(a.ckpt_slot);
+    R* seg = static_cast<R*>(a.seg);
+    const R* dW = static_cast<const R*>(tb.dw);
+    const R cap = (R)a.cap;
+    R Y[NMAX], L[NMAX];
 #pragma unroll
     for (int j = 0; j < NMAX; j++) {
-        if (j < N) {
-            const dd s = block_dd_sum(dd{dsum[j], 0.0});
-            if (tid == 0) a.delta_partials[(size_t)blockIdx.x * N + j] = s.hi + s.lo;
+        L[j] = (j < NE) ? ck[(size_t)j * P + p] : R(0);
+        Y[j] = (j < NE) ? flog<R>(L[j]) : R(0);
+        if (j < NE) seg[(size_t)j * P + p] = L[j];
+    }
+    for (int n = a.n0; n < a.n_stop; n++) {
+        const int first = __ldg(a.first + n);
+        const R dt = tb.dt[n];
+        const R* lam = tb.lam + (size_t)n * N * F;
+        R dw[FMAX], S[FMAX];
+#pragma unroll
+        for (int k = 0; k < FMAX; k++) {
+            dw[k] = (k < F) ? dW[((size_t)n * F + k) * P + p] : R(0);
+            S[k] = R(0);
         }
+#pragma unroll
+        for (int j = 0; j < NMAX; j++) {
+            if (j < NE && j >= first) {
+                const R os = fdiv<R>(L[j], L[j] + tb.inv_delta[j]);
+                R mu = tb.var_half[(size_t)n * N + j], diff = R(0);
+#pragma unroll
+                for (int k = 0; k < FMAX; k++) {
+                    if (k < F) {
+                        const R l = lam[j * F + k];
+                        S[k] = S[k] + os * l;
+                        mu = mu + S[k] * l;
+                        diff = diff + dw[k] * l;
+                    }
+                }
+                Y[j] = Y[j] + (mu * dt + diff);
+                R v = fexp<R>(Y[j]);
+                if (a.capped && v > cap) v = cap;
+                L[j] = v;
+            }
+        }
+        R* out = seg + (size_t)(n + 1 - a.n0) * N * P;
+#pragma unroll
+        for (int j = 0; j < NMAX; j++)
+            if (j < NE) out[(size_t)j * P + p] = L[j];
     }
 }
 
@@ -343,64 +424,151 @@ __global__ void __launch_bounds__(256) seed_kernel(const SeedParams a)
     for (int m = 0; m < a.N; m++) a.seeds[(size_t)m * a.P + p] = lb[m] * invP;
 }
 
-// column sums of [rows][cols] partials in fixed order (grid: cols/32 blocks of 256 threads)
-__global__ void __launch_bounds__(256) column_sum_kernel(const double* in, int rows, int cols, double scale, double* out)
+// column sums of [rows][cols] partials in fixed order (grid: cols/32 blocks of 1024 threads)
+__global__ void __launch_bounds__(1024) column_sum_kernel(const double* in, int rows, int cols, double scale, double* out)
 {
-    __shared__ double part[8][33];
+    __shared__ double part[32][33];
     const int c = blockIdx.x * 32 + (threadIdx.x & 31), r0 = threadIdx.x >> 5;
     double s = 0.0;
     if (c < cols)
-        for (int r = r0; r < rows; r += 8) s += in[(size_t)r * cols + c];
+        for (int r = r0; r < rows; r += 32) s += in[(size_t)r * cols + c];
     part[r0][threadIdx.x & 31] = s;
     __syncthreads();
     if (r0 == 0 && c < cols) {
         double t = 0.0;
-        for (int k = 0; k < 8; k++) t += part[k][threadIdx.x & 31];
+        for (int k = 0; k < 32; k++) t += part[k][threadIdx.x & 31];
         out[c] = t * scale;
     }
 }
 
 template <typename R, int NMAX, int FMAX, int TH>
-int launch_adj(const AdjParams& a, const AdjTables<R>& tb, int blocks, cudaStream_t s)
+int launch_rev(const RevParams& a, const AdjTables<R>& tb, int blocks, cudaStream_t s)
 {
-    const size_t smem = (size_t)a.T * a.N * sizeof(double) + (TH / 32) * NMAX * sizeof(R);
-    if (smem > 200 * 1024) return fail(LMM_ERR_INVALID, "adjoint: time steps x forward rates too large");
+    const size_t smem = (size_t)(TH / 32) * NMAX * red_pitch<R>() * sizeof(R);
     static bool attr_set = false;  // set once, before any stream capture
     if (!attr_set) {
-        LMM_CUDA(cudaFuncSetAttribute(adjoint_kernel<R, NMAX, FMAX, TH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      200 * 1024));
+        LMM_CUDA(cudaFuncSetAttribute(reverse_kernel<R, NMAX, FMAX, TH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
         attr_set = true;
     }
-    adjoint_kernel<R, NMAX, FMAX, TH><<<blocks, TH, smem, s>>>(a, tb);
+    reverse_kernel<R, NMAX, FMAX, TH><<<blocks, TH, smem, s>>>(a, tb);
     LMM_CUDA(cudaGetLastError());
     return LMM_OK;
 }
 
 template <typename R, int NMAX, int FMAX>
-int launch_adj_threads(const AdjParams& a, const AdjTables<R>& tb, int threads, int blocks, cudaStream_t s)
+int launch_rev_threads(const RevParams& a, const AdjTables<R>& tb, int threads, int blocks, cudaStream_t s)
 {
-    if (threads == 64) return launch_adj<R, NMAX, FMAX, 64>(a, tb, blocks, s);
-    if (threads == 256) return launch_adj<R, NMAX, FMAX, 256>(a, tb, blocks, s);
-    return launch_adj<R, NMAX, FMAX, 128>(a, tb, blocks, s);
+    if (threads == 64) return launch_rev<R, NMAX, FMAX, 64>(a, tb, blocks, s);
+    if (threads == 256) return launch_rev<R, NMAX, FMAX, 256>(a, tb, blocks, s);
+    return launch_rev<R, NMAX, FMAX, 128>(a, tb, blocks, s);
 }
 
 template <typename R>
-int launch_adj_dispatch(const AdjParams& a, const AdjTables<R>& tb, int threads, int blocks, cudaStream_t s)
+int launch_rev_dispatch(const RevParams& a, const AdjTables<R>& tb, int threads, int blocks, cudaStream_t s)
 {
-    if (a.N <= 24 && a.F <= 4) return launch_adj_threads<R, 24, 4>(a, tb, threads, blocks, s);
-    if (a.N <= 40 && a.F <= 10) return launch_adj_threads<R, 40, 10>(a, tb, threads, blocks, s);
+    if (a.N <= 24 && a.F <= 4) return launch_rev_threads<R, 24, 4>(a, tb, threads, blocks, s);
+    if (a.N <= 40 && a.F <= 10) return launch_rev_threads<R, 40, 10>(a, tb, threads, blocks, s);
     return fail(LMM_ERR_INVALID, "adjoint supports at most 40 forward rates and 10 factors");
+}
+
+template <typename R>
+int launch_replay_dispatch(const ReplayParams& a, const AdjTables<R>& tb, cudaStream_t s)
+{
+    const int blocks = (a.P + 127) / 128;
+    if (a.N <= 24 && a.F <= 4) replay_kernel<R, 24, 4><<<blocks, 128, 0, s>>>(a, tb);
+    else if (a.N <= 40 && a.F <= 10) replay_kernel<R, 40, 10><<<blocks, 128, 0, s>>>(a, tb);
+    else return fail(LMM_ERR_INVALID, "adjoint supports at most 40 forward rates and 10 factors");
+    LMM_CUDA(cudaGetLastError());
+    return LMM_OK;
+}
+
+template <typename R>
+int reverse_sweeps(const AdjointLaunch& L, const AdjTables<R>& tb, cudaStream_t s)
+{
+    RevParams rp;
+    std::memset(&rp, 0, sizeof(rp));
+    rp.T = L.T;
+    rp.N = L.N;
+    rp.F = L.F;
+    rp.P = L.P;
+    rp.t_end = L.t_end;
+    rp.n_eff = L.n_eff;
+    rp.capped = !std::isinf(L.cap);
+    rp.cap = L.cap;
+    rp.first = L.d_first;
+    rp.init = L.d_init;
+    rp.seeds = L.d_seeds;
+    rp.ybar = L.d_ybar;
+    rp.vega_partials = L.d_vega_partials;
+    rp.delta_partials = L.d_delta_partials;
+    if (L.stride == 1) {
+        // every step's forward rates are stored: one sweep over [0, t_end)
+        rp.n_lo = 0;
+        rp.n_hi = L.t_end;
+        rp.base_step = 0;
+        rp.seed = 1;
+        rp.states = L.d_ckpt;
+        return launch_rev_dispatch<R>(rp, tb, L.threads, L.blocks, s);
+    }
+    ReplayParams q;
+    std::memset(&q, 0, sizeof(q));
+    q.T = L.T;
+    q.N = L.N;
+    q.F = L.F;
+    q.P = L.P;
+    q.n_eff = L.n_eff;
+    q.capped = rp.capped;
+    q.cap = L.cap;
+    q.first = L.d_first;
+    q.seg = L.d_seg;
+    const int nseg = (L.t_end + L.stride - 1) / L.stride;
+    for (int sgi = nseg - 1; sgi >= 0; sgi--) {
+        const int n0 = sgi * L.stride, n1 = std::min(n0 + L.stride, L.t_end);
+        q.n0 = n0;
+        q.n_stop = (sgi == nseg - 1) ? n1 : n1 - 1;  // the last segment also needs the state at t_end
+        q.ckpt_slot = static_cast<const R*>(L.d_ckpt) + (size_t)sgi * L.N * L.P;
+        int rc = launch_replay_dispatch<R>(q, tb, s);
+        if (rc) return rc;
+        rp.n_lo = n0;
+        rp.n_hi = n1;
+        rp.base_step = n0;
+        rp.seed = sgi == nseg - 1;
+        rp.states = L.d_seg;
+        if ((rc = launch_rev_dispatch<R>(rp, tb, L.threads, L.blocks, s))) return rc;
+    }
+    return LMM_OK;
 }
 
 }  // namespace
 
-int adjoint_blocks(int P, int threads)
+int adjoint_f_pitch(int N, int F, int fp32)
+{
+    const bool small = N <= 24 && F <= 4;  // the (forward rates, factors) templates of the reverse kernel
+    if (fp32) return small ? f_pitch<float, 4>() : f_pitch<float, 10>();
+    return small ? f_pitch<double, 4>() : f_pitch<double, 10>();
+}
+
+int adjoint_blocks(int P, int threads, int fp32)
 {
     int dev = 0, sms = 152;
     if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int want = sms * (512 / threads);
+    const int want = sms * std::max(1, (fp32 ? 384 : 256) / threads);  // the resident blocks of rev_min_blocks
     const int need = (P + threads - 1) / threads;
     return need < want ? need : want;
+}
+
+AdjointScratch adjoint_scratch(int T, int N, int P, int threads, int stride, int fp32)
+{
+    AdjointScratch z;
+    z.blocks = adjoint_blocks(P, threads, fp32);
+    z.warps = z.blocks * (threads / 32);
+    z.vega_partials = (size_t)z.warps * T * N;
+    z.delta_partials = (size_t)z.warps * N;
+    const size_t esz = fp32 ? sizeof(float) : sizeof(double);
+    z.seg_bytes = stride > 1 ? (size_t)(stride + 1) * N * (size_t)P * esz : 0;
+    z.ybar_bytes = stride > 1 ? (size_t)N * (size_t)P * esz : 0;
+    return z;
 }
 
 int launch_adjoint(const AdjointLaunch& L, cudaStream_t s)
@@ -437,51 +605,38 @@ int launch_adjoint(const AdjointLaunch& L, cudaStream_t s)
         sp.pass = 1;
         if (L.fp32) seed_kernel<float><<<sb, 256, 0, s>>>(sp);
         else seed_kernel<double><<<sb, 256, 0, s>>>(sp);
-        column_sum_kernel<<<(L.N + 1 + 31) / 32, 256, 0, s>>>(L.d_abar_partials, sb, L.N + 1, 1.0 / (double)L.P, L.d_abar);
-        column_sum_kernel<<<1, 256, 0, s>>>(L.d_value_partials, sb, 1, 1.0 / (double)L.P, L.d_value_out);
+        column_sum_kernel<<<(L.N + 1 + 31) / 32, 1024, 0, s>>>(L.d_abar_partials, sb, L.N + 1, 1.0 / (double)L.P, L.d_abar);
+        column_sum_kernel<<<1, 1024, 0, s>>>(L.d_value_partials, sb, 1, 1.0 / (double)L.P, L.d_value_out);
         sp.pass = 2;
         if (L.fp32) seed_kernel<float><<<sb, 256, 0, s>>>(sp);
         else seed_kernel<double><<<sb, 256, 0, s>>>(sp);
         LMM_CUDA(cudaGetLastError());
     }
-    // ---- reverse sweep over the paths
-    AdjParams ap;
-    ap.T = L.T;
-    ap.N = L.N;
-    ap.F = L.F;
-    ap.P = L.P;
-    ap.stride = L.stride;
-    ap.ckpt_is_L = L.ckpt_is_L;
-    ap.capped = !std::isinf(L.cap);
-    ap.t_end = L.t_end;
-    ap.n_eff = L.n_eff;
-    ap.cap = L.cap;
-    ap.first = L.d_first;
-    ap.init = L.d_init;
-    ap.seeds = L.d_seeds;
-    ap.vega_partials = L.d_vega_partials;
-    ap.delta_partials = L.d_delta_partials;
-    const int blocks = L.blocks;
+    // ---- reverse sweeps over the paths (per-warp partials, then fixed-order column sums)
+    const int warps = L.blocks * (L.threads / 32);
+    LMM_CUDA(cudaMemsetAsync(L.d_vega_partials, 0, sizeof(double) * (size_t)warps * L.T * L.N, s));
+    LMM_CUDA(cudaMemsetAsync(L.d_delta_partials, 0, sizeof(double) * (size_t)warps * L.N, s));
+    const int nsweeps = L.stride == 1 ? 1 : 2 * ((L.t_end + L.stride - 1) / L.stride);
     int rc;
     {
-        KernelTimer kt(K_ADJOINT, s);
+        KernelTimer kt(K_ADJOINT, s, nsweeps);
         if (L.fp32) {
-            AdjTables<float> tb{static_cast<const float*>(L.d_lam), static_cast<const float*>(L.d_f),
-                                static_cast<const float*>(L.d_sigma), static_cast<const float*>(L.d_var_half),
-                                static_cast<const float*>(L.d_inv_delta), static_cast<const float*>(L.d_dt), L.d_dw, L.d_ckpt};
-            rc = launch_adj_dispatch<float>(ap, tb, L.threads, blocks, s);
+            AdjTables<float> tb{static_cast<const float*>(L.d_lam), static_cast<const float*>(L.d_var_half),
+                                static_cast<const float*>(L.d_f), static_cast<const float*>(L.d_sigma),
+                                static_cast<const float*>(L.d_inv_delta), static_cast<const float*>(L.d_dt), L.d_dw};
+            rc = reverse_sweeps<float>(L, tb, s);
         } else {
-            AdjTables<double> tb{static_cast<const double*>(L.d_lam), static_cast<const double*>(L.d_f),
-                                 static_cast<const double*>(L.d_sigma), static_cast<const double*>(L.d_var_half),
-                                 static_cast<const double*>(L.d_inv_delta), static_cast<const double*>(L.d_dt), L.d_dw, L.d_ckpt};
-            rc = launch_adj_dispatch<double>(ap, tb, L.threads, blocks, s);
+            AdjTables<double> tb{static_cast<const double*>(L.d_lam), static_cast<const double*>(L.d_var_half),
+                                 static_cast<const double*>(L.d_f), static_cast<const double*>(L.d_sigma),
+                                 static_cast<const double*>(L.d_inv_delta), static_cast<const double*>(L.d_dt), L.d_dw};
+            rc = reverse_sweeps<double>(L, tb, s);
         }
     }
     if (rc) return rc;
     {
         KernelTimer kt(K_ADJOINT, s, 2);
-        column_sum_kernel<<<(L.T * L.N + 31) / 32, 256, 0, s>>>(L.d_vega_partials, blocks, L.T * L.N, 1.0, L.d_vegas);
-        column_sum_kernel<<<(L.N + 31) / 32, 256, 0, s>>>(L.d_delta_partials, blocks, L.N, 1.0, L.d_deltas);
+        column_sum_kernel<<<(L.T * L.N + 31) / 32, 1024, 0, s>>>(L.d_vega_partials, warps, L.T * L.N, 1.0, L.d_vegas);
+        column_sum_kernel<<<(L.N + 31) / 32, 1024, 0, s>>>(L.d_delta_partials, warps, L.N, 1.0, L.d_deltas);
         LMM_CUDA(cudaGetLastError());
     }
     return LMM_OK;

@@ -183,7 +183,7 @@ struct lmm_process {
     // device tables
     double *d_loadings = nullptr, *d_variance = nullptr, *d_dt = nullptr, *d_delta = nullptr, *d_init = nullptr;
     double *d_inv_delta = nullptr, *d_var_half = nullptr;
-    float *d_lam32 = nullptr, *d_var32 = nullptr;
+    float *d_lam32 = nullptr, *d_var32 = nullptr, *d_inv_delta32 = nullptr, *d_dt32 = nullptr;
     int *d_first = nullptr, *d_obs_slot = nullptr;
     uint8_t* d_det = nullptr;
     // results
@@ -211,6 +211,8 @@ struct lmm_process {
     double *d_abar = nullptr, *d_abar_partials = nullptr, *d_seeds = nullptr, *d_value_partials = nullptr,
            *d_value_out = nullptr, *d_vega_partials = nullptr, *d_delta_partials = nullptr, *d_vegas = nullptr,
            *d_deltas = nullptr;
+    unsigned char *d_adj_seg = nullptr, *d_adj_ybar = nullptr;  // stride > 1 segment buffers
+    size_t adj_seg_bytes = 0, adj_ybar_bytes = 0;
 };
 
 extern "C" {
@@ -459,8 +461,13 @@ int lmm_process_create(const lmm_model_desc* m, lmm_brownian* bm, lmm_process** 
         std::vector<float> l32((size_t)T * N * F), v32((size_t)T * N);
         for (size_t i = 0; i < l32.size(); i++) l32[i] = (float)m->factor_loadings[i];
         for (size_t i = 0; i < v32.size(); i++) v32[i] = (float)m->variance[i];
+        std::vector<float> id32(N), dt32(T);
+        for (int j = 0; j < N; j++) id32[j] = (float)inv_delta[j];
+        for (int i = 0; i < T; i++) dt32[i] = (float)dt[i];
         rc = upload(&pr->d_lam32, l32.data(), l32.size(), s);
         if (!rc) rc = upload(&pr->d_var32, v32.data(), v32.size(), s);
+        if (!rc) rc = upload(&pr->d_inv_delta32, id32.data(), id32.size(), s);
+        if (!rc) rc = upload(&pr->d_dt32, dt32.data(), dt32.size(), s);
         if (!rc) rc = cudaStreamSynchronize(s) == cudaSuccess ? 0 : fail(LMM_ERR_CUDA, "stream sync");
     }
     if (!rc) rc = cudaStreamSynchronize(s) == cudaSuccess ? 0 : fail(LMM_ERR_CUDA, "stream sync");
@@ -523,6 +530,8 @@ static int process_ensure(lmm_process* pr)
     a.d_delta = pr->d_delta;
     a.d_inv_delta = pr->d_inv_delta;
     a.d_var_half = pr->d_var_half;
+    a.d_inv_delta32 = pr->d_inv_delta32;
+    a.d_dt32 = pr->d_dt32;
     a.d_init = pr->d_init;
     a.d_obs_slot = pr->d_obs_slot;
     a.d_dw = pr->bm->d_dw;
@@ -616,6 +625,8 @@ int lmm_process_destroy(lmm_process* pr)
     dfree(pr->d_init, s);
     dfree(pr->d_lam32, s);
     dfree(pr->d_var32, s);
+    dfree(pr->d_inv_delta32, s);
+    dfree(pr->d_dt32, s);
     dfree(pr->d_first, s);
     dfree(pr->d_det, s);
     dfree(pr->d_values, s);
@@ -640,6 +651,8 @@ int lmm_process_destroy(lmm_process* pr)
                           pr->d_vega_partials, pr->d_delta_partials, pr->d_vegas, pr->d_deltas};
     for (double* q : adj_bufs)
         if (q) cudaFreeAsync(q, s);
+    dfree(pr->d_adj_seg, s);
+    dfree(pr->d_adj_ybar, s);
     cudaStreamSynchronize(s);
     delete pr;
     return LMM_OK;
@@ -893,7 +906,8 @@ static int adjoint_tables(lmm_process* pr)
 {
     if (pr->d_adj_f) return LMM_OK;
     const int T = pr->T, N = pr->N, F = pr->F;
-    std::vector<double> sigma((size_t)T * N), f((size_t)T * N * F, 0.0), vh((size_t)T * N), invd(N), dt(T);
+    const int FP = adjoint_f_pitch(N, F, pr->precision == LMM_PRECISION_MIXED);
+    std::vector<double> sigma((size_t)T * N), f((size_t)T * N * FP, 0.0), vh((size_t)T * N), invd(N), dt(T);
     for (size_t q = 0; q < sigma.size(); q++) {
         sigma[q] = pr->h_vol.empty() ? std::sqrt(pr->h_variance[q]) : pr->h_vol[q];
         vh[q] = pr->h_variance[q] * -0.5;
@@ -902,7 +916,7 @@ static int adjoint_tables(lmm_process* pr)
         for (int j = 0; j < N; j++) {
             const double sg = sigma[(size_t)i * N + j];
             for (int k = 0; k < F; k++)
-                f[((size_t)i * N + j) * F + k] = sg != 0.0 ? pr->h_loadings[((size_t)i * N + j) * F + k] / sg : 0.0;
+                f[((size_t)i * N + j) * FP + k] = sg != 0.0 ? pr->h_loadings[((size_t)i * N + j) * F + k] / sg : 0.0;
         }
     for (int j = 0; j < N; j++) invd[j] = 1.0 / (pr->tenor[j + 1] - pr->tenor[j]);
     for (int i = 0; i < T; i++) dt[i] = pr->times[i + 1] - pr->times[i];
@@ -945,18 +959,28 @@ int lmm_bermudan_get_gradient(lmm_process* pr, const lmm_bermudan_desc* d, int s
     const int T = pr->T, N = pr->N, P = pr->P;
     const int sb = (P + 255) / 256;
     const int threads = 128;
-    const int blocks = adjoint_blocks(P, threads);
+    const AdjointScratch z = adjoint_scratch(T, N, P, threads, stride, pr->precision == LMM_PRECISION_MIXED);
     if (!pr->d_seeds) {
         if (!rc) rc = dalloc(&pr->d_abar, (size_t)N + 1, s);
         if (!rc) rc = dalloc(&pr->d_abar_partials, (size_t)sb * (N + 1), s);
         if (!rc) rc = dalloc(&pr->d_seeds, (size_t)N * P, s);
         if (!rc) rc = dalloc(&pr->d_value_partials, (size_t)sb, s);
         if (!rc) rc = dalloc(&pr->d_value_out, (size_t)1, s);
-        if (!rc) rc = dalloc(&pr->d_vega_partials, (size_t)blocks * T * N, s);
-        if (!rc) rc = dalloc(&pr->d_delta_partials, (size_t)blocks * N, s);
+        if (!rc) rc = dalloc(&pr->d_vega_partials, z.vega_partials, s);
+        if (!rc) rc = dalloc(&pr->d_delta_partials, z.delta_partials, s);
         if (!rc) rc = dalloc(&pr->d_vegas, (size_t)T * N, s);
         if (!rc) rc = dalloc(&pr->d_deltas, (size_t)N, s);
         if (rc) return rc;
+    }
+    if (z.seg_bytes > pr->adj_seg_bytes) {
+        dfree(pr->d_adj_seg, s);
+        if ((rc = dalloc(&pr->d_adj_seg, z.seg_bytes, s))) return rc;
+        pr->adj_seg_bytes = z.seg_bytes;
+    }
+    if (z.ybar_bytes > pr->adj_ybar_bytes) {
+        dfree(pr->d_adj_ybar, s);
+        if ((rc = dalloc(&pr->d_adj_ybar, z.ybar_bytes, s))) return rc;
+        pr->adj_ybar_bytes = z.ybar_bytes;
     }
     LMM_CUDA(cudaMemsetAsync(pr->d_abar_partials, 0, sizeof(double) * (size_t)sb * (N + 1), s));
     std::vector<double> delta(N);
@@ -969,12 +993,11 @@ int lmm_bermudan_get_gradient(lmm_process* pr, const lmm_bermudan_desc* d, int s
     L.P = P;
     L.nper = bl.nper;
     L.stride = stride;
-    L.ckpt_is_L = (pr->precision == LMM_PRECISION_FP64 && pr->scheme == LMM_SCHEME_EULER_FUNCTIONAL) ? 1 : 0;
     L.callable = bl.callable;
     L.freeze_adjustment = freeze ? 1 : 0;
     L.fp32 = pr->precision == LMM_PRECISION_MIXED;
     L.T_slot = pr->obs_slot[T];
-    L.blocks = blocks;
+    L.blocks = z.blocks;
     L.threads = threads;
     // the product reads forwards up to its last period: reverse from that fixing over components <= it
     int m_end = 0;
@@ -994,6 +1017,8 @@ int lmm_bermudan_get_gradient(lmm_process* pr, const lmm_bermudan_desc* d, int s
     L.d_init = pr->d_init;
     L.d_dw = pr->bm->d_dw;
     L.d_ckpt = pr->d_ckpt;
+    L.d_seg = pr->d_adj_seg;
+    L.d_ybar = pr->d_adj_ybar;
     L.d_lam = pr->d_adj_lam;
     L.d_f = pr->d_adj_f;
     L.d_sigma = pr->d_adj_sigma;
@@ -1053,6 +1078,7 @@ struct PortfolioBranch {
            *rhs = nullptr, *beta = nullptr, *reduce = nullptr;
     double *seeds = nullptr, *abar = nullptr, *abar_partials = nullptr, *value_partials = nullptr,
            *value_out = nullptr, *vega_partials = nullptr, *delta_partials = nullptr;
+    unsigned char *seg = nullptr, *ybar = nullptr;  // stride > 1 segment buffers
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
 };
@@ -1096,6 +1122,8 @@ static int portfolio_free(lmm_portfolio* pf)
                           b.abar_partials, b.value_partials, b.value_out, b.vega_partials, b.delta_partials};
         for (double* q : bufs)
             if (q) cudaFreeAsync(q, s);
+        if (b.seg) cudaFreeAsync(b.seg, s);
+        if (b.ybar) cudaFreeAsync(b.ybar, s);
         if (b.done) cudaEventDestroy(b.done);
         if (b.stream) cudaStreamDestroy(b.stream);
     }
@@ -1151,12 +1179,11 @@ static int portfolio_enqueue(lmm_portfolio* pf, int q, PortfolioBranch& b)
         L.P = P;
         L.nper = a.nper;
         L.stride = pf->stride;
-        L.ckpt_is_L = (pr->precision == LMM_PRECISION_FP64 && pr->scheme == LMM_SCHEME_EULER_FUNCTIONAL) ? 1 : 0;
         L.callable = a.callable;
         L.fp32 = pr->precision == LMM_PRECISION_MIXED;
         L.T_slot = pr->obs_slot[T];
         L.threads = pf->threads;
-        L.blocks = adjoint_blocks(P, pf->threads);
+        L.blocks = adjoint_blocks(P, pf->threads, L.fp32);
         int m_end = 0;
         for (int k = 0; k < a.nper; k++) m_end = std::max(m_end, a.per[k].libor_index);
         L.n_eff = m_end + 1;
@@ -1174,6 +1201,8 @@ static int portfolio_enqueue(lmm_portfolio* pf, int q, PortfolioBranch& b)
         L.d_init = pr->d_init;
         L.d_dw = pr->bm->d_dw;
         L.d_ckpt = pr->d_ckpt;
+        L.d_seg = b.seg;
+        L.d_ybar = b.ybar;
         L.d_lam = pr->d_adj_lam;
         L.d_f = pr->d_adj_f;
         L.d_sigma = pr->d_adj_sigma;
@@ -1320,7 +1349,8 @@ int lmm_portfolio_create(lmm_process* pr, const lmm_portfolio_desc* desc, lmm_po
     // ---- per-branch scratch
     const int blocks = bermudan_blocks(P);
     const int sb = (P + 255) / 256;
-    const int ablocks = adjoint_blocks(P, pf->threads);
+    const AdjointScratch z = adjoint_scratch(T, N, P, pf->threads, std::max(1, pf->stride),
+                                             pr->precision == LMM_PRECISION_MIXED);
     pf->br.resize(pf->conc);
     for (auto& b : pf->br) {
         if (!rc) rc = cudaStreamCreateWithFlags(&b.stream, cudaStreamNonBlocking) == cudaSuccess ? 0 : fail(LMM_ERR_CUDA, "stream");
@@ -1340,8 +1370,10 @@ int lmm_portfolio_create(lmm_process* pr, const lmm_portfolio_desc* desc, lmm_po
             if (!rc) rc = dalloc(&b.abar_partials, (size_t)sb * (N + 1), s);
             if (!rc) rc = dalloc(&b.value_partials, (size_t)sb, s);
             if (!rc) rc = dalloc(&b.value_out, (size_t)1, s);
-            if (!rc) rc = dalloc(&b.vega_partials, (size_t)ablocks * T * N, s);
-            if (!rc) rc = dalloc(&b.delta_partials, (size_t)ablocks * N, s);
+            if (!rc) rc = dalloc(&b.vega_partials, z.vega_partials, s);
+            if (!rc) rc = dalloc(&b.delta_partials, z.delta_partials, s);
+            if (!rc && z.seg_bytes) rc = dalloc(&b.seg, z.seg_bytes, s);
+            if (!rc && z.ybar_bytes) rc = dalloc(&b.ybar, z.ybar_bytes, s);
         }
     }
     if (!rc) rc = cudaEventCreateWithFlags(&pf->fork, cudaEventDisableTiming) == cudaSuccess ? 0 : fail(LMM_ERR_CUDA, "event");

@@ -98,6 +98,8 @@ struct PathLaunch {
     const double* d_delta;     // [N] period lengths
     const double* d_inv_delta; // [N] 1.0 / delta (delta/delta == 1.0 exactly for the validated tenor)
     const double* d_var_half;  // [T][N] variance * -0.5 (exact scaling)
+    const float* d_inv_delta32;// [N] 1/delta in FP32 (mixed form)
+    const float* d_dt32;       // [T] time steps in FP32 (mixed form)
     const double* d_init;      // [N] initial forwards
     const int* d_obs_slot;     // [T+1] observation slot or -1
     const void* d_dw;          // [T][F][P] fp64 or fp32
@@ -106,7 +108,7 @@ struct PathLaunch {
     double* d_inv_num_partials;// [blocks][N][2] double-double partial sums of 1/N(T_{l+1})
     int num_det_prefix;        // numeraire deterministic for l < num_det_prefix
     void* d_ckpt;              // [T/stride+1][N][P] path state every ckpt_stride steps (nullptr: none)
-    int ckpt_stride;           // state = L (FP64 EULER_FUNCTIONAL) or log L (EULER, mixed)
+    int ckpt_stride;           // forward rates L every ckpt_stride steps (in the path precision)
 };
 int launch_paths_fp64(const PathLaunch& a, cudaStream_t s, int* blocks_out);
 int launch_paths_fp32(const PathLaunch& a, const float* lam32, const float* var32, cudaStream_t s, int* blocks_out);
@@ -186,7 +188,7 @@ int bermudan_blocks(int P);
 int bermudan_gram_blocks(int P, int ne);
 
 struct AdjointLaunch {
-    int T, N, F, P, nper, stride, ckpt_is_L, callable, freeze_adjustment, fp32, T_slot, blocks;
+    int T, N, F, P, nper, stride, callable, freeze_adjustment, fp32, T_slot, blocks;
     int threads;        // adjoint threads per block (64, 128, 256)
     int t_end, n_eff;   // reverse sweep from time index t_end over components 0..n_eff-1
     double cap;
@@ -201,12 +203,23 @@ struct AdjointLaunch {
     const int* d_first;            // [T]
     const double* d_init;          // [N]
     const void* d_dw;              // [T][F][P]
-    const void* d_ckpt;            // [T/stride+1][N][P]
+    const void* d_ckpt;            // [T/stride+1][N][P] forward rates every stride steps
+    void* d_seg;                   // stride > 1: [stride+1][N][P] replayed forward rates of a segment
+    void* d_ybar;                  // stride > 1: [N][P] adjoint of log L between segments
     const void *d_lam, *d_f, *d_sigma, *d_var_half, *d_inv_delta, *d_dt;  // tables in the path precision
     double *d_abar, *d_abar_partials, *d_seeds, *d_value_partials, *d_value_out;
     double *d_vega_partials, *d_delta_partials, *d_vegas, *d_deltas;
 };
-int adjoint_blocks(int P, int threads);
+int adjoint_blocks(int P, int threads, int fp32);
+// scratch of one adjoint evaluation: per-warp partial rows and the segment buffers of stride > 1
+struct AdjointScratch {
+    int blocks, warps;
+    size_t vega_partials, delta_partials;  // doubles
+    size_t seg_bytes, ybar_bytes;
+};
+AdjointScratch adjoint_scratch(int T, int N, int P, int threads, int stride, int fp32);
+// row pitch (elements) of the factor table f[T][N][pitch] the reverse kernel reads
+int adjoint_f_pitch(int N, int F, int fp32);
 int launch_adjoint(const AdjointLaunch& a, cudaStream_t s);
 int launch_bermudan(const ProductView& v, const BermudanLaunch& a, const BermudanScratch& sc, cudaStream_t s,
                     int* launches);

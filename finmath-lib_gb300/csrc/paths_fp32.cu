@@ -52,12 +52,12 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp32_kernel(const PathLaun
             float* ck = static_cast<float*>(a.d_ckpt);
 #pragma unroll
             for (int j = 0; j < NMAX; j++)
-                if (j < N) ck[(size_t)j * P + p] = Y[j];
+                if (j < N) ck[(size_t)j * P + p] = L[j];
         }
     }
     for (int i = 0; i < a.T; i++) {
         const int first = __ldg(a.d_first + i);
-        const float dt = (float)__ldg(a.d_dt + i);
+        const float dt = __ldg(a.d_dt32 + i);
         const float* lam = lam32 + (size_t)i * N * F;
         const float* var = var32 + (size_t)i * N;
         float dw[FMAX], S[FMAX];
@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp32_kernel(const PathLaun
 #pragma unroll
         for (int j = 0; j < NMAX; j++) {
             if (j < N && j >= first) {
-                const float invd = (float)__ldg(a.d_inv_delta + j);
+                const float invd = __ldg(a.d_inv_delta32 + j);
                 const float os = __fdividef(L[j], L[j] + invd);
                 float mu = -0.5f * __ldg(var + j);
                 float diff = 0.0f;
@@ -98,7 +98,7 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp32_kernel(const PathLaun
             float* ck = static_cast<float*>(a.d_ckpt) + (size_t)((i + 1) / a.ckpt_stride) * N * P;
 #pragma unroll
             for (int j = 0; j < NMAX; j++)
-                if (j < N) ck[(size_t)j * P + p] = Y[j];
+                if (j < N) ck[(size_t)j * P + p] = L[j];
         }
     }
     // FP64 spot numeraire from the frozen fixings (as paths_fp64.cu)

@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp64_kernel(const PathLaun
             double* ck = static_cast<double*>(a.d_ckpt);
 #pragma unroll
             for (int j = 0; j < NMAX; j++)
-                if (j < N) ck[(size_t)j * P + p] = FUNCTIONAL ? L[j] : Y[FUNCTIONAL ? 0 : j];
+                if (j < N) ck[(size_t)j * P + p] = L[j];
         }
     }
 
@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp64_kernel(const PathLaun
             double* ck = static_cast<double*>(a.d_ckpt) + (size_t)((i + 1) / a.ckpt_stride) * N * P;
 #pragma unroll
             for (int j = 0; j < NMAX; j++)
-                if (j < N) ck[(size_t)j * P + p] = FUNCTIONAL ? L[j] : Y[FUNCTIONAL ? 0 : j];
+                if (j < N) ck[(size_t)j * P + p] = L[j];
         }
     }
 

@@ -16,12 +16,17 @@
 // round exactly like the reference's unfused Java arithmetic.
 #include "lmm_internal.h"
 
+#include <cmath>
+
 namespace lmm {
 namespace {
 
 constexpr int kRngThreads = 320;
 
 struct RngParams {
+    int64_t central_max;      // |m - 2^51| <= central_max  <=>  |u - 0.5| <= 0.425 for u = m 2^-52
+    uint32_t magic_tf;        // floor((2^32-1)/TF): division by the values per path
+    uint32_t magic_f;         // floor((2^32-1)/F)
     const uint32_t* seeded;   // [624]
     const uint64_t* jumps;    // [njumps][312]
     int njumps;
@@ -34,6 +39,18 @@ struct RngParams {
     const double* sqrt_dt;
     void* out;
 };
+
+// x / d and x % d for a block-uniform divisor d < 2^31 and x < 2^31, with M = floor((2^32-1)/d):
+// __umulhi(x, M) is the quotient or one less.
+__device__ __forceinline__ void divmod_u32(uint32_t x, uint32_t d, uint32_t M, uint32_t& q, uint32_t& r)
+{
+    q = __umulhi(x, M);
+    r = x - q * d;
+    if (r >= d) {
+        q++;
+        r -= d;
+    }
+}
 
 __device__ __forceinline__ uint32_t mt_temper(uint32_t y)
 {
@@ -112,13 +129,14 @@ __device__ double icdf_wichura(double p)
     return (q < 0.0) ? -v : v;
 }
 
-// FP32 evaluation of the same rational approximations (mixed-precision form).  The
-// branch test and the tail argument 1-u are formed in FP64 where they are exact.
-__device__ float icdf_wichura_f32(double p)
+// FP32 evaluation of the same rational approximations (mixed-precision form), from the
+// draw's 52-bit grid value m (u = m 2^-52): the branch test and the tail argument are
+// exact integer operations, the polynomials FP32.
+__device__ float icdf_wichura_f32(int64_t m, int64_t central_max)
 {
-    const double qd = p - 0.5;
-    if (fabs(qd) <= 0.425) {
-        const float q = (float)qd;
+    const int64_t dq = m - ((int64_t)1 << 51);
+    if ((dq < 0 ? -dq : dq) <= central_max) {
+        const float q = __ll2float_rn(dq) * 0x1.0p-52f;
         const float r = 0.180625f - q * q;
         const float num = (((((((2.5090809287301226727e+03f * r + 3.3430575583588128105e+04f) * r +
                                 6.7265770927008700853e+04f) * r + 4.5921953931549871457e+04f) * r +
@@ -130,9 +148,9 @@ __device__ float icdf_wichura_f32(double p)
                             4.2313330701600911252e+01f) * r + 1.0f);
         return __fdividef(q * num, den);
     }
-    const double rd = (qd < 0.0) ? p : 1.0 - p;
-    if (rd <= 0.0) return 0.0f;
-    float r = sqrtf(-__logf((float)rd));
+    const int64_t ri = (dq < 0) ? m : ((int64_t)1 << 52) - m;
+    if (ri <= 0) return 0.0f;
+    float r = sqrtf(-__logf(__ll2float_rn(ri) * 0x1.0p-52f));
     float v;
     if (r <= 5.0f) {
         r -= 1.6f;
@@ -155,7 +173,7 @@ __device__ float icdf_wichura_f32(double p)
                            1.48753612908506148525e-02f) * r + 1.36929880922735805310e-01f) * r +
                          5.99832206555887937690e-01f) * r + 1.0f));
     }
-    return (qd < 0.0) ? -v : v;
+    return (dq < 0) ? -v : v;
 }
 
 __global__ void __launch_bounds__(kRngThreads, 2) mt_generate_kernel(const RngParams prm)
@@ -207,6 +225,9 @@ __global__ void __launch_bounds__(kRngThreads, 2) mt_generate_kernel(const RngPa
     const int TF = prm.values_per_path;
     const int F = prm.num_factors;
     const int P = prm.num_paths;
+    const bool normals = prm.mode != 0;      // uniforms (mode 0) carry no path position
+    int64_t path0 = normals ? v0 / TF : 0;   // path of the chunk's first value
+    int tf0 = (int)(v0 - path0 * TF);        // its position within the path
     for (int64_t v = v0; v < v1; v += kMtN / 2) {
         if (tid < 227) nxt[tid] = mt_next(cur[tid + kMtM], cur[tid], cur[tid + 1]);
         __syncthreads();
@@ -221,28 +242,28 @@ __global__ void __launch_bounds__(kRngThreads, 2) mt_generate_kernel(const RngPa
             nxt[k] = mt_next(nxt[k - 227], cur[k], (k == kMtN - 1) ? nxt[0] : cur[k + 1]);
         }
         __syncthreads();
-        const int64_t path0 = v / TF;          // first path of this round (uniform)
-        const int tf0 = (int)(v - path0 * TF);
+        // first path of this round and its offset (carried from round to round: no 64-bit division)
         if (tid < kMtN / 2) {
             const int64_t vv = v + tid;
             if (vv < v1) {
                 const uint32_t w1 = mt_temper(nxt[2 * tid]);
                 const uint32_t w2 = mt_temper(nxt[2 * tid + 1]);
-                const double u = (double)(((uint64_t)(w1 >> 6) << 26) | (uint64_t)(w2 >> 6)) * 0x1.0p-52;
+                const int64_t m = (int64_t)(((uint64_t)(w1 >> 6) << 26) | (uint64_t)(w2 >> 6));  // u = m 2^-52
                 if (prm.mode == 0) {
-                    static_cast<double*>(prm.out)[vv] = u;
+                    static_cast<double*>(prm.out)[vv] = (double)m * 0x1.0p-52;
                 } else {
-                    const double q = u - 0.5;
-                    if (fabs(q) <= 0.425) {
-                        const int loc = tf0 + tid;
-                        const int tf = loc % TF;
-                        const size_t o = (size_t)tf * (size_t)P + (size_t)(path0 + loc / TF);
-                        const double sq = __ldg(prm.sqrt_dt + tf / F);
-                        if (prm.mode == 1) static_cast<double*>(prm.out)[o] = icdf_central(q) * sq;
-                        else static_cast<float*>(prm.out)[o] = icdf_wichura_f32(u) * (float)sq;
+                    const int64_t dq = m - ((int64_t)1 << 51);
+                    if ((dq < 0 ? -dq : dq) <= prm.central_max) {
+                        uint32_t po, tf, t, kf;
+                        divmod_u32((uint32_t)(tf0 + tid), (uint32_t)TF, prm.magic_tf, po, tf);
+                        divmod_u32(tf, (uint32_t)F, prm.magic_f, t, kf);
+                        const size_t o = (size_t)tf * (size_t)P + (size_t)(path0 + po);
+                        const double sq = __ldg(prm.sqrt_dt + t);
+                        if (prm.mode == 1) static_cast<double*>(prm.out)[o] = icdf_central((double)dq * 0x1.0p-52) * sq;
+                        else static_cast<float*>(prm.out)[o] = icdf_wichura_f32(m, prm.central_max) * (float)sq;
                     } else {
                         const int slot = atomicAdd(&tail_n, 1);
-                        tail_u[slot] = u;
+                        tail_u[slot] = (double)m;
                         tail_i[slot] = (short)tid;
                     }
                 }
@@ -252,14 +273,22 @@ __global__ void __launch_bounds__(kRngThreads, 2) mt_generate_kernel(const RngPa
             __syncthreads();
             const int n_tail = tail_n;
             for (int k = tid; k < n_tail; k += kRngThreads) {
-                const double u = tail_u[k];
-                const int loc = tf0 + tail_i[k];
-                const int tf = loc % TF;
-                const size_t o = (size_t)tf * (size_t)P + (size_t)(path0 + loc / TF);
-                const double sq = __ldg(prm.sqrt_dt + tf / F);
-                if (prm.mode == 1) static_cast<double*>(prm.out)[o] = icdf_wichura(u) * sq;
-                else static_cast<float*>(prm.out)[o] = icdf_wichura_f32(u) * (float)sq;
+                const int64_t m = (int64_t)tail_u[k];
+                uint32_t po, tf, t, kf;
+                divmod_u32((uint32_t)(tf0 + tail_i[k]), (uint32_t)TF, prm.magic_tf, po, tf);
+                divmod_u32(tf, (uint32_t)F, prm.magic_f, t, kf);
+                const size_t o = (size_t)tf * (size_t)P + (size_t)(path0 + po);
+                const double sq = __ldg(prm.sqrt_dt + t);
+                if (prm.mode == 1) static_cast<double*>(prm.out)[o] = icdf_wichura((double)m * 0x1.0p-52) * sq;
+                else static_cast<float*>(prm.out)[o] = icdf_wichura_f32(m, prm.central_max) * (float)sq;
             }
+        }
+        // advance the (path, value-in-path) position by the 312 values of this round
+        tf0 += kMtN / 2;
+        if (normals && tf0 >= TF) {
+            const int64_t adv = tf0 / TF;
+            path0 += adv;
+            tf0 -= (int)(adv * TF);
         }
         uint32_t* tmp = cur;
         cur = nxt;
@@ -315,6 +344,11 @@ int launch_mt_generate(const RngLaunch& a, cudaStream_t s, int* num_launches)
     prm.mode = a.mode;
     prm.sqrt_dt = a.d_sqrt_dt;
     prm.out = a.d_out;
+    prm.central_max = (int64_t)std::floor(0.425 * 4503599627370496.0);  // exact: 0.425 scaled by 2^52
+    prm.magic_tf = a.values_per_path > 0 ? 0xFFFFFFFFu / (uint32_t)a.values_per_path : 0u;
+    prm.magic_f = a.num_factors > 0 ? 0xFFFFFFFFu / (uint32_t)a.num_factors : 0u;
+    if (a.mode != 0 && (a.values_per_path <= 0 || a.num_factors <= 0 || a.values_per_path >= (1 << 30)))
+        return fail(LMM_ERR_INVALID, "Brownian increments need 1 <= factors and values per path < 2^30");
     {
         KernelTimer kt(K_MT_JUMP_GENERATE, s);
         mt_generate_kernel<<<(unsigned)a.plan->chunks, kRngThreads, kJumpWindow * sizeof(uint32_t), s>>>(prm);

@@ -10,7 +10,7 @@ from __future__ import annotations
 import json
 import os
 
-DEFAULT = {"adjointThreads": 128, "checkpointStride": 8, "concurrency": 4, "gramBlocks": 0}
+DEFAULT = {"adjointThreads": 128, "checkpointStride": 1, "concurrency": 4, "gramBlocks": 0}
 
 
 def _cache_path():
@@ -39,7 +39,7 @@ def _store(db):
 
 
 def key(gpu_name: str, paths: int, steps: int, periods: int, factors: int, precision: int) -> str:
-    return f"{gpu_name}|P{paths}|T{steps}|N{periods}|F{factors}|prec{precision}"
+    return f"v2|{gpu_name}|P{paths}|T{steps}|N{periods}|F{factors}|prec{precision}"
 
 
 def tune(model, products, cache_key: str, subset: int = 16, force: bool = False, log=None):
@@ -65,7 +65,7 @@ def tune(model, products, cache_key: str, subset: int = 16, force: bool = False,
 
     best = dict(DEFAULT)
     best_t = measure(best)
-    trials = [("adjointThreads", [64, 256]), ("checkpointStride", [4, 16]), ("concurrency", [2, 8]),
+    trials = [("adjointThreads", [64, 256]), ("checkpointStride", [2, 8]), ("concurrency", [2, 8]),
               ("gramBlocks", [16, 64])]
     results = [(dict(best), best_t)]
     for knob, values in trials:

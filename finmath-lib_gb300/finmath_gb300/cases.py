@@ -1,7 +1,7 @@
 """Named valuation cases, run from the command line (used to profile single kernels):
 
     python -m finmath_gb300.cases --case valuation|greeks|portfolio --precision fp64|mixed \\
-        --paths 65536 --repeat 3 [--workload lmm40]
+        --paths 65536 --repeat 3 [--workload lmm40] [--stride 1] [--timing]
 
 Each repetition regenerates the increments (new seed set) and values the workload's
 Bermudan swaption; 'greeks' adds its adjoint deltas and vegas; 'portfolio' runs a
@@ -26,8 +26,13 @@ def main(argv=None):
     ap.add_argument("--paths", type=int, default=65536)
     ap.add_argument("--repeat", type=int, default=3)
     ap.add_argument("--workload", default="lmm40")
-    ap.add_argument("--stride", type=int, default=8)
+    ap.add_argument("--stride", type=int, default=1)
+    ap.add_argument("--timing", action="store_true", help="CUDA-event time per kernel family, after the first repetition")
     args = ap.parse_args(argv)
+    from ._lib import load
+    lib = load()
+    if args.timing:
+        lib.lmm_stats_enable_timing(1)
     cfg = W.WORKLOADS[args.workload]
     prec = PRECISION_MIXED if args.precision == "mixed" else PRECISION_FP64
     sim = W.build(cfg, paths=args.paths, precision=prec)
@@ -36,8 +41,10 @@ def main(argv=None):
     out = None
     if args.case == "portfolio":
         pf = F.Portfolio(sim, W.portfolio_products(cfg, n=16, seed=20261203), True, args.stride, 4, 128, 0)
-        for _ in range(args.repeat):
+        for r in range(args.repeat):
             out = pf.run()["total_ms"]
+            if r == 0:
+                lib.lmm_stats_reset()
         pf.close()
     else:
         for r in range(args.repeat):
@@ -46,6 +53,8 @@ def main(argv=None):
                 out = berm.getGradient(sim, checkpointStride=args.stride)["value"]
             else:
                 out = berm.getValue(sim)
+            if r == 0:
+                lib.lmm_stats_reset()
     print(json.dumps({"case": args.case, "precision": args.precision, "paths": args.paths, "last": out,
                       "kernels": F.kernel_stats()}))
 

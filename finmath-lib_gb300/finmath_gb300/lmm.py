@@ -433,7 +433,7 @@ class BermudanSwaption:
                                     _p(self.fixingDates), _p(self.periodLengths), _p(self.paymentDates),
                                     _p(self.periodNotionals), _p(self.swaprates), int(self.isCallable), self.basis)
 
-    def getGradient(self, model: LIBORMonteCarloSimulationFromLIBORModel, checkpointStride: int = 8,
+    def getGradient(self, model: LIBORMonteCarloSimulationFromLIBORModel, checkpointStride: int = 1,
                     freezeNumeraireAdjustment: bool = False):
         """Value, deltas d V / d L_j(0) and vegas d V / d sigma_{i,j} by the adjoint kernel
         (the role of RandomVariableDifferentiable.getGradient with these leaves)."""
@@ -453,7 +453,7 @@ class Portfolio:
     """Bermudan swaptions valued together (with deltas and vegas) on one shared simulation:
     the per-product kernels are recorded once into a CUDA graph; run() launches it."""
 
-    def __init__(self, model: LIBORMonteCarloSimulationFromLIBORModel, products, withGreeks=True, checkpointStride=8,
+    def __init__(self, model: LIBORMonteCarloSimulationFromLIBORModel, products, withGreeks=True, checkpointStride=1,
                  concurrency=4, adjointThreads=128, gramBlocks=0):
         self._L = _lib.load()
         self.model = model
