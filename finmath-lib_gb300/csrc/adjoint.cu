@@ -123,14 +123,36 @@ __device__ __forceinline__ double row_sum(const R* red, int r)
     return (double)acc;
 }
 
-// Reverse sweep over the steps [n_lo, n_hi) of every path, from stored forward rates.
-// One thread per path (grid-stride over path batches; the partition is fixed by the grid, so
-// the per-warp partial sums and their order do not depend on the checkpoint stride).
+// asynchronous 4- or 8-byte copy global -> shared (completes at cp_async_wait)
+template <typename R>
+__device__ __forceinline__ void cp_async(R* dst, const R* src)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    if (sizeof(R) == 4) asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+    else asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
 // resident warps per SM the register budget is sized for: 12 in FP32, 8 in FP64 (whose
 // arrays are twice as wide and whose FP64 pipe, not latency, bounds the sweep)
 template <typename R, int TH>
 __host__ __device__ constexpr int rev_min_blocks() { return (sizeof(R) == 4 ? 384 : 256) / TH > 0 ? (sizeof(R) == 4 ? 384 : 256) / TH : 1; }
 
+// shared memory of the reverse kernel: the warps' transpose buffers, the step buffer
+// [NMAX][TH] of one step's forward rates, and two increment buffers [2][FMAX][TH]
+template <typename R, int NMAX, int FMAX, int TH>
+__host__ __device__ constexpr size_t rev_red_bytes() { return (size_t)(TH / 32) * NMAX * red_pitch<R>() * sizeof(R); }
+template <typename R, int NMAX, int FMAX, int TH>
+__host__ __device__ constexpr size_t rev_smem_bytes() { return rev_red_bytes<R, NMAX, FMAX, TH>() + (size_t)(NMAX + 2 * FMAX) * TH * sizeof(R); }
+
+// Reverse sweep over the steps [n_lo, n_hi) of every path, from stored forward rates.
+// One thread per path (grid-stride over path batches; the partition is fixed by the grid, so
+// the per-warp partial sums and their order do not depend on the checkpoint stride).  Each
+// thread prefetches its own path's forward rates and increments of the next step into shared
+// memory (cp.async) while it works on the current step.  The copy into the rate buffer is
+// issued only after every rate of the current step has been consumed (FP32: by the forward
+// pass; FP64: by the reverse pass); the increments alternate between two buffers.
 template <typename R, int NMAX, int FMAX, int TH>
 __global__ void __launch_bounds__(TH, rev_min_blocks<R, TH>()) reverse_kernel(const RevParams a, const AdjTables<R> tb)
 {
@@ -141,6 +163,8 @@ __global__ void __launch_bounds__(TH, rev_min_blocks<R, TH>()) reverse_kernel(co
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     R* red = reinterpret_cast<R*>(smem_raw) + (size_t)warp * NMAX * RS;  // [NMAX][RS] of this warp
+    R* sbuf = reinterpret_cast<R*>(smem_raw + rev_red_bytes<R, NMAX, FMAX, TH>()) + tid;  // [NMAX][TH], own column
+    R* wbuf = sbuf + NMAX * TH;                                                            // [2][FMAX][TH], own column
     const int N = a.N, F = a.F, NE = a.n_eff;
     const size_t gw = (size_t)blockIdx.x * (TH / 32) + warp;
     double* vp = a.vega_partials + gw * a.T * N;
@@ -151,6 +175,22 @@ __global__ void __launch_bounds__(TH, rev_min_blocks<R, TH>()) reverse_kernel(co
     for (int base = blockIdx.x * TH; base < a.P; base += gridDim.x * TH) {
         const int p = base + tid;
         const bool active = p < a.P;
+        // this path's forward rates (components first..NE-1) and increments of step n
+        auto prefetch = [&](int n) {
+            if (active) {
+                const int fst = __ldg(a.first + n);
+                const R* Ls = states + (size_t)(n - a.base_step) * N * a.P + p;
+#pragma unroll
+                for (int j = 0; j < NMAX; j++)
+                    if (j < NE && j >= fst) cp_async(sbuf + j * TH, Ls + (size_t)j * a.P);
+                R* wb = wbuf + (n & 1) * FMAX * TH;
+#pragma unroll
+                for (int k = 0; k < FMAX; k++)
+                    if (k < F) cp_async(wb + k * TH, dW + ((size_t)n * F + k) * a.P + p);
+            }
+            cp_async_commit();
+        };
+        prefetch(a.n_hi - 1);
         R Ybar[NMAX];
         if (a.seed) {
             const R* Ls = states + (size_t)(a.t_end - a.base_step) * N * a.P;
@@ -172,13 +212,13 @@ __global__ void __launch_bounds__(TH, rev_min_blocks<R, TH>()) reverse_kernel(co
         for (int n = a.n_hi - 1; n >= a.n_lo; n--) {
             const int first = __ldg(a.first + n);
             const R dt = tb.dt[n];
-            const R* Ls = states + (size_t)(n - a.base_step) * N * a.P;
             const R* sig = tb.sigma + (size_t)n * N;
             const R* frow = tb.f + (size_t)n * N * FP;
+            cp_async_wait();
             R dw[FMAX], S[FMAX], Rk[FMAX];
 #pragma unroll
             for (int k = 0; k < FMAX; k++) {
-                dw[k] = (k < F && active) ? dW[((size_t)n * F + k) * a.P + p] : R(0);
+                dw[k] = (k < F && active) ? wbuf[((n & 1) * FMAX + k) * TH] : R(0);
                 S[k] = R(0);
                 Rk[k] = R(0);
             }
@@ -188,7 +228,7 @@ __global__ void __launch_bounds__(TH, rev_min_blocks<R, TH>()) reverse_kernel(co
 #pragma unroll
             for (int j = 0; j < NMAX; j++) {
                 if (j < NE && j >= first) {
-                    const R L = active ? Ls[(size_t)j * a.P + p] : R(0);
+                    const R L = active ? sbuf[j * TH] : R(0);
                     if (a.capped && L >= cap) capmask |= 1ull << j;
                     const R o = fdiv<R>(L, L + tb.inv_delta[j]);
                     if (kKeepOs) os[kKeepOs ? j : 0] = o;
@@ -201,6 +241,8 @@ __global__ void __launch_bounds__(TH, rev_min_blocks<R, TH>()) reverse_kernel(co
                         if (k < F) S[k] = S[k] + oss * fr[k];
                 }
             }
+            // the step buffer is free once the forward pass consumed it (FP32) -- fetch the next step
+            if (kKeepOs && n - 1 >= a.n_lo) prefetch(n - 1);
             // reverse pass over the components
 #pragma unroll
             for (int jj = NMAX - 1; jj >= 0; jj--) {
@@ -210,7 +252,7 @@ __global__ void __launch_bounds__(TH, rev_min_blocks<R, TH>()) reverse_kernel(co
                     if (kKeepOs) {
                         o = os[kKeepOs ? j : 0];
                     } else {
-                        const R L = active ? Ls[(size_t)j * a.P + p] : R(0);
+                        const R L = active ? sbuf[j * TH] : R(0);
                         o = fdiv<R>(L, L + tb.inv_delta[j]);
                     }
                     const R sg = sig[j];
@@ -239,6 +281,7 @@ __global__ void __launch_bounds__(TH, rev_min_blocks<R, TH>()) reverse_kernel(co
                     if (!((capmask >> j) & 1ull)) Ybar[j] = yb + (sg * A) * (o * (R(1) - o));
                 }
             }
+            if (!kKeepOs && n - 1 >= a.n_lo) prefetch(n - 1);
             __syncwarp();
 #pragma unroll
             for (int h = 0; h < (NMAX + 31) / 32; h++) {
@@ -267,6 +310,7 @@ __global__ void __launch_bounds__(TH, rev_min_blocks<R, TH>()) reverse_kernel(co
             __syncwarp();
         }
     }
+    cp_async_wait();
 }
 
 // Replays the Euler-log steps [n0, n_stop) of every path from the checkpoint at n0 (forward
@@ -343,7 +387,7 @@ struct SeedParams {
     const double* numeraire;       // [N+1][P]
     const double* adj;             // [N+1]
     const double* abar;            // [N+1] (pass 2)
-    double pd[65];
+    double inv_pd[65];             // 1 / P^d(T_l)
     unsigned char det[65];
     double delta[64];              // tenor period lengths
     const double* ex_time;         // [P]
@@ -378,19 +422,20 @@ __global__ void __launch_bounds__(256) seed_kernel(const SeedParams a)
             const double L = st<TS>(a, c.libor_slot, c.libor_index, p);
             const int l = c.pay_num_index;
             const double Nu = a.numeraire[(size_t)l * a.P + p];
-            const double Nadj = a.has_discount ? (a.det[l] ? (1.0 / a.pd[l]) * (Nu * a.adj[l]) : (Nu * a.adj[l]) / a.pd[l]) : Nu;
+            const double Nadj = a.has_discount ? (Nu * a.adj[l]) * a.inv_pd[l] : Nu;
+            const double invN = 1.0 / Nadj;  // the one division of the period
             const double A = ((L - c.strike) * c.period_length) * c.notional;
-            const double cf = A / Nadj;
+            const double cf = A * invN;
             x += cf;
-            lb[c.libor_index] += c.period_length * c.notional / Nadj;
-            if (!a.det[l]) nb[l] += -cf / Nadj;
+            lb[c.libor_index] += (c.period_length * c.notional) * invN;
+            if (!a.det[l]) nb[l] -= cf * invN;
         }
     }
     if (a.pass == 1) {
         // sum over paths of Nbar_adj,l * N_l / P^d_l: the adjoint of the adjustment a_l
         for (int l = 1; l <= a.N; l++) {
             double v = 0.0;
-            if (active && a.has_discount && !a.det[l]) v = nb[l] * a.numeraire[(size_t)l * a.P + p] / a.pd[l];
+            if (active && a.has_discount && !a.det[l]) v = (nb[l] * a.numeraire[(size_t)l * a.P + p]) * a.inv_pd[l];
             const dd s = block_dd_sum(dd{v, 0.0});
             if (threadIdx.x == 0) a.abar_partials[(size_t)blockIdx.x * (a.N + 1) + l] = s.hi + s.lo;
         }
@@ -409,8 +454,11 @@ __global__ void __launch_bounds__(256) seed_kernel(const SeedParams a)
         double t = un;
         if (a.has_discount) {
             if (!a.det[l]) {
-                t += nb[l] * a.adj[l] / a.pd[l];
-                if (!a.freeze_adjustment) t -= a.abar[l] / (Nl * Nl);
+                t += (nb[l] * a.adj[l]) * a.inv_pd[l];
+                if (!a.freeze_adjustment) {
+                    const double iN = 1.0 / Nl;
+                    t -= a.abar[l] * (iN * iN);
+                }
             }
         } else {
             t += nb[l];
@@ -444,7 +492,7 @@ __global__ void __launch_bounds__(1024) column_sum_kernel(const double* in, int 
 template <typename R, int NMAX, int FMAX, int TH>
 int launch_rev(const RevParams& a, const AdjTables<R>& tb, int blocks, cudaStream_t s)
 {
-    const size_t smem = (size_t)(TH / 32) * NMAX * red_pitch<R>() * sizeof(R);
+    const size_t smem = rev_smem_bytes<R, NMAX, FMAX, TH>();
     static bool attr_set = false;  // set once, before any stream capture
     if (!attr_set) {
         LMM_CUDA(cudaFuncSetAttribute(reverse_kernel<R, NMAX, FMAX, TH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -591,7 +639,7 @@ int launch_adjoint(const AdjointLaunch& L, cudaStream_t s)
     sp.adj = L.d_num_adj;
     sp.abar = L.d_abar;
     for (int l = 0; l <= L.N && l < 65; l++) {
-        sp.pd[l] = L.h_discount ? L.h_discount[l] : 1.0;
+        sp.inv_pd[l] = L.h_discount ? 1.0 / L.h_discount[l] : 1.0;
         sp.det[l] = L.h_num_det[l];
     }
     for (int j = 0; j < L.N && j < 64; j++) sp.delta[j] = L.h_delta[j];

@@ -165,6 +165,7 @@ struct lmm_brownian {
     uint32_t* d_seeded = nullptr;
     uint64_t* d_jumps = nullptr;
     double* d_sqrt_dt = nullptr;
+    float* d_sqrt_dt32 = nullptr;
     void* d_dw = nullptr;
     bool generated = false;
     uint64_t generation = 0;   // bumped whenever the increments change
@@ -183,7 +184,7 @@ struct lmm_process {
     // device tables
     double *d_loadings = nullptr, *d_variance = nullptr, *d_dt = nullptr, *d_delta = nullptr, *d_init = nullptr;
     double *d_inv_delta = nullptr, *d_var_half = nullptr;
-    float *d_lam32 = nullptr, *d_var32 = nullptr, *d_inv_delta32 = nullptr, *d_dt32 = nullptr;
+    float *d_lam32 = nullptr, *d_var32 = nullptr, *d_inv_delta32 = nullptr, *d_dt32 = nullptr, *d_init_log32 = nullptr;
     int *d_first = nullptr, *d_obs_slot = nullptr;
     uint8_t* d_det = nullptr;
     // results
@@ -261,6 +262,10 @@ static int brownian_ensure(lmm_brownian* b)
     LMM_CUDA(cudaMemcpyAsync(b->d_seeded, seeded, sizeof(seeded), cudaMemcpyHostToDevice, b->stream));
     if (!b->d_jumps && (rc = upload(&b->d_jumps, b->plan.polys.data(), b->plan.polys.size(), b->stream))) return rc;
     if (!b->d_sqrt_dt && (rc = upload(&b->d_sqrt_dt, sq.data(), sq.size(), b->stream))) return rc;
+    if (b->precision == LMM_PRECISION_MIXED && !b->d_sqrt_dt32) {
+        std::vector<float> sq32(sq.begin(), sq.end());
+        if ((rc = upload(&b->d_sqrt_dt32, sq32.data(), sq32.size(), b->stream))) return rc;
+    }
     const size_t esz = b->precision == LMM_PRECISION_FP64 ? sizeof(double) : sizeof(float);
     if (!b->d_dw && (rc = dalloc((unsigned char**)&b->d_dw, (size_t)values * esz, b->stream))) return rc;
     RngLaunch a;
@@ -273,6 +278,7 @@ static int brownian_ensure(lmm_brownian* b)
     a.num_factors = b->F;
     a.mode = b->precision == LMM_PRECISION_FP64 ? 1 : 2;
     a.d_sqrt_dt = b->d_sqrt_dt;
+    a.d_sqrt_dt32 = b->d_sqrt_dt32;
     a.d_out = b->d_dw;
     rc = launch_mt_generate(a, b->stream, nullptr);
     if (rc) return rc;
@@ -323,6 +329,7 @@ int lmm_brownian_destroy(lmm_brownian* b)
     dfree(b->d_seeded, b->stream);
     dfree(b->d_jumps, b->stream);
     dfree(b->d_sqrt_dt, b->stream);
+    dfree(b->d_sqrt_dt32, b->stream);
     dfree(b->d_dw, b->stream);
     cudaStreamSynchronize(b->stream);
     cudaStreamDestroy(b->stream);
@@ -360,6 +367,7 @@ int lmm_mt19937_uniforms(int64_t seed, int64_t offset, int64_t count, double* ou
         a.num_factors = 1;
         a.mode = 0;
         a.d_sqrt_dt = nullptr;
+        a.d_sqrt_dt32 = nullptr;
         a.d_out = d_out;
         rc = launch_mt_generate(a, s, nullptr);
     }
@@ -461,13 +469,15 @@ int lmm_process_create(const lmm_model_desc* m, lmm_brownian* bm, lmm_process** 
         std::vector<float> l32((size_t)T * N * F), v32((size_t)T * N);
         for (size_t i = 0; i < l32.size(); i++) l32[i] = (float)m->factor_loadings[i];
         for (size_t i = 0; i < v32.size(); i++) v32[i] = (float)m->variance[i];
-        std::vector<float> id32(N), dt32(T);
+        std::vector<float> id32(N), dt32(T), y32(N);
         for (int j = 0; j < N; j++) id32[j] = (float)inv_delta[j];
+        for (int j = 0; j < N; j++) y32[j] = (float)std::log(std::max(m->initial_forwards[j], 0.0));  // getInitialState
         for (int i = 0; i < T; i++) dt32[i] = (float)dt[i];
         rc = upload(&pr->d_lam32, l32.data(), l32.size(), s);
         if (!rc) rc = upload(&pr->d_var32, v32.data(), v32.size(), s);
         if (!rc) rc = upload(&pr->d_inv_delta32, id32.data(), id32.size(), s);
         if (!rc) rc = upload(&pr->d_dt32, dt32.data(), dt32.size(), s);
+        if (!rc) rc = upload(&pr->d_init_log32, y32.data(), y32.size(), s);
         if (!rc) rc = cudaStreamSynchronize(s) == cudaSuccess ? 0 : fail(LMM_ERR_CUDA, "stream sync");
     }
     if (!rc) rc = cudaStreamSynchronize(s) == cudaSuccess ? 0 : fail(LMM_ERR_CUDA, "stream sync");
@@ -532,6 +542,7 @@ static int process_ensure(lmm_process* pr)
     a.d_var_half = pr->d_var_half;
     a.d_inv_delta32 = pr->d_inv_delta32;
     a.d_dt32 = pr->d_dt32;
+    a.d_init_log32 = pr->d_init_log32;
     a.d_init = pr->d_init;
     a.d_obs_slot = pr->d_obs_slot;
     a.d_dw = pr->bm->d_dw;
@@ -627,6 +638,7 @@ int lmm_process_destroy(lmm_process* pr)
     dfree(pr->d_var32, s);
     dfree(pr->d_inv_delta32, s);
     dfree(pr->d_dt32, s);
+    dfree(pr->d_init_log32, s);
     dfree(pr->d_first, s);
     dfree(pr->d_det, s);
     dfree(pr->d_values, s);

@@ -82,7 +82,8 @@ struct RngLaunch {
     int num_paths;             // P (row stride of the [T*F][P] layout)
     int num_factors;           // F
     int mode;                  // 0 uniforms (double), 1 increments fp64, 2 increments fp32
-    const double* d_sqrt_dt;   // [T] (modes 1,2)
+    const double* d_sqrt_dt;   // [T] (mode 1)
+    const float* d_sqrt_dt32;  // [T] (mode 2)
     void* d_out;
 };
 int launch_mt_generate(const RngLaunch& a, cudaStream_t s, int* num_launches);
@@ -100,6 +101,7 @@ struct PathLaunch {
     const double* d_var_half;  // [T][N] variance * -0.5 (exact scaling)
     const float* d_inv_delta32;// [N] 1/delta in FP32 (mixed form)
     const float* d_dt32;       // [T] time steps in FP32 (mixed form)
+    const float* d_init_log32; // [N] log of the initial forwards in FP32 (mixed form)
     const double* d_init;      // [N] initial forwards
     const int* d_obs_slot;     // [T+1] observation slot or -1
     const void* d_dw;          // [T][F][P] fp64 or fp32

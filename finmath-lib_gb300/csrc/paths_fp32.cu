@@ -31,8 +31,7 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp32_kernel(const PathLaun
 #pragma unroll
     for (int j = 0; j < NMAX; j++) {
         if (j < N) {
-            const double f = __ldg(a.d_init + j);
-            Y[j] = (float)log(f > 0.0 ? f : 0.0);
+            Y[j] = __ldg(a.d_init_log32 + j);
             float v = __expf(Y[j]);
             if (capped && v > cap) v = cap;
             L[j] = v;
@@ -101,7 +100,11 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp32_kernel(const PathLaun
                 if (j < N) ck[(size_t)j * P + p] = L[j];
         }
     }
-    // FP64 spot numeraire from the frozen fixings (as paths_fp64.cu)
+    // FP64 spot numeraire from the frozen fixings (as paths_fp64.cu).  The block partial
+    // sums of 1/N_l for the numeraire adjustment: plain FP64 within a warp (lane order),
+    // compensated across the block's warps (warp order).
+    __shared__ double wsum[kPathThreads / 32][NMAX];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     double Nv = 1.0;
     if (active) a.d_numeraire[p] = 1.0;
 #pragma unroll
@@ -112,9 +115,20 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp32_kernel(const PathLaun
             if (l < a.num_det_prefix) Nv = Ll * (delta * Nv) + Nv;
             else Nv = Nv * (1.0 + Ll * delta);
             if (active) a.d_numeraire[(size_t)(l + 1) * P + p] = Nv;
-            const double inv = (1.0 / Nv) * 1.0;
-            block_dd_partial(active ? inv : 0.0, a.d_inv_num_partials + ((size_t)blockIdx.x * N + l) * 2);
+            double v = active ? 1.0 / Nv : 0.0;
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+            if (lane == 0) wsum[warp][l] = v;
         }
+    }
+    __syncthreads();
+    if (threadIdx.x < N) {
+        dd acc{0.0, 0.0};
+#pragma unroll
+        for (int w = 0; w < kPathThreads / 32; w++) acc = dd_add_d(acc, wsum[w][threadIdx.x]);
+        double* o = a.d_inv_num_partials + ((size_t)blockIdx.x * N + threadIdx.x) * 2;
+        o[0] = acc.hi;
+        o[1] = acc.lo;
     }
 }
 

@@ -146,7 +146,31 @@ struct BermShared {
 template <typename TS>
 __device__ void bermudan_basis(const BermShared& a, const BermudanPeriod& c, int p, double B[5])
 {
-    if (a.basis == 1) {
+    if (a.basis == 1 && sizeof(TS) == 4) {
+        // mixed form: the same par-rate recursion in FP32 (the state's precision); the basis
+        // values are widened to FP64 for the Gram accumulation and the solve
+        float H = 0.0f, prod = 1.0f;
+        const float* st = static_cast<const float*>(a.states) + (size_t)c.ex_slot * a.N * a.P + p;
+        for (int q = c.swap_first; q < c.swap_last; q++) {
+            const float Lq = st[(size_t)a.period_index[q] * a.P];
+            const float dq = (float)a.period_length[q];
+            const float g = fmaf(Lq, dq, 1.0f);
+            if (q == c.swap_first) {
+                prod = g;
+                H = dq;
+            } else {
+                prod = prod * g;
+                H = fmaf(H, g, dq);
+            }
+        }
+        const double S = (double)((prod - 1.0f) / H);
+        const double Nn = numeraire_adj(a.num, c.ex_num_index, p);
+        B[0] = S;
+        B[1] = S * S;
+        B[2] = Nn;
+        B[3] = Nn * Nn;
+        B[4] = S * Nn;
+    } else if (a.basis == 1) {
         // {S, S^2, N, N^2, S*N}: S = par rate of the remaining periods from L_j(T_ex),
         // S = (prod g_q - 1) / sum_s d_s prod_{r>s} g_r with g_q = 1 + L_q d_q, both by a
         // forward recursion (one division per path instead of one per period)

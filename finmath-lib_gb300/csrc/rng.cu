@@ -36,7 +36,8 @@ struct RngParams {
     int num_paths;
     int num_factors;
     int mode;
-    const double* sqrt_dt;
+    const double* sqrt_dt;    // mode 1
+    const float* sqrt_dt32;   // mode 2
     void* out;
 };
 
@@ -129,51 +130,47 @@ __device__ double icdf_wichura(double p)
     return (q < 0.0) ? -v : v;
 }
 
-// FP32 evaluation of the same rational approximations (mixed-precision form), from the
-// draw's 52-bit grid value m (u = m 2^-52): the branch test and the tail argument are
-// exact integer operations, the polynomials FP32.
-__device__ float icdf_wichura_f32(int64_t m, int64_t central_max)
+// FP32 evaluation of the same rational approximations (mixed-precision form).  The draw
+// u = (hi 2^26 + lo) 2^-52 is handled in 32-bit pieces: q = u - 1/2 = (dh 2^26 + lo) 2^-52
+// with dh = hi - 2^25, and a tail probability min(u, 1-u) from the same pieces.
+__device__ __forceinline__ float icdf_central_f32(float q)
 {
-    const int64_t dq = m - ((int64_t)1 << 51);
-    if ((dq < 0 ? -dq : dq) <= central_max) {
-        const float q = __ll2float_rn(dq) * 0x1.0p-52f;
-        const float r = 0.180625f - q * q;
-        const float num = (((((((2.5090809287301226727e+03f * r + 3.3430575583588128105e+04f) * r +
-                                6.7265770927008700853e+04f) * r + 4.5921953931549871457e+04f) * r +
-                              1.3731693765509461125e+04f) * r + 1.9715909503065514427e+03f) * r +
-                            1.3314166789178437745e+02f) * r + 3.3871328727963666080e+00f);
-        const float den = (((((((5.2264952788528545610e+03f * r + 2.8729085735721942674e+04f) * r +
-                                3.9307895800092710610e+04f) * r + 2.1213794301586595867e+04f) * r +
-                              5.3941960214247511077e+03f) * r + 6.8718700749205790830e+02f) * r +
-                            4.2313330701600911252e+01f) * r + 1.0f);
-        return __fdividef(q * num, den);
-    }
-    const int64_t ri = (dq < 0) ? m : ((int64_t)1 << 52) - m;
-    if (ri <= 0) return 0.0f;
-    float r = sqrtf(-__logf(__ll2float_rn(ri) * 0x1.0p-52f));
-    float v;
+    const float r = 0.180625f - q * q;
+    const float num = (((((((2.5090809287301226727e+03f * r + 3.3430575583588128105e+04f) * r +
+                            6.7265770927008700853e+04f) * r + 4.5921953931549871457e+04f) * r +
+                          1.3731693765509461125e+04f) * r + 1.9715909503065514427e+03f) * r +
+                        1.3314166789178437745e+02f) * r + 3.3871328727963666080e+00f);
+    const float den = (((((((5.2264952788528545610e+03f * r + 2.8729085735721942674e+04f) * r +
+                            3.9307895800092710610e+04f) * r + 2.1213794301586595867e+04f) * r +
+                          5.3941960214247511077e+03f) * r + 6.8718700749205790830e+02f) * r +
+                        4.2313330701600911252e+01f) * r + 1.0f);
+    return __fdividef(q * num, den);
+}
+
+// tail branch for the tail probability t = min(u, 1-u) > 0; the sign is the caller's
+__device__ __forceinline__ float icdf_tail_f32(float t)
+{
+    float r = sqrtf(-__logf(t));
     if (r <= 5.0f) {
         r -= 1.6f;
-        v = __fdividef((((((((7.74545014278341407640e-04f * r + 2.27238449892691845833e-02f) * r +
-                             2.41780725177450611770e-01f) * r + 1.27045825245236838258e+00f) * r +
-                           3.64784832476320460504e+00f) * r + 5.76949722146069140550e+00f) * r +
-                         4.63033784615654529590e+00f) * r + 1.42343711074968357734e+00f),
-                       (((((((1.05075007164441684324e-09f * r + 5.47593808499534494600e-04f) * r +
-                             1.51986665636164571966e-02f) * r + 1.48103976427480074590e-01f) * r +
-                           6.89767334985100004550e-01f) * r + 1.67638483018380384940e+00f) * r +
-                         2.05319162663775882187e+00f) * r + 1.0f));
-    } else {
-        r -= 5.0f;
-        v = __fdividef((((((((2.01033439929228813265e-07f * r + 2.71155556874348757815e-05f) * r +
-                             1.24266094738807843860e-03f) * r + 2.65321895265761230930e-02f) * r +
-                           2.96560571828504891230e-01f) * r + 1.78482653991729133580e+00f) * r +
-                         5.46378491116411436990e+00f) * r + 6.65790464350110377720e+00f),
-                       (((((((2.04426310338993978564e-15f * r + 1.42151175831644588870e-07f) * r +
-                             1.84631831751005468180e-05f) * r + 7.86869131145613259100e-04f) * r +
-                           1.48753612908506148525e-02f) * r + 1.36929880922735805310e-01f) * r +
-                         5.99832206555887937690e-01f) * r + 1.0f));
+        return __fdividef((((((((7.74545014278341407640e-04f * r + 2.27238449892691845833e-02f) * r +
+                                2.41780725177450611770e-01f) * r + 1.27045825245236838258e+00f) * r +
+                              3.64784832476320460504e+00f) * r + 5.76949722146069140550e+00f) * r +
+                            4.63033784615654529590e+00f) * r + 1.42343711074968357734e+00f),
+                          (((((((1.05075007164441684324e-09f * r + 5.47593808499534494600e-04f) * r +
+                                1.51986665636164571966e-02f) * r + 1.48103976427480074590e-01f) * r +
+                              6.89767334985100004550e-01f) * r + 1.67638483018380384940e+00f) * r +
+                            2.05319162663775882187e+00f) * r + 1.0f));
     }
-    return (dq < 0) ? -v : v;
+    r -= 5.0f;
+    return __fdividef((((((((2.01033439929228813265e-07f * r + 2.71155556874348757815e-05f) * r +
+                            1.24266094738807843860e-03f) * r + 2.65321895265761230930e-02f) * r +
+                          2.96560571828504891230e-01f) * r + 1.78482653991729133580e+00f) * r +
+                        5.46378491116411436990e+00f) * r + 6.65790464350110377720e+00f),
+                      (((((((2.04426310338993978564e-15f * r + 1.42151175831644588870e-07f) * r +
+                            1.84631831751005468180e-05f) * r + 7.86869131145613259100e-04f) * r +
+                          1.48753612908506148525e-02f) * r + 1.36929880922735805310e-01f) * r +
+                        5.99832206555887937690e-01f) * r + 1.0f));
 }
 
 __global__ void __launch_bounds__(kRngThreads, 2) mt_generate_kernel(const RngParams prm)
@@ -219,7 +216,7 @@ __global__ void __launch_bounds__(kRngThreads, 2) mt_generate_kernel(const RngPa
     uint32_t* cur = x;
     uint32_t* nxt = x + kMtN;
     // tail draws of a round, processed by consecutive lanes after the central ones
-    __shared__ double tail_u[kMtN / 2];
+    __shared__ unsigned long long tail_w[kMtN / 2];
     __shared__ short tail_i[kMtN / 2];
     __shared__ int tail_n;
     const int TF = prm.values_per_path;
@@ -242,45 +239,78 @@ __global__ void __launch_bounds__(kRngThreads, 2) mt_generate_kernel(const RngPa
             nxt[k] = mt_next(nxt[k - 227], cur[k], (k == kMtN - 1) ? nxt[0] : cur[k + 1]);
         }
         __syncthreads();
-        // first path of this round and its offset (carried from round to round: no 64-bit division)
-        if (tid < kMtN / 2) {
-            const int64_t vv = v + tid;
-            if (vv < v1) {
-                const uint32_t w1 = mt_temper(nxt[2 * tid]);
-                const uint32_t w2 = mt_temper(nxt[2 * tid + 1]);
-                const int64_t m = (int64_t)(((uint64_t)(w1 >> 6) << 26) | (uint64_t)(w2 >> 6));  // u = m 2^-52
-                if (prm.mode == 0) {
-                    static_cast<double*>(prm.out)[vv] = (double)m * 0x1.0p-52;
+        if (prm.mode == 2) {
+            // FP32 increments: 32-bit integer and FP32 arithmetic only
+            if (tid < kMtN / 2 && v + tid < v1) {
+                const uint32_t hi = mt_temper(nxt[2 * tid]) >> 6;   // u = (hi 2^26 + lo) 2^-52
+                const uint32_t lo = mt_temper(nxt[2 * tid + 1]) >> 6;
+                const int dh = (int)hi - (1 << 25);
+                const float q = fmaf((float)lo, 0x1.0p-52f, (float)dh * 0x1.0p-26f);
+                if (fabsf(q) <= 0.425f) {
+                    uint32_t po, tf, t, kf;
+                    divmod_u32((uint32_t)(tf0 + tid), (uint32_t)TF, prm.magic_tf, po, tf);
+                    divmod_u32(tf, (uint32_t)F, prm.magic_f, t, kf);
+                    static_cast<float*>(prm.out)[(size_t)tf * (size_t)P + (size_t)(path0 + po)] =
+                        icdf_central_f32(q) * __ldg(prm.sqrt_dt32 + t);
                 } else {
-                    const int64_t dq = m - ((int64_t)1 << 51);
-                    if ((dq < 0 ? -dq : dq) <= prm.central_max) {
-                        uint32_t po, tf, t, kf;
-                        divmod_u32((uint32_t)(tf0 + tid), (uint32_t)TF, prm.magic_tf, po, tf);
-                        divmod_u32(tf, (uint32_t)F, prm.magic_f, t, kf);
-                        const size_t o = (size_t)tf * (size_t)P + (size_t)(path0 + po);
-                        const double sq = __ldg(prm.sqrt_dt + t);
-                        if (prm.mode == 1) static_cast<double*>(prm.out)[o] = icdf_central((double)dq * 0x1.0p-52) * sq;
-                        else static_cast<float*>(prm.out)[o] = icdf_wichura_f32(m, prm.central_max) * (float)sq;
-                    } else {
-                        const int slot = atomicAdd(&tail_n, 1);
-                        tail_u[slot] = (double)m;
-                        tail_i[slot] = (short)tid;
-                    }
+                    const int slot = atomicAdd(&tail_n, 1);
+                    tail_w[slot] = ((unsigned long long)hi << 32) | lo;
+                    tail_i[slot] = (short)tid;
                 }
             }
-        }
-        if (prm.mode != 0) {
             __syncthreads();
             const int n_tail = tail_n;
             for (int k = tid; k < n_tail; k += kRngThreads) {
-                const int64_t m = (int64_t)tail_u[k];
+                const unsigned long long w = tail_w[k];
+                const uint32_t hi = (uint32_t)(w >> 32), lo = (uint32_t)w;
+                const bool lower = hi < (1u << 25);
+                // min(u, 1-u): u itself below 1/2; 1-u = ((2^26-1-hi) 2^26 + (2^26-lo)) 2^-52 above
+                const float tp = lower ? fmaf((float)lo, 0x1.0p-52f, (float)hi * 0x1.0p-26f)
+                                       : fmaf((float)((1u << 26) - lo), 0x1.0p-52f, (float)((1u << 26) - 1u - hi) * 0x1.0p-26f);
+                float x = tp > 0.0f ? icdf_tail_f32(tp) : 0.0f;
+                if (lower) x = -x;
                 uint32_t po, tf, t, kf;
                 divmod_u32((uint32_t)(tf0 + tail_i[k]), (uint32_t)TF, prm.magic_tf, po, tf);
                 divmod_u32(tf, (uint32_t)F, prm.magic_f, t, kf);
-                const size_t o = (size_t)tf * (size_t)P + (size_t)(path0 + po);
-                const double sq = __ldg(prm.sqrt_dt + t);
-                if (prm.mode == 1) static_cast<double*>(prm.out)[o] = icdf_wichura((double)m * 0x1.0p-52) * sq;
-                else static_cast<float*>(prm.out)[o] = icdf_wichura_f32(m, prm.central_max) * (float)sq;
+                static_cast<float*>(prm.out)[(size_t)tf * (size_t)P + (size_t)(path0 + po)] = x * __ldg(prm.sqrt_dt32 + t);
+            }
+        } else {
+            if (tid < kMtN / 2) {
+                const int64_t vv = v + tid;
+                if (vv < v1) {
+                    const uint32_t w1 = mt_temper(nxt[2 * tid]);
+                    const uint32_t w2 = mt_temper(nxt[2 * tid + 1]);
+                    const int64_t m = (int64_t)(((uint64_t)(w1 >> 6) << 26) | (uint64_t)(w2 >> 6));  // u = m 2^-52
+                    if (prm.mode == 0) {
+                        static_cast<double*>(prm.out)[vv] = (double)m * 0x1.0p-52;
+                    } else {
+                        // exact FP64 increments: |u - 1/2| <= 0.425 tested on the integer grid
+                        const int64_t dq = m - ((int64_t)1 << 51);
+                        if ((dq < 0 ? -dq : dq) <= prm.central_max) {
+                            uint32_t po, tf, t, kf;
+                            divmod_u32((uint32_t)(tf0 + tid), (uint32_t)TF, prm.magic_tf, po, tf);
+                            divmod_u32(tf, (uint32_t)F, prm.magic_f, t, kf);
+                            const size_t o = (size_t)tf * (size_t)P + (size_t)(path0 + po);
+                            static_cast<double*>(prm.out)[o] = icdf_central((double)dq * 0x1.0p-52) * __ldg(prm.sqrt_dt + t);
+                        } else {
+                            const int slot = atomicAdd(&tail_n, 1);
+                            tail_w[slot] = (unsigned long long)m;
+                            tail_i[slot] = (short)tid;
+                        }
+                    }
+                }
+            }
+            if (prm.mode == 1) {
+                __syncthreads();
+                const int n_tail = tail_n;
+                for (int k = tid; k < n_tail; k += kRngThreads) {
+                    const int64_t m = (int64_t)tail_w[k];
+                    uint32_t po, tf, t, kf;
+                    divmod_u32((uint32_t)(tf0 + tail_i[k]), (uint32_t)TF, prm.magic_tf, po, tf);
+                    divmod_u32(tf, (uint32_t)F, prm.magic_f, t, kf);
+                    const size_t o = (size_t)tf * (size_t)P + (size_t)(path0 + po);
+                    static_cast<double*>(prm.out)[o] = icdf_wichura((double)m * 0x1.0p-52) * __ldg(prm.sqrt_dt + t);
+                }
             }
         }
         // advance the (path, value-in-path) position by the 312 values of this round
@@ -343,10 +373,12 @@ int launch_mt_generate(const RngLaunch& a, cudaStream_t s, int* num_launches)
     prm.num_factors = a.num_factors;
     prm.mode = a.mode;
     prm.sqrt_dt = a.d_sqrt_dt;
+    prm.sqrt_dt32 = a.d_sqrt_dt32;
     prm.out = a.d_out;
     prm.central_max = (int64_t)std::floor(0.425 * 4503599627370496.0);  // exact: 0.425 scaled by 2^52
     prm.magic_tf = a.values_per_path > 0 ? 0xFFFFFFFFu / (uint32_t)a.values_per_path : 0u;
     prm.magic_f = a.num_factors > 0 ? 0xFFFFFFFFu / (uint32_t)a.num_factors : 0u;
+    if (a.mode == 2 && !a.d_sqrt_dt32) return fail(LMM_ERR_INVALID, "FP32 increments need the FP32 step table");
     if (a.mode != 0 && (a.values_per_path <= 0 || a.num_factors <= 0 || a.values_per_path >= (1 << 30)))
         return fail(LMM_ERR_INVALID, "Brownian increments need 1 <= factors and values per path < 2^30");
     {
