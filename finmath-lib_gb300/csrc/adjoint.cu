@@ -123,6 +123,19 @@ __device__ __forceinline__ double row_sum(const R* red, int r)
     return (double)acc;
 }
 
+// FP32 sweeps stage each step's factor table in shared memory; FP64 ones read it from L1/L2
+template <typename R>
+__host__ __device__ constexpr bool rev_stage_tables() { return sizeof(R) == 4; }
+
+// one 16-byte vector of a factor row (shared memory when staged, else the read-only path)
+template <typename R>
+__device__ __forceinline__ typename Vec<R>::T load_row(const R* row, int q)
+{
+    const typename Vec<R>::T* v = reinterpret_cast<const typename Vec<R>::T*>(row) + q;
+    if (rev_stage_tables<R>()) return *v;
+    return __ldg(v);
+}
+
 // asynchronous 4- or 8-byte copy global -> shared (completes at cp_async_wait)
 template <typename R>
 __device__ __forceinline__ void cp_async(R* dst, const R* src)
@@ -130,6 +143,11 @@ __device__ __forceinline__ void cp_async(R* dst, const R* src)
     const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
     if (sizeof(R) == 4) asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
     else asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async16(void* dst, const void* src)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
@@ -140,11 +158,18 @@ template <typename R, int TH>
 __host__ __device__ constexpr int rev_min_blocks() { return (sizeof(R) == 4 ? 384 : 256) / TH > 0 ? (sizeof(R) == 4 ? 384 : 256) / TH : 1; }
 
 // shared memory of the reverse kernel: the warps' transpose buffers, the step buffer
-// [NMAX][TH] of one step's forward rates, and two increment buffers [2][FMAX][TH]
+// [NMAX][TH] of one step's forward rates, two increment buffers [2][FMAX][TH], and (FP32)
+// per warp two copies of a step's factor rows and volatilities [2][NMAX*pitch + NMAX]
+template <typename R, int NMAX, int FMAX>
+__host__ __device__ constexpr int rev_table_elems() { return NMAX * f_pitch<R, FMAX>() + NMAX; }
 template <typename R, int NMAX, int FMAX, int TH>
 __host__ __device__ constexpr size_t rev_red_bytes() { return (size_t)(TH / 32) * NMAX * red_pitch<R>() * sizeof(R); }
 template <typename R, int NMAX, int FMAX, int TH>
-__host__ __device__ constexpr size_t rev_smem_bytes() { return rev_red_bytes<R, NMAX, FMAX, TH>() + (size_t)(NMAX + 2 * FMAX) * TH * sizeof(R); }
+__host__ __device__ constexpr size_t rev_smem_bytes()
+{
+    return rev_red_bytes<R, NMAX, FMAX, TH>() + (size_t)(NMAX + 2 * FMAX) * TH * sizeof(R) +
+           (rev_stage_tables<R>() ? (size_t)(TH / 32) * 2 * rev_table_elems<R, NMAX, FMAX>() * sizeof(R) : 0);
+}
 
 // Reverse sweep over the steps [n_lo, n_hi) of every path, from stored forward rates.
 // One thread per path (grid-stride over path batches; the partition is fixed by the grid, so
@@ -152,7 +177,10 @@ __host__ __device__ constexpr size_t rev_smem_bytes() { return rev_red_bytes<R, 
 // thread prefetches its own path's forward rates and increments of the next step into shared
 // memory (cp.async) while it works on the current step.  The copy into the rate buffer is
 // issued only after every rate of the current step has been consumed (FP32: by the forward
-// pass; FP64: by the reverse pass); the increments alternate between two buffers.
+// pass; FP64: by the reverse pass); the increments alternate between two buffers.  In FP32
+// each warp also stages the next step's factor rows and volatilities (16-byte copies by its
+// lanes, two buffers), read back as broadcast shared-memory vectors.  The per-warp partial
+// sums are fire-and-forget reductions (one lane per entry, so their order is program order).
 template <typename R, int NMAX, int FMAX, int TH>
 __global__ void __launch_bounds__(TH, rev_min_blocks<R, TH>()) reverse_kernel(const RevParams a, const AdjTables<R> tb)
 {
@@ -165,6 +193,9 @@ __global__ void __launch_bounds__(TH, rev_min_blocks<R, TH>()) reverse_kernel(co
     R* red = reinterpret_cast<R*>(smem_raw) + (size_t)warp * NMAX * RS;  // [NMAX][RS] of this warp
     R* sbuf = reinterpret_cast<R*>(smem_raw + rev_red_bytes<R, NMAX, FMAX, TH>()) + tid;  // [NMAX][TH], own column
     R* wbuf = sbuf + NMAX * TH;                                                            // [2][FMAX][TH], own column
+    constexpr int TE_ = rev_table_elems<R, NMAX, FMAX>();
+    R* tbuf = reinterpret_cast<R*>(smem_raw + rev_red_bytes<R, NMAX, FMAX, TH>()) + (NMAX + 2 * FMAX) * TH +
+              (size_t)warp * 2 * TE_;                                                      // [2][NMAX*FP + NMAX] of this warp
     const int N = a.N, F = a.F, NE = a.n_eff;
     const size_t gw = (size_t)blockIdx.x * (TH / 32) + warp;
     double* vp = a.vega_partials + gw * a.T * N;
@@ -175,8 +206,16 @@ __global__ void __launch_bounds__(TH, rev_min_blocks<R, TH>()) reverse_kernel(co
     for (int base = blockIdx.x * TH; base < a.P; base += gridDim.x * TH) {
         const int p = base + tid;
         const bool active = p < a.P;
-        // this path's forward rates (components first..NE-1) and increments of step n
+        // this path's forward rates (components first..NE-1) and increments of step n, and
+        // (FP32) the warp's copy of the step's factor rows and volatilities
         auto prefetch = [&](int n) {
+            if (rev_stage_tables<R>()) {
+                R* tb_dst = tbuf + (n & 1) * TE_;
+                const R* fsrc = tb.f + (size_t)n * N * FP;
+                constexpr int kVec = 16 / sizeof(R);
+                for (int q = lane; q < NE * FP / kVec; q += 32) cp_async16(tb_dst + q * kVec, fsrc + q * kVec);
+                for (int j = lane; j < NE; j += 32) cp_async(tb_dst + NMAX * FP + j, tb.sigma + (size_t)n * N + j);
+            }
             if (active) {
                 const int fst = __ldg(a.first + n);
                 const R* Ls = states + (size_t)(n - a.base_step) * N * a.P + p;
@@ -212,9 +251,10 @@ __global__ void __launch_bounds__(TH, rev_min_blocks<R, TH>()) reverse_kernel(co
         for (int n = a.n_hi - 1; n >= a.n_lo; n--) {
             const int first = __ldg(a.first + n);
             const R dt = tb.dt[n];
-            const R* sig = tb.sigma + (size_t)n * N;
-            const R* frow = tb.f + (size_t)n * N * FP;
             cp_async_wait();
+            if (rev_stage_tables<R>()) __syncwarp();  // the warp's staged table is visible to all its lanes
+            const R* sig = rev_stage_tables<R>() ? tbuf + (n & 1) * TE_ + NMAX * FP : tb.sigma + (size_t)n * N;
+            const R* frow = rev_stage_tables<R>() ? tbuf + (n & 1) * TE_ : tb.f + (size_t)n * N * FP;
             R dw[FMAX], S[FMAX], Rk[FMAX];
 #pragma unroll
             for (int k = 0; k < FMAX; k++) {
@@ -235,7 +275,7 @@ __global__ void __launch_bounds__(TH, rev_min_blocks<R, TH>()) reverse_kernel(co
                     const R oss = o * sig[j];
                     R fr[FP];
 #pragma unroll
-                    for (int q = 0; q < FP / V::W; q++) V::unpack(__ldg(reinterpret_cast<const typename V::T*>(frow + j * FP) + q), fr + q * V::W);
+                    for (int q = 0; q < FP / V::W; q++) V::unpack(load_row<R>(frow + j * FP, q), fr + q * V::W);
 #pragma unroll
                     for (int k = 0; k < FMAX; k++)
                         if (k < F) S[k] = S[k] + oss * fr[k];
@@ -262,7 +302,7 @@ __global__ void __launch_bounds__(TH, rev_min_blocks<R, TH>()) reverse_kernel(co
                     const R oss = o * sg;
                     R fr[FP];
 #pragma unroll
-                    for (int q = 0; q < FP / V::W; q++) V::unpack(__ldg(reinterpret_cast<const typename V::T*>(frow + j * FP) + q), fr + q * V::W);
+                    for (int q = 0; q < FP / V::W; q++) V::unpack(load_row<R>(frow + j * FP, q), fr + q * V::W);
                     R A = R(0), B = R(0), D = R(0);
 #pragma unroll
                     for (int k = 0; k < FMAX; k++) {
@@ -286,7 +326,7 @@ __global__ void __launch_bounds__(TH, rev_min_blocks<R, TH>()) reverse_kernel(co
 #pragma unroll
             for (int h = 0; h < (NMAX + 31) / 32; h++) {
                 const int r = lane + 32 * h;
-                if (r < NE && r >= first) vp[(size_t)n * N + r] += row_sum<R>(red, r);
+                if (r < NE && r >= first) atomicAdd(vp + (size_t)n * N + r, row_sum<R>(red, r));
             }
             __syncwarp();
         }
@@ -305,7 +345,7 @@ __global__ void __launch_bounds__(TH, rev_min_blocks<R, TH>()) reverse_kernel(co
 #pragma unroll
             for (int h = 0; h < (NMAX + 31) / 32; h++) {
                 const int r = lane + 32 * h;
-                if (r < NE) a.delta_partials[gw * N + r] += row_sum<R>(red, r);
+                if (r < NE) atomicAdd(a.delta_partials + gw * N + r, row_sum<R>(red, r));
             }
             __syncwarp();
         }

@@ -253,7 +253,8 @@ static int brownian_ensure(lmm_brownian* b)
     if (b->generated) return LMM_OK;
     const int64_t values = (int64_t)b->T * b->F * (int64_t)b->P;
     int rc = LMM_OK;
-    if (b->plan.chunks == 0 && (rc = plan_mt_generate(values, &b->plan))) return rc;
+    const int elem = b->precision == LMM_PRECISION_FP64 ? (int)sizeof(double) : (int)sizeof(float);
+    if (b->plan.chunks == 0 && (rc = plan_mt_generate(values, b->T * b->F, elem, &b->plan))) return rc;
     uint32_t seeded[kMtN];
     mt_seeded_state((int64_t)b->seed, seeded);  // int seed widened to long (BrownianMotionFromMersenneRandomNumbers.java:147)
     std::vector<double> sq(b->T);
@@ -352,7 +353,7 @@ int lmm_mt19937_uniforms(int64_t seed, int64_t offset, int64_t count, double* ou
     uint32_t* d_seeded = nullptr;
     uint64_t* d_jumps = nullptr;
     double* d_out = nullptr;
-    rc = plan_mt_generate(n, &plan);
+    rc = plan_mt_generate(n, 1, (int)sizeof(double), &plan);
     if (!rc) rc = upload(&d_seeded, seeded, kMtN, s);
     if (!rc) rc = upload(&d_jumps, plan.polys.data(), plan.polys.size(), s);
     if (!rc) rc = dalloc(&d_out, (size_t)n, s);

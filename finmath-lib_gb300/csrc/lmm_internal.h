@@ -64,14 +64,22 @@ void mt_seeded_state(int64_t seed, uint32_t out[kMtN]);
 const std::vector<uint64_t>& mt_jump_polynomials(uint64_t stride_words, int count);
 
 // ---------------------------------------------------------------- device launchers
+constexpr int kMaxJumps = 32;
 struct RngPlan {
     int64_t chunks = 0;
     int64_t chunk_values = 0;
     int njumps = 0;
-    std::vector<uint64_t> polys;   // [njumps][312]
+    // set-bit positions of the jump polynomials x^(2^j stride) mod phi, as 16-bit indices
+    // packed four to a word; list j starts at index bit_off[j] (a multiple of 8)
+    std::vector<uint64_t> polys;
+    int bit_off[kMaxJumps] = {};
+    int bit_cnt[kMaxJumps] = {};
+    int tile_k = 1;       // paths per increments tile
+    int smem_bytes = 0;   // dynamic shared memory of a generator block
 };
-// Chunking of a stream of num_values values (2 words each) over the resident CTAs.
-int plan_mt_generate(int64_t num_values, RngPlan* plan);
+// Chunking of a stream of num_values values (2 words each) over the resident CTAs, for
+// values_per_path increments per path of elem_bytes each (1 and 8 for plain uniforms).
+int plan_mt_generate(int64_t num_values, int values_per_path, int elem_bytes, RngPlan* plan);
 
 struct RngLaunch {
     const RngPlan* plan;

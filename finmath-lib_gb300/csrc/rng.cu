@@ -17,6 +17,7 @@
 #include "lmm_internal.h"
 
 #include <cmath>
+#include <cstring>
 
 namespace lmm {
 namespace {
@@ -28,7 +29,8 @@ struct RngParams {
     uint32_t magic_tf;        // floor((2^32-1)/TF): division by the values per path
     uint32_t magic_f;         // floor((2^32-1)/F)
     const uint32_t* seeded;   // [624]
-    const uint64_t* jumps;    // [njumps][312]
+    const uint16_t* jump_bits;  // set-bit positions of the jump polynomials (see RngPlan)
+    int bit_off[kMaxJumps], bit_cnt[kMaxJumps];
     int njumps;
     int64_t num_values;
     int64_t chunk_values;
@@ -36,6 +38,7 @@ struct RngParams {
     int num_paths;
     int num_factors;
     int mode;
+    int tile_k;               // paths per increments tile (a power of two <= 32)
     const double* sqrt_dt;    // mode 1
     const float* sqrt_dt32;   // mode 2
     void* out;
@@ -173,9 +176,164 @@ __device__ __forceinline__ float icdf_tail_f32(float t)
                         5.99832206555887937690e-01f) * r + 1.0f));
 }
 
+constexpr int kStateWords = 2 * kMtN;  // the two state buffers at the start of shared memory
+
+// nxt = one regeneration of the 624-word state cur (three dependent phases of <= 227 words)
+__device__ __forceinline__ void mt_regenerate(const uint32_t* cur, uint32_t* nxt, int tid, int* tail_n)
+{
+    if (tid < 227) nxt[tid] = mt_next(cur[tid + kMtM], cur[tid], cur[tid + 1]);
+    __syncthreads();
+    if (tid < 227) {
+        const int k = 227 + tid;
+        nxt[k] = mt_next(nxt[k - 227], cur[k], cur[k + 1]);
+    }
+    if (tid == 0) *tail_n = 0;  // every lane finished the previous round's tails before the barrier above
+    __syncthreads();
+    if (tid < 170) {
+        const int k = 454 + tid;
+        nxt[k] = mt_next(nxt[k - 227], cur[k], (k == kMtN - 1) ? nxt[0] : cur[k + 1]);
+    }
+    __syncthreads();
+}
+
+// Brownian increments dW[t*F+k][p] of the chunk [v0, v1) of the stream.  The stream runs
+// path-major (path p's T*F draws are consecutive) while the output rows are [t*F+k][P]:
+// the draws go to a shared-memory tile of K consecutive paths x T*F values, and each full
+// tile leaves as row segments of K consecutive paths (K x element size = 128 bytes when the
+// tile fits).  Column k of row r of the tile sits at k ^ (r mod K), so that both the
+// column-wise fill and the row-wise drain are free of bank conflicts.
+template <typename OutT>
+__device__ __forceinline__ void increments_loop(const RngParams& prm, uint32_t* x, int tid, int64_t v0, int64_t v1,
+                                                unsigned long long* tail_w, short* tail_i, int* tail_n)
+{
+    constexpr bool kExact = sizeof(OutT) == 8;  // FP64: the reference's arithmetic, bit for bit
+    const int TF = prm.values_per_path, F = prm.num_factors, P = prm.num_paths, K = prm.tile_k;
+    OutT* tile = reinterpret_cast<OutT*>(x + kStateWords);
+    OutT* out = static_cast<OutT*>(prm.out);
+    const int64_t ps = v0 / TF, pe = v1 / TF;
+    const int ts = (int)(v0 - ps * TF), te = (int)(v1 - pe * TF);  // chunk = [(ps, ts), (pe, te))
+    int64_t path0 = ps;  // path and position of the round's first draw
+    int tf0 = ts;
+    int64_t pt = ps;     // first path of the tile
+    const int lane = tid & 31, warp = tid >> 5;
+    const int rpp = 32 / K;  // tile rows drained per warp pass
+    const int dk = lane % K, dr = lane / K;
+    uint32_t* cur = x;
+    uint32_t* nxt = x + kMtN;
+    for (int64_t v = v0; v < v1; v += kMtN / 2) {
+        mt_regenerate(cur, nxt, tid, tail_n);
+        const int nv = (int)min((int64_t)(kMtN / 2), v1 - v);
+        OutT hv0 = OutT(0), hv1 = OutT(0);
+        int hp0 = -1, hf0 = 0, hp1 = -1, hf1 = 0;  // held draws: path offset from path0 (-1: none), row
+        if (tid < nv) {
+            const uint32_t w1 = mt_temper(nxt[2 * tid]), w2 = mt_temper(nxt[2 * tid + 1]);
+            bool central;
+            if constexpr (kExact) {
+                // |u - 1/2| <= 0.425 tested exactly on the 52-bit grid, u = m 2^-52
+                const int64_t m = (int64_t)(((uint64_t)(w1 >> 6) << 26) | (uint64_t)(w2 >> 6));
+                const int64_t dq = m - ((int64_t)1 << 51);
+                central = (dq < 0 ? -dq : dq) <= prm.central_max;
+                if (central) {
+                    hv0 = icdf_central((double)dq * 0x1.0p-52);
+                } else {
+                    const int slot = atomicAdd(tail_n, 1);
+                    tail_w[slot] = (unsigned long long)m;
+                    tail_i[slot] = (short)tid;
+                }
+            } else {
+                const uint32_t hi = w1 >> 6, lo = w2 >> 6;  // u = (hi 2^26 + lo) 2^-52
+                const float q = fmaf((float)lo, 0x1.0p-52f, (float)((int)hi - (1 << 25)) * 0x1.0p-26f);
+                central = fabsf(q) <= 0.425f;
+                if (central) {
+                    hv0 = icdf_central_f32(q);
+                } else {
+                    const int slot = atomicAdd(tail_n, 1);
+                    tail_w[slot] = ((unsigned long long)hi << 32) | lo;
+                    tail_i[slot] = (short)tid;
+                }
+            }
+            if (central) {
+                uint32_t po, tf, t, kf;
+                divmod_u32((uint32_t)(tf0 + tid), (uint32_t)TF, prm.magic_tf, po, tf);
+                divmod_u32(tf, (uint32_t)F, prm.magic_f, t, kf);
+                hv0 = hv0 * (kExact ? (OutT)__ldg(prm.sqrt_dt + t) : (OutT)__ldg(prm.sqrt_dt32 + t));
+                hp0 = (int)po;
+                hf0 = (int)tf;
+            }
+        }
+        __syncthreads();
+        const int n_tail = *tail_n;
+        if (tid < n_tail) {
+            const unsigned long long w = tail_w[tid];
+            const int src = tail_i[tid];
+            OutT val;
+            if constexpr (kExact) {
+                val = icdf_wichura((double)(int64_t)w * 0x1.0p-52);
+            } else {
+                const uint32_t hi = (uint32_t)(w >> 32), lo = (uint32_t)w;
+                const bool lower = hi < (1u << 25);
+                // min(u, 1-u): u itself below 1/2; 1-u = ((2^26-1-hi) 2^26 + (2^26-lo)) 2^-52 above
+                const float tp = lower ? fmaf((float)lo, 0x1.0p-52f, (float)hi * 0x1.0p-26f)
+                                       : fmaf((float)((1u << 26) - lo), 0x1.0p-52f, (float)((1u << 26) - 1u - hi) * 0x1.0p-26f);
+                val = tp > 0.0f ? icdf_tail_f32(tp) : 0.0f;
+                if (lower) val = -val;
+            }
+            uint32_t po, tf, t, kf;
+            divmod_u32((uint32_t)(tf0 + src), (uint32_t)TF, prm.magic_tf, po, tf);
+            divmod_u32(tf, (uint32_t)F, prm.magic_f, t, kf);
+            hv1 = val * (kExact ? (OutT)__ldg(prm.sqrt_dt + t) : (OutT)__ldg(prm.sqrt_dt32 + t));
+            hp1 = (int)po;
+            hf1 = (int)tf;
+        }
+        // place the held draws; drain the tile whenever this round reaches past it
+        uint32_t plast, tflast;
+        divmod_u32((uint32_t)(tf0 + nv - 1), (uint32_t)TF, prm.magic_tf, plast, tflast);
+        while (true) {
+            if (hp0 >= 0 && path0 + hp0 < pt + K) {
+                tile[hf0 * K + ((int)(path0 + hp0 - pt) ^ (hf0 & (K - 1)))] = hv0;
+                hp0 = -1;
+            }
+            if (hp1 >= 0 && path0 + hp1 < pt + K) {
+                tile[hf1 * K + ((int)(path0 + hp1 - pt) ^ (hf1 & (K - 1)))] = hv1;
+                hp1 = -1;
+            }
+            if (path0 + (int64_t)plast < pt + K) break;
+            __syncthreads();
+            for (int r = warp * rpp + dr; r < TF; r += (kRngThreads / 32) * rpp) {
+                const int64_t path = pt + dk;
+                if (path < P && (path > ps || r >= ts) && (path < pe || (path == pe && r < te)))
+                    out[(size_t)r * P + path] = tile[r * K + (dk ^ (r & (K - 1)))];
+            }
+            __syncthreads();
+            pt += K;
+        }
+        // advance the position by the round's 312 draws
+        tf0 += kMtN / 2;
+        if (tf0 >= TF) {
+            const int adv = tf0 / TF;
+            path0 += adv;
+            tf0 -= adv * TF;
+        }
+        uint32_t* tmp = cur;
+        cur = nxt;
+        nxt = tmp;
+    }
+    __syncthreads();
+    for (int r = warp * rpp + dr; r < TF; r += (kRngThreads / 32) * rpp) {
+        const int64_t path = pt + dk;
+        if (path < P && (path > ps || r >= ts) && (path < pe || (path == pe && r < te)))
+            out[(size_t)r * P + path] = tile[r * K + (dk ^ (r & (K - 1)))];
+    }
+}
+
 __global__ void __launch_bounds__(kRngThreads, 2) mt_generate_kernel(const RngParams prm)
 {
-    extern __shared__ uint32_t x[];  // kJumpWindow words: jump window, then 2 x 624 state buffers
+    // shared memory: the jump window (kJumpWindow words); afterwards the two state buffers
+    // (kStateWords words) followed by the increments tile
+    extern __shared__ __align__(16) uint32_t x[];
+    __shared__ unsigned long long tail_w[kMtN / 2];  // tail draws of a round, handled by consecutive lanes
+    __shared__ short tail_i[kMtN / 2];
+    __shared__ int tail_n;
     const int tid = threadIdx.x;
     const int64_t c = blockIdx.x;
     const int64_t v0 = c * prm.chunk_values;
@@ -193,18 +351,28 @@ __global__ void __launch_bounds__(kRngThreads, 2) mt_generate_kernel(const RngPa
             if (tid < 227 && n < kJumpWindow) x[n] = mt_next(x[n - 227], x[n - kMtN], x[n - kMtN + 1]);
             __syncthreads();
         }
-        const uint64_t* g = prm.jumps + (size_t)j * kPolyWords;
-        uint32_t acc0 = 0, acc1 = 0;
+        // the new state word n is the XOR over the set bits i of the polynomial of x[i + n]
+        const uint16_t* bits = prm.jump_bits + prm.bit_off[j];
+        const int cnt = prm.bit_cnt[j];
         const bool two = tid + kRngThreads < kMtN;
-        for (int q = 0; q < kPolyWords; q++) {
-            uint64_t bits = __ldg(g + q);
-            while (bits) {
-                const int b = __ffsll((long long)bits) - 1;
-                bits &= bits - 1;
-                const int i = q * 64 + b;
-                acc0 ^= x[i + tid];
-                if (two) acc1 ^= x[i + tid + kRngThreads];
+        const uint32_t* x0 = x + tid;
+        const uint32_t* x1 = x + (two ? tid + kRngThreads : tid);
+        uint32_t acc0 = 0, acc1 = 0;
+        int k = 0;
+        for (; k + 8 <= cnt; k += 8) {
+            const uint4 w = __ldg(reinterpret_cast<const uint4*>(bits + k));  // eight 16-bit positions
+            const uint32_t ww[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+            for (int h = 0; h < 4; h++) {
+                const uint32_t i0 = ww[h] & 0xffffu, i1 = ww[h] >> 16;
+                acc0 ^= x0[i0] ^ x0[i1];
+                acc1 ^= x1[i0] ^ x1[i1];
             }
+        }
+        for (; k < cnt; k++) {
+            const uint32_t i = __ldg(bits + k);
+            acc0 ^= x0[i];
+            acc1 ^= x1[i];
         }
         __syncthreads();
         x[tid] = acc0;
@@ -212,135 +380,50 @@ __global__ void __launch_bounds__(kRngThreads, 2) mt_generate_kernel(const RngPa
         __syncthreads();
     }
 
-    // ---- generate: 624 words -> 312 values per round
-    uint32_t* cur = x;
-    uint32_t* nxt = x + kMtN;
-    // tail draws of a round, processed by consecutive lanes after the central ones
-    __shared__ unsigned long long tail_w[kMtN / 2];
-    __shared__ short tail_i[kMtN / 2];
-    __shared__ int tail_n;
-    const int TF = prm.values_per_path;
-    const int F = prm.num_factors;
-    const int P = prm.num_paths;
-    const bool normals = prm.mode != 0;      // uniforms (mode 0) carry no path position
-    int64_t path0 = normals ? v0 / TF : 0;   // path of the chunk's first value
-    int tf0 = (int)(v0 - path0 * TF);        // its position within the path
-    for (int64_t v = v0; v < v1; v += kMtN / 2) {
-        if (tid < 227) nxt[tid] = mt_next(cur[tid + kMtM], cur[tid], cur[tid + 1]);
-        __syncthreads();
-        if (tid < 227) {
-            const int k = 227 + tid;
-            nxt[k] = mt_next(nxt[k - 227], cur[k], cur[k + 1]);
-        }
-        if (tid == 0) tail_n = 0;  // every lane finished the previous round's tails before the barrier above
-        __syncthreads();
-        if (tid < 170) {
-            const int k = 454 + tid;
-            nxt[k] = mt_next(nxt[k - 227], cur[k], (k == kMtN - 1) ? nxt[0] : cur[k + 1]);
-        }
-        __syncthreads();
-        if (prm.mode == 2) {
-            // FP32 increments: 32-bit integer and FP32 arithmetic only
+    if (prm.mode == 1) {
+        increments_loop<double>(prm, x, tid, v0, v1, tail_w, tail_i, &tail_n);
+    } else if (prm.mode == 2) {
+        increments_loop<float>(prm, x, tid, v0, v1, tail_w, tail_i, &tail_n);
+    } else {
+        // uniforms in stream order (contiguous stores)
+        uint32_t* cur = x;
+        uint32_t* nxt = x + kMtN;
+        for (int64_t v = v0; v < v1; v += kMtN / 2) {
+            mt_regenerate(cur, nxt, tid, &tail_n);
             if (tid < kMtN / 2 && v + tid < v1) {
-                const uint32_t hi = mt_temper(nxt[2 * tid]) >> 6;   // u = (hi 2^26 + lo) 2^-52
-                const uint32_t lo = mt_temper(nxt[2 * tid + 1]) >> 6;
-                const int dh = (int)hi - (1 << 25);
-                const float q = fmaf((float)lo, 0x1.0p-52f, (float)dh * 0x1.0p-26f);
-                if (fabsf(q) <= 0.425f) {
-                    uint32_t po, tf, t, kf;
-                    divmod_u32((uint32_t)(tf0 + tid), (uint32_t)TF, prm.magic_tf, po, tf);
-                    divmod_u32(tf, (uint32_t)F, prm.magic_f, t, kf);
-                    static_cast<float*>(prm.out)[(size_t)tf * (size_t)P + (size_t)(path0 + po)] =
-                        icdf_central_f32(q) * __ldg(prm.sqrt_dt32 + t);
-                } else {
-                    const int slot = atomicAdd(&tail_n, 1);
-                    tail_w[slot] = ((unsigned long long)hi << 32) | lo;
-                    tail_i[slot] = (short)tid;
-                }
+                const uint32_t w1 = mt_temper(nxt[2 * tid]);
+                const uint32_t w2 = mt_temper(nxt[2 * tid + 1]);
+                const int64_t m = (int64_t)(((uint64_t)(w1 >> 6) << 26) | (uint64_t)(w2 >> 6));  // u = m 2^-52
+                static_cast<double*>(prm.out)[v + tid] = (double)m * 0x1.0p-52;
             }
-            __syncthreads();
-            const int n_tail = tail_n;
-            for (int k = tid; k < n_tail; k += kRngThreads) {
-                const unsigned long long w = tail_w[k];
-                const uint32_t hi = (uint32_t)(w >> 32), lo = (uint32_t)w;
-                const bool lower = hi < (1u << 25);
-                // min(u, 1-u): u itself below 1/2; 1-u = ((2^26-1-hi) 2^26 + (2^26-lo)) 2^-52 above
-                const float tp = lower ? fmaf((float)lo, 0x1.0p-52f, (float)hi * 0x1.0p-26f)
-                                       : fmaf((float)((1u << 26) - lo), 0x1.0p-52f, (float)((1u << 26) - 1u - hi) * 0x1.0p-26f);
-                float x = tp > 0.0f ? icdf_tail_f32(tp) : 0.0f;
-                if (lower) x = -x;
-                uint32_t po, tf, t, kf;
-                divmod_u32((uint32_t)(tf0 + tail_i[k]), (uint32_t)TF, prm.magic_tf, po, tf);
-                divmod_u32(tf, (uint32_t)F, prm.magic_f, t, kf);
-                static_cast<float*>(prm.out)[(size_t)tf * (size_t)P + (size_t)(path0 + po)] = x * __ldg(prm.sqrt_dt32 + t);
-            }
-        } else {
-            if (tid < kMtN / 2) {
-                const int64_t vv = v + tid;
-                if (vv < v1) {
-                    const uint32_t w1 = mt_temper(nxt[2 * tid]);
-                    const uint32_t w2 = mt_temper(nxt[2 * tid + 1]);
-                    const int64_t m = (int64_t)(((uint64_t)(w1 >> 6) << 26) | (uint64_t)(w2 >> 6));  // u = m 2^-52
-                    if (prm.mode == 0) {
-                        static_cast<double*>(prm.out)[vv] = (double)m * 0x1.0p-52;
-                    } else {
-                        // exact FP64 increments: |u - 1/2| <= 0.425 tested on the integer grid
-                        const int64_t dq = m - ((int64_t)1 << 51);
-                        if ((dq < 0 ? -dq : dq) <= prm.central_max) {
-                            uint32_t po, tf, t, kf;
-                            divmod_u32((uint32_t)(tf0 + tid), (uint32_t)TF, prm.magic_tf, po, tf);
-                            divmod_u32(tf, (uint32_t)F, prm.magic_f, t, kf);
-                            const size_t o = (size_t)tf * (size_t)P + (size_t)(path0 + po);
-                            static_cast<double*>(prm.out)[o] = icdf_central((double)dq * 0x1.0p-52) * __ldg(prm.sqrt_dt + t);
-                        } else {
-                            const int slot = atomicAdd(&tail_n, 1);
-                            tail_w[slot] = (unsigned long long)m;
-                            tail_i[slot] = (short)tid;
-                        }
-                    }
-                }
-            }
-            if (prm.mode == 1) {
-                __syncthreads();
-                const int n_tail = tail_n;
-                for (int k = tid; k < n_tail; k += kRngThreads) {
-                    const int64_t m = (int64_t)tail_w[k];
-                    uint32_t po, tf, t, kf;
-                    divmod_u32((uint32_t)(tf0 + tail_i[k]), (uint32_t)TF, prm.magic_tf, po, tf);
-                    divmod_u32(tf, (uint32_t)F, prm.magic_f, t, kf);
-                    const size_t o = (size_t)tf * (size_t)P + (size_t)(path0 + po);
-                    static_cast<double*>(prm.out)[o] = icdf_wichura((double)m * 0x1.0p-52) * __ldg(prm.sqrt_dt + t);
-                }
-            }
+            uint32_t* tmp = cur;
+            cur = nxt;
+            nxt = tmp;
         }
-        // advance the (path, value-in-path) position by the 312 values of this round
-        tf0 += kMtN / 2;
-        if (normals && tf0 >= TF) {
-            const int64_t adv = tf0 / TF;
-            path0 += adv;
-            tf0 -= (int)(adv * TF);
-        }
-        uint32_t* tmp = cur;
-        cur = nxt;
-        nxt = tmp;
     }
 }
 
 }  // namespace
 
-int plan_mt_generate(int64_t num_values, RngPlan* plan)
+int plan_mt_generate(int64_t num_values, int values_per_path, int elem_bytes, RngPlan* plan)
 {
-    static int resident = 0;
-    if (!resident) {
-        int dev = 0, sms = 0, per_sm = 0;
-        LMM_CUDA(cudaGetDevice(&dev));
-        LMM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        LMM_CUDA(cudaFuncSetAttribute(mt_generate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      kJumpWindow * (int)sizeof(uint32_t)));
-        LMM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mt_generate_kernel, kRngThreads,
-                                                               kJumpWindow * sizeof(uint32_t)));
-        resident = sms * (per_sm > 0 ? per_sm : 1);
+    int dev = 0, sms = 0, per_sm = 0;
+    LMM_CUDA(cudaGetDevice(&dev));
+    LMM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    // the increments tile: K paths x values_per_path, K x element = 128 bytes when it fits
+    int kbytes = 128;
+    const size_t budget = 200 * 1024;
+    if (values_per_path > 1) {
+        while (kbytes > elem_bytes && (size_t)values_per_path * kbytes + kStateWords * 4 > budget) kbytes /= 2;
+        if ((size_t)values_per_path * kbytes + kStateWords * 4 > budget)
+            return fail(LMM_ERR_INVALID, "too many increments per path for the generator tile");
     }
+    plan->tile_k = values_per_path > 1 ? kbytes / elem_bytes : 1;
+    const size_t tile_bytes = values_per_path > 1 ? (size_t)values_per_path * kbytes : 0;
+    plan->smem_bytes = (int)std::max<size_t>((size_t)kJumpWindow * 4, (size_t)kStateWords * 4 + tile_bytes);
+    LMM_CUDA(cudaFuncSetAttribute(mt_generate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 210 * 1024));
+    LMM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mt_generate_kernel, kRngThreads, plan->smem_bytes));
+    const int resident = sms * (per_sm > 0 ? per_sm : 1);
     // one chunk per resident CTA, at least 4096 values per chunk
     int64_t chunks = resident;
     int64_t chunk_values = (num_values + chunks - 1) / chunks;
@@ -352,9 +435,21 @@ int plan_mt_generate(int64_t num_values, RngPlan* plan)
     plan->chunk_values = chunk_values;
     plan->njumps = njumps;
     plan->polys.clear();
+    if (njumps > kMaxJumps) return fail(LMM_ERR_INVALID, "too many generator chunks");
     if (njumps > 0) {
         const std::vector<uint64_t>& v = mt_jump_polynomials(2ull * (uint64_t)chunk_values, njumps);
-        plan->polys.assign(v.begin(), v.begin() + (size_t)njumps * kPolyWords);
+        std::vector<uint16_t> list;
+        for (int j = 0; j < njumps; j++) {
+            while (list.size() % 8) list.push_back(0);  // each list starts 16-byte aligned
+            plan->bit_off[j] = (int)list.size();
+            for (int q = 0; q < kPolyWords; q++)
+                for (int b = 0; b < 64; b++)
+                    if ((v[(size_t)j * kPolyWords + q] >> b) & 1ull) list.push_back((uint16_t)(q * 64 + b));
+            plan->bit_cnt[j] = (int)list.size() - plan->bit_off[j];
+        }
+        while (list.size() % 8) list.push_back(0);
+        plan->polys.resize(list.size() / 4);
+        std::memcpy(plan->polys.data(), list.data(), list.size() * sizeof(uint16_t));
     }
     return LMM_OK;
 }
@@ -364,8 +459,13 @@ int launch_mt_generate(const RngLaunch& a, cudaStream_t s, int* num_launches)
     if (a.num_values <= 0) return LMM_OK;
     RngParams prm;
     prm.seeded = a.d_seeded;
-    prm.jumps = a.d_jumps;
+    prm.jump_bits = reinterpret_cast<const uint16_t*>(a.d_jumps);
     prm.njumps = a.plan->njumps;
+    if (prm.njumps > kMaxJumps) return fail(LMM_ERR_INVALID, "too many generator chunks");
+    for (int j = 0; j < prm.njumps; j++) {
+        prm.bit_off[j] = a.plan->bit_off[j];
+        prm.bit_cnt[j] = a.plan->bit_cnt[j];
+    }
     prm.num_values = a.num_values;
     prm.chunk_values = a.plan->chunk_values;
     prm.values_per_path = a.values_per_path;
@@ -381,9 +481,17 @@ int launch_mt_generate(const RngLaunch& a, cudaStream_t s, int* num_launches)
     if (a.mode == 2 && !a.d_sqrt_dt32) return fail(LMM_ERR_INVALID, "FP32 increments need the FP32 step table");
     if (a.mode != 0 && (a.values_per_path <= 0 || a.num_factors <= 0 || a.values_per_path >= (1 << 30)))
         return fail(LMM_ERR_INVALID, "Brownian increments need 1 <= factors and values per path < 2^30");
+    prm.tile_k = a.plan->tile_k;
+    if (a.mode != 0) {
+        const size_t elem = a.mode == 1 ? sizeof(double) : sizeof(float);
+        const int K = a.plan->tile_k;
+        if (K < 1 || K > 32 || (K & (K - 1)) ||
+            (size_t)a.plan->smem_bytes < kStateWords * sizeof(uint32_t) + (size_t)a.values_per_path * K * elem)
+            return fail(LMM_ERR_INVALID, "generator plan does not match the increments layout");
+    }
     {
         KernelTimer kt(K_MT_JUMP_GENERATE, s);
-        mt_generate_kernel<<<(unsigned)a.plan->chunks, kRngThreads, kJumpWindow * sizeof(uint32_t), s>>>(prm);
+        mt_generate_kernel<<<(unsigned)a.plan->chunks, kRngThreads, (size_t)a.plan->smem_bytes, s>>>(prm);
         LMM_CUDA(cudaGetLastError());
     }
     if (num_launches) (*num_launches)++;
