@@ -467,8 +467,10 @@ int lmm_process_create(const lmm_model_desc* m, lmm_brownian* bm, lmm_process** 
     if (!rc) rc = upload(&pr->d_first, pr->first.data(), pr->first.size(), s);
     if (!rc) rc = upload(&pr->d_det, pr->num_det.data(), pr->num_det.size(), s);
     if (!rc && pr->precision == LMM_PRECISION_MIXED) {
-        std::vector<float> l32((size_t)T * N * F), v32((size_t)T * N);
-        for (size_t i = 0; i < l32.size(); i++) l32[i] = (float)m->factor_loadings[i];
+        const int FP = paths_fp32_pitch(N, F);
+        std::vector<float> l32((size_t)T * N * FP, 0.0f), v32((size_t)T * N);
+        for (size_t r = 0; r < (size_t)T * N; r++)
+            for (int k = 0; k < F; k++) l32[r * FP + k] = (float)m->factor_loadings[r * F + k];
         for (size_t i = 0; i < v32.size(); i++) v32[i] = (float)m->variance[i];
         std::vector<float> id32(N), dt32(T), y32(N);
         for (int j = 0; j < N; j++) id32[j] = (float)inv_delta[j];

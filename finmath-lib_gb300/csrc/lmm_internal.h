@@ -121,6 +121,8 @@ struct PathLaunch {
     int ckpt_stride;           // forward rates L every ckpt_stride steps (in the path precision)
 };
 int launch_paths_fp64(const PathLaunch& a, cudaStream_t s, int* blocks_out);
+// lam32: [T][N][paths_fp32_pitch(N, F)] FP32 loadings, zero padded beyond F; var32: [T][N]
+int paths_fp32_pitch(int N, int F);
 int launch_paths_fp32(const PathLaunch& a, const float* lam32, const float* var32, cudaStream_t s, int* blocks_out);
 int path_blocks(int P);
 

@@ -7,6 +7,13 @@
 // __fdividef).  The numeraire accrual and its adjustment sums stay FP64, as do all
 // product arithmetic and payoff sums downstream.  The error against the FP64 form is
 // measured and reported, not assumed.
+//
+// GB300 layout: one thread per path, the forward vector in registers for all steps.  Each
+// warp stages the next step's factor rows (zero padded to whole float4 vectors) and
+// variances in shared memory with cp.async while it works on the current step, and each
+// thread prefetches its own path's next increments the same way, so the step loop does
+// not wait on global memory.  The sums over factors run on paired FP32 FMAs (__ffma2_rn,
+// two factors per instruction).
 #include "lmm_internal.h"
 #include "reduce.cuh"
 
@@ -15,17 +22,61 @@ namespace {
 
 constexpr int kPathThreads = 128;
 
+// factor-row pitch of the staged loadings: FMAX rounded up to whole float4 vectors
+__host__ __device__ constexpr int row_pitch(int fmax) { return (fmax + 3) / 4 * 4; }
+
+__device__ __forceinline__ void cp_async4(float* dst, const float* src)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async16(float* dst, const float* src)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+template <int NMAX, int FMAX>
+struct Smem32 {
+    static constexpr int FP = row_pitch(FMAX);
+    static constexpr int TABLE = NMAX * FP + NMAX;  // loadings rows [NMAX][FP], then variances [NMAX]
+    float table[kPathThreads / 32][2][TABLE];       // per warp, two steps
+    float dw[2][FMAX][kPathThreads];                // per thread column, two steps
+    double wsum[kPathThreads / 32][NMAX];           // numeraire-adjustment warp sums
+};
+
 template <int NMAX, int FMAX>
 __global__ void __launch_bounds__(kPathThreads) paths_fp32_kernel(const PathLaunch a, const float* __restrict__ lam32,
                                                                   const float* __restrict__ var32)
 {
-    const int p = blockIdx.x * kPathThreads + threadIdx.x;
+    using SM = Smem32<NMAX, FMAX>;
+    constexpr int FP = SM::FP;
+    constexpr int FH = (FMAX + 1) / 2;  // factor pairs
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    SM& sm = *reinterpret_cast<SM*>(smem_raw);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int p = blockIdx.x * kPathThreads + tid;
     const bool active = p < a.P;
     const int N = a.N, F = a.F, P = a.P;
     const bool capped = !isinf(a.libor_cap);
     const float cap = capped ? (float)a.libor_cap : 0.0f;
     const float* dW = static_cast<const float*>(a.d_dw);
     float* states = static_cast<float*>(a.d_states);
+
+    // step i's loadings (pitch FP) and variances into this warp's buffer i&1, and this
+    // thread's increments into dw[i&1]
+    auto prefetch = [&](int i) {
+        float* tb = sm.table[warp][i & 1];
+        const float* ls = lam32 + (size_t)i * N * FP;
+        for (int q = lane; q < N * FP / 4; q += 32) cp_async16(tb + 4 * q, ls + 4 * q);
+        for (int j = lane; j < N; j += 32) cp_async4(tb + NMAX * FP + j, var32 + (size_t)i * N + j);
+        if (active)
+            for (int k = 0; k < F; k++) cp_async4(&sm.dw[i & 1][k][tid], dW + ((size_t)i * F + k) * P + p);
+        cp_async_commit();
+    };
+    if (a.T > 0) prefetch(0);
 
     float Y[NMAX], L[NMAX];
 #pragma unroll
@@ -57,31 +108,46 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp32_kernel(const PathLaun
     for (int i = 0; i < a.T; i++) {
         const int first = __ldg(a.d_first + i);
         const float dt = __ldg(a.d_dt32 + i);
-        const float* lam = lam32 + (size_t)i * N * F;
-        const float* var = var32 + (size_t)i * N;
-        float dw[FMAX], S[FMAX];
+        cp_async_wait();
+        __syncwarp();  // the warp's staged table of step i is visible to every lane
+        float2 dw2[FH];
 #pragma unroll
-        for (int k = 0; k < FMAX; k++) {
-            dw[k] = (k < F && active) ? dW[((size_t)i * F + k) * P + p] : 0.0f;
-            S[k] = 0.0f;
+        for (int m = 0; m < FH; m++) {
+            const int k0 = 2 * m, k1 = 2 * m + 1;
+            dw2[m].x = (k0 < F && active) ? sm.dw[i & 1][k0][tid] : 0.0f;
+            dw2[m].y = (k1 < F && k1 < FMAX && active) ? sm.dw[i & 1][k1 < FMAX ? k1 : 0][tid] : 0.0f;
         }
+        if (i + 1 < a.T) prefetch(i + 1);  // buffers (i+1)&1 were last read in step i-1
+        const float* tb = sm.table[warp][i & 1];
+        float2 S2[FH];
+#pragma unroll
+        for (int m = 0; m < FH; m++) S2[m] = make_float2(0.0f, 0.0f);
 #pragma unroll
         for (int j = 0; j < NMAX; j++) {
             if (j < N && j >= first) {
+                float lr[FP];
+#pragma unroll
+                for (int q = 0; q < FP / 4; q++) {
+                    const float4 v = *reinterpret_cast<const float4*>(tb + j * FP + 4 * q);
+                    lr[4 * q] = v.x;
+                    lr[4 * q + 1] = v.y;
+                    lr[4 * q + 2] = v.z;
+                    lr[4 * q + 3] = v.w;
+                }
                 const float invd = __ldg(a.d_inv_delta32 + j);
                 const float os = __fdividef(L[j], L[j] + invd);
-                float mu = -0.5f * __ldg(var + j);
-                float diff = 0.0f;
+                const float2 os2 = make_float2(os, os);
+                float2 mu2 = make_float2(-0.5f * tb[NMAX * FP + j], 0.0f);
+                float2 df2 = make_float2(0.0f, 0.0f);
 #pragma unroll
-                for (int k = 0; k < FMAX; k++) {
-                    if (k < F) {
-                        const float l = __ldg(lam + j * F + k);
-                        S[k] = fmaf(os, l, S[k]);
-                        mu = fmaf(S[k], l, mu);
-                        diff = fmaf(dw[k], l, diff);
-                    }
+                for (int m = 0; m < FH; m++) {
+                    // factors 2m and 2m+1 (the rows are zero padded beyond F)
+                    const float2 l2 = make_float2(lr[2 * m], lr[2 * m + 1]);
+                    S2[m] = __ffma2_rn(os2, l2, S2[m]);
+                    mu2 = __ffma2_rn(S2[m], l2, mu2);
+                    df2 = __ffma2_rn(dw2[m], l2, df2);
                 }
-                Y[j] = Y[j] + fmaf(mu, dt, diff);
+                Y[j] = Y[j] + fmaf(mu2.x + mu2.y, dt, df2.x + df2.y);
                 float v = __expf(Y[j]);
                 if (capped && v > cap) v = cap;
                 L[j] = v;
@@ -100,11 +166,10 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp32_kernel(const PathLaun
                 if (j < N) ck[(size_t)j * P + p] = L[j];
         }
     }
+    cp_async_wait();
     // FP64 spot numeraire from the frozen fixings (as paths_fp64.cu).  The block partial
     // sums of 1/N_l for the numeraire adjustment: plain FP64 within a warp (lane order),
     // compensated across the block's warps (warp order).
-    __shared__ double wsum[kPathThreads / 32][NMAX];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     double Nv = 1.0;
     if (active) a.d_numeraire[p] = 1.0;
 #pragma unroll
@@ -118,15 +183,15 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp32_kernel(const PathLaun
             double v = active ? 1.0 / Nv : 0.0;
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-            if (lane == 0) wsum[warp][l] = v;
+            if (lane == 0) sm.wsum[warp][l] = v;
         }
     }
     __syncthreads();
-    if (threadIdx.x < N) {
+    if (tid < N) {
         dd acc{0.0, 0.0};
 #pragma unroll
-        for (int w = 0; w < kPathThreads / 32; w++) acc = dd_add_d(acc, wsum[w][threadIdx.x]);
-        double* o = a.d_inv_num_partials + ((size_t)blockIdx.x * N + threadIdx.x) * 2;
+        for (int w = 0; w < kPathThreads / 32; w++) acc = dd_add_d(acc, sm.wsum[w][tid]);
+        double* o = a.d_inv_num_partials + ((size_t)blockIdx.x * N + tid) * 2;
         o[0] = acc.hi;
         o[1] = acc.lo;
     }
@@ -135,12 +200,25 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp32_kernel(const PathLaun
 template <int NMAX, int FMAX>
 int launch_t(const PathLaunch& a, const float* lam32, const float* var32, cudaStream_t s, int blocks)
 {
-    paths_fp32_kernel<NMAX, FMAX><<<blocks, kPathThreads, 0, s>>>(a, lam32, var32);
+    const size_t smem = sizeof(Smem32<NMAX, FMAX>);
+    static bool attr_set = false;  // set once, before any stream capture
+    if (!attr_set) {
+        LMM_CUDA(cudaFuncSetAttribute(paths_fp32_kernel<NMAX, FMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        attr_set = true;
+    }
+    paths_fp32_kernel<NMAX, FMAX><<<blocks, kPathThreads, smem, s>>>(a, lam32, var32);
     LMM_CUDA(cudaGetLastError());
     return LMM_OK;
 }
 
 }  // namespace
+
+int paths_fp32_pitch(int N, int F)
+{
+    if (N <= 24 && F <= 4) return row_pitch(4);
+    if (N <= 40 && F <= 10) return row_pitch(10);
+    return row_pitch(16);
+}
 
 int launch_paths_fp32(const PathLaunch& a, const float* lam32, const float* var32, cudaStream_t s, int* blocks_out)
 {
