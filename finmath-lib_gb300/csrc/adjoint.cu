@@ -425,6 +425,7 @@ struct SeedParams {
     const void* states;            // [nobs][N][P]
     int fp32;
     const double* numeraire;       // [N+1][P]
+    const double* inv_numeraire;   // [N+1][P] 1/N
     const double* adj;             // [N+1]
     const double* abar;            // [N+1] (pass 2)
     double inv_pd[65];             // 1 / P^d(T_l)
@@ -432,9 +433,12 @@ struct SeedParams {
     double delta[64];              // tenor period lengths
     const double* ex_time;         // [P]
     double* abar_partials;         // [blocks][N+1] (pass 1)
-    double* seeds;                 // [N][P] (pass 2)
+    double* seeds;                 // [N][P]: pass 1 the payoff part, pass 2 final (divided by P)
+    double* nb;                    // [N+1][P] adjoints of the adjusted numeraires (pass 1 -> 2)
     double* value_partials;        // [blocks] (pass 1): sum of the frozen-decision values
 };
+
+constexpr int kSeedThreads = 256;
 
 template <typename TS>
 __device__ __forceinline__ double st(const SeedParams& a, int slot, int j, int p)
@@ -442,45 +446,69 @@ __device__ __forceinline__ double st(const SeedParams& a, int slot, int j, int p
     return (double)static_cast<const TS*>(a.states)[((size_t)slot * a.N + j) * a.P + p];
 }
 
+// Pass 1: per path the frozen-decision cash flows cf = A / N_adj of the periods paid, their
+// adjoints to the fixings (into seeds, not yet divided by P) and to the adjusted numeraires
+// (into nb), and per block the sums over paths of cf by payment date and of the value.  With
+// N_adj = N a / P^d, the adjoint of the adjustment a_l is
+//   abar_l = sum_p nbar_l N_l / P^d_l = -(1/a_l) sum_p (cf of the periods paid at l),
+// so the per-date cash-flow sums are all pass 1 has to reduce.
+// Pass 2: the numeraire chain N_l = N_{l-1} (1 + L_{l-1} d_{l-1}) downward, and the seeds.
+// Both passes are division-free: 1/N comes from the table the path kernel kept.
 template <typename TS>
-__global__ void __launch_bounds__(256) seed_kernel(const SeedParams a)
+__global__ void __launch_bounds__(kSeedThreads) seed_kernel(const SeedParams a)
 {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ double r_adj[65];                      // P^d_l / a_l: 1/N_adj = (1/N) r_adj
+    __shared__ double wsum[kSeedThreads / 32][66];    // per warp: cash-flow sums by date, then the value
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int p = blockIdx.x * kSeedThreads + tid;
     const bool active = p < a.P;
-    double nb[65], lb[64];
-    for (int l = 0; l <= a.N; l++) nb[l] = 0.0;
-    for (int m = 0; m < a.N; m++) lb[m] = 0.0;
-    double x = 0.0;
-    if (active) {
-        const double tau = a.ex_time[p];
+    const int N = a.N, P = a.P;
+    if (a.pass == 1) {
+        for (int l = tid; l <= N; l += kSeedThreads) {
+            r_adj[l] = a.has_discount ? 1.0 / (a.adj[l] * a.inv_pd[l]) : 1.0;
+            for (int w = 0; w < kSeedThreads / 32; w++) wsum[w][l] = 0.0;
+        }
+        __syncthreads();
+        const double tau = active ? a.ex_time[p] : 0.0;
+        double x = 0.0;
         for (int q = 0; q < a.nper; q++) {
             const BermudanPeriod c = a.per[q];
             // a callable payer receives the periods from its exercise date on; a cancelable one
             // receives the periods before its exercise date
-            const bool paid = a.callable ? (c.fixing >= tau) : (c.fixing < tau);
-            if (!paid) continue;
-            const double L = st<TS>(a, c.libor_slot, c.libor_index, p);
+            const bool paid = active && (a.callable ? (c.fixing >= tau) : (c.fixing < tau));
             const int l = c.pay_num_index;
-            const double Nu = a.numeraire[(size_t)l * a.P + p];
-            const double Nadj = a.has_discount ? (Nu * a.adj[l]) * a.inv_pd[l] : Nu;
-            const double invN = 1.0 / Nadj;  // the one division of the period
-            const double A = ((L - c.strike) * c.period_length) * c.notional;
-            const double cf = A * invN;
+            double cf = 0.0;
+            if (paid) {
+                const double L = st<TS>(a, c.libor_slot, c.libor_index, p);
+                const double invN = a.inv_numeraire[(size_t)l * P + p] * r_adj[l];
+                const double A = ((L - c.strike) * c.period_length) * c.notional;
+                cf = A * invN;
+                a.seeds[(size_t)c.libor_index * P + p] += (c.period_length * c.notional) * invN;
+                if (!a.det[l]) a.nb[(size_t)l * P + p] -= cf * invN;
+            }
             x += cf;
-            lb[c.libor_index] += (c.period_length * c.notional) * invN;
-            if (!a.det[l]) nb[l] -= cf * invN;
+            double v = cf;
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+            if (lane == 0) wsum[warp][l] += v;
         }
-    }
-    if (a.pass == 1) {
-        // sum over paths of Nbar_adj,l * N_l / P^d_l: the adjoint of the adjustment a_l
-        for (int l = 1; l <= a.N; l++) {
-            double v = 0.0;
-            if (active && a.has_discount && !a.det[l]) v = (nb[l] * a.numeraire[(size_t)l * a.P + p]) * a.inv_pd[l];
-            const dd s = block_dd_sum(dd{v, 0.0});
-            if (threadIdx.x == 0) a.abar_partials[(size_t)blockIdx.x * (a.N + 1) + l] = s.hi + s.lo;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
+        if (lane == 0) wsum[warp][65] = x;
+        __syncthreads();
+        // block partials, compensated across the warps (warp order)
+        for (int l = tid; l <= N + 1; l += kSeedThreads) {
+            const int col = (l <= N) ? l : 65;
+            dd acc{0.0, 0.0};
+            for (int w = 0; w < kSeedThreads / 32; w++) acc = dd_add_d(acc, wsum[w][col]);
+            const double sum = acc.hi + acc.lo;
+            if (l <= N) {
+                const bool adjusted = a.has_discount && !a.det[l] && l >= 1;
+                a.abar_partials[(size_t)blockIdx.x * (N + 1) + l] = adjusted ? -sum / a.adj[l] : 0.0;
+            } else {
+                a.value_partials[blockIdx.x] = sum;
+            }
         }
-        const dd s = block_dd_sum(dd{active ? x : 0.0, 0.0});
-        if (threadIdx.x == 0) a.value_partials[blockIdx.x] = s.hi + s.lo;
         return;
     }
     if (!active) return;
@@ -488,28 +516,27 @@ __global__ void __launch_bounds__(256) seed_kernel(const SeedParams a)
     // them to adjoints of the unadjusted N (Nbar = Nbar_adj a / P^d - abar / N^2) and run the
     // chain N_l = N_{l-1} (1 + L_{l-1} d_{l-1}) downward, whose adjoint (un) is already
     // with respect to the unadjusted numeraire.
+    const double invP = 1.0 / (double)P;
     double un = 0.0;
-    for (int l = a.N; l >= 1; l--) {
-        const double Nl = a.numeraire[(size_t)l * a.P + p];
+    for (int l = N; l >= 1; l--) {
         double t = un;
         if (a.has_discount) {
             if (!a.det[l]) {
-                t += (nb[l] * a.adj[l]) * a.inv_pd[l];
+                t += (a.nb[(size_t)l * P + p] * a.adj[l]) * a.inv_pd[l];
                 if (!a.freeze_adjustment) {
-                    const double iN = 1.0 / Nl;
+                    const double iN = a.inv_numeraire[(size_t)l * P + p];
                     t -= a.abar[l] * (iN * iN);
                 }
             }
         } else {
-            t += nb[l];
+            t += a.nb[(size_t)l * P + p];
         }
-        const double Nprev = a.numeraire[(size_t)(l - 1) * a.P + p];
+        const double Nprev = a.numeraire[(size_t)(l - 1) * P + p];
         const double Lf = st<TS>(a, a.T_slot, l - 1, p);  // frozen fixing L_{l-1}(T_{l-1})
-        lb[l - 1] += t * Nprev * a.delta[l - 1];
+        double* sd = a.seeds + (size_t)(l - 1) * P + p;
+        *sd = (*sd + t * Nprev * a.delta[l - 1]) * invP;
         un = t * (1.0 + Lf * a.delta[l - 1]);
     }
-    const double invP = 1.0 / (double)a.P;
-    for (int m = 0; m < a.N; m++) a.seeds[(size_t)m * a.P + p] = lb[m] * invP;
 }
 
 // column sums of [rows][cols] partials in fixed order (grid: cols/32 blocks of 1024 threads)
@@ -655,6 +682,7 @@ AdjointScratch adjoint_scratch(int T, int N, int P, int threads, int stride, int
     z.delta_partials = (size_t)z.warps * N;
     const size_t esz = fp32 ? sizeof(float) : sizeof(double);
     z.seg_bytes = stride > 1 ? (size_t)(stride + 1) * N * (size_t)P * esz : 0;
+    z.nb_doubles = (size_t)(N + 1) * P;
     z.ybar_bytes = stride > 1 ? (size_t)N * (size_t)P * esz : 0;
     return z;
 }
@@ -687,17 +715,23 @@ int launch_adjoint(const AdjointLaunch& L, cudaStream_t s)
     sp.abar_partials = L.d_abar_partials;
     sp.seeds = L.d_seeds;
     sp.value_partials = L.d_value_partials;
-    const int sb = (L.P + 255) / 256;
+    sp.nb = L.d_nb;
+    sp.inv_numeraire = L.d_inv_numeraire;
+    if (!L.d_inv_numeraire || !L.d_nb) return fail(LMM_ERR_STATE, "adjoint: the simulation kept no reciprocal numeraire");
+    if (L.nper > 0 && L.N > 64) return fail(LMM_ERR_INVALID, "adjoint: at most 64 forward rates");
+    const int sb = (L.P + kSeedThreads - 1) / kSeedThreads;
     {
         KernelTimer kt(K_ADJOINT, s, 4);
+        LMM_CUDA(cudaMemsetAsync(L.d_seeds, 0, sizeof(double) * (size_t)L.N * L.P, s));
+        LMM_CUDA(cudaMemsetAsync(L.d_nb, 0, sizeof(double) * (size_t)(L.N + 1) * L.P, s));
         sp.pass = 1;
-        if (L.fp32) seed_kernel<float><<<sb, 256, 0, s>>>(sp);
-        else seed_kernel<double><<<sb, 256, 0, s>>>(sp);
+        if (L.fp32) seed_kernel<float><<<sb, kSeedThreads, 0, s>>>(sp);
+        else seed_kernel<double><<<sb, kSeedThreads, 0, s>>>(sp);
         column_sum_kernel<<<(L.N + 1 + 31) / 32, 1024, 0, s>>>(L.d_abar_partials, sb, L.N + 1, 1.0 / (double)L.P, L.d_abar);
         column_sum_kernel<<<1, 1024, 0, s>>>(L.d_value_partials, sb, 1, 1.0 / (double)L.P, L.d_value_out);
         sp.pass = 2;
-        if (L.fp32) seed_kernel<float><<<sb, 256, 0, s>>>(sp);
-        else seed_kernel<double><<<sb, 256, 0, s>>>(sp);
+        if (L.fp32) seed_kernel<float><<<sb, kSeedThreads, 0, s>>>(sp);
+        else seed_kernel<double><<<sb, kSeedThreads, 0, s>>>(sp);
         LMM_CUDA(cudaGetLastError());
     }
     // ---- reverse sweeps over the paths (per-warp partials, then fixed-order column sums)

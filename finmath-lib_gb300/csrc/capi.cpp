@@ -190,6 +190,7 @@ struct lmm_process {
     // results
     void* d_states = nullptr;
     double *d_numeraire = nullptr, *d_partials = nullptr, *d_num_adj = nullptr;
+    double* d_inv_numeraire = nullptr;  // kept for the adjoint (allocated with the checkpoints)
     int path_blocks = 0;
     bool simulated = false;
     uint64_t bm_generation = 0;  // Brownian generation the results were simulated from
@@ -213,6 +214,7 @@ struct lmm_process {
            *d_value_out = nullptr, *d_vega_partials = nullptr, *d_delta_partials = nullptr, *d_vegas = nullptr,
            *d_deltas = nullptr;
     unsigned char *d_adj_seg = nullptr, *d_adj_ybar = nullptr;  // stride > 1 segment buffers
+    double* d_adj_nb = nullptr;                                 // seed scratch [N+1][P]
     size_t adj_seg_bytes = 0, adj_ybar_bytes = 0;
 };
 
@@ -496,6 +498,7 @@ static void process_free_results(lmm_process* pr)
 {
     dfree(pr->d_states, pr->stream);
     dfree(pr->d_numeraire, pr->stream);
+    dfree(pr->d_inv_numeraire, pr->stream);
     dfree(pr->d_partials, pr->stream);
     dfree(pr->d_num_adj, pr->stream);
     dfree(pr->d_obs_slot, pr->stream);
@@ -551,6 +554,7 @@ static int process_ensure(lmm_process* pr)
     a.d_dw = pr->bm->d_dw;
     a.d_states = pr->d_states;
     a.d_numeraire = pr->d_numeraire;
+    a.d_inv_numeraire = nullptr;
     a.d_inv_num_partials = pr->d_partials;
     a.num_det_prefix = pr->num_det_prefix;
     a.d_ckpt = nullptr;
@@ -565,6 +569,8 @@ static int process_ensure(lmm_process* pr)
         }
         a.d_ckpt = pr->d_ckpt;
         a.ckpt_stride = pr->want_ckpt;
+        if (!pr->d_inv_numeraire && (rc = dalloc(&pr->d_inv_numeraire, (size_t)(pr->N + 1) * pr->P, s))) return rc;
+        a.d_inv_numeraire = pr->d_inv_numeraire;
     }
     int blocks = 0;
     rc = pr->precision == LMM_PRECISION_FP64 ? launch_paths_fp64(a, s, &blocks)
@@ -668,6 +674,7 @@ int lmm_process_destroy(lmm_process* pr)
         if (q) cudaFreeAsync(q, s);
     dfree(pr->d_adj_seg, s);
     dfree(pr->d_adj_ybar, s);
+    dfree(pr->d_adj_nb, s);
     cudaStreamSynchronize(s);
     delete pr;
     return LMM_OK;
@@ -985,6 +992,7 @@ int lmm_bermudan_get_gradient(lmm_process* pr, const lmm_bermudan_desc* d, int s
         if (!rc) rc = dalloc(&pr->d_delta_partials, z.delta_partials, s);
         if (!rc) rc = dalloc(&pr->d_vegas, (size_t)T * N, s);
         if (!rc) rc = dalloc(&pr->d_deltas, (size_t)N, s);
+        if (!rc) rc = dalloc(&pr->d_adj_nb, z.nb_doubles, s);
         if (rc) return rc;
     }
     if (z.seg_bytes > pr->adj_seg_bytes) {
@@ -1026,8 +1034,10 @@ int lmm_bermudan_get_gradient(lmm_process* pr, const lmm_bermudan_desc* d, int s
     L.d_per = pr->d_per;
     L.d_states = pr->d_states;
     L.d_numeraire = pr->d_numeraire;
+    L.d_inv_numeraire = pr->d_inv_numeraire;
     L.d_num_adj = pr->d_num_adj;
     L.d_ex = pr->d_ex;
+    L.d_nb = pr->d_adj_nb;
     L.d_first = pr->d_first;
     L.d_init = pr->d_init;
     L.d_dw = pr->bm->d_dw;
@@ -1094,6 +1104,7 @@ struct PortfolioBranch {
     double *seeds = nullptr, *abar = nullptr, *abar_partials = nullptr, *value_partials = nullptr,
            *value_out = nullptr, *vega_partials = nullptr, *delta_partials = nullptr;
     unsigned char *seg = nullptr, *ybar = nullptr;  // stride > 1 segment buffers
+    double* nb = nullptr;                           // seed scratch [N+1][P]
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
 };
@@ -1114,16 +1125,17 @@ struct lmm_portfolio {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     int max_ne = 0;
-    const void* captured[5] = {};  // process buffers the graph reads (re-recorded if any moves)
+    const void* captured[6] = {};  // process buffers the graph reads (re-recorded if any moves)
 };
 
-static void portfolio_fingerprint(const lmm_portfolio* pf, const void* out[5])
+static void portfolio_fingerprint(const lmm_portfolio* pf, const void* out[6])
 {
     out[0] = pf->pr->d_states;
     out[1] = pf->pr->d_numeraire;
     out[2] = pf->pr->d_num_adj;
     out[3] = pf->pr->d_ckpt;
     out[4] = pf->pr->bm->d_dw;
+    out[5] = pf->pr->d_inv_numeraire;
 }
 
 static int portfolio_free(lmm_portfolio* pf)
@@ -1138,6 +1150,7 @@ static int portfolio_free(lmm_portfolio* pf)
         for (double* q : bufs)
             if (q) cudaFreeAsync(q, s);
         if (b.seg) cudaFreeAsync(b.seg, s);
+        if (b.nb) cudaFreeAsync(b.nb, s);
         if (b.ybar) cudaFreeAsync(b.ybar, s);
         if (b.done) cudaEventDestroy(b.done);
         if (b.stream) cudaStreamDestroy(b.stream);
@@ -1210,6 +1223,8 @@ static int portfolio_enqueue(lmm_portfolio* pf, int q, PortfolioBranch& b)
         L.d_per = sc.d_per;
         L.d_states = pr->d_states;
         L.d_numeraire = pr->d_numeraire;
+        L.d_inv_numeraire = pr->d_inv_numeraire;
+        L.d_nb = b.nb;
         L.d_num_adj = pr->d_num_adj;
         L.d_ex = b.ex;
         L.d_first = pr->d_first;
@@ -1389,6 +1404,7 @@ int lmm_portfolio_create(lmm_process* pr, const lmm_portfolio_desc* desc, lmm_po
             if (!rc) rc = dalloc(&b.delta_partials, z.delta_partials, s);
             if (!rc && z.seg_bytes) rc = dalloc(&b.seg, z.seg_bytes, s);
             if (!rc && z.ybar_bytes) rc = dalloc(&b.ybar, z.ybar_bytes, s);
+            if (!rc) rc = dalloc(&b.nb, z.nb_doubles, s);
         }
     }
     if (!rc) rc = cudaEventCreateWithFlags(&pf->fork, cudaEventDisableTiming) == cudaSuccess ? 0 : fail(LMM_ERR_CUDA, "event");
@@ -1418,7 +1434,7 @@ int lmm_portfolio_run(lmm_portfolio* pf, double* values, double* errors, double*
     int rc = process_ensure(pr);
     if (rc) return rc;
     if (stale) LMM_CUDA(cudaStreamSynchronize(pr->stream));
-    const void* now[5];
+    const void* now[6];
     portfolio_fingerprint(pf, now);
     if (std::memcmp(now, pf->captured, sizeof(now)) != 0 && (rc = portfolio_record(pf))) return rc;
     cudaStream_t s = pf->stream;

@@ -115,6 +115,7 @@ struct PathLaunch {
     const void* d_dw;          // [T][F][P] fp64 or fp32
     void* d_states;            // [nobs][N][P] fp64 or fp32
     double* d_numeraire;       // [N+1][P] unadjusted spot numeraire
+    double* d_inv_numeraire;   // [N+1][P] its reciprocal 1/N (nullptr: not kept)
     double* d_inv_num_partials;// [blocks][N][2] double-double partial sums of 1/N(T_{l+1})
     int num_det_prefix;        // numeraire deterministic for l < num_det_prefix
     void* d_ckpt;              // [T/stride+1][N][P] path state every ckpt_stride steps (nullptr: none)
@@ -210,6 +211,7 @@ struct AdjointLaunch {
     const BermudanPeriod* d_per;   // [nper]
     const void* d_states;          // [nobs][N][P]
     const double* d_numeraire;     // [N+1][P]
+    const double* d_inv_numeraire; // [N+1][P] 1/N
     const double* d_num_adj;       // [N+1]
     const double* d_ex;            // [P] exercise time of the forward valuation
     const int* d_first;            // [T]
@@ -220,6 +222,7 @@ struct AdjointLaunch {
     void* d_ybar;                  // stride > 1: [N][P] adjoint of log L between segments
     const void *d_lam, *d_f, *d_sigma, *d_var_half, *d_inv_delta, *d_dt;  // tables in the path precision
     double *d_abar, *d_abar_partials, *d_seeds, *d_value_partials, *d_value_out;
+    double* d_nb;                  // [N+1][P] adjoints of the adjusted numeraires (scratch)
     double *d_vega_partials, *d_delta_partials, *d_vegas, *d_deltas;
 };
 int adjoint_blocks(int P, int threads, int fp32);
@@ -228,6 +231,7 @@ struct AdjointScratch {
     int blocks, warps;
     size_t vega_partials, delta_partials;  // doubles
     size_t seg_bytes, ybar_bytes;
+    size_t nb_doubles;                     // the d_nb scratch
 };
 AdjointScratch adjoint_scratch(int T, int N, int P, int threads, int stride, int fp32);
 // row pitch (elements) of the factor table f[T][N][pitch] the reverse kernel reads

@@ -172,6 +172,7 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp32_kernel(const PathLaun
     // compensated across the block's warps (warp order).
     double Nv = 1.0;
     if (active) a.d_numeraire[p] = 1.0;
+    if (a.d_inv_numeraire && active) a.d_inv_numeraire[p] = 1.0;
 #pragma unroll
     for (int l = 0; l < NMAX; l++) {
         if (l < N) {
@@ -181,6 +182,7 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp32_kernel(const PathLaun
             else Nv = Nv * (1.0 + Ll * delta);
             if (active) a.d_numeraire[(size_t)(l + 1) * P + p] = Nv;
             double v = active ? 1.0 / Nv : 0.0;
+            if (a.d_inv_numeraire && active) a.d_inv_numeraire[(size_t)(l + 1) * P + p] = v;
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
             if (lane == 0) sm.wsum[warp][l] = v;

@@ -125,6 +125,7 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp64_kernel(const PathLaun
     // the numeraire is deterministic, RandomVariableFromDoubleArray.accrue afterwards.
     double Nv = 1.0;
     if (active) a.d_numeraire[p] = 1.0;
+    if (a.d_inv_numeraire && active) a.d_inv_numeraire[p] = 1.0;
 #pragma unroll
     for (int l = 0; l < NMAX; l++) {
         if (l < N) {
@@ -134,6 +135,7 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp64_kernel(const PathLaun
             if (active) a.d_numeraire[(size_t)(l + 1) * P + p] = Nv;
             // numeraire adjustment input: mean of N(T)^-1 * N(0) (:869-874)
             const double inv = (1.0 / Nv) * 1.0;
+            if (a.d_inv_numeraire && active) a.d_inv_numeraire[(size_t)(l + 1) * P + p] = inv;
             block_dd_partial(active ? inv : 0.0, a.d_inv_num_partials + ((size_t)blockIdx.x * N + l) * 2);
         }
     }
