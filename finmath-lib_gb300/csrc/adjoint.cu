@@ -70,6 +70,22 @@ struct Vec<double> {
     static __device__ __forceinline__ void unpack(const T& v, double* o) { o[0] = v.x; o[1] = v.y; }
 };
 
+// two factors at a time: FP32 on the paired FMA (__ffma2_rn), FP64 as two scalar FMAs
+template <typename R>
+struct Pair;
+template <>
+struct Pair<float> {
+    using T = float2;
+    static __device__ __forceinline__ T mk(float x, float y) { return make_float2(x, y); }
+    static __device__ __forceinline__ T fma(T a, T b, T c) { return __ffma2_rn(a, b, c); }
+};
+template <>
+struct Pair<double> {
+    using T = double2;
+    static __device__ __forceinline__ T mk(double x, double y) { return make_double2(x, y); }
+    static __device__ __forceinline__ T fma(T a, T b, T c) { return make_double2(::fma(a.x, b.x, c.x), ::fma(a.y, b.y, c.y)); }
+};
+
 // row pitch of the factor table f[T][N][pitch]: FMAX rounded up to whole 16-byte vectors
 template <typename R, int FMAX>
 __host__ __device__ constexpr int f_pitch() { return (FMAX + Vec<R>::W - 1) / Vec<R>::W * Vec<R>::W; }
@@ -255,12 +271,17 @@ __global__ void __launch_bounds__(TH, rev_min_blocks<R, TH>()) reverse_kernel(co
             if (rev_stage_tables<R>()) __syncwarp();  // the warp's staged table is visible to all its lanes
             const R* sig = rev_stage_tables<R>() ? tbuf + (n & 1) * TE_ + NMAX * FP : tb.sigma + (size_t)n * N;
             const R* frow = rev_stage_tables<R>() ? tbuf + (n & 1) * TE_ : tb.f + (size_t)n * N * FP;
-            R dw[FMAX], S[FMAX], Rk[FMAX];
+            // factor pairs (2m, 2m+1); the factor rows are zero beyond F, so padded pairs add nothing
+            constexpr int FH = (FMAX + 1) / 2;
+            using PT = typename Pair<R>::T;
+            PT dw[FH], S[FH], Rk[FH];
 #pragma unroll
-            for (int k = 0; k < FMAX; k++) {
-                dw[k] = (k < F && active) ? wbuf[((n & 1) * FMAX + k) * TH] : R(0);
-                S[k] = R(0);
-                Rk[k] = R(0);
+            for (int m = 0; m < FH; m++) {
+                const int k0 = 2 * m, k1 = 2 * m + 1;
+                dw[m] = Pair<R>::mk((k0 < F && active) ? wbuf[((n & 1) * FMAX + k0) * TH] : R(0),
+                                    (k1 < F && active) ? wbuf[((n & 1) * FMAX + (k1 < FMAX ? k1 : 0)) * TH] : R(0));
+                S[m] = Pair<R>::mk(R(0), R(0));
+                Rk[m] = Pair<R>::mk(R(0), R(0));
             }
             // forward pass of the step: S_k = sum_j os_j sigma_j f_jk
             R os[kKeepOs ? NMAX : 1];
@@ -276,9 +297,9 @@ __global__ void __launch_bounds__(TH, rev_min_blocks<R, TH>()) reverse_kernel(co
                     R fr[FP];
 #pragma unroll
                     for (int q = 0; q < FP / V::W; q++) V::unpack(load_row<R>(frow + j * FP, q), fr + q * V::W);
+                    const PT oss2 = Pair<R>::mk(oss, oss);
 #pragma unroll
-                    for (int k = 0; k < FMAX; k++)
-                        if (k < F) S[k] = S[k] + oss * fr[k];
+                    for (int m = 0; m < FH; m++) S[m] = Pair<R>::fma(oss2, Pair<R>::mk(fr[2 * m], fr[2 * m + 1]), S[m]);
                 }
             }
             // the step buffer is free once the forward pass consumed it (FP32) -- fetch the next step
@@ -303,22 +324,23 @@ __global__ void __launch_bounds__(TH, rev_min_blocks<R, TH>()) reverse_kernel(co
                     R fr[FP];
 #pragma unroll
                     for (int q = 0; q < FP / V::W; q++) V::unpack(load_row<R>(frow + j * FP, q), fr + q * V::W);
-                    R A = R(0), B = R(0), D = R(0);
+                    const PT mubs2 = Pair<R>::mk(mubs, mubs), noss2 = Pair<R>::mk(-oss, -oss);
+                    PT A2 = Pair<R>::mk(R(0), R(0)), B2 = A2, D2 = A2;
 #pragma unroll
-                    for (int k = 0; k < FMAX; k++) {
-                        if (k < F) {
-                            Rk[k] = Rk[k] + mubs * fr[k];  // R_k = sum_{l>=j} mubar_l lam_lk
-                            A = A + Rk[k] * fr[k];
-                            B = B + S[k] * fr[k];          // S^(j)
-                            D = D + dw[k] * fr[k];
-                            S[k] = S[k] - oss * fr[k];     // S^(j-1)
-                        }
+                    for (int m = 0; m < FH; m++) {
+                        const PT f2 = Pair<R>::mk(fr[2 * m], fr[2 * m + 1]);
+                        Rk[m] = Pair<R>::fma(mubs2, f2, Rk[m]);  // R_k = sum_{l>=j} mubar_l lam_lk
+                        A2 = Pair<R>::fma(Rk[m], f2, A2);
+                        B2 = Pair<R>::fma(S[m], f2, B2);         // S^(j)
+                        D2 = Pair<R>::fma(dw[m], f2, D2);
+                        S[m] = Pair<R>::fma(noss2, f2, S[m]);    // S^(j-1)
                     }
+                    const R A = A2.x + A2.y, B = B2.x + B2.y, D = D2.x + D2.y;
                     // sigmabar_ij = sum_k lambar_jk f_jk - mubar_j sigma_ij with
                     // lambar_jk = mubar_j S_k + os_j R_k + Ybar'_j dW_k
                     red[j * RS + lane] = active ? (mub * B + o * A + yb * D - mubs) : R(0);
                     // osbar_j = sigma_j A;  d os_j / d Y_j = os_j (1 - os_j) (zero where capped)
-                    if (!((capmask >> j) & 1ull)) Ybar[j] = yb + (sg * A) * (o * (R(1) - o));
+                    if (!(a.capped && ((capmask >> j) & 1ull))) Ybar[j] = yb + (sg * A) * (o * (R(1) - o));
                 }
             }
             if (!kKeepOs && n - 1 >= a.n_lo) prefetch(n - 1);
