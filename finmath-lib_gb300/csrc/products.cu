@@ -246,13 +246,18 @@ __global__ void __launch_bounds__(kProdThreads) bermudan_gram_kernel(const BermS
                 k++;
             }
     }
+    if (sizeof(TS) == 4) {
+        // mixed form: FP64 sums, compensated across warps only
+        block_sums_warp_plain<kGram>(acc, partials + ((size_t)e * gridDim.x + blockIdx.x) * kGram * 2, 1);
+    } else {
 #pragma unroll
-    for (int k = 0; k < kGram; k++) {
-        const dd s = block_dd_sum(dd{acc[k], 0.0});
-        if (threadIdx.x == 0) {
-            double* q = partials + (((size_t)e * gridDim.x + blockIdx.x) * kGram + k) * 2;
-            q[0] = s.hi;
-            q[1] = s.lo;
+        for (int k = 0; k < kGram; k++) {
+            const dd s = block_dd_sum(dd{acc[k], 0.0});
+            if (threadIdx.x == 0) {
+                double* q = partials + (((size_t)e * gridDim.x + blockIdx.x) * kGram + k) * 2;
+                q[0] = s.hi;
+                q[1] = s.lo;
+            }
         }
     }
 }
@@ -408,12 +413,17 @@ __global__ void __launch_bounds__(kProdThreads) bermudan_step_kernel(const BermS
         a.under[p] = u;
     }
     if (bcur) {
+        if (sizeof(TS) == 4) {
+            // mixed form: FP64 sums, compensated across warps only
+            block_sums_warp_plain<kRhs>(acc, a.partials + (size_t)blockIdx.x * kRhs * 2, 1);
+        } else {
 #pragma unroll
-        for (int i = 0; i < kRhs; i++) {
-            const dd s = block_dd_sum(dd{acc[i], 0.0});
-            if (threadIdx.x == 0) {
-                a.partials[((size_t)blockIdx.x * kRhs + i) * 2] = s.hi;
-                a.partials[((size_t)blockIdx.x * kRhs + i) * 2 + 1] = s.lo;
+            for (int i = 0; i < kRhs; i++) {
+                const dd s = block_dd_sum(dd{acc[i], 0.0});
+                if (threadIdx.x == 0) {
+                    a.partials[((size_t)blockIdx.x * kRhs + i) * 2] = s.hi;
+                    a.partials[((size_t)blockIdx.x * kRhs + i) * 2 + 1] = s.lo;
+                }
             }
         }
     }

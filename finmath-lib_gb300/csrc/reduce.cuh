@@ -79,4 +79,29 @@ __device__ __forceinline__ void block_dd_partial(double x, double* out)
     }
 }
 
+// Block sums of NV doubles per thread, for the mixed-precision form: plain FP64 within each
+// warp (lane order), compensated across the warps (warp order).  Thread i < NV writes the
+// (hi, lo) pair of sum i to out + 2 (i * stride).  All threads must call it.
+template <int NV>
+__device__ __forceinline__ void block_sums_warp_plain(const double (&v)[NV], double* out, int stride)
+{
+    __shared__ double ws[32][NV];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nwarps = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int i = 0; i < NV; i++) {
+        double x = v[i];
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
+        if (lane == 0) ws[warp][i] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < NV) {
+        dd acc{0.0, 0.0};
+        for (int w = 0; w < nwarps; w++) acc = dd_add_d(acc, ws[w][threadIdx.x]);
+        out[2 * (size_t)threadIdx.x * stride] = acc.hi;
+        out[2 * (size_t)threadIdx.x * stride + 1] = acc.lo;
+    }
+}
+
 }  // namespace lmm

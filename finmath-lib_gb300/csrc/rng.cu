@@ -136,44 +136,49 @@ __device__ double icdf_wichura(double p)
 // FP32 evaluation of the same rational approximations (mixed-precision form).  The draw
 // u = (hi 2^26 + lo) 2^-52 is handled in 32-bit pieces: q = u - 1/2 = (dh 2^26 + lo) 2^-52
 // with dh = hi - 2^25, and a tail probability min(u, 1-u) from the same pieces.
+__device__ __forceinline__ float horner8f(float r, const float (&c)[8])
+{
+    // c[0] r^7 + ... + c[7], with fused multiply-adds (this file is built without contraction)
+    float v = c[0];
+#pragma unroll
+    for (int i = 1; i < 8; i++) v = fmaf(v, r, c[i]);
+    return v;
+}
+
 __device__ __forceinline__ float icdf_central_f32(float q)
 {
-    const float r = 0.180625f - q * q;
-    const float num = (((((((2.5090809287301226727e+03f * r + 3.3430575583588128105e+04f) * r +
-                            6.7265770927008700853e+04f) * r + 4.5921953931549871457e+04f) * r +
-                          1.3731693765509461125e+04f) * r + 1.9715909503065514427e+03f) * r +
-                        1.3314166789178437745e+02f) * r + 3.3871328727963666080e+00f);
-    const float den = (((((((5.2264952788528545610e+03f * r + 2.8729085735721942674e+04f) * r +
-                            3.9307895800092710610e+04f) * r + 2.1213794301586595867e+04f) * r +
-                          5.3941960214247511077e+03f) * r + 6.8718700749205790830e+02f) * r +
-                        4.2313330701600911252e+01f) * r + 1.0f);
-    return __fdividef(q * num, den);
+    constexpr float a[8] = {2.5090809287301226727e+03f, 3.3430575583588128105e+04f, 6.7265770927008700853e+04f,
+                            4.5921953931549871457e+04f, 1.3731693765509461125e+04f, 1.9715909503065514427e+03f,
+                            1.3314166789178437745e+02f, 3.3871328727963666080e+00f};
+    constexpr float b[8] = {5.2264952788528545610e+03f, 2.8729085735721942674e+04f, 3.9307895800092710610e+04f,
+                            2.1213794301586595867e+04f, 5.3941960214247511077e+03f, 6.8718700749205790830e+02f,
+                            4.2313330701600911252e+01f, 1.0f};
+    const float r = fmaf(-q, q, 0.180625f);
+    return __fdividef(q * horner8f(r, a), horner8f(r, b));
 }
 
 // tail branch for the tail probability t = min(u, 1-u) > 0; the sign is the caller's
 __device__ __forceinline__ float icdf_tail_f32(float t)
 {
+    constexpr float c[8] = {7.74545014278341407640e-04f, 2.27238449892691845833e-02f, 2.41780725177450611770e-01f,
+                            1.27045825245236838258e+00f, 3.64784832476320460504e+00f, 5.76949722146069140550e+00f,
+                            4.63033784615654529590e+00f, 1.42343711074968357734e+00f};
+    constexpr float d[8] = {1.05075007164441684324e-09f, 5.47593808499534494600e-04f, 1.51986665636164571966e-02f,
+                            1.48103976427480074590e-01f, 6.89767334985100004550e-01f, 1.67638483018380384940e+00f,
+                            2.05319162663775882187e+00f, 1.0f};
+    constexpr float e[8] = {2.01033439929228813265e-07f, 2.71155556874348757815e-05f, 1.24266094738807843860e-03f,
+                            2.65321895265761230930e-02f, 2.96560571828504891230e-01f, 1.78482653991729133580e+00f,
+                            5.46378491116411436990e+00f, 6.65790464350110377720e+00f};
+    constexpr float f[8] = {2.04426310338993978564e-15f, 1.42151175831644588870e-07f, 1.84631831751005468180e-05f,
+                            7.86869131145613259100e-04f, 1.48753612908506148525e-02f, 1.36929880922735805310e-01f,
+                            5.99832206555887937690e-01f, 1.0f};
     float r = sqrtf(-__logf(t));
     if (r <= 5.0f) {
         r -= 1.6f;
-        return __fdividef((((((((7.74545014278341407640e-04f * r + 2.27238449892691845833e-02f) * r +
-                                2.41780725177450611770e-01f) * r + 1.27045825245236838258e+00f) * r +
-                              3.64784832476320460504e+00f) * r + 5.76949722146069140550e+00f) * r +
-                            4.63033784615654529590e+00f) * r + 1.42343711074968357734e+00f),
-                          (((((((1.05075007164441684324e-09f * r + 5.47593808499534494600e-04f) * r +
-                                1.51986665636164571966e-02f) * r + 1.48103976427480074590e-01f) * r +
-                              6.89767334985100004550e-01f) * r + 1.67638483018380384940e+00f) * r +
-                            2.05319162663775882187e+00f) * r + 1.0f));
+        return __fdividef(horner8f(r, c), horner8f(r, d));
     }
     r -= 5.0f;
-    return __fdividef((((((((2.01033439929228813265e-07f * r + 2.71155556874348757815e-05f) * r +
-                            1.24266094738807843860e-03f) * r + 2.65321895265761230930e-02f) * r +
-                          2.96560571828504891230e-01f) * r + 1.78482653991729133580e+00f) * r +
-                        5.46378491116411436990e+00f) * r + 6.65790464350110377720e+00f),
-                      (((((((2.04426310338993978564e-15f * r + 1.42151175831644588870e-07f) * r +
-                            1.84631831751005468180e-05f) * r + 7.86869131145613259100e-04f) * r +
-                          1.48753612908506148525e-02f) * r + 1.36929880922735805310e-01f) * r +
-                        5.99832206555887937690e-01f) * r + 1.0f));
+    return __fdividef(horner8f(r, e), horner8f(r, f));
 }
 
 constexpr int kStateWords = 2 * kMtN;  // the two state buffers at the start of shared memory
