@@ -569,6 +569,9 @@ static int process_ensure(lmm_process* pr)
         }
         a.d_ckpt = pr->d_ckpt;
         a.ckpt_stride = pr->want_ckpt;
+    }
+    // 1/N per path: read by the adjoint seeds, and by the mixed form's products (no divisions)
+    if (pr->want_ckpt > 0 || pr->precision == LMM_PRECISION_MIXED) {
         if (!pr->d_inv_numeraire && (rc = dalloc(&pr->d_inv_numeraire, (size_t)(pr->N + 1) * pr->P, s))) return rc;
         a.d_inv_numeraire = pr->d_inv_numeraire;
     }
@@ -698,6 +701,7 @@ static ProductView product_view(lmm_process* pr)
     v.d_states = pr->d_states;
     v.h_obs_slot = pr->obs_slot.data();
     v.d_numeraire = pr->d_numeraire;
+    v.d_inv_numeraire = pr->precision == LMM_PRECISION_MIXED ? pr->d_inv_numeraire : nullptr;
     v.d_num_adj = pr->d_num_adj;
     v.h_discount = pr->has_discount ? pr->discount.data() : nullptr;
     v.h_num_det = pr->num_det.data();

@@ -137,6 +137,7 @@ struct ProductView {
     const void* d_states;        // [nobs][N][P]
     const int* h_obs_slot;       // host copy [T+1]
     const double* d_numeraire;   // [N+1][P]
+    const double* d_inv_numeraire;  // [N+1][P] 1/N, kept by the mixed form (else nullptr)
     const double* d_num_adj;     // [N+1] mean of 1/N (or deterministic value)
     const double* h_discount;    // [N+1] P^d chain (nullptr = none)
     const uint8_t* h_num_det;    // [N+1]

@@ -27,7 +27,9 @@ struct NumeraireInfo {
     int has_discount;
     const double* numeraire;   // [N+1][P] unadjusted
     const double* adj;         // [N+1] mean of 1/N (device)
+    const double* inv_numeraire;  // [N+1][P] 1/N (mixed form; else nullptr)
     double pd[kMaxN + 1];      // P^d(T_l)
+    double inv_pd[kMaxN + 1];  // 1 / P^d(T_l)
     unsigned char det[kMaxN + 1];
 };
 
@@ -39,6 +41,22 @@ __device__ __forceinline__ double numeraire_adj(const NumeraireInfo& n, int l, i
     const double a = n.adj[l];
     if (n.det[l]) return (1.0 / n.pd[l]) * (Nu * a);  // Scalar.div: invert, then mult
     return (Nu * a) / n.pd[l];
+}
+
+// Mixed form only: N_adj = N (a / P^d) and 1/N_adj = (1/N) (P^d / a) with the per-date
+// factor uniform across paths, so no division per path.
+__device__ __forceinline__ double numeraire_adj_mixed(const NumeraireInfo& n, int l, int p)
+{
+    const double Nu = n.numeraire[(size_t)l * n.P + p];
+    if (!n.has_discount) return Nu;
+    return Nu * (n.adj[l] * n.inv_pd[l]);
+}
+__device__ __forceinline__ double inv_numeraire_adj_mixed(const NumeraireInfo& n, int l, int p)
+{
+    if (!n.inv_numeraire) return 1.0 / numeraire_adj_mixed(n, l, p);
+    const double iN = n.inv_numeraire[(size_t)l * n.P + p];
+    if (!n.has_discount) return iN;
+    return iN * (n.pd[l] / n.adj[l]);
 }
 
 template <typename TS>
@@ -143,19 +161,27 @@ struct BermShared {
     double* basis_buf;             // [ne][5][P]
 };
 
+// the swap periods of one exercise date in FP32 (period index, length), staged per block
+struct SwapRows32 {
+    int idx[kMaxN];
+    float len[kMaxN];
+};
+
 template <typename TS>
-__device__ void bermudan_basis(const BermShared& a, const BermudanPeriod& c, int p, double B[5])
+__device__ void bermudan_basis(const BermShared& a, const BermudanPeriod& c, int p, double B[5], const SwapRows32* rows)
 {
     if (a.basis == 1 && sizeof(TS) == 4) {
-        // mixed form: the same par-rate recursion in FP32 (the state's precision); the basis
-        // values are widened to FP64 for the Gram accumulation and the solve
+        // mixed form: the same par-rate recursion in FP32 (the state's precision) over the
+        // staged FP32 period table; the basis values are widened to FP64 for the Gram
+        // accumulation and the solve
         float H = 0.0f, prod = 1.0f;
         const float* st = static_cast<const float*>(a.states) + (size_t)c.ex_slot * a.N * a.P + p;
-        for (int q = c.swap_first; q < c.swap_last; q++) {
-            const float Lq = st[(size_t)a.period_index[q] * a.P];
-            const float dq = (float)a.period_length[q];
+        const int nq = c.swap_last - c.swap_first;
+        for (int q = 0; q < nq; q++) {
+            const float Lq = st[(size_t)rows->idx[q] * a.P];
+            const float dq = rows->len[q];
             const float g = fmaf(Lq, dq, 1.0f);
-            if (q == c.swap_first) {
+            if (q == 0) {
                 prod = g;
                 H = dq;
             } else {
@@ -164,7 +190,7 @@ __device__ void bermudan_basis(const BermShared& a, const BermudanPeriod& c, int
             }
         }
         const double S = (double)((prod - 1.0f) / H);
-        const double Nn = numeraire_adj(a.num, c.ex_num_index, p);
+        const double Nn = numeraire_adj_mixed(a.num, c.ex_num_index, p);
         B[0] = S;
         B[1] = S * S;
         B[2] = Nn;
@@ -225,13 +251,21 @@ __global__ void __launch_bounds__(kProdThreads) bermudan_gram_kernel(const BermS
 {
     const int e = blockIdx.y;
     const BermudanPeriod c = a.per[a.ex_period[e]];
+    __shared__ SwapRows32 rows;
+    if (sizeof(TS) == 4) {
+        for (int q = threadIdx.x; q < c.swap_last - c.swap_first; q += blockDim.x) {
+            rows.idx[q] = a.period_index[c.swap_first + q];
+            rows.len[q] = (float)a.period_length[c.swap_first + q];
+        }
+        __syncthreads();
+    }
     double acc[kGram];
 #pragma unroll
     for (int k = 0; k < kGram; k++) acc[k] = 0.0;
     double* bb = a.basis_buf + (size_t)e * 5 * a.P;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.P; p += gridDim.x * blockDim.x) {
         double B[5];
-        bermudan_basis<TS>(a, c, p, B);
+        bermudan_basis<TS>(a, c, p, B, &rows);
 #pragma unroll
         for (int i = 0; i < 5; i++) bb[(size_t)i * a.P + p] = B[i];
         int k = 0;
@@ -396,7 +430,8 @@ __global__ void __launch_bounds__(kProdThreads) bermudan_step_kernel(const BermS
         if (a.cur >= 0) {
             const double L = state_at<TS>(sh.states, c.libor_slot, sh.N, sh.P, c.libor_index, p);
             double payoff = ((L - c.strike) * c.period_length) * c.notional;
-            payoff = payoff / numeraire_adj(sh.num, c.pay_num_index, p);
+            if (sizeof(TS) == 4) payoff = payoff * inv_numeraire_adj_mixed(sh.num, c.pay_num_index, p);
+            else payoff = payoff / numeraire_adj(sh.num, c.pay_num_index, p);
             payoff = payoff * w;
             if (sh.callable) u = u + payoff;
             else v = v + payoff;
@@ -469,9 +504,11 @@ NumeraireInfo make_numeraire_info(const ProductView& v)
     n.P = v.P;
     n.has_discount = v.h_discount != nullptr;
     n.numeraire = v.d_numeraire;
+    n.inv_numeraire = v.d_inv_numeraire;
     n.adj = v.d_num_adj;
     for (int l = 0; l <= kMaxN; l++) {
         n.pd[l] = (v.h_discount && l <= v.N) ? v.h_discount[l] : 1.0;
+        n.inv_pd[l] = 1.0 / n.pd[l];
         n.det[l] = (l <= v.N) ? v.h_num_det[l] : 0;
     }
     return n;
