@@ -207,31 +207,72 @@ __device__ __forceinline__ void mt_regenerate(const uint32_t* cur, uint32_t* nxt
 // tile leaves as row segments of K consecutive paths (K x element size = 128 bytes when the
 // tile fits).  Column k of row r of the tile sits at k ^ (r mod K), so that both the
 // column-wise fill and the row-wise drain are free of bank conflicts.
+// Drain the tile of paths [pt, pt+K) to the increment rows.  An interior tile (all its
+// draws inside the chunk) needs no per-element test.
+template <typename OutT>
+__device__ __forceinline__ void drain_tile(const OutT* tile, OutT* out, int TF, int K, int P, int64_t pt, int64_t ps,
+                                           int ts, int64_t pe, int te, int r0, int rstep, int dk)
+{
+    const int64_t path = pt + dk;
+    const bool interior = (pt > ps || ts == 0) && pt + K - 1 < pe;
+    if (interior) {
+        OutT* o = out + (size_t)r0 * P + path;
+        const size_t ostep = (size_t)rstep * P;
+        for (int r = r0; r < TF; r += rstep, o += ostep) *o = tile[r * K + (dk ^ (r & (K - 1)))];
+    } else {
+        for (int r = r0; r < TF; r += rstep)
+            if (path < P && (path > ps || r >= ts) && (path < pe || (path == pe && r < te)))
+                out[(size_t)r * P + path] = tile[r * K + (dk ^ (r & (K - 1)))];
+    }
+}
+
+// Brownian increments dW[t*F+k][p] of the chunk [v0, v1) of the stream.  The stream runs
+// path-major (path p's T*F draws are consecutive) while the output rows are [t*F+k][P]:
+// the draws go to a shared-memory tile of K consecutive paths x T*F values, and each full
+// tile leaves as row segments of K consecutive paths (K x element size = 128 bytes when the
+// tile fits).  Column k of row r of the tile sits at k ^ (r mod K), so that both the
+// column-wise fill and the row-wise drain are free of bank conflicts.  Thread i owns draw i
+// of every round; its position (path, step, factor) advances by the round's 312 draws
+// without divisions.
 template <typename OutT>
 __device__ __forceinline__ void increments_loop(const RngParams& prm, uint32_t* x, int tid, int64_t v0, int64_t v1,
-                                                unsigned long long* tail_w, short* tail_i, int* tail_n)
+                                                unsigned long long* tail_w, int2* tail_pos, int* tail_n)
 {
     constexpr bool kExact = sizeof(OutT) == 8;  // FP64: the reference's arithmetic, bit for bit
+    constexpr int kRound = kMtN / 2;
     const int TF = prm.values_per_path, F = prm.num_factors, P = prm.num_paths, K = prm.tile_k;
+    const int T = TF / F;
     OutT* tile = reinterpret_cast<OutT*>(x + kStateWords);
     OutT* out = static_cast<OutT*>(prm.out);
     const int64_t ps = v0 / TF, pe = v1 / TF;
     const int ts = (int)(v0 - ps * TF), te = (int)(v1 - pe * TF);  // chunk = [(ps, ts), (pe, te))
-    int64_t path0 = ps;  // path and position of the round's first draw
-    int tf0 = ts;
-    int64_t pt = ps;     // first path of the tile
+    // positions relative to the chunk's first path ps
+    int rpo = 0, rtf = ts;  // the round's first draw
+    int spo, st, sk;        // this thread's draw: path, time step, factor
+    {
+        uint32_t q, r, t, k;
+        divmod_u32((uint32_t)(ts + tid), (uint32_t)TF, prm.magic_tf, q, r);
+        divmod_u32(r, (uint32_t)F, prm.magic_f, t, k);
+        spo = (int)q;
+        st = (int)t;
+        sk = (int)k;
+    }
+    const int a_tf = kRound % TF, a_po = kRound / TF, a_t = a_tf / F, a_k = a_tf % F;
+    int pt = 0;  // first path of the tile, relative to ps
     const int lane = tid & 31, warp = tid >> 5;
     const int rpp = 32 / K;  // tile rows drained per warp pass
-    const int dk = lane % K, dr = lane / K;
+    const int dk = lane % K, r0 = warp * rpp + lane / K, rstep = (kRngThreads / 32) * rpp;
+    const int rounds = (int)((v1 - v0 + kRound - 1) / kRound);
     uint32_t* cur = x;
     uint32_t* nxt = x + kMtN;
-    for (int64_t v = v0; v < v1; v += kMtN / 2) {
+    for (int rd = 0; rd < rounds; rd++) {
         mt_regenerate(cur, nxt, tid, tail_n);
-        const int nv = (int)min((int64_t)(kMtN / 2), v1 - v);
+        const int nv = min(kRound, (int)(v1 - v0 - (int64_t)rd * kRound));
         OutT hv0 = OutT(0), hv1 = OutT(0);
-        int hp0 = -1, hf0 = 0, hp1 = -1, hf1 = 0;  // held draws: path offset from path0 (-1: none), row
+        int hp0 = -1, hf0 = 0, hp1 = -1, hf1 = 0;  // held draws: path (relative to ps; -1: none), row
         if (tid < nv) {
-            const uint32_t w1 = mt_temper(nxt[2 * tid]), w2 = mt_temper(nxt[2 * tid + 1]);
+            const uint2 ww = *reinterpret_cast<const uint2*>(nxt + 2 * tid);
+            const uint32_t w1 = mt_temper(ww.x), w2 = mt_temper(ww.y);
             bool central;
             if constexpr (kExact) {
                 // |u - 1/2| <= 0.425 tested exactly on the 52-bit grid, u = m 2^-52
@@ -239,96 +280,96 @@ __device__ __forceinline__ void increments_loop(const RngParams& prm, uint32_t* 
                 const int64_t dq = m - ((int64_t)1 << 51);
                 central = (dq < 0 ? -dq : dq) <= prm.central_max;
                 if (central) {
-                    hv0 = icdf_central((double)dq * 0x1.0p-52);
+                    hv0 = icdf_central((double)dq * 0x1.0p-52) * __ldg(prm.sqrt_dt + st);
                 } else {
                     const int slot = atomicAdd(tail_n, 1);
                     tail_w[slot] = (unsigned long long)m;
-                    tail_i[slot] = (short)tid;
+                    tail_pos[slot] = make_int2(spo, st * F + sk);
                 }
             } else {
                 const uint32_t hi = w1 >> 6, lo = w2 >> 6;  // u = (hi 2^26 + lo) 2^-52
                 const float q = fmaf((float)lo, 0x1.0p-52f, (float)((int)hi - (1 << 25)) * 0x1.0p-26f);
                 central = fabsf(q) <= 0.425f;
                 if (central) {
-                    hv0 = icdf_central_f32(q);
+                    hv0 = icdf_central_f32(q) * __ldg(prm.sqrt_dt32 + st);
                 } else {
                     const int slot = atomicAdd(tail_n, 1);
                     tail_w[slot] = ((unsigned long long)hi << 32) | lo;
-                    tail_i[slot] = (short)tid;
+                    tail_pos[slot] = make_int2(spo, st * F + sk);
                 }
             }
             if (central) {
-                uint32_t po, tf, t, kf;
-                divmod_u32((uint32_t)(tf0 + tid), (uint32_t)TF, prm.magic_tf, po, tf);
-                divmod_u32(tf, (uint32_t)F, prm.magic_f, t, kf);
-                hv0 = hv0 * (kExact ? (OutT)__ldg(prm.sqrt_dt + t) : (OutT)__ldg(prm.sqrt_dt32 + t));
-                hp0 = (int)po;
-                hf0 = (int)tf;
+                hp0 = spo;
+                hf0 = st * F + sk;
             }
         }
         __syncthreads();
         const int n_tail = *tail_n;
         if (tid < n_tail) {
             const unsigned long long w = tail_w[tid];
-            const int src = tail_i[tid];
+            const int2 pos = tail_pos[tid];
+            uint32_t t, k;
+            divmod_u32((uint32_t)pos.y, (uint32_t)F, prm.magic_f, t, k);
             OutT val;
             if constexpr (kExact) {
-                val = icdf_wichura((double)(int64_t)w * 0x1.0p-52);
+                val = icdf_wichura((double)(int64_t)w * 0x1.0p-52) * __ldg(prm.sqrt_dt + t);
             } else {
                 const uint32_t hi = (uint32_t)(w >> 32), lo = (uint32_t)w;
                 const bool lower = hi < (1u << 25);
                 // min(u, 1-u): u itself below 1/2; 1-u = ((2^26-1-hi) 2^26 + (2^26-lo)) 2^-52 above
                 const float tp = lower ? fmaf((float)lo, 0x1.0p-52f, (float)hi * 0x1.0p-26f)
                                        : fmaf((float)((1u << 26) - lo), 0x1.0p-52f, (float)((1u << 26) - 1u - hi) * 0x1.0p-26f);
-                val = tp > 0.0f ? icdf_tail_f32(tp) : 0.0f;
-                if (lower) val = -val;
+                float v = tp > 0.0f ? icdf_tail_f32(tp) : 0.0f;
+                if (lower) v = -v;
+                val = v * __ldg(prm.sqrt_dt32 + t);
             }
-            uint32_t po, tf, t, kf;
-            divmod_u32((uint32_t)(tf0 + src), (uint32_t)TF, prm.magic_tf, po, tf);
-            divmod_u32(tf, (uint32_t)F, prm.magic_f, t, kf);
-            hv1 = val * (kExact ? (OutT)__ldg(prm.sqrt_dt + t) : (OutT)__ldg(prm.sqrt_dt32 + t));
-            hp1 = (int)po;
-            hf1 = (int)tf;
+            hv1 = val;
+            hp1 = pos.x;
+            hf1 = pos.y;
         }
         // place the held draws; drain the tile whenever this round reaches past it
-        uint32_t plast, tflast;
-        divmod_u32((uint32_t)(tf0 + nv - 1), (uint32_t)TF, prm.magic_tf, plast, tflast);
+        uint32_t dl, rl;
+        divmod_u32((uint32_t)(rtf + nv - 1), (uint32_t)TF, prm.magic_tf, dl, rl);
+        const int plast = rpo + (int)dl;  // path of the round's last draw
         while (true) {
-            if (hp0 >= 0 && path0 + hp0 < pt + K) {
-                tile[hf0 * K + ((int)(path0 + hp0 - pt) ^ (hf0 & (K - 1)))] = hv0;
+            if (hp0 >= 0 && hp0 < pt + K) {
+                tile[hf0 * K + ((hp0 - pt) ^ (hf0 & (K - 1)))] = hv0;
                 hp0 = -1;
             }
-            if (hp1 >= 0 && path0 + hp1 < pt + K) {
-                tile[hf1 * K + ((int)(path0 + hp1 - pt) ^ (hf1 & (K - 1)))] = hv1;
+            if (hp1 >= 0 && hp1 < pt + K) {
+                tile[hf1 * K + ((hp1 - pt) ^ (hf1 & (K - 1)))] = hv1;
                 hp1 = -1;
             }
-            if (path0 + (int64_t)plast < pt + K) break;
+            if (plast < pt + K) break;
             __syncthreads();
-            for (int r = warp * rpp + dr; r < TF; r += (kRngThreads / 32) * rpp) {
-                const int64_t path = pt + dk;
-                if (path < P && (path > ps || r >= ts) && (path < pe || (path == pe && r < te)))
-                    out[(size_t)r * P + path] = tile[r * K + (dk ^ (r & (K - 1)))];
-            }
+            drain_tile<OutT>(tile, out, TF, K, P, ps + pt, ps, ts, pe, te, r0, rstep, dk);
             __syncthreads();
             pt += K;
         }
-        // advance the position by the round's 312 draws
-        tf0 += kMtN / 2;
-        if (tf0 >= TF) {
-            const int adv = tf0 / TF;
-            path0 += adv;
-            tf0 -= adv * TF;
+        // advance the round's and this thread's positions by 312 draws
+        rtf += a_tf;
+        rpo += a_po;
+        if (rtf >= TF) {
+            rtf -= TF;
+            rpo++;
+        }
+        sk += a_k;
+        st += a_t;
+        spo += a_po;
+        if (sk >= F) {
+            sk -= F;
+            st++;
+        }
+        if (st >= T) {
+            st -= T;
+            spo++;
         }
         uint32_t* tmp = cur;
         cur = nxt;
         nxt = tmp;
     }
     __syncthreads();
-    for (int r = warp * rpp + dr; r < TF; r += (kRngThreads / 32) * rpp) {
-        const int64_t path = pt + dk;
-        if (path < P && (path > ps || r >= ts) && (path < pe || (path == pe && r < te)))
-            out[(size_t)r * P + path] = tile[r * K + (dk ^ (r & (K - 1)))];
-    }
+    drain_tile<OutT>(tile, out, TF, K, P, ps + pt, ps, ts, pe, te, r0, rstep, dk);
 }
 
 __global__ void __launch_bounds__(kRngThreads, 2) mt_generate_kernel(const RngParams prm)
@@ -337,7 +378,7 @@ __global__ void __launch_bounds__(kRngThreads, 2) mt_generate_kernel(const RngPa
     // (kStateWords words) followed by the increments tile
     extern __shared__ __align__(16) uint32_t x[];
     __shared__ unsigned long long tail_w[kMtN / 2];  // tail draws of a round, handled by consecutive lanes
-    __shared__ short tail_i[kMtN / 2];
+    __shared__ int2 tail_pos[kMtN / 2];               // their positions (path, step * F + factor)
     __shared__ int tail_n;
     const int tid = threadIdx.x;
     const int64_t c = blockIdx.x;
@@ -386,9 +427,9 @@ __global__ void __launch_bounds__(kRngThreads, 2) mt_generate_kernel(const RngPa
     }
 
     if (prm.mode == 1) {
-        increments_loop<double>(prm, x, tid, v0, v1, tail_w, tail_i, &tail_n);
+        increments_loop<double>(prm, x, tid, v0, v1, tail_w, tail_pos, &tail_n);
     } else if (prm.mode == 2) {
-        increments_loop<float>(prm, x, tid, v0, v1, tail_w, tail_i, &tail_n);
+        increments_loop<float>(prm, x, tid, v0, v1, tail_w, tail_pos, &tail_n);
     } else {
         // uniforms in stream order (contiguous stores)
         uint32_t* cur = x;
