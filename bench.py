@@ -143,16 +143,58 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def _traffic_from_profile():
-    """DRAM bytes per launch of the path kernel from the committed ncu summary, if present."""
+def _from_profile(key):
+    """A figure of the path kernel's committed ncu summary (DRAM bytes per launch, FP64 pipe
+    share), if present."""
     path = os.path.join(HERE, "profiles", "lmm_paths_fp64_lmm40.md")
     try:
         for ln in open(path):
-            if ln.startswith("traffic_bytes_per_launch:"):
+            if ln.startswith(key + ":"):
                 return float(ln.split(":", 1)[1].strip())
     except OSError:
         pass
     return None
+
+
+def _measured_hbm_gbs():
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs (measured copy bandwidth)"
+    except (OSError, ValueError, KeyError):
+        return 6800.0, "fallback 6.8 TB/s (MEASURED_PEAKS.json absent)"
+
+
+def kernel_rooflines(stats, steps, P, T, N, Fk, comp_steps, ne, fp64, fp64_peak_tflops):
+    """Per kernel family: algorithmic bytes and flops per step over its measured time per step,
+    against the measured HBM copy bandwidth and the live FP64 FMA peak; frac = the larger."""
+    hbm, hbm_src = _measured_hbm_gbs()
+    esz = 8 if fp64 else 4
+    nobs = N + 1
+    work = {
+        # name: (bytes per step, flops per step, flops peak in TFLOP/s or None)
+        "mt19937_jump_generate": (T * Fk * P * esz, 0.0, None),
+        "lmm_paths_fp64" if fp64 else "lmm_paths_fp32": (
+            T * Fk * P * esz + nobs * N * P * esz + (N + 1) * P * 8, P * comp_steps * (6 * Fk + 11),
+            fp64_peak_tflops if fp64 else None),
+        # Gram pass + backward induction: per exercise date and path ~64 bytes
+        "bermudan_regress_step": (64.0 * P * ne, 0.0, None),
+        "swaption_value": (P * (10 * esz + 8 + 8), 0.0, None),
+    }
+    out = {}
+    for name, (nbytes, flops, fpeak) in work.items():
+        if name not in stats or stats[name][0] == 0:
+            continue
+        sec = stats[name][1] / max(steps, 1) * 1e-3
+        gbs = nbytes / sec / 1e9
+        e = {"ms_per_step": sec * 1e3, "algorithmic_bytes": nbytes, "achieved_gbs": gbs, "hbm_frac": gbs / hbm}
+        if flops and fpeak:
+            e["achieved_tflops"] = flops / sec / 1e12
+            e["flop_frac"] = e["achieved_tflops"] / fpeak
+        e["frac"] = max(e["hbm_frac"], e.get("flop_frac", 0.0))
+        out[name] = e
+    out["peaks"] = {"hbm_gbs": hbm, "hbm_source": hbm_src, "fp64_tflops": fp64_peak_tflops,
+                    "fp64_source": "live DFMA probe x2"}
+    return out
 
 
 def run_ours(args):
@@ -233,14 +275,19 @@ def run_ours(args):
     L.lmm_probe_fp64_fma_rate(ctypes.byref(fma))
     peak = 2.0 * fma.value / 1e12
     achieved = flops / k_avg_s / 1e12
-    traffic = _traffic_from_profile() if prec == F.PRECISION_FP64 and P == (1 << 20) else None
+    traffic = _from_profile("traffic_bytes_per_launch") if prec == F.PRECISION_FP64 and P == (1 << 20) else None
     roofline = {"bound": "fp64" if prec == F.PRECISION_FP64 else "fp32", "kernel": kname,
                 "achieved": achieved, "peak": peak if prec == F.PRECISION_FP64 else None, "unit": "TFLOP/s",
                 "frac": achieved / peak if prec == F.PRECISION_FP64 else None, "traffic": traffic,
                 "algorithmic_flops_per_launch": flops, "avg_launch_ms": k_avg_s * 1e3,
                 "peak_source": "FP64 FMA rate measured live by the library's DFMA probe (x2 flops); "
                                "MEASURED_PEAKS.json holds no FP64 figure",
-                "component_steps_per_path": comp_steps}
+                "component_steps_per_path": comp_steps,
+                "transcendentals_per_launch": {"log": P * comp_steps, "exp": P * comp_steps, "div": P * comp_steps},
+                "ncu_fp64_pipe_active": _from_profile("fp64_pipe_active") if prec == F.PRECISION_FP64 else None,
+                "note": "algorithmic flops count add/mul only; each component-step also takes one log, one exp "
+                        "and one correctly rounded reciprocal in the reference's order, which keep the FP64 "
+                        "pipe ~83 % busy (ncu, profiles/lmm_paths_fp64_lmm40.md)"}
 
     # ---------------- end to end through the C ABI with host buffers (tables in, prices out)
     e2e_times = []
@@ -279,10 +326,13 @@ def run_ours(args):
                        "parallelism": f"replicas x{ws}", "l2": "inputs larger than L2 (Brownian increments 6.7 GB)"},
             "prices": {"bermudan": res[0], "swaption": res[1]},
             "e2e": e2e, "roofline": roofline, "clocks": clk, "gpu_launches": int(launches),
+            "kernel_rooflines": kernel_rooflines(stats, args.steps, P, T, N, Fk, comp_steps, len(fix),
+                                                 prec == F.PRECISION_FP64, peak),
             "kernels_ms": {k: v[1] / max(args.steps, 1) for k, v in stats.items() if v[0]}}
 
     if rank == 0 and args.precision == "fp64" and not args.no_forms:
         line["forms"] = {"mixed": mixed_form(args, F, W, cfg, P, T, berm, swpt, res),
+                         "mixed_2e22_paths": mixed_form_large(args, F, W, cfg, T, berm, swpt),
                          "greeks": greeks_form(args, F, W, cfg, P, T, berm,
                                                ms - stats["mt19937_jump_generate"][1] / max(args.steps, 1))}
         if not args.no_portfolio:
@@ -323,6 +373,36 @@ def mixed_form(args, F, W, cfg, P, T, berm, swpt, res64):
     sim.process.close()
     bm.close()
     return out
+
+
+def mixed_form_large(args, F, W, cfg, T, berm, swpt, P=1 << 22):
+    """The mixed-precision form at 2^22 paths (the second size of the precision form), with
+    its price error against an FP64 valuation of the same 2^22 paths."""
+    import torch
+    sim64 = W.build(cfg, paths=P)
+    b64, s64 = berm.getValues(sim64), swpt.getValues(sim64)
+    sim64.process.close()
+    sim64.process.brownianMotion.close()
+    sim = W.build(cfg, paths=P, precision=F.PRECISION_MIXED)
+    bm = sim.process.brownianMotion
+    bm.setSeed(cfg["seed"])
+    b, s = berm.getValues(sim), swpt.getValues(sim)
+    reps = max(1, min(args.steps, 3))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        bm.setSeed(cfg["seed"])
+        b = berm.getValues(sim)
+        s = swpt.getValues(sim)
+    torch.cuda.synchronize()
+    ms = 1e3 * (time.perf_counter() - t0) / reps
+    sim.process.close()
+    bm.close()
+    return {"paths": P, "value": P * T / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "bermudan": b, "swaption": s,
+            "fp64": {"bermudan": b64, "swaption": s64},
+            "bermudan_error_bp": 1e4 * (b["value"] - b64["value"]),
+            "bermudan_error_in_se": (b["value"] - b64["value"]) / b64["error"],
+            "swaption_error_bp": 1e4 * (s["value"] - s64["value"])}
 
 
 def greeks_form(args, F, W, cfg, P, T, berm, fp64_valuation_ms):

@@ -173,7 +173,7 @@ struct lmm_brownian {
 
 struct lmm_process {
     lmm_brownian* bm = nullptr;
-    int T = 0, N = 0, F = 0, P = 0, scheme = 1, precision = 0;
+    int T = 0, N = 0, F = 0, P = 0, scheme = 1, precision = 0, measure = 0, state_space = 0;
     double cap = 1e5;
     std::vector<double> times, tenor, discount;
     bool has_discount = false;
@@ -185,7 +185,7 @@ struct lmm_process {
     double *d_loadings = nullptr, *d_variance = nullptr, *d_dt = nullptr, *d_delta = nullptr, *d_init = nullptr;
     double *d_inv_delta = nullptr, *d_var_half = nullptr;
     float *d_lam32 = nullptr, *d_var32 = nullptr, *d_inv_delta32 = nullptr, *d_dt32 = nullptr, *d_init_log32 = nullptr;
-    int *d_first = nullptr, *d_obs_slot = nullptr;
+    int *d_first = nullptr, *d_obs_slot = nullptr, *d_tenor_tidx = nullptr;
     uint8_t* d_det = nullptr;
     // results
     void* d_states = nullptr;
@@ -400,9 +400,13 @@ int lmm_process_create(const lmm_model_desc* m, lmm_brownian* bm, lmm_process** 
     if (F != bm->F) return fail(LMM_ERR_INVALID, "number of factors differs from the Brownian motion's");
     if (N <= 0 || N > 64 || F > 16) return fail(LMM_ERR_INVALID, "supported sizes: 1 <= forward rates <= 64, factors <= 16");
     if (!m->tenor || !m->factor_loadings || !m->variance || !m->initial_forwards) return fail(LMM_ERR_INVALID, "model tables missing");
-    if (m->measure != 0) return fail(LMM_ERR_INVALID, "only the SPOT measure is implemented on this path");
-    if (m->state_space != 0) return fail(LMM_ERR_INVALID, "only the LOGNORMAL state space is implemented on this path");
-    if (m->scheme != LMM_SCHEME_EULER && m->scheme != LMM_SCHEME_EULER_FUNCTIONAL) return fail(LMM_ERR_INVALID, "unknown scheme");
+    if (m->measure != LMM_MEASURE_SPOT && m->measure != LMM_MEASURE_TERMINAL) return fail(LMM_ERR_INVALID, "unknown measure");
+    if (m->state_space != LMM_STATE_SPACE_LOGNORMAL && m->state_space != LMM_STATE_SPACE_NORMAL)
+        return fail(LMM_ERR_INVALID, "unknown state space");
+    if (m->scheme < LMM_SCHEME_EULER || m->scheme > LMM_SCHEME_PREDICTOR_CORRECTOR_FUNCTIONAL) return fail(LMM_ERR_INVALID, "unknown scheme");
+    if (bm->precision == LMM_PRECISION_MIXED &&
+        (m->measure != LMM_MEASURE_SPOT || m->state_space != LMM_STATE_SPACE_LOGNORMAL || m->scheme > LMM_SCHEME_EULER_FUNCTIONAL))
+        return fail(LMM_ERR_INVALID, "the mixed-precision form takes the SPOT measure, LOGNORMAL state space and Euler schemes");
     for (int j = 1; j <= N; j++)
         if (!(m->tenor[j] > m->tenor[j - 1])) return fail(LMM_ERR_INVALID, "tenor must be strictly increasing");
     if (m->tenor[N - 1] > m->times[T]) return fail(LMM_ERR_INVALID, "every forward rate must fix within the simulation horizon");
@@ -413,6 +417,8 @@ int lmm_process_create(const lmm_model_desc* m, lmm_brownian* bm, lmm_process** 
     pr->F = F;
     pr->P = bm->P;
     pr->scheme = m->scheme;
+    pr->measure = m->measure;
+    pr->state_space = m->state_space;
     pr->precision = bm->precision;
     pr->cap = m->libor_cap;
     pr->times.assign(m->times, m->times + T + 1);
@@ -438,8 +444,13 @@ int lmm_process_create(const lmm_model_desc* m, lmm_brownian* bm, lmm_process** 
         pr->tenor_tidx[l] = ti;
     }
     pr->num_det.assign(N + 1, 0);
-    pr->num_det[0] = 1;
-    for (int l = 0; l < N; l++) pr->num_det[l + 1] = (uint8_t)(pr->num_det[l] && pr->tenor_tidx[l] == 0);
+    if (pr->measure == LMM_MEASURE_SPOT) {
+        pr->num_det[0] = 1;
+        for (int l = 0; l < N; l++) pr->num_det[l + 1] = (uint8_t)(pr->num_det[l] && pr->tenor_tidx[l] == 0);
+    } else {
+        // TERMINAL: N(T_N) = 1 and N(T_l) whose rates are all read at time index 0
+        for (int l = 0; l <= N; l++) pr->num_det[l] = (uint8_t)(l == N || pr->tenor_tidx[l] == 0);
+    }
     pr->num_det_prefix = 0;
     while (pr->num_det_prefix < N && pr->num_det[pr->num_det_prefix]) pr->num_det_prefix++;
     pr->obs_slot.resize(T + 1);
@@ -468,6 +479,7 @@ int lmm_process_create(const lmm_model_desc* m, lmm_brownian* bm, lmm_process** 
     if (!rc) rc = upload(&pr->d_init, m->initial_forwards, (size_t)N, s);
     if (!rc) rc = upload(&pr->d_first, pr->first.data(), pr->first.size(), s);
     if (!rc) rc = upload(&pr->d_det, pr->num_det.data(), pr->num_det.size(), s);
+    if (!rc) rc = upload(&pr->d_tenor_tidx, pr->tenor_tidx.data(), pr->tenor_tidx.size(), s);
     if (!rc && pr->precision == LMM_PRECISION_MIXED) {
         const int FP = paths_fp32_pitch(N, F);
         std::vector<float> l32((size_t)T * N * FP, 0.0f), v32((size_t)T * N);
@@ -538,6 +550,9 @@ static int process_ensure(lmm_process* pr)
     a.F = pr->F;
     a.P = pr->P;
     a.scheme = pr->scheme;
+    a.measure = pr->measure;
+    a.state_space = pr->state_space;
+    a.d_tenor_tidx = pr->d_tenor_tidx;
     a.libor_cap = pr->cap;
     a.d_loadings = pr->d_loadings;
     a.d_variance = pr->d_variance;
@@ -652,6 +667,7 @@ int lmm_process_destroy(lmm_process* pr)
     dfree(pr->d_dt32, s);
     dfree(pr->d_init_log32, s);
     dfree(pr->d_first, s);
+    dfree(pr->d_tenor_tidx, s);
     dfree(pr->d_det, s);
     dfree(pr->d_values, s);
     dfree(pr->d_reduce, s);
@@ -975,6 +991,8 @@ int lmm_bermudan_get_gradient(lmm_process* pr, const lmm_bermudan_desc* d, int s
     if (!pr || !d || !value || !deltas || !vegas) return fail(LMM_ERR_INVALID, "null argument");
     if (stride < 1 || stride > 16) return fail(LMM_ERR_INVALID, "checkpoint stride must be in [1, 16]");
     if (pr->N > 40 || pr->F > 10) return fail(LMM_ERR_INVALID, "the adjoint supports at most 40 forward rates and 10 factors");
+    if (pr->measure != LMM_MEASURE_SPOT || pr->state_space != LMM_STATE_SPACE_LOGNORMAL || pr->scheme > LMM_SCHEME_EULER_FUNCTIONAL)
+        return fail(LMM_ERR_INVALID, "the adjoint takes the SPOT measure, LOGNORMAL state space and Euler schemes");
     if (pr->obs_slot[pr->T] < 0) return fail(LMM_ERR_STATE, "the adjoint needs the last simulation time observed");
     pr->want_ckpt = stride;
     BermudanLaunch bl;
@@ -1311,6 +1329,9 @@ int lmm_portfolio_create(lmm_process* pr, const lmm_portfolio_desc* desc, lmm_po
     if (desc->concurrency < 1 || desc->concurrency > 16) return fail(LMM_ERR_INVALID, "concurrency must be in [1, 16]");
     if (desc->adjoint_threads != 64 && desc->adjoint_threads != 128 && desc->adjoint_threads != 256)
         return fail(LMM_ERR_INVALID, "adjoint threads must be 64, 128 or 256");
+    if (desc->with_greeks &&
+        (pr->measure != LMM_MEASURE_SPOT || pr->state_space != LMM_STATE_SPACE_LOGNORMAL || pr->scheme > LMM_SCHEME_EULER_FUNCTIONAL))
+        return fail(LMM_ERR_INVALID, "the adjoint takes the SPOT measure, LOGNORMAL state space and Euler schemes");
     if (desc->with_greeks && (pr->N > 40 || pr->F > 10))
         return fail(LMM_ERR_INVALID, "the adjoint supports at most 40 forward rates and 10 factors");
     if (pr->obs_slot[pr->T] < 0) return fail(LMM_ERR_STATE, "the portfolio needs the last simulation time observed");

@@ -98,7 +98,10 @@ int launch_mt_generate(const RngLaunch& a, cudaStream_t s, int* num_launches);
 
 struct PathLaunch {
     int T, N, F, P;
-    int scheme;                // 0 EULER, 1 EULER_FUNCTIONAL
+    int scheme;                // 0 EULER, 1 EULER_FUNCTIONAL, 2 PREDICTOR_CORRECTOR, 3 ..._FUNCTIONAL
+    int measure;               // 0 SPOT, 1 TERMINAL
+    int state_space;           // 0 LOGNORMAL, 1 NORMAL
+    const int* d_tenor_tidx;   // [N+1] process time index of each tenor time (TERMINAL numeraire)
     double libor_cap;          // +inf: no cap
     const double* d_loadings;  // [T][N][F]
     const double* d_variance;  // [T][N]

@@ -141,10 +141,198 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp64_kernel(const PathLaun
     }
 }
 
+// ------------------------------------------------------------------ general form
+// getDrift (LIBORMarketModelFromCovarianceModel.java:1125-1191) for any measure and state
+// space: SPOT sums the one-step transforms of l <= j (updated before j reads them), TERMINAL
+// those of l > j (walking down, read before j adds to them); LOGNORMAL multiplies the
+// transform by L and adds -variance/2.  Scalar(+-delta).discount(L, delta) =
+// 1/(L (delta/(+-delta)) + 1/(+-delta)) (stochastic/Scalar.java:321-328).
+template <int NMAX, int FMAX>
+__device__ __forceinline__ void drift_general(const PathLaunch& a, int i, int first, const double* L, double* mu)
+{
+    const int N = a.N, F = a.F;
+    const double* lam = a.d_loadings + (size_t)i * N * F;
+    const bool lognormal = a.state_space == 0;
+    double S[FMAX];
+#pragma unroll
+    for (int k = 0; k < FMAX; k++) S[k] = 0.0;
+    if (a.measure == 0) {
+#pragma unroll
+        for (int j = 0; j < NMAX; j++) {
+            if (j < N && j >= first) {
+                const double delta = __ldg(a.d_delta + j);
+                double os = 1.0 / (L[j] * (delta / delta) + 1.0 / delta);
+                if (lognormal) os = os * L[j];
+                double d = 0.0;
+#pragma unroll
+                for (int k = 0; k < FMAX; k++)
+                    if (k < F) S[k] = S[k] + os * __ldg(lam + j * F + k);
+#pragma unroll
+                for (int k = 0; k < FMAX; k++)
+                    if (k < F) d = d + S[k] * __ldg(lam + j * F + k);
+                mu[j] = d;
+            }
+        }
+    } else {
+#pragma unroll
+        for (int jj = NMAX - 1; jj >= 0; jj--) {
+            const int j = jj;
+            if (j < N && j >= first) {
+                const double delta = __ldg(a.d_delta + j);
+                double os = 1.0 / (L[j] * (delta / -delta) + 1.0 / -delta);
+                if (lognormal) os = os * L[j];
+                double d = 0.0;
+#pragma unroll
+                for (int k = 0; k < FMAX; k++)
+                    if (k < F) d = d + S[k] * __ldg(lam + j * F + k);
+                mu[j] = d;
+#pragma unroll
+                for (int k = 0; k < FMAX; k++)
+                    if (k < F) S[k] = S[k] + os * __ldg(lam + j * F + k);
+            }
+        }
+    }
+    if (lognormal) {
+#pragma unroll
+        for (int j = 0; j < NMAX; j++)
+            if (j < N && j >= first) mu[j] = mu[j] + __ldg(a.d_variance + (size_t)i * N + j) * -0.5;
+    }
+}
+
+// applyStateSpaceTransform (:1200-1212): exp for LOGNORMAL, then the cap
+__device__ __forceinline__ double transform_general(const PathLaunch& a, double y)
+{
+    double v = a.state_space == 0 ? exp(y) : y;
+    if (!isinf(a.libor_cap) && v > a.libor_cap) v = a.libor_cap;
+    return v;
+}
+
+// TERMINAL numeraire at tenor index l from the state at the time of T_l
+// (getNumerairetUnAdjustedAtLIBORIndex :1029-1048): Scalar.discount steps while deterministic,
+// RandomVariableFromDoubleArray.discount (x / (1 + L delta), :1308-1333) afterwards
+template <int NMAX>
+__device__ __forceinline__ double terminal_numeraire(const PathLaunch& a, int l, const double* L, bool deterministic)
+{
+    double x = 1.0;
+#pragma unroll
+    for (int k = 0; k < NMAX; k++) {
+        if (k >= l && k < a.N) {
+            const double delta = __ldg(a.d_delta + k);
+            if (deterministic || k == l) x = 1.0 / (L[k] * (delta / x) + 1.0 / x);
+            else x = x / (1.0 + L[k] * delta);
+        }
+    }
+    return x;
+}
+
+// The Euler scheme (EulerSchemeFromProcessModel.java:170-326) for any scheme, measure and state
+// space: the predictor-corrector step adds ((mu(predictor) - mu)/2) dt to the state and
+// transforms again (:292-314).  Rarely used forms: one kernel with run-time switches.
+template <int NMAX, int FMAX>
+__global__ void __launch_bounds__(kPathThreads) paths_fp64_general_kernel(const PathLaunch a)
+{
+    const int p = blockIdx.x * kPathThreads + threadIdx.x;
+    const bool active = p < a.P;
+    const int N = a.N, F = a.F, P = a.P;
+    const bool functional = a.scheme == 1 || a.scheme == 3;
+    const bool pc = a.scheme == 2 || a.scheme == 3;
+    const bool lognormal = a.state_space == 0;
+    const bool terminal = a.measure == 1;
+    const double* dW = static_cast<const double*>(a.d_dw);
+    double* states = static_cast<double*>(a.d_states);
+    double L[NMAX], Y[NMAX], mu0[NMAX], Ln[NMAX];
+#pragma unroll
+    for (int j = 0; j < NMAX; j++) {
+        L[j] = Y[j] = mu0[j] = Ln[j] = 0.0;
+        if (j < N) {
+            const double f = __ldg(a.d_init + j);
+            Y[j] = lognormal ? log(f > 0.0 ? f : 0.0) : f;
+            L[j] = transform_general(a, Y[j]);
+        }
+    }
+    {
+        const int slot = __ldg(a.d_obs_slot + 0);
+        if (slot >= 0 && active) {
+#pragma unroll
+            for (int j = 0; j < NMAX; j++)
+                if (j < N) states[((size_t)slot * N + j) * P + p] = L[j];
+        }
+        if (terminal && active)
+            for (int l = 0; l <= N; l++)
+                if (__ldg(a.d_tenor_tidx + l) == 0) a.d_numeraire[(size_t)l * P + p] = terminal_numeraire<NMAX>(a, l, L, true);
+    }
+    for (int i = 0; i < a.T; i++) {
+        const int first = __ldg(a.d_first + i);
+        const double dt = __ldg(a.d_dt + i);
+        const double* lam = a.d_loadings + (size_t)i * N * F;
+        drift_general<NMAX, FMAX>(a, i, first, L, mu0);
+#pragma unroll
+        for (int j = 0; j < NMAX; j++) {
+            Ln[j] = L[j];
+            if (j < N && j >= first) {
+                double y = functional ? (lognormal ? log(L[j]) : L[j]) : Y[j];
+                y = y + mu0[j] * dt;
+#pragma unroll
+                for (int k = 0; k < FMAX; k++)
+                    if (k < F) y = y + (active ? dW[((size_t)i * F + k) * P + p] : 0.0) * __ldg(lam + j * F + k);
+                Y[j] = y;
+                Ln[j] = transform_general(a, y);
+            }
+        }
+        if (pc) {
+            double mu1[NMAX];
+            drift_general<NMAX, FMAX>(a, i, first, Ln, mu1);
+#pragma unroll
+            for (int j = 0; j < NMAX; j++) {
+                if (j < N && j >= first) {
+                    Y[j] = Y[j] + ((mu1[j] - mu0[j]) / 2.0) * dt;
+                    Ln[j] = transform_general(a, Y[j]);
+                }
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < NMAX; j++) L[j] = Ln[j];
+        const int slot = __ldg(a.d_obs_slot + i + 1);
+        if (slot >= 0 && active) {
+#pragma unroll
+            for (int j = 0; j < NMAX; j++)
+                if (j < N) states[((size_t)slot * N + j) * P + p] = L[j];
+        }
+        if (terminal && active)
+            for (int l = 0; l <= N; l++)
+                if (__ldg(a.d_tenor_tidx + l) == i + 1)
+                    a.d_numeraire[(size_t)l * P + p] = terminal_numeraire<NMAX>(a, l, L, false);
+    }
+    if (!terminal) {
+        // SPOT numeraire from the frozen fixings (as paths_fp64_kernel)
+        double Nv = 1.0;
+        if (active) a.d_numeraire[p] = 1.0;
+#pragma unroll
+        for (int l = 0; l < NMAX; l++) {
+            if (l < N) {
+                const double delta = __ldg(a.d_delta + l);
+                if (l < a.num_det_prefix) Nv = L[l] * (delta * Nv) + Nv;
+                else Nv = Nv * (1.0 + L[l] * delta);
+                if (active) a.d_numeraire[(size_t)(l + 1) * P + p] = Nv;
+            }
+        }
+    } else if (active && __ldg(a.d_tenor_tidx + N) > a.T) {
+        a.d_numeraire[(size_t)N * P + p] = 1.0;
+    }
+    // block partials of N(T_l)^-1 * N(0) for the numeraire adjustment (:869-874)
+    const double N0 = active ? a.d_numeraire[p] : 1.0;
+    for (int l = 1; l <= N; l++) {
+        const double inv = active ? (1.0 / a.d_numeraire[(size_t)l * P + p]) * N0 : 0.0;
+        block_dd_partial(inv, a.d_inv_num_partials + ((size_t)blockIdx.x * N + (l - 1)) * 2);
+    }
+}
+
 template <int NMAX, int FMAX>
 int launch_t(const PathLaunch& a, cudaStream_t s, int blocks)
 {
-    if (a.scheme == 1)
+    if (a.scheme > 1 || a.measure != 0 || a.state_space != 0)
+        paths_fp64_general_kernel<NMAX, FMAX><<<blocks, kPathThreads, 0, s>>>(a);
+    else if (a.scheme == 1)
         paths_fp64_kernel<NMAX, FMAX, true><<<blocks, kPathThreads, 0, s>>>(a);
     else
         paths_fp64_kernel<NMAX, FMAX, false><<<blocks, kPathThreads, 0, s>>>(a);

@@ -72,7 +72,8 @@ __global__ void numeraire_finish_kernel(const double* partials, int blocks, int 
     const int l = blockIdx.x;  // numeraire index 0..N
     if (l > N) return;
     if (det[l]) {
-        if (threadIdx.x == 0) adj[l] = 1.0 * (1.0 / numeraire[(size_t)l * P]);
+        // N(T)^-1 * N(0) of a deterministic numeraire (N(0) = 1 under SPOT)
+        if (threadIdx.x == 0) adj[l] = numeraire[0] * (1.0 / numeraire[(size_t)l * P]);
         return;
     }
     dd acc{0.0, 0.0};
@@ -134,7 +135,7 @@ __global__ void __launch_bounds__(kProdThreads) swaption_kernel(const SwaptionPa
     double x = isnan(v) ? v : (v > 0.0 ? v : 0.0);
     x = x / numeraire_adj(a.num, a.s.num_index, p);
     x = x * w;
-    x = x * 1.0;
+    x = x * numeraire_adj(a.num, 0, 0);  // numeraire at evaluation time 0 (exactly 1 under SPOT)
     x = x / w;
     a.values[p] = x;
 }
@@ -442,7 +443,7 @@ __global__ void __launch_bounds__(kProdThreads) bermudan_step_kernel(const BermS
                 for (int i = 0; i < 5; i++) acc[1 + i] = acc[1 + i] + y * bcur[(size_t)i * sh.P + p];
             }
         } else {
-            v = (v * 1.0) / w;
+            v = (v * numeraire_adj(sh.num, 0, 0)) / w;  // numeraire at time 0 (exactly 1 under SPOT)
         }
         a.values[p] = v;
         a.under[p] = u;

@@ -25,6 +25,12 @@ PRECISION_FP64 = 0
 PRECISION_MIXED = 1
 SCHEME_EULER = 0
 SCHEME_EULER_FUNCTIONAL = 1
+SCHEME_PREDICTOR_CORRECTOR = 2
+SCHEME_PREDICTOR_CORRECTOR_FUNCTIONAL = 3
+MEASURE_SPOT = 0
+MEASURE_TERMINAL = 1
+STATE_SPACE_LOGNORMAL = 0
+STATE_SPACE_NORMAL = 1
 BASIS_REFERENCE = 0
 BASIS_SWAPRATE = 1
 

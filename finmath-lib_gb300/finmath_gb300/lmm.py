@@ -184,15 +184,21 @@ class LIBORMarketModelFromCovarianceModel:
     """The model's tables as finmath-lib evaluates them (LIBORMarketModelFromCovarianceModel.java:388-444)."""
 
     MEASURE_SPOT = "SPOT"
+    MEASURE_TERMINAL = "TERMINAL"
     STATE_LOGNORMAL = "LOGNORMAL"
+    STATE_NORMAL = "NORMAL"
 
     def __init__(self, liborPeriodDiscretization, analyticModel, forwardRateCurve, discountCurve, randomVariableFactory,
                  covarianceModel, calibrationItems=None, properties=None):
         props = dict(properties or {})
-        if str(props.get("measure", "SPOT")).upper() != "SPOT":
-            raise ValueError("only the SPOT measure is implemented on this path")
-        if str(props.get("stateSpace", "LOGNORMAL")).upper() != "LOGNORMAL":
-            raise ValueError("only the LOGNORMAL state space is implemented on this path")
+        measures = {"SPOT": _lib.MEASURE_SPOT, "TERMINAL": _lib.MEASURE_TERMINAL}
+        spaces = {"LOGNORMAL": _lib.STATE_SPACE_LOGNORMAL, "NORMAL": _lib.STATE_SPACE_NORMAL}
+        m, sp = str(props.get("measure", "SPOT")).upper(), str(props.get("stateSpace", "LOGNORMAL")).upper()
+        if m not in measures:
+            raise ValueError(f"measure {m} is not implemented on this path")
+        if sp not in spaces:
+            raise ValueError(f"state space {sp} is not implemented on this path")
+        self.measure, self.stateSpace = measures[m], spaces[sp]
         if calibrationItems:
             raise ValueError("calibration is not part of this path")
         self.liborPeriodDiscretization = liborPeriodDiscretization
@@ -284,6 +290,8 @@ def mersenne_twister_uniforms(seed: int, count: int, offset: int = 0) -> np.ndar
 class EulerSchemeFromProcessModel:
     EULER = _lib.SCHEME_EULER
     EULER_FUNCTIONAL = _lib.SCHEME_EULER_FUNCTIONAL
+    PREDICTOR_CORRECTOR = _lib.SCHEME_PREDICTOR_CORRECTOR
+    PREDICTOR_CORRECTOR_FUNCTIONAL = _lib.SCHEME_PREDICTOR_CORRECTOR_FUNCTIONAL
 
     def __init__(self, model: LIBORMarketModelFromCovarianceModel, brownianMotion: BrownianMotionFromMersenneRandomNumbers,
                  scheme=None, observedTimeIndices=None):
@@ -301,8 +309,8 @@ class EulerSchemeFromProcessModel:
         vol = getattr(cov, "volatility", None)
         k["vol"] = None if vol is None else _f64(vol)
         desc = _lib.LmmModelDesc(T, _p(k["times"]), N, _p(k["tenor"]), cov.getNumberOfFactors(), _p(k["lam"]),
-                                 _p(k["var"]), _p(k["init"]), _p(k["chain"]), model.liborCap, int(self.scheme), 0, 0,
-                                 _p(k["vol"]))
+                                 _p(k["var"]), _p(k["init"]), _p(k["chain"]), model.liborCap, int(self.scheme),
+                                 int(model.measure), int(model.stateSpace), _p(k["vol"]))
         h = ctypes.c_void_p()
         check(self._L.lmm_process_create(ctypes.byref(desc), brownianMotion._h, ctypes.byref(h)), "EulerSchemeFromProcessModel")
         self._h = h

@@ -53,8 +53,10 @@ def tenor_time_indices(cfg):
     return list(range(0, T + 1, step))
 
 
-def build(cfg, paths=None, precision=0, observe_tenor_only=True, seed=None):
-    """Assemble the finmath-style simulation of a workload on the GPU library."""
+def build(cfg, paths=None, precision=0, observe_tenor_only=True, seed=None, measure="SPOT", state_space="LOGNORMAL",
+          scheme=None):
+    """Assemble the finmath-style simulation of a workload on the GPU library (default: the
+    reference's SPOT measure, LOGNORMAL state space and EULER_FUNCTIONAL scheme)."""
     from . import lmm as F
     td = F.TimeDiscretizationFromArray(0.0, int(round(cfg["T_end"] / cfg["dt"])), cfg["dt"])
     tenor = F.TimeDiscretizationFromArray(0.0, int(round(cfg["tenor_end"] / cfg["period"])), cfg["period"])
@@ -64,11 +66,11 @@ def build(cfg, paths=None, precision=0, observe_tenor_only=True, seed=None):
     corr = F.LIBORCorrelationModelExponentialDecay(td, tenor, cfg["F"], cfg["corr_decay"])
     cov = F.LIBORCovarianceModelFromVolatilityAndCorrelation(td, tenor, vol, corr)
     model = F.LIBORMarketModelFromCovarianceModel.of(tenor, None, curve, F.DiscountCurveFromForwardCurve(curve), None, cov,
-                                                     None, {"measure": "SPOT", "stateSpace": "LOGNORMAL"})
+                                                     None, {"measure": measure, "stateSpace": state_space})
     P = cfg["paths"] if paths is None else paths
     bm = F.BrownianMotionFromMersenneRandomNumbers(td, cfg["F"], P, cfg["seed"] if seed is None else seed, precision)
     obs = tenor_time_indices(cfg) if observe_tenor_only else None
-    process = F.EulerSchemeFromProcessModel(model, bm, observedTimeIndices=obs)
+    process = F.EulerSchemeFromProcessModel(model, bm, scheme=scheme, observedTimeIndices=obs)
     return F.LIBORMonteCarloSimulationFromLIBORModel(process)
 
 

@@ -43,6 +43,17 @@ extern "C" {
 /* Discretisation schemes: EulerSchemeFromProcessModel.Scheme (montecarlo/process/EulerSchemeFromProcessModel.java:68-73). */
 #define LMM_SCHEME_EULER 0
 #define LMM_SCHEME_EULER_FUNCTIONAL 1
+#define LMM_SCHEME_PREDICTOR_CORRECTOR 2             /* FP64 only */
+#define LMM_SCHEME_PREDICTOR_CORRECTOR_FUNCTIONAL 3  /* FP64 only */
+
+/* LIBORMarketModelFromCovarianceModel.Measure and .StateSpace
+ * (…/interestrate/models/LIBORMarketModelFromCovarianceModel.java:1148-1189, :1081-1093).
+ * TERMINAL and NORMAL are FP64 only, and the adjoint takes SPOT, LOGNORMAL and the Euler
+ * schemes. */
+#define LMM_MEASURE_SPOT 0
+#define LMM_MEASURE_TERMINAL 1
+#define LMM_STATE_SPACE_LOGNORMAL 0
+#define LMM_STATE_SPACE_NORMAL 1
 
 /* Regression bases of the Bermudan swaption. */
 #define LMM_BASIS_REFERENCE 0  /* BermudanSwaption.getBasisFunctions: {1, P_short, P_short^2, P_long, P_long^2, 1/N} (…/products/BermudanSwaption.java:215-252) */
@@ -135,8 +146,8 @@ typedef struct {
     const double* discount_chain;   /* [N+1]      P^d(T_l), or NULL for no discount curve */
     double libor_cap;               /* liborCap property (default 1e5); +inf disables */
     int scheme;                     /* LMM_SCHEME_* */
-    int measure;                    /* 0 = SPOT (the only measure of this path) */
-    int state_space;                /* 0 = LOGNORMAL (the only state space of this path) */
+    int measure;                    /* LMM_MEASURE_* */
+    int state_space;                /* LMM_STATE_SPACE_* */
     const double* volatility;       /* [T][N] sigma_{i,j}, optional: the leaves of the vegas
                                        (NULL: sqrt(variance), i.e. rho_jj = 1) */
 } lmm_model_desc;

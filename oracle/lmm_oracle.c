@@ -522,6 +522,71 @@ struct orc_sim {
     double* tenor_copy;
 };
 
+/* LIBORMarketModelFromCovarianceModel.getDrift (:1125-1191) for components first..N-1 of the
+ * state L at simulation step i: SPOT sums the measure-change terms of l <= j (the running sum
+ * is updated before component j reads it), TERMINAL those of l > j (walking down from N-1, the
+ * sum is read before j adds to it); LOGNORMAL multiplies the one-step transform by L and adds
+ * -variance/2.  Scalar(+-delta).discount(L, delta) = 1/(L*(delta/(+-delta)) + 1/(+-delta))
+ * (M:stochastic/Scalar.java:321-328). */
+static void orc_drift(const orc_lmm* m, int i, int first, const double* L, double* mu)
+{
+    const int N = m->N, F = m->F;
+    const double* lam = m->loadings + (size_t)i * N * F;
+    const double* var = m->variance + (size_t)i * N;
+    const int lognormal = m->state_space == 0;
+    double S[64];
+    for (int k = 0; k < F; k++) S[k] = 0.0;
+    if (m->measure == 0) {
+        for (int j = first; j < N; j++) {
+            const double delta = m->tenor[j + 1] - m->tenor[j];
+            double os = 1.0 / (L[j] * (delta / delta) + 1.0 / delta);
+            if (lognormal) os = os * L[j];
+            const double* lj = lam + (size_t)j * F;
+            for (int k = 0; k < F; k++) S[k] = S[k] + os * lj[k];
+            double d = 0.0;
+            for (int k = 0; k < F; k++) d = d + S[k] * lj[k];
+            mu[j] = d;
+        }
+    } else {
+        for (int j = N - 1; j >= first; j--) {
+            const double delta = m->tenor[j + 1] - m->tenor[j];
+            double os = 1.0 / (L[j] * (delta / -delta) + 1.0 / -delta);
+            if (lognormal) os = os * L[j];
+            const double* lj = lam + (size_t)j * F;
+            double d = 0.0;
+            for (int k = 0; k < F; k++) d = d + S[k] * lj[k];
+            mu[j] = d;
+            for (int k = 0; k < F; k++) S[k] = S[k] + os * lj[k];
+        }
+    }
+    if (lognormal)
+        for (int j = first; j < N; j++) mu[j] = mu[j] + var[j] * -0.5;
+}
+
+/* applyStateSpaceTransform (:1200-1212): exp for LOGNORMAL, then the cap (Math.min). */
+static double orc_transform(const orc_lmm* m, double y)
+{
+    double v = m->state_space == 0 ? exp(y) : y;
+    if (!isinf(m->libor_cap) && v > m->libor_cap) v = m->libor_cap;
+    return v;
+}
+
+/* Terminal-measure numeraire at tenor index l from the state L at the process time index of
+ * T_l (getNumerairetUnAdjustedAtLIBORIndex :1029-1048): prod_{m=l}^{N-1} 1/(1 + L_m delta_m),
+ * as Scalar.discount steps while the value is deterministic (time index 0) and as
+ * RandomVariableFromDoubleArray.discount (x / (1 + L delta), :1308-1333) afterwards. */
+static double orc_terminal_numeraire(const orc_lmm* m, int l, const double* L, int deterministic)
+{
+    const int N = m->N;
+    double x = 1.0;
+    for (int k = l; k < N; k++) {
+        const double delta = m->tenor[k + 1] - m->tenor[k];
+        if (deterministic || k == l) x = 1.0 / (L[k] * (delta / x) + 1.0 / x);
+        else x = x / (1.0 + L[k] * delta);
+    }
+    return x;
+}
+
 static int first_alive_component(const double* tenor, int N1, double t)
 {
     /* LIBORMarketModelFromCovarianceModel.getDrift (:1127-1130) */
@@ -557,9 +622,14 @@ orc_sim* orc_simulate(const orc_lmm* m, int P, const double* dW, const uint8_t* 
         if (ti < 0) ti = -ti - 1;
         s->tenor_tidx[l] = ti;
     }
-    /* deterministic numeraire flags: N(T_0) = 1; N(T_{l+1}) deterministic iff N(T_l) is and L_l is read at index 0 */
-    s->num_det[0] = 1;
-    for (int l = 0; l < N; l++) s->num_det[l + 1] = (uint8_t)(s->num_det[l] && s->tenor_tidx[l] == 0);
+    /* deterministic numeraire flags.  SPOT: N(T_0) = 1; N(T_{l+1}) deterministic iff N(T_l) is
+     * and L_l is read at index 0.  TERMINAL: N(T_N) = 1 and N(T_l) with all rates read at index 0. */
+    if (m->measure == 0) {
+        s->num_det[0] = 1;
+        for (int l = 0; l < N; l++) s->num_det[l + 1] = (uint8_t)(s->num_det[l] && s->tenor_tidx[l] == 0);
+    } else {
+        for (int l = 0; l <= N; l++) s->num_det[l] = (uint8_t)(l == N || s->tenor_tidx[l] == 0);
+    }
 
     int* first = (int*)malloc(sizeof(int) * (size_t)T);
     double* dt = (double*)malloc(sizeof(double) * (size_t)T);
@@ -567,7 +637,11 @@ orc_sim* orc_simulate(const orc_lmm* m, int P, const double* dW, const uint8_t* 
         first[i] = first_alive_component(m->tenor, N + 1, m->times[i]);
         dt[i] = m->times[i + 1] - m->times[i];
     }
-    const int functional = (m->scheme == 1);
+    const int functional = (m->scheme == 1 || m->scheme == 3);
+    const int pc = (m->scheme == 2 || m->scheme == 3);
+    const int lognormal = (m->state_space == 0);
+    const int terminal = (m->measure == 1);
+    const int general = pc || !lognormal || terminal;
     const int capped = !isinf(m->libor_cap);
 
 #ifdef _OPENMP
@@ -576,6 +650,67 @@ orc_sim* orc_simulate(const orc_lmm* m, int P, const double* dW, const uint8_t* 
 #endif
     for (int p = 0; p < P; p++) {
         double L[256], Y[256], S[64], fixed_libor[257];
+        if (general) {
+            /* the general Euler step (EulerSchemeFromProcessModel.java:170-326) for any scheme,
+             * measure and state space */
+            double mu0[256], mu1[256], Ln[256];
+            for (int j = 0; j < N; j++) {
+                const double f = m->initial_forwards[j];
+                Y[j] = lognormal ? log(f > 0.0 ? f : 0.0) : f;
+                L[j] = orc_transform(m, Y[j]);
+            }
+            if (s->obs_slot[0] >= 0)
+                for (int j = 0; j < N; j++) s->states[((size_t)s->obs_slot[0] * N + j) * P + p] = L[j];
+            for (int l = 0; l < N; l++)
+                if (s->tenor_tidx[l] == 0) fixed_libor[l] = L[l];
+            if (terminal) {
+                for (int l = 0; l <= N; l++)
+                    if (s->tenor_tidx[l] == 0) s->numeraire[(size_t)l * P + p] = orc_terminal_numeraire(m, l, L, 1);
+            }
+            for (int n = 1; n <= T; n++) {
+                const int i = n - 1;
+                const double* lam = m->loadings + (size_t)i * N * F;
+                orc_drift(m, i, first[i], L, mu0);
+                for (int j = 0; j < N; j++) Ln[j] = L[j];
+                for (int j = first[i]; j < N; j++) {
+                    double y = functional ? (lognormal ? log(L[j]) : L[j]) : Y[j];
+                    y = y + mu0[j] * dt[i];
+                    for (int k = 0; k < F; k++) y = y + dW[((size_t)i * F + k) * (size_t)P + p] * lam[(size_t)j * F + k];
+                    Y[j] = y;
+                    Ln[j] = orc_transform(m, y);
+                }
+                if (pc) {
+                    /* corrector (:292-314): state += ((mu(predictor) - mu)/2) dt, transform again */
+                    orc_drift(m, i, first[i], Ln, mu1);
+                    for (int j = first[i]; j < N; j++) {
+                        Y[j] = Y[j] + ((mu1[j] - mu0[j]) / 2.0) * dt[i];
+                        Ln[j] = orc_transform(m, Y[j]);
+                    }
+                }
+                for (int j = 0; j < N; j++) L[j] = Ln[j];
+                if (s->obs_slot[n] >= 0)
+                    for (int j = 0; j < N; j++) s->states[((size_t)s->obs_slot[n] * N + j) * P + p] = L[j];
+                for (int l = 0; l < N; l++)
+                    if (s->tenor_tidx[l] == n) fixed_libor[l] = L[l];
+                if (terminal)
+                    for (int l = 0; l <= N; l++)
+                        if (s->tenor_tidx[l] == n) s->numeraire[(size_t)l * P + p] = orc_terminal_numeraire(m, l, L, 0);
+            }
+            if (!terminal) {
+                double Nv = 1.0;
+                s->numeraire[p] = 1.0;
+                for (int l = 0; l < N; l++) {
+                    const double delta = m->tenor[l + 1] - m->tenor[l];
+                    const double Ll = fixed_libor[l];
+                    if (s->num_det[l]) Nv = Ll * (delta * Nv) + Nv;
+                    else Nv = Nv * (1.0 + Ll * delta);
+                    s->numeraire[(size_t)(l + 1) * P + p] = Nv;
+                }
+            } else if (s->tenor_tidx[N] > T) {
+                s->numeraire[(size_t)N * P + p] = 1.0;
+            }
+            continue;
+        }
         /* initial state: Y0 = log(max(f,0)), L = cap(exp(Y0)) (:1081-1093, EulerScheme :186-190) */
         for (int j = 0; j < N; j++) {
             double f = m->initial_forwards[j];
@@ -686,6 +821,8 @@ double orc_standard_error(const double* x, int64_t n)
     return sqrt(var) / sqrt((double)n);
 }
 
+static double orc_numeraire_at_zero(const orc_sim* s);
+
 /* getNumeraire(time) at a tenor time (:860-876, :915-944). out[P]; returns 1 if deterministic. */
 int orc_sim_numeraire(const orc_sim* s, double time, double* out)
 {
@@ -699,14 +836,16 @@ int orc_sim_numeraire(const orc_sim* s, double time, double* out)
         return det;
     }
     const double pd = s->m.discount_chain[l];
+    /* nonDefaultableZeroBond = mean(N(T)^-1 * N(0)) (:869-874); N(0) = 1 under SPOT */
+    const double N0 = s->numeraire[0];
     if (det) {
-        double a = 1.0 * (1.0 / Nu[0]);
+        double a = N0 * (1.0 / Nu[0]);
         double v = (1.0 / pd) * (Nu[0] * a);
         for (int p = 0; p < P; p++) out[p] = v;
         return 1;
     }
     double* tmp = (double*)malloc(sizeof(double) * (size_t)P);
-    for (int p = 0; p < P; p++) tmp[p] = (1.0 / Nu[p]) * 1.0;
+    for (int p = 0; p < P; p++) tmp[p] = (1.0 / Nu[p]) * N0;
     double a = orc_kahan_average(tmp, P);
     free(tmp);
     for (int p = 0; p < P; p++) out[p] = (Nu[p] * a) / pd;
@@ -757,11 +896,12 @@ int orc_swaption(const orc_sim* s, double exercise, int nper, const double* fixi
         }
     }
     if (orc_sim_numeraire(s, exercise, num) < 0) { free(v); free(num); return -2; }
+    const double num0 = orc_numeraire_at_zero(s);
     for (int p = 0; p < P; p++) {
         double x = isnan(v[p]) ? v[p] : (v[p] > 0.0 ? v[p] : 0.0); /* Math.max(v, 0.0) */
         x = x / num[p];
         x = x * w;
-        x = x * 1.0;  /* numeraire at evaluation time 0 */
+        x = x * num0;  /* numeraire at evaluation time 0 (1 under SPOT) */
         x = x / w;
         v[p] = x;
     }
@@ -917,7 +1057,10 @@ int orc_bermudan(const orc_sim* s, int nper, const uint8_t* exercisable, const d
             ex[p] = cont ? ex[p] : fix;
         }
     }
-    for (int p = 0; p < P; p++) values[p] = (values[p] * 1.0) / w;
+    {
+        const double num0 = orc_numeraire_at_zero(s);  /* 1 under SPOT */
+        for (int p = 0; p < P; p++) values[p] = (values[p] * num0) / w;
+    }
     *value = orc_kahan_average(values, P);
     if (stderr_out) *stderr_out = orc_standard_error(values, P);
     if (per_path) memcpy(per_path, values, sizeof(double) * (size_t)P);
@@ -949,8 +1092,19 @@ int orc_bermudan_frozen(const orc_sim* s, int nper, const double* fixing, const 
             if (paid) x[p] += ((L[p] - strike[per]) * period_length[per]) * notional[per] / num[p];
         }
     }
-    if (!rc) *value = orc_kahan_average(x, P);
+    if (!rc) *value = orc_kahan_average(x, P) * orc_numeraire_at_zero(s);
     free(x);
     free(num);
     return rc;
+}
+
+/* The (adjusted, deterministic) numeraire at evaluation time 0 that product values are
+ * multiplied by (AbstractLIBORMonteCarloProduct: values * N(0) / w(0)); exactly 1 under SPOT. */
+static double orc_numeraire_at_zero(const orc_sim* s)
+{
+    double* tmp = (double*)malloc(sizeof(double) * (size_t)s->P);
+    orc_sim_numeraire(s, s->m.tenor[0], tmp);
+    const double v = tmp[0];
+    free(tmp);
+    return v;
 }

@@ -95,7 +95,10 @@ typedef struct {
     const double* initial_forwards; /* [N] */
     const double* discount_chain;   /* [N+1] P^d(T_i), or NULL for no discount curve */
     double libor_cap;               /* +inf disables the cap */
-    int scheme;                     /* 0 = EULER, 1 = EULER_FUNCTIONAL */
+    int scheme;                     /* 0 = EULER, 1 = EULER_FUNCTIONAL, 2 = PREDICTOR_CORRECTOR,
+                                       3 = PREDICTOR_CORRECTOR_FUNCTIONAL */
+    int measure;                    /* 0 = SPOT, 1 = TERMINAL */
+    int state_space;                /* 0 = LOGNORMAL, 1 = NORMAL */
 } orc_lmm;
 
 typedef struct orc_sim orc_sim;

@@ -44,7 +44,7 @@ class _OrcLmm(ctypes.Structure):
     _fields_ = [("T", ctypes.c_int), ("times", _D), ("N", ctypes.c_int), ("tenor", _D),
                 ("F", ctypes.c_int), ("loadings", _D), ("variance", _D),
                 ("initial_forwards", _D), ("discount_chain", _D), ("libor_cap", ctypes.c_double),
-                ("scheme", ctypes.c_int)]
+                ("scheme", ctypes.c_int), ("measure", ctypes.c_int), ("state_space", ctypes.c_int)]
 
 
 _lib = None
@@ -168,7 +168,9 @@ class Model:
     initial_forwards: np.ndarray  # [N]
     discount_chain: np.ndarray | None  # [N+1]
     libor_cap: float = 1e5
-    scheme: int = 1            # EULER_FUNCTIONAL
+    scheme: int = 1            # EULER_FUNCTIONAL (0 EULER, 2 PREDICTOR_CORRECTOR, 3 ..._FUNCTIONAL)
+    measure: int = 0           # SPOT (1 TERMINAL)
+    state_space: int = 0       # LOGNORMAL (1 NORMAL)
 
     @property
     def T(self):
@@ -186,7 +188,7 @@ class Model:
 def build_model(*, dt: float, T_end: float, period: float, tenor_end: float, F: int,
                 corr_decay: float, abcd, curve_nodes, curve_values, payment_offset=None,
                 discount_curve: bool = True, libor_cap: float = 1e5, scheme: int = 1,
-                vol_matrix=None) -> Model:
+                vol_matrix=None, measure: int = 0, state_space: int = 0) -> Model:
     L = lib()
     times = time_discretization(0.0, int(round(T_end / dt)), dt)
     tenor = time_discretization(0.0, int(round(tenor_end / period)), period)
@@ -215,7 +217,8 @@ def build_model(*, dt: float, T_end: float, period: float, tenor_end: float, F: 
         df = np.array([L.orc_discount_factor_from_forward_curve(_p(cx), _p(cy), len(cx), po, t) for t in tenor])
         chain = np.empty(N + 1)
         L.orc_numeraire_discount_chain(_p(tenor), N, _p(df), _p(chain))
-    return Model(times, tenor, factor, corr, vol, loadings, variance, fwd, chain, libor_cap, scheme)
+    return Model(times, tenor, factor, corr, vol, loadings, variance, fwd, chain, libor_cap, scheme, measure,
+                 state_space)
 
 
 class Simulation:
@@ -228,7 +231,7 @@ class Simulation:
                       None if model.discount_chain is None else f64(model.discount_chain)]
         t, tn, ld, var, fw, ch = self._keep
         self._s = _OrcLmm(model.T, _p(t), model.N, _p(tn), model.F, _p(ld), _p(var), _p(fw), _p(ch),
-                          model.libor_cap, model.scheme)
+                          model.libor_cap, model.scheme, model.measure, model.state_space)
         self.P = dW.shape[2]
         dW = f64(dW)
         obs = None if observe is None else np.ascontiguousarray(observe, dtype=np.uint8)

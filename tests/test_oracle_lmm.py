@@ -101,3 +101,49 @@ def test_euler_and_functional_schemes_agree_to_rounding():
     a = po.Simulation(mf, dW).process_value(20, 19)
     b = po.Simulation(me, dW).process_value(20, 19)
     assert np.allclose(a, b, rtol=1e-12, atol=0)
+
+
+# --------------------------------------------------------------------------- variants
+@pytest.mark.parametrize("measure,state_space,scheme", [(0, 0, 3), (0, 0, 2), (1, 0, 1), (0, 1, 1), (1, 1, 2)])
+def test_oracle_variants_reprice_zero_bonds(measure, state_space, scheme):
+    """Every scheme / measure / state space: the adjusted numeraire reprices the discount
+    curve's zero bonds, N(0) E[1/N(T_l)] = P^d(T_l), to rounding."""
+    cfg = dict(W.LMM20)
+    if state_space == 1:
+        a, b, c, d = cfg["abcd"]
+        cfg["abcd"] = (a * 0.05, b * 0.05, c, d * 0.05)
+    m = oracle_model(cfg, measure=measure, state_space=state_space, scheme=scheme)
+    P = 2000
+    sim = po.Simulation(m, po.brownian_increments(m.times, m.F, P, cfg["seed"]))
+    n0 = sim.numeraire(0.0)[0]
+    if measure == 0:
+        assert n0 == 1.0
+    for l in range(1, m.N + 1):
+        zb = n0 * np.mean(1.0 / sim.numeraire(m.tenor[l]))
+        assert zb == pytest.approx(m.discount_chain[l], rel=1e-13)
+
+
+def test_oracle_terminal_and_spot_agree_statistically():
+    cfg = W.LMM20
+    P = 20000
+    ex, fix, pay, K = W.swaption_schedule(cfg)
+    out = []
+    for measure in (0, 1):
+        m = oracle_model(cfg, measure=measure)
+        sim = po.Simulation(m, po.brownian_increments(m.times, m.F, P, cfg["seed"]))
+        out.append(sim.swaption(ex, fix, pay, K))
+    (vs, es), (vt, et) = out
+    assert abs(vs - vt) < 4.0 * np.hypot(es, et)
+
+
+def test_oracle_euler_and_functional_agree_to_rounding():
+    """EULER keeps the log state, EULER_FUNCTIONAL re-takes log(L) every step: without a cap
+    they differ only by the rounding of log(exp(y))."""
+    cfg = W.LMM20
+    P = 500
+    m1 = oracle_model(cfg, scheme=1)
+    m0 = oracle_model(cfg, scheme=0)
+    dW = po.brownian_increments(m1.times, m1.F, P, cfg["seed"])
+    a = po.Simulation(m1, dW).process_value(m1.T, m1.N - 1)
+    b = po.Simulation(m0, dW).process_value(m0.T, m0.N - 1)
+    np.testing.assert_allclose(a, b, rtol=1e-12)
