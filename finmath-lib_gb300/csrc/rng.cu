@@ -263,15 +263,21 @@ __device__ __forceinline__ void increments_loop(const RngParams& prm, uint32_t* 
     const int rpp = 32 / K;  // tile rows drained per warp pass
     const int dk = lane % K, r0 = warp * rpp + lane / K, rstep = (kRngThreads / 32) * rpp;
     const int rounds = (int)((v1 - v0 + kRound - 1) / kRound);
-    uint32_t* cur = x;
-    uint32_t* nxt = x + kMtN;
+    // Software pipeline: the words of round rd sit in `cur`; while the block turns them into
+    // increments it also twists them into round rd+1's words in `nxt` (the three phases of
+    // the twist share the three barrier intervals of the round's draws, tails and placement).
+    uint32_t* cur = x + kMtN;
+    uint32_t* nxt = x;
+    mt_regenerate(x, cur, tid, tail_n);  // round 0 from the jumped state; resets the tail queue
     for (int rd = 0; rd < rounds; rd++) {
-        mt_regenerate(cur, nxt, tid, tail_n);
+        const bool more = rd + 1 < rounds;
         const int nv = min(kRound, (int)(v1 - v0 - (int64_t)rd * kRound));
+        // ---- interval 1: twist phase 1 of round rd+1; draws of round rd
+        if (more && tid < 227) nxt[tid] = mt_next(cur[tid + kMtM], cur[tid], cur[tid + 1]);
         OutT hv0 = OutT(0), hv1 = OutT(0);
         int hp0 = -1, hf0 = 0, hp1 = -1, hf1 = 0;  // held draws: path (relative to ps; -1: none), row
         if (tid < nv) {
-            const uint2 ww = *reinterpret_cast<const uint2*>(nxt + 2 * tid);
+            const uint2 ww = *reinterpret_cast<const uint2*>(cur + 2 * tid);
             const uint32_t w1 = mt_temper(ww.x), w2 = mt_temper(ww.y);
             bool central;
             if constexpr (kExact) {
@@ -304,6 +310,11 @@ __device__ __forceinline__ void increments_loop(const RngParams& prm, uint32_t* 
             }
         }
         __syncthreads();
+        // ---- interval 2: twist phase 2; the round's tail draws on consecutive lanes
+        if (more && tid < 227) {
+            const int k = 227 + tid;
+            nxt[k] = mt_next(nxt[k - 227], cur[k], cur[k + 1]);
+        }
         const int n_tail = *tail_n;
         if (tid < n_tail) {
             const unsigned long long w = tail_w[tid];
@@ -327,7 +338,13 @@ __device__ __forceinline__ void increments_loop(const RngParams& prm, uint32_t* 
             hp1 = pos.x;
             hf1 = pos.y;
         }
-        // place the held draws; drain the tile whenever this round reaches past it
+        __syncthreads();
+        // ---- interval 3: twist phase 3; place the held draws, draining the tile when needed
+        if (more && tid < 170) {
+            const int k = 454 + tid;
+            nxt[k] = mt_next(nxt[k - 227], cur[k], (k == kMtN - 1) ? nxt[0] : cur[k + 1]);
+        }
+        if (tid == 0) *tail_n = 0;  // every lane read the round's tails before the barrier above
         uint32_t dl, rl;
         divmod_u32((uint32_t)(rtf + nv - 1), (uint32_t)TF, prm.magic_tf, dl, rl);
         const int plast = rpo + (int)dl;  // path of the round's last draw
@@ -346,6 +363,7 @@ __device__ __forceinline__ void increments_loop(const RngParams& prm, uint32_t* 
             __syncthreads();
             pt += K;
         }
+        __syncthreads();  // round rd+1's words complete; `cur` is free for round rd+2
         // advance the round's and this thread's positions by 312 draws
         rtf += a_tf;
         rpo += a_po;
