@@ -16,6 +16,7 @@
 // two factors per instruction).
 #include "lmm_internal.h"
 #include "reduce.cuh"
+#include "unroll_range.cuh"
 
 namespace lmm {
 namespace {
@@ -48,7 +49,7 @@ struct Smem32 {
 };
 
 template <int NMAX, int FMAX>
-__global__ void __launch_bounds__(kPathThreads) paths_fp32_kernel(const PathLaunch a, const float* __restrict__ lam32,
+__global__ void __launch_bounds__(kPathThreads, NMAX <= 40 ? 4 : 2) paths_fp32_kernel(const PathLaunch a, const float* __restrict__ lam32,
                                                                   const float* __restrict__ var32)
 {
     using SM = Smem32<NMAX, FMAX>;
@@ -122,9 +123,9 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp32_kernel(const PathLaun
         float2 S2[FH];
 #pragma unroll
         for (int m = 0; m < FH; m++) S2[m] = make_float2(0.0f, 0.0f);
-#pragma unroll
-        for (int j = 0; j < NMAX; j++) {
-            if (j < N && j >= first) {
+        for_up_from<NMAX>(first, [&](auto jc) {
+            constexpr int j = decltype(jc)::value;
+            if (j < N) {
                 float lr[FP];
 #pragma unroll
                 for (int q = 0; q < FP / 4; q++) {
@@ -152,7 +153,7 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp32_kernel(const PathLaun
                 if (capped && v > cap) v = cap;
                 L[j] = v;
             }
-        }
+        });
         const int slot = __ldg(a.d_obs_slot + i + 1);
         if (slot >= 0 && active) {
 #pragma unroll
