@@ -47,3 +47,29 @@ def test_brownian_increments_mixed_precision():
     for t in (0, 7, 19):
         g = bm.getBrownianIncrement(t, 2)
         assert np.max(np.abs(g - ref[t, 2])) < 2e-6 * np.max(np.abs(ref[t, 2]))
+
+
+@pytest.mark.parametrize("P,T,Fk", [(40000, 3, 2), (700, 80, 10), (12345, 11, 7)])
+def test_increments_tile_edges_fp64(P, T, Fk):
+    """The generator writes the increments through a tile of 16 (FP64) paths: fewer draws per
+    path than one round (several drains per round), 800 per path, and chunk edges inside paths."""
+    td = F.TimeDiscretizationFromArray(0.0, T, 0.25)
+    bm = F.BrownianMotionFromMersenneRandomNumbers(td, Fk, P, 7)
+    ref = po.brownian_increments(td.getAsDoubleArray(), Fk, P, 7)
+    for t in sorted({0, T // 2, T - 1}):
+        for k in sorted({0, Fk - 1}):
+            g = bm.getBrownianIncrement(t, k)
+            r = ref[t, k]
+            assert float(np.max(np.abs(g - r) / np.maximum(np.abs(r), 1e-300))) <= 4e-15
+
+
+@pytest.mark.parametrize("P,T,Fk", [(40000, 3, 2), (12345, 11, 7)])
+def test_increments_tile_edges_mixed(P, T, Fk):
+    """FP32 increments (tile of 32 paths) over every row against the FP64 oracle."""
+    td = F.TimeDiscretizationFromArray(0.0, T, 0.25)
+    bm = F.BrownianMotionFromMersenneRandomNumbers(td, Fk, P, 7, F.PRECISION_MIXED)
+    ref = po.brownian_increments(td.getAsDoubleArray(), Fk, P, 7)
+    for t in range(T):
+        for k in range(Fk):
+            g = bm.getBrownianIncrement(t, k)
+            assert np.max(np.abs(g - ref[t, k])) < 2e-6 * np.max(np.abs(ref[t, k]))
