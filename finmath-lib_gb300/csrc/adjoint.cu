@@ -605,7 +605,18 @@ template <typename R>
 int launch_rev_dispatch(const RevParams& a, const AdjTables<R>& tb, int threads, int blocks, cudaStream_t s)
 {
     if (a.N <= 24 && a.F <= 4) return launch_rev_threads<R, 24, 4>(a, tb, threads, blocks, s);
-    if (a.N <= 40 && a.F <= 10) return launch_rev_threads<R, 40, 10>(a, tb, threads, blocks, s);
+    if (a.N <= 40 && a.F <= 10) {
+        // the sweep touches components below n_eff only: products that end early (a portfolio's
+        // short swaps) take a narrower register-resident state (same factor-row pitch)
+        if constexpr (sizeof(R) == 4) {
+            if (threads == 128) {
+                if (a.n_eff <= 16) return launch_rev<R, 16, 10, 128>(a, tb, blocks, s);
+                if (a.n_eff <= 24) return launch_rev<R, 24, 10, 128>(a, tb, blocks, s);
+                if (a.n_eff <= 32) return launch_rev<R, 32, 10, 128>(a, tb, blocks, s);
+            }
+        }
+        return launch_rev_threads<R, 40, 10>(a, tb, threads, blocks, s);
+    }
     return fail(LMM_ERR_INVALID, "adjoint supports at most 40 forward rates and 10 factors");
 }
 

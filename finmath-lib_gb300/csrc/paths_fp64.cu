@@ -1,346 +1,10 @@
-// paths_fp64.cu -- K2 (plain FP64 form): fused Euler-log path kernel.
-//
-// Reference: EulerSchemeFromProcessModel.doPrecalculateProcess
-// (montecarlo/process/EulerSchemeFromProcessModel.java:170-326) with the drift of
-// LIBORMarketModelFromCovarianceModel.getDrift (…/models/LIBORMarketModelFromCovarianceModel.java:1125-1191),
-// the state-space transforms (:1200-1223) and the spot numeraire (:1017-1074).
-//
-// One thread owns one path.  Its forward vector lives in registers across all T
-// steps; the spot-measure drift is the running sum S_k += L_j/(L_j + 1/delta_j) * lambda_jk
-// over alive components j, so a step costs O(N*F) instead of O(N^2*F).  Only the time
-// indices that products observe are written, as [slot][component][path] rows (coalesced
-// across the warp).  The spot numeraire N(T_l) = prod (1 + L_i(T_i) delta_i) is formed
-// at the end from the frozen fixings, and each block writes compensated partial sums
-// of 1/N(T_l) for the numeraire adjustment.
-//
-// Compiled with -fmad=false: every + and * rounds separately, as in the reference's
-// Java; exp/log/division are CUDA's (division correctly rounded, exp/log within 1 ulp).
-#include "lmm_internal.h"
-#include "reduce.cuh"
+// paths_fp64.cu -- launchers of the FP64 path kernels (paths_fp64.cuh); the 64-rate
+// instantiations compile separately (paths_fp64_n64.cu) so that the two build in parallel.
+#include "paths_fp64.cuh"
 
 namespace lmm {
-namespace {
 
-constexpr int kPathThreads = 128;
-
-template <int NMAX, int FMAX, bool FUNCTIONAL>
-__global__ void __launch_bounds__(kPathThreads) paths_fp64_kernel(const PathLaunch a)
-{
-    const int p = blockIdx.x * kPathThreads + threadIdx.x;
-    const bool active = p < a.P;
-    const int N = a.N, F = a.F, P = a.P;
-    const bool capped = !isinf(a.libor_cap);
-    const double* dW = static_cast<const double*>(a.d_dw);
-    double* states = static_cast<double*>(a.d_states);
-
-    double L[NMAX];
-    double Y[FUNCTIONAL ? 1 : NMAX];
-#pragma unroll
-    for (int j = 0; j < NMAX; j++) {
-        if (j < N) {
-            // getInitialState (:1081-1093): log(max(f,0)); applyStateSpaceTransform (:1200-1212)
-            const double f = __ldg(a.d_init + j);
-            const double y0 = log(f > 0.0 ? f : 0.0);
-            double v = exp(y0);
-            if (capped && v > a.libor_cap) v = a.libor_cap;
-            L[j] = v;
-            if (!FUNCTIONAL) Y[FUNCTIONAL ? 0 : j] = y0;
-        } else {
-            L[j] = 0.0;
-        }
-    }
-    {
-        const int slot = __ldg(a.d_obs_slot + 0);
-        if (slot >= 0 && active) {
-#pragma unroll
-            for (int j = 0; j < NMAX; j++)
-                if (j < N) states[((size_t)slot * N + j) * P + p] = L[j];
-        }
-        if (a.d_ckpt && active) {
-            double* ck = static_cast<double*>(a.d_ckpt);
-#pragma unroll
-            for (int j = 0; j < NMAX; j++)
-                if (j < N) ck[(size_t)j * P + p] = L[j];
-        }
-    }
-
-    for (int i = 0; i < a.T; i++) {
-        const int first = __ldg(a.d_first + i);
-        const double dt = __ldg(a.d_dt + i);
-        const double* lam = a.d_loadings + (size_t)i * N * F;
-        const double* var_half = a.d_var_half + (size_t)i * N;
-        double dw[FMAX];
-#pragma unroll
-        for (int k = 0; k < FMAX; k++) dw[k] = (k < F && active) ? dW[((size_t)i * F + k) * P + p] : 0.0;
-        double S[FMAX];
-#pragma unroll
-        for (int k = 0; k < FMAX; k++) S[k] = 0.0;
-#pragma unroll
-        for (int j = 0; j < NMAX; j++) {
-            if (j < N && j >= first) {
-                const double Lj = L[j];
-                // Scalar(delta).discount(L, delta) = 1/(L*(delta/delta) + 1/delta) (stochastic/Scalar.java:321-328),
-                // times L (:1149-1153); delta/delta is exactly 1.0 and 1/delta is precomputed.
-                const double os = (1.0 / (Lj + __ldg(a.d_inv_delta + j))) * Lj;
-                double mu = 0.0;
-                double lj[FMAX];
-#pragma unroll
-                for (int k = 0; k < FMAX; k++) {
-                    if (k < F) {
-                        lj[k] = __ldg(lam + j * F + k);
-                        S[k] = S[k] + os * lj[k];  // :1156-1158
-                    }
-                }
-#pragma unroll
-                for (int k = 0; k < FMAX; k++)
-                    if (k < F) mu = mu + S[k] * lj[k];  // :1159 (addSumProduct, left to right)
-                mu = mu + __ldg(var_half + j);           // :1183-1189, variance * -0.5
-                // Euler step (EulerSchemeFromProcessModel.java:235-255)
-                double y = FUNCTIONAL ? log(Lj) : Y[FUNCTIONAL ? 0 : j];
-                y = y + mu * dt;
-#pragma unroll
-                for (int k = 0; k < FMAX; k++)
-                    if (k < F) y = y + dw[k] * lj[k];
-                if (!FUNCTIONAL) Y[FUNCTIONAL ? 0 : j] = y;
-                double v = exp(y);
-                if (capped && v > a.libor_cap) v = a.libor_cap;
-                L[j] = v;
-            }
-        }
-        const int slot = __ldg(a.d_obs_slot + i + 1);
-        if (slot >= 0 && active) {
-#pragma unroll
-            for (int j = 0; j < NMAX; j++)
-                if (j < N) states[((size_t)slot * N + j) * P + p] = L[j];
-        }
-        if (a.d_ckpt && active && (i + 1) % a.ckpt_stride == 0) {
-            double* ck = static_cast<double*>(a.d_ckpt) + (size_t)((i + 1) / a.ckpt_stride) * N * P;
-#pragma unroll
-            for (int j = 0; j < NMAX; j++)
-                if (j < N) ck[(size_t)j * P + p] = L[j];
-        }
-    }
-
-    // Spot numeraire from the frozen fixings L_l(T_l) (:1050-1066): Scalar.accrue while
-    // the numeraire is deterministic, RandomVariableFromDoubleArray.accrue afterwards.
-    double Nv = 1.0;
-    if (active) a.d_numeraire[p] = 1.0;
-    if (a.d_inv_numeraire && active) a.d_inv_numeraire[p] = 1.0;
-#pragma unroll
-    for (int l = 0; l < NMAX; l++) {
-        if (l < N) {
-            const double delta = __ldg(a.d_delta + l);
-            if (l < a.num_det_prefix) Nv = L[l] * (delta * Nv) + Nv;
-            else Nv = Nv * (1.0 + L[l] * delta);
-            if (active) a.d_numeraire[(size_t)(l + 1) * P + p] = Nv;
-            // numeraire adjustment input: mean of N(T)^-1 * N(0) (:869-874)
-            const double inv = (1.0 / Nv) * 1.0;
-            if (a.d_inv_numeraire && active) a.d_inv_numeraire[(size_t)(l + 1) * P + p] = inv;
-            block_dd_partial(active ? inv : 0.0, a.d_inv_num_partials + ((size_t)blockIdx.x * N + l) * 2);
-        }
-    }
-}
-
-// ------------------------------------------------------------------ general form
-// getDrift (LIBORMarketModelFromCovarianceModel.java:1125-1191) for any measure and state
-// space: SPOT sums the one-step transforms of l <= j (updated before j reads them), TERMINAL
-// those of l > j (walking down, read before j adds to them); LOGNORMAL multiplies the
-// transform by L and adds -variance/2.  Scalar(+-delta).discount(L, delta) =
-// 1/(L (delta/(+-delta)) + 1/(+-delta)) (stochastic/Scalar.java:321-328).
-template <int NMAX, int FMAX>
-__device__ __forceinline__ void drift_general(const PathLaunch& a, int i, int first, const double* L, double* mu)
-{
-    const int N = a.N, F = a.F;
-    const double* lam = a.d_loadings + (size_t)i * N * F;
-    const bool lognormal = a.state_space == 0;
-    double S[FMAX];
-#pragma unroll
-    for (int k = 0; k < FMAX; k++) S[k] = 0.0;
-    if (a.measure == 0) {
-#pragma unroll
-        for (int j = 0; j < NMAX; j++) {
-            if (j < N && j >= first) {
-                const double delta = __ldg(a.d_delta + j);
-                double os = 1.0 / (L[j] * (delta / delta) + 1.0 / delta);
-                if (lognormal) os = os * L[j];
-                double d = 0.0;
-#pragma unroll
-                for (int k = 0; k < FMAX; k++)
-                    if (k < F) S[k] = S[k] + os * __ldg(lam + j * F + k);
-#pragma unroll
-                for (int k = 0; k < FMAX; k++)
-                    if (k < F) d = d + S[k] * __ldg(lam + j * F + k);
-                mu[j] = d;
-            }
-        }
-    } else {
-#pragma unroll
-        for (int jj = NMAX - 1; jj >= 0; jj--) {
-            const int j = jj;
-            if (j < N && j >= first) {
-                const double delta = __ldg(a.d_delta + j);
-                double os = 1.0 / (L[j] * (delta / -delta) + 1.0 / -delta);
-                if (lognormal) os = os * L[j];
-                double d = 0.0;
-#pragma unroll
-                for (int k = 0; k < FMAX; k++)
-                    if (k < F) d = d + S[k] * __ldg(lam + j * F + k);
-                mu[j] = d;
-#pragma unroll
-                for (int k = 0; k < FMAX; k++)
-                    if (k < F) S[k] = S[k] + os * __ldg(lam + j * F + k);
-            }
-        }
-    }
-    if (lognormal) {
-#pragma unroll
-        for (int j = 0; j < NMAX; j++)
-            if (j < N && j >= first) mu[j] = mu[j] + __ldg(a.d_variance + (size_t)i * N + j) * -0.5;
-    }
-}
-
-// applyStateSpaceTransform (:1200-1212): exp for LOGNORMAL, then the cap
-__device__ __forceinline__ double transform_general(const PathLaunch& a, double y)
-{
-    double v = a.state_space == 0 ? exp(y) : y;
-    if (!isinf(a.libor_cap) && v > a.libor_cap) v = a.libor_cap;
-    return v;
-}
-
-// TERMINAL numeraire at tenor index l from the state at the time of T_l
-// (getNumerairetUnAdjustedAtLIBORIndex :1029-1048): Scalar.discount steps while deterministic,
-// RandomVariableFromDoubleArray.discount (x / (1 + L delta), :1308-1333) afterwards
-template <int NMAX>
-__device__ __forceinline__ double terminal_numeraire(const PathLaunch& a, int l, const double* L, bool deterministic)
-{
-    double x = 1.0;
-#pragma unroll
-    for (int k = 0; k < NMAX; k++) {
-        if (k >= l && k < a.N) {
-            const double delta = __ldg(a.d_delta + k);
-            if (deterministic || k == l) x = 1.0 / (L[k] * (delta / x) + 1.0 / x);
-            else x = x / (1.0 + L[k] * delta);
-        }
-    }
-    return x;
-}
-
-// The Euler scheme (EulerSchemeFromProcessModel.java:170-326) for any scheme, measure and state
-// space: the predictor-corrector step adds ((mu(predictor) - mu)/2) dt to the state and
-// transforms again (:292-314).  Rarely used forms: one kernel with run-time switches.
-template <int NMAX, int FMAX>
-__global__ void __launch_bounds__(kPathThreads) paths_fp64_general_kernel(const PathLaunch a)
-{
-    const int p = blockIdx.x * kPathThreads + threadIdx.x;
-    const bool active = p < a.P;
-    const int N = a.N, F = a.F, P = a.P;
-    const bool functional = a.scheme == 1 || a.scheme == 3;
-    const bool pc = a.scheme == 2 || a.scheme == 3;
-    const bool lognormal = a.state_space == 0;
-    const bool terminal = a.measure == 1;
-    const double* dW = static_cast<const double*>(a.d_dw);
-    double* states = static_cast<double*>(a.d_states);
-    double L[NMAX], Y[NMAX], mu0[NMAX], Ln[NMAX];
-#pragma unroll
-    for (int j = 0; j < NMAX; j++) {
-        L[j] = Y[j] = mu0[j] = Ln[j] = 0.0;
-        if (j < N) {
-            const double f = __ldg(a.d_init + j);
-            Y[j] = lognormal ? log(f > 0.0 ? f : 0.0) : f;
-            L[j] = transform_general(a, Y[j]);
-        }
-    }
-    {
-        const int slot = __ldg(a.d_obs_slot + 0);
-        if (slot >= 0 && active) {
-#pragma unroll
-            for (int j = 0; j < NMAX; j++)
-                if (j < N) states[((size_t)slot * N + j) * P + p] = L[j];
-        }
-        if (terminal && active)
-            for (int l = 0; l <= N; l++)
-                if (__ldg(a.d_tenor_tidx + l) == 0) a.d_numeraire[(size_t)l * P + p] = terminal_numeraire<NMAX>(a, l, L, true);
-    }
-    for (int i = 0; i < a.T; i++) {
-        const int first = __ldg(a.d_first + i);
-        const double dt = __ldg(a.d_dt + i);
-        const double* lam = a.d_loadings + (size_t)i * N * F;
-        drift_general<NMAX, FMAX>(a, i, first, L, mu0);
-#pragma unroll
-        for (int j = 0; j < NMAX; j++) {
-            Ln[j] = L[j];
-            if (j < N && j >= first) {
-                double y = functional ? (lognormal ? log(L[j]) : L[j]) : Y[j];
-                y = y + mu0[j] * dt;
-#pragma unroll
-                for (int k = 0; k < FMAX; k++)
-                    if (k < F) y = y + (active ? dW[((size_t)i * F + k) * P + p] : 0.0) * __ldg(lam + j * F + k);
-                Y[j] = y;
-                Ln[j] = transform_general(a, y);
-            }
-        }
-        if (pc) {
-            double mu1[NMAX];
-            drift_general<NMAX, FMAX>(a, i, first, Ln, mu1);
-#pragma unroll
-            for (int j = 0; j < NMAX; j++) {
-                if (j < N && j >= first) {
-                    Y[j] = Y[j] + ((mu1[j] - mu0[j]) / 2.0) * dt;
-                    Ln[j] = transform_general(a, Y[j]);
-                }
-            }
-        }
-#pragma unroll
-        for (int j = 0; j < NMAX; j++) L[j] = Ln[j];
-        const int slot = __ldg(a.d_obs_slot + i + 1);
-        if (slot >= 0 && active) {
-#pragma unroll
-            for (int j = 0; j < NMAX; j++)
-                if (j < N) states[((size_t)slot * N + j) * P + p] = L[j];
-        }
-        if (terminal && active)
-            for (int l = 0; l <= N; l++)
-                if (__ldg(a.d_tenor_tidx + l) == i + 1)
-                    a.d_numeraire[(size_t)l * P + p] = terminal_numeraire<NMAX>(a, l, L, false);
-    }
-    if (!terminal) {
-        // SPOT numeraire from the frozen fixings (as paths_fp64_kernel)
-        double Nv = 1.0;
-        if (active) a.d_numeraire[p] = 1.0;
-#pragma unroll
-        for (int l = 0; l < NMAX; l++) {
-            if (l < N) {
-                const double delta = __ldg(a.d_delta + l);
-                if (l < a.num_det_prefix) Nv = L[l] * (delta * Nv) + Nv;
-                else Nv = Nv * (1.0 + L[l] * delta);
-                if (active) a.d_numeraire[(size_t)(l + 1) * P + p] = Nv;
-            }
-        }
-    } else if (active && __ldg(a.d_tenor_tidx + N) > a.T) {
-        a.d_numeraire[(size_t)N * P + p] = 1.0;
-    }
-    // block partials of N(T_l)^-1 * N(0) for the numeraire adjustment (:869-874)
-    const double N0 = active ? a.d_numeraire[p] : 1.0;
-    for (int l = 1; l <= N; l++) {
-        const double inv = active ? (1.0 / a.d_numeraire[(size_t)l * P + p]) * N0 : 0.0;
-        block_dd_partial(inv, a.d_inv_num_partials + ((size_t)blockIdx.x * N + (l - 1)) * 2);
-    }
-}
-
-template <int NMAX, int FMAX>
-int launch_t(const PathLaunch& a, cudaStream_t s, int blocks)
-{
-    if (a.scheme > 1 || a.measure != 0 || a.state_space != 0)
-        paths_fp64_general_kernel<NMAX, FMAX><<<blocks, kPathThreads, 0, s>>>(a);
-    else if (a.scheme == 1)
-        paths_fp64_kernel<NMAX, FMAX, true><<<blocks, kPathThreads, 0, s>>>(a);
-    else
-        paths_fp64_kernel<NMAX, FMAX, false><<<blocks, kPathThreads, 0, s>>>(a);
-    LMM_CUDA(cudaGetLastError());
-    return LMM_OK;
-}
-
-}  // namespace
+int launch_paths_fp64_n64(const PathLaunch& a, cudaStream_t s, int blocks);
 
 int path_blocks(int P) { return (P + kPathThreads - 1) / kPathThreads; }
 
@@ -351,7 +15,7 @@ int launch_paths_fp64(const PathLaunch& a, cudaStream_t s, int* blocks_out)
     KernelTimer kt(K_PATHS_FP64, s);
     if (a.N <= 24 && a.F <= 4) return launch_t<24, 4>(a, s, blocks);
     if (a.N <= 40 && a.F <= 10) return launch_t<40, 10>(a, s, blocks);
-    if (a.N <= 64 && a.F <= 16) return launch_t<64, 16>(a, s, blocks);
+    if (a.N <= 64 && a.F <= 16) return launch_paths_fp64_n64(a, s, blocks);
     return fail(LMM_ERR_INVALID, "FP64 path kernel supports at most 64 forward rates and 16 factors");
 }
 
