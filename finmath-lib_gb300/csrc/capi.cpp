@@ -877,7 +877,10 @@ static int bermudan_run(lmm_process* pr, const lmm_bermudan_desc* d, double* val
     if (!pr->d_under) {
         if (!rc) rc = dalloc(&pr->d_under, (size_t)pr->P, s);
         if (!rc) rc = dalloc(&pr->d_ex, (size_t)pr->P, s);
-        if (!rc) rc = dalloc(&pr->d_rhs, (size_t)blocks * 6 * 2, s);
+        // X^T y block partials, then the step kernel's completion counter (zero between dates)
+        if (!rc) rc = dalloc(&pr->d_rhs, (size_t)blocks * 6 * 2 + 2, s);
+        if (!rc) rc = cudaMemsetAsync(pr->d_rhs, 0, sizeof(double) * ((size_t)blocks * 6 * 2 + 2), s) == cudaSuccess
+                          ? LMM_OK : fail(LMM_ERR_CUDA, "memset");
         if (!rc) rc = dalloc(&pr->d_beta, (size_t)64 * 6, s);
         if (!rc) rc = dalloc(&pr->d_svd, (size_t)64 * 80, s);
         if (!rc) rc = dalloc(&pr->d_period_length, (size_t)64, s);
@@ -1416,7 +1419,9 @@ int lmm_portfolio_create(lmm_process* pr, const lmm_portfolio_desc* desc, lmm_po
         if (!rc) rc = dalloc(&b.basis, (size_t)std::max(1, pf->max_ne) * 5 * P, s);
         if (!rc) rc = dalloc(&b.gram, (size_t)(blocks + 64 + (pf->gram_blocks > 0 ? pf->gram_blocks * 64 : 0)) * 40, s);
         if (!rc) rc = dalloc(&b.svd, (size_t)64 * 80, s);
-        if (!rc) rc = dalloc(&b.rhs, (size_t)blocks * 12, s);
+        if (!rc) rc = dalloc(&b.rhs, (size_t)blocks * 12 + 2, s);  // partials, then the completion counter
+        if (!rc) rc = cudaMemsetAsync(b.rhs, 0, sizeof(double) * ((size_t)blocks * 12 + 2), s) == cudaSuccess
+                          ? LMM_OK : fail(LMM_ERR_CUDA, "memset");
         if (!rc) rc = dalloc(&b.beta, (size_t)64 * 6, s);
         if (!rc) rc = dalloc(&b.reduce, (size_t)2 * 1024 + 2, s);
         if (pf->greeks) {

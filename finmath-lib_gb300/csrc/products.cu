@@ -377,6 +377,40 @@ __global__ void __launch_bounds__(32) bermudan_svd_kernel(const double* partials
     }
 }
 
+// X^T y sums of one date and beta = V diag(1/s) U^T (X^T y) with the SVD's cutoff,
+// in the oracle's order (MonteCarloConditionalExpectationRegression.java:141-147).  Run by
+// one block of at least 6 warps (all its threads call it).
+__device__ void regression_solve(const double* partials, int blocks, int P, const double* svd, double* beta_out)
+{
+    __shared__ double b[kRhs];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (warp < kRhs) {
+        dd acc{0.0, 0.0};
+        for (int k = lane; k < blocks; k += 32) {
+            const double* q = partials + ((size_t)k * kRhs + warp) * 2;
+            acc = dd_add(acc, dd{q[0], q[1]});
+        }
+        acc = warp_dd_sum(acc);
+        if (lane == 0) b[warp] = (acc.hi + acc.lo) / (double)P;
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        const double* U = svd;
+        const double* s = svd + 36;
+        const double* V = svd + 42;
+        const double tol = svd[78];
+        const int i = threadIdx.x;
+        double acc = 0.0;
+        for (int j = 0; j < 6; j++) {
+            if (!(s[j] > tol)) continue;
+            double utb = 0.0;
+            for (int r = 0; r < 6; r++) utb += U[r * 6 + j] * b[r];
+            acc += V[i * 6 + j] * (utb / s[j]);
+        }
+        beta_out[i] = acc;
+    }
+}
+
 struct BermStepParams {
     BermShared sh;
     int cur;                   // period processed by this launch (-1: final pass)
@@ -387,7 +421,9 @@ struct BermStepParams {
     double* values;
     double* under;
     double* ex;
-    double* partials;          // [blocks][6][2]
+    double* partials;          // [blocks][6][2], then an unsigned completion counter
+    const double* svd_cur;     // SVD factors of the date cur_ex (when it regresses)
+    double* beta_cur;          // its coefficients, written by the launch's last block
     int init;
 };
 
@@ -462,40 +498,19 @@ __global__ void __launch_bounds__(kProdThreads) bermudan_step_kernel(const BermS
                 }
             }
         }
-    }
-}
-
-// X^T y sums of one date and beta = V diag(1/s) U^T (X^T y) with the SVD's cutoff,
-// in the oracle's order (MonteCarloConditionalExpectationRegression.java:141-147).
-__global__ void __launch_bounds__(192) bermudan_apply_kernel(const double* partials, int blocks, int P, const double* svd,
-                                                             double* beta_out)
-{
-    __shared__ double b[kRhs];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (warp < kRhs) {
-        dd acc{0.0, 0.0};
-        for (int k = lane; k < blocks; k += 32) {
-            const double* q = partials + ((size_t)k * kRhs + warp) * 2;
-            acc = dd_add(acc, dd{q[0], q[1]});
+        // the last block to finish reduces every block's partials (in block order) and solves
+        // for this date's coefficients; nothing waits on another block
+        __shared__ bool last;
+        __threadfence();
+        __syncthreads();
+        unsigned int* done = reinterpret_cast<unsigned int*>(a.partials + (size_t)gridDim.x * kRhs * 2);
+        if (threadIdx.x == 0) last = atomicAdd(done, 1u) == gridDim.x - 1;
+        __syncthreads();
+        if (last) {
+            __threadfence();
+            regression_solve(a.partials, gridDim.x, sh.P, a.svd_cur, a.beta_cur);
+            if (threadIdx.x == 0) *done = 0u;  // ready for the next date
         }
-        acc = warp_dd_sum(acc);
-        if (lane == 0) b[warp] = (acc.hi + acc.lo) / (double)P;
-    }
-    __syncthreads();
-    if (threadIdx.x < 6) {
-        const double* U = svd;
-        const double* s = svd + 36;
-        const double* V = svd + 42;
-        const double tol = svd[78];
-        const int i = threadIdx.x;
-        double acc = 0.0;
-        for (int j = 0; j < 6; j++) {
-            if (!(s[j] > tol)) continue;
-            double utb = 0.0;
-            for (int r = 0; r < 6; r++) utb += U[r * 6 + j] * b[r];
-            acc += V[i * 6 + j] * (utb / s[j]);
-        }
-        beta_out[i] = acc;
     }
 }
 
@@ -680,6 +695,8 @@ int launch_bermudan(const ProductView& v, const BermudanLaunch& a, const Bermuda
     for (int per = a.nper - 1; per >= -1; per--) {
         prm.cur = per;
         prm.cur_ex = per >= 0 ? ex_of_period[per] : -1;
+        prm.svd_cur = prm.cur_ex >= 0 ? sc.d_svd + (size_t)prm.cur_ex * kSvdStride : nullptr;
+        prm.beta_cur = prm.cur_ex >= 0 ? sc.d_beta + (size_t)prm.cur_ex * 6 : nullptr;
         prm.pending_ex = pending;
         prm.pending_fixing = pending >= 0 ? a.per[ex_period[pending]].fixing : 0.0;
         prm.init = per == a.nper - 1;
@@ -691,14 +708,7 @@ int launch_bermudan(const ProductView& v, const BermudanLaunch& a, const Bermuda
         }
         if (launches) (*launches)++;
         pending = -1;
-        if (per >= 0 && prm.cur_ex >= 0) {
-            KernelTimer kt(K_BERMUDAN_SOLVE, s);
-            bermudan_apply_kernel<<<1, 192, 0, s>>>(sc.d_partials, blocks, v.P, sc.d_svd + (size_t)prm.cur_ex * kSvdStride,
-                                                    sc.d_beta + (size_t)prm.cur_ex * 6);
-            LMM_CUDA(cudaGetLastError());
-            if (launches) (*launches)++;
-            pending = prm.cur_ex;
-        }
+        if (per >= 0 && prm.cur_ex >= 0) pending = prm.cur_ex;  // its coefficients come from the step's last block
     }
     return LMM_OK;
 }
