@@ -38,7 +38,7 @@ int cuda_fail(cudaError_t e, const char* what)
 // ------------------------------------------------------------------ stats
 static const char* kKernelNames[K_COUNT] = {
     "mt19937_jump_generate", "lmm_paths_fp64", "lmm_paths_fp32", "numeraire_adjust_reduce", "swaption_value",
-    "bermudan_regress_step", "bermudan_solve6", "value_mean_stderr", "lmm_adjoint", "portfolio_persistent", "misc"};
+    "bermudan_regress_step", "bermudan_solve6", "value_mean_stderr", "lmm_adjoint", "portfolio_graph", "misc"};
 
 const char* kernel_name(int id) { return (id >= 0 && id < K_COUNT) ? kKernelNames[id] : "?"; }
 
@@ -1468,7 +1468,10 @@ int lmm_portfolio_run(lmm_portfolio* pf, double* values, double* errors, double*
     portfolio_fingerprint(pf, now);
     if (std::memcmp(now, pf->captured, sizeof(now)) != 0 && (rc = portfolio_record(pf))) return rc;
     cudaStream_t s = pf->stream;
-    LMM_CUDA(cudaGraphLaunch(pf->exec, s));
+    {
+        KernelTimer kt(K_PORTFOLIO, s);  // one launch of the recorded graph (all products)
+        LMM_CUDA(cudaGraphLaunch(pf->exec, s));
+    }
     const int n = pf->n, T = pr->T, N = pr->N, P = pr->P;
     std::vector<double> mv(2 * (size_t)n);
     std::vector<unsigned long long> ts(n + 1);

@@ -37,7 +37,7 @@ enum KernelId : int {
     K_BERMUDAN_SOLVE,
     K_VALUE_REDUCE,
     K_ADJOINT,
-    K_PORTFOLIO,
+    K_PORTFOLIO,        // one launch of a recorded portfolio graph
     K_MISC,
     K_COUNT
 };
