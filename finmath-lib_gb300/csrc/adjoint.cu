@@ -11,16 +11,18 @@
 //   forward  os_j = L_j/(L_j + 1/d_j),  S_k += os_j lam_jk,  mu_j = sum_k S_k lam_jk - sigma_ij^2/2,
 //            Y_j' = Y_j + mu_j dt + sum_k dW_k lam_jk,  L_j' = exp(Y_j')          (lam_jk = sigma_ij f_jk)
 //   reverse  mubar_j = Ybar'_j dt,  R_k = sum_{l>=j} mubar_l lam_lk (a reverse running sum),
-//            osbar_j = sum_k lam_jk R_k,  Ybar_j = Ybar'_j + osbar_j (1/d_j)/(L_j+1/d_j)^2 L_j,
+//            osbar_j = sum_k lam_jk R_k,  Ybar_j = Ybar'_j + osbar_j os_j (1 - os_j),
 //            lambar_jk = mubar_j S_k^(j) + os_j R_k + Ybar'_j dW_k,
 //            sigmabar_ij = sum_k lambar_jk f_jk - mubar_j sigma_ij
 //
-// so a reverse step costs O(N F) like the forward one.  The path state is recomputed
-// from checkpoints written by the forward kernel every `stride` steps (the states of a
-// segment live in thread-local memory).  The Bermudan's exercise decisions are frozen from
-// the forward valuation (regression coefficients fixed); the seed kernel turns each path's
-// realised cash flows into adjoints of the fixings L_m(T_m), through the payment numeraires,
-// their cross-path adjustment a_l = mean(1/N_l) (:869-874) and the numeraire chain.
+// so a reverse step costs O(N F) like the forward one.  The forward rates come from the
+// path kernel's checkpoints: with stride 1 (the default: HBM holds every state) one sweep
+// reads them directly; with a larger stride a replay kernel regenerates each segment from
+// its checkpoint into a global buffer before that segment's sweep.  The Bermudan's exercise
+// decisions are frozen from the forward valuation (regression coefficients fixed); the seed
+// kernel turns each path's realised cash flows into adjoints of the fixings L_m(T_m),
+// through the payment numeraires, their cross-path adjustment a_l = mean(1/N_l)
+// (:869-874) and the numeraire chain.
 #include <math_constants.h>
 
 #include <algorithm>

@@ -10,7 +10,9 @@
 // polynomials (one per set bit of its chunk index; each jump is an XOR of windows of
 // the raw word sequence held in shared memory), then regenerates 624 words at a time
 // in three dependency phases (227/227/170 words) over a double-buffered state, and
-// converts word pairs to values.  Uniforms are bit-identical to the single stream.
+// converts word pairs to values.  Uniforms are bit-identical to the single stream.  The
+// increments leave through a shared-memory tile (increments_loop) so that each [t][f] row
+// is written in 128-byte segments although the stream runs path-major.
 //
 // This translation unit is compiled with -fmad=false: the FP64 inverse normal must
 // round exactly like the reference's unfused Java arithmetic.
