@@ -277,7 +277,8 @@ __global__ void __launch_bounds__(kProdThreads) bermudan_gram_kernel(const BermS
         for (int i = 0; i < 5; i++)
 #pragma unroll
             for (int j = i; j < 5; j++) {
-                acc[k] = acc[k] + B[i] * B[j];
+                // the mixed form fuses (no parity constraint); the FP64 form rounds the product first
+                acc[k] = sizeof(TS) == 4 ? fma(B[i], B[j], acc[k]) : acc[k] + B[i] * B[j];
                 k++;
             }
     }
@@ -459,7 +460,10 @@ __global__ void __launch_bounds__(kProdThreads) bermudan_step_kernel(const BermS
             // conditional expectation X beta (:104-107), then choose (:139, :141)
             double ce = 1.0 * beta[0];
 #pragma unroll
-            for (int i = 1; i < 6; i++) ce = ce + bprev[(size_t)(i - 1) * sh.P + p] * beta[i];
+            for (int i = 1; i < 6; i++) {
+                const double bi = bprev[(size_t)(i - 1) * sh.P + p];
+                ce = sizeof(TS) == 4 ? fma(bi, beta[i], ce) : ce + bi * beta[i];
+            }
             const bool cont = ce >= 0.0;
             v = cont ? v : u;
             if (!cont) a.ex[p] = a.pending_fixing;
@@ -476,7 +480,10 @@ __global__ void __launch_bounds__(kProdThreads) bermudan_step_kernel(const BermS
                 const double y = v - u;
                 acc[0] = acc[0] + y * 1.0;
 #pragma unroll
-                for (int i = 0; i < 5; i++) acc[1 + i] = acc[1 + i] + y * bcur[(size_t)i * sh.P + p];
+                for (int i = 0; i < 5; i++) {
+                    const double bi = bcur[(size_t)i * sh.P + p];
+                    acc[1 + i] = sizeof(TS) == 4 ? fma(y, bi, acc[1 + i]) : acc[1 + i] + y * bi;
+                }
             }
         } else {
             v = (v * numeraire_adj(sh.num, 0, 0)) / w;  // numeraire at time 0 (exactly 1 under SPOT)
