@@ -185,6 +185,7 @@ struct lmm_process {
     double *d_loadings = nullptr, *d_variance = nullptr, *d_dt = nullptr, *d_delta = nullptr, *d_init = nullptr;
     double *d_inv_delta = nullptr, *d_var_half = nullptr;
     float *d_lam32 = nullptr, *d_var32 = nullptr, *d_inv_delta32 = nullptr, *d_dt32 = nullptr, *d_init_log32 = nullptr;
+    float* d_delta_pair = nullptr;
     int *d_first = nullptr, *d_obs_slot = nullptr, *d_tenor_tidx = nullptr;
     uint8_t* d_det = nullptr;
     // results
@@ -486,8 +487,12 @@ int lmm_process_create(const lmm_model_desc* m, lmm_brownian* bm, lmm_process** 
         for (size_t r = 0; r < (size_t)T * N; r++)
             for (int k = 0; k < F; k++) l32[r * FP + k] = (float)m->factor_loadings[r * F + k];
         for (size_t i = 0; i < v32.size(); i++) v32[i] = (float)m->variance[i];
-        std::vector<float> id32(N), dt32(T), y32(N);
+        std::vector<float> id32(N), dt32(T), y32(N), dp32(2 * (size_t)N);
         for (int j = 0; j < N; j++) id32[j] = (float)inv_delta[j];
+        for (int j = 0; j < N; j++) {
+            dp32[2 * j] = (float)delta[j];
+            dp32[2 * j + 1] = (float)(delta[j] - (double)dp32[2 * j]);
+        }
         for (int j = 0; j < N; j++) y32[j] = (float)std::log(std::max(m->initial_forwards[j], 0.0));  // getInitialState
         for (int i = 0; i < T; i++) dt32[i] = (float)dt[i];
         rc = upload(&pr->d_lam32, l32.data(), l32.size(), s);
@@ -495,6 +500,7 @@ int lmm_process_create(const lmm_model_desc* m, lmm_brownian* bm, lmm_process** 
         if (!rc) rc = upload(&pr->d_inv_delta32, id32.data(), id32.size(), s);
         if (!rc) rc = upload(&pr->d_dt32, dt32.data(), dt32.size(), s);
         if (!rc) rc = upload(&pr->d_init_log32, y32.data(), y32.size(), s);
+        if (!rc) rc = upload(&pr->d_delta_pair, dp32.data(), dp32.size(), s);
         if (!rc) rc = cudaStreamSynchronize(s) == cudaSuccess ? 0 : fail(LMM_ERR_CUDA, "stream sync");
     }
     if (!rc) rc = cudaStreamSynchronize(s) == cudaSuccess ? 0 : fail(LMM_ERR_CUDA, "stream sync");
@@ -564,6 +570,7 @@ static int process_ensure(lmm_process* pr)
     a.d_inv_delta32 = pr->d_inv_delta32;
     a.d_dt32 = pr->d_dt32;
     a.d_init_log32 = pr->d_init_log32;
+    a.d_delta_pair = pr->d_delta_pair;
     a.d_init = pr->d_init;
     a.d_obs_slot = pr->d_obs_slot;
     a.d_dw = pr->bm->d_dw;
@@ -666,6 +673,7 @@ int lmm_process_destroy(lmm_process* pr)
     dfree(pr->d_inv_delta32, s);
     dfree(pr->d_dt32, s);
     dfree(pr->d_init_log32, s);
+    dfree(pr->d_delta_pair, s);
     dfree(pr->d_first, s);
     dfree(pr->d_tenor_tidx, s);
     dfree(pr->d_det, s);
@@ -891,8 +899,8 @@ static int bermudan_run(lmm_process* pr, const lmm_bermudan_desc* d, double* val
         if (rc) return rc;
     }
     if (!pr->d_gram) {
-        // Gram partials: at most bermudan_blocks(P) + 64 blocks over all exercise dates
-        if ((rc = dalloc(&pr->d_gram, (size_t)(blocks + 64) * 20 * 2, s))) return rc;
+        // Gram partials: at most bermudan_gram_capacity(P) blocks over all exercise dates
+        if ((rc = dalloc(&pr->d_gram, (size_t)bermudan_gram_capacity(pr->P) * 20 * 2, s))) return rc;
     }
     if (ne > pr->berm_capacity) {
         dfree(pr->d_basis, s);
@@ -1417,7 +1425,7 @@ int lmm_portfolio_create(lmm_process* pr, const lmm_portfolio_desc* desc, lmm_po
         if (!rc) rc = dalloc(&b.under, (size_t)P, s);
         if (!rc) rc = dalloc(&b.ex, (size_t)P, s);
         if (!rc) rc = dalloc(&b.basis, (size_t)std::max(1, pf->max_ne) * 5 * P, s);
-        if (!rc) rc = dalloc(&b.gram, (size_t)(blocks + 64 + (pf->gram_blocks > 0 ? pf->gram_blocks * 64 : 0)) * 40, s);
+        if (!rc) rc = dalloc(&b.gram, (size_t)(bermudan_gram_capacity(P) + (pf->gram_blocks > 0 ? pf->gram_blocks * 64 : 0)) * 40, s);
         if (!rc) rc = dalloc(&b.svd, (size_t)64 * 80, s);
         if (!rc) rc = dalloc(&b.rhs, (size_t)blocks * 12 + 2, s);  // partials, then the completion counter
         if (!rc) rc = cudaMemsetAsync(b.rhs, 0, sizeof(double) * ((size_t)blocks * 12 + 2), s) == cudaSuccess

@@ -1,0 +1,101 @@
+// dfloat.cuh -- FP32 sums and dot products carried in twice the working precision.
+//
+// Ogita, Rump and Oishi, "Accurate sum and dot product", SIAM J. Sci. Comput. 26(6), 2005:
+// Sum2 and Dot2 keep the running FP32 sum p and, in s, the FP32 sum of the exact rounding
+// errors of every addition (Knuth's TwoSum) and every product (TwoProduct by one fused
+// multiply-add).  p + s is as accurate as the sum evaluated in twice the precision and
+// rounded, i.e. about 2^-48 relative per accumulated term instead of FP32's 2^-24.
+// Products that feed an error-free sum use __fmul_rn, which the compiler never contracts
+// into a fused multiply-add (a contraction would break the exactness these steps rely on
+// in translation units built with FMA contraction on).
+//
+// The mixed-precision form uses these where its sums need FP64-class accuracy (the
+// regression's Gram matrix and X^T y, the conditional expectation X beta) but FP64 would
+// cost the GB300's narrow FP64 pipe: a Dot2 term is nine FP32 operations.  The operations
+// below must not be reassociated; nvcc does not reassociate FP32 arithmetic, and the one
+// product that has to be fused is an explicit fmaf.
+#pragma once
+
+namespace lmm {
+
+struct Sum2 {
+    float p;  // running sum
+    float s;  // sum of the rounding errors of p
+};
+
+// x + y = a + b exactly, x = fl(a + b) (TwoSum, no ordering condition on a and b)
+__device__ __forceinline__ void two_sum(float a, float b, float& x, float& y)
+{
+    const float s = a + b;
+    const float z = s - a;
+    y = (a - (s - z)) + (b - z);
+    x = s;
+}
+
+// acc += x
+__device__ __forceinline__ void sum2_add(Sum2& acc, float x)
+{
+    float p, q;
+    two_sum(acc.p, x, p, q);
+    acc.p = p;
+    acc.s += q;
+}
+
+// acc += x * y, the product's rounding error included
+__device__ __forceinline__ void dot2_add(Sum2& acc, float x, float y)
+{
+    const float h = __fmul_rn(x, y);
+    const float r = fmaf(x, y, -h);
+    float p, q;
+    two_sum(acc.p, h, p, q);
+    acc.p = p;
+    acc.s += q + r;
+}
+
+__device__ __forceinline__ double sum2_value(const Sum2& acc) { return (double)acc.p + (double)acc.s; }
+
+// a + b of two partial sums (the error of the leading parts kept exactly)
+__device__ __forceinline__ Sum2 sum2_merge(const Sum2& a, const Sum2& b)
+{
+    float p, q;
+    two_sum(a.p, b.p, p, q);
+    return Sum2{p, (a.s + b.s) + q};
+}
+
+// a double split into two floats with hi + lo = v to about 2^-48 relative
+__device__ __forceinline__ void split_double(double v, float& hi, float& lo)
+{
+    hi = (float)v;
+    lo = (float)(v - (double)hi);
+}
+
+// IEEE 754 binary64 -> binary32, round to nearest even, in integer operations: on this GPU a
+// hardware conversion from FP64 issues to the narrow FP64 pipe.  Results outside the normal
+// float range (zero, subnormal, overflow, infinity, NaN) take the hardware conversion.
+__device__ __forceinline__ float f64_to_f32_int(double x)
+{
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
+    if (e <= 0 || e >= 255) return (float)x;
+    const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);  // the leading 23 fraction bits
+    const unsigned rest = lo & 0x1fffffffu;                   // the 29 bits rounded away
+    unsigned bits = (hi & 0x80000000u) | ((unsigned)e << 23) | m;
+    if (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) bits += 1u;  // a carry moves into the exponent
+    return __uint_as_float(bits);
+}
+
+// binary32 -> binary64 (exact) in integer operations; zero, subnormal, infinity and NaN
+// take the hardware conversion
+__device__ __forceinline__ double f32_to_f64_int(float f)
+{
+    const unsigned b = __float_as_uint(f);
+    const unsigned e = (b >> 23) & 0xffu;
+    if (e == 0u || e == 255u) {
+        if ((b & 0x7fffffffu) == 0u) return __hiloint2double((int)(b & 0x80000000u), 0);
+        return (double)f;
+    }
+    const unsigned hi = (b & 0x80000000u) | ((e - 127u + 1023u) << 20) | ((b & 0x7fffffu) >> 3);
+    return __hiloint2double((int)hi, (int)(b << 29));
+}
+
+}  // namespace lmm

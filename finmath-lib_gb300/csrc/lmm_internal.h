@@ -60,17 +60,21 @@ constexpr int kJumpWindow = kMtDegree + kMtN - 1;  // raw words needed by one ju
 
 // Seeded 624-word array of commons-math3 MersenneTwister(long seed).
 void mt_seeded_state(int64_t seed, uint32_t out[kMtN]);
-// Jump polynomials x^(2^j * stride) mod phi for j = 0..count-1 (cached per stride).
-const std::vector<uint64_t>& mt_jump_polynomials(uint64_t stride_words, int count);
+// Chunk jumps by base-8 digits: polynomial [j * 7 + (d - 1)] = x^(d 8^j stride) mod phi for
+// the digit values d = 1..7 of the digit positions j < ndigits (cached per stride).
+constexpr int kJumpDigitBits = 3;
+constexpr int kJumpBase = 1 << kJumpDigitBits;
+const std::vector<uint64_t>& mt_jump_digit_polynomials(uint64_t stride_words, int ndigits);
 
 // ---------------------------------------------------------------- device launchers
-constexpr int kMaxJumps = 32;
+constexpr int kMaxJumps = 32;  // jump polynomial lists: 7 per base-8 digit, so at most 4 digits
 struct RngPlan {
     int64_t chunks = 0;
     int64_t chunk_values = 0;
-    int njumps = 0;
-    // set-bit positions of the jump polynomials x^(2^j stride) mod phi, as 16-bit indices
-    // packed four to a word; list j starts at index bit_off[j] (a multiple of 8)
+    int ndigits = 0;      // base-8 digits of the largest chunk index
+    // set-bit positions of the jump polynomials x^(d 8^j stride) mod phi, as 16-bit indices
+    // packed four to a word; list j * 7 + d - 1 starts at index bit_off[j * 7 + d - 1] (a
+    // multiple of 8)
     std::vector<uint64_t> polys;
     int bit_off[kMaxJumps] = {};
     int bit_cnt[kMaxJumps] = {};
@@ -113,6 +117,7 @@ struct PathLaunch {
     const float* d_inv_delta32;// [N] 1/delta in FP32 (mixed form)
     const float* d_dt32;       // [T] time steps in FP32 (mixed form)
     const float* d_init_log32; // [N] log of the initial forwards in FP32 (mixed form)
+    const float* d_delta_pair; // [N][2] period lengths as FP32 pairs hi + lo (mixed form)
     const double* d_init;      // [N] initial forwards
     const int* d_obs_slot;     // [T+1] observation slot or -1
     const void* d_dw;          // [T][F][P] fp64 or fp32
@@ -202,7 +207,9 @@ struct BermudanScratch {
 int reduce_mean_var_device(const double* d_values, int P, double* d_scratch, double* d_out2, cudaStream_t s);
 int launch_timestamp(unsigned long long* d_out, cudaStream_t s);
 int bermudan_blocks(int P);
-int bermudan_gram_blocks(int P, int ne);
+int bermudan_gram_blocks(int P, int ne, bool fp32);
+// capacity (in blocks) of the Gram partials buffer for any exercise-date count <= 64
+inline int bermudan_gram_capacity(int P) { return 4 * bermudan_blocks(P) + 64; }
 
 struct AdjointLaunch {
     int T, N, F, P, nper, stride, callable, freeze_adjustment, fp32, T_slot, blocks;

@@ -11,9 +11,12 @@
 //
 // Here: phi is recovered once with Berlekamp-Massey from a 2*19937-bit output
 // sequence (phi is primitive, so the minimal polynomial of any nonzero output bit
-// sequence is phi itself); jump polynomials are computed by square-and-multiply-by-x
-// modulo phi and cached per chunk stride.  The device applies g(A) to a state as an
-// XOR of the windows x[i..i+623] of the raw word sequence for which g_i = 1.
+// sequence is phi itself).  Chunk c starts at word offset c * stride; with the base-8
+// digits d_j of c that is the product of the jumps x^(d_j 8^j stride) mod phi, so a
+// block applies at most one jump per nonzero digit.  Those 7 polynomials per digit are
+// computed by square-and-multiply-by-x, squaring and GF(2) products modulo phi, and
+// cached per chunk stride.  The device applies g(A) to a state as an XOR of the windows
+// x[i..i+623] of the raw word sequence for which g_i = 1.
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -209,29 +212,68 @@ static Poly poly_x_pow(uint64_t e)
     return r;
 }
 
-const std::vector<uint64_t>& mt_jump_polynomials(uint64_t stride_words, int count)
+// a b mod phi over GF(2): the shifted copies of b for the set bits of a, then the
+// reduction of the bits >= 19937 from the top
+static Poly poly_mul_mod(const Poly& a, const Poly& b)
+{
+    const Phi& f = phi();
+    Poly prod(2 * kPolyWords + 2, 0);
+    for (int i = 0; i < kPolyWords; i++) {
+        uint64_t v = a[i];
+        while (v) {
+            const int k = __builtin_ctzll(v);
+            v &= v - 1;
+            xor_shifted(prod, b, kMtDegree, (size_t)i * 64 + (size_t)k);
+        }
+    }
+    for (size_t i = 2 * (size_t)(kMtDegree - 1); i >= (size_t)kMtDegree; i--)
+        if (get_bit(prod, i)) xor_shifted(prod, f.coeff, kMtDegree + 1, i - kMtDegree);
+    prod.resize(kPolyWords);
+    return prod;
+}
+
+const std::vector<uint64_t>& mt_jump_digit_polynomials(uint64_t stride_words, int ndigits)
 {
     static std::mutex mu;
     static std::map<uint64_t, std::vector<uint64_t>> cache;
     std::lock_guard<std::mutex> lock(mu);
+    constexpr int per = kJumpBase - 1;
     std::vector<uint64_t>& v = cache[stride_words];
-    size_t have = v.size() / kPolyWords;
-    if ((int)have >= count) return v;
-    Poly cur;
-    if (have == 0) {
-        cur = poly_x_pow(stride_words);
-        v.insert(v.end(), cur.begin(), cur.end());
-        have = 1;
-    } else {
-        cur.assign(v.end() - kPolyWords, v.end());
-    }
-    while ((int)have < count) {
-        poly_square_mod(cur);  // x^(2^(j+1) L) = (x^(2^j L))^2
-        v.insert(v.end(), cur.begin(), cur.end());
-        have++;
+    if (v.size() >= (size_t)ndigits * per * kPolyWords) return v;
+    v.clear();
+    Poly g1 = poly_x_pow(stride_words);  // x^(8^j stride) for the digit j
+    for (int j = 0; j < ndigits; j++) {
+        Poly g[kJumpBase];
+        g[1] = g1;
+        for (int d = 2; d < kJumpBase; d++) {
+            if (d % 2 == 0) {
+                g[d] = g[d / 2];
+                poly_square_mod(g[d]);  // x^(2e) = (x^e)^2
+            } else {
+                g[d] = poly_mul_mod(g[d - 1], g[1]);
+            }
+        }
+        for (int d = 1; d < kJumpBase; d++) v.insert(v.end(), g[d].begin(), g[d].end());
+        g1 = g[kJumpBase / 2];
+        poly_square_mod(g1);  // x^(8^(j+1) stride)
     }
     return v;
 }
+
+// the raw state after the jump g applied to st (in place)
+static void apply_jump(uint32_t* st, const Poly& g)
+{
+    std::vector<uint32_t> x;
+    mt_raw_sequence(st, (size_t)kJumpWindow, x);
+    for (int w = 0; w < kMtN; w++) {
+        uint32_t acc = 0;
+        for (int i = 0; i < kMtDegree; i++)
+            if (get_bit(g, (size_t)i)) acc ^= x[(size_t)i + w];
+        st[w] = acc;
+    }
+}
+
+static void tempered_words(const uint32_t* st, uint64_t count, uint32_t* out);
 
 // Host restatement of the device jump (used to check the jump polynomials without a GPU):
 // the tempered words [skip, skip+count) of MersenneTwister(seed), reached by one jump.
@@ -239,17 +281,33 @@ void mt_words_after_jump(int64_t seed, uint64_t skip, uint64_t count, uint32_t* 
 {
     uint32_t st[kMtN];
     mt_seeded_state(seed, st);
-    std::vector<uint32_t> x;
-    if (skip > 0) {
-        const Poly g = poly_x_pow(skip);
-        mt_raw_sequence(st, (size_t)kJumpWindow, x);
-        for (int w = 0; w < kMtN; w++) {
-            uint32_t acc = 0;
-            for (int i = 0; i < kMtDegree; i++)
-                if (get_bit(g, (size_t)i)) acc ^= x[(size_t)i + w];
-            st[w] = acc;
+    if (skip > 0) apply_jump(st, poly_x_pow(skip));
+    tempered_words(st, count, out);
+}
+
+// The same for the start of chunk `chunk` of a partition with `stride_words` words per
+// chunk, reached as the device reaches it: one jump per nonzero base-8 digit of the chunk.
+void mt_words_at_chunk(int64_t seed, uint64_t stride_words, uint64_t chunk, uint64_t count, uint32_t* out)
+{
+    uint32_t st[kMtN];
+    mt_seeded_state(seed, st);
+    int ndigits = 0;
+    while (ndigits < 21 && (chunk >> (kJumpDigitBits * ndigits)) != 0) ndigits++;
+    if (ndigits > 0) {
+        const std::vector<uint64_t>& v = mt_jump_digit_polynomials(stride_words, ndigits);
+        for (int j = 0; j < ndigits; j++) {
+            const int d = (int)((chunk >> (kJumpDigitBits * j)) & (kJumpBase - 1));
+            if (!d) continue;
+            const size_t off = ((size_t)j * (kJumpBase - 1) + (size_t)(d - 1)) * kPolyWords;
+            apply_jump(st, Poly(v.begin() + off, v.begin() + off + kPolyWords));
         }
     }
+    tempered_words(st, count, out);
+}
+
+static void tempered_words(const uint32_t* st, uint64_t count, uint32_t* out)
+{
+    std::vector<uint32_t> x;
     mt_raw_sequence(st, (size_t)kMtN + count, x);
     for (uint64_t k = 0; k < count; k++) {
         uint32_t y = x[kMtN + k];
@@ -262,6 +320,19 @@ void mt_words_after_jump(int64_t seed, uint64_t skip, uint64_t count, uint32_t* 
 }
 
 }  // namespace lmm
+
+extern "C" int lmm_mt19937_chunk_words_host(int64_t seed, uint64_t stride_words, uint64_t chunk, uint64_t count,
+                                            uint32_t* out)
+{
+    if (!out) return lmm::fail(LMM_ERR_INVALID, "null argument");
+    if (stride_words == 0 && chunk > 0) return lmm::fail(LMM_ERR_INVALID, "a chunk stride of zero words");
+    try {
+        lmm::mt_words_at_chunk(seed, stride_words, chunk, count, out);
+    } catch (const std::exception& e) {
+        return lmm::fail(LMM_ERR_INVALID, e.what());
+    }
+    return LMM_OK;
+}
 
 extern "C" int lmm_mt19937_words_host(int64_t seed, uint64_t skip, uint64_t count, uint32_t* out)
 {

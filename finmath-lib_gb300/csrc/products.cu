@@ -169,35 +169,9 @@ struct SwapRows32 {
 };
 
 template <typename TS>
-__device__ void bermudan_basis(const BermShared& a, const BermudanPeriod& c, int p, double B[5], const SwapRows32* rows)
+__device__ __forceinline__ void bermudan_basis(const BermShared& a, const BermudanPeriod& c, int p, double B[5])
 {
-    if (a.basis == 1 && sizeof(TS) == 4) {
-        // mixed form: the same par-rate recursion in FP32 (the state's precision) over the
-        // staged FP32 period table; the basis values are widened to FP64 for the Gram
-        // accumulation and the solve
-        float H = 0.0f, prod = 1.0f;
-        const float* st = static_cast<const float*>(a.states) + (size_t)c.ex_slot * a.N * a.P + p;
-        const int nq = c.swap_last - c.swap_first;
-        for (int q = 0; q < nq; q++) {
-            const float Lq = st[(size_t)rows->idx[q] * a.P];
-            const float dq = rows->len[q];
-            const float g = fmaf(Lq, dq, 1.0f);
-            if (q == 0) {
-                prod = g;
-                H = dq;
-            } else {
-                prod = prod * g;
-                H = fmaf(H, g, dq);
-            }
-        }
-        const double S = (double)((prod - 1.0f) / H);
-        const double Nn = numeraire_adj_mixed(a.num, c.ex_num_index, p);
-        B[0] = S;
-        B[1] = S * S;
-        B[2] = Nn;
-        B[3] = Nn * Nn;
-        B[4] = S * Nn;
-    } else if (a.basis == 1) {
+    if (a.basis == 1) {
         // {S, S^2, N, N^2, S*N}: S = par rate of the remaining periods from L_j(T_ex),
         // S = (prod g_q - 1) / sum_s d_s prod_{r>s} g_r with g_q = 1 + L_q d_q, both by a
         // forward recursion (one division per path instead of one per period)
@@ -246,27 +220,102 @@ __device__ void bermudan_basis(const BermShared& a, const BermudanPeriod& c, int
     }
 }
 
+// Mixed form: the basis in FP32.  The {S, S^2, N, N^2, S*N} basis runs the same par-rate
+// recursion in FP32 (the state's precision) over the staged FP32 period table, with the
+// adjusted numeraire rounded to FP32 (nfac = adjustment / P^d of the date); the reference
+// basis is evaluated in FP64 and rounded.  The Gram matrix and X^T y are accumulated from
+// these same rounded values, so the regression is the exact least-squares fit of them.
+__device__ __forceinline__ void bermudan_basis32(const BermShared& a, const BermudanPeriod& c, int p, float B[5],
+                                 const SwapRows32* rows, float nfac)
+{
+    if (a.basis == 1) {
+        float H = 0.0f, prod = 1.0f;
+        const float* st = static_cast<const float*>(a.states) + (size_t)c.ex_slot * a.N * a.P + p;
+        const int nq = c.swap_last - c.swap_first;
+        for (int q0 = 0; q0 < nq; q0 += 8) {
+            float Lb[8];  // eight independent loads in flight per thread
+#pragma unroll
+            for (int k = 0; k < 8; k++) Lb[k] = q0 + k < nq ? st[(size_t)rows->idx[q0 + k] * a.P] : 0.0f;
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                const int q = q0 + k;
+                if (q < nq) {
+                    const float dq = rows->len[q];
+                    const float g = fmaf(Lb[k], dq, 1.0f);
+                    if (q == 0) {
+                        prod = g;
+                        H = dq;
+                    } else {
+                        prod = prod * g;
+                        H = fmaf(H, g, dq);
+                    }
+                }
+            }
+        }
+        const float S = (prod - 1.0f) / H;
+        const float Nn = f64_to_f32_int(a.num.numeraire[(size_t)c.ex_num_index * a.P + p]) * nfac;
+        B[0] = S;
+        B[1] = S * S;
+        B[2] = Nn;
+        B[3] = Nn * Nn;
+        B[4] = S * Nn;
+    } else {
+        double Bd[5];
+        bermudan_basis<float>(a, c, p, Bd);
+#pragma unroll
+        for (int i = 0; i < 5; i++) B[i] = (float)Bd[i];
+    }
+}
+
 // grid (bx, ne): basis functions of exercise date blockIdx.y and their Gram partial sums
 template <typename TS>
-__global__ void __launch_bounds__(kProdThreads) bermudan_gram_kernel(const BermShared a, double* partials)
+__global__ void __launch_bounds__(kProdThreads, sizeof(TS) == 4 ? 3 : 1) bermudan_gram_kernel(const BermShared a, double* partials)
 {
     const int e = blockIdx.y;
     const BermudanPeriod c = a.per[a.ex_period[e]];
-    __shared__ SwapRows32 rows;
+    double acc[kGram];
     if (sizeof(TS) == 4) {
+        // mixed form: FP32 basis (stored as FP32), Gram sums in twice FP32 precision
+        // (Sum2 / Dot2 per thread), FP64 across threads
+        __shared__ SwapRows32 rows;
         for (int q = threadIdx.x; q < c.swap_last - c.swap_first; q += blockDim.x) {
             rows.idx[q] = a.period_index[c.swap_first + q];
             rows.len[q] = (float)a.period_length[c.swap_first + q];
         }
         __syncthreads();
+        __shared__ float nfac_s;  // adjustment / P^d of the date, once per block (no FP64 per thread)
+        if (threadIdx.x == 0) {
+            const int l = c.ex_num_index;
+            nfac_s = a.num.has_discount ? (float)(a.num.adj[l] * a.num.inv_pd[l]) : 1.0f;
+        }
+        __syncthreads();
+        const float nfac = nfac_s;
+        Sum2 g[kGram];
+#pragma unroll
+        for (int k = 0; k < kGram; k++) g[k] = Sum2{0.0f, 0.0f};
+        float* bb = reinterpret_cast<float*>(a.basis_buf) + (size_t)e * 5 * a.P;
+        for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.P; p += gridDim.x * blockDim.x) {
+            float B[5];
+            bermudan_basis32(a, c, p, B, &rows, nfac);
+#pragma unroll
+            for (int i = 0; i < 5; i++) bb[(size_t)i * a.P + p] = B[i];
+#pragma unroll
+            for (int i = 0; i < 5; i++) sum2_add(g[i], B[i]);
+            int k = 5;
+#pragma unroll
+            for (int i = 0; i < 5; i++)
+#pragma unroll
+                for (int j = i; j < 5; j++) dot2_add(g[k++], B[i], B[j]);
+        }
+        block_sums_sum2<kGram>(g, partials + ((size_t)e * gridDim.x + blockIdx.x) * kGram * 2, 1);
+        return;
     }
-    double acc[kGram];
 #pragma unroll
     for (int k = 0; k < kGram; k++) acc[k] = 0.0;
     double* bb = a.basis_buf + (size_t)e * 5 * a.P;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.P; p += gridDim.x * blockDim.x) {
         double B[5];
-        bermudan_basis<TS>(a, c, p, B, &rows);
+        bermudan_basis<TS>(a, c, p, B);
 #pragma unroll
         for (int i = 0; i < 5; i++) bb[(size_t)i * a.P + p] = B[i];
         int k = 0;
@@ -277,28 +326,21 @@ __global__ void __launch_bounds__(kProdThreads) bermudan_gram_kernel(const BermS
         for (int i = 0; i < 5; i++)
 #pragma unroll
             for (int j = i; j < 5; j++) {
-                // the mixed form fuses (no parity constraint); the FP64 form rounds the product first
-                acc[k] = sizeof(TS) == 4 ? fma(B[i], B[j], acc[k]) : acc[k] + B[i] * B[j];
+                acc[k] = acc[k] + B[i] * B[j];  // the product rounds first, as the reference's
                 k++;
             }
     }
-    if (sizeof(TS) == 4) {
-        // mixed form: FP64 sums, compensated across warps only
-        block_sums_warp_plain<kGram>(acc, partials + ((size_t)e * gridDim.x + blockIdx.x) * kGram * 2, 1);
-    } else {
 #pragma unroll
-        for (int k = 0; k < kGram; k++) {
-            const dd s = block_dd_sum(dd{acc[k], 0.0});
-            if (threadIdx.x == 0) {
-                double* q = partials + (((size_t)e * gridDim.x + blockIdx.x) * kGram + k) * 2;
-                q[0] = s.hi;
-                q[1] = s.lo;
-            }
+    for (int k = 0; k < kGram; k++) {
+        const dd s = block_dd_sum(dd{acc[k], 0.0});
+        if (threadIdx.x == 0) {
+            double* q = partials + (((size_t)e * gridDim.x + blockIdx.x) * kGram + k) * 2;
+            q[0] = s.hi;
+            q[1] = s.lo;
         }
     }
 }
 
-// One-sided Jacobi SVD G V = U diag(s) of the 6x6 Gram matrix (the oracle's algorithm).
 __device__ void svd6(const double G[36], double U[36], double s[6], double V[36])
 {
     for (int i = 0; i < 36; i++) U[i] = G[i];
@@ -381,7 +423,10 @@ __global__ void __launch_bounds__(32) bermudan_svd_kernel(const double* partials
 // X^T y sums of one date and beta = V diag(1/s) U^T (X^T y) with the SVD's cutoff,
 // in the oracle's order (MonteCarloConditionalExpectationRegression.java:141-147).  Run by
 // one block of at least 6 warps (all its threads call it).
-__device__ void regression_solve(const double* partials, int blocks, int P, const double* svd, double* beta_out)
+// With pairs set (mixed form) the coefficients are stored as FP32 pairs hi, lo (beta_out
+// then holds 12 floats) for the FP32 conditional expectation of the next step.
+__device__ void regression_solve(const double* partials, int blocks, int P, const double* svd, double* beta_out,
+                                 bool pairs = false)
 {
     __shared__ double b[kRhs];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -408,7 +453,14 @@ __device__ void regression_solve(const double* partials, int blocks, int P, cons
             for (int r = 0; r < 6; r++) utb += U[r * 6 + j] * b[r];
             acc += V[i * 6 + j] * (utb / s[j]);
         }
-        beta_out[i] = acc;
+        if (pairs) {
+            float hi, lo;
+            split_double(acc, hi, lo);
+            reinterpret_cast<float*>(beta_out)[2 * i] = hi;
+            reinterpret_cast<float*>(beta_out)[2 * i + 1] = lo;
+        } else {
+            beta_out[i] = acc;
+        }
     }
 }
 
@@ -428,7 +480,25 @@ struct BermStepParams {
     int init;
 };
 
-template <typename TS>
+// The last block of a step launch to finish reduces every block's X^T y partials (in block
+// order) and solves for the date's coefficients; nothing waits on another block.  All
+// threads of every block call it after writing their block's partials.
+__device__ void finish_date_last_block(const BermStepParams& a, bool pairs)
+{
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    unsigned int* done = reinterpret_cast<unsigned int*>(a.partials + (size_t)gridDim.x * kRhs * 2);
+    if (threadIdx.x == 0) last = atomicAdd(done, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (last) {
+        __threadfence();
+        regression_solve(a.partials, gridDim.x, a.sh.P, a.svd_cur, a.beta_cur, pairs);
+        if (threadIdx.x == 0) *done = 0u;  // ready for the next date
+    }
+}
+
+// FP64 form: the reference's arithmetic and order (BermudanSwaption.java:91-157).
 __global__ void __launch_bounds__(kProdThreads) bermudan_step_kernel(const BermStepParams a)
 {
     const BermShared& sh = a.sh;
@@ -460,19 +530,15 @@ __global__ void __launch_bounds__(kProdThreads) bermudan_step_kernel(const BermS
             // conditional expectation X beta (:104-107), then choose (:139, :141)
             double ce = 1.0 * beta[0];
 #pragma unroll
-            for (int i = 1; i < 6; i++) {
-                const double bi = bprev[(size_t)(i - 1) * sh.P + p];
-                ce = sizeof(TS) == 4 ? fma(bi, beta[i], ce) : ce + bi * beta[i];
-            }
+            for (int i = 1; i < 6; i++) ce = ce + bprev[(size_t)(i - 1) * sh.P + p] * beta[i];
             const bool cont = ce >= 0.0;
             v = cont ? v : u;
             if (!cont) a.ex[p] = a.pending_fixing;
         }
         if (a.cur >= 0) {
-            const double L = state_at<TS>(sh.states, c.libor_slot, sh.N, sh.P, c.libor_index, p);
+            const double L = state_at<double>(sh.states, c.libor_slot, sh.N, sh.P, c.libor_index, p);
             double payoff = ((L - c.strike) * c.period_length) * c.notional;
-            if (sizeof(TS) == 4) payoff = payoff * inv_numeraire_adj_mixed(sh.num, c.pay_num_index, p);
-            else payoff = payoff / numeraire_adj(sh.num, c.pay_num_index, p);
+            payoff = payoff / numeraire_adj(sh.num, c.pay_num_index, p);
             payoff = payoff * w;
             if (sh.callable) u = u + payoff;
             else v = v + payoff;
@@ -480,10 +546,7 @@ __global__ void __launch_bounds__(kProdThreads) bermudan_step_kernel(const BermS
                 const double y = v - u;
                 acc[0] = acc[0] + y * 1.0;
 #pragma unroll
-                for (int i = 0; i < 5; i++) {
-                    const double bi = bcur[(size_t)i * sh.P + p];
-                    acc[1 + i] = sizeof(TS) == 4 ? fma(y, bi, acc[1 + i]) : acc[1 + i] + y * bi;
-                }
+                for (int i = 0; i < 5; i++) acc[1 + i] = acc[1 + i] + y * bcur[(size_t)i * sh.P + p];
             }
         } else {
             v = (v * numeraire_adj(sh.num, 0, 0)) / w;  // numeraire at time 0 (exactly 1 under SPOT)
@@ -492,32 +555,121 @@ __global__ void __launch_bounds__(kProdThreads) bermudan_step_kernel(const BermS
         a.under[p] = u;
     }
     if (bcur) {
-        if (sizeof(TS) == 4) {
-            // mixed form: FP64 sums, compensated across warps only
-            block_sums_warp_plain<kRhs>(acc, a.partials + (size_t)blockIdx.x * kRhs * 2, 1);
-        } else {
 #pragma unroll
-            for (int i = 0; i < kRhs; i++) {
-                const dd s = block_dd_sum(dd{acc[i], 0.0});
-                if (threadIdx.x == 0) {
-                    a.partials[((size_t)blockIdx.x * kRhs + i) * 2] = s.hi;
-                    a.partials[((size_t)blockIdx.x * kRhs + i) * 2 + 1] = s.lo;
-                }
+        for (int i = 0; i < kRhs; i++) {
+            const dd s = block_dd_sum(dd{acc[i], 0.0});
+            if (threadIdx.x == 0) {
+                a.partials[((size_t)blockIdx.x * kRhs + i) * 2] = s.hi;
+                a.partials[((size_t)blockIdx.x * kRhs + i) * 2 + 1] = s.lo;
             }
         }
-        // the last block to finish reduces every block's partials (in block order) and solves
-        // for this date's coefficients; nothing waits on another block
-        __shared__ bool last;
-        __threadfence();
-        __syncthreads();
-        unsigned int* done = reinterpret_cast<unsigned int*>(a.partials + (size_t)gridDim.x * kRhs * 2);
-        if (threadIdx.x == 0) last = atomicAdd(done, 1u) == gridDim.x - 1;
-        __syncthreads();
-        if (last) {
-            __threadfence();
-            regression_solve(a.partials, gridDim.x, sh.P, a.svd_cur, a.beta_cur);
-            if (threadIdx.x == 0) *done = 0u;  // ready for the next date
+        finish_date_last_block(a, false);
+    }
+}
+
+// Mixed form: the same backward induction with FP32 path values (continuation v and
+// underlying u, kept as two FP32 arrays in the under buffer), FP32 payoffs, the FP32
+// basis, and the conditional expectation and X^T y sums in twice FP32 precision
+// (Dot2).  Payoffs are not scaled by 1/P (the reference's weight, which cancels in the
+// final value and scales X^T y and beta alike, leaving the exercise decisions unchanged).
+// Only the final values are written in FP64.
+__global__ void __launch_bounds__(kProdThreads) bermudan_step_mixed_kernel(const BermStepParams a)
+{
+    const BermShared& sh = a.sh;
+    const int P = sh.P;
+    float* v32 = reinterpret_cast<float*>(a.under);
+    float* u32 = v32 + P;
+    Sum2 acc[kRhs];
+#pragma unroll
+    for (int i = 0; i < kRhs; i++) acc[i] = Sum2{0.0f, 0.0f};
+    float bh[6], bl[6];
+    const float* bprev = nullptr;
+    if (a.pending_ex >= 0) {
+        const float* b32 = reinterpret_cast<const float*>(a.beta + a.pending_ex * 6);  // (hi, lo) pairs
+#pragma unroll
+        for (int i = 0; i < 6; i++) {
+            bh[i] = b32[2 * i];
+            bl[i] = b32[2 * i + 1];
         }
+        bprev = reinterpret_cast<const float*>(sh.basis_buf) + (size_t)a.pending_ex * 5 * P;
+    }
+    const float* bcur = a.cur_ex >= 0 ? reinterpret_cast<const float*>(sh.basis_buf) + (size_t)a.cur_ex * 5 * P : nullptr;
+    const float* Lrow = nullptr;
+    const double* inv_num = nullptr;
+    const double* num = nullptr;
+    // per-date constants, evaluated once per block: FP64 work per thread would load the
+    // narrow FP64 pipe more than the paths themselves do
+    __shared__ float consts_s[2];
+    __shared__ double num0_s;
+    if (threadIdx.x == 0) {
+        if (a.cur >= 0) {
+            const BermudanPeriod c = sh.per[a.cur];
+            const int l = c.pay_num_index;
+            double f = c.period_length * c.notional;
+            if (sh.num.has_discount) f = f * (sh.num.pd[l] / sh.num.adj[l]);  // 1/N_adj = (1/N) P^d / adjustment
+            consts_s[0] = (float)c.strike;
+            consts_s[1] = (float)f;
+        } else {
+            num0_s = numeraire_adj(sh.num, 0, 0);  // numeraire at time 0 (exactly 1 under SPOT)
+        }
+    }
+    __syncthreads();
+    float strike = 0.0f, fac = 0.0f;
+    double num0 = 0.0;
+    if (a.cur >= 0) {
+        const BermudanPeriod& c = sh.per[a.cur];
+        const int l = c.pay_num_index;
+        Lrow = static_cast<const float*>(sh.states) + ((size_t)c.libor_slot * sh.N + c.libor_index) * P;
+        strike = consts_s[0];
+        fac = consts_s[1];
+        if (sh.num.inv_numeraire) inv_num = sh.num.inv_numeraire + (size_t)l * P;
+        else num = sh.num.numeraire + (size_t)l * P;
+    } else {
+        num0 = num0_s;
+    }
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x) {
+        float v, u;
+        if (a.init) {
+            v = 0.0f;
+            u = 0.0f;
+            a.ex[p] = CUDART_INF;
+        } else {
+            v = v32[p];
+            u = u32[p];
+        }
+        if (bprev) {
+            Sum2 ce{bh[0], bl[0]};
+#pragma unroll
+            for (int i = 1; i < 6; i++) {
+                const float x = bprev[(size_t)(i - 1) * P + p];
+                dot2_add(ce, bh[i], x);
+                ce.s = fmaf(bl[i], x, ce.s);
+            }
+            if (!(ce.p + ce.s >= 0.0f)) {
+                v = u;
+                a.ex[p] = a.pending_fixing;
+            }
+        }
+        if (a.cur >= 0) {
+            const float iN = inv_num ? f64_to_f32_int(inv_num[p]) : (float)(1.0 / num[p]);
+            const float payoff = ((Lrow[p] - strike) * fac) * iN;
+            if (sh.callable) u = u + payoff;
+            else v = v + payoff;
+            if (bcur) {
+                const float y = v - u;
+                sum2_add(acc[0], y);
+#pragma unroll
+                for (int i = 0; i < 5; i++) dot2_add(acc[1 + i], y, bcur[(size_t)i * P + p]);
+            }
+            v32[p] = v;
+            u32[p] = u;
+        } else {
+            a.values[p] = (double)v * num0;
+        }
+    }
+    if (bcur) {
+        block_sums_sum2<kRhs>(acc, a.partials + (size_t)blockIdx.x * kRhs * 2, 1);
+        finish_date_last_block(a, true);
     }
 }
 
@@ -607,9 +759,11 @@ int bermudan_blocks(int P)
     return grid_for(P, kProdThreads, cap);
 }
 
-int bermudan_gram_blocks(int P, int ne)
+// Gram blocks per exercise date.  The mixed form spreads its (latency-bound, unevenly
+// sized: early dates have long swaps) dates over four times as many blocks.
+int bermudan_gram_blocks(int P, int ne, bool fp32)
 {
-    const int total = bermudan_blocks(P);
+    const int total = bermudan_blocks(P) * (fp32 ? 4 : 1);
     int bx = (total + ne - 1) / (ne > 0 ? ne : 1);
     const int need = (P + kProdThreads - 1) / kProdThreads;
     if (bx > need) bx = need;
@@ -675,7 +829,7 @@ int launch_bermudan(const ProductView& v, const BermudanLaunch& a, const Bermuda
     sh.period_length = sc.d_period_length;
     sh.basis_buf = sc.d_basis;
     if (ne > 0) {
-        const int bx = sc.gram_blocks > 0 ? sc.gram_blocks : bermudan_gram_blocks(v.P, ne);
+        const int bx = sc.gram_blocks > 0 ? sc.gram_blocks : bermudan_gram_blocks(v.P, ne, v.state_fp32 != 0);
         {
             KernelTimer kt(K_BERMUDAN_STEP, s);
             const dim3 grid(bx, ne);
@@ -709,8 +863,8 @@ int launch_bermudan(const ProductView& v, const BermudanLaunch& a, const Bermuda
         prm.init = per == a.nper - 1;
         {
             KernelTimer kt(K_BERMUDAN_STEP, s);
-            if (v.state_fp32) bermudan_step_kernel<float><<<blocks, kProdThreads, 0, s>>>(prm);
-            else bermudan_step_kernel<double><<<blocks, kProdThreads, 0, s>>>(prm);
+            if (v.state_fp32) bermudan_step_mixed_kernel<<<blocks, kProdThreads, 0, s>>>(prm);
+            else bermudan_step_kernel<<<blocks, kProdThreads, 0, s>>>(prm);
             LMM_CUDA(cudaGetLastError());
         }
         if (launches) (*launches)++;

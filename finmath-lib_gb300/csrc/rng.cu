@@ -7,8 +7,9 @@
 //
 // GB300 design: the stream of V values (2 words each) is cut into one contiguous chunk
 // per CTA.  A CTA first moves the seeded state to its chunk start with GF(2) jump
-// polynomials (one per set bit of its chunk index; each jump is an XOR of windows of
-// the raw word sequence held in shared memory), then regenerates 624 words at a time
+// polynomials (one per nonzero base-8 digit of its chunk index, at most three for 512
+// chunks; each jump is an XOR of windows of the raw word sequence held in shared
+// memory), then regenerates 624 words at a time
 // in three dependency phases (227/227/170 words) over a double-buffered state, and
 // converts word pairs to values.  Uniforms are bit-identical to the single stream.  The
 // increments leave through a shared-memory tile (increments_loop) so that each [t][f] row
@@ -32,8 +33,8 @@ struct RngParams {
     uint32_t magic_f;         // floor((2^32-1)/F)
     const uint32_t* seeded;   // [624]
     const uint16_t* jump_bits;  // set-bit positions of the jump polynomials (see RngPlan)
-    int bit_off[kMaxJumps], bit_cnt[kMaxJumps];
-    int njumps;
+    int bit_off[kMaxJumps], bit_cnt[kMaxJumps];  // list j * 7 + d - 1: digit j has the value d
+    int ndigits;
     int64_t num_values;
     int64_t chunk_values;
     int values_per_path;
@@ -409,17 +410,20 @@ __global__ void __launch_bounds__(kRngThreads, 2) mt_generate_kernel(const RngPa
     for (int i = tid; i < kMtN; i += kRngThreads) x[i] = prm.seeded[i];
     __syncthreads();
 
-    // ---- jump to word offset 2*v0 = c * stride: apply x^(2^j stride) for every set bit j of c
-    for (int j = 0; j < prm.njumps; j++) {
-        if (!((c >> j) & 1)) continue;
+    // ---- jump to word offset 2*v0 = c * stride: apply x^(d 8^j stride) for every nonzero
+    // base-8 digit d of c (position j)
+    for (int j = 0; j < prm.ndigits; j++) {
+        const int d = (int)((c >> (kJumpDigitBits * j)) & (kJumpBase - 1));
+        if (d == 0) continue;
+        const int list = j * (kJumpBase - 1) + d - 1;
         for (int base = kMtN; base < kJumpWindow; base += 227) {
             const int n = base + tid;
             if (tid < 227 && n < kJumpWindow) x[n] = mt_next(x[n - 227], x[n - kMtN], x[n - kMtN + 1]);
             __syncthreads();
         }
         // the new state word n is the XOR over the set bits i of the polynomial of x[i + n]
-        const uint16_t* bits = prm.jump_bits + prm.bit_off[j];
-        const int cnt = prm.bit_cnt[j];
+        const uint16_t* bits = prm.jump_bits + prm.bit_off[list];
+        const int cnt = prm.bit_cnt[list];
         const bool two = tid + kRngThreads < kMtN;
         const uint32_t* x0 = x + tid;
         const uint32_t* x1 = x + (two ? tid + kRngThreads : tid);
@@ -495,17 +499,18 @@ int plan_mt_generate(int64_t num_values, int values_per_path, int elem_bytes, Rn
     int64_t chunk_values = (num_values + chunks - 1) / chunks;
     if (chunk_values < 4096) chunk_values = 4096;
     chunks = (num_values + chunk_values - 1) / chunk_values;
-    int njumps = 0;
-    while (((int64_t)1 << njumps) < chunks) njumps++;
+    int ndigits = 0;
+    while (ndigits < 21 && ((int64_t)1 << (kJumpDigitBits * ndigits)) < chunks) ndigits++;
     plan->chunks = chunks;
     plan->chunk_values = chunk_values;
-    plan->njumps = njumps;
+    plan->ndigits = ndigits;
     plan->polys.clear();
-    if (njumps > kMaxJumps) return fail(LMM_ERR_INVALID, "too many generator chunks");
-    if (njumps > 0) {
-        const std::vector<uint64_t>& v = mt_jump_polynomials(2ull * (uint64_t)chunk_values, njumps);
+    const int nlists = ndigits * (kJumpBase - 1);
+    if (nlists > kMaxJumps) return fail(LMM_ERR_INVALID, "too many generator chunks");
+    if (ndigits > 0) {
+        const std::vector<uint64_t>& v = mt_jump_digit_polynomials(2ull * (uint64_t)chunk_values, ndigits);
         std::vector<uint16_t> list;
-        for (int j = 0; j < njumps; j++) {
+        for (int j = 0; j < nlists; j++) {
             while (list.size() % 8) list.push_back(0);  // each list starts 16-byte aligned
             plan->bit_off[j] = (int)list.size();
             for (int q = 0; q < kPolyWords; q++)
@@ -526,9 +531,10 @@ int launch_mt_generate(const RngLaunch& a, cudaStream_t s, int* num_launches)
     RngParams prm;
     prm.seeded = a.d_seeded;
     prm.jump_bits = reinterpret_cast<const uint16_t*>(a.d_jumps);
-    prm.njumps = a.plan->njumps;
-    if (prm.njumps > kMaxJumps) return fail(LMM_ERR_INVALID, "too many generator chunks");
-    for (int j = 0; j < prm.njumps; j++) {
+    prm.ndigits = a.plan->ndigits;
+    if (prm.ndigits * (kJumpBase - 1) > kMaxJumps || ((int64_t)1 << (kJumpDigitBits * prm.ndigits)) < a.plan->chunks)
+        return fail(LMM_ERR_INVALID, "generator plan does not cover its chunks");
+    for (int j = 0; j < prm.ndigits * (kJumpBase - 1); j++) {
         prm.bit_off[j] = a.plan->bit_off[j];
         prm.bit_cnt[j] = a.plan->bit_cnt[j];
     }

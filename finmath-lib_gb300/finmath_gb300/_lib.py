@@ -81,6 +81,8 @@ SIGNATURES = {
     "lmm_mt19937_uniforms": (ctypes.c_int, [ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, _D]),
     "lmm_mt19937_words_host": (ctypes.c_int, [ctypes.c_int64, ctypes.c_uint64, ctypes.c_uint64,
                                               ctypes.POINTER(ctypes.c_uint32)]),
+    "lmm_mt19937_chunk_words_host": (ctypes.c_int, [ctypes.c_int64, ctypes.c_uint64, ctypes.c_uint64,
+                                                    ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint32)]),
     "lmm_process_create": (ctypes.c_int, [ctypes.POINTER(LmmModelDesc), _VP, ctypes.POINTER(_VP)]),
     "lmm_process_set_observed_times": (ctypes.c_int, [_VP, _U8]),
     "lmm_process_simulate": (ctypes.c_int, [_VP]),

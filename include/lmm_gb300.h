@@ -133,6 +133,13 @@ int lmm_mt19937_uniforms(int64_t seed, int64_t offset, int64_t count, double* ou
  * polynomials that needs no GPU; not a production path. */
 int lmm_mt19937_words_host(int64_t seed, uint64_t skip, uint64_t count, uint32_t* out);
 
+/* Tempered words [chunk * stride_words, + count) of the same stream, reached on the host the
+ * way a generator block reaches its chunk: one GF(2) jump x^(d 8^j stride) per nonzero
+ * base-8 digit d (position j) of the chunk index.  A check of the chunk jump polynomials
+ * that needs no GPU; not a production path. */
+int lmm_mt19937_chunk_words_host(int64_t seed, uint64_t stride_words, uint64_t chunk, uint64_t count,
+                                 uint32_t* out);
+
 /* ---------------------------------------------------------------- LMM process */
 typedef struct {
     int num_steps;                  /* T: simulation time steps */

@@ -80,6 +80,17 @@ def test_mt19937_jump_polynomials_host(seed, skip):
     assert np.array_equal(out, po.mt_words(seed, 40, skip=skip))
 
 
+@pytest.mark.parametrize("chunk", [0, 1, 7, 8, 9, 63, 64, 303, 511, 512, 777])
+def test_mt19937_chunk_jumps_host(chunk):
+    # the generator's chunk starts, reached by one jump per nonzero base-8 digit of the chunk
+    seed, stride = 3141, 2 * 27_594
+    out = np.empty(24, dtype=np.uint32)
+    rc = F.load().lmm_mt19937_chunk_words_host(seed, stride, chunk, 24,
+                                               out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)))
+    assert rc == 0
+    assert np.array_equal(out, po.mt_words(seed, 24, skip=chunk * stride))
+
+
 def test_invalid_arguments_are_rejected_with_messages():
     lib = F.load()
     out = np.empty(4)
