@@ -117,7 +117,7 @@ struct RevParams {
     double cap;
     const int* first;     // [T]
     const double* init;   // [N]
-    const double* seeds;  // [N][P]  d value / d L_m(T_m), already divided by P
+    const void* seeds;    // [N][P] (type R) d value / d L_m(T_m), already divided by P
     const void* states;   // [slots][N][P] forward rates L (type R)
     void* ybar;           // [N][P] (type R): adjoint of log L carried between sweeps
     double* vega_partials;   // [warps][T][N]
@@ -256,7 +256,7 @@ __global__ void __launch_bounds__(TH, rev_min_blocks<R, TH>()) reverse_kernel(co
                 R yb = R(0);
                 if (j < NE && active) {
                     const R L = Ls[(size_t)j * a.P + p];
-                    if (!(a.capped && L >= cap)) yb = (R)a.seeds[(size_t)j * a.P + p] * L;
+                    if (!(a.capped && L >= cap)) yb = static_cast<const R*>(a.seeds)[(size_t)j * a.P + p] * L;
                 }
                 Ybar[j] = yb;
             }
@@ -361,15 +361,16 @@ __global__ void __launch_bounds__(TH, rev_min_blocks<R, TH>()) reverse_kernel(co
             for (int j = 0; j < NMAX; j++)
                 if (j < NE && active) yb[(size_t)j * a.P + p] = Ybar[j];
         } else {
-            // deltas: Y_0 = log(L_0(0)) -> d value / d L_0 = Ybar / L_0
+            // deltas: Y_0 = log(L_0(0)) -> d value / d L_0 = Ybar / L_0, the uniform division
+            // applied to the warp's sum (one division per component and warp, not per path)
 #pragma unroll
             for (int j = 0; j < NMAX; j++)
-                if (j < NE) red[j * RS + lane] = active ? (R)((double)Ybar[j] / a.init[j]) : R(0);
+                if (j < NE) red[j * RS + lane] = active ? Ybar[j] : R(0);
             __syncwarp();
 #pragma unroll
             for (int h = 0; h < (NMAX + 31) / 32; h++) {
                 const int r = lane + 32 * h;
-                if (r < NE) atomicAdd(a.delta_partials + gw * N + r, row_sum<R>(red, r));
+                if (r < NE) atomicAdd(a.delta_partials + gw * N + r, row_sum<R>(red, r) / a.init[r]);
             }
             __syncwarp();
         }
@@ -560,6 +561,122 @@ __global__ void __launch_bounds__(kSeedThreads) seed_kernel(const SeedParams a)
         double* sd = a.seeds + (size_t)(l - 1) * P + p;
         *sd = (*sd + t * Nprev * a.delta[l - 1]) * invP;
         un = t * (1.0 + Lf * a.delta[l - 1]);
+    }
+}
+
+// Mixed form: the same two passes in FP32 (seeds and numeraire adjoints kept as FP32
+// arrays, which the FP32 reverse sweep reads), with the per-date cash-flow sums and the
+// value as Sum2 pairs (twice FP32 precision) and every per-date constant converted once per
+// block: on this GPU an FP64 instruction per path would cost more than the pass itself.
+// Exercise times are compared as the bit patterns of non-negative doubles (the IEEE order).
+struct SeedSmem32 {
+    float r_adj[65];    // P^d_l / a_l
+    float adj_pd[65];   // a_l / P^d_l
+    float abar[65];     // pass 2
+    float delta[64];
+    float strike[64], lennot[64];
+    long long fixbits[64];
+    int libor_slot[64], libor_index[64], pay[64];
+};
+
+__global__ void __launch_bounds__(kSeedThreads) seed_mixed_kernel(const SeedParams a)
+{
+    __shared__ SeedSmem32 c;
+    __shared__ Sum2 wsum[kSeedThreads / 32][66];  // per warp: cash-flow sums by date, then the value
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int p = blockIdx.x * kSeedThreads + tid;
+    const bool active = p < a.P;
+    const int N = a.N, P = a.P;
+    float* seeds = static_cast<float*>(static_cast<void*>(a.seeds));
+    float* nb = static_cast<float*>(static_cast<void*>(a.nb));
+    for (int l = tid; l <= N; l += kSeedThreads) {
+        const double ap = a.has_discount ? a.adj[l] * a.inv_pd[l] : 1.0;
+        c.r_adj[l] = (float)(1.0 / ap);
+        c.adj_pd[l] = (float)ap;
+        if (a.pass == 2) c.abar[l] = (float)a.abar[l];
+        if (l < N) c.delta[l] = (float)a.delta[l];
+        for (int w = 0; w < kSeedThreads / 32; w++) wsum[w][l] = Sum2{0.0f, 0.0f};
+    }
+    for (int q = tid; q < a.nper; q += kSeedThreads) {
+        const BermudanPeriod pq = a.per[q];
+        c.strike[q] = (float)pq.strike;
+        c.lennot[q] = (float)(pq.period_length * pq.notional);
+        c.fixbits[q] = __double_as_longlong(pq.fixing);
+        c.libor_slot[q] = pq.libor_slot;
+        c.libor_index[q] = pq.libor_index;
+        c.pay[q] = pq.pay_num_index;
+    }
+    if (tid < kSeedThreads / 32) wsum[tid][65] = Sum2{0.0f, 0.0f};
+    __syncthreads();
+    const float* states = static_cast<const float*>(a.states);
+    if (a.pass == 1) {
+        const long long taubits = active ? __double_as_longlong(a.ex_time[p]) : 0;
+        Sum2 x{0.0f, 0.0f};
+        for (int q = 0; q < a.nper; q++) {
+            // a callable payer receives the periods from its exercise date on; a cancelable one
+            // receives the periods before its exercise date (times >= 0: bit order = value order)
+            const bool paid = active && (a.callable ? (c.fixbits[q] >= taubits) : (c.fixbits[q] < taubits));
+            const int l = c.pay[q];
+            float cf = 0.0f;
+            if (paid) {
+                const float L = states[((size_t)c.libor_slot[q] * N + c.libor_index[q]) * P + p];
+                const float invN = f64_to_f32_int(a.inv_numeraire[(size_t)l * P + p]) * c.r_adj[l];
+                cf = __fmul_rn((L - c.strike[q]) * c.lennot[q], invN);  // exact input of the Sum2 below
+                seeds[(size_t)c.libor_index[q] * P + p] += c.lennot[q] * invN;
+                if (!a.det[l]) nb[(size_t)l * P + p] -= cf * invN;
+            }
+            sum2_add(x, cf);
+            Sum2 v{cf, 0.0f};
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                const Sum2 y{__shfl_down_sync(0xffffffffu, v.p, off), __shfl_down_sync(0xffffffffu, v.s, off)};
+                v = sum2_merge(v, y);
+            }
+            if (lane == 0) wsum[warp][l] = sum2_merge(wsum[warp][l], v);
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const Sum2 y{__shfl_down_sync(0xffffffffu, x.p, off), __shfl_down_sync(0xffffffffu, x.s, off)};
+            x = sum2_merge(x, y);
+        }
+        if (lane == 0) wsum[warp][65] = x;
+        __syncthreads();
+        // block partials, the warps merged in warp order
+        for (int l = tid; l <= N + 1; l += kSeedThreads) {
+            const int col = (l <= N) ? l : 65;
+            Sum2 acc = wsum[0][col];
+            for (int w = 1; w < kSeedThreads / 32; w++) acc = sum2_merge(acc, wsum[w][col]);
+            const double sum = sum2_value(acc);
+            if (l <= N) {
+                const bool adjusted = a.has_discount && !a.det[l] && l >= 1;
+                a.abar_partials[(size_t)blockIdx.x * (N + 1) + l] = adjusted ? -sum / a.adj[l] : 0.0;
+            } else {
+                a.value_partials[blockIdx.x] = sum;
+            }
+        }
+        return;
+    }
+    if (!active) return;
+    const float invP = 1.0f / (float)P;
+    float un = 0.0f;
+    for (int l = N; l >= 1; l--) {
+        float t = un;
+        if (a.has_discount) {
+            if (!a.det[l]) {
+                t += nb[(size_t)l * P + p] * c.adj_pd[l];
+                if (!a.freeze_adjustment) {
+                    const float iN = f64_to_f32_int(a.inv_numeraire[(size_t)l * P + p]);
+                    t -= c.abar[l] * (iN * iN);
+                }
+            }
+        } else {
+            t += nb[(size_t)l * P + p];
+        }
+        const float Nprev = f64_to_f32_int(a.numeraire[(size_t)(l - 1) * P + p]);
+        const float Lf = states[((size_t)a.T_slot * N + (l - 1)) * P + p];  // frozen fixing L_{l-1}(T_{l-1})
+        float* sd = seeds + (size_t)(l - 1) * P + p;
+        *sd = (*sd + t * Nprev * c.delta[l - 1]) * invP;
+        un = t * (1.0f + Lf * c.delta[l - 1]);
     }
 }
 
@@ -757,15 +874,16 @@ int launch_adjoint(const AdjointLaunch& L, cudaStream_t s)
     const int sb = (L.P + kSeedThreads - 1) / kSeedThreads;
     {
         KernelTimer kt(K_ADJOINT, s, 4);
-        LMM_CUDA(cudaMemsetAsync(L.d_seeds, 0, sizeof(double) * (size_t)L.N * L.P, s));
-        LMM_CUDA(cudaMemsetAsync(L.d_nb, 0, sizeof(double) * (size_t)(L.N + 1) * L.P, s));
+        const size_t esz = L.fp32 ? sizeof(float) : sizeof(double);  // the mixed form keeps FP32 seeds
+        LMM_CUDA(cudaMemsetAsync(L.d_seeds, 0, esz * (size_t)L.N * L.P, s));
+        LMM_CUDA(cudaMemsetAsync(L.d_nb, 0, esz * (size_t)(L.N + 1) * L.P, s));
         sp.pass = 1;
-        if (L.fp32) seed_kernel<float><<<sb, kSeedThreads, 0, s>>>(sp);
+        if (L.fp32) seed_mixed_kernel<<<sb, kSeedThreads, 0, s>>>(sp);
         else seed_kernel<double><<<sb, kSeedThreads, 0, s>>>(sp);
         column_sum_kernel<<<(L.N + 1 + 31) / 32, 1024, 0, s>>>(L.d_abar_partials, sb, L.N + 1, 1.0 / (double)L.P, L.d_abar);
         column_sum_kernel<<<1, 1024, 0, s>>>(L.d_value_partials, sb, 1, 1.0 / (double)L.P, L.d_value_out);
         sp.pass = 2;
-        if (L.fp32) seed_kernel<float><<<sb, kSeedThreads, 0, s>>>(sp);
+        if (L.fp32) seed_mixed_kernel<<<sb, kSeedThreads, 0, s>>>(sp);
         else seed_kernel<double><<<sb, kSeedThreads, 0, s>>>(sp);
         LMM_CUDA(cudaGetLastError());
     }

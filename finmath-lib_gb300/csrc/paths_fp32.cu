@@ -48,7 +48,10 @@ struct Smem32 {
     Sum2 wsum[kPathThreads / 32][NMAX];             // numeraire-adjustment warp sums
 };
 
-template <int NMAX, int FMAX>
+// CAPPED: the model caps the forward rates.  The cap is a compile-time variant: on this GPU
+// the compiler's min/select for `v > cap ? cap : v` issues to the narrow FP64 pipe, once per
+// component and step, which costs the uncapped models several percent if left in.
+template <int NMAX, int FMAX, bool CAPPED>
 __global__ void __launch_bounds__(kPathThreads, NMAX <= 40 ? 4 : 2) paths_fp32_kernel(const PathLaunch a, const float* __restrict__ lam32,
                                                                   const float* __restrict__ var32)
 {
@@ -61,8 +64,7 @@ __global__ void __launch_bounds__(kPathThreads, NMAX <= 40 ? 4 : 2) paths_fp32_k
     const int p = blockIdx.x * kPathThreads + tid;
     const bool active = p < a.P;
     const int N = a.N, F = a.F, P = a.P;
-    const bool capped = !isinf(a.libor_cap);
-    const float cap = capped ? (float)a.libor_cap : 0.0f;
+    const float cap = CAPPED ? (float)a.libor_cap : 0.0f;
     const float* dW = static_cast<const float*>(a.d_dw);
     float* states = static_cast<float*>(a.d_states);
 
@@ -85,7 +87,7 @@ __global__ void __launch_bounds__(kPathThreads, NMAX <= 40 ? 4 : 2) paths_fp32_k
         if (j < N) {
             Y[j] = __ldg(a.d_init_log32 + j);
             float v = __expf(Y[j]);
-            if (capped && v > cap) v = cap;
+            if (CAPPED && v > cap) v = cap;
             L[j] = v;
         } else {
             Y[j] = 0.0f;
@@ -150,7 +152,7 @@ __global__ void __launch_bounds__(kPathThreads, NMAX <= 40 ? 4 : 2) paths_fp32_k
                 }
                 Y[j] = Y[j] + fmaf(mu2.x + mu2.y, dt, df2.x + df2.y);
                 float v = __expf(Y[j]);
-                if (capped && v > cap) v = cap;
+                if (CAPPED && v > cap) v = cap;
                 L[j] = v;
             }
         });
@@ -225,18 +227,26 @@ __global__ void __launch_bounds__(kPathThreads, NMAX <= 40 ? 4 : 2) paths_fp32_k
     }
 }
 
-template <int NMAX, int FMAX>
+template <int NMAX, int FMAX, bool CAPPED>
 int launch_t(const PathLaunch& a, const float* lam32, const float* var32, cudaStream_t s, int blocks)
 {
     const size_t smem = sizeof(Smem32<NMAX, FMAX>);
     static bool attr_set = false;  // set once, before any stream capture
     if (!attr_set) {
-        LMM_CUDA(cudaFuncSetAttribute(paths_fp32_kernel<NMAX, FMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        LMM_CUDA(cudaFuncSetAttribute(paths_fp32_kernel<NMAX, FMAX, CAPPED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
         attr_set = true;
     }
-    paths_fp32_kernel<NMAX, FMAX><<<blocks, kPathThreads, smem, s>>>(a, lam32, var32);
+    paths_fp32_kernel<NMAX, FMAX, CAPPED><<<blocks, kPathThreads, smem, s>>>(a, lam32, var32);
     LMM_CUDA(cudaGetLastError());
     return LMM_OK;
+}
+
+template <int NMAX, int FMAX>
+int launch_c(const PathLaunch& a, const float* lam32, const float* var32, cudaStream_t s, int blocks)
+{
+    if (isinf(a.libor_cap)) return launch_t<NMAX, FMAX, false>(a, lam32, var32, s, blocks);
+    return launch_t<NMAX, FMAX, true>(a, lam32, var32, s, blocks);
 }
 
 }  // namespace
@@ -253,9 +263,9 @@ int launch_paths_fp32(const PathLaunch& a, const float* lam32, const float* var3
     const int blocks = path_blocks(a.P);
     if (blocks_out) *blocks_out = blocks;
     KernelTimer kt(K_PATHS_FP32, s);
-    if (a.N <= 24 && a.F <= 4) return launch_t<24, 4>(a, lam32, var32, s, blocks);
-    if (a.N <= 40 && a.F <= 10) return launch_t<40, 10>(a, lam32, var32, s, blocks);
-    if (a.N <= 64 && a.F <= 16) return launch_t<64, 16>(a, lam32, var32, s, blocks);
+    if (a.N <= 24 && a.F <= 4) return launch_c<24, 4>(a, lam32, var32, s, blocks);
+    if (a.N <= 40 && a.F <= 10) return launch_c<40, 10>(a, lam32, var32, s, blocks);
+    if (a.N <= 64 && a.F <= 16) return launch_c<64, 16>(a, lam32, var32, s, blocks);
     return fail(LMM_ERR_INVALID, "mixed path kernel supports at most 64 forward rates and 16 factors");
 }
 

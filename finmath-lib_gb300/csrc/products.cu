@@ -423,10 +423,7 @@ __global__ void __launch_bounds__(32) bermudan_svd_kernel(const double* partials
 // X^T y sums of one date and beta = V diag(1/s) U^T (X^T y) with the SVD's cutoff,
 // in the oracle's order (MonteCarloConditionalExpectationRegression.java:141-147).  Run by
 // one block of at least 6 warps (all its threads call it).
-// With pairs set (mixed form) the coefficients are stored as FP32 pairs hi, lo (beta_out
-// then holds 12 floats) for the FP32 conditional expectation of the next step.
-__device__ void regression_solve(const double* partials, int blocks, int P, const double* svd, double* beta_out,
-                                 bool pairs = false)
+__device__ void regression_solve(const double* partials, int blocks, int P, const double* svd, double* beta_out)
 {
     __shared__ double b[kRhs];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -453,14 +450,48 @@ __device__ void regression_solve(const double* partials, int blocks, int P, cons
             for (int r = 0; r < 6; r++) utb += U[r * 6 + j] * b[r];
             acc += V[i * 6 + j] * (utb / s[j]);
         }
-        if (pairs) {
-            float hi, lo;
-            split_double(acc, hi, lo);
-            reinterpret_cast<float*>(beta_out)[2 * i] = hi;
-            reinterpret_cast<float*>(beta_out)[2 * i + 1] = lo;
-        } else {
-            beta_out[i] = acc;
+        beta_out[i] = acc;
+    }
+}
+
+// Mixed form: the same solve from block partials that are FP32 Sum2 pairs, merged in FP32
+// (block order within a lane, then tree order across the lanes) before the FP64 apply, and
+// the coefficients stored as FP32 pairs.
+__device__ void regression_solve_mixed(const float* partials, int blocks, int P, const double* svd, double* beta_out)
+{
+    __shared__ double b[kRhs];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (warp < kRhs) {
+        Sum2 acc{0.0f, 0.0f};
+        for (int k = lane; k < blocks; k += 32) {
+            const float* q = partials + ((size_t)k * kRhs + warp) * 2;
+            acc = sum2_merge(acc, Sum2{q[0], q[1]});
         }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const Sum2 y{__shfl_down_sync(0xffffffffu, acc.p, off), __shfl_down_sync(0xffffffffu, acc.s, off)};
+            acc = sum2_merge(acc, y);
+        }
+        if (lane == 0) b[warp] = sum2_value(acc) / (double)P;
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        const double* U = svd;
+        const double* s = svd + 36;
+        const double* V = svd + 42;
+        const double tol = svd[78];
+        const int i = threadIdx.x;
+        double acc = 0.0;
+        for (int j = 0; j < 6; j++) {
+            if (!(s[j] > tol)) continue;
+            double utb = 0.0;
+            for (int r = 0; r < 6; r++) utb += U[r * 6 + j] * b[r];
+            acc += V[i * 6 + j] * (utb / s[j]);
+        }
+        float hi, lo;
+        split_double(acc, hi, lo);
+        reinterpret_cast<float*>(beta_out)[2 * i] = hi;
+        reinterpret_cast<float*>(beta_out)[2 * i + 1] = lo;
     }
 }
 
@@ -483,7 +514,7 @@ struct BermStepParams {
 // The last block of a step launch to finish reduces every block's X^T y partials (in block
 // order) and solves for the date's coefficients; nothing waits on another block.  All
 // threads of every block call it after writing their block's partials.
-__device__ void finish_date_last_block(const BermStepParams& a, bool pairs)
+__device__ void finish_date_last_block(const BermStepParams& a, bool mixed)
 {
     __shared__ bool last;
     __threadfence();
@@ -493,7 +524,8 @@ __device__ void finish_date_last_block(const BermStepParams& a, bool pairs)
     __syncthreads();
     if (last) {
         __threadfence();
-        regression_solve(a.partials, gridDim.x, a.sh.P, a.svd_cur, a.beta_cur, pairs);
+        if (mixed) regression_solve_mixed(reinterpret_cast<const float*>(a.partials), gridDim.x, a.sh.P, a.svd_cur, a.beta_cur);
+        else regression_solve(a.partials, gridDim.x, a.sh.P, a.svd_cur, a.beta_cur);
         if (threadIdx.x == 0) *done = 0u;  // ready for the next date
     }
 }
@@ -668,7 +700,7 @@ __global__ void __launch_bounds__(kProdThreads) bermudan_step_mixed_kernel(const
         }
     }
     if (bcur) {
-        block_sums_sum2<kRhs>(acc, a.partials + (size_t)blockIdx.x * kRhs * 2, 1);
+        block_sums_sum2<kRhs, float>(acc, reinterpret_cast<float*>(a.partials) + (size_t)blockIdx.x * kRhs * 2, 1);
         finish_date_last_block(a, true);
     }
 }

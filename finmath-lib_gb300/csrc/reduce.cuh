@@ -108,11 +108,12 @@ __device__ __forceinline__ void block_sums_warp_plain(const double (&v)[NV], dou
 
 // Block sums of NV Sum2 partials per thread (mixed-precision form) with no FP64 arithmetic:
 // the pairs are merged exactly in FP32 across the lanes (tree order) and then the warps
-// (warp order); thread i < NV writes sum i as the unnormalised pair (p, s) widened to FP64
-// to out + 2 (i * stride), which the compensated FP64 block-order sums downstream accept.
+// (warp order); thread i < NV writes sum i as the unnormalised pair (p, s) to out + 2 (i *
+// stride): widened to FP64 for compensated FP64 block-order sums downstream, or kept as
+// FP32 for Sum2 merges downstream.
 // All threads must call it.
-template <int NV>
-__device__ __forceinline__ void block_sums_sum2(const Sum2 (&v)[NV], double* out, int stride)
+template <int NV, typename OutT = double>
+__device__ __forceinline__ void block_sums_sum2(const Sum2 (&v)[NV], OutT* out, int stride)
 {
     __shared__ Sum2 ws[32][NV];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -131,8 +132,8 @@ __device__ __forceinline__ void block_sums_sum2(const Sum2 (&v)[NV], double* out
     if (threadIdx.x < NV) {
         Sum2 acc = ws[0][threadIdx.x];
         for (int w = 1; w < nwarps; w++) acc = sum2_merge(acc, ws[w][threadIdx.x]);
-        out[2 * (size_t)threadIdx.x * stride] = (double)acc.p;
-        out[2 * (size_t)threadIdx.x * stride + 1] = (double)acc.s;
+        out[2 * (size_t)threadIdx.x * stride] = (OutT)acc.p;
+        out[2 * (size_t)threadIdx.x * stride + 1] = (OutT)acc.s;
     }
 }
 
