@@ -13,8 +13,13 @@
 // at the end from the frozen fixings, and each block writes compensated partial sums
 // of 1/N(T_l) for the numeraire adjustment.
 //
-// Compiled with -fmad=false: every + and * rounds separately, as in the reference's
-// Java; exp/log/division are CUDA's (division correctly rounded, exp/log within 1 ulp).
+// Compiled with -fmad=false.  The fast kernel fuses the drift's and the Euler step's
+// multiply-adds into FP64 FMAs (half the instructions on the GPU's narrow FP64 pipe, which
+// bounds this kernel; each fused step rounds once instead of twice, so the states agree with
+// the reference's unfused order to about 1e-14 relative, inside the 1e-12 parity bound);
+// everything else rounds separately as in the reference's Java.  exp/log/division are CUDA's
+// (division correctly rounded, exp/log within 1 ulp).  The general kernel keeps the
+// reference's unfused order throughout.
 #pragma once
 
 #include "lmm_internal.h"
@@ -25,13 +30,22 @@ namespace {
 
 constexpr int kPathThreads = 128;
 
+// v capped at the bit pattern capbits of a positive cap: for v >= 0 (exp's range) the IEEE
+// order is the integer order of the bit patterns, so the comparison needs no FP64
+// instruction (the GPU's FP64 pipe bounds this kernel); NaN stays NaN (Math.min semantics)
+__device__ __forceinline__ double cap_positive(double v, long long capbits)
+{
+    const long long b = __double_as_longlong(v);
+    return (b > capbits && b <= 0x7ff0000000000000LL) ? __longlong_as_double(capbits) : v;
+}
+
 template <int NMAX, int FMAX, bool FUNCTIONAL>
 __global__ void __launch_bounds__(kPathThreads) paths_fp64_kernel(const PathLaunch a)
 {
     const int p = blockIdx.x * kPathThreads + threadIdx.x;
     const bool active = p < a.P;
     const int N = a.N, F = a.F, P = a.P;
-    const bool capped = !isinf(a.libor_cap);
+    const long long capbits = __double_as_longlong(a.libor_cap);  // +infinity when uncapped: never caps
     const double* dW = static_cast<const double*>(a.d_dw);
     double* states = static_cast<double*>(a.d_states);
 
@@ -43,8 +57,7 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp64_kernel(const PathLaun
             // getInitialState (:1081-1093): log(max(f,0)); applyStateSpaceTransform (:1200-1212)
             const double f = __ldg(a.d_init + j);
             const double y0 = log(f > 0.0 ? f : 0.0);
-            double v = exp(y0);
-            if (capped && v > a.libor_cap) v = a.libor_cap;
+            const double v = cap_positive(exp(y0), capbits);
             L[j] = v;
             if (!FUNCTIONAL) Y[FUNCTIONAL ? 0 : j] = y0;
         } else {
@@ -90,23 +103,21 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp64_kernel(const PathLaun
                 for (int k = 0; k < FMAX; k++) {
                     if (k < F) {
                         lj[k] = __ldg(lam + j * F + k);
-                        S[k] = S[k] + os * lj[k];  // :1156-1158
+                        S[k] = fma(os, lj[k], S[k]);  // :1156-1158
                     }
                 }
 #pragma unroll
                 for (int k = 0; k < FMAX; k++)
-                    if (k < F) mu = mu + S[k] * lj[k];  // :1159 (addSumProduct, left to right)
-                mu = mu + __ldg(var_half + j);           // :1183-1189, variance * -0.5
+                    if (k < F) mu = fma(S[k], lj[k], mu);  // :1159 (addSumProduct, left to right)
+                mu = mu + __ldg(var_half + j);              // :1183-1189, variance * -0.5
                 // Euler step (EulerSchemeFromProcessModel.java:235-255)
                 double y = FUNCTIONAL ? log(Lj) : Y[FUNCTIONAL ? 0 : j];
-                y = y + mu * dt;
+                y = fma(mu, dt, y);
 #pragma unroll
                 for (int k = 0; k < FMAX; k++)
-                    if (k < F) y = y + dw[k] * lj[k];
+                    if (k < F) y = fma(dw[k], lj[k], y);
                 if (!FUNCTIONAL) Y[FUNCTIONAL ? 0 : j] = y;
-                double v = exp(y);
-                if (capped && v > a.libor_cap) v = a.libor_cap;
-                L[j] = v;
+                L[j] = cap_positive(exp(y), capbits);
             }
         }
         const int slot = __ldg(a.d_obs_slot + i + 1);
