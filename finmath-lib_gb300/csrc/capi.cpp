@@ -183,6 +183,7 @@ struct lmm_process {
     cudaStream_t stream = nullptr;
     // device tables
     double *d_loadings = nullptr, *d_variance = nullptr, *d_dt = nullptr, *d_delta = nullptr, *d_init = nullptr;
+    double* d_exp_tab = nullptr;
     double *d_inv_delta = nullptr, *d_var_half = nullptr;
     float *d_lam32 = nullptr, *d_var32 = nullptr, *d_inv_delta32 = nullptr, *d_dt32 = nullptr, *d_init_log32 = nullptr;
     float* d_delta_pair = nullptr;
@@ -475,6 +476,9 @@ int lmm_process_create(const lmm_model_desc* m, lmm_brownian* bm, lmm_process** 
     if (!rc) rc = upload(&pr->d_variance, m->variance, (size_t)T * N, s);
     if (!rc) rc = upload(&pr->d_dt, dt.data(), dt.size(), s);
     if (!rc) rc = upload(&pr->d_delta, delta.data(), delta.size(), s);
+    std::vector<double> etab(129);  // lives until the stream synchronisation below
+    fp64_exp_table(etab.data());
+    if (!rc) rc = upload(&pr->d_exp_tab, etab.data(), etab.size(), s);
     if (!rc) rc = upload(&pr->d_inv_delta, inv_delta.data(), inv_delta.size(), s);
     if (!rc) rc = upload(&pr->d_var_half, var_half.data(), var_half.size(), s);
     if (!rc) rc = upload(&pr->d_init, m->initial_forwards, (size_t)N, s);
@@ -565,6 +569,7 @@ static int process_ensure(lmm_process* pr)
     a.d_dt = pr->d_dt;
     a.d_first = pr->d_first;
     a.d_delta = pr->d_delta;
+    a.d_exp_tab = pr->d_exp_tab;
     a.d_inv_delta = pr->d_inv_delta;
     a.d_var_half = pr->d_var_half;
     a.d_inv_delta32 = pr->d_inv_delta32;
@@ -665,6 +670,7 @@ int lmm_process_destroy(lmm_process* pr)
     dfree(pr->d_variance, s);
     dfree(pr->d_dt, s);
     dfree(pr->d_delta, s);
+    dfree(pr->d_exp_tab, s);
     dfree(pr->d_inv_delta, s);
     dfree(pr->d_var_half, s);
     dfree(pr->d_init, s);

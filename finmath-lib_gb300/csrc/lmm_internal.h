@@ -118,6 +118,7 @@ struct PathLaunch {
     const float* d_dt32;       // [T] time steps in FP32 (mixed form)
     const float* d_init_log32; // [N] log of the initial forwards in FP32 (mixed form)
     const float* d_delta_pair; // [N][2] period lengths as FP32 pairs hi + lo (mixed form)
+    const double* d_exp_tab;   // [129] exp(k/64), k = -64..64 (FP64 form, see fp64math.cuh)
     const double* d_init;      // [N] initial forwards
     const int* d_obs_slot;     // [T+1] observation slot or -1
     const void* d_dw;          // [T][F][P] fp64 or fp32
@@ -134,6 +135,8 @@ int launch_paths_fp64(const PathLaunch& a, cudaStream_t s, int* blocks_out);
 int paths_fp32_pitch(int N, int F);
 int launch_paths_fp32(const PathLaunch& a, const float* lam32, const float* var32, cudaStream_t s, int* blocks_out);
 int path_blocks(int P);
+// exp(k/64) for k = -64..64, rounded to FP64 from extended precision (the table of exp_small)
+void fp64_exp_table(double out[129]);
 
 // numeraire adjustment: adj[l] = mean over paths of 1/N_l (or the deterministic value)
 int launch_numeraire_finish(const double* d_partials, int blocks, int N, int P, const double* d_numeraire,

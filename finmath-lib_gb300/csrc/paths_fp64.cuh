@@ -13,15 +13,20 @@
 // at the end from the frozen fixings, and each block writes compensated partial sums
 // of 1/N(T_l) for the numeraire adjustment.
 //
-// Compiled with -fmad=false.  The fast kernel fuses the drift's and the Euler step's
-// multiply-adds into FP64 FMAs (half the instructions on the GPU's narrow FP64 pipe, which
-// bounds this kernel; each fused step rounds once instead of twice, so the states agree with
-// the reference's unfused order to about 1e-14 relative, inside the 1e-12 parity bound);
-// everything else rounds separately as in the reference's Java.  exp/log/division are CUDA's
-// (division correctly rounded, exp/log within 1 ulp).  The general kernel keeps the
-// reference's unfused order throughout.
+// Compiled with -fmad=false.  The GPU's narrow FP64 pipe bounds the fast kernel, so it
+// spends fewer FP64 instructions than the reference's literal arithmetic, all in FP64:
+//  * the drift's and the Euler step's multiply-adds are fused FP64 FMAs (each rounds once
+//    instead of twice);
+//  * the Euler-log step exp(log L + d) (EULER_FUNCTIONAL) is evaluated as L exp(d), and the
+//    EULER step exp(Y + d) as exp(Y) exp(d) with exp(Y) carried instead of Y, where exp(d)
+//    of the small step increment d is exp_small (fp64math.cuh) -- no log, and a 12-FMA exp;
+//  * the drift's L / (L + 1/delta) takes a Newton reciprocal (rcp_newton) for the division.
+// The states agree with the reference's order to about 1e-14 relative, inside the 1e-12
+// parity bound.  The general kernel keeps the reference's literal order throughout
+// (CUDA's exp/log, correctly rounded division, unfused).
 #pragma once
 
+#include "fp64math.cuh"
 #include "lmm_internal.h"
 #include "reduce.cuh"
 
@@ -49,17 +54,17 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp64_kernel(const PathLaun
     const double* dW = static_cast<const double*>(a.d_dw);
     double* states = static_cast<double*>(a.d_states);
 
+    const double* etab = a.d_exp_tab;
     double L[NMAX];
-    double Y[FUNCTIONAL ? 1 : NMAX];
+    double E[FUNCTIONAL ? 1 : NMAX];  // EULER: exp of the uncapped log state Y
 #pragma unroll
     for (int j = 0; j < NMAX; j++) {
         if (j < N) {
             // getInitialState (:1081-1093): log(max(f,0)); applyStateSpaceTransform (:1200-1212)
             const double f = __ldg(a.d_init + j);
-            const double y0 = log(f > 0.0 ? f : 0.0);
-            const double v = cap_positive(exp(y0), capbits);
-            L[j] = v;
-            if (!FUNCTIONAL) Y[FUNCTIONAL ? 0 : j] = y0;
+            const double e0 = exp(log(f > 0.0 ? f : 0.0));
+            L[j] = cap_positive(e0, capbits);
+            if (!FUNCTIONAL) E[FUNCTIONAL ? 0 : j] = e0;
         } else {
             L[j] = 0.0;
         }
@@ -96,7 +101,7 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp64_kernel(const PathLaun
                 const double Lj = L[j];
                 // Scalar(delta).discount(L, delta) = 1/(L*(delta/delta) + 1/delta) (stochastic/Scalar.java:321-328),
                 // times L (:1149-1153); delta/delta is exactly 1.0 and 1/delta is precomputed.
-                const double os = (1.0 / (Lj + __ldg(a.d_inv_delta + j))) * Lj;
+                const double os = rcp_newton(Lj + __ldg(a.d_inv_delta + j)) * Lj;
                 double mu = 0.0;
                 double lj[FMAX];
 #pragma unroll
@@ -110,14 +115,21 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp64_kernel(const PathLaun
                 for (int k = 0; k < FMAX; k++)
                     if (k < F) mu = fma(S[k], lj[k], mu);  // :1159 (addSumProduct, left to right)
                 mu = mu + __ldg(var_half + j);              // :1183-1189, variance * -0.5
-                // Euler step (EulerSchemeFromProcessModel.java:235-255)
-                double y = FUNCTIONAL ? log(Lj) : Y[FUNCTIONAL ? 0 : j];
-                y = fma(mu, dt, y);
+                // Euler step (EulerSchemeFromProcessModel.java:235-255): the increment d of
+                // the log state, then L exp(d) (FUNCTIONAL: log L is the state) or
+                // exp(Y) exp(d) (EULER)
+                double d = mu * dt;
 #pragma unroll
                 for (int k = 0; k < FMAX; k++)
-                    if (k < F) y = fma(dw[k], lj[k], y);
-                if (!FUNCTIONAL) Y[FUNCTIONAL ? 0 : j] = y;
-                L[j] = cap_positive(exp(y), capbits);
+                    if (k < F) d = fma(dw[k], lj[k], d);
+                const double g = exp_small(d, etab);
+                if (FUNCTIONAL) {
+                    L[j] = cap_positive(Lj * g, capbits);
+                } else {
+                    const double e = E[FUNCTIONAL ? 0 : j] * g;
+                    E[FUNCTIONAL ? 0 : j] = e;
+                    L[j] = cap_positive(e, capbits);
+                }
             }
         }
         const int slot = __ldg(a.d_obs_slot + i + 1);

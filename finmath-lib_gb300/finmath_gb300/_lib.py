@@ -102,6 +102,7 @@ SIGNATURES = {
     "lmm_stats_get": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_char_p), _I64, _D]),
     "lmm_process_stream": (ctypes.c_int, [_VP, ctypes.POINTER(_VP)]),
     "lmm_probe_fp64_fma_rate": (ctypes.c_int, [_D]),
+    "lmm_fp64_math_check": (ctypes.c_int, [ctypes.c_int64, _D, _D]),
 }
 
 

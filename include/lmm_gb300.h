@@ -287,6 +287,11 @@ int lmm_process_stream(lmm_process* proc, void** out_stream);
 /* A FP64 fused-multiply-add throughput probe (DFMA/s), used to report the FP64 roofline. */
 int lmm_probe_fp64_fma_rate(double* out_fma_per_second);
 
+/* Self-check of the FP64 path kernel's small-argument exp (table-driven, |d| <= 1) and
+ * Newton reciprocal against CUDA's exp and correctly rounded division on n grid points:
+ * the largest errors in ulps.  A test of the device arithmetic; not a production path. */
+int lmm_fp64_math_check(int64_t n, double* max_ulp_exp, double* max_ulp_rcp);
+
 #ifdef __cplusplus
 }
 #endif

@@ -92,3 +92,13 @@ def test_repeatable_bitwise():
     a = W.build(W.LMM20, paths=3000)
     b = W.build(W.LMM20, paths=3000)
     assert np.array_equal(a.getLIBOR(20, 19), b.getLIBOR(20, 19))
+
+
+def test_fp64_small_exp_and_newton_reciprocal():
+    # the FP64 path kernel's exp(d) of the step increment (table-driven, |d| <= 1) and its
+    # Newton reciprocal against CUDA's exp and correctly rounded division
+    import ctypes
+    e, r = ctypes.c_double(), ctypes.c_double()
+    assert F.load().lmm_fp64_math_check(1 << 20, ctypes.byref(e), ctypes.byref(r)) == 0
+    assert e.value <= 4.0, e.value
+    assert r.value <= 1.0, r.value
