@@ -117,7 +117,6 @@ struct PathLaunch {
     const float* d_inv_delta32;// [N] 1/delta in FP32 (mixed form)
     const float* d_dt32;       // [T] time steps in FP32 (mixed form)
     const float* d_init_log32; // [N] log of the initial forwards in FP32 (mixed form)
-    const float* d_delta_pair; // [N][2] period lengths as FP32 pairs hi + lo (mixed form)
     const double* d_exp_tab;   // [129] exp(k/64), k = -64..64 (FP64 form, see fp64math.cuh)
     const double* d_init;      // [N] initial forwards
     const int* d_obs_slot;     // [T+1] observation slot or -1

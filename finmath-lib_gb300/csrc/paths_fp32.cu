@@ -15,6 +15,7 @@
 // not wait on global memory.  The sums over factors run on paired FP32 FMAs (__ffma2_rn,
 // two factors per instruction).
 #include "lmm_internal.h"
+#include "fp64math.cuh"
 #include "reduce.cuh"
 #include "unroll_range.cuh"
 
@@ -45,7 +46,7 @@ struct Smem32 {
     static constexpr int TABLE = NMAX * FP + NMAX;  // loadings rows [NMAX][FP], then variances [NMAX]
     float table[kPathThreads / 32][2][TABLE];       // per warp, two steps
     float dw[2][FMAX][kPathThreads];                // per thread column, two steps
-    Sum2 wsum[kPathThreads / 32][NMAX];             // numeraire-adjustment warp sums
+    double wsum[kPathThreads / 32][NMAX];           // numeraire-adjustment warp sums
 };
 
 // CAPPED: the model caps the forward rates.  The cap is a compile-time variant: on this GPU
@@ -170,60 +171,36 @@ __global__ void __launch_bounds__(kPathThreads, NMAX <= 40 ? 4 : 2) paths_fp32_k
         }
     }
     cp_async_wait();
-    // Spot numeraire from the frozen fixings, N_{l+1} = N_l (1 + L_l delta_l), and 1/N, in
-    // double-float arithmetic (FP32 pairs hi + lo, about 2^-47 relative per factor; FP64
-    // instructions would issue to the narrow FP64 pipe), stored in FP64 (each pair widened
-    // in integer operations and added: one FP64 add per value).  The block partial sums of
-    // 1/N_l for the numeraire adjustment are Sum2 pairs merged across lanes (tree order) and
-    // warps (warp order) in FP32.
-    float Nh = 1.0f, Nl = 0.0f;
+    // FP64 spot numeraire from the frozen fixings (as paths_fp64.cu), 1/N by a Newton
+    // reciprocal in FP64 (fp64math.cuh), the FP32 fixings widened in integer operations.
+    // The block partial sums of 1/N_l for the numeraire adjustment: plain FP64 within a warp
+    // (lane order), compensated across the block's warps (warp order).
+    double Nv = 1.0;
     if (active) a.d_numeraire[p] = 1.0;
     if (a.d_inv_numeraire && active) a.d_inv_numeraire[p] = 1.0;
-    const float2* dpair = reinterpret_cast<const float2*>(a.d_delta_pair);
 #pragma unroll
     for (int l = 0; l < NMAX; l++) {
         if (l < N) {
-            const float2 dl = __ldg(dpair + l);
-            // g = 1 + L_l delta_l as a pair (the product exact, then one TwoSum)
-            const float ph = __fmul_rn(L[l], dl.x);
-            float pl = fmaf(L[l], dl.x, -ph);
-            pl = fmaf(L[l], dl.y, pl);
-            float gh, gl;
-            two_sum(1.0f, ph, gh, gl);
-            gl += pl;
-            // N = N g (Dekker's product with a fused multiply-add), renormalised
-            const float mh = __fmul_rn(Nh, gh);
-            float ml = fmaf(Nh, gh, -mh);
-            ml = fmaf(Nh, gl, ml);
-            ml = fmaf(Nl, gh, ml);
-            Nh = mh + ml;
-            Nl = ml - (Nh - mh);
-            // 1/N: the FP32 reciprocal and one Newton correction r e, e = 1 - N r
-            const float r = __frcp_rn(Nh);
-            float e = fmaf(-Nh, r, 1.0f);
-            e = fmaf(-Nl, r, e);
-            const float rl = __fmul_rn(r, e);
-            if (active) {
-                a.d_numeraire[(size_t)(l + 1) * P + p] = f32_to_f64_int(Nh) + f32_to_f64_int(Nl);
-                if (a.d_inv_numeraire) a.d_inv_numeraire[(size_t)(l + 1) * P + p] = f32_to_f64_int(r) + f32_to_f64_int(rl);
-            }
-            Sum2 v = active ? Sum2{r, rl} : Sum2{0.0f, 0.0f};
+            const double delta = __ldg(a.d_delta + l);
+            const double Ll = f32_to_f64_int(L[l]);
+            if (l < a.num_det_prefix) Nv = Ll * (delta * Nv) + Nv;
+            else Nv = Nv * (1.0 + Ll * delta);
+            if (active) a.d_numeraire[(size_t)(l + 1) * P + p] = Nv;
+            double v = active ? rcp_newton(Nv) : 0.0;
+            if (a.d_inv_numeraire && active) a.d_inv_numeraire[(size_t)(l + 1) * P + p] = v;
 #pragma unroll
-            for (int off = 16; off > 0; off >>= 1) {
-                const Sum2 y{__shfl_down_sync(0xffffffffu, v.p, off), __shfl_down_sync(0xffffffffu, v.s, off)};
-                v = sum2_merge(v, y);
-            }
+            for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
             if (lane == 0) sm.wsum[warp][l] = v;
         }
     }
     __syncthreads();
     if (tid < N) {
-        Sum2 acc = sm.wsum[0][tid];
+        dd acc{0.0, 0.0};
 #pragma unroll
-        for (int w = 1; w < kPathThreads / 32; w++) acc = sum2_merge(acc, sm.wsum[w][tid]);
+        for (int w = 0; w < kPathThreads / 32; w++) acc = dd_add_d(acc, sm.wsum[w][tid]);
         double* o = a.d_inv_num_partials + ((size_t)blockIdx.x * N + tid) * 2;
-        o[0] = (double)acc.p;
-        o[1] = (double)acc.s;
+        o[0] = acc.hi;
+        o[1] = acc.lo;
     }
 }
 

@@ -275,8 +275,8 @@ __global__ void __launch_bounds__(kProdThreads, sizeof(TS) == 4 ? 3 : 1) bermuda
     const BermudanPeriod c = a.per[a.ex_period[e]];
     double acc[kGram];
     if (sizeof(TS) == 4) {
-        // mixed form: FP32 basis (stored as FP32), Gram sums in twice FP32 precision
-        // (Sum2 / Dot2 per thread), FP64 across threads
+        // mixed form: the basis in FP32 (stored as FP32), the Gram sums in FP64 (plain within
+        // a thread and a warp, compensated across warps and blocks)
         __shared__ SwapRows32 rows;
         for (int q = threadIdx.x; q < c.swap_last - c.swap_first; q += blockDim.x) {
             rows.idx[q] = a.period_index[c.swap_first + q];
@@ -290,24 +290,27 @@ __global__ void __launch_bounds__(kProdThreads, sizeof(TS) == 4 ? 3 : 1) bermuda
         }
         __syncthreads();
         const float nfac = nfac_s;
-        Sum2 g[kGram];
 #pragma unroll
-        for (int k = 0; k < kGram; k++) g[k] = Sum2{0.0f, 0.0f};
+        for (int k = 0; k < kGram; k++) acc[k] = 0.0;
         float* bb = reinterpret_cast<float*>(a.basis_buf) + (size_t)e * 5 * a.P;
         for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.P; p += gridDim.x * blockDim.x) {
-            float B[5];
-            bermudan_basis32(a, c, p, B, &rows, nfac);
+            float B32[5];
+            bermudan_basis32(a, c, p, B32, &rows, nfac);
+            double B[5];
 #pragma unroll
-            for (int i = 0; i < 5; i++) bb[(size_t)i * a.P + p] = B[i];
+            for (int i = 0; i < 5; i++) {
+                bb[(size_t)i * a.P + p] = B32[i];
+                B[i] = f32_to_f64_int(B32[i]);  // exact, in integer operations
+            }
 #pragma unroll
-            for (int i = 0; i < 5; i++) sum2_add(g[i], B[i]);
+            for (int i = 0; i < 5; i++) acc[i] = acc[i] + B[i];
             int k = 5;
 #pragma unroll
             for (int i = 0; i < 5; i++)
 #pragma unroll
-                for (int j = i; j < 5; j++) dot2_add(g[k++], B[i], B[j]);
+                for (int j = i; j < 5; j++, k++) acc[k] = fma(B[i], B[j], acc[k]);  // the product is exact in FP64
         }
-        block_sums_sum2<kGram>(g, partials + ((size_t)e * gridDim.x + blockIdx.x) * kGram * 2, 1);
+        block_sums_warp_plain<kGram>(acc, partials + ((size_t)e * gridDim.x + blockIdx.x) * kGram * 2, 1);
         return;
     }
 #pragma unroll
@@ -454,25 +457,20 @@ __device__ void regression_solve(const double* partials, int blocks, int P, cons
     }
 }
 
-// Mixed form: the same solve from block partials that are FP32 Sum2 pairs, merged in FP32
-// (block order within a lane, then tree order across the lanes) before the FP64 apply, and
-// the coefficients stored as FP32 pairs.
-__device__ void regression_solve_mixed(const float* partials, int blocks, int P, const double* svd, double* beta_out)
+// Mixed form: the same solve, the coefficients stored as FP32 pairs (hi, lo) for the
+// Dot2 conditional expectation of the next step.
+__device__ void regression_solve_mixed(const double* partials, int blocks, int P, const double* svd, double* beta_out)
 {
     __shared__ double b[kRhs];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (warp < kRhs) {
-        Sum2 acc{0.0f, 0.0f};
+        dd acc{0.0, 0.0};
         for (int k = lane; k < blocks; k += 32) {
-            const float* q = partials + ((size_t)k * kRhs + warp) * 2;
-            acc = sum2_merge(acc, Sum2{q[0], q[1]});
+            const double* q = partials + ((size_t)k * kRhs + warp) * 2;
+            acc = dd_add(acc, dd{q[0], q[1]});
         }
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            const Sum2 y{__shfl_down_sync(0xffffffffu, acc.p, off), __shfl_down_sync(0xffffffffu, acc.s, off)};
-            acc = sum2_merge(acc, y);
-        }
-        if (lane == 0) b[warp] = sum2_value(acc) / (double)P;
+        acc = warp_dd_sum(acc);
+        if (lane == 0) b[warp] = (acc.hi + acc.lo) / (double)P;
     }
     __syncthreads();
     if (threadIdx.x < 6) {
@@ -485,8 +483,8 @@ __device__ void regression_solve_mixed(const float* partials, int blocks, int P,
         for (int j = 0; j < 6; j++) {
             if (!(s[j] > tol)) continue;
             double utb = 0.0;
-            for (int r = 0; r < 6; r++) utb += U[r * 6 + j] * b[r];
-            acc += V[i * 6 + j] * (utb / s[j]);
+            for (int r = 0; r < 6; r++) utb = fma(U[r * 6 + j], b[r], utb);
+            acc = fma(V[i * 6 + j], utb / s[j], acc);
         }
         float hi, lo;
         split_double(acc, hi, lo);
@@ -524,7 +522,7 @@ __device__ void finish_date_last_block(const BermStepParams& a, bool mixed)
     __syncthreads();
     if (last) {
         __threadfence();
-        if (mixed) regression_solve_mixed(reinterpret_cast<const float*>(a.partials), gridDim.x, a.sh.P, a.svd_cur, a.beta_cur);
+        if (mixed) regression_solve_mixed(a.partials, gridDim.x, a.sh.P, a.svd_cur, a.beta_cur);
         else regression_solve(a.partials, gridDim.x, a.sh.P, a.svd_cur, a.beta_cur);
         if (threadIdx.x == 0) *done = 0u;  // ready for the next date
     }
@@ -600,9 +598,9 @@ __global__ void __launch_bounds__(kProdThreads) bermudan_step_kernel(const BermS
 }
 
 // Mixed form: the same backward induction with FP32 path values (continuation v and
-// underlying u, kept as two FP32 arrays in the under buffer), FP32 payoffs, the FP32
-// basis, and the conditional expectation and X^T y sums in twice FP32 precision
-// (Dot2).  Payoffs are not scaled by 1/P (the reference's weight, which cancels in the
+// underlying u, kept as two FP32 arrays in the under buffer), FP32 payoffs and the FP32
+// basis; the X^T y sums in FP64 (the products of FP32 values exact), the conditional
+// expectation X beta in twice FP32 precision (Dot2).  Payoffs are not scaled by 1/P (the reference's weight, which cancels in the
 // final value and scales X^T y and beta alike, leaving the exercise decisions unchanged).
 // Only the final values are written in FP64.
 __global__ void __launch_bounds__(kProdThreads) bermudan_step_mixed_kernel(const BermStepParams a)
@@ -611,9 +609,9 @@ __global__ void __launch_bounds__(kProdThreads) bermudan_step_mixed_kernel(const
     const int P = sh.P;
     float* v32 = reinterpret_cast<float*>(a.under);
     float* u32 = v32 + P;
-    Sum2 acc[kRhs];
+    double acc[kRhs];
 #pragma unroll
-    for (int i = 0; i < kRhs; i++) acc[i] = Sum2{0.0f, 0.0f};
+    for (int i = 0; i < kRhs; i++) acc[i] = 0.0;
     float bh[6], bl[6];
     const float* bprev = nullptr;
     if (a.pending_ex >= 0) {
@@ -688,10 +686,10 @@ __global__ void __launch_bounds__(kProdThreads) bermudan_step_mixed_kernel(const
             if (sh.callable) u = u + payoff;
             else v = v + payoff;
             if (bcur) {
-                const float y = v - u;
-                sum2_add(acc[0], y);
+                const double y = f32_to_f64_int(v - u);  // widened in integer operations
+                acc[0] = acc[0] + y;
 #pragma unroll
-                for (int i = 0; i < 5; i++) dot2_add(acc[1 + i], y, bcur[(size_t)i * P + p]);
+                for (int i = 0; i < 5; i++) acc[1 + i] = fma(y, f32_to_f64_int(bcur[(size_t)i * P + p]), acc[1 + i]);
             }
             v32[p] = v;
             u32[p] = u;
@@ -700,7 +698,7 @@ __global__ void __launch_bounds__(kProdThreads) bermudan_step_mixed_kernel(const
         }
     }
     if (bcur) {
-        block_sums_sum2<kRhs, float>(acc, reinterpret_cast<float*>(a.partials) + (size_t)blockIdx.x * kRhs * 2, 1);
+        block_sums_warp_plain<kRhs>(acc, a.partials + (size_t)blockIdx.x * kRhs * 2, 1);
         finish_date_last_block(a, true);
     }
 }

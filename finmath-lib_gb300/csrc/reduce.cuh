@@ -106,35 +106,4 @@ __device__ __forceinline__ void block_sums_warp_plain(const double (&v)[NV], dou
     }
 }
 
-// Block sums of NV Sum2 partials per thread (mixed-precision form) with no FP64 arithmetic:
-// the pairs are merged exactly in FP32 across the lanes (tree order) and then the warps
-// (warp order); thread i < NV writes sum i as the unnormalised pair (p, s) to out + 2 (i *
-// stride): widened to FP64 for compensated FP64 block-order sums downstream, or kept as
-// FP32 for Sum2 merges downstream.
-// All threads must call it.
-template <int NV, typename OutT = double>
-__device__ __forceinline__ void block_sums_sum2(const Sum2 (&v)[NV], OutT* out, int stride)
-{
-    __shared__ Sum2 ws[32][NV];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int nwarps = (blockDim.x + 31) >> 5;
-#pragma unroll
-    for (int i = 0; i < NV; i++) {
-        Sum2 x = v[i];
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            const Sum2 y{__shfl_down_sync(0xffffffffu, x.p, off), __shfl_down_sync(0xffffffffu, x.s, off)};
-            x = sum2_merge(x, y);
-        }
-        if (lane == 0) ws[warp][i] = x;
-    }
-    __syncthreads();
-    if (threadIdx.x < NV) {
-        Sum2 acc = ws[0][threadIdx.x];
-        for (int w = 1; w < nwarps; w++) acc = sum2_merge(acc, ws[w][threadIdx.x]);
-        out[2 * (size_t)threadIdx.x * stride] = (OutT)acc.p;
-        out[2 * (size_t)threadIdx.x * stride + 1] = (OutT)acc.s;
-    }
-}
-
 }  // namespace lmm
