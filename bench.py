@@ -283,17 +283,21 @@ def run_ours(args):
                 "peak_source": "FP64 FMA rate measured live by the library's DFMA probe (x2 flops); "
                                "MEASURED_PEAKS.json holds no FP64 figure",
                 "component_steps_per_path": comp_steps,
-                "transcendentals_per_launch": {"log": P * comp_steps, "exp": P * comp_steps, "div": P * comp_steps},
+                "transcendentals_per_launch": {"exp_small": P * comp_steps, "rcp_newton": P * comp_steps},
                 "ncu_fp64_pipe_active": _from_profile("fp64_pipe_active") if prec == F.PRECISION_FP64 else None,
-                "note": "algorithmic flops count add/mul only; each component-step also takes one log, one exp "
-                        "and one correctly rounded reciprocal in the reference's order, which keep the FP64 "
-                        "pipe ~83 % busy (ncu, profiles/lmm_paths_fp64_lmm40.md)"}
+                "note": "algorithmic flops count the reference algorithm's add/mul per component-step (its "
+                        "log, exp and division as one each); the FP64 kernel fuses them into FMAs, evaluates "
+                        "the log-Euler step as L exp(d) with a table-driven 12-FMA exp and replaces the "
+                        "division by a 4-FMA Newton reciprocal, and is FP64-pipe bound "
+                        "(ncu, profiles/lmm_paths_fp64_lmm40.md)"}
 
     # ---------------- end to end through the C ABI with host buffers (tables in, prices out)
     e2e_times = []
     h2d = d2h = 0
     for i in range(args.steps + 1):
         torch.cuda.synchronize()
+        h2d0 = ctypes.c_int64()
+        L.lmm_stats_h2d_bytes(ctypes.byref(h2d0))
         t0 = time.perf_counter()
         s2 = W.build(cfg, paths=P, precision=prec)
         b2 = berm.getValues(s2)
@@ -304,9 +308,11 @@ def run_ours(args):
         if i > 0:
             e2e_times.append(time.perf_counter() - t0)
         if i == 0:
-            cov = s2.process.model.covarianceModel
-            h2d = (cov.factorLoadings.nbytes + cov.variance.nbytes + 8 * (2 * (T + 1) + 4 * (N + 1))
-                   + 624 * 4 + 9 * 312 * 8 + 3 * 64 * 8)
+            # every host-to-device copy the library made during the valuation (tables, the
+            # seeded state, the generator's jump lists, product schedules), as it counts them
+            h2d1 = ctypes.c_int64()
+            L.lmm_stats_h2d_bytes(ctypes.byref(h2d1))
+            h2d = int(h2d1.value - h2d0.value)
             d2h = 4 * 16
     e2e_ms = 1e3 * statistics.mean(e2e_times)
     if dist is not None:

@@ -54,6 +54,9 @@ static double g_total_ms[K_COUNT];
 
 bool timing_enabled() { return g_timing.load(); }
 
+static std::atomic<int64_t> g_h2d_bytes{0};
+void count_h2d(size_t bytes) { g_h2d_bytes += (int64_t)bytes; }
+
 KernelTimer::KernelTimer(int id_, cudaStream_t s, int launches) : id(id_), stream(s)
 {
     g_launches[id] += launches;
@@ -129,6 +132,7 @@ static int upload(T** d, const T* h, size_t count, cudaStream_t s)
     int rc = dalloc(d, count, s);
     if (rc) return rc;
     if (count) LMM_CUDA(cudaMemcpyAsync(*d, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+    count_h2d(count * sizeof(T));
     return LMM_OK;
 }
 
@@ -264,6 +268,7 @@ static int brownian_ensure(lmm_brownian* b)
     for (int t = 0; t < b->T; t++) sq[t] = std::sqrt(b->times[t + 1] - b->times[t]);
     if (!b->d_seeded && (rc = dalloc(&b->d_seeded, kMtN, b->stream))) return rc;
     LMM_CUDA(cudaMemcpyAsync(b->d_seeded, seeded, sizeof(seeded), cudaMemcpyHostToDevice, b->stream));
+    count_h2d(sizeof(seeded));
     if (!b->d_jumps && (rc = upload(&b->d_jumps, b->plan.polys.data(), b->plan.polys.size(), b->stream))) return rc;
     if (!b->d_sqrt_dt && (rc = upload(&b->d_sqrt_dt, sq.data(), sq.size(), b->stream))) return rc;
     if (b->precision == LMM_PRECISION_MIXED && !b->d_sqrt_dt32) {
@@ -909,6 +914,7 @@ static int bermudan_run(lmm_process* pr, const lmm_bermudan_desc* d, double* val
     LMM_CUDA(cudaMemcpyAsync(pr->d_period_length, plen.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
     LMM_CUDA(cudaMemcpyAsync(pr->d_period_index, pidx.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
     LMM_CUDA(cudaMemcpyAsync(pr->d_tenor_delta, tdelta.data(), sizeof(double) * pr->N, cudaMemcpyHostToDevice, s));
+    count_h2d(sizeof(double) * (size_t)n + sizeof(int) * (size_t)n + sizeof(double) * (size_t)pr->N);
     BermudanScratch sc;
     sc.d_values = pr->d_values;
     sc.d_under = pr->d_under;
@@ -1101,6 +1107,13 @@ int lmm_bermudan_get_gradient(lmm_process* pr, const lmm_bermudan_desc* d, int s
 int lmm_stats_enable_timing(int enable)
 {
     g_timing.store(enable != 0);
+    return LMM_OK;
+}
+
+int lmm_stats_h2d_bytes(int64_t* out)
+{
+    if (!out) return lmm::fail(LMM_ERR_INVALID, "null argument");
+    *out = lmm::g_h2d_bytes.load();
     return LMM_OK;
 }
 

@@ -9,9 +9,10 @@
 // into a fused multiply-add (a contraction would break the exactness these steps rely on
 // in translation units built with FMA contraction on).
 //
-// The mixed-precision form uses these where its sums need FP64-class accuracy (the
-// regression's Gram matrix and X^T y, the conditional expectation X beta) but FP64 would
-// cost the GB300's narrow FP64 pipe: a Dot2 term is nine FP32 operations.  The operations
+// The mixed-precision form uses these where a value needs more than FP32 accuracy but FP64
+// would cost the GB300's narrow FP64 pipe (a Dot2 term is nine FP32 operations): the
+// conditional expectation X beta of the backward induction and the adjoint seeds' per-date
+// cash-flow sums.  The regression's Gram and X^T y sums stay FP64.  The operations
 // below must not be reassociated; nvcc does not reassociate FP32 arithmetic, and the one
 // product that has to be fused is an explicit fmaf.
 #pragma once

@@ -50,6 +50,8 @@ struct KernelTimer {
     cudaEvent_t start = nullptr;
 };
 bool timing_enabled();
+// host-to-device bytes copied by the library (every table and parameter upload)
+void count_h2d(size_t bytes);
 
 // ---------------------------------------------------------------- MT19937 (host side)
 constexpr int kMtN = 624;

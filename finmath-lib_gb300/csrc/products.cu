@@ -842,6 +842,7 @@ int launch_bermudan(const ProductView& v, const BermudanLaunch& a, const Bermuda
     if (!sc.tables_on_device) {
         LMM_CUDA(cudaMemcpyAsync(sc.d_per, a.per.data(), sizeof(BermudanPeriod) * a.nper, cudaMemcpyHostToDevice, s));
         if (ne) LMM_CUDA(cudaMemcpyAsync(sc.d_ex_period, ex_period.data(), sizeof(int) * ne, cudaMemcpyHostToDevice, s));
+        count_h2d(sizeof(BermudanPeriod) * (size_t)a.nper + sizeof(int) * (size_t)ne);
     }
     BermShared sh;
     std::memset(&sh, 0, sizeof(sh));

@@ -282,6 +282,9 @@ int lmm_stats_enable_timing(int enable);
 int lmm_stats_reset(void);
 /* Fills names[i] (static strings), launches[i], total_ms[i] for up to max entries; returns the count. */
 int lmm_stats_get(int max, const char** names, int64_t* launches, double* total_ms);
+/* Bytes this library has copied from host to device since it was loaded (tables, states,
+ * parameters): the difference across a call is that call's host-to-device traffic. */
+int lmm_stats_h2d_bytes(int64_t* out);
 /* The CUDA stream (as an opaque pointer) on which a process enqueues its work. */
 int lmm_process_stream(lmm_process* proc, void** out_stream);
 /* A FP64 fused-multiply-add throughput probe (DFMA/s), used to report the FP64 roofline. */
