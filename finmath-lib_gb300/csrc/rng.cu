@@ -15,8 +15,11 @@
 // increments leave through a shared-memory tile (increments_loop) so that each [t][f] row
 // is written in 128-byte segments although the stream runs path-major.
 //
-// This translation unit is compiled with -fmad=false: the FP64 inverse normal must
-// round exactly like the reference's unfused Java arithmetic.
+// This translation unit is compiled with -fmad=false.  The FP64 inverse normal, which the
+// GPU's narrow FP64 pipe bounds, evaluates the reference's rational functions with fused
+// Horner steps and a Newton quotient (within a few ulp of the reference's normals; the
+// uniforms stay bit-exact).
+#include "fp64math.cuh"
 #include "lmm_internal.h"
 
 #include <cmath>
@@ -76,63 +79,91 @@ __device__ __forceinline__ uint32_t mt_next(uint32_t x_m, uint32_t x_0, uint32_t
 }
 
 // NormalDistribution.inverseCumulativeNormalDistributionWichura (functions/NormalDistribution.java:67-162),
-// AS241 (Wichura 1988) with the reference's evaluation order.  The central branch
-// (|p - 0.5| <= 0.425, ~85 % of draws) and the tails are separate functions so that the
-// generator can run each on a compacted set of lanes.
-__device__ __forceinline__ double icdf_central(double q)
+// AS241 (Wichura 1988): the reference's coefficients and branches, evaluated with fused
+// Horner steps.  The central branch (|p - 0.5| <= 0.425, ~85 % of draws) and the tails are
+// separate functions so that the generator can run each on a compacted set of lanes.
+// The central branch for q = dq 2^-52 (|q| <= 0.425): q converted in integer operations,
+// the two degree-7 polynomials by fused Horner steps, and q num / den as the Newton
+// reciprocal of den (den >= 1 on the branch) times q num, corrected once by the residual
+// q num - den y.  About 23 FP64 instructions instead of 43.
+__device__ __forceinline__ double icdf_central(int64_t dq)
 {
-    const double r = 0.180625 - q * q;
-    const double num = (((((((2.5090809287301226727e+03 * r + 3.3430575583588128105e+04) * r +
-                             6.7265770927008700853e+04) * r + 4.5921953931549871457e+04) * r +
-                           1.3731693765509461125e+04) * r + 1.9715909503065514427e+03) * r +
-                         1.3314166789178437745e+02) * r + 3.3871328727963666080e+00);
-    const double den = (((((((5.2264952788528545610e+03 * r + 2.8729085735721942674e+04) * r +
-                             3.9307895800092710610e+04) * r + 2.1213794301586595867e+04) * r +
-                           5.3941960214247511077e+03) * r + 6.8718700749205790830e+02) * r +
-                         4.2313330701600911252e+01) * r + 1.0);
-    return q * num / den;
+    double q = 0.0;
+    if (dq != 0) {
+        // |dq| < 2^51: exact as a double; exponent from the leading bit, scaled by 2^-52
+        const unsigned long long m = (unsigned long long)(dq < 0 ? -dq : dq);
+        const int lead = 63 - __clzll((long long)m);  // m in [2^lead, 2^(lead+1))
+        const unsigned long long frac = (m << (52 - lead)) & 0xfffffffffffffull;
+        const unsigned long long bits = (dq < 0 ? 0x8000000000000000ull : 0ull) |
+                                        ((unsigned long long)(1023 + lead - 52) << 52) | frac;
+        q = __longlong_as_double((long long)bits);
+    }
+    const double r = fma(-q, q, 0.180625);
+    double num = 2.5090809287301226727e+03;
+    num = fma(num, r, 3.3430575583588128105e+04);
+    num = fma(num, r, 6.7265770927008700853e+04);
+    num = fma(num, r, 4.5921953931549871457e+04);
+    num = fma(num, r, 1.3731693765509461125e+04);
+    num = fma(num, r, 1.9715909503065514427e+03);
+    num = fma(num, r, 1.3314166789178437745e+02);
+    num = fma(num, r, 3.3871328727963666080e+00);
+    double den = 5.2264952788528545610e+03;
+    den = fma(den, r, 2.8729085735721942674e+04);
+    den = fma(den, r, 3.9307895800092710610e+04);
+    den = fma(den, r, 2.1213794301586595867e+04);
+    den = fma(den, r, 5.3941960214247511077e+03);
+    den = fma(den, r, 6.8718700749205790830e+02);
+    den = fma(den, r, 4.2313330701600911252e+01);
+    den = fma(den, r, 1.0);
+    const double n = q * num;
+    const double rd = rcp_newton(den);
+    const double y = n * rd;
+    return fma(rd, fma(-den, y, n), y);
 }
 
-__device__ double icdf_wichura(double p)
+// c[0] r^7 + ... + c[7] by fused Horner steps
+__device__ __forceinline__ double horner8d(double r, const double (&c)[8])
 {
+    double v = c[0];
+#pragma unroll
+    for (int i = 1; i < 8; i++) v = fma(v, r, c[i]);
+    return v;
+}
+
+// The tail branch (|p - 1/2| > 0.425, the draws the central test rejected) of the same
+// transform: CUDA's log and sqrt, the rational functions by fused Horner steps and a
+// Newton quotient (the denominators are >= 1 on their branches).
+__device__ double icdf_tail(double p)
+{
+    constexpr double c[8] = {7.74545014278341407640e-04, 2.27238449892691845833e-02, 2.41780725177450611770e-01,
+                             1.27045825245236838258e+00, 3.64784832476320460504e+00, 5.76949722146069140550e+00,
+                             4.63033784615654529590e+00, 1.42343711074968357734e+00};
+    constexpr double d[8] = {1.05075007164441684324e-09, 5.47593808499534494600e-04, 1.51986665636164571966e-02,
+                             1.48103976427480074590e-01, 6.89767334985100004550e-01, 1.67638483018380384940e+00,
+                             2.05319162663775882187e+00, 1.0};
+    constexpr double e[8] = {2.01033439929228813265e-07, 2.71155556874348757815e-05, 1.24266094738807843860e-03,
+                             2.65321895265761230930e-02, 2.96560571828504891230e-01, 1.78482653991729133580e+00,
+                             5.46378491116411436990e+00, 6.65790464350110377720e+00};
+    constexpr double f[8] = {2.04426310338993978564e-15, 1.42151175831644588870e-07, 1.84631831751005468180e-05,
+                             7.86869131145613259100e-04, 1.48753612908506148525e-02, 1.36929880922735805310e-01,
+                             5.99832206555887937690e-01, 1.0};
     const double q = p - 0.5;
-    if (fabs(q) <= 0.425) {
-        const double r = 0.180625 - q * q;
-        const double num = (((((((2.5090809287301226727e+03 * r + 3.3430575583588128105e+04) * r +
-                                 6.7265770927008700853e+04) * r + 4.5921953931549871457e+04) * r +
-                               1.3731693765509461125e+04) * r + 1.9715909503065514427e+03) * r +
-                             1.3314166789178437745e+02) * r + 3.3871328727963666080e+00);
-        const double den = (((((((5.2264952788528545610e+03 * r + 2.8729085735721942674e+04) * r +
-                                 3.9307895800092710610e+04) * r + 2.1213794301586595867e+04) * r +
-                               5.3941960214247511077e+03) * r + 6.8718700749205790830e+02) * r +
-                             4.2313330701600911252e+01) * r + 1.0);
-        return q * num / den;
-    }
     double r = (q < 0.0) ? p : 1.0 - p;
     if (r <= 0.0) return 0.0;
     r = sqrt(-log(r));
-    double v;
+    double num, den;
     if (r <= 5.0) {
         r -= 1.6;
-        v = (((((((7.74545014278341407640e-04 * r + 2.27238449892691845833e-02) * r +
-                  2.41780725177450611770e-01) * r + 1.27045825245236838258e+00) * r +
-                3.64784832476320460504e+00) * r + 5.76949722146069140550e+00) * r +
-              4.63033784615654529590e+00) * r + 1.42343711074968357734e+00) /
-            (((((((1.05075007164441684324e-09 * r + 5.47593808499534494600e-04) * r +
-                  1.51986665636164571966e-02) * r + 1.48103976427480074590e-01) * r +
-                6.89767334985100004550e-01) * r + 1.67638483018380384940e+00) * r +
-              2.05319162663775882187e+00) * r + 1.0);
+        num = horner8d(r, c);
+        den = horner8d(r, d);
     } else {
         r -= 5.0;
-        v = (((((((2.01033439929228813265e-07 * r + 2.71155556874348757815e-05) * r +
-                  1.24266094738807843860e-03) * r + 2.65321895265761230930e-02) * r +
-                2.96560571828504891230e-01) * r + 1.78482653991729133580e+00) * r +
-              5.46378491116411436990e+00) * r + 6.65790464350110377720e+00) /
-            (((((((2.04426310338993978564e-15 * r + 1.42151175831644588870e-07) * r +
-                  1.84631831751005468180e-05) * r + 7.86869131145613259100e-04) * r +
-                1.48753612908506148525e-02) * r + 1.36929880922735805310e-01) * r +
-              5.99832206555887937690e-01) * r + 1.0);
+        num = horner8d(r, e);
+        den = horner8d(r, f);
     }
+    const double rd = rcp_newton(den);
+    const double y = num * rd;
+    const double v = fma(rd, fma(-den, y, num), y);
     return (q < 0.0) ? -v : v;
 }
 
@@ -289,7 +320,7 @@ __device__ __forceinline__ void increments_loop(const RngParams& prm, uint32_t* 
                 const int64_t dq = m - ((int64_t)1 << 51);
                 central = (dq < 0 ? -dq : dq) <= prm.central_max;
                 if (central) {
-                    hv0 = icdf_central((double)dq * 0x1.0p-52) * __ldg(prm.sqrt_dt + st);
+                    hv0 = icdf_central(dq) * __ldg(prm.sqrt_dt + st);
                 } else {
                     const int slot = atomicAdd(tail_n, 1);
                     tail_w[slot] = (unsigned long long)m;
@@ -326,7 +357,7 @@ __device__ __forceinline__ void increments_loop(const RngParams& prm, uint32_t* 
             divmod_u32((uint32_t)pos.y, (uint32_t)F, prm.magic_f, t, k);
             OutT val;
             if constexpr (kExact) {
-                val = icdf_wichura((double)(int64_t)w * 0x1.0p-52) * __ldg(prm.sqrt_dt + t);
+                val = icdf_tail((double)(int64_t)w * 0x1.0p-52) * __ldg(prm.sqrt_dt + t);
             } else {
                 const uint32_t hi = (uint32_t)(w >> 32), lo = (uint32_t)w;
                 const bool lower = hi < (1u << 25);

@@ -36,7 +36,8 @@ def test_brownian_increments_fp64(P, T, Fk):
             g = bm.getBrownianIncrement(t, k)
             r = ref[t, k]
             worst = max(worst, float(np.max(np.abs(g - r) / np.maximum(np.abs(r), 1e-300))))
-    # central branch is unfused +,*,/ (bit-identical); tails go through log (CUDA vs libm, <= a few ulp)
+    # the GPU evaluates the same rational functions with fused Horner steps and a Newton
+    # quotient, tails through CUDA's log: a few ulp from the reference's unfused order
     assert worst <= 4e-15
 
 
