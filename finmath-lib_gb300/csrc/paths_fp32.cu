@@ -114,18 +114,18 @@ __global__ void __launch_bounds__(kPathThreads, NMAX <= 40 ? 4 : 2) paths_fp32_k
         const float dt = __ldg(a.d_dt32 + i);
         cp_async_wait();
         __syncwarp();  // the warp's staged table of step i is visible to every lane
-        float2 dw2[FH];
+        // G_k = dW_k + dt S_k, the drift's running sum S_k = sum_{l<=j} os_l lambda_lk carried
+        // with dt and the increments: the step increment of component j is
+        // sum_k G_k lambda_jk - dt variance_j / 2 (two paired FMAs per factor pair, not three)
+        float2 G2[FH];
 #pragma unroll
         for (int m = 0; m < FH; m++) {
             const int k0 = 2 * m, k1 = 2 * m + 1;
-            dw2[m].x = (k0 < F && active) ? sm.dw[i & 1][k0][tid] : 0.0f;
-            dw2[m].y = (k1 < F && k1 < FMAX && active) ? sm.dw[i & 1][k1 < FMAX ? k1 : 0][tid] : 0.0f;
+            G2[m].x = (k0 < F && active) ? sm.dw[i & 1][k0][tid] : 0.0f;
+            G2[m].y = (k1 < F && k1 < FMAX && active) ? sm.dw[i & 1][k1 < FMAX ? k1 : 0][tid] : 0.0f;
         }
         if (i + 1 < a.T) prefetch(i + 1);  // buffers (i+1)&1 were last read in step i-1
         const float* tb = sm.table[warp][i & 1];
-        float2 S2[FH];
-#pragma unroll
-        for (int m = 0; m < FH; m++) S2[m] = make_float2(0.0f, 0.0f);
         for_up_from<NMAX>(first, [&](auto jc) {
             constexpr int j = decltype(jc)::value;
             if (j < N) {
@@ -139,19 +139,17 @@ __global__ void __launch_bounds__(kPathThreads, NMAX <= 40 ? 4 : 2) paths_fp32_k
                     lr[4 * q + 3] = v.w;
                 }
                 const float invd = __ldg(a.d_inv_delta32 + j);
-                const float os = __fdividef(L[j], L[j] + invd);
-                const float2 os2 = make_float2(os, os);
-                float2 mu2 = make_float2(-0.5f * tb[NMAX * FP + j], 0.0f);
-                float2 df2 = make_float2(0.0f, 0.0f);
+                const float osdt = __fdividef(L[j], L[j] + invd) * dt;
+                const float2 os2 = make_float2(osdt, osdt);
+                float2 d2 = make_float2(-0.5f * tb[NMAX * FP + j] * dt, 0.0f);
 #pragma unroll
                 for (int m = 0; m < FH; m++) {
                     // factors 2m and 2m+1 (the rows are zero padded beyond F)
                     const float2 l2 = make_float2(lr[2 * m], lr[2 * m + 1]);
-                    S2[m] = __ffma2_rn(os2, l2, S2[m]);
-                    mu2 = __ffma2_rn(S2[m], l2, mu2);
-                    df2 = __ffma2_rn(dw2[m], l2, df2);
+                    G2[m] = __ffma2_rn(os2, l2, G2[m]);
+                    d2 = __ffma2_rn(G2[m], l2, d2);
                 }
-                Y[j] = Y[j] + fmaf(mu2.x + mu2.y, dt, df2.x + df2.y);
+                Y[j] = Y[j] + (d2.x + d2.y);
                 float v = __expf(Y[j]);
                 if (CAPPED && v > cap) v = cap;
                 L[j] = v;

@@ -16,7 +16,8 @@
 // Compiled with -fmad=false.  The GPU's narrow FP64 pipe bounds the fast kernel, so it
 // spends fewer FP64 instructions than the reference's literal arithmetic, all in FP64:
 //  * the drift's and the Euler step's multiply-adds are fused FP64 FMAs (each rounds once
-//    instead of twice);
+//    instead of twice), and the drift's running sums S_k carry dt and the increments dW_k
+//    along (G_k = dW_k + dt S_k), so that a component costs 2F FMAs instead of 3F;
 //  * the Euler-log step exp(log L + d) (EULER_FUNCTIONAL) is evaluated as L exp(d), and the
 //    EULER step exp(Y + d) as exp(Y) exp(d) with exp(Y) carried instead of Y, where exp(d)
 //    of the small step increment d is exp_small (fp64math.cuh) -- no log, and a 12-FMA exp;
@@ -92,9 +93,13 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp64_kernel(const PathLaun
         double dw[FMAX];
 #pragma unroll
         for (int k = 0; k < FMAX; k++) dw[k] = (k < F && active) ? dW[((size_t)i * F + k) * P + p] : 0.0;
-        double S[FMAX];
+        // G_k = dW_k + dt S_k with the drift's running sum S_k = sum_{l<=j} os_l lambda_lk
+        // (:1156-1158): the step increment of component j is then
+        //   d_j = mu_j dt + sum_k dW_k lambda_jk = sum_k G_k lambda_jk - dt variance_j / 2,
+        // two fused multiply-adds per factor instead of three
+        double G[FMAX];
 #pragma unroll
-        for (int k = 0; k < FMAX; k++) S[k] = 0.0;
+        for (int k = 0; k < FMAX; k++) G[k] = dw[k];
 #pragma unroll
         for (int j = 0; j < NMAX; j++) {
             if (j < N && j >= first) {
@@ -102,26 +107,22 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp64_kernel(const PathLaun
                 // Scalar(delta).discount(L, delta) = 1/(L*(delta/delta) + 1/delta) (stochastic/Scalar.java:321-328),
                 // times L (:1149-1153); delta/delta is exactly 1.0 and 1/delta is precomputed.
                 const double os = rcp_newton(Lj + __ldg(a.d_inv_delta + j)) * Lj;
-                double mu = 0.0;
+                const double osdt = os * dt;
                 double lj[FMAX];
 #pragma unroll
                 for (int k = 0; k < FMAX; k++) {
                     if (k < F) {
                         lj[k] = __ldg(lam + j * F + k);
-                        S[k] = fma(os, lj[k], S[k]);  // :1156-1158
+                        G[k] = fma(osdt, lj[k], G[k]);
                     }
                 }
+                // Euler step (EulerSchemeFromProcessModel.java:235-255) with the drift of
+                // :1159 and :1183-1189 (variance * -0.5): the increment d of the log state,
+                // then L exp(d) (FUNCTIONAL: log L is the state) or exp(Y) exp(d) (EULER)
+                double d = __ldg(var_half + j) * dt;
 #pragma unroll
                 for (int k = 0; k < FMAX; k++)
-                    if (k < F) mu = fma(S[k], lj[k], mu);  // :1159 (addSumProduct, left to right)
-                mu = mu + __ldg(var_half + j);              // :1183-1189, variance * -0.5
-                // Euler step (EulerSchemeFromProcessModel.java:235-255): the increment d of
-                // the log state, then L exp(d) (FUNCTIONAL: log L is the state) or
-                // exp(Y) exp(d) (EULER)
-                double d = mu * dt;
-#pragma unroll
-                for (int k = 0; k < FMAX; k++)
-                    if (k < F) d = fma(dw[k], lj[k], d);
+                    if (k < F) d = fma(G[k], lj[k], d);
                 const double g = exp_small(d, etab);
                 if (FUNCTIONAL) {
                     L[j] = cap_positive(Lj * g, capbits);
