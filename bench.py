@@ -343,6 +343,7 @@ def run_ours(args):
                                                ms - stats["mt19937_jump_generate"][1] / max(args.steps, 1))}
         if not args.no_portfolio:
             line["forms"]["portfolio"] = portfolio_form(args, F, W, cfg, P)
+        line["forms"]["random_variable"] = random_variable_form(args, F, W, cfg, P)
     if rank == 0 and not args.no_cpu_baseline:
         v, dt, _, _ = cpu_baseline(args.cpu_paths, os.cpu_count() or 1)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
@@ -499,6 +500,63 @@ def greeks_form(args, F, W, cfg, P, T, berm, fp64_valuation_ms):
     out["fd_check"] = fd_check(F, W, cfg, P, berm, grads)
     out["note"] = ("bump-and-revalue estimate = (2 x (deltas + nonzero vegas) + 1) x the measured FP64 valuation; "
                    "delta differences are price bp per 1 bp of forward, vega differences price bp per 1 vol point")
+    return out
+
+
+def random_variable_form(args, F, W, cfg, P, n=1 << 26):
+    """The device RandomVariable layer (include/lmm_rv.h): streaming elementwise operations
+    and a reduction at n = 2^26 realizations (512 MB per operand, above L2), against the
+    measured HBM copy bandwidth; and a strip of 40 caplets written against the
+    RandomVariable API on the FP64 lmm40 simulation (Caplet.getValue's operations)."""
+    from finmath_gb300.randomvariable import RandomVariableGPU as RV
+    rng = np.random.default_rng(7)
+    x, y, z = (RV.from_array(0.0, rng.random(n)) for _ in range(3))
+    hbm, _ = _measured_hbm_gbs()
+
+    import torch
+    h = ctypes.c_void_p()
+    F.load().lmm_rv_stream(ctypes.byref(h))
+    stream = torch.cuda.ExternalStream(h.value)
+
+    def timed(fn, nbytes, reps=10):
+        fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        sec = e0.elapsed_time(e1) * 1e-3 / reps
+        return {"ms": sec * 1e3, "gbs": nbytes / sec / 1e9, "hbm_frac": nbytes / sec / 1e9 / hbm}
+
+    out = {"n": n, "unit": "GB/s of algorithmic bytes (8 B per operand read and per value written)",
+           "mult": timed(lambda: x.mult(y).close(), 24 * n),
+           "add_product": timed(lambda: x.addProduct(y, z).close(), 32 * n),
+           "discount": timed(lambda: x.discount(y, 0.5).close(), 24 * n),
+           "exp": timed(lambda: x.exp().close(), 16 * n),
+           "average": timed(lambda: x.getAverage(), 8 * n),
+           "note": "CUDA events on the library stream over 10 operations (each allocates its result from "
+                   "the stream-ordered pool and frees it); discount's correctly rounded division, exp and "
+                   "the compensated average are bound by the GPU's FP64 pipe, not HBM"}
+    for r in (x, y, z):
+        r.close()
+    sim = W.build(cfg, paths=P)
+    period, w = cfg["period"], 1.0 / P
+    N0 = sim.getNumeraireRandomVariable(0.0)  # simulates the paths (lazily, as the reference)
+    N0.getAverage()
+    t0 = time.perf_counter()
+    total = 0.0
+    for j in range(1, 40):
+        t = int(round(j * period / cfg["dt"]))
+        v = sim.getLIBORRandomVariable(t, j).sub(0.04).floor(0.0).mult(period)
+        v = v.div(sim.getNumeraireRandomVariable((j + 1) * period)).mult(w).mult(N0).div(w)
+        total += v.getAverage()
+    out["caplet_strip"] = {"caplets": 39, "paths": P, "ms": 1e3 * (time.perf_counter() - t0), "value_sum": total,
+                           "note": "39 caplets 1y-20y K=4% through getLIBOR/getNumeraire random variables: "
+                                   "7 elementwise operations and one compensated average each, on the simulated paths"}
+    N0.close()
+    sim.process.close()
+    sim.process.brownianMotion.close()
     return out
 
 

@@ -659,6 +659,31 @@ int lmm_process_get_numeraire(lmm_process* pr, double time, double* out)
     return LMM_OK;
 }
 
+int lmm_process_get_value_rv(lmm_process* pr, int t, int j, lmm_rv** out)
+{
+    if (!pr || !out) return fail(LMM_ERR_INVALID, "null argument");
+    if (t < 0 || t > pr->T || j < 0 || j >= pr->N) return fail(LMM_ERR_INVALID, "time index or component out of range");
+    if (pr->obs_slot[t] < 0) return fail(LMM_ERR_STATE, "time index not among the observed times of this process");
+    int rc = process_ensure(pr);
+    if (rc) return rc;
+    const size_t off = ((size_t)pr->obs_slot[t] * pr->N + j) * (size_t)pr->P;
+    const bool fp32 = pr->precision != LMM_PRECISION_FP64;
+    const void* src = fp32 ? (const void*)(static_cast<const float*>(pr->d_states) + off)
+                           : (const void*)(static_cast<const double*>(pr->d_states) + off);
+    return rv_from_device(pr->times[t], src, fp32 ? 1 : 0, pr->P, pr->stream, out);
+}
+
+int lmm_process_get_numeraire_rv(lmm_process* pr, double time, lmm_rv** out)
+{
+    if (!pr || !out) return fail(LMM_ERR_INVALID, "null argument");
+    const int l = time_index(pr->tenor, time);
+    if (l < 0) return fail(LMM_ERR_INVALID, "numeraire requested off the tenor grid");
+    int rc = process_ensure(pr);
+    if (rc) return rc;
+    return rv_numeraire(time, pr->d_numeraire + (size_t)l * pr->P, pr->d_num_adj + l, pr->has_discount ? 1 : 0,
+                        pr->num_det[l], pr->has_discount ? pr->discount[l] : 1.0, pr->P, pr->stream, out);
+}
+
 int lmm_process_destroy(lmm_process* pr)
 {
     if (!pr) return LMM_OK;

@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include "lmm_gb300.h"
+#include "lmm_rv.h"
 
 namespace lmm {
 
@@ -138,6 +139,12 @@ int launch_paths_fp32(const PathLaunch& a, const float* lam32, const float* var3
 int path_blocks(int P);
 // exp(k/64) for k = -64..64, rounded to FP64 from extended precision (the table of exp_small)
 void fp64_exp_table(double out[129]);
+
+// device random variables (randomvariable.cu) from process buffers: a copy (FP32 states
+// widened) or the adjusted numeraire, ordered after the work so far on src_stream
+int rv_from_device(double time, const void* src, int fp32, int64_t n, cudaStream_t src_stream, lmm_rv** out);
+int rv_numeraire(double time, const double* d_num, const double* d_adj, int has_discount, int det, double pd, int64_t n,
+                 cudaStream_t src_stream, lmm_rv** out);
 
 // numeraire adjustment: adj[l] = mean over paths of 1/N_l (or the deterministic value)
 int launch_numeraire_finish(const double* d_partials, int blocks, int N, int P, const double* d_numeraire,

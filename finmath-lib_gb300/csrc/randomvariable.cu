@@ -1,0 +1,563 @@
+// randomvariable.cu -- device random variables (lmm_rv.h): the elementwise algebra of
+// RandomVariableFromDoubleArray (montecarlo/RandomVariableFromDoubleArray.java) on GB300.
+//
+// A random variable is one deterministic value or n FP64 realizations in device memory.
+// Each operation is one streaming kernel over its operands (an HBM-bound pass: 8 bytes read
+// per stochastic operand and 8 written per realization), launched on one library stream.
+// Deterministic operands are broadcast as kernel arguments; an operation whose operands
+// are all deterministic is evaluated on the host with the same formula.  This translation
+// unit is compiled with -fmad=false and the host side with -ffp-contract=off, so that every
+// + - * / rounds separately, as the reference's Java does.
+#include <algorithm>
+#include <cmath>
+#include <mutex>
+#include <vector>
+
+#include "lmm_internal.h"
+#include "lmm_rv.h"
+#include "reduce.cuh"
+
+struct lmm_rv {
+    double time = 0.0;
+    int64_t n = 0;          // 0: deterministic
+    double value = 0.0;     // the deterministic value
+    double* d = nullptr;    // n realizations (device), nullptr when deterministic
+};
+
+namespace lmm {
+namespace {
+
+constexpr int kRvThreads = 256;
+
+cudaStream_t rv_stream()
+{
+    static cudaStream_t s = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] { cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking); });
+    return s;
+}
+
+// Math.min / Math.max: a NaN operand gives NaN, and -0.0 is below +0.0
+__host__ __device__ __forceinline__ double java_min(double a, double b)
+{
+    if (a != a) return a;
+    if (b != b) return b;
+    if (a < b) return a;
+    if (b < a) return b;
+    return signbit(a) ? a : b;
+}
+__host__ __device__ __forceinline__ double java_max(double a, double b)
+{
+    if (a != a) return a;
+    if (b != b) return b;
+    if (a > b) return a;
+    if (b > a) return b;
+    return signbit(a) ? b : a;
+}
+
+// Math.pow where its special cases differ from C's pow: a NaN exponent gives NaN, and
+// |x| = 1 with an infinite exponent gives NaN
+__host__ __device__ __forceinline__ double java_pow(double x, double y)
+{
+    if (y != y) return y;
+    if (fabs(x) == 1.0 && isinf(y)) return y - y;  // NaN
+    return pow(x, y);
+}
+
+// One realization of operation OP; a, b are the operands' realizations (or values), c the
+// double argument, has_b whether b is given (addProduct with a double factor otherwise).
+template <int OP>
+__host__ __device__ __forceinline__ double rv_op(double x, double a, double b, double c, bool has_b)
+{
+    switch (OP) {
+        case LMM_RV_ADD: return x + a;
+        case LMM_RV_SUB: return x - a;
+        case LMM_RV_BUS: return a - x;
+        case LMM_RV_MULT: return x * a;
+        case LMM_RV_DIV: return x / a;
+        case LMM_RV_VID: return a / x;
+        case LMM_RV_CAP: return java_min(x, a);
+        case LMM_RV_FLOOR: return java_max(x, a);
+        case LMM_RV_POW: return java_pow(x, a);
+        case LMM_RV_SQUARED: return x * x;
+        case LMM_RV_SQRT: return sqrt(x);
+        case LMM_RV_EXP: return exp(x);
+        case LMM_RV_LOG: return log(x);
+        case LMM_RV_SIN: return sin(x);
+        case LMM_RV_COS: return cos(x);
+        case LMM_RV_INVERT: return 1.0 / x;
+        case LMM_RV_ABS: return fabs(x);
+        case LMM_RV_ISNAN: return (x != x) ? 1.0 : 0.0;
+        case LMM_RV_EXPM1: return expm1(x);
+        case LMM_RV_ACCRUE: return x * (1 + a * c);
+        case LMM_RV_DISCOUNT: return x / (1.0 + a * c);
+        case LMM_RV_CHOOSE: return x >= 0.0 ? a : b;
+        case LMM_RV_ADD_PRODUCT: return has_b ? x + a * b : x + a * c;
+        case LMM_RV_ADD_RATIO: return x + a / b;
+        case LMM_RV_SUB_RATIO: return x - a / b;
+        default: return x;
+    }
+}
+
+struct Operand {
+    const double* p;  // realizations, or nullptr for the value v
+    double v;
+};
+
+__device__ __forceinline__ double load(const Operand& o, int64_t i) { return o.p ? __ldg(o.p + i) : o.v; }
+
+// Four independent elements per thread per iteration (strided by the grid) keep enough
+// loads in flight to stream at HBM bandwidth.
+template <int OP>
+__global__ void __launch_bounds__(kRvThreads) rv_kernel(Operand x, Operand a, Operand b, double c, bool has_b, double* out,
+                                                        int64_t n)
+{
+    const int64_t stride = (int64_t)gridDim.x * kRvThreads;
+    for (int64_t i0 = (int64_t)blockIdx.x * kRvThreads + threadIdx.x; i0 < n; i0 += 4 * stride) {
+        double r[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const int64_t i = i0 + k * stride;
+            r[k] = i < n ? rv_op<OP>(load(x, i), load(a, i), load(b, i), c, has_b) : 0.0;
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const int64_t i = i0 + k * stride;
+            if (i < n) out[i] = r[k];
+        }
+    }
+}
+
+int rv_blocks(int64_t n)
+{
+    static int cap = 0;
+    if (!cap) {
+        int dev = 0, sms = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            sms = 152;
+        cap = sms * 8;
+    }
+    const int64_t need = (n + 4 * kRvThreads - 1) / (4 * kRvThreads);
+    return (int)(need < cap ? (need > 0 ? need : 1) : cap);
+}
+
+template <int OP>
+void launch_op(const Operand& x, const Operand& a, const Operand& b, double c, bool has_b, double* out, int64_t n)
+{
+    rv_kernel<OP><<<rv_blocks(n), kRvThreads, 0, rv_stream()>>>(x, a, b, c, has_b, out, n);
+}
+
+template <int OP>
+double host_op(double x, double a, double b, double c, bool has_b)
+{
+    return rv_op<OP>(x, a, b, c, has_b);
+}
+
+#define LMM_RV_OPS(X)                                                                                                     \
+    X(LMM_RV_ADD) X(LMM_RV_SUB) X(LMM_RV_BUS) X(LMM_RV_MULT) X(LMM_RV_DIV) X(LMM_RV_VID) X(LMM_RV_CAP) X(LMM_RV_FLOOR)     \
+    X(LMM_RV_POW) X(LMM_RV_SQUARED) X(LMM_RV_SQRT) X(LMM_RV_EXP) X(LMM_RV_LOG) X(LMM_RV_SIN) X(LMM_RV_COS)                \
+    X(LMM_RV_INVERT) X(LMM_RV_ABS) X(LMM_RV_ISNAN) X(LMM_RV_EXPM1) X(LMM_RV_ACCRUE) X(LMM_RV_DISCOUNT) X(LMM_RV_CHOOSE)  \
+    X(LMM_RV_ADD_PRODUCT) X(LMM_RV_ADD_RATIO) X(LMM_RV_SUB_RATIO)
+
+bool valid_op(int op)
+{
+    switch (op) {
+#define LMM_RV_CASE(o) case o:
+        LMM_RV_OPS(LMM_RV_CASE)
+#undef LMM_RV_CASE
+        return true;
+        default: return false;
+    }
+}
+
+// evaluate op: on the host when every operand is deterministic, else one kernel
+int dispatch(int op, const Operand& x, const Operand& a, const Operand& b, double c, bool has_b, double* out, int64_t n,
+             double* host_out)
+{
+    if (n == 0) {
+        switch (op) {
+#define LMM_RV_CASE(o) \
+    case o: *host_out = host_op<o>(x.v, a.v, b.v, c, has_b); return LMM_OK;
+            LMM_RV_OPS(LMM_RV_CASE)
+#undef LMM_RV_CASE
+            default: return fail(LMM_ERR_INVALID, "unknown random-variable operation");
+        }
+    }
+    switch (op) {
+#define LMM_RV_CASE(o) \
+    case o: launch_op<o>(x, a, b, c, has_b, out, n); break;
+        LMM_RV_OPS(LMM_RV_CASE)
+#undef LMM_RV_CASE
+        default: return fail(LMM_ERR_INVALID, "unknown random-variable operation");
+    }
+    LMM_CUDA(cudaGetLastError());
+    return LMM_OK;
+}
+
+// block partial sums of x, or of (x - center)^2 when centered: each thread runs the
+// reference's Kahan loop over its elements (four FP64 operations per value; this GPU's
+// FP64 pipe, not HBM, bounds a reduction), the threads' (sum, -compensation) pairs are
+// merged as double-doubles in a fixed tree
+__global__ void __launch_bounds__(kRvThreads) rv_sum_kernel(const double* x, int64_t n, const double* center, double* partials)
+{
+    double sum = 0.0, err = 0.0;
+    const double m = center ? *center : 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * kRvThreads + threadIdx.x; i < n; i += (int64_t)gridDim.x * kRvThreads) {
+        const double v = (center ? (x[i] - m) * (x[i] - m) : x[i]) - err;
+        const double t = sum + v;
+        err = (t - sum) - v;
+        sum = t;
+    }
+    dd acc = block_dd_sum(dd{sum, -err});
+    if (threadIdx.x == 0) {
+        partials[2 * blockIdx.x] = acc.hi;
+        partials[2 * blockIdx.x + 1] = acc.lo;
+    }
+}
+
+__global__ void __launch_bounds__(kRvThreads) rv_finish_kernel(const double* partials, int blocks, int64_t n, double* out)
+{
+    dd acc{0.0, 0.0};
+    for (int b = threadIdx.x; b < blocks; b += kRvThreads) acc = dd_add(acc, dd{partials[2 * b], partials[2 * b + 1]});
+    acc = block_dd_sum(acc);
+    if (threadIdx.x == 0) *out = (acc.hi + acc.lo) / (double)n;
+}
+
+// Math.min / Math.max over the realizations (tree order; NaN propagates, -0.0 < +0.0)
+__global__ void __launch_bounds__(kRvThreads) rv_minmax_kernel(const double* x, int64_t n, double* partials)
+{
+    __shared__ double smin[kRvThreads], smax[kRvThreads];
+    double mn = x[0], mx = x[0];
+    for (int64_t i = (int64_t)blockIdx.x * kRvThreads + threadIdx.x; i < n; i += (int64_t)gridDim.x * kRvThreads) {
+        mn = java_min(mn, x[i]);
+        mx = java_max(mx, x[i]);
+    }
+    smin[threadIdx.x] = mn;
+    smax[threadIdx.x] = mx;
+    __syncthreads();
+    for (int h = kRvThreads / 2; h > 0; h >>= 1) {
+        if (threadIdx.x < h) {
+            smin[threadIdx.x] = java_min(smin[threadIdx.x], smin[threadIdx.x + h]);
+            smax[threadIdx.x] = java_max(smax[threadIdx.x], smax[threadIdx.x + h]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        partials[2 * blockIdx.x] = smin[0];
+        partials[2 * blockIdx.x + 1] = smax[0];
+    }
+}
+
+// float states (mixed form) widened to FP64
+__global__ void __launch_bounds__(kRvThreads) rv_widen_kernel(const float* src, double* out, int64_t n)
+{
+    for (int64_t i = (int64_t)blockIdx.x * kRvThreads + threadIdx.x; i < n; i += (int64_t)gridDim.x * kRvThreads)
+        out[i] = (double)src[i];
+}
+
+// getNumeraire with the discount-curve adjustment (LIBORMarketModelFromCovarianceModel.java:869-874):
+// Scalar.div on a deterministic numeraire date (invert, then multiply), else (N a) / P^d
+__global__ void __launch_bounds__(kRvThreads) rv_numeraire_kernel(const double* num, const double* adj, double pd, int det,
+                                                                  double* out, int64_t n)
+{
+    const double a = *adj;
+    for (int64_t i = (int64_t)blockIdx.x * kRvThreads + threadIdx.x; i < n; i += (int64_t)gridDim.x * kRvThreads)
+        out[i] = det ? (1.0 / pd) * (num[i] * a) : (num[i] * a) / pd;
+}
+
+int rv_alloc(double time, int64_t n, lmm_rv** out)
+{
+    lmm_rv* r = new lmm_rv;
+    r->time = time;
+    r->n = n;
+    if (n > 0) {
+        const cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&r->d), sizeof(double) * (size_t)n, rv_stream());
+        if (e != cudaSuccess) {
+            delete r;
+            return cuda_fail(e, "cudaMallocAsync (random variable)");
+        }
+    }
+    *out = r;
+    return LMM_OK;
+}
+
+Operand operand(const lmm_rv* r) { return Operand{r && r->n > 0 ? r->d : nullptr, r ? r->value : 0.0}; }
+
+int64_t common_size(const lmm_rv* x, const lmm_rv* a, const lmm_rv* b, bool* ok)
+{
+    int64_t n = 0;
+    *ok = true;
+    for (const lmm_rv* r : {x, a, b}) {
+        if (!r || r->n == 0) continue;
+        if (n != 0 && r->n != n) *ok = false;
+        n = r->n;
+    }
+    return n;
+}
+
+double later_time(const lmm_rv* x, const lmm_rv* a, const lmm_rv* b)
+{
+    double t = x->time;
+    if (a && a->time > t) t = a->time;
+    if (b && b->time > t) t = b->time;
+    return t;
+}
+
+int apply_any(const lmm_rv* x, int op, const lmm_rv* a, const lmm_rv* b, double c, bool has_b, lmm_rv** out)
+{
+    if (!x || !out) return fail(LMM_ERR_INVALID, "null argument");
+    if (!valid_op(op)) return fail(LMM_ERR_INVALID, "unknown random-variable operation");
+    bool ok;
+    const int64_t n = common_size(x, a, b, &ok);
+    if (!ok) return fail(LMM_ERR_INVALID, "random variables of different sizes");
+    lmm_rv* r = nullptr;
+    int rc = rv_alloc(later_time(x, a, b), n, &r);
+    if (rc) return rc;
+    rc = dispatch(op, operand(x), operand(a), operand(b), c, has_b, r->d, n, &r->value);
+    if (rc) {
+        lmm_rv_destroy(r);
+        return rc;
+    }
+    *out = r;
+    return LMM_OK;
+}
+
+// order the library stream after the work so far on src, and src after the copy that follows
+struct StreamHandoff {
+    cudaEvent_t before = nullptr, after = nullptr;
+    cudaStream_t src;
+    explicit StreamHandoff(cudaStream_t s) : src(s)
+    {
+        cudaEventCreateWithFlags(&before, cudaEventDisableTiming);
+        cudaEventCreateWithFlags(&after, cudaEventDisableTiming);
+        cudaEventRecord(before, src);
+        cudaStreamWaitEvent(rv_stream(), before, 0);
+    }
+    ~StreamHandoff()
+    {
+        cudaEventRecord(after, rv_stream());
+        cudaStreamWaitEvent(src, after, 0);  // the source buffers outlive the copy
+        cudaEventDestroy(before);
+        cudaEventDestroy(after);
+    }
+};
+
+}  // namespace
+
+int rv_from_device(double time, const void* src, int fp32, int64_t n, cudaStream_t src_stream, lmm_rv** out)
+{
+    lmm_rv* r = nullptr;
+    int rc = rv_alloc(time, n, &r);
+    if (rc) return rc;
+    {
+        StreamHandoff h(src_stream);
+        if (fp32) {
+            const int blocks = rv_blocks(n);
+            rv_widen_kernel<<<blocks, kRvThreads, 0, rv_stream()>>>(static_cast<const float*>(src), r->d, n);
+        } else {
+            cudaMemcpyAsync(r->d, src, sizeof(double) * (size_t)n, cudaMemcpyDeviceToDevice, rv_stream());
+        }
+    }
+    LMM_CUDA(cudaGetLastError());
+    *out = r;
+    return LMM_OK;
+}
+
+int rv_numeraire(double time, const double* d_num, const double* d_adj, int has_discount, int det, double pd, int64_t n,
+                 cudaStream_t src_stream, lmm_rv** out)
+{
+    lmm_rv* r = nullptr;
+    int rc = rv_alloc(time, n, &r);
+    if (rc) return rc;
+    {
+        StreamHandoff h(src_stream);
+        if (has_discount)
+            rv_numeraire_kernel<<<rv_blocks(n), kRvThreads, 0, rv_stream()>>>(d_num, d_adj, pd, det, r->d, n);
+        else
+            cudaMemcpyAsync(r->d, d_num, sizeof(double) * (size_t)n, cudaMemcpyDeviceToDevice, rv_stream());
+    }
+    LMM_CUDA(cudaGetLastError());
+    *out = r;
+    return LMM_OK;
+}
+
+}  // namespace lmm
+
+using namespace lmm;
+
+extern "C" {
+
+int lmm_rv_create_constant(double time, double value, lmm_rv** out)
+{
+    if (!out) return fail(LMM_ERR_INVALID, "null argument");
+    lmm_rv* r = new lmm_rv;
+    r->time = time;
+    r->value = value;
+    *out = r;
+    return LMM_OK;
+}
+
+int lmm_rv_create(double time, const double* host, int64_t n, lmm_rv** out)
+{
+    if (!out || (!host && n > 0)) return fail(LMM_ERR_INVALID, "null argument");
+    if (n < 1) return fail(LMM_ERR_INVALID, "a stochastic random variable needs at least one realization");
+    lmm_rv* r = nullptr;
+    int rc = rv_alloc(time, n, &r);
+    if (rc) return rc;
+    const cudaError_t e = cudaMemcpyAsync(r->d, host, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, rv_stream());
+    if (e != cudaSuccess) {
+        lmm_rv_destroy(r);
+        return cuda_fail(e, "cudaMemcpyAsync (random variable)");
+    }
+    count_h2d(sizeof(double) * (size_t)n);
+    *out = r;
+    return LMM_OK;
+}
+
+int lmm_rv_stream(void** out_stream)
+{
+    if (!out_stream) return fail(LMM_ERR_INVALID, "null argument");
+    *out_stream = (void*)rv_stream();
+    return LMM_OK;
+}
+
+int lmm_rv_destroy(lmm_rv* x)
+{
+    if (!x) return LMM_OK;
+    if (x->d) cudaFreeAsync(x->d, rv_stream());
+    delete x;
+    return LMM_OK;
+}
+
+int lmm_rv_describe(const lmm_rv* x, double* out_time, int64_t* out_n, int* out_deterministic, double* out_value)
+{
+    if (!x) return fail(LMM_ERR_INVALID, "null argument");
+    if (out_time) *out_time = x->time;
+    if (out_n) *out_n = x->n;
+    if (out_deterministic) *out_deterministic = x->n == 0;
+    if (out_value) *out_value = x->value;
+    return LMM_OK;
+}
+
+int lmm_rv_get(const lmm_rv* x, double* out_host)
+{
+    if (!x || !out_host) return fail(LMM_ERR_INVALID, "null argument");
+    if (x->n == 0) {
+        *out_host = x->value;
+        return LMM_OK;
+    }
+    LMM_CUDA(cudaMemcpyAsync(out_host, x->d, sizeof(double) * (size_t)x->n, cudaMemcpyDeviceToHost, rv_stream()));
+    LMM_CUDA(cudaStreamSynchronize(rv_stream()));
+    return LMM_OK;
+}
+
+int lmm_rv_apply_scalar(const lmm_rv* x, int op, double y, lmm_rv** out)
+{
+    if (op >= LMM_RV_ACCRUE) return fail(LMM_ERR_INVALID, "three-argument operation: use lmm_rv_apply3");
+    lmm_rv c;  // y as a deterministic operand
+    c.value = y;
+    c.time = x ? x->time : 0.0;
+    return apply_any(x, op, &c, nullptr, 0.0, false, out);
+}
+
+int lmm_rv_apply(const lmm_rv* x, int op, const lmm_rv* y, lmm_rv** out)
+{
+    if (!y) return fail(LMM_ERR_INVALID, "null argument");
+    if (op > LMM_RV_FLOOR) return fail(LMM_ERR_INVALID, "not a binary random-variable operation");
+    return apply_any(x, op, y, nullptr, 0.0, false, out);
+}
+
+int lmm_rv_apply3(const lmm_rv* x, int op, const lmm_rv* a, const lmm_rv* b, double c, lmm_rv** out)
+{
+    if (op < LMM_RV_ACCRUE) return fail(LMM_ERR_INVALID, "not a three-argument random-variable operation");
+    if (!a) return fail(LMM_ERR_INVALID, "null argument");
+    const bool needs_b = op == LMM_RV_CHOOSE || op == LMM_RV_ADD_RATIO || op == LMM_RV_SUB_RATIO;
+    if (needs_b && !b) return fail(LMM_ERR_INVALID, "null argument");
+    return apply_any(x, op, a, b, c, b != nullptr, out);
+}
+
+static int reduce_sum(const lmm_rv* x, const double* center, double* out)
+{
+    const int blocks = (int)std::min<int64_t>((x->n + kRvThreads - 1) / kRvThreads, 1024);
+    double* scratch = nullptr;
+    LMM_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&scratch), sizeof(double) * (2 * (size_t)blocks + 1), rv_stream()));
+    rv_sum_kernel<<<blocks, kRvThreads, 0, rv_stream()>>>(x->d, x->n, center, scratch);
+    rv_finish_kernel<<<1, kRvThreads, 0, rv_stream()>>>(scratch, blocks, x->n, scratch + 2 * blocks);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, scratch + 2 * blocks, sizeof(double), cudaMemcpyDeviceToHost, rv_stream());
+    cudaFreeAsync(scratch, rv_stream());
+    if (e == cudaSuccess) e = cudaStreamSynchronize(rv_stream());
+    return e == cudaSuccess ? LMM_OK : cuda_fail(e, "random-variable reduction");
+}
+
+int lmm_rv_average(const lmm_rv* x, double* out)
+{
+    if (!x || !out) return fail(LMM_ERR_INVALID, "null argument");
+    if (x->n == 0) {
+        *out = x->value;
+        return LMM_OK;
+    }
+    return reduce_sum(x, nullptr, out);
+}
+
+int lmm_rv_variance(const lmm_rv* x, double* out)
+{
+    if (!x || !out) return fail(LMM_ERR_INVALID, "null argument");
+    if (x->n <= 1) {
+        *out = 0.0;
+        return LMM_OK;
+    }
+    double avg = 0.0;
+    int rc = reduce_sum(x, nullptr, &avg);
+    if (rc) return rc;
+    double* d_avg = nullptr;
+    LMM_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&d_avg), sizeof(double), rv_stream()));
+    cudaError_t e = cudaMemcpyAsync(d_avg, &avg, sizeof(double), cudaMemcpyHostToDevice, rv_stream());
+    if (e == cudaSuccess) rc = reduce_sum(x, d_avg, out);
+    cudaFreeAsync(d_avg, rv_stream());
+    if (e != cudaSuccess) return cuda_fail(e, "random-variable variance");
+    return rc;
+}
+
+int lmm_rv_standard_error(const lmm_rv* x, double* out)
+{
+    if (!x || !out) return fail(LMM_ERR_INVALID, "null argument");
+    if (x->n == 0) {
+        *out = 0.0;
+        return LMM_OK;
+    }
+    double var = 0.0;
+    const int rc = lmm_rv_variance(x, &var);
+    if (rc) return rc;
+    *out = std::sqrt(var) / std::sqrt((double)x->n);  // getStandardDeviation() / Math.sqrt(size())
+    return LMM_OK;
+}
+
+int lmm_rv_min_max(const lmm_rv* x, double* out_min, double* out_max)
+{
+    if (!x || !out_min || !out_max) return fail(LMM_ERR_INVALID, "null argument");
+    if (x->n == 0) {
+        *out_min = *out_max = x->value;
+        return LMM_OK;
+    }
+    const int blocks = (int)std::min<int64_t>((x->n + kRvThreads - 1) / kRvThreads, 1024);
+    double* scratch = nullptr;
+    LMM_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&scratch), sizeof(double) * 2 * (size_t)blocks, rv_stream()));
+    rv_minmax_kernel<<<blocks, kRvThreads, 0, rv_stream()>>>(x->d, x->n, scratch);
+    std::vector<double> h(2 * (size_t)blocks);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h.data(), scratch, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, rv_stream());
+    cudaFreeAsync(scratch, rv_stream());
+    if (e == cudaSuccess) e = cudaStreamSynchronize(rv_stream());
+    if (e != cudaSuccess) return cuda_fail(e, "random-variable min/max");
+    double mn = h[0], mx = h[1];
+    for (int b = 1; b < blocks; b++) {
+        mn = java_min(mn, h[2 * b]);
+        mx = java_max(mx, h[2 * b + 1]);
+    }
+    *out_min = mn;
+    *out_max = mx;
+    return LMM_OK;
+}
+
+}  // extern "C"

@@ -1,7 +1,7 @@
 """GB300-native LIBOR Market Model Monte Carlo path with finmath-lib's API surface.
 
 The numeric work runs in liblmm_gb300.so (CUDA kernels for sm_103a behind the C ABI of
-include/lmm_gb300.h).  Importing this package does not touch the GPU; the first call
+include/lmm_gb300.h and include/lmm_rv.h).  Importing this package does not touch the GPU; the first call
 that needs the library loads it (and builds it from source if it is not built yet).
 """
 from ._lib import (CalculationException, PRECISION_FP64, PRECISION_MIXED, SCHEME_EULER, SCHEME_EULER_FUNCTIONAL,
@@ -12,6 +12,7 @@ from .lmm import (TimeDiscretizationFromArray, ForwardCurveInterpolation, Discou
                   LIBORMarketModelFromCovarianceModel, BrownianMotionFromMersenneRandomNumbers,
                   EulerSchemeFromProcessModel, LIBORMonteCarloSimulationFromLIBORModel, Swaption, BermudanSwaption, Portfolio,
                   mersenne_twister_uniforms, kernel_stats)
+from .randomvariable import RandomVariableGPU, RandomVariableGPUFactory
 from . import workloads, autotune
 
 __all__ = [n for n in dir() if not n.startswith("_")]

@@ -1,4 +1,4 @@
-"""ctypes binding of liblmm_gb300.so (the C ABI declared in include/lmm_gb300.h).
+"""ctypes binding of liblmm_gb300.so (the C ABI declared in include/lmm_gb300.h and lmm_rv.h).
 
 The library is the product: every call below runs the CUDA implementation.  There is
 no CPU fallback; if the library or a GPU is missing, calls raise.
@@ -88,6 +88,21 @@ SIGNATURES = {
     "lmm_process_simulate": (ctypes.c_int, [_VP]),
     "lmm_process_get_value": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, _D]),
     "lmm_process_get_numeraire": (ctypes.c_int, [_VP, ctypes.c_double, _D]),
+    "lmm_process_get_value_rv": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_VP)]),
+    "lmm_process_get_numeraire_rv": (ctypes.c_int, [_VP, ctypes.c_double, ctypes.POINTER(_VP)]),
+    "lmm_rv_create_constant": (ctypes.c_int, [ctypes.c_double, ctypes.c_double, ctypes.POINTER(_VP)]),
+    "lmm_rv_create": (ctypes.c_int, [ctypes.c_double, _D, ctypes.c_int64, ctypes.POINTER(_VP)]),
+    "lmm_rv_destroy": (ctypes.c_int, [_VP]),
+    "lmm_rv_stream": (ctypes.c_int, [ctypes.POINTER(_VP)]),
+    "lmm_rv_describe": (ctypes.c_int, [_VP, _D, _I64, ctypes.POINTER(ctypes.c_int), _D]),
+    "lmm_rv_get": (ctypes.c_int, [_VP, _D]),
+    "lmm_rv_apply_scalar": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_double, ctypes.POINTER(_VP)]),
+    "lmm_rv_apply": (ctypes.c_int, [_VP, ctypes.c_int, _VP, ctypes.POINTER(_VP)]),
+    "lmm_rv_apply3": (ctypes.c_int, [_VP, ctypes.c_int, _VP, _VP, ctypes.c_double, ctypes.POINTER(_VP)]),
+    "lmm_rv_average": (ctypes.c_int, [_VP, _D]),
+    "lmm_rv_variance": (ctypes.c_int, [_VP, _D]),
+    "lmm_rv_standard_error": (ctypes.c_int, [_VP, _D]),
+    "lmm_rv_min_max": (ctypes.c_int, [_VP, _D, _D]),
     "lmm_process_destroy": (ctypes.c_int, [_VP]),
     "lmm_swaption_get_value": (ctypes.c_int, [_VP, ctypes.POINTER(LmmSwaptionDesc), _D, _D]),
     "lmm_bermudan_get_value": (ctypes.c_int, [_VP, ctypes.POINTER(LmmBermudanDesc), _D, _D, _D]),

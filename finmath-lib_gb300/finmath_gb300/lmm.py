@@ -360,6 +360,21 @@ class LIBORMonteCarloSimulationFromLIBORModel:
     def getNumeraire(self, time):
         return self.process.getNumeraire(time)
 
+    def getLIBORRandomVariable(self, timeIndex, liborIndex):
+        """getLIBOR as a device random variable (no host copy), LIBORMonteCarloSimulationFromLIBORModel.java:123-126."""
+        from .randomvariable import RandomVariableGPU
+        h = ctypes.c_void_p()
+        check(_lib.load().lmm_process_get_value_rv(self.process._h, int(timeIndex), int(liborIndex), ctypes.byref(h)),
+              "getLIBOR")
+        return RandomVariableGPU(h)
+
+    def getNumeraireRandomVariable(self, time):
+        """getNumeraire as a device random variable (adjusted, as getNumeraire), :153-155."""
+        from .randomvariable import RandomVariableGPU
+        h = ctypes.c_void_p()
+        check(_lib.load().lmm_process_get_numeraire_rv(self.process._h, float(time), ctypes.byref(h)), "getNumeraire")
+        return RandomVariableGPU(h)
+
     def getNumberOfPaths(self):
         return self.process.numberOfPaths
 

@@ -305,3 +305,9 @@ Simulation.bermudan_frozen = _bermudan_frozen
 def kahan_average(x) -> float:
     x = f64(x)
     return lib().orc_kahan_average(_p(x), len(x))
+
+
+def standard_error(x) -> float:
+    """getStandardError of RandomVariableFromDoubleArray.java:419-428 (Kahan mean and variance)."""
+    x = f64(x)
+    return lib().orc_standard_error(_p(x), len(x))

@@ -1,0 +1,188 @@
+"""Device random variables (include/lmm_rv.h) against the reference's semantics.
+
+The elementwise operations of RandomVariableFromDoubleArray round every + - * / separately,
+so on the same inputs the GPU equals numpy's IEEE arithmetic bit for bit; Math.min/max
+rules (NaN wins, -0.0 < +0.0) are checked on special values; exp/log/pow/sin/cos are
+CUDA's (within 2 ulp).  Averages are compensated sums (as the reference's Kahan sums).
+Finmath products written against the random-variable API (caplet, swap) reprice against
+the oracle's paths to 1e-12."""
+import numpy as np
+import pytest
+
+import finmath_gb300 as F
+from finmath_gb300 import workloads as W
+from finmath_gb300.randomvariable import RandomVariableGPU as RV
+from oracle import pyoracle as po
+from conftest import oracle_model
+
+pytestmark = pytest.mark.gpu
+
+N = 100_003  # ragged: not a multiple of the launch geometry
+
+
+def bits(a):
+    return np.ascontiguousarray(a, dtype=np.float64).view(np.int64)
+
+
+@pytest.fixture(scope="module")
+def xy():
+    rng = np.random.default_rng(20261204)
+    x = rng.normal(0.03, 0.02, N)
+    y = rng.normal(0.5, 0.3, N)
+    z = rng.normal(1.0, 0.1, N)
+    return x, y, z
+
+
+def test_binary_operations_bit_exact(xy):
+    x, y, _ = xy
+    X, Y = RV.from_array(1.0, x), RV.from_array(2.0, y)
+    cases = {"add": x + y, "sub": x - y, "bus": y - x, "mult": x * y, "div": x / y, "vid": y / x}
+    for name, ref in cases.items():
+        r = getattr(X, name)(Y)
+        assert np.array_equal(bits(r.getRealizations()), bits(ref)), name
+        assert r.getFiltrationTime() == 2.0  # the later filtration time
+    for name, ref in {"add": x + 0.7, "sub": x - 0.7, "bus": 0.7 - x, "mult": x * 0.7, "div": x / 0.7,
+                      "vid": 0.7 / x}.items():
+        assert np.array_equal(bits(getattr(X, name)(0.7).getRealizations()), bits(ref)), name
+
+
+def test_three_argument_operations_bit_exact(xy):
+    x, y, z = xy
+    X, Y, Z = RV.from_array(0.0, x), RV.from_array(0.0, y), RV.from_array(0.0, z)
+    assert np.array_equal(bits(Z.accrue(X, 0.5).getRealizations()), bits(z * (1 + x * 0.5)))
+    assert np.array_equal(bits(Z.discount(X, 0.5).getRealizations()), bits(z / (1.0 + x * 0.5)))
+    assert np.array_equal(bits(X.addProduct(Y, Z).getRealizations()), bits(x + y * z))
+    assert np.array_equal(bits(X.addProduct(Y, 0.25).getRealizations()), bits(x + y * 0.25))
+    assert np.array_equal(bits(X.addRatio(Y, Z).getRealizations()), bits(x + y / z))
+    assert np.array_equal(bits(X.subRatio(Y, Z).getRealizations()), bits(x - y / z))
+    assert np.array_equal(bits(X.choose(Y, Z).getRealizations()), bits(np.where(x >= 0.0, y, z)))
+    # deterministic rate: x (1 + r c) with the same rounding
+    assert np.array_equal(bits(Z.accrue(0.04, 0.5).getRealizations()), bits(z * (1 + 0.04 * 0.5)))
+
+
+def test_unary_operations(xy):
+    x, y, z = xy
+    Z = RV.from_array(0.0, z)
+    assert np.array_equal(bits(Z.squared().getRealizations()), bits(z * z))
+    assert np.array_equal(bits(Z.sqrt().getRealizations()), bits(np.sqrt(z)))  # correctly rounded
+    assert np.array_equal(bits(Z.invert().getRealizations()), bits(1.0 / z))
+    assert np.array_equal(bits(RV.from_array(0.0, x).abs().getRealizations()), bits(np.abs(x)))
+    for name, ref in {"exp": np.exp(z), "log": np.log(z), "sin": np.sin(z), "cos": np.cos(z), "expm1": np.expm1(x)}.items():
+        src = RV.from_array(0.0, x if name == "expm1" else z)
+        got = getattr(src, name)().getRealizations()
+        assert np.max(np.abs(got - ref) / np.abs(ref)) <= 4.5e-16, name
+    got = Z.pow(1.7).getRealizations()
+    assert np.max(np.abs(got - z ** 1.7) / z ** 1.7) <= 4.5e-16
+
+
+def test_min_max_nan_and_signed_zero():
+    x = np.array([1.0, np.nan, -0.0, 0.0, 2.0, -3.0, 0.0, -0.0])
+    y = np.array([2.0, 1.0, 0.0, -0.0, np.nan, -3.0, 0.0, -0.0])
+    X, Y = RV.from_array(0.0, x), RV.from_array(0.0, y)
+
+    def jmin(a, b):
+        if a != a or b != b:
+            return np.nan
+        if a < b:
+            return a
+        if b < a:
+            return b
+        return a if np.signbit(a) else b
+
+    def jmax(a, b):
+        if a != a or b != b:
+            return np.nan
+        if a > b:
+            return a
+        if b > a:
+            return b
+        return b if np.signbit(a) else a
+
+    cap = X.cap(Y).getRealizations()
+    flo = X.floor(Y).getRealizations()
+    for i in range(len(x)):
+        for got, ref in ((cap[i], jmin(x[i], y[i])), (flo[i], jmax(x[i], y[i]))):
+            assert (np.isnan(got) and np.isnan(ref)) or (got == ref and np.signbit(got) == np.signbit(ref)), (i, got, ref)
+    assert np.array_equal(X.isNaN().getRealizations(), np.isnan(x).astype(float))
+    mn, mx = X.getMin(), X.getMax()
+    assert np.isnan(mn) and np.isnan(mx)  # a NaN realization makes Math.min/max NaN
+    Zs = RV.from_array(0.0, np.array([0.0, -0.0, 3.0]))
+    assert Zs.getMin() == 0.0 and np.signbit(Zs.getMin()) and Zs.getMax() == 3.0
+
+
+def test_deterministic_and_broadcast(xy):
+    x, _, _ = xy
+    a, b = RV.constant(0.5, 0.04), RV.constant(1.5, 0.5)
+    c = a.mult(b).add(1.0)
+    assert c.isDeterministic() and c.doubleValue() == 0.04 * 0.5 + 1.0 and c.getFiltrationTime() == 1.5
+    assert c.getAverage() == c.doubleValue() and c.getStandardError() == 0.0 and c.getVariance() == 0.0
+    X = RV.from_array(1.0, x)
+    assert np.array_equal(bits(X.add(a).getRealizations()), bits(x + 0.04))
+    assert np.array_equal(bits(a.sub(X).getRealizations()), bits(0.04 - x))
+    with pytest.raises(ValueError):
+        X.add(RV.from_array(0.0, np.ones(7)))
+
+
+def test_reductions(xy):
+    x, _, _ = xy
+    X = RV.from_array(0.0, x)
+    assert X.getAverage() == pytest.approx(po.kahan_average(x), rel=1e-15, abs=1e-18)
+    m = po.kahan_average(x)
+    var = po.kahan_average((x - m) * (x - m))
+    assert X.getVariance() == pytest.approx(var, rel=1e-14)
+    assert X.getStandardError() == pytest.approx(np.sqrt(var) / np.sqrt(N), rel=1e-14)
+    assert X.getMin() == np.min(x) and X.getMax() == np.max(x)
+
+
+@pytest.fixture(scope="module")
+def lmm20():
+    cfg = W.LMM20
+    m = oracle_model(cfg)
+    P = 5000
+    dW = po.brownian_increments(m.times, m.F, P, cfg["seed"])
+    obs = np.zeros(m.T + 1, np.uint8)
+    obs[W.tenor_time_indices(cfg)] = 1
+    return cfg, m, po.Simulation(m, dW, observe=obs), W.build(cfg, paths=P)
+
+
+def test_caplets_and_swap_through_the_random_variable_api(lmm20):
+    # Caplet.getValue (montecarlo/interestrate/products/Caplet.java:115-141) as a user writes
+    # it against RandomVariable, on the GPU simulation, against the same operations in numpy
+    # on the oracle's paths
+    cfg, m, osim, sim = lmm20
+    P = sim.getNumberOfPaths()
+    w = 1.0 / P
+    N0g, N0o = sim.getNumeraireRandomVariable(0.0), osim.numeraire(0.0)
+    dt, period = cfg["dt"], cfg["period"]
+    for j, K in ((2, 0.04), (9, 0.05), (15, 0.06)):
+        T_fix, T_pay = j * period, (j + 1) * period
+        t = int(round(T_fix / dt))
+        g = sim.getLIBORRandomVariable(t, j).sub(K).floor(0.0).mult(period)
+        g = g.div(sim.getNumeraireRandomVariable(T_pay)).mult(w).mult(N0g).div(w)
+        o = np.maximum(osim.process_value(t, j) - K, 0.0) * period
+        o = o / osim.numeraire(T_pay) * w * N0o / w
+        assert g.getAverage() == pytest.approx(po.kahan_average(o), rel=1e-12)
+        assert g.getStandardError() == pytest.approx(po.standard_error(o), rel=1e-10)
+    # a payer swap: sum over periods of (L_j(T_j) - K) delta / N(T_{j+1})
+    K = 0.05
+    g = F.RandomVariableGPU.constant(0.0, 0.0)
+    o = np.zeros(P)
+    for j in range(2, 12):
+        t = int(round(j * period / dt))
+        N = sim.getNumeraireRandomVariable((j + 1) * period)
+        g = g.addRatio(sim.getLIBORRandomVariable(t, j).sub(K).mult(period), N)
+        o = o + (osim.process_value(t, j) - K) * period / osim.numeraire((j + 1) * period)
+    assert g.getAverage() == pytest.approx(po.kahan_average(o), rel=1e-12)
+
+
+def test_process_values_as_random_variables_match_host_copies():
+    cfg = W.LMM20
+    for prec in (F.PRECISION_FP64, F.PRECISION_MIXED):
+        sim = W.build(cfg, paths=3001, precision=prec)
+        t = W.tenor_time_indices(cfg)[5]
+        assert np.array_equal(sim.getLIBORRandomVariable(t, 7).getRealizations(), sim.getLIBOR(t, 7))
+        assert np.array_equal(sim.getNumeraireRandomVariable(3.0).getRealizations(), sim.getNumeraire(3.0))
+        with pytest.raises(ValueError):
+            sim.getNumeraireRandomVariable(0.25)  # off the tenor grid
+        sim.process.close()
+        sim.process.brownianMotion.close()
