@@ -206,6 +206,10 @@ class LIBORMarketModelFromCovarianceModel:
         self.discountCurve = discountCurve
         self.covarianceModel = covarianceModel
         self.liborCap = float(props.get("liborCap", 1e5))
+        # getForwardRate's tenor interpolation and simulation-time rounding (:191-192, :407-410)
+        self.interpolationMethod = str(props.get("interpolationMethod", "LOG_LINEAR_UNCORRECTED")).upper()
+        self.simulationTimeInterpolationMethod = str(props.get("simulationTimeInterpolationMethod",
+                                                               "ROUND_NEAREST")).upper()
         tenor = liborPeriodDiscretization.getAsDoubleArray()
         N = len(tenor) - 1
         # getInitialState (:1081-1093): forward over [T_j, T_j + delta_j]
@@ -374,6 +378,70 @@ class LIBORMonteCarloSimulationFromLIBORModel:
         h = ctypes.c_void_p()
         check(_lib.load().lmm_process_get_numeraire_rv(self.process._h, float(time), ctypes.byref(h)), "getNumeraire")
         return RandomVariableGPU(h)
+
+    def getForwardRate(self, time, periodStart, periodEnd):
+        """LIBORMarketModelFromCovarianceModel.getForwardRate (…/models/LIBORMarketModelFromCovarianceModel.java:1238-1305)
+        as device random variables: the model primitive L_j(t), the accrual over several tenor
+        periods, or an off-tenor period by the model's interpolationMethod (:1318-1381; LINEAR
+        and LOG_LINEAR_UNCORRECTED with the analytic forward-curve adjustment)."""
+        m = self.model
+        tenor, td = m.liborPeriodDiscretization, self.process.getTimeDiscretization()
+        ps_i, pe_i = tenor.getTimeIndex(periodStart), tenor.getTimeIndex(periodEnd)
+        time = min(time, periodStart)  # beyond the fixing: the fixing time
+        ti = td.getTimeIndex(time)
+        if ti < 0:
+            ti = -ti - 2
+            if m.simulationTimeInterpolationMethod == "ROUND_NEAREST" and time - td.getTime(ti) > td.getTime(ti + 1) - time:
+                ti += 1
+        if pe_i < 0:
+            prev = (-pe_i - 1) - 1
+            next_end = tenor.getTime(prev + 1)
+            long_ = self.getForwardRate(time, periodStart, next_end).mult(next_end - periodStart).add(1.0)
+            interp = self._onePlusInterpolatedLIBORDt(ti, periodEnd, prev)
+            return long_.div(interp).sub(1.0).div(periodEnd - periodStart)
+        if ps_i < 0:
+            prev = (-ps_i - 1) - 1
+            next_start = tenor.getTime(prev + 1)
+            if next_start > periodEnd:
+                raise ValueError("Interpolation not possible.")
+            if next_start == periodEnd:
+                return self._onePlusInterpolatedLIBORDt(ti, periodStart, prev).sub(1.0).div(periodEnd - periodStart)
+            long_ = self.getForwardRate(time, next_start, periodEnd).mult(periodEnd - next_start).add(1.0)
+            interp = self._onePlusInterpolatedLIBORDt(ti, periodStart, prev)
+            return long_.mult(interp).sub(1.0).div(periodEnd - periodStart)
+        if ps_i + 1 == pe_i:
+            return self.getLIBORRandomVariable(ti, ps_i)
+        acc = None
+        for k in range(ps_i, pe_i):
+            sub = tenor.getTime(k + 1) - tenor.getTime(k)
+            L = self.getLIBORRandomVariable(ti, k)
+            acc = L.mult(sub).add(1.0) if acc is None else acc.accrue(L, sub)
+        return acc.sub(1.0).div(periodEnd - periodStart)
+
+    def _onePlusInterpolatedLIBORDt(self, ti, periodStartTime, idx):
+        """getOnePlusInterpolatedLIBORDt (:1318-1381)."""
+        m = self.model
+        tenor, td = m.liborPeriodDiscretization, self.process.getTimeDiscretization()
+        ts, te = tenor.getTime(idx), tenor.getTime(idx + 1)
+        tdt = te - ts
+        if ts < td.getTime(ti):
+            ti = min(ti, td.getTimeIndex(ts))  # fixed at the long period's start
+            if ti < 0:
+                raise ValueError("Tenor discretization not part of time discretization.")
+        long_ = self.getLIBORRandomVariable(ti, idx).mult(tdt).add(1.0)
+        small = te - periodStartTime
+        alpha = small / tdt
+        if m.interpolationMethod == "LINEAR":
+            interp = long_.mult(alpha).add(1 - alpha)
+        elif m.interpolationMethod == "LOG_LINEAR_UNCORRECTED":
+            interp = long_.log().mult(alpha).exp()
+        else:
+            raise ValueError(f"interpolation method {m.interpolationMethod} is not supported")
+        fc = m.forwardRateCurve
+        a_long = 1 + fc.getForward(None, ts, tdt) * tdt
+        a_short = 1 + fc.getForward(None, periodStartTime, small) * small
+        a_interp = a_long * alpha + (1 - alpha) if m.interpolationMethod == "LINEAR" else np.exp(np.log(a_long) * alpha)
+        return interp.mult(a_short / a_interp)
 
     def getNumberOfPaths(self):
         return self.process.numberOfPaths

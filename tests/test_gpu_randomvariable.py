@@ -186,3 +186,86 @@ def test_process_values_as_random_variables_match_host_copies():
             sim.getNumeraireRandomVariable(0.25)  # off the tenor grid
         sim.process.close()
         sim.process.brownianMotion.close()
+
+
+def _forward_rate_numpy(osim, m, cfg, method, time, ps, pe):
+    """The same getForwardRate (LIBORMarketModelFromCovarianceModel.java:1238-1381) in numpy on
+    the oracle's paths, with the forward curve interpolated linearly on values."""
+    tenor = np.asarray(m.tenor)
+    times = np.asarray(m.times)
+    nodes, values = np.asarray(cfg["curve_nodes"]), np.asarray(cfg["curve_values"])
+    po_off = cfg["period"]
+
+    def fwd(t, dt):  # ForwardCurveInterpolation.getForward with a payment offset dt
+        f = float(np.interp(t, nodes, values))
+        return f if dt == po_off else (np.exp(np.log(1 + f * po_off) * dt / po_off) - 1.0) / dt
+
+    def idx(grid, t):
+        i = int(np.searchsorted(grid, t))
+        return i if i < len(grid) and grid[i] == t else -(i + 1)
+
+    def one_plus(ti, pst, k):
+        ts, te = tenor[k], tenor[k + 1]
+        tdt = te - ts
+        if ts < times[ti]:
+            ti = min(ti, idx(times, ts))
+        lg = osim.process_value(ti, k) * tdt + 1.0
+        small = te - pst
+        alpha = small / tdt
+        interp = lg * alpha + (1 - alpha) if method == "LINEAR" else np.exp(np.log(lg) * alpha)
+        a_long = 1 + fwd(ts, tdt) * tdt
+        a_short = 1 + fwd(pst, small) * small
+        a_int = a_long * alpha + (1 - alpha) if method == "LINEAR" else np.exp(np.log(a_long) * alpha)
+        return interp * (a_short / a_int)
+
+    def fr(time, ps, pe):
+        psi, pei = idx(tenor, ps), idx(tenor, pe)
+        time = min(time, ps)
+        ti = idx(times, time)
+        if ti < 0:
+            ti = -ti - 2
+            if time - times[ti] > times[ti + 1] - time:
+                ti += 1
+        if pei < 0:
+            prev = -pei - 2
+            ne = tenor[prev + 1]
+            return ((fr(time, ps, ne) * (ne - ps) + 1.0) / one_plus(ti, pe, prev) - 1.0) / (pe - ps)
+        if psi < 0:
+            prev = -psi - 2
+            ns = tenor[prev + 1]
+            if ns == pe:
+                return (one_plus(ti, ps, prev) - 1.0) / (pe - ps)
+            return ((fr(time, ns, pe) * (pe - ns) + 1.0) * one_plus(ti, ps, prev) - 1.0) / (pe - ps)
+        if psi + 1 == pei:
+            return osim.process_value(ti, psi)
+        acc = None
+        for k in range(psi, pei):
+            sub = tenor[k + 1] - tenor[k]
+            L = osim.process_value(ti, k)
+            acc = L * sub + 1.0 if acc is None else acc * (1 + L * sub)
+        return (acc - 1.0) / (pe - ps)
+
+    return fr(time, ps, pe)
+
+
+@pytest.mark.parametrize("method", ["LOG_LINEAR_UNCORRECTED", "LINEAR"])
+def test_forward_rates_primitive_accrued_and_interpolated(lmm20, method):
+    cfg, m, osim, sim = lmm20
+    old = sim.model.interpolationMethod
+    sim.model.interpolationMethod = method
+    try:
+        for (t, ps, pe) in ((2.0, 2.0, 2.5), (1.0, 1.0, 3.0), (1.0, 1.0, 1.75), (1.25, 1.25, 2.0), (1.25, 1.25, 1.5),
+                            (0.9, 1.2, 3.3), (5.0, 3.0, 3.5)):
+            g = sim.getForwardRate(t, ps, pe).getRealizations()
+            o = _forward_rate_numpy(osim, m, cfg, method, t, ps, pe)
+            assert np.max(np.abs(g - o) / np.abs(o)) <= 1e-12, (t, ps, pe)
+        # the model primitive is getLIBOR itself
+        assert np.array_equal(sim.getForwardRate(2.0, 2.0, 2.5).getRealizations(), sim.getLIBOR(4, 4))
+    finally:
+        sim.model.interpolationMethod = old
+    with pytest.raises(ValueError):
+        sim.model.interpolationMethod = "LOG_LINEAR_CORRECTED"
+        try:
+            sim.getForwardRate(1.0, 1.0, 1.75)
+        finally:
+            sim.model.interpolationMethod = old
