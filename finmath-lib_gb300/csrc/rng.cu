@@ -424,24 +424,20 @@ __device__ __forceinline__ void increments_loop(const RngParams& prm, uint32_t* 
     drain_tile<OutT>(tile, out, TF, K, P, ps + pt, ps, ts, pe, te, r0, rstep, dk);
 }
 
-__global__ void __launch_bounds__(kRngThreads, 2) mt_generate_kernel(const RngParams prm)
+// Chunk start states: the seeded state moved to word offset 2 v0 = c * stride by one GF(2)
+// jump per nonzero base-8 digit of the chunk index c, written to states[c][624].  Its own
+// kernel: the jump window (kJumpWindow words of shared memory) would otherwise cap the
+// generator at two blocks per SM.
+__global__ void __launch_bounds__(kRngThreads) mt_jump_kernel(const RngParams prm, uint32_t* states)
 {
-    // shared memory: the jump window (kJumpWindow words); afterwards the two state buffers
-    // (kStateWords words) followed by the increments tile
-    extern __shared__ __align__(16) uint32_t x[];
-    __shared__ unsigned long long tail_w[kMtN / 2];  // tail draws of a round, handled by consecutive lanes
-    __shared__ int2 tail_pos[kMtN / 2];               // their positions (path, step * F + factor)
-    __shared__ int tail_n;
+    extern __shared__ __align__(16) uint32_t x[];  // the jump window
     const int tid = threadIdx.x;
     const int64_t c = blockIdx.x;
-    const int64_t v0 = c * prm.chunk_values;
-    if (v0 >= prm.num_values) return;
-    const int64_t v1 = min(v0 + prm.chunk_values, prm.num_values);
-
+    if (c * prm.chunk_values >= prm.num_values) return;
     for (int i = tid; i < kMtN; i += kRngThreads) x[i] = prm.seeded[i];
     __syncthreads();
 
-    // ---- jump to word offset 2*v0 = c * stride: apply x^(d 8^j stride) for every nonzero
+    // jump to word offset 2*v0 = c * stride: apply x^(d 8^j stride) for every nonzero
     // base-8 digit d of c (position j)
     for (int j = 0; j < prm.ndigits; j++) {
         const int d = (int)((c >> (kJumpDigitBits * j)) & (kJumpBase - 1));
@@ -481,6 +477,25 @@ __global__ void __launch_bounds__(kRngThreads, 2) mt_generate_kernel(const RngPa
         __syncthreads();
     }
 
+    for (int i = tid; i < kMtN; i += kRngThreads) states[c * kMtN + i] = x[i];
+}
+
+__global__ void __launch_bounds__(kRngThreads, 3) mt_generate_kernel(const RngParams prm, const uint32_t* states)
+{
+    // shared memory: the two state buffers (kStateWords words) followed by the increments tile
+    extern __shared__ __align__(16) uint32_t x[];
+    __shared__ unsigned long long tail_w[kMtN / 2];  // tail draws of a round, handled by consecutive lanes
+    __shared__ int2 tail_pos[kMtN / 2];               // their positions (path, step * F + factor)
+    __shared__ int tail_n;
+    const int tid = threadIdx.x;
+    const int64_t c = blockIdx.x;
+    const int64_t v0 = c * prm.chunk_values;
+    if (v0 >= prm.num_values) return;
+    const int64_t v1 = min(v0 + prm.chunk_values, prm.num_values);
+
+    for (int i = tid; i < kMtN; i += kRngThreads) x[i] = states[c * kMtN + i];  // the chunk's start state
+    __syncthreads();
+
     if (prm.mode == 1) {
         increments_loop<double>(prm, x, tid, v0, v1, tail_w, tail_pos, &tail_n);
     } else if (prm.mode == 2) {
@@ -513,16 +528,17 @@ int plan_mt_generate(int64_t num_values, int values_per_path, int elem_bytes, Rn
     LMM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     // the increments tile: K paths x values_per_path, K x element = 128 bytes when it fits
     int kbytes = 128;
-    const size_t budget = 200 * 1024;
+    const size_t budget = 72 * 1024;  // three generator CTAs per SM
     if (values_per_path > 1) {
         while (kbytes > elem_bytes && (size_t)values_per_path * kbytes + kStateWords * 4 > budget) kbytes /= 2;
         if ((size_t)values_per_path * kbytes + kStateWords * 4 > budget)
             return fail(LMM_ERR_INVALID, "too many increments per path for the generator tile");
     }
     plan->tile_k = values_per_path > 1 ? kbytes / elem_bytes : 1;
-    const size_t tile_bytes = values_per_path > 1 ? (size_t)values_per_path * kbytes : 0;
-    plan->smem_bytes = (int)std::max<size_t>((size_t)kJumpWindow * 4, (size_t)kStateWords * 4 + tile_bytes);
+    const size_t tile_bytes = (size_t)values_per_path * plan->tile_k * elem_bytes;  // a one-path tile when 1 value per path
+    plan->smem_bytes = (int)((size_t)kStateWords * 4 + tile_bytes);
     LMM_CUDA(cudaFuncSetAttribute(mt_generate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 210 * 1024));
+    LMM_CUDA(cudaFuncSetAttribute(mt_jump_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kJumpWindow * 4));
     LMM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mt_generate_kernel, kRngThreads, plan->smem_bytes));
     const int resident = sms * (per_sm > 0 ? per_sm : 1);
     // one chunk per resident CTA, at least 4096 values per chunk
@@ -593,11 +609,17 @@ int launch_mt_generate(const RngLaunch& a, cudaStream_t s, int* num_launches)
             return fail(LMM_ERR_INVALID, "generator plan does not match the increments layout");
     }
     {
-        KernelTimer kt(K_MT_JUMP_GENERATE, s);
-        mt_generate_kernel<<<(unsigned)a.plan->chunks, kRngThreads, (size_t)a.plan->smem_bytes, s>>>(prm);
+        KernelTimer kt(K_MT_JUMP_GENERATE, s, 2);
+        uint32_t* states = nullptr;  // [chunks][624] chunk start states
+        LMM_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&states), sizeof(uint32_t) * kMtN * (size_t)a.plan->chunks, s));
+        mt_jump_kernel<<<(unsigned)a.plan->chunks, kRngThreads, (size_t)kJumpWindow * 4, s>>>(prm, states);
+        mt_generate_kernel<<<(unsigned)a.plan->chunks, kRngThreads, (size_t)a.plan->smem_bytes, s>>>(prm, states);
+        const cudaError_t e = cudaGetLastError();
+        cudaFreeAsync(states, s);
+        if (e != cudaSuccess) return cuda_fail(e, "generator launch");
         LMM_CUDA(cudaGetLastError());
     }
-    if (num_launches) (*num_launches)++;
+    if (num_launches) (*num_launches) += 2;
     return LMM_OK;
 }
 
