@@ -3,9 +3,9 @@
 // Same recurrence as paths_fp64.cu (EulerSchemeFromProcessModel.java:170-326 with the
 // spot drift of LIBORMarketModelFromCovarianceModel.java:1125-1191), but the path state
 // is kept as Y = log L in FP32 (the EULER form in log coordinates), the drift running
-// sums use FP32 FMAs, and exp / the measure-change ratio use the SFU (__expf,
-// __fdividef).  The numeraire accrual and its adjustment sums stay FP64, as do all
-// product arithmetic and payoff sums downstream.  The error against the FP64 form is
+// sums (carried with dt and the increments, G_k = dW_k + dt S_k) use FP32 FMAs, and exp /
+// the measure-change ratio use the SFU (__expf, __fdividef).  The numeraire accrual and
+// its adjustment sums stay FP64, as do the regression sums and payoff averages downstream.  The error against the FP64 form is
 // measured and reported, not assumed.
 //
 // GB300 layout: one thread per path, the forward vector in registers for all steps.  Each

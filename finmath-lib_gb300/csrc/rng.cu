@@ -6,14 +6,15 @@
 // dW[t][f][p] = NormalDistribution.inverseCumulativeDistribution(u) * sqrt(dt_t).
 //
 // GB300 design: the stream of V values (2 words each) is cut into one contiguous chunk
-// per CTA.  A CTA first moves the seeded state to its chunk start with GF(2) jump
-// polynomials (one per nonzero base-8 digit of its chunk index, at most three for 512
-// chunks; each jump is an XOR of windows of the raw word sequence held in shared
-// memory), then regenerates 624 words at a time
-// in three dependency phases (227/227/170 words) over a double-buffered state, and
-// converts word pairs to values.  Uniforms are bit-identical to the single stream.  The
-// increments leave through a shared-memory tile (increments_loop) so that each [t][f] row
-// is written in 128-byte segments although the stream runs path-major.
+// per resident generator CTA.  mt_jump_kernel moves the seeded state to each chunk start
+// with GF(2) jump polynomials (one per nonzero base-8 digit of the chunk index, at most
+// three for 512 chunks; each jump is an XOR of windows of the raw word sequence held in
+// shared memory) and writes the start states to HBM.  mt_generate_kernel (three CTAs per
+// SM) then regenerates 624 words at a time in three dependency phases (227/227/170 words)
+// over a double-buffered state and converts word pairs to values.  Uniforms are
+// bit-identical to the single stream.  The increments leave through a shared-memory tile
+// (increments_loop) so that each [t][f] row is written in 64-byte segments although the
+// stream runs path-major.
 //
 // This translation unit is compiled with -fmad=false.  The FP64 inverse normal, which the
 // GPU's narrow FP64 pipe bounds, evaluates the reference's rational functions with fused

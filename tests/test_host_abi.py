@@ -116,3 +116,35 @@ def _have_gpu():
 def test_gpu_entry_points_fail_loudly_without_gpu():
     with pytest.raises(F.CalculationException):
         F.mersenne_twister_uniforms(3141, 10)
+    from finmath_gb300.randomvariable import RandomVariableGPU
+    with pytest.raises(F.CalculationException):
+        RandomVariableGPU.from_array(0.0, np.ones(8))  # realizations live in GPU memory
+
+
+def test_deterministic_random_variables_on_the_host():
+    # operations on deterministic random variables run on the host with the reference's
+    # formulas (RandomVariableFromDoubleArray.java:743-1486): no GPU involved
+    from finmath_gb300.randomvariable import RandomVariableGPU as RV
+    a = RV.constant(0.5, 0.04)
+    assert a.mult(0.5).add(1.0).doubleValue() == 0.04 * 0.5 + 1.0
+    assert a.isDeterministic() and a.size() == 1
+    assert a.getAverage() == 0.04 and a.getVariance() == 0.0 and a.getStandardError() == 0.0
+    assert a.mult(RV.constant(2.0, 1.0)).getFiltrationTime() == 2.0  # the later filtration time
+    # Math.min / Math.max: NaN wins, -0.0 < +0.0
+    z, nz = RV.constant(0.0, 0.0), RV.constant(0.0, -0.0)
+    m = z.cap(nz).doubleValue()
+    assert m == 0.0 and np.signbit(m)
+    M = nz.floor(z).doubleValue()
+    assert M == 0.0 and not np.signbit(M)
+    assert np.isnan(RV.constant(0.0, float("nan")).cap(1.0).doubleValue())
+    # Math.pow's special cases where C's pow differs
+    assert np.isnan(RV.constant(0.0, 1.0).pow(float("nan")).doubleValue())
+    assert np.isnan(RV.constant(0.0, -1.0).pow(float("inf")).doubleValue())
+    assert RV.constant(0.0, 2.0).pow(10.0).doubleValue() == 1024.0
+    assert a.accrue(RV.constant(0.0, 0.03), 0.5).doubleValue() == 0.04 * (1 + 0.03 * 0.5)
+    assert a.discount(RV.constant(0.0, 0.03), 0.5).doubleValue() == 0.04 / (1.0 + 0.03 * 0.5)
+    assert a.choose(RV.constant(0.0, 1.0), RV.constant(0.0, 2.0)).doubleValue() == 1.0
+    assert a.addRatio(RV.constant(0.0, 1.0), RV.constant(0.0, 3.0)).doubleValue() == 0.04 + 1.0 / 3.0
+    assert RV.constant(0.0, float("nan")).isNaN().doubleValue() == 1.0
+    with pytest.raises(ValueError):
+        a._scalar(99)  # unknown operation
