@@ -287,7 +287,7 @@ def run_ours(args):
                 "ncu_fp64_pipe_active": _from_profile("fp64_pipe_active") if prec == F.PRECISION_FP64 else None,
                 "note": "algorithmic flops count the reference algorithm's add/mul per component-step (its "
                         "log, exp and division as one each); the FP64 kernel fuses them into FMAs, evaluates "
-                        "the log-Euler step as L exp(d) with a table-driven 12-FMA exp and replaces the "
+                        "the log-Euler step as L exp(d) with a table-driven 9-instruction exp and replaces the "
                         "division by a 4-FMA Newton reciprocal, and is FP64-pipe bound "
                         "(ncu, profiles/lmm_paths_fp64_lmm40.md)"}
 

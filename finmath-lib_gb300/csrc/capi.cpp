@@ -188,7 +188,7 @@ struct lmm_process {
     // device tables
     double *d_loadings = nullptr, *d_variance = nullptr, *d_dt = nullptr, *d_delta = nullptr, *d_init = nullptr;
     double* d_exp_tab = nullptr;
-    double *d_inv_delta = nullptr, *d_var_half = nullptr;
+    double *d_inv_delta = nullptr, *d_var_half_dt = nullptr;
     float *d_lam32 = nullptr, *d_var32 = nullptr, *d_inv_delta32 = nullptr, *d_dt32 = nullptr, *d_init_log32 = nullptr;
     int *d_first = nullptr, *d_obs_slot = nullptr, *d_tenor_tidx = nullptr;
     uint8_t* d_det = nullptr;
@@ -474,17 +474,20 @@ int lmm_process_create(const lmm_model_desc* m, lmm_brownian* bm, lmm_process** 
         }
     }
     for (size_t i = 0; i < var_half.size(); i++) var_half[i] = m->variance[i] * -0.5;
+    std::vector<double> var_half_dt(var_half.size());  // the same product the path kernel took per component
+    for (int i = 0; i < T; i++)
+        for (int j = 0; j < N; j++) var_half_dt[(size_t)i * N + j] = var_half[(size_t)i * N + j] * dt[i];
     cudaStream_t s = pr->stream;
     int rc = 0;
     if (!rc) rc = upload(&pr->d_loadings, m->factor_loadings, (size_t)T * N * F, s);
     if (!rc) rc = upload(&pr->d_variance, m->variance, (size_t)T * N, s);
     if (!rc) rc = upload(&pr->d_dt, dt.data(), dt.size(), s);
     if (!rc) rc = upload(&pr->d_delta, delta.data(), delta.size(), s);
-    std::vector<double> etab(129);  // lives until the stream synchronisation below
+    std::vector<double> etab(2 * kExpTableHalf + 1);  // lives until the stream synchronisation below
     fp64_exp_table(etab.data());
     if (!rc) rc = upload(&pr->d_exp_tab, etab.data(), etab.size(), s);
     if (!rc) rc = upload(&pr->d_inv_delta, inv_delta.data(), inv_delta.size(), s);
-    if (!rc) rc = upload(&pr->d_var_half, var_half.data(), var_half.size(), s);
+    if (!rc) rc = upload(&pr->d_var_half_dt, var_half_dt.data(), var_half_dt.size(), s);
     if (!rc) rc = upload(&pr->d_init, m->initial_forwards, (size_t)N, s);
     if (!rc) rc = upload(&pr->d_first, pr->first.data(), pr->first.size(), s);
     if (!rc) rc = upload(&pr->d_det, pr->num_det.data(), pr->num_det.size(), s);
@@ -570,7 +573,7 @@ static int process_ensure(lmm_process* pr)
     a.d_delta = pr->d_delta;
     a.d_exp_tab = pr->d_exp_tab;
     a.d_inv_delta = pr->d_inv_delta;
-    a.d_var_half = pr->d_var_half;
+    a.d_var_half_dt = pr->d_var_half_dt;
     a.d_inv_delta32 = pr->d_inv_delta32;
     a.d_dt32 = pr->d_dt32;
     a.d_init_log32 = pr->d_init_log32;
@@ -695,7 +698,7 @@ int lmm_process_destroy(lmm_process* pr)
     dfree(pr->d_delta, s);
     dfree(pr->d_exp_tab, s);
     dfree(pr->d_inv_delta, s);
-    dfree(pr->d_var_half, s);
+    dfree(pr->d_var_half_dt, s);
     dfree(pr->d_init, s);
     dfree(pr->d_lam32, s);
     dfree(pr->d_var32, s);

@@ -116,11 +116,11 @@ struct PathLaunch {
     const int* d_first;        // [T] first alive component at t_i
     const double* d_delta;     // [N] period lengths
     const double* d_inv_delta; // [N] 1.0 / delta (delta/delta == 1.0 exactly for the validated tenor)
-    const double* d_var_half;  // [T][N] variance * -0.5 (exact scaling)
+    const double* d_var_half_dt; // [T][N] (variance * -0.5) * dt_i, the drift's deterministic part of a step
     const float* d_inv_delta32;// [N] 1/delta in FP32 (mixed form)
     const float* d_dt32;       // [T] time steps in FP32 (mixed form)
     const float* d_init_log32; // [N] log of the initial forwards in FP32 (mixed form)
-    const double* d_exp_tab;   // [129] exp(k/64), k = -64..64 (FP64 form, see fp64math.cuh)
+    const double* d_exp_tab;   // [2 kExpTableHalf + 1] exp(k/kExpTableHalf) (FP64 form, see fp64math.cuh)
     const double* d_init;      // [N] initial forwards
     const int* d_obs_slot;     // [T+1] observation slot or -1
     const void* d_dw;          // [T][F][P] fp64 or fp32
@@ -137,8 +137,10 @@ int launch_paths_fp64(const PathLaunch& a, cudaStream_t s, int* blocks_out);
 int paths_fp32_pitch(int N, int F);
 int launch_paths_fp32(const PathLaunch& a, const float* lam32, const float* var32, cudaStream_t s, int* blocks_out);
 int path_blocks(int P);
-// exp(k/64) for k = -64..64, rounded to FP64 from extended precision (the table of exp_small)
-void fp64_exp_table(double out[129]);
+// exp(k/kExpTableHalf) for |k| <= kExpTableHalf, rounded to FP64 from extended precision
+// (the table of exp_small in fp64math.cuh)
+constexpr int kExpTableHalf = 256;
+void fp64_exp_table(double out[2 * kExpTableHalf + 1]);
 
 // device random variables (randomvariable.cu) from process buffers: a copy (FP32 states
 // widened) or the adjusted numeraire, ordered after the work so far on src_stream

@@ -20,7 +20,7 @@
 //    along (G_k = dW_k + dt S_k), so that a component costs 2F FMAs instead of 3F;
 //  * the Euler-log step exp(log L + d) (EULER_FUNCTIONAL) is evaluated as L exp(d), and the
 //    EULER step exp(Y + d) as exp(Y) exp(d) with exp(Y) carried instead of Y, where exp(d)
-//    of the small step increment d is exp_small (fp64math.cuh) -- no log, and a 12-FMA exp;
+//    of the small step increment d is exp_small (fp64math.cuh) -- no log, and a 9-instruction exp;
 //  * the drift's L / (L + 1/delta) takes a Newton reciprocal (rcp_newton) for the division.
 // The states agree with the reference's order to about 1e-14 relative, inside the 1e-12
 // parity bound.  The general kernel keeps the reference's literal order throughout
@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp64_kernel(const PathLaun
         const int first = __ldg(a.d_first + i);
         const double dt = __ldg(a.d_dt + i);
         const double* lam = a.d_loadings + (size_t)i * N * F;
-        const double* var_half = a.d_var_half + (size_t)i * N;
+        const double* var_half_dt = a.d_var_half_dt + (size_t)i * N;
         double dw[FMAX];
 #pragma unroll
         for (int k = 0; k < FMAX; k++) dw[k] = (k < F && active) ? dW[((size_t)i * F + k) * P + p] : 0.0;
@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp64_kernel(const PathLaun
                 // Euler step (EulerSchemeFromProcessModel.java:235-255) with the drift of
                 // :1159 and :1183-1189 (variance * -0.5): the increment d of the log state,
                 // then L exp(d) (FUNCTIONAL: log L is the state) or exp(Y) exp(d) (EULER)
-                double d = __ldg(var_half + j) * dt;
+                double d = __ldg(var_half_dt + j);  // (variance * -0.5) * dt, from the host
 #pragma unroll
                 for (int k = 0; k < FMAX; k++)
                     if (k < F) d = fma(G[k], lj[k], d);
