@@ -2,8 +2,8 @@
 //
 // These are the pieces of finmath-lib that run once per model on the host: time grids
 // with tick rounding, exponential-decay correlation and its factor reduction, the
-// four-parameter volatility, covariance tables, forward/discount curves and the
-// deterministic numeraire-adjustment chain.  A Java shim can take the same tables from
+// four-parameter volatility, covariance tables, forward/discount curves, the
+// deterministic numeraire-adjustment chain, and the small SVD solve of a regression.  A Java shim can take the same tables from
 // finmath's own objects; C/C++/Python callers use these.  Compiled without FMA
 // contraction (-ffp-contract=off), as the reference's Java never fuses.
 #include <algorithm>
@@ -93,9 +93,77 @@ void factor_matrix(const double* corr, int n, int F, double* out)
     }
 }
 
+// A = U diag(s) V^T of a square n x n matrix by one-sided Jacobi rotations on the columns
+// of U (initially A), V accumulating the rotations; s the column norms, U normalised.
+void svd_jacobi(int n, const double* A, std::vector<double>& U, std::vector<double>& s, std::vector<double>& V)
+{
+    U.assign(A, A + (size_t)n * n);
+    V.assign((size_t)n * n, 0.0);
+    for (int i = 0; i < n; i++) V[(size_t)i * n + i] = 1.0;
+    for (int sweep = 0; sweep < 60; sweep++) {
+        bool rotated = false;
+        for (int p = 0; p < n - 1; p++)
+            for (int q = p + 1; q < n; q++) {
+                double alpha = 0.0, beta = 0.0, gamma = 0.0;
+                for (int k = 0; k < n; k++) {
+                    const double up = U[(size_t)k * n + p], uq = U[(size_t)k * n + q];
+                    alpha += up * up;
+                    beta += uq * uq;
+                    gamma += up * uq;
+                }
+                if (gamma == 0.0 || std::fabs(gamma) <= 0x1.0p-52 * std::sqrt(alpha * beta)) continue;
+                rotated = true;
+                const double zeta = (beta - alpha) / (2.0 * gamma);
+                const double t = (zeta >= 0.0 ? 1.0 : -1.0) / (std::fabs(zeta) + std::sqrt(1.0 + zeta * zeta));
+                const double cs = 1.0 / std::sqrt(1.0 + t * t), sn = cs * t;
+                for (int k = 0; k < n; k++) {
+                    const double up = U[(size_t)k * n + p], uq = U[(size_t)k * n + q];
+                    U[(size_t)k * n + p] = cs * up - sn * uq;
+                    U[(size_t)k * n + q] = sn * up + cs * uq;
+                    const double vp = V[(size_t)k * n + p], vq = V[(size_t)k * n + q];
+                    V[(size_t)k * n + p] = cs * vp - sn * vq;
+                    V[(size_t)k * n + q] = sn * vp + cs * vq;
+                }
+            }
+        if (!rotated) break;
+    }
+    s.assign(n, 0.0);
+    for (int j = 0; j < n; j++) {
+        double nn = 0.0;
+        for (int k = 0; k < n; k++) nn += U[(size_t)k * n + j] * U[(size_t)k * n + j];
+        s[j] = std::sqrt(nn);
+        if (s[j] > 0.0)
+            for (int k = 0; k < n; k++) U[(size_t)k * n + j] = U[(size_t)k * n + j] / s[j];
+    }
+}
+
 }  // namespace
 
 extern "C" {
+
+int lmm_solve_svd(int n, const double* A, const double* b, double* x)
+{
+    if (!A || !b || !x || n < 1 || n > 64) return lmm::fail(LMM_ERR_INVALID, "lmm_solve_svd: bad arguments (1 <= n <= 64)");
+    std::vector<double> U, s, V;
+    svd_jacobi(n, A, U, s, V);
+    double smax = 0.0;
+    for (int j = 0; j < n; j++) smax = std::max(smax, s[j]);
+    // the solver's cutoff: max(n sigma_max 2^-52, sqrt(the smallest normal double))
+    const double tol = std::max((double)n * smax * 0x1.0p-52, std::sqrt(0x1.0p-1022));
+    std::vector<double> w(n, 0.0);
+    for (int j = 0; j < n; j++) {
+        if (!(s[j] > tol)) continue;
+        double utb = 0.0;
+        for (int r = 0; r < n; r++) utb += U[(size_t)r * n + j] * b[r];
+        w[j] = utb / s[j];
+    }
+    for (int i = 0; i < n; i++) {
+        double acc = 0.0;
+        for (int j = 0; j < n; j++) acc += V[(size_t)i * n + j] * w[j];
+        x[i] = acc;
+    }
+    return LMM_OK;
+}
 
 int lmm_time_discretization(double initial, int num_steps, double dt, double* out_times)
 {

@@ -12,7 +12,7 @@ from .lmm import (TimeDiscretizationFromArray, ForwardCurveInterpolation, Discou
                   LIBORMarketModelFromCovarianceModel, BrownianMotionFromMersenneRandomNumbers,
                   EulerSchemeFromProcessModel, LIBORMonteCarloSimulationFromLIBORModel, Swaption, BermudanSwaption, Portfolio,
                   mersenne_twister_uniforms, kernel_stats)
-from .randomvariable import RandomVariableGPU, RandomVariableGPUFactory
+from .randomvariable import RandomVariableGPU, RandomVariableGPUFactory, MonteCarloConditionalExpectationRegression
 from . import workloads, autotune
 
 __all__ = [n for n in dir() if not n.startswith("_")]

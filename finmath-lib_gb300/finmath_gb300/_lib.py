@@ -72,6 +72,7 @@ SIGNATURES = {
     "lmm_forward_curve_value": (ctypes.c_int, [_D, _D, ctypes.c_int, ctypes.c_double, _D]),
     "lmm_discount_factor_from_forward_curve": (ctypes.c_int, [_D, _D, ctypes.c_int, ctypes.c_double, ctypes.c_double, _D]),
     "lmm_numeraire_discount_chain": (ctypes.c_int, [_D, ctypes.c_int, _D, _D]),
+    "lmm_solve_svd": (ctypes.c_int, [ctypes.c_int, _D, _D, _D]),
     "lmm_brownian_create": (ctypes.c_int, [_D, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                            ctypes.POINTER(_VP)]),
     "lmm_brownian_get_increment": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, _D]),

@@ -115,6 +115,10 @@ class RandomVariableGPU:
     def average(self) -> "RandomVariableGPU":
         return RandomVariableGPU.constant(0.0, self.getAverage())
 
+    def getConditionalExpectation(self, conditionalExpectationOperator):
+        """RandomVariableFromDoubleArray.getConditionalExpectation: the estimator's estimate of this."""
+        return conditionalExpectationOperator.getConditionalExpectation(self)
+
     # -- operations
     def _scalar(self, op, y=0.0) -> "RandomVariableGPU":
         h = ctypes.c_void_p()
@@ -195,3 +199,46 @@ class RandomVariableGPUFactory:
         if np.ndim(value) == 0:
             return RandomVariableGPU.constant(time, value)
         return RandomVariableGPU.from_array(time, value)
+
+
+class MonteCarloConditionalExpectationRegression:
+    """MonteCarloConditionalExpectationRegression (montecarlo/conditionalexpectation/
+    MonteCarloConditionalExpectationRegression.java:79-150) over device random variables: the
+    scalar products X^T X and X^T y as compensated averages of products on the GPU, the
+    small system solved by the library's SVD pseudo-inverse (lmm_solve_svd, the reference's
+    commons-math solver and cutoff), and the estimate X beta as the reference builds it
+    (mult, then addProduct per basis function)."""
+
+    def __init__(self, basisFunctions, basisFunctionsPredictor=None):
+        self._est = [b for b in basisFunctions if b is not None]
+        self._pred = self._est if basisFunctionsPredictor is None else [b for b in basisFunctionsPredictor if b is not None]
+        self._xtx = None
+
+    def getLinearRegressionParameters(self, dependents: "RandomVariableGPU") -> np.ndarray:
+        b = self._est
+        n = len(b)
+        if self._xtx is None:  # the reference caches its solver per estimator
+            xtx = np.empty((n, n))
+            for i in range(n):
+                for j in range(i, n):
+                    prod = b[i].mult(b[j])
+                    xtx[i, j] = xtx[j, i] = prod.getAverage()
+                    prod.close()
+            self._xtx = np.ascontiguousarray(xtx)
+        xty = np.empty(n)
+        for i in range(n):
+            prod = dependents.mult(b[i])
+            xty[i] = prod.getAverage()
+            prod.close()
+        x = np.empty(n)
+        dp = ctypes.POINTER(ctypes.c_double)
+        check(load().lmm_solve_svd(n, self._xtx.ctypes.data_as(dp), xty.ctypes.data_as(dp), x.ctypes.data_as(dp)),
+              "getLinearRegressionParameters")
+        return x
+
+    def getConditionalExpectation(self, randomVariable: "RandomVariableGPU") -> "RandomVariableGPU":
+        beta = self.getLinearRegressionParameters(randomVariable)
+        ce = self._pred[0].mult(float(beta[0]))
+        for i in range(1, len(self._pred)):
+            ce = ce.addProduct(self._pred[i], float(beta[i]))
+        return ce

@@ -105,6 +105,13 @@ int lmm_discount_factor_from_forward_curve(const double* nodes, const double* va
 int lmm_numeraire_discount_chain(const double* tenor, int num_periods, const double* discount_factors,
                                  double* out_chain);
 
+/* x solving A x = b (A n x n, row-major) by the SVD pseudo-inverse with the cutoff
+ * max(n sigma_max 2^-52, sqrt(2^-1022)): new SingularValueDecomposition(A).getSolver().solve(b)
+ * as MonteCarloConditionalExpectationRegression.getLinearRegressionParameters uses it
+ * (montecarlo/conditionalexpectation/MonteCarloConditionalExpectationRegression.java:125-147,
+ * commons-math3 3.6.1).  Host computation, n <= 64. */
+int lmm_solve_svd(int n, const double* A, const double* b, double* x);
+
 /* ---------------------------------------------------------------- Brownian motion */
 typedef struct lmm_brownian lmm_brownian;
 

@@ -269,3 +269,27 @@ def test_forward_rates_primitive_accrued_and_interpolated(lmm20, method):
             sim.getForwardRate(1.0, 1.0, 1.75)
         finally:
             sim.model.interpolationMethod = old
+
+
+def test_conditional_expectation_regression():
+    # MonteCarloConditionalExpectationRegression on device random variables against the same
+    # scalar products (Kahan averages of IEEE products) and the oracle's pseudo-inverse
+    rng = np.random.default_rng(3)
+    n = 50_001
+    s = rng.normal(0.05, 0.01, n)
+    y = np.maximum(s - 0.05, 0.0) + rng.normal(0.0, 0.002, n)
+    X = [np.ones(n), s, s * s, s * s * s]
+    basis = [F.RandomVariableGPU.constant(1.0, 1.0), RV.from_array(1.0, s), RV.from_array(1.0, s * s),
+             RV.from_array(1.0, s * s * s)]
+    est = F.MonteCarloConditionalExpectationRegression(basis)
+    Y = RV.from_array(2.0, y)
+    beta = est.getLinearRegressionParameters(Y)
+    xtx = np.array([[po.kahan_average(X[i] * X[j]) for j in range(4)] for i in range(4)])
+    xty = np.array([po.kahan_average(y * X[i]) for i in range(4)])
+    ref = po.lstsq_pinv(xtx, xty)
+    fit_ref = ref[0] * X[0]
+    for i in range(1, 4):
+        fit_ref = fit_ref + X[i] * ref[i]
+    fit = Y.getConditionalExpectation(est).getRealizations()
+    assert np.max(np.abs(fit - fit_ref)) <= 1e-9 * np.max(np.abs(fit_ref))
+    assert np.max(np.abs(beta - ref) / np.maximum(np.abs(ref), 1.0)) <= 1e-6  # beta is ill-determined, the fit is not

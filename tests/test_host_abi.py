@@ -148,3 +148,18 @@ def test_deterministic_random_variables_on_the_host():
     assert RV.constant(0.0, float("nan")).isNaN().doubleValue() == 1.0
     with pytest.raises(ValueError):
         a._scalar(99)  # unknown operation
+
+
+@pytest.mark.parametrize("n,rank", [(1, 1), (4, 4), (6, 6), (6, 4), (12, 9)])
+def test_svd_solve_matches_the_pinned_pseudo_inverse(n, rank):
+    # lmm_solve_svd: the regression's SVD solver (cutoff max(n s_max 2^-52, sqrt(2^-1022)))
+    # against the oracle's pseudo-inverse, pinned by finmath's LinearAlgebraTest KATs
+    rng = np.random.default_rng(n * 100 + rank)
+    B = rng.normal(size=(n, rank))
+    A = np.ascontiguousarray(B @ B.T + (0.0 if rank < n else 0.05) * np.eye(n))
+    b = rng.normal(size=n)
+    x = np.empty(n)
+    dp = ctypes.POINTER(ctypes.c_double)
+    assert F.load().lmm_solve_svd(n, A.ctypes.data_as(dp), b.ctypes.data_as(dp), x.ctypes.data_as(dp)) == 0
+    ref = po.lstsq_pinv(A, b)
+    assert np.max(np.abs(x - ref)) <= 1e-10 * max(1.0, np.max(np.abs(ref)))
