@@ -293,3 +293,35 @@ def test_conditional_expectation_regression():
     fit = Y.getConditionalExpectation(est).getRealizations()
     assert np.max(np.abs(fit - fit_ref)) <= 1e-9 * np.max(np.abs(fit_ref))
     assert np.max(np.abs(beta - ref) / np.maximum(np.abs(ref), 1.0)) <= 1e-6  # beta is ill-determined, the fit is not
+
+
+def test_bermudan_written_against_the_random_variable_api_equals_the_fused_kernel(lmm20):
+    # BermudanSwaption.getValues (montecarlo/interestrate/products/BermudanSwaption.java:91-157)
+    # with its built-in basis (:215-252), written only against getForwardRate / getNumeraire
+    # random variables and the regression estimator, against the fused Bermudan kernel on the
+    # same simulation
+    cfg, m, osim, sim = lmm20
+    fix, plen, pay, K = W.bermudan_schedule(cfg)
+    P = sim.getNumberOfPaths()
+    w = 1.0 / P
+    values = F.RandomVariableGPU.constant(0.0, 0.0)
+    under = F.RandomVariableGPU.constant(0.0, 0.0)
+    for period in range(len(fix) - 1, -1, -1):
+        f, dt, p = fix[period], plen[period], pay[period]
+        libor = sim.getForwardRate(f, f, f + dt)
+        payoff = libor.sub(K).mult(dt).mult(1.0).div(sim.getNumeraireRandomVariable(p)).mult(w)
+        under = under.add(payoff)  # callable
+        # the built-in basis at the exercise date (the fixing date)
+        i = int(np.searchsorted(fix, f))
+        ds = sim.getForwardRate(f, f, pay[i]).mult(pay[i] - f).add(1.0).invert()
+        dl = sim.getForwardRate(f, fix[i], pay[-1]).mult(pay[-1] - fix[i]).add(1.0).invert()
+        basis = [F.RandomVariableGPU.constant(0.0, 1.0), ds, ds.pow(2.0), dl, dl.pow(2.0),
+                 sim.getNumeraireRandomVariable(f).invert()]
+        trigger = values.sub(under).getConditionalExpectation(F.MonteCarloConditionalExpectationRegression(basis))
+        values = trigger.choose(values, under)
+    values = values.mult(sim.getNumeraireRandomVariable(0.0)).div(w)
+    fused = F.BermudanSwaption(np.ones(len(fix)), fix, plen, pay, 1.0, K, True, None).getValues(sim, per_path=True)
+    assert values.getAverage() == pytest.approx(fused["value"], rel=1e-12)
+    assert values.getStandardError() == pytest.approx(fused["error"], rel=1e-10)
+    got = values.getRealizations()
+    assert np.max(np.abs(got - fused["values"])) <= 1e-12 * np.max(np.abs(fused["values"]))
