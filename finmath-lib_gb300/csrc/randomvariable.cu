@@ -194,16 +194,16 @@ int dispatch(int op, const Operand& x, const Operand& a, const Operand& b, doubl
     return LMM_OK;
 }
 
-// block partial sums of x, or of (x - center)^2 when centered: each thread runs the
+// block partial sums of x, or of (x - m)^2 when centered: each thread runs the
 // reference's Kahan loop over its elements (four FP64 operations per value; this GPU's
 // FP64 pipe, not HBM, bounds a reduction), the threads' (sum, -compensation) pairs are
 // merged as double-doubles in a fixed tree
-__global__ void __launch_bounds__(kRvThreads) rv_sum_kernel(const double* x, int64_t n, const double* center, double* partials)
+__global__ void __launch_bounds__(kRvThreads) rv_sum_kernel(const double* x, int64_t n, int centered, double m,
+                                                            double* partials)
 {
     double sum = 0.0, err = 0.0;
-    const double m = center ? *center : 0.0;
     for (int64_t i = (int64_t)blockIdx.x * kRvThreads + threadIdx.x; i < n; i += (int64_t)gridDim.x * kRvThreads) {
-        const double v = (center ? (x[i] - m) * (x[i] - m) : x[i]) - err;
+        const double v = (centered ? (x[i] - m) * (x[i] - m) : x[i]) - err;
         const double t = sum + v;
         err = (t - sum) - v;
         sum = t;
@@ -476,12 +476,12 @@ int lmm_rv_apply3(const lmm_rv* x, int op, const lmm_rv* a, const lmm_rv* b, dou
     return apply_any(x, op, a, b, c, b != nullptr, out);
 }
 
-static int reduce_sum(const lmm_rv* x, const double* center, double* out)
+static int reduce_sum(const lmm_rv* x, bool centered, double center, double* out)
 {
     const int blocks = (int)std::min<int64_t>((x->n + kRvThreads - 1) / kRvThreads, 1024);
     double* scratch = nullptr;
     LMM_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&scratch), sizeof(double) * (2 * (size_t)blocks + 1), rv_stream()));
-    rv_sum_kernel<<<blocks, kRvThreads, 0, rv_stream()>>>(x->d, x->n, center, scratch);
+    rv_sum_kernel<<<blocks, kRvThreads, 0, rv_stream()>>>(x->d, x->n, centered ? 1 : 0, center, scratch);
     rv_finish_kernel<<<1, kRvThreads, 0, rv_stream()>>>(scratch, blocks, x->n, scratch + 2 * blocks);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpyAsync(out, scratch + 2 * blocks, sizeof(double), cudaMemcpyDeviceToHost, rv_stream());
@@ -497,7 +497,7 @@ int lmm_rv_average(const lmm_rv* x, double* out)
         *out = x->value;
         return LMM_OK;
     }
-    return reduce_sum(x, nullptr, out);
+    return reduce_sum(x, false, 0.0, out);
 }
 
 int lmm_rv_variance(const lmm_rv* x, double* out)
@@ -508,15 +508,9 @@ int lmm_rv_variance(const lmm_rv* x, double* out)
         return LMM_OK;
     }
     double avg = 0.0;
-    int rc = reduce_sum(x, nullptr, &avg);
+    const int rc = reduce_sum(x, false, 0.0, &avg);  // getVariance centres on getAverage (two passes)
     if (rc) return rc;
-    double* d_avg = nullptr;
-    LMM_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&d_avg), sizeof(double), rv_stream()));
-    cudaError_t e = cudaMemcpyAsync(d_avg, &avg, sizeof(double), cudaMemcpyHostToDevice, rv_stream());
-    if (e == cudaSuccess) rc = reduce_sum(x, d_avg, out);
-    cudaFreeAsync(d_avg, rv_stream());
-    if (e != cudaSuccess) return cuda_fail(e, "random-variable variance");
-    return rc;
+    return reduce_sum(x, true, avg, out);
 }
 
 int lmm_rv_standard_error(const lmm_rv* x, double* out)

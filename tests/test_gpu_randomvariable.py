@@ -163,6 +163,13 @@ def test_caplets_and_swap_through_the_random_variable_api(lmm20):
         o = o / osim.numeraire(T_pay) * w * N0o / w
         assert g.getAverage() == pytest.approx(po.kahan_average(o), rel=1e-12)
         assert g.getStandardError() == pytest.approx(po.standard_error(o), rel=1e-10)
+    # the library's Caplet (Caplet.java's operations) is the same computation
+    j, K = 9, 0.05
+    t = int(round(j * period / dt))
+    o = np.maximum(osim.process_value(t, j) - K, 0.0) * period / osim.numeraire((j + 1) * period) * w * N0o / w
+    assert F.Caplet(j * period, period, K).getValue(sim) == pytest.approx(po.kahan_average(o), rel=1e-12)
+    of = -np.minimum(osim.process_value(t, j) - K, 0.0) * period / osim.numeraire((j + 1) * period) * w * N0o / w
+    assert F.Caplet(j * period, period, K, isFloorlet=True).getValue(sim) == pytest.approx(po.kahan_average(of), rel=1e-12)
     # a payer swap: sum over periods of (L_j(T_j) - K) delta / N(T_{j+1})
     K = 0.05
     g = F.RandomVariableGPU.constant(0.0, 0.0)
@@ -173,6 +180,13 @@ def test_caplets_and_swap_through_the_random_variable_api(lmm20):
         g = g.addRatio(sim.getLIBORRandomVariable(t, j).sub(K).mult(period), N)
         o = o + (osim.process_value(t, j) - K) * period / osim.numeraire((j + 1) * period)
     assert g.getAverage() == pytest.approx(po.kahan_average(o), rel=1e-12)
+    fixes = [j * period for j in range(2, 12)]
+    swap = F.SimpleSwap(fixes, [x + period for x in fixes], [K] * len(fixes))
+    ref = po.kahan_average(o * N0o)  # the same sum, times N(0), as SimpleSwap.java values it
+    scale = po.kahan_average(np.abs(o * N0o))  # an at-the-money swap: cancellation in the sum
+    assert swap.getValue(sim) == pytest.approx(ref, rel=1e-12, abs=1e-13 * scale)
+    receiver = F.SimpleSwap(fixes, [x + period for x in fixes], [K] * len(fixes), isPayFix=False)
+    assert receiver.getValue(sim) == pytest.approx(-ref, rel=1e-12, abs=1e-13 * scale)
 
 
 def test_process_values_as_random_variables_match_host_copies():
