@@ -3,7 +3,7 @@
 //
 // Device memory comes from the stream-ordered allocator with the default pool's release
 // threshold raised, so repeated create/destroy cycles (one per valuation in a service)
-// reuse HBM instead of returning it to the driver.
+// reuse HBM instead of returning it to the CUDA driver.
 #include <algorithm>
 #include <atomic>
 #include <cmath>

@@ -1,6 +1,7 @@
 // probe.cu -- FP64 FMA throughput probe.  The plain-FP64 path kernel is bound by the
-// FP64 pipe, whose rate is not part of the measured peaks; this kernel measures
-// it on the running GPU (independent DFMA chains, enough warps to saturate the pipe).
+// FP64 pipe, whose rate is not among the separately measured peaks (copy bandwidth, bf16
+// GEMM); this kernel measures it on the running GPU (independent DFMA chains, enough
+// warps to saturate the pipe).
 #include <algorithm>
 #include <cmath>
 #include <vector>
