@@ -13,7 +13,8 @@ from .lmm import (TimeDiscretizationFromArray, ForwardCurveInterpolation, Discou
                   EulerSchemeFromProcessModel, LIBORMonteCarloSimulationFromLIBORModel, Swaption, BermudanSwaption, Portfolio,
                   mersenne_twister_uniforms, kernel_stats)
 from .randomvariable import RandomVariableGPU, RandomVariableGPUFactory, MonteCarloConditionalExpectationRegression
-from .rvproducts import Caplet, SimpleSwap
+from .rvproducts import (Bond, Caplet, DigitalCaplet, DigitalFloorlet, LIBORBond, MoneyMarketAccount, SimpleSwap,
+                         SimpleZeroSwap)
 from . import workloads, autotune
 
 __all__ = [n for n in dir() if not n.startswith("_")]

@@ -51,6 +51,8 @@ class TimeDiscretizationFromArray:
         return len(self._t) - 1
 
     def getTime(self, i):
+        if i < 0:  # Java arrays do not wrap
+            raise IndexError(f"time index {i} out of range")
         return float(self._t[i])
 
     def getTimeStep(self, i):
@@ -382,8 +384,9 @@ class LIBORMonteCarloSimulationFromLIBORModel:
     def getForwardRate(self, time, periodStart, periodEnd):
         """LIBORMarketModelFromCovarianceModel.getForwardRate (…/models/LIBORMarketModelFromCovarianceModel.java:1238-1305)
         as device random variables: the model primitive L_j(t), the accrual over several tenor
-        periods, or an off-tenor period by the model's interpolationMethod (:1318-1381; LINEAR
-        and LOG_LINEAR_UNCORRECTED with the analytic forward-curve adjustment)."""
+        periods, or an off-tenor period by the model's interpolationMethod (:1318-1381; LINEAR,
+        LOG_LINEAR_UNCORRECTED and LOG_LINEAR_CORRECTED, each with the analytic forward-curve
+        adjustment)."""
         m = self.model
         tenor, td = m.liborPeriodDiscretization, self.process.getTimeDiscretization()
         ps_i, pe_i = tenor.getTimeIndex(periodStart), tenor.getTimeIndex(periodEnd)
@@ -435,6 +438,10 @@ class LIBORMonteCarloSimulationFromLIBORModel:
             interp = long_.mult(alpha).add(1 - alpha)
         elif m.interpolationMethod == "LOG_LINEAR_UNCORRECTED":
             interp = long_.log().mult(alpha).exp()
+        elif m.interpolationMethod == "LOG_LINEAR_CORRECTED":
+            adjustmentCoefficient = 0.5 * small * (ts - periodStartTime)
+            adjustment = self._interpolationDriftAdjustment(ti, idx).mult(adjustmentCoefficient)
+            interp = long_.log().mult(alpha).sub(adjustment).exp()
         else:
             raise ValueError(f"interpolation method {m.interpolationMethod} is not supported")
         fc = m.forwardRateCurve
@@ -442,6 +449,46 @@ class LIBORMonteCarloSimulationFromLIBORModel:
         a_short = 1 + fc.getForward(None, periodStartTime, small) * small
         a_interp = a_long * alpha + (1 - alpha) if m.interpolationMethod == "LINEAR" else np.exp(np.log(a_long) * alpha)
         return interp.mult(a_short / a_interp)
+
+    def _interpolationDriftAdjustment(self, evaluationTimeIndex, liborIndex):
+        """getInterpolationDriftAdjustmentEvaluated (:1433-1497): the trapezoid integral over the
+        simulation times 0..evaluationTimeIndex of |lambda_j(t)|^2 / (1 + L_j(t) dT_j)^2 (times
+        L_j(t)^2 in the lognormal state space), with L_j read at min(t, T_j) (the simulation
+        time at or before T_j when T_j is off the simulation grid).  The factor
+        loadings are the covariance model's deterministic ones, summed on the host in the
+        reference's order; the L-dependent part runs as device random-variable operations.
+        The reference caches the value per LIBOR index when evaluated at the period start
+        (:1405-1422); every evaluation gives the same numbers, so none is cached here."""
+        from .randomvariable import RandomVariableGPU
+        m = self.model
+        tenor, td = m.liborPeriodDiscretization, self.process.getTimeDiscretization()
+        cov = m.covarianceModel
+        tenorDt = tenor.getTime(liborIndex + 1) - tenor.getTime(liborIndex)
+        lognormal = m.stateSpace == _lib.STATE_SPACE_LOGNORMAL
+        start = td.getTimeIndex(tenor.getTime(liborIndex))  # raw: negative off the simulation grid
+
+        def integrand(sumTimeIndex, realizationIndex):
+            ct = cov.timeDiscretization.getTimeIndex(td.getTime(sumTimeIndex))
+            if ct < 0:
+                ct = -ct - 2
+            if ct >= cov.factorLoadings.shape[0]:
+                raise ValueError("factor loading beyond the covariance model's time discretization")
+            squares = 0.0  # getRandomVariableForConstant(0.0).add(oneFactor.squared()) per factor
+            for loading in cov.getFactorLoading(ct, liborIndex):
+                squares = squares + float(loading) * float(loading)
+            libor = self.getLIBORRandomVariable(realizationIndex, liborIndex)
+            value = RandomVariableGPU.constant(float("-inf"), squares).div(libor.mult(tenorDt).add(1.0).squared())
+            return value.mult(libor.squared()) if lognormal else value
+
+        previous = integrand(0, 0)
+        adjustment = RandomVariableGPU.constant(float("-inf"), 0.0)
+        for sumTimeIndex in range(1, evaluationTimeIndex + 1):
+            k = min(sumTimeIndex, start)  # :1473-1478, the minimum taken before the off-grid mapping
+            current = integrand(sumTimeIndex, k if k >= 0 else -k - 2)
+            integralDt = 0.5 * (td.getTime(sumTimeIndex) - td.getTime(sumTimeIndex - 1))
+            adjustment = adjustment.add(current.add(previous).mult(integralDt))
+            previous = current
+        return adjustment
 
     def getNumberOfPaths(self):
         return self.process.numberOfPaths
@@ -451,6 +498,18 @@ class LIBORMonteCarloSimulationFromLIBORModel:
 
     def getLiborPeriodDiscretization(self):
         return self.model.liborPeriodDiscretization
+
+    def getLiborPeriod(self, timeIndex):
+        return self.model.liborPeriodDiscretization.getTime(timeIndex)
+
+    def getLiborPeriodIndex(self, time):
+        """LIBORMarketModelFromCovarianceModel.getLiborPeriodIndex (:1528-1530): the tenor index of
+        time, negative (-insertion point - 1) off the tenor grid."""
+        return self.model.liborPeriodDiscretization.getTimeIndex(time)
+
+    def getRandomVariableForConstant(self, value):
+        from .randomvariable import RandomVariableGPU
+        return RandomVariableGPU.constant(float("-inf"), value)
 
 
 # --------------------------------------------------------------------------- products

@@ -193,8 +193,8 @@ class RandomVariableGPUFactory:
     """RandomVariableFactory.createRandomVariable (RandomVariableFactory.java:56-94) on the GPU."""
 
     def createRandomVariable(self, *args) -> RandomVariableGPU:
-        if len(args) == 1:
-            return RandomVariableGPU.constant(0.0, args[0])
+        if len(args) == 1:  # AbstractRandomVariableFactory.java:22-24: measurable at -infinity
+            return RandomVariableGPU.constant(float("-inf"), args[0])
         time, value = args
         if np.ndim(value) == 0:
             return RandomVariableGPU.constant(time, value)

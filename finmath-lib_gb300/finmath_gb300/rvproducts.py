@@ -10,9 +10,22 @@ from __future__ import annotations
 from .randomvariable import RandomVariableGPU
 
 
+_NEG_INF = float("-inf")
+
+
 def _weights(model) -> RandomVariableGPU:
     # getMonteCarloWeights: equal weights 1/P
     return RandomVariableGPU.constant(0.0, 1.0 / model.getNumberOfPaths())
+
+
+def _constant(value) -> RandomVariableGPU:
+    # getRandomVariableForConstant / Scalar: deterministic, measurable at -infinity
+    return RandomVariableGPU.constant(_NEG_INF, value)
+
+
+def _to_evaluation_time(values, evaluationTime, model) -> RandomVariableGPU:
+    # the products' common tail: values.mult(N(evaluationTime)).div(weights(evaluationTime))
+    return values.mult(model.getNumeraireRandomVariable(evaluationTime)).div(_weights(model))
 
 
 class Caplet:
@@ -69,6 +82,147 @@ class SimpleSwap:
             payoff = payoff.div(model.getNumeraireRandomVariable(paymentDate)).mult(_weights(model))
             values = values.add(payoff)
         return values.mult(model.getNumeraireRandomVariable(evaluationTime)).div(_weights(model))
+
+    def getValue(self, model, evaluationTime: float = 0.0) -> float:
+        return self.getValueRandomVariable(evaluationTime, model).getAverage()
+
+
+class SimpleZeroSwap:
+    """SimpleZeroSwap (montecarlo/interestrate/products/SimpleZeroSwap.java:94-130): SimpleSwap
+    with a notional that compounds by swaprate * periodLength after every period, the LIBOR
+    as the float index."""
+
+    def __init__(self, fixingDates, paymentDates, swaprates, isPayFix=True):
+        self.fixingDates = [float(x) for x in fixingDates]
+        self.paymentDates = [float(x) for x in paymentDates]
+        self.swaprates = [float(x) for x in swaprates]
+        self.isPayFix = bool(isPayFix)
+
+    def getValueRandomVariable(self, evaluationTime, model) -> RandomVariableGPU:
+        values = _constant(0.0)
+        notional = _constant(1.0)
+        for fixingDate, paymentDate, swaprate in zip(self.fixingDates, self.paymentDates, self.swaprates):
+            periodLength = paymentDate - fixingDate
+            if paymentDate < evaluationTime:
+                continue
+            index = model.getForwardRate(fixingDate, fixingDate, paymentDate)
+            payoff = index.sub(swaprate).mult(periodLength).mult(notional)
+            if not self.isPayFix:
+                payoff = payoff.mult(-1.0)
+            payoff = payoff.div(model.getNumeraireRandomVariable(paymentDate)).mult(_weights(model))
+            values = values.add(payoff)
+            notional = notional.mult(swaprate * periodLength)
+        return _to_evaluation_time(values, evaluationTime, model)
+
+    def getValue(self, model, evaluationTime: float = 0.0) -> float:
+        return self.getValueRandomVariable(evaluationTime, model).getAverage()
+
+
+class Bond:
+    """Zero-coupon bond (montecarlo/interestrate/products/Bond.java:58-88): 1 / N(T) * N(t),
+    zero after maturity (model time offset 0: no reference date)."""
+
+    def __init__(self, maturity):
+        self.maturity = float(maturity)
+
+    def getValueRandomVariable(self, evaluationTime, model) -> RandomVariableGPU:
+        if evaluationTime > self.maturity:
+            return _constant(0.0)
+        values = _constant(1.0).div(model.getNumeraireRandomVariable(self.maturity)).mult(_weights(model))
+        return _to_evaluation_time(values, evaluationTime, model)
+
+    def getValue(self, model, evaluationTime: float = 0.0) -> float:
+        return self.getValueRandomVariable(evaluationTime, model).getAverage()
+
+
+class LIBORBond:
+    """Bond valued from the forward rate (montecarlo/interestrate/products/LIBORBond.java:43-50):
+    1 / (1 + L(t; t, T) (T - t)) at the evaluation time t, not discounted further."""
+
+    def __init__(self, maturity):
+        self.maturity = float(maturity)
+
+    def getValueRandomVariable(self, evaluationTime, model) -> RandomVariableGPU:
+        if evaluationTime > self.maturity:
+            return _constant(0.0)
+        return (model.getForwardRate(evaluationTime, evaluationTime, self.maturity)
+                .mult(self.maturity - evaluationTime).add(1.0).invert())
+
+    def getValue(self, model, evaluationTime: float = 0.0) -> float:
+        return self.getValueRandomVariable(evaluationTime, model).getAverage()
+
+
+class DigitalCaplet:
+    """Digital caplet (montecarlo/interestrate/products/DigitalCaplet.java:58-85): pays the period
+    length at periodEnd when L(optionMaturity; periodStart, periodEnd) - K >= 0 (choose on the
+    trigger), discounted by the numeraire."""
+
+    def __init__(self, optionMaturity, periodStart, periodEnd, strike):
+        self.optionMaturity = float(optionMaturity)
+        self.periodStart = float(periodStart)
+        self.periodEnd = float(periodEnd)
+        self.strike = float(strike)
+
+    def getValueRandomVariable(self, evaluationTime, model) -> RandomVariableGPU:
+        paymentDate = self.periodEnd
+        periodLength = self.periodEnd - self.periodStart
+        libor = model.getForwardRate(self.optionMaturity, self.periodStart, self.periodEnd)
+        values = libor.sub(self.strike).choose(_constant(periodLength), _constant(0.0))
+        values = values.div(model.getNumeraireRandomVariable(paymentDate)).mult(_weights(model))
+        return _to_evaluation_time(values, evaluationTime, model)
+
+    def getValue(self, model, evaluationTime: float = 0.0) -> float:
+        return self.getValueRandomVariable(evaluationTime, model).getAverage()
+
+
+class DigitalFloorlet:
+    """Digital floorlet (montecarlo/interestrate/products/DigitalFloorlet.java:44-82): the period
+    length where L(T; T, T_next) < K, else 0, on the tenor period that contains the maturity.
+    The reference discards the results of its numeraire division and weighting (:77-78:
+    RandomVariable is immutable), so its value is the undiscounted payoff with filtration
+    time paymentDate; that behaviour is kept.  L < K is taken as L - K < 0 (equal for all
+    non-NaN rates: a difference of distinct finite doubles is never zero)."""
+
+    def __init__(self, maturity, strike):
+        self.maturity = float(maturity)
+        self.strike = float(strike)
+
+    def getValueRandomVariable(self, evaluationTime, model) -> RandomVariableGPU:
+        liborIndex = model.getLiborPeriodIndex(self.maturity)
+        paymentDate = model.getLiborPeriod(liborIndex + 1)
+        periodLength = paymentDate - self.maturity
+        libor = model.getForwardRate(self.maturity, self.maturity, paymentDate)
+        payoff = libor.sub(self.strike).choose(RandomVariableGPU.constant(paymentDate, 0.0),
+                                               RandomVariableGPU.constant(paymentDate, periodLength))
+        return payoff
+
+    def getValue(self, model, evaluationTime: float = 0.0) -> float:
+        return self.getValueRandomVariable(evaluationTime, model).getAverage()
+
+
+class MoneyMarketAccount:
+    """Money market account (montecarlo/interestrate/products/MoneyMarketAccount.java:70-94):
+    initialValue accrued at the forward rate L(t; t, t + accrualPeriod) over accrual periods
+    from the inception time to the evaluation time (the last period cut at the evaluation
+    time); zero before inception, Double.MAX_VALUE for a non-positive accrual period."""
+
+    def __init__(self, inceptionTime=0.0, initialValue=1.0, accrualPeriod=-1.0):
+        self.inceptionTime = float(inceptionTime)
+        self.initialValue = float(initialValue)
+        self.accrualPeriod = float(accrualPeriod)
+
+    def getValueRandomVariable(self, evaluationTime, model) -> RandomVariableGPU:
+        if self.inceptionTime > evaluationTime:
+            return _constant(0.0)
+        if self.accrualPeriod <= 0:
+            return _constant(1.7976931348623157e308)
+        value = _constant(self.initialValue)
+        time = self.inceptionTime
+        while time < evaluationTime:
+            forwardRate = model.getForwardRate(time, time, time + self.accrualPeriod)
+            value = value.accrue(forwardRate, min(self.accrualPeriod, evaluationTime - time))
+            time += self.accrualPeriod
+        return value
 
     def getValue(self, model, evaluationTime: float = 0.0) -> float:
         return self.getValueRandomVariable(evaluationTime, model).getAverage()

@@ -4,8 +4,9 @@ The elementwise operations of RandomVariableFromDoubleArray round every + - * / 
 so on the same inputs the GPU equals numpy's IEEE arithmetic bit for bit; Math.min/max
 rules (NaN wins, -0.0 < +0.0) are checked on special values; exp/log/pow/sin/cos are
 CUDA's (within 2 ulp).  Averages are compensated sums (as the reference's Kahan sums).
-Finmath products written against the random-variable API (caplet, swap) reprice against
-the oracle's paths to 1e-12."""
+Finmath products written against the random-variable API (caplets, swaps, bonds, digitals,
+money market account) reprice against the same operations in numpy on the oracle's paths
+to 1e-12."""
 import numpy as np
 import pytest
 
@@ -203,8 +204,9 @@ def test_process_values_as_random_variables_match_host_copies():
 
 
 def _forward_rate_numpy(osim, m, cfg, method, time, ps, pe):
-    """The same getForwardRate (LIBORMarketModelFromCovarianceModel.java:1238-1381) in numpy on
-    the oracle's paths, with the forward curve interpolated linearly on values."""
+    """The same getForwardRate (LIBORMarketModelFromCovarianceModel.java:1238-1497) in numpy on
+    the oracle's paths and factor loadings, with the forward curve interpolated linearly on
+    values."""
     tenor = np.asarray(m.tenor)
     times = np.asarray(m.times)
     nodes, values = np.asarray(cfg["curve_nodes"]), np.asarray(cfg["curve_values"])
@@ -218,6 +220,28 @@ def _forward_rate_numpy(osim, m, cfg, method, time, ps, pe):
         i = int(np.searchsorted(grid, t))
         return i if i < len(grid) and grid[i] == t else -(i + 1)
 
+    def drift_adjustment(ti, j):
+        # getInterpolationDriftAdjustmentEvaluated (:1433-1497): trapezoid rule over 0..ti of
+        # |lambda_j|^2 / (1 + L_j dT)^2 * L_j^2, L_j at min(s, index of T_j)
+        tdt = tenor[j + 1] - tenor[j]
+        start = idx(times, tenor[j])
+
+        def integrand(s, k):
+            sq = 0.0
+            for lam in m.loadings[s, j]:
+                sq = sq + lam * lam
+            L = osim.process_value(k, j)
+            x = L * tdt + 1.0
+            return sq / (x * x) * (L * L)
+
+        prev, acc = integrand(0, 0), 0.0
+        for s in range(1, ti + 1):
+            k = min(s, start)
+            cur = integrand(s, k if k >= 0 else -k - 2)
+            acc = acc + (cur + prev) * (0.5 * (times[s] - times[s - 1]))
+            prev = cur
+        return acc
+
     def one_plus(ti, pst, k):
         ts, te = tenor[k], tenor[k + 1]
         tdt = te - ts
@@ -226,7 +250,12 @@ def _forward_rate_numpy(osim, m, cfg, method, time, ps, pe):
         lg = osim.process_value(ti, k) * tdt + 1.0
         small = te - pst
         alpha = small / tdt
-        interp = lg * alpha + (1 - alpha) if method == "LINEAR" else np.exp(np.log(lg) * alpha)
+        if method == "LINEAR":
+            interp = lg * alpha + (1 - alpha)
+        elif method == "LOG_LINEAR_CORRECTED":
+            interp = np.exp(np.log(lg) * alpha - drift_adjustment(ti, k) * (0.5 * small * (ts - pst)))
+        else:
+            interp = np.exp(np.log(lg) * alpha)
         a_long = 1 + fwd(ts, tdt) * tdt
         a_short = 1 + fwd(pst, small) * small
         a_int = a_long * alpha + (1 - alpha) if method == "LINEAR" else np.exp(np.log(a_long) * alpha)
@@ -262,7 +291,7 @@ def _forward_rate_numpy(osim, m, cfg, method, time, ps, pe):
     return fr(time, ps, pe)
 
 
-@pytest.mark.parametrize("method", ["LOG_LINEAR_UNCORRECTED", "LINEAR"])
+@pytest.mark.parametrize("method", ["LOG_LINEAR_UNCORRECTED", "LINEAR", "LOG_LINEAR_CORRECTED"])
 def test_forward_rates_primitive_accrued_and_interpolated(lmm20, method):
     cfg, m, osim, sim = lmm20
     old = sim.model.interpolationMethod
@@ -278,7 +307,7 @@ def test_forward_rates_primitive_accrued_and_interpolated(lmm20, method):
     finally:
         sim.model.interpolationMethod = old
     with pytest.raises(ValueError):
-        sim.model.interpolationMethod = "LOG_LINEAR_CORRECTED"
+        sim.model.interpolationMethod = "CUBIC"
         try:
             sim.getForwardRate(1.0, 1.0, 1.75)
         finally:
@@ -339,3 +368,70 @@ def test_bermudan_written_against_the_random_variable_api_equals_the_fused_kerne
     assert values.getStandardError() == pytest.approx(fused["error"], rel=1e-10)
     got = values.getRealizations()
     assert np.max(np.abs(got - fused["values"])) <= 1e-12 * np.max(np.abs(fused["values"]))
+
+
+def test_bonds_digitals_zero_swap_and_money_market_account(lmm20):
+    # Bond, LIBORBond, DigitalCaplet, DigitalFloorlet, SimpleZeroSwap and MoneyMarketAccount
+    # (montecarlo/interestrate/products/) on the GPU simulation against their operations in
+    # numpy on the oracle's paths
+    cfg, m, osim, sim = lmm20
+    P = sim.getNumberOfPaths()
+    w = 1.0 / P
+    N0 = osim.numeraire(0.0)
+    fr = lambda t, ps, pe: _forward_rate_numpy(osim, m, cfg, "LOG_LINEAR_UNCORRECTED", t, ps, pe)
+    avg = po.kahan_average
+
+    # zero-coupon bonds: 1 / N(T), and zero once the evaluation time is past maturity
+    for T in (0.5, 3.0, 10.0):
+        assert F.Bond(T).getValue(sim) == pytest.approx(avg(1.0 / osim.numeraire(T) * w * N0 / w), rel=1e-12)
+    assert F.Bond(3.0).getValue(sim, evaluationTime=3.5) == 0.0
+    assert F.Bond(3.0).getValueRandomVariable(3.5, sim).isDeterministic()
+
+    # LIBORBond: 1 / (1 + L(t; t, T) (T - t)) at t
+    for t, T in ((0.0, 4.0), (1.0, 3.0), (1.25, 2.75)):
+        o = 1.0 / (fr(t, t, T) * (T - t) + 1.0)
+        assert F.LIBORBond(T).getValue(sim, evaluationTime=t) == pytest.approx(avg(o), rel=1e-12)
+
+    # digital caplets on and off the tenor grid
+    for (tm, ps, pe, K) in ((2.0, 2.0, 2.5, 0.05), (4.5, 4.5, 5.0, 0.055), (1.25, 1.25, 2.0, 0.05)):
+        L = fr(tm, ps, pe)
+        o = np.where(L - K >= 0, pe - ps, 0.0) / osim.numeraire(pe) * w * N0 / w
+        g = F.DigitalCaplet(tm, ps, pe, K).getValueRandomVariable(0.0, sim)
+        assert g.getAverage() == pytest.approx(avg(o), rel=1e-12)
+        assert np.count_nonzero(g.getRealizations()) == np.count_nonzero(o)  # the same exercise set
+
+    # digital floorlet: the reference's undiscounted payoff (its discounting results are discarded)
+    L = osim.process_value(6, 6)
+    o = np.where(L < 0.05, 0.5, 0.0)
+    g = F.DigitalFloorlet(3.0, 0.05).getValueRandomVariable(0.0, sim)
+    assert np.array_equal(g.getRealizations(), o) and g.getFiltrationTime() == 3.5
+    with pytest.raises(IndexError):  # an off-tenor maturity has no period index, as in the reference
+        F.DigitalFloorlet(3.2, 0.05).getValue(sim)
+
+    # zero swap: the notional compounds by swaprate * periodLength after each period
+    fixes = [2.0, 2.5, 3.0, 3.5, 4.0]
+    pays = [x + 0.5 for x in fixes]
+    rates = [0.05, 0.045, 0.05, 0.055, 0.05]
+    for payFix in (True, False):
+        o, notional = np.zeros(P), 1.0
+        for fx, pm, r in zip(fixes, pays, rates):
+            payoff = (fr(fx, fx, pm) - r) * (pm - fx) * notional
+            if not payFix:
+                payoff = payoff * -1.0
+            o = o + payoff / osim.numeraire(pm) * w
+            notional = notional * (r * (pm - fx))
+        o = o * N0 / w
+        v = F.SimpleZeroSwap(fixes, pays, rates, isPayFix=payFix).getValue(sim)
+        assert v == pytest.approx(avg(o), rel=1e-12, abs=1e-13 * avg(np.abs(o)))
+
+    # money market account: tenor-aligned accrual, and 0.75y periods whose forwards are
+    # interpolated (off-tenor starts and ends, the last period cut at the evaluation time)
+    for (accrual, t_eval) in ((0.5, 3.0), (0.75, 2.0)):
+        o, time = np.ones(P), 0.0
+        while time < t_eval:
+            o = o * (1 + fr(time, time, time + accrual) * min(accrual, t_eval - time))
+            time += accrual
+        g = F.MoneyMarketAccount(0.0, 1.0, accrual).getValueRandomVariable(t_eval, sim).getRealizations()
+        assert np.max(np.abs(g - o) / o) <= 1e-12
+    assert F.MoneyMarketAccount(1.0, 1.0, 0.5).getValue(sim, evaluationTime=0.5) == 0.0
+    assert F.MoneyMarketAccount().getValue(sim, evaluationTime=1.0) == 1.7976931348623157e308
