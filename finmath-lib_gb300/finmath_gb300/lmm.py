@@ -514,14 +514,36 @@ class LIBORMonteCarloSimulationFromLIBORModel:
 
 # --------------------------------------------------------------------------- products
 class Swaption:
-    """net.finmath.montecarlo.interestrate.products.Swaption."""
+    """net.finmath.montecarlo.interestrate.products.Swaption, with the reference's constructors
+    (Swaption.java:58-127), told apart by their arguments after exerciseDate:
+      (fixingDates, paymentDates, periodLengths, swaprates, notional)
+      (fixingDates, paymentDates, periodLengths, swaprates)   notional 1
+      (fixingDates, paymentDates, swaprates)                  period lengths from the dates
+      (swapTenor: TimeDiscretizationFromArray, swaprate)      one period per tenor step
+    periodLengths=None means payment - fixing, as the reference's null.  A scalar swaprate is
+    used for every period."""
 
-    def __init__(self, exerciseDate, fixingDates, paymentDates, swaprates, periodLengths=None, notional=1.0):
+    def __init__(self, exerciseDate, *args, periodLengths=None, notional=1.0):
+        if len(args) == 2 and isinstance(args[0], TimeDiscretizationFromArray):
+            t = args[0].getAsDoubleArray()
+            fixingDates, paymentDates, swaprates = t[:-1], t[1:], args[1]
+        elif len(args) == 3:
+            fixingDates, paymentDates, swaprates = args
+        elif len(args) == 4:
+            fixingDates, paymentDates, periodLengths, swaprates = args
+        elif len(args) == 5:
+            fixingDates, paymentDates, periodLengths, swaprates, notional = args
+        else:
+            raise TypeError("Swaption(exerciseDate, fixingDates, paymentDates[, periodLengths], swaprates[, notional]) "
+                            "or Swaption(exerciseDate, swapTenor, swaprate)")
         self.exerciseDate = float(exerciseDate)
         self.fixingDates = _f64(fixingDates)
         self.paymentDates = _f64(paymentDates)
+        if self.paymentDates.shape != self.fixingDates.shape:
+            raise ValueError("paymentDates must have the length of fixingDates")
         self.swaprates = _f64(np.broadcast_to(swaprates, self.fixingDates.shape))
-        self.periodLengths = None if periodLengths is None else _f64(periodLengths)
+        self.periodLengths = None if periodLengths is None else _f64(np.broadcast_to(periodLengths,
+                                                                                     self.fixingDates.shape))
         self.notional = float(notional)
 
     def getValues(self, model: LIBORMonteCarloSimulationFromLIBORModel):

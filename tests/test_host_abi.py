@@ -163,3 +163,21 @@ def test_svd_solve_matches_the_pinned_pseudo_inverse(n, rank):
     assert F.load().lmm_solve_svd(n, A.ctypes.data_as(dp), b.ctypes.data_as(dp), x.ctypes.data_as(dp)) == 0
     ref = po.lstsq_pinv(A, b)
     assert np.max(np.abs(x - ref)) <= 1e-10 * max(1.0, np.max(np.abs(ref)))
+
+
+def test_swaption_constructors_follow_the_reference_overloads():
+    # Swaption.java:58-127: (fix, pay, periodLengths, swaprates[, notional]), (fix, pay, swaprates)
+    # and (exerciseDate, swapTenor, swaprate); no GPU call
+    fix, pay = [5.0, 5.5, 6.0], [5.5, 6.0, 6.5]
+    a = F.Swaption(5.0, fix, pay, [0.5, 0.5, 0.5], [0.04, 0.05, 0.06], 2.0)
+    assert list(a.periodLengths) == [0.5] * 3 and list(a.swaprates) == [0.04, 0.05, 0.06] and a.notional == 2.0
+    b = F.Swaption(5.0, fix, pay, [0.5, 0.5, 0.5], 0.05)
+    assert list(b.swaprates) == [0.05] * 3 and b.notional == 1.0
+    c = F.Swaption(5.0, fix, pay, 0.05)
+    assert c.periodLengths is None and list(c.swaprates) == [0.05] * 3
+    d = F.Swaption(5.0, F.TimeDiscretizationFromArray(5.0, 3, 0.5), 0.05)
+    assert list(d.fixingDates) == fix and list(d.paymentDates) == pay and d.periodLengths is None
+    with pytest.raises(TypeError):
+        F.Swaption(5.0, fix)
+    with pytest.raises(ValueError):
+        F.Swaption(5.0, fix, pay[:2], 0.05)
