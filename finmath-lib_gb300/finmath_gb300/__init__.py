@@ -13,8 +13,10 @@ from .lmm import (TimeDiscretizationFromArray, ForwardCurveInterpolation, Discou
                   EulerSchemeFromProcessModel, LIBORMonteCarloSimulationFromLIBORModel, Swaption, BermudanSwaption, Portfolio,
                   mersenne_twister_uniforms, kernel_stats)
 from .randomvariable import RandomVariableGPU, RandomVariableGPUFactory, MonteCarloConditionalExpectationRegression
-from .rvproducts import (Bond, Caplet, DigitalCaplet, DigitalFloorlet, LIBORBond, MoneyMarketAccount, SimpleSwap,
-                         SimpleZeroSwap)
+from .rvproducts import (Bond, BermudanSwaptionFromSwapSchedules, Caplet, DigitalCaplet, DigitalFloorlet, LIBORBond,
+                         MoneyMarketAccount, SimpleSwap, SimpleZeroSwap, SwaptionFromSwapSchedules)
+from .schedule import (DayCountConvention_ACT_360, DayCountConvention_ACT_365, FloatingpointDate, Period,
+                       ScheduleFromPeriods)
 from . import workloads, autotune
 
 __all__ = [n for n in dir() if not n.startswith("_")]

@@ -73,15 +73,19 @@ class TimeDiscretizationFromArray:
 class ForwardCurveInterpolation:
     """ForwardCurveInterpolation with LINEAR interpolation on values, CONSTANT extrapolation."""
 
-    def __init__(self, name, times, forwards, paymentOffset):
+    def __init__(self, name, times, forwards, paymentOffset, referenceDate=None):
         self.name = name
         self.times = _f64(times)
         self.forwards = _f64(forwards)
         self.paymentOffset = float(paymentOffset)
+        self.referenceDate = referenceDate  # a datetime.date, or None
 
     @staticmethod
-    def createForwardCurveFromForwards(name, times, givenForwards, paymentOffset):
-        return ForwardCurveInterpolation(name, times, givenForwards, paymentOffset)
+    def createForwardCurveFromForwards(name, times, givenForwards, paymentOffset, referenceDate=None):
+        return ForwardCurveInterpolation(name, times, givenForwards, paymentOffset, referenceDate)
+
+    def getReferenceDate(self):
+        return self.referenceDate
 
     def getPaymentOffset(self, fixingTime=None):
         return self.paymentOffset
@@ -233,6 +237,24 @@ class LIBORMarketModelFromCovarianceModel:
 
     def getNumberOfComponents(self):
         return self.liborPeriodDiscretization.getNumberOfTimeSteps()
+
+    def getReferenceDate(self):
+        """The forward curve's reference date (LIBORMarketModelFromCovarianceModel.java:844-846)."""
+        return self.forwardRateCurve.getReferenceDate() if self.forwardRateCurve is not None else None
+
+    def getNumeraireDefaultableZeroBondAsOfTimeZero(self, time):
+        """The deterministic numeraire adjustment at time (:883-943): the discount-curve chain at
+        a tenor date, interpolated geometrically between tenor dates."""
+        if self.discountChain is None:
+            raise ValueError("the numeraire adjustment needs the model's discount curve")
+        tenor = self.liborPeriodDiscretization
+        i = tenor.getTimeIndex(time)
+        if i >= 0:
+            return float(self.discountChain[i])
+        prev = min(-i - 2, tenor.getNumberOfTimes() - 2)
+        t0, t1 = tenor.getTime(prev), tenor.getTime(prev + 1)
+        a0, a1 = float(self.discountChain[prev]), float(self.discountChain[prev + 1])
+        return a0 * ((a1 / a0) ** ((time - t0) / (t1 - t0)))
 
 
 # --------------------------------------------------------------------------- Brownian motion
@@ -510,6 +532,24 @@ class LIBORMonteCarloSimulationFromLIBORModel:
     def getRandomVariableForConstant(self, value):
         from .randomvariable import RandomVariableGPU
         return RandomVariableGPU.constant(float("-inf"), value)
+
+    def getReferenceDate(self):
+        return self.model.getReferenceDate()
+
+    def getModel(self):
+        return self.model
+
+    def getForwardDiscountBond(self, time, maturity):
+        """LIBORMarketModelFromCovarianceModel.getForwardDiscountBond (:947-952): P(time; maturity)
+        from the forward rates as of time and as of zero and the deterministic numeraire
+        adjustment, as device random variables."""
+        from .randomvariable import RandomVariableGPU
+        asOfTime = self.getForwardRate(time, time, maturity).mult(maturity - time).add(1.0)
+        asOfZero = self.getForwardRate(0.0, time, maturity).mult(maturity - time).add(1.0)
+        m = self.model
+        zb = (RandomVariableGPU.constant(float("-inf"), m.getNumeraireDefaultableZeroBondAsOfTimeZero(maturity))
+              .div(RandomVariableGPU.constant(float("-inf"), m.getNumeraireDefaultableZeroBondAsOfTimeZero(time))))
+        return zb.mult(asOfZero).div(asOfTime)
 
 
 # --------------------------------------------------------------------------- products

@@ -226,3 +226,190 @@ class MoneyMarketAccount:
 
     def getValue(self, model, evaluationTime: float = 0.0) -> float:
         return self.getValueRandomVariable(evaluationTime, model).getAverage()
+
+
+# ----------------------------------------------------------------------------- schedule products
+def _java_binary_search(a, key) -> int:
+    # java.util.Arrays.binarySearch on a sorted double[]: the index, else -(insertion point) - 1
+    import bisect
+    i = bisect.bisect_left(a, key)
+    return i if i < len(a) and a[i] == key else -i - 1
+
+
+def _model_reference_date(model, fallback):
+    ref = model.getReferenceDate() if hasattr(model, "getReferenceDate") else None
+    return fallback if ref is None else ref
+
+
+class SwaptionFromSwapSchedules:
+    """European swaption on date schedules (montecarlo/interestrate/products/
+    SwaptionFromSwapSchedules.java:67-170): both legs valued analytically at the exercise time
+    from forward rates and forward discount bonds (getValueOfLegAnalytic, :184-218), the
+    payer or receiver difference floored at zero and discounted by the numeraire at exercise.
+    valueUnit VALUE; the implied-volatility units are not part of this path."""
+
+    PAYER, RECEIVER = "PAYER", "RECEIVER"
+
+    def __init__(self, referenceDate, swaptionType, exerciseDate, scheduleFixedLeg, scheduleFloatLeg, swaprate,
+                 notional=1.0, valueUnit="VALUE"):
+        from .schedule import _as_date
+        if str(swaptionType).upper() not in (self.PAYER, self.RECEIVER):
+            raise ValueError(f"Unkown swaptionType {swaptionType}")
+        if str(valueUnit).upper() != "VALUE":
+            raise ValueError(f"value unit {valueUnit} is not supported")
+        self.referenceDate = None if referenceDate is None else _as_date(referenceDate)
+        self.swaptionType = str(swaptionType).upper()
+        self.exerciseDate = _as_date(exerciseDate)
+        self.scheduleFixedLeg, self.scheduleFloatLeg = scheduleFixedLeg, scheduleFloatLeg
+        self.swaprate, self.notional = float(swaprate), float(notional)
+
+    @staticmethod
+    def getValueOfLegAnalytic(evaluationTime, model, schedule, paysFloatingRate, fixRate, notional):
+        """The time-t value of a leg: sum over periods, last to first, of the cash flow times
+        P(t; payment) (getForwardDiscountBond), forward rates observed at t."""
+        from .schedule import FloatingpointDate
+        ref = _model_reference_date(model, schedule.getReferenceDate())
+        value = _constant(0.0)
+        for i in range(schedule.getNumberOfPeriods() - 1, -1, -1):
+            period = schedule.getPeriod(i)
+            paymentTime = FloatingpointDate.getFloatingPointDateFromDate(ref, period.getPayment())
+            fixingTime = FloatingpointDate.getFloatingPointDateFromDate(ref, period.getFixing())
+            periodLength = schedule.getPeriodLength(i)
+            discountBond = model.getForwardDiscountBond(evaluationTime, paymentTime)
+            if paysFloatingRate:
+                libor = model.getForwardRate(evaluationTime, fixingTime, paymentTime)
+                value = value.add(libor.mult(periodLength).mult(notional).mult(discountBond))
+            if fixRate != 0:
+                value = value.add(_constant(fixRate * periodLength * notional).mult(discountBond))
+        return value
+
+    def getValueRandomVariable(self, evaluationTime, model) -> RandomVariableGPU:
+        from .schedule import FloatingpointDate
+        ref = _model_reference_date(model, self.referenceDate)
+        exerciseTime = FloatingpointDate.getFloatingPointDateFromDate(ref, self.exerciseDate)
+        fixLeg = self.getValueOfLegAnalytic(exerciseTime, model, self.scheduleFixedLeg, False, self.swaprate,
+                                            self.notional)
+        floatLeg = self.getValueOfLegAnalytic(exerciseTime, model, self.scheduleFloatLeg, True, 0.0, self.notional)
+        values = floatLeg.sub(fixLeg) if self.swaptionType == self.PAYER else fixLeg.sub(floatLeg)
+        values = values.floor(0.0)
+        values = values.div(model.getNumeraireRandomVariable(exerciseTime)).mult(_weights(model))
+        return _to_evaluation_time(values, evaluationTime, model)
+
+    def getValue(self, model, evaluationTime: float = 0.0) -> float:
+        return self.getValueRandomVariable(evaluationTime, model).getAverage()
+
+
+class BermudanSwaptionFromSwapSchedules:
+    """Bermudan swaption on date schedules (montecarlo/interestrate/products/
+    BermudanSwaptionFromSwapSchedules.java:77-92 constructor, :191-254 getValues, :316-349
+    the analytic underlying, :361-428 the basis): backward induction over the exercise dates;
+    at each, the underlying swap of that date valued analytically at its first fixing and
+    made numeraire-relative, the continuation estimated by MonteCarloConditionalExpectation-
+    Regression on the product's own basis (constant, 1/N(t), the discounted swap rates of the
+    remaining underlyings and their squares, the discounted short rate to the next date and
+    its square), and the exercise taken where the estimate is negative.  Schedules are given
+    explicitly (the reference's ScheduleGenerator constructors, with business-day calendars,
+    are not part of this path)."""
+
+    PAYER, RECEIVER = "PAYER", "RECEIVER"
+
+    def __init__(self, referenceDate, swaptionType, exerciseDates, swapEndDate, swaprates, notionals, fixSchedules,
+                 floatSchedules, conditionalExpectationRegressionFactory=None, regressionBasisFunctionProvider=None):
+        from .schedule import _as_date
+        if str(swaptionType).upper() not in (self.PAYER, self.RECEIVER):
+            raise ValueError(f"Unkown swaptionType {swaptionType}")
+        n = len(exerciseDates)
+        if not (len(swaprates) == len(notionals) == len(fixSchedules) == len(floatSchedules) == n):
+            raise ValueError("one swaprate, notional and pair of schedules per exercise date")
+        self.referenceDate = None if referenceDate is None else _as_date(referenceDate)
+        self.swaptionType = str(swaptionType).upper()
+        self.exerciseDates = [_as_date(d) for d in exerciseDates]
+        self.swapEndDate = _as_date(swapEndDate)
+        self.swaprates = [float(x) for x in swaprates]
+        self.notionals = [float(x) for x in notionals]
+        self.fixSchedules, self.floatSchedules = list(fixSchedules), list(floatSchedules)
+        self.regressionBasisFunctionProvider = regressionBasisFunctionProvider or self
+        self.conditionalExpectationRegressionFactory = conditionalExpectationRegressionFactory
+
+    def _reference_date(self, model):
+        ref = model.getReferenceDate() if hasattr(model, "getReferenceDate") else None
+        if ref is None:
+            raise ValueError("the model needs a reference date (its forward curve's) for date schedules")
+        return ref
+
+    def _underlying(self, model, legSchedule, paysFloat, swaprate, notional):
+        # getValueUnderlyingNumeraireRelative with isUseAnalyticSwapValuationAtExercise (:316-328)
+        from .schedule import FloatingpointDate
+        valuationTime = FloatingpointDate.getFloatingPointDateFromDate(self._reference_date(model),
+                                                                        legSchedule.getPeriod(0).getFixing())
+        value = SwaptionFromSwapSchedules.getValueOfLegAnalytic(valuationTime, model, legSchedule, paysFloat, swaprate,
+                                                                notional)
+        return value.div(model.getNumeraireRandomVariable(valuationTime)).mult(_weights(model))
+
+    def getBasisFunctions(self, evaluationTime, model):
+        """The product's own regression basis at an exercise time (:361-428)."""
+        from .schedule import FloatingpointDate
+        ref = self._reference_date(model)
+        times = sorted([FloatingpointDate.getFloatingPointDateFromDate(ref, d) for d in self.exerciseDates]
+                       + [FloatingpointDate.getFloatingPointDateFromDate(ref, self.swapEndDate)])
+        exerciseTime = evaluationTime
+        exerciseIndex = _java_binary_search(times, exerciseTime)
+        if exerciseIndex < 0:
+            exerciseIndex = -exerciseIndex  # as the reference: one past the insertion point
+        if exerciseIndex >= len(self.exerciseDates):
+            exerciseIndex = len(self.exerciseDates) - 1
+        basis = [_constant(1.0)]
+        discountFactor = model.getNumeraireRandomVariable(exerciseTime).invert()
+        basis.append(discountFactor)
+        for u in range(exerciseIndex, len(self.exerciseDates)):
+            floatLeg = SwaptionFromSwapSchedules.getValueOfLegAnalytic(exerciseTime, model, self.floatSchedules[u], True,
+                                                                       0.0, 1.0)
+            annuity = SwaptionFromSwapSchedules.getValueOfLegAnalytic(exerciseTime, model, self.fixSchedules[u], False,
+                                                                      1.0, 1.0)
+            basisFunction = floatLeg.div(annuity).mult(discountFactor)
+            basis.append(basisFunction)
+            basis.append(basisFunction.squared())
+        rateShort = model.getForwardRate(exerciseTime, exerciseTime, times[exerciseIndex + 1])
+        basis.append(rateShort.mult(discountFactor))
+        basis.append(rateShort.mult(discountFactor).pow(2.0))
+        return basis
+
+    def getValues(self, evaluationTime, model):
+        from .randomvariable import MonteCarloConditionalExpectationRegression
+        from .schedule import FloatingpointDate
+        ref = self._reference_date(model)
+        values = _constant(0.0)
+        exerciseTimes = _constant(float("inf"))
+        for k in range(len(self.exerciseDates) - 1, -1, -1):
+            exerciseTime = FloatingpointDate.getFloatingPointDateFromDate(ref, self.exerciseDates[k])
+            fixLeg = self._underlying(model, self.fixSchedules[k], False, self.swaprates[k], self.notionals[k])
+            floatLeg = self._underlying(model, self.floatSchedules[k], True, 0.0, self.notionals[k])
+            underlying = floatLeg.sub(fixLeg) if self.swaptionType == self.PAYER else fixLeg.sub(floatLeg)
+            basis = self.regressionBasisFunctionProvider.getBasisFunctions(exerciseTime, model)
+            factory = self.conditionalExpectationRegressionFactory or MonteCarloConditionalExpectationRegression
+            estimator = factory(basis, basis)
+            trigger = values.sub(underlying).getConditionalExpectation(estimator)
+            values = trigger.choose(values, underlying)
+            exerciseTimes = trigger.choose(exerciseTimes, _constant(exerciseTime))
+        values = _to_evaluation_time(values, evaluationTime, model)
+        return {"values": values, "exerciseTimes": exerciseTimes}
+
+    def getValueRandomVariable(self, evaluationTime, model) -> RandomVariableGPU:
+        return self.getValues(evaluationTime, model)["values"]
+
+    def getValue(self, model, evaluationTime: float = 0.0) -> float:
+        return self.getValueRandomVariable(evaluationTime, model).getAverage()
+
+    def getExerciseProbabilitiesFromTimes(self, referenceDate, exerciseTimes):
+        """:268-283: the probability of exercise at each date (after the previous ones) and,
+        last, of no exercise, from the exerciseTimes random variable."""
+        from .schedule import FloatingpointDate
+        probabilities = []
+        toExercise = 1.0
+        for d in self.exerciseDates:
+            t = FloatingpointDate.getFloatingPointDateFromDate(referenceDate, d)
+            after = exerciseTimes.sub(t + 1.0 / 365.0).choose(_constant(1.0), _constant(0.0)).getAverage()
+            probabilities.append(toExercise - after)
+            toExercise = after
+        probabilities.append(toExercise)
+        return probabilities

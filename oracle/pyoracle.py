@@ -188,10 +188,12 @@ class Model:
 def build_model(*, dt: float, T_end: float, period: float, tenor_end: float, F: int,
                 corr_decay: float, abcd, curve_nodes, curve_values, payment_offset=None,
                 discount_curve: bool = True, libor_cap: float = 1e5, scheme: int = 1,
-                vol_matrix=None, measure: int = 0, state_space: int = 0) -> Model:
+                vol_matrix=None, measure: int = 0, state_space: int = 0, times=None, tenor=None) -> Model:
+    """times / tenor, when given, replace the uniform grids of dt / T_end and period / tenor_end
+    (date-derived grids, already tick-rounded as TimeDiscretizationFromArray rounds them)."""
     L = lib()
-    times = time_discretization(0.0, int(round(T_end / dt)), dt)
-    tenor = time_discretization(0.0, int(round(tenor_end / period)), period)
+    times = time_discretization(0.0, int(round(T_end / dt)), dt) if times is None else f64(times)
+    tenor = time_discretization(0.0, int(round(tenor_end / period)), period) if tenor is None else f64(tenor)
     T, N = len(times) - 1, len(tenor) - 1
     factor = np.empty((N, F)); corr = np.empty((N, N))
     L.orc_exp_decay_correlation(_p(tenor), N, F, corr_decay, _p(factor), _p(corr))

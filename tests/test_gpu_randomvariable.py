@@ -216,9 +216,11 @@ def _forward_rate_numpy(osim, m, cfg, method, time, ps, pe):
         f = float(np.interp(t, nodes, values))
         return f if dt == po_off else (np.exp(np.log(1 + f * po_off) * dt / po_off) - 1.0) / dt
 
-    def idx(grid, t):
-        i = int(np.searchsorted(grid, t))
-        return i if i < len(grid) and grid[i] == t else -(i + 1)
+    def idx(grid, t):  # TimeDiscretizationFromArray.getTimeIndex: the time rounded to the 1-hour tick
+        tick = 1.0 / (365.0 * 24.0)
+        key = np.rint(t / tick) * tick
+        i = int(np.searchsorted(grid, key))
+        return i if i < len(grid) and grid[i] == key else -(i + 1)
 
     def drift_adjustment(ti, j):
         # getInterpolationDriftAdjustmentEvaluated (:1433-1497): trapezoid rule over 0..ti of
@@ -435,3 +437,175 @@ def test_bonds_digitals_zero_swap_and_money_market_account(lmm20):
         assert np.max(np.abs(g - o) / o) <= 1e-12
     assert F.MoneyMarketAccount(1.0, 1.0, 0.5).getValue(sim, evaluationTime=0.5) == 0.0
     assert F.MoneyMarketAccount().getValue(sim, evaluationTime=1.0) == 1.7976931348623157e308
+
+
+# ----------------------------------------------------------------------------- date schedules
+import datetime as _dt  # noqa: E402
+
+REF_DATE = _dt.date(2026, 1, 5)
+DATED = dict(curve_nodes=[0.5, 1.0, 2.0, 5.0, 40.0], curve_values=[0.03, 0.035, 0.04, 0.045, 0.045], period=0.5,
+             F=3, corr_decay=0.04, abcd=(0.2, 0.1, 0.25, 0.1), seed=2718)
+
+
+def dated_dates():
+    """Semi-annual dates over 5 years from 2026-01-05: 181- to 184-day periods."""
+    def add_months(d, k):
+        y, m = divmod(d.month - 1 + k, 12)
+        return d.replace(year=d.year + y, month=m + 1)
+    return [add_months(REF_DATE, 6 * i) for i in range(11)]
+
+
+def dated_model():
+    """An LMM whose tenor and simulation times are the ACT/365 times of the dates, and whose
+    forward curve carries the reference date (finmath_gb300 classes; host tables only)."""
+    D = dated_dates()
+    times = [F.FloatingpointDate.getFloatingPointDateFromDate(REF_DATE, d) for d in D]
+    td = F.TimeDiscretizationFromArray(times)
+    tenor = F.TimeDiscretizationFromArray(times)
+    c = DATED
+    curve = F.ForwardCurveInterpolation.createForwardCurveFromForwards("forwardCurve", c["curve_nodes"],
+                                                                       c["curve_values"], c["period"], REF_DATE)
+    vol = F.LIBORVolatilityModelFourParameterExponentialForm(td, tenor, *c["abcd"], False)
+    corr = F.LIBORCorrelationModelExponentialDecay(td, tenor, c["F"], c["corr_decay"])
+    cov = F.LIBORCovarianceModelFromVolatilityAndCorrelation(td, tenor, vol, corr)
+    model = F.LIBORMarketModelFromCovarianceModel.of(tenor, None, curve, F.DiscountCurveFromForwardCurve(curve), None,
+                                                     cov, None, {})
+    return td, tenor, model
+
+
+def dated_oracle(td, tenor, P):
+    c = DATED
+    m = po.build_model(dt=0.5, T_end=5.0, period=c["period"], tenor_end=5.0, F=c["F"], corr_decay=c["corr_decay"],
+                       abcd=c["abcd"], curve_nodes=c["curve_nodes"], curve_values=c["curve_values"],
+                       times=td.getAsDoubleArray(), tenor=tenor.getAsDoubleArray())
+    return m, po.Simulation(m, po.brownian_increments(m.times, m.F, P, c["seed"]))
+
+
+@pytest.fixture(scope="module")
+def dated():
+    P = 2000
+    td, tenor, model = dated_model()
+    m, osim = dated_oracle(td, tenor, P)
+    bm = F.BrownianMotionFromMersenneRandomNumbers(td, DATED["F"], P, DATED["seed"])
+    sim = F.LIBORMonteCarloSimulationFromLIBORModel(F.EulerSchemeFromProcessModel(model, bm))
+    return DATED, m, osim, sim
+
+
+def _schedule(D, first, last, daycount):
+    periods = [F.Period(D[i], D[i + 1], D[i], D[i + 1]) for i in range(first, last)]
+    return F.ScheduleFromPeriods(REF_DATE, periods, daycount)
+
+
+def _schedule_numpy(osim, m, cfg):
+    """Forward discount bonds and analytic legs (LIBORMarketModelFromCovarianceModel.java:947-952,
+    SwaptionFromSwapSchedules.java:184-218) in numpy on the oracle's paths."""
+    fr = lambda t, ps, pe: _forward_rate_numpy(osim, m, cfg, "LOG_LINEAR_UNCORRECTED", t, ps, pe)
+    tenor, chain = np.asarray(m.tenor), np.asarray(m.discount_chain)
+    tick = 1.0 / (365.0 * 24.0)
+
+    def zb(t):
+        key = np.rint(t / tick) * tick
+        i = int(np.searchsorted(tenor, key))
+        if i < len(tenor) and tenor[i] == key:
+            return chain[i]
+        p = min(i - 1, len(tenor) - 2)
+        return chain[p] * ((chain[p + 1] / chain[p]) ** ((t - tenor[p]) / (tenor[p + 1] - tenor[p])))
+
+    def bond(t, T):
+        return (zb(T) / zb(t)) * (fr(0.0, t, T) * (T - t) + 1.0) / (fr(t, t, T) * (T - t) + 1.0)
+
+    def leg(t, sched, pays_float, fix_rate, notional):
+        acc = 0.0
+        for i in range(sched.getNumberOfPeriods() - 1, -1, -1):
+            per = sched.getPeriod(i)
+            pt = F.FloatingpointDate.getFloatingPointDateFromDate(REF_DATE, per.getPayment())
+            ft = F.FloatingpointDate.getFloatingPointDateFromDate(REF_DATE, per.getFixing())
+            pl = sched.getPeriodLength(i)
+            pb = bond(t, pt)
+            if pays_float:
+                acc = acc + fr(t, ft, pt) * pl * notional * pb
+            if fix_rate != 0:
+                acc = acc + (fix_rate * pl * notional) * pb
+        return acc
+
+    return fr, leg
+
+
+def test_swaptions_on_date_schedules(dated):
+    # SwaptionFromSwapSchedules and BermudanSwaptionFromSwapSchedules on an LMM built on the
+    # schedule's dates, against their operations in numpy (the regression by the oracle's
+    # pinned pseudo-inverse of the same Kahan scalar products)
+    cfg, m, osim, sim = dated
+    D = dated_dates()
+    P = sim.getNumberOfPaths()
+    w = 1.0 / P
+    N0 = osim.numeraire(0.0)
+    fd = lambda d: F.FloatingpointDate.getFloatingPointDateFromDate(REF_DATE, d)
+    fr, leg = _schedule_numpy(osim, m, cfg)
+    act360, act365 = F.DayCountConvention_ACT_360(), F.DayCountConvention_ACT_365()
+    assert sim.getReferenceDate() == REF_DATE
+    assert act360.getDaycountFraction(D[0], D[1]) == 181 / 360.0 and act365.getDaycountFraction(D[1], D[0]) == -181 / 365.0
+
+    # forward discount bonds P(t; T)
+    for (t, T) in ((fd(D[2]), fd(D[6])), (fd(D[4]), fd(D[5])), (0.0, fd(D[3]))):
+        g = sim.getForwardDiscountBond(t, T).getRealizations()
+        o = (np.ones(P) * (m.discount_chain[int(np.argmin(np.abs(m.tenor - T)))] /
+                           m.discount_chain[int(np.argmin(np.abs(m.tenor - t)))]))
+        o = o * (fr(0.0, t, T) * (T - t) + 1.0) / (fr(t, t, T) * (T - t) + 1.0)
+        assert np.max(np.abs(g - o) / o) <= 1e-12
+
+    # European: exercise 1y into a 4y swap, fixed leg ACT/360, float leg ACT/365
+    fixS, floatS = _schedule(D, 2, 10, act360), _schedule(D, 2, 10, act365)
+    te = fd(D[2])
+    for K, kind in ((0.04, "PAYER"), (0.045, "RECEIVER")):
+        fixl, flol = leg(te, fixS, False, K, 1.0), leg(te, floatS, True, 0.0, 1.0)
+        o = flol - fixl if kind == "PAYER" else fixl - flol
+        o = np.maximum(o, 0.0) / osim.numeraire(te) * w * N0 / w
+        g = F.SwaptionFromSwapSchedules(REF_DATE, kind, D[2], fixS, floatS, K, 1.0).getValue(sim)
+        assert g == pytest.approx(po.kahan_average(o), rel=1e-12)
+    with pytest.raises(ValueError):
+        F.SwaptionFromSwapSchedules(REF_DATE, "STRADDLE", D[2], fixS, floatS, 0.04)
+
+    # Bermudan: exercise at 1y, 1.5y, 2y, 2.5y into swaps ending at 5y
+    ex = D[2:6]
+    fixes = [_schedule(D, 2 + k, 10, act360) for k in range(4)]
+    floats = [_schedule(D, 2 + k, 10, act365) for k in range(4)]
+    K = 0.042
+    berm = F.BermudanSwaptionFromSwapSchedules(REF_DATE, "PAYER", ex, D[10], [K] * 4, [1.0] * 4, fixes, floats)
+    res = berm.getValues(0.0, sim)
+    times = sorted([fd(d) for d in ex] + [fd(D[10])])
+    values, ex_time = np.zeros(P), np.full(P, np.inf)
+    for k in range(3, -1, -1):
+        t = fd(ex[k])
+
+        def underlying(s, pays_float, rate):
+            vt = fd(s.getPeriod(0).getFixing())
+            return leg(vt, s, pays_float, rate, 1.0) / osim.numeraire(vt) * w
+
+        u = underlying(floats[k], True, 0.0) - underlying(fixes[k], False, K)
+        i = times.index(t)
+        df = 1.0 / osim.numeraire(t)
+        X = [np.ones(P), df]
+        for j in range(i, 4):
+            b = leg(t, floats[j], True, 0.0, 1.0) / leg(t, fixes[j], False, 1.0, 1.0) * df
+            X += [b, b * b]
+        rs = fr(t, t, times[i + 1]) * df
+        X += [rs, rs ** 2.0]
+        y = values - u
+        n = len(X)
+        xtx = np.array([[po.kahan_average(X[a] * X[b]) for b in range(n)] for a in range(n)])
+        beta = po.lstsq_pinv(xtx, np.array([po.kahan_average(y * X[a]) for a in range(n)]))
+        ce = X[0] * beta[0]
+        for a in range(1, n):
+            ce = ce + X[a] * beta[a]
+        values = np.where(ce >= 0, values, u)
+        ex_time = np.where(ce >= 0, ex_time, t)
+    values = values * N0 / w
+    g_ex = res["exerciseTimes"].getRealizations()
+    flips = g_ex != ex_time  # exercise decisions on regression estimates within rounding of zero
+    assert flips.sum() <= 2
+    g = res["values"].getRealizations()
+    assert np.max(np.abs(g - values)[~flips]) <= 1e-10 * np.max(np.abs(values))
+    probs = berm.getExerciseProbabilitiesFromTimes(REF_DATE, res["exerciseTimes"])
+    assert sum(probs) == pytest.approx(1.0, abs=1e-15) and len(probs) == 5
+    assert probs[0] == pytest.approx(np.mean(ex_time == fd(ex[0])), abs=2.0 / P)

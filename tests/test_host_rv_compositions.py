@@ -73,6 +73,19 @@ class NumpyRV:
         (tn, vn), (td, vd) = self._operand(numerator), self._operand(denominator)
         return NumpyRV(max(self.t, tn, td), self.v + vn / vd)
 
+    def pow(self, e):
+        return NumpyRV(self.t, np.power(self.v, float(e)))
+
+    def addProduct(self, factor1, factor2):
+        (t1, v1), (t2, v2) = self._operand(factor1), self._operand(factor2)
+        return NumpyRV(max(self.t, t1, t2), self.v + v1 * v2)
+
+    def getConditionalExpectation(self, estimator):
+        return estimator.getConditionalExpectation(self)
+
+    def close(self):
+        pass
+
     def choose(self, a, b):
         (ta, va), (tb, vb) = self._operand(a), self._operand(b)
         return NumpyRV(max(self.t, ta, tb), np.where(np.asarray(self.v) >= 0, va, vb))
@@ -134,3 +147,30 @@ def test_log_linear_corrected_moves_interpolated_rates_only(lmm20_host):
 def test_product_compositions(lmm20_host):
     TG.test_bonds_digitals_zero_swap_and_money_market_account(lmm20_host)
     TG.test_caplets_and_swap_through_the_random_variable_api(lmm20_host)
+
+
+@pytest.fixture
+def dated_host(monkeypatch):
+    monkeypatch.setattr(R, "RandomVariableGPU", NumpyRV)
+    monkeypatch.setattr(RP, "RandomVariableGPU", NumpyRV)
+    monkeypatch.setattr(finmath_gb300, "RandomVariableGPU", NumpyRV)
+    P = 1000
+    td, tenor, model = TG.dated_model()
+    m, osim = TG.dated_oracle(td, tenor, P)
+
+    class HostSimulation(LM.LIBORMonteCarloSimulationFromLIBORModel):
+        def __init__(self):
+            self.model = model
+            self.process = types.SimpleNamespace(getTimeDiscretization=lambda: td, numberOfPaths=P)
+
+        def getLIBORRandomVariable(self, timeIndex, liborIndex):
+            return NumpyRV(td.getTime(timeIndex), osim.process_value(timeIndex, liborIndex))
+
+        def getNumeraireRandomVariable(self, time):
+            return NumpyRV(time, osim.numeraire(time))
+
+    return TG.DATED, m, osim, HostSimulation()
+
+
+def test_schedule_swaption_compositions(dated_host):
+    TG.test_swaptions_on_date_schedules(dated_host)
