@@ -15,6 +15,7 @@ from .lmm import (TimeDiscretizationFromArray, ForwardCurveInterpolation, Discou
 from .randomvariable import RandomVariableGPU, RandomVariableGPUFactory, MonteCarloConditionalExpectationRegression
 from .rvproducts import (Bond, BermudanSwaptionFromSwapSchedules, Caplet, DigitalCaplet, DigitalFloorlet, LIBORBond,
                          MoneyMarketAccount, SimpleSwap, SimpleZeroSwap, SwaptionFromSwapSchedules)
+from .calibration import CalibrationProduct, LevenbergMarquardt, OptimizerFactoryLevenbergMarquardt
 from .schedule import (DayCountConvention_ACT_360, DayCountConvention_ACT_365, FloatingpointDate, Period,
                        ScheduleFromPeriods)
 from . import workloads, autotune

@@ -119,6 +119,8 @@ class DiscountCurveFromForwardCurve:
 # --------------------------------------------------------------------------- covariance
 class LIBORCorrelationModelExponentialDecay:
     def __init__(self, timeDiscretization, liborPeriodDiscretization, numberOfFactors, a, isCalibrateable=False):
+        self.timeDiscretization, self.liborPeriodDiscretization = timeDiscretization, liborPeriodDiscretization
+        self.numberOfFactors, self.a, self.isCalibrateable = int(numberOfFactors), float(a), bool(isCalibrateable)
         tenor = liborPeriodDiscretization.getAsDoubleArray()
         N = len(tenor) - 1
         self.factorMatrix = np.empty((N, numberOfFactors))
@@ -136,9 +138,24 @@ class LIBORCorrelationModelExponentialDecay:
     def getCorrelation(self, timeIndex, component1, component2):
         return float(self.correlationMatrix[component1, component2])
 
+    def getParameter(self):
+        """LIBORCorrelationModelExponentialDecay.java:137-147: [a] when calibrateable, else None."""
+        return [self.a] if self.isCalibrateable else None
+
+    def getCloneWithModifiedParameter(self, parameter):
+        """:74-80: the same model for an unchanged a; else a new, non-calibrateable one (the
+        reference's four-argument constructor)."""
+        if not self.isCalibrateable or self.a == float(parameter[0]):
+            return self
+        return LIBORCorrelationModelExponentialDecay(self.timeDiscretization, self.liborPeriodDiscretization,
+                                                     self.numberOfFactors, float(parameter[0]), False)
+
 
 class LIBORVolatilityModelFourParameterExponentialForm:
     def __init__(self, timeDiscretization, liborPeriodDiscretization, a, b, c, d, isCalibrateable=False):
+        self.timeDiscretization, self.liborPeriodDiscretization = timeDiscretization, liborPeriodDiscretization
+        self.a, self.b, self.c, self.d = float(a), float(b), float(c), float(d)
+        self.isCalibrateable = bool(isCalibrateable)
         t = _f64(timeDiscretization.getAsDoubleArray())
         tn = _f64(liborPeriodDiscretization.getAsDoubleArray())
         T, N = len(t) - 1, len(tn) - 1
@@ -149,10 +166,24 @@ class LIBORVolatilityModelFourParameterExponentialForm:
     def getVolatility(self, timeIndex, liborIndex):
         return float(self.volatility[timeIndex, liborIndex])
 
+    def getParameter(self):
+        """LIBORVolatilityModelFourParameterExponentialForm.java:135-147: [a, b, c, d] when calibrateable."""
+        return [self.a, self.b, self.c, self.d] if self.isCalibrateable else None
+
+    def getCloneWithModifiedParameter(self, parameter):
+        """:150-162: a calibrateable clone with the new a, b, c, d."""
+        if not self.isCalibrateable:
+            return self
+        return LIBORVolatilityModelFourParameterExponentialForm(self.timeDiscretization, self.liborPeriodDiscretization,
+                                                                *[float(x) for x in parameter[:4]], True)
+
 
 class LIBORVolatilityModelFromGivenMatrix:
     def __init__(self, timeDiscretization, liborPeriodDiscretization, volatility):
         self.volatility = _f64(volatility)
+
+    def getParameter(self):
+        return None  # a given matrix is not calibrated on this path
 
     def getVolatility(self, timeIndex, liborIndex):
         return float(self.volatility[timeIndex, liborIndex])
@@ -172,9 +203,54 @@ class LIBORCovarianceModelFromVolatilityAndCorrelation:
         self.timeDiscretization = timeDiscretization
         self.liborPeriodDiscretization = liborPeriodDiscretization
         self.volatility = vol
+        self.volatilityModel, self.correlationModel = volatilityModel, correlationModel
 
     def getNumberOfFactors(self):
         return self.factorLoadings.shape[2]
+
+    def getVolatilityModel(self):
+        return self.volatilityModel
+
+    def getCorrelationModel(self):
+        return self.correlationModel
+
+    def getParameter(self):
+        """LIBORCovarianceModelFromVolatilityAndCorrelation.java:96-117: the volatility model's
+        parameters followed by the correlation model's (each only when calibrateable)."""
+        out = []
+        for m in (self.volatilityModel, self.correlationModel):
+            p = m.getParameter() if hasattr(m, "getParameter") else None
+            out += list(p or [])
+        return out
+
+    def getParameterAsDouble(self):
+        return np.asarray(self.getParameter(), dtype=np.float64)
+
+    def getCloneWithModifiedParameters(self, parameters):
+        """:143-169: the parameters split between the volatility and correlation models; a model
+        whose parameters did not change is kept."""
+        parameters = [float(x) for x in parameters]
+        vol, corr, i = self.volatilityModel, self.correlationModel, 0
+        vp = vol.getParameter() if hasattr(vol, "getParameter") else None
+        cp = corr.getParameter() if hasattr(corr, "getParameter") else None
+        if vp is not None:
+            new = parameters[i:i + len(vp)]
+            i += len(vp)
+            if new != list(vp):
+                vol = vol.getCloneWithModifiedParameter(new)
+        if cp is not None:
+            new = parameters[i:i + len(cp)]
+            i += len(cp)
+            if new != list(cp):
+                corr = corr.getCloneWithModifiedParameter(new)
+        return LIBORCovarianceModelFromVolatilityAndCorrelation(self.timeDiscretization, self.liborPeriodDiscretization,
+                                                                vol, corr)
+
+    def getCloneCalibrated(self, calibrationModel, calibrationProducts, calibrationParameters=None):
+        """AbstractLIBORCovarianceModelParametric.getCloneCalibrated (:150-315, its Levenberg-Marquardt
+        branch :333-460): see finmath_gb300.calibration."""
+        from .calibration import calibrate_covariance_model
+        return calibrate_covariance_model(self, calibrationModel, calibrationProducts, calibrationParameters)
 
     def getFactorLoading(self, timeIndex, component):
         return self.factorLoadings[timeIndex, component].copy()
@@ -206,7 +282,9 @@ class LIBORMarketModelFromCovarianceModel:
             raise ValueError(f"state space {sp} is not implemented on this path")
         self.measure, self.stateSpace = measures[m], spaces[sp]
         if calibrationItems:
-            raise ValueError("calibration is not part of this path")
+            raise ValueError("calibrating models are built by LIBORMarketModelFromCovarianceModel.of(...)")
+        self._args = (liborPeriodDiscretization, analyticModel, forwardRateCurve, discountCurve, randomVariableFactory)
+        self.properties = props
         self.liborPeriodDiscretization = liborPeriodDiscretization
         self.forwardRateCurve = forwardRateCurve
         self.discountCurve = discountCurve
@@ -231,9 +309,29 @@ class LIBORMarketModelFromCovarianceModel:
     @staticmethod
     def of(liborPeriodDiscretization, analyticModel, forwardRateCurve, discountCurve, randomVariableFactory,
            covarianceModel, calibrationItems=None, properties=None):
-        return LIBORMarketModelFromCovarianceModel(liborPeriodDiscretization, analyticModel, forwardRateCurve,
-                                                   discountCurve, randomVariableFactory, covarianceModel,
-                                                   calibrationItems, properties)
+        """:270-322: the model, calibrated first when calibration products are given (the
+        covariance model must be calibrateable; properties["calibrationParameters"] as in the
+        reference: numberOfPaths, seed, maxIterations, accuracy, parameterStep, brownianMotion)."""
+        model = LIBORMarketModelFromCovarianceModel(liborPeriodDiscretization, analyticModel, forwardRateCurve,
+                                                    discountCurve, randomVariableFactory, covarianceModel, None,
+                                                    properties)
+        if not calibrationItems:
+            return model
+        if not hasattr(covarianceModel, "getCloneCalibrated"):
+            raise TypeError("Calibration restricted to covariance models implementing LIBORCovarianceModelCalibrateable.")
+        calibrationParameters = (properties or {}).get("calibrationParameters")
+        calibrated = covarianceModel.getCloneCalibrated(model, calibrationItems, calibrationParameters)
+        return model.getCloneWithModifiedCovarianceModel(calibrated)
+
+    def getCovarianceModel(self):
+        return self.covarianceModel
+
+    def getCloneWithModifiedCovarianceModel(self, covarianceModel):
+        """:1646-1650: the same model with another covariance model."""
+        clone = LIBORMarketModelFromCovarianceModel(*self._args, covarianceModel, None, self.properties)
+        clone.interpolationMethod = self.interpolationMethod
+        clone.simulationTimeInterpolationMethod = self.simulationTimeInterpolationMethod
+        return clone
 
     def getNumberOfComponents(self):
         return self.liborPeriodDiscretization.getNumberOfTimeSteps()
