@@ -10,7 +10,8 @@ from .lmm import (TimeDiscretizationFromArray, ForwardCurveInterpolation, Discou
                   LIBORCorrelationModelExponentialDecay, LIBORVolatilityModelFourParameterExponentialForm,
                   LIBORVolatilityModelFromGivenMatrix, LIBORCovarianceModelFromVolatilityAndCorrelation,
                   LIBORMarketModelFromCovarianceModel, BrownianMotionFromMersenneRandomNumbers,
-                  EulerSchemeFromProcessModel, LIBORMonteCarloSimulationFromLIBORModel, Swaption, BermudanSwaption, Portfolio,
+                  EulerSchemeFromProcessModel, LIBORMonteCarloSimulationFromLIBORModel, Swaption, SwaptionSimple,
+                  BermudanSwaption, Portfolio,
                   mersenne_twister_uniforms, kernel_stats)
 from .randomvariable import RandomVariableGPU, RandomVariableGPUFactory, MonteCarloConditionalExpectationRegression
 from .rvproducts import (Bond, BermudanSwaptionFromSwapSchedules, Caplet, DigitalCaplet, DigitalFloorlet, LIBORBond,
@@ -18,6 +19,6 @@ from .rvproducts import (Bond, BermudanSwaptionFromSwapSchedules, Caplet, Digita
 from .calibration import CalibrationProduct, LevenbergMarquardt, OptimizerFactoryLevenbergMarquardt
 from .schedule import (DayCountConvention_ACT_360, DayCountConvention_ACT_365, FloatingpointDate, Period,
                        ScheduleFromPeriods)
-from . import workloads, autotune
+from . import analytic, workloads, autotune
 
 __all__ = [n for n in dir() if not n.startswith("_")]

@@ -696,6 +696,48 @@ class Swaption:
         return self.getValues(model)["value"]
 
 
+class SwaptionSimple:
+    """net.finmath.montecarlo.interestrate.products.SwaptionSimple (SwaptionSimple.java): the
+    swaption on a swap tenor, exercised at its first date, valued by the fused swaption
+    kernel; the value unit VALUE returns the price, VOLATILITY / VOLATILITYLOGNORMAL and
+    VOLATILITYNORMAL the Black and Bachelier volatilities implied from it on the par swap
+    rate and annuity of the model's forward curve (single curve: the model carries no
+    analytic model), INTEGRATEDVARIANCE* their variance times maturity."""
+
+    _UNITS = ("VALUE", "VOLATILITY", "VOLATILITYLOGNORMAL", "VOLATILITYNORMAL", "INTEGRATEDVARIANCE",
+              "INTEGRATEDVARIANCELOGNORMAL", "INTEGRATEDLOGNORMALVARIANCE", "INTEGRATEDVARIANCENORMAL",
+              "INTEGRATEDNORMALVARIANCE")
+
+    def __init__(self, swaprate, swapTenor, valueUnit="VALUE"):
+        t = swapTenor.getAsDoubleArray() if isinstance(swapTenor, TimeDiscretizationFromArray) else _f64(swapTenor)
+        self.tenor = TimeDiscretizationFromArray(list(t))
+        self.swaprate = float(swaprate)
+        self.valueUnit = str(valueUnit).upper()
+        if self.valueUnit not in self._UNITS:
+            raise ValueError("Provided valueUnit not implemented.")
+        self.swaption = Swaption(float(t[0]), self.tenor, self.swaprate)
+
+    def getValue(self, model):
+        from . import analytic as A
+        value = self.swaption.getValue(model)
+        if self.valueUnit == "VALUE":
+            return value
+        forwardCurve = model.model.forwardRateCurve
+        discountCurve = DiscountCurveFromForwardCurve(forwardCurve)
+        parSwaprate = A.forward_swap_rate(self.tenor, forwardCurve, discountCurve)
+        optionMaturity = self.tenor.getTime(0)
+        annuity = A.swap_annuity(self.tenor, discountCurve)
+        if self.valueUnit in ("VOLATILITY", "VOLATILITYLOGNORMAL"):
+            return A.blackScholesOptionImpliedVolatility(parSwaprate, optionMaturity, self.swaprate, annuity, value)
+        if self.valueUnit == "VOLATILITYNORMAL":
+            return A.bachelierOptionImpliedVolatility(parSwaprate, optionMaturity, self.swaprate, annuity, value)
+        if self.valueUnit in ("INTEGRATEDVARIANCE", "INTEGRATEDVARIANCELOGNORMAL", "INTEGRATEDLOGNORMALVARIANCE"):
+            v = A.blackScholesOptionImpliedVolatility(parSwaprate, optionMaturity, self.swaprate, annuity, value)
+        else:
+            v = A.bachelierOptionImpliedVolatility(parSwaprate, optionMaturity, self.swaprate, annuity, value)
+        return v * v * optionMaturity
+
+
 class BermudanSwaption:
     """net.finmath.montecarlo.interestrate.products.BermudanSwaption.
 
