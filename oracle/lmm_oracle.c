@@ -1,6 +1,6 @@
 /*
  * lmm_oracle.c -- CPU restatement (FP64) of finmath-lib's LIBOR Market Model
- * Monte Carlo path.  TEST INFRASTRUCTURE ONLY (checker + timed CPU baseline); the
+ * Monte Carlo path.  TEST INFRASTRUCTURE ONLY (parity reference + timed CPU baseline); the
  * CUDA product never calls into this file.  See lmm_oracle.h for the parity status.
  *
  * Build: gcc -O2 -ffp-contract=off -fopenmp -fPIC -shared (Java never contracts

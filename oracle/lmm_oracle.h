@@ -1,7 +1,7 @@
 /*
  * lmm_oracle.h -- CPU restatement of finmath-lib's Monte Carlo LIBOR Market Model
- * path (FP64).  TEST INFRASTRUCTURE ONLY: the oracle is the checker for the CUDA
- * library and the timed CPU baseline.  Product code never links, loads or calls it.
+ * path (FP64).  TEST INFRASTRUCTURE ONLY: the oracle is the parity reference for the
+ * CUDA library and the timed CPU baseline.  Product code never links, loads or calls it.
  *
  * Every function restates the reference's arithmetic in the reference's operation
  * order (no fused multiply-add; compile with -ffp-contract=off).  File:line citations
