@@ -298,6 +298,17 @@ class SwaptionFromSwapSchedules:
     def getValue(self, model, evaluationTime: float = 0.0) -> float:
         return self.getValueRandomVariable(evaluationTime, model).getAverage()
 
+    def getProcessTimeDiscretization(self, referenceDate):
+        """ProcessTimeDiscretizationProvider (SwaptionFromSwapSchedules.java:172-186): the
+        exercise time and the payment times of both legs."""
+        from .lmm import TimeDiscretizationFromArray
+        from .schedule import FloatingpointDate
+        f = lambda d: FloatingpointDate.getFloatingPointDateFromDate(referenceDate, d)
+        times = {f(self.exerciseDate)}
+        for s in (self.scheduleFixedLeg, self.scheduleFloatLeg):
+            times.update(f(p.getPayment()) for p in s.getPeriods())
+        return TimeDiscretizationFromArray(sorted(times))
+
 
 class BermudanSwaptionFromSwapSchedules:
     """Bermudan swaption on date schedules (montecarlo/interestrate/products/
@@ -399,6 +410,19 @@ class BermudanSwaptionFromSwapSchedules:
 
     def getValue(self, model, evaluationTime: float = 0.0) -> float:
         return self.getValueRandomVariable(evaluationTime, model).getAverage()
+
+    def getProcessTimeDiscretization(self, referenceDate):
+        """ProcessTimeDiscretizationProvider (BermudanSwaptionFromSwapSchedules.java:286-304): the
+        exercise times and the payment times of every underlying's legs."""
+        from .lmm import TimeDiscretizationFromArray
+        from .schedule import FloatingpointDate
+        f = lambda d: FloatingpointDate.getFloatingPointDateFromDate(referenceDate, d)
+        times = set()
+        for k, d in enumerate(self.exerciseDates):
+            times.add(f(d))
+            for s in (self.fixSchedules[k], self.floatSchedules[k]):
+                times.update(f(p.getPayment()) for p in s.getPeriods())
+        return TimeDiscretizationFromArray(sorted(times))
 
     def getExerciseProbabilitiesFromTimes(self, referenceDate, exerciseTimes):
         """:268-283: the probability of exercise at each date (after the previous ones) and,

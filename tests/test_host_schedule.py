@@ -44,3 +44,23 @@ def test_java_binary_search_semantics():
     a = [0.5, 1.0, 2.0]
     assert _java_binary_search(a, 1.0) == 1
     assert _java_binary_search(a, 0.1) == -1 and _java_binary_search(a, 1.5) == -3 and _java_binary_search(a, 9.0) == -4
+
+
+def test_process_time_discretizations_of_the_schedule_products():
+    # ProcessTimeDiscretizationProvider: exercise and payment times, as the model grid for the products
+    ref = dt.date(2026, 1, 5)
+    d = [dt.date(2026 + (i // 2), 1 + 6 * (i % 2), 5) for i in range(7)]
+    leg = lambda first, dc: F.ScheduleFromPeriods(ref, [F.Period(d[i], d[i + 1], d[i], d[i + 1])
+                                                        for i in range(first, 6)], dc)
+    fd = lambda x: F.FloatingpointDate.getFloatingPointDateFromDate(ref, x)
+    euro = F.SwaptionFromSwapSchedules(ref, "PAYER", d[2], leg(2, F.DayCountConvention_ACT_360()),
+                                       leg(2, F.DayCountConvention_ACT_365()), 0.04)
+    assert list(euro.getProcessTimeDiscretization(ref).getAsDoubleArray()) == \
+        list(F.TimeDiscretizationFromArray([fd(x) for x in d[2:7]]).getAsDoubleArray())
+    berm = F.BermudanSwaptionFromSwapSchedules(ref, "RECEIVER", d[1:3], d[6], [0.04] * 2, [1.0] * 2,
+                                               [leg(1, F.DayCountConvention_ACT_360()), leg(2, F.DayCountConvention_ACT_360())],
+                                               [leg(1, F.DayCountConvention_ACT_365()), leg(2, F.DayCountConvention_ACT_365())])
+    assert list(berm.getProcessTimeDiscretization(ref).getAsDoubleArray()) == \
+        list(F.TimeDiscretizationFromArray([fd(x) for x in d[1:7]]).getAsDoubleArray())
+    with pytest.raises(ValueError):
+        F.BermudanSwaptionFromSwapSchedules(ref, "PAYER", d[1:3], d[6], [0.04], [1.0] * 2, [], [])
