@@ -49,7 +49,10 @@ class RandomVariableGPU:
             self._h = None
 
     def __del__(self):
-        self.close()
+        try:
+            self.close()
+        except Exception:  # interpreter shutdown: the library may already be unloaded
+            pass
 
     # -- description
     def _describe(self):
