@@ -56,11 +56,17 @@ __host__ __device__ __forceinline__ double java_max(double a, double b)
 }
 
 // Math.pow where its special cases differ from C's pow: a NaN exponent gives NaN, and
-// |x| = 1 with an infinite exponent gives NaN
+// |x| = 1 with an infinite exponent gives NaN.  Java's pow (fdlibm's e_pow) also answers
+// the exponents +-1, 2 and 0.5 exactly: x, 1/x, x*x and, for x >= +0, sqrt(x); so do these,
+// which keeps x.pow(2.0) == x.squared() and x.pow(0.5) == x.sqrt() bit for bit.
 __host__ __device__ __forceinline__ double java_pow(double x, double y)
 {
     if (y != y) return y;
     if (fabs(x) == 1.0 && isinf(y)) return y - y;  // NaN
+    if (y == 1.0) return x;
+    if (y == -1.0) return 1.0 / x;
+    if (y == 2.0) return x * x;
+    if (y == 0.5 && !signbit(x)) return sqrt(x);
     return pow(x, y);
 }
 

@@ -124,6 +124,20 @@ def test_deterministic_and_broadcast(xy):
         X.add(RV.from_array(0.0, np.ones(7)))
 
 
+def test_reference_random_variable_kats():
+    # montecarlo/RandomVariableTest.java:72-137 on device random variables: exact averages and
+    # variances of small integer samples, pow(0.5) == sqrt and pow(2) == squared bit for bit
+    r2 = RV.from_array(0.0, [-4.0, -2.0, 0.0, 2.0, 4.0]).add(4.0).div(2.0)
+    assert r2.getAverage() == 2.0
+    assert r2.getVariance() == pytest.approx(2.0, abs=1e-12)
+    r = RV.constant(float("-inf"), 3.0).mult(r2)
+    assert r.getAverage() == 6.0 and r.getVariance() == 2.0 * 9.0
+    x = RV.from_array(0.0, [3.0, 1.0, 0.0, 2.0, 4.0, 1.0 / 3.0])
+    for check in (x.sqrt().sub(x.pow(0.5)), x.squared().sub(x.pow(2.0))):
+        assert check.getAverage() == 0.0 and check.getVariance() == 0.0
+    assert x.getStandardDeviation() - np.sqrt(x.getVariance()) == 0.0
+
+
 def test_reductions(xy):
     x, _, _ = xy
     X = RV.from_array(0.0, x)

@@ -141,6 +141,15 @@ def test_deterministic_random_variables_on_the_host():
     assert np.isnan(RV.constant(0.0, 1.0).pow(float("nan")).doubleValue())
     assert np.isnan(RV.constant(0.0, -1.0).pow(float("inf")).doubleValue())
     assert RV.constant(0.0, 2.0).pow(10.0).doubleValue() == 1024.0
+    # ... and its exact exponents (fdlibm e_pow): +-1, 2, and 0.5 for x >= +0
+    for x in (3.0, 1.0 / 3.0, 0.1, 7.25e-300, 1e300):
+        r = RV.constant(0.0, x)
+        assert r.pow(2.0).doubleValue() == r.squared().doubleValue() == x * x
+        assert r.pow(0.5).doubleValue() == r.sqrt().doubleValue() == np.sqrt(x)
+        assert r.pow(1.0).doubleValue() == x and r.pow(-1.0).doubleValue() == 1.0 / x
+    p = RV.constant(0.0, -0.0).pow(0.5).doubleValue()
+    assert p == 0.0 and not np.signbit(p)  # pow(-0, 0.5) = +0 where sqrt(-0) = -0
+    assert np.isnan(RV.constant(0.0, -4.0).pow(0.5).doubleValue())
     assert a.accrue(RV.constant(0.0, 0.03), 0.5).doubleValue() == 0.04 * (1 + 0.03 * 0.5)
     assert a.discount(RV.constant(0.0, 0.03), 0.5).doubleValue() == 0.04 / (1.0 + 0.03 * 0.5)
     assert a.choose(RV.constant(0.0, 1.0), RV.constant(0.0, 2.0)).doubleValue() == 1.0
@@ -148,6 +157,16 @@ def test_deterministic_random_variables_on_the_host():
     assert RV.constant(0.0, float("nan")).isNaN().doubleValue() == 1.0
     with pytest.raises(ValueError):
         a._scalar(99)  # unknown operation
+
+
+def test_reference_random_variable_kats_on_deterministic_values():
+    # montecarlo/RandomVariableTest.java:52-70: ((2 * 2 + 1)^2 - 4) / 7 = 3 on a deterministic value
+    from finmath_gb300.randomvariable import RandomVariableGPU as RV
+    r = F.RandomVariableGPUFactory().createRandomVariable(2.0)
+    r = r.mult(2.0).add(1.0).squared().sub(4.0).div(7.0)
+    assert r.getAverage() == 3.0 and r.getVariance() == 0.0 and r.isDeterministic()
+    assert r.getFiltrationTime() == float("-inf")  # createRandomVariable(value): measurable at -infinity
+    assert RV.constant(0.0, 3.0).getStandardDeviation() == 0.0
 
 
 @pytest.mark.parametrize("n,rank", [(1, 1), (4, 4), (6, 6), (6, 4), (12, 9)])
