@@ -118,6 +118,20 @@ class RandomVariableGPU:
     def average(self) -> "RandomVariableGPU":
         return RandomVariableGPU.constant(0.0, self.getAverage())
 
+    def apply(self, operator, *arguments):
+        """apply(DoubleUnaryOperator / DoubleBinaryOperator / DoubleTernaryOperator): a host
+        function cannot run on the device; unsupported, as the reference's own tests allow
+        (RandomVariableTest.java:233-272 accept UnsupportedOperationException)."""
+        raise NotImplementedError("apply(operator) is not supported on device random variables")
+
+    def getQuantile(self, quantile, *args):
+        """getQuantile / getQuantileExpectation / getHistogram need a device sort; not part of
+        this layer."""
+        raise NotImplementedError("quantiles are not supported on device random variables")
+
+    getQuantileExpectation = getQuantile
+    getHistogram = getQuantile
+
     def getConditionalExpectation(self, conditionalExpectationOperator):
         """RandomVariableFromDoubleArray.getConditionalExpectation: the estimator's estimate of this."""
         return conditionalExpectationOperator.getConditionalExpectation(self)

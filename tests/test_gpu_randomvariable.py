@@ -136,6 +136,20 @@ def test_reference_random_variable_kats():
     for check in (x.sqrt().sub(x.pow(0.5)), x.squared().sub(x.pow(2.0))):
         assert check.getAverage() == 0.0 and check.getVariance() == 0.0
     assert x.getStandardDeviation() - np.sqrt(x.getVariance()) == 0.0
+    # testAdd, testCap, testFloor (:175-231)
+    a = RV.from_array(0.0, [-4.0, -2.0, 0.0, 2.0, 4.0])
+    s = a.add(RV.from_array(0.0, [4.0, 2.0, 0.0, -2.0, -4.0]))
+    assert abs(s.getAverage()) <= 1e-15 and abs(s.getVariance()) <= 1e-15
+    var = (1.0 / 5.0) ** 2 * 4.0 / 5.0 + (1.0 - 1.0 / 5 - 0) ** 2 * 1.0 / 5.0
+    capped = a.cap(RV.from_array(0.0, [-3.0] * 5))
+    assert capped.getAverage() == pytest.approx(-3.0 - 1.0 / 5, abs=1e-15)
+    assert capped.getVariance() == pytest.approx(var, abs=1e-15)
+    floored = a.floor(RV.from_array(0.0, [3.0] * 5))
+    assert floored.getAverage() == pytest.approx(3.0 + 1.0 / 5, abs=1e-15)
+    assert floored.getVariance() == pytest.approx(var, abs=1e-15)
+    # testApply: apply(DoubleUnaryOperator) is allowed to be unsupported (:233-251)
+    with pytest.raises(NotImplementedError):
+        a.apply(lambda v: np.exp(v * 2.0))
 
 
 def test_reductions(xy):

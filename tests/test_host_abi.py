@@ -200,3 +200,12 @@ def test_swaption_constructors_follow_the_reference_overloads():
         F.Swaption(5.0, fix)
     with pytest.raises(ValueError):
         F.Swaption(5.0, fix, pay[:2], 0.05)
+
+
+def test_unsupported_random_variable_operations_raise():
+    # apply(operator) and quantiles: UnsupportedOperationException in the reference's terms
+    from finmath_gb300.randomvariable import RandomVariableGPU as RV
+    r = RV.constant(0.0, 1.0)
+    for call in (lambda: r.apply(abs), lambda: r.getQuantile(0.5), lambda: r.getHistogram([0.0])):
+        with pytest.raises(NotImplementedError):
+            call()
