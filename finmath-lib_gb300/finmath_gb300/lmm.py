@@ -631,6 +631,40 @@ class LIBORMonteCarloSimulationFromLIBORModel:
         from .randomvariable import RandomVariableGPU
         return RandomVariableGPU.constant(float("-inf"), value)
 
+    # -- the rest of the facade (LIBORMonteCarloSimulationFromLIBORModel.java:53-165)
+    def getMonteCarloWeights(self, timeOrIndex):
+        """Equal weights 1/P (MonteCarloProcessFromProcessModel's weights), as a deterministic
+        random variable; a time is mapped to the index at or before it (:58-64)."""
+        from .randomvariable import RandomVariableGPU
+        if isinstance(timeOrIndex, float):
+            i = self.getTimeIndex(timeOrIndex)
+            timeOrIndex = i if i >= 0 else (-i - 1) - 1
+        return RandomVariableGPU.constant(self.getTime(int(timeOrIndex)), 1.0 / self.getNumberOfPaths())
+
+    def getNumberOfFactors(self):
+        return self.process.brownianMotion.getNumberOfFactors()
+
+    def getTime(self, timeIndex):
+        return self.process.getTimeDiscretization().getTime(timeIndex)
+
+    def getTimeIndex(self, time):
+        return self.process.getTimeDiscretization().getTimeIndex(time)
+
+    def getBrownianMotion(self):
+        return self.process.brownianMotion
+
+    def getNumberOfComponents(self):
+        return self.model.getNumberOfComponents()
+
+    getNumberOfLibors = getNumberOfComponents
+
+    def getProcess(self):
+        return self.process
+
+    def getLIBORs(self, timeIndex):
+        """getLIBORs (:113-121): every component at a time index, as device random variables."""
+        return [self.getLIBORRandomVariable(timeIndex, j) for j in range(self.getNumberOfComponents())]
+
     def getReferenceDate(self):
         return self.model.getReferenceDate()
 

@@ -174,3 +174,16 @@ def dated_host(monkeypatch):
 
 def test_schedule_swaption_compositions(dated_host):
     TG.test_swaptions_on_date_schedules(dated_host)
+
+
+def test_simulation_facade(lmm20_host):
+    # LIBORMonteCarloSimulationFromLIBORModel.java:53-165 over the host double
+    cfg, m, osim, sim = lmm20_host
+    w = sim.getMonteCarloWeights(1.2)  # a time between simulation times: the index before it
+    assert w.isDeterministic() and w.getAverage() == 1.0 / sim.getNumberOfPaths() and w.getFiltrationTime() == 1.0
+    assert sim.getMonteCarloWeights(3).getFiltrationTime() == 1.5
+    assert sim.getTimeIndex(2.0) == 4 and sim.getTime(4) == 2.0 and sim.getTimeIndex(2.1) < 0
+    assert sim.getNumberOfComponents() == sim.getNumberOfLibors() == 20
+    libors = sim.getLIBORs(4)
+    assert len(libors) == 20 and np.array_equal(libors[7].getRealizations(), osim.process_value(4, 7))
+    assert sim.getLiborPeriod(3) == 1.5 and sim.getLiborPeriodIndex(1.5) == 3 and sim.getLiborPeriodIndex(1.6) < 0
