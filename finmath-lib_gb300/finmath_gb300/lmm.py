@@ -10,7 +10,6 @@ setup in its C++ part, simulation and valuation in its CUDA kernels.
 from __future__ import annotations
 
 import ctypes
-from dataclasses import dataclass, field
 
 import numpy as np
 

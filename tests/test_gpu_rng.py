@@ -3,7 +3,6 @@ import numpy as np
 import pytest
 
 import finmath_gb300 as F
-from finmath_gb300 import workloads as W
 from oracle import pyoracle as po
 
 pytestmark = pytest.mark.gpu

@@ -1,7 +1,6 @@
 """Analytic formulas of the calibration products and SwaptionSimple's value units, host only."""
 import math
 
-import numpy as np
 import pytest
 
 import finmath_gb300 as F
