@@ -775,7 +775,10 @@ class BermudanSwaption:
     """net.finmath.montecarlo.interestrate.products.BermudanSwaption.
 
     regressionBasisFunctionsProvider: None for the reference's built-in basis, or
-    "swaprate" for the {1, S, S^2, N, N^2, S*N} provider.
+    "swaprate" for the {1, S, S^2, N, N^2, S*N} provider (both fused into the library's
+    Bermudan kernels); or any object with getBasisFunctions(fixingDate, model) returning
+    random variables (RegressionBasisFunctionsProvider.java:28), which runs the reference's
+    getValues (BermudanSwaption.java:91-157) on device random variables with that basis.
     """
 
     def __init__(self, isPeriodStartDateExerciseDate, fixingDates, periodLength, paymentDates, periodNotionals, swaprates,
@@ -788,14 +791,69 @@ class BermudanSwaption:
         self.periodNotionals = _f64(np.broadcast_to(periodNotionals, (n,)))
         self.swaprates = _f64(np.broadcast_to(swaprates, (n,)))
         self.isCallable = bool(isCallable)
-        if regressionBasisFunctionsProvider in (None, "reference"):
+        self.provider = None
+        if regressionBasisFunctionsProvider is None or (isinstance(regressionBasisFunctionsProvider, str)
+                                                        and regressionBasisFunctionsProvider == "reference"):
             self.basis = _lib.BASIS_REFERENCE
-        elif regressionBasisFunctionsProvider == "swaprate":
+        elif isinstance(regressionBasisFunctionsProvider, str) and regressionBasisFunctionsProvider == "swaprate":
             self.basis = _lib.BASIS_SWAPRATE
+        elif hasattr(regressionBasisFunctionsProvider, "getBasisFunctions"):
+            self.basis, self.provider = None, regressionBasisFunctionsProvider
         else:
             raise ValueError("unknown regression basis provider")
 
+    def getExerciseTimes(self):
+        """BermudanSwaption.getExerciseTimes (:254-262): the exercisable fixing dates."""
+        return [float(f) for f, e in zip(self.fixingDates, self.isPeriodStartDateExerciseDate) if e]
+
+    def getBasisFunctions(self, fixingDate, model):
+        """The built-in basis (:215-252) as device random variables: 1, the discount factor to the
+        next payment and to the end and their squares, and 1/N(fixingDate)."""
+        from .randomvariable import RandomVariableGPU
+        fix, pay = list(self.fixingDates), list(self.paymentDates)
+        import bisect
+        i = bisect.bisect_left(fix, fixingDate)
+        if not (i < len(fix) and fix[i] == fixingDate):
+            i = i + 1  # the reference's -(-(insertion) - 1)
+        i = min(i, len(fix) - 1)
+        rateShort = model.getForwardRate(fixingDate, fixingDate, pay[i])
+        discountShort = rateShort.mult(pay[i] - fixingDate).add(1.0).invert()
+        rateLong = model.getForwardRate(fixingDate, fix[i], pay[-1])
+        discountLong = rateLong.mult(pay[-1] - fix[i]).add(1.0).invert()
+        return [RandomVariableGPU.constant(float("-inf"), 1.0), discountShort, discountShort.pow(2.0), discountLong,
+                discountLong.pow(2.0), model.getNumeraireRandomVariable(fixingDate).invert()]
+
+    def _getValuesRandomVariable(self, model, evaluationTime=0.0):
+        # BermudanSwaption.getValues (:91-157) on device random variables
+        from .randomvariable import MonteCarloConditionalExpectationRegression, RandomVariableGPU
+        const = lambda v: RandomVariableGPU.constant(float("-inf"), v)
+        values, underlying, exerciseTime = const(0.0), const(0.0), const(float("inf"))
+        for period in range(len(self.fixingDates) - 1, -1, -1):
+            fixingDate, periodLength = float(self.fixingDates[period]), float(self.periodLengths[period])
+            paymentDate, notional = float(self.paymentDates[period]), float(self.periodNotionals[period])
+            libor = model.getForwardRate(fixingDate, fixingDate, fixingDate + periodLength)
+            payoff = libor.sub(float(self.swaprates[period])).mult(periodLength).mult(notional)
+            payoff = payoff.div(model.getNumeraireRandomVariable(paymentDate)).mult(model.getMonteCarloWeights(paymentDate))
+            if self.isCallable:
+                underlying = underlying.add(payoff)
+            else:
+                values = values.add(payoff)
+            if self.isPeriodStartDateExerciseDate[period]:
+                estimator = MonteCarloConditionalExpectationRegression(self.provider.getBasisFunctions(fixingDate, model))
+                trigger = values.sub(underlying).getConditionalExpectation(estimator)
+                values = trigger.choose(values, underlying)
+                exerciseTime = trigger.choose(exerciseTime, const(fixingDate))
+        values = values.mult(model.getNumeraireRandomVariable(evaluationTime)).div(
+            model.getMonteCarloWeights(evaluationTime))
+        return values, exerciseTime
+
     def getValues(self, model: LIBORMonteCarloSimulationFromLIBORModel, per_path: bool = False):
+        if self.provider is not None:
+            values, exerciseTime = self._getValuesRandomVariable(model)
+            out = {"value": values.getAverage(), "error": values.getStandardError(), "exerciseTime": exerciseTime}
+            if per_path:
+                out["values"] = values.getRealizations()
+            return out
         d = _lib.LmmBermudanDesc(len(self.fixingDates),
                                  self.isPeriodStartDateExerciseDate.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)),
                                  _p(self.fixingDates), _p(self.periodLengths), _p(self.paymentDates),
@@ -813,6 +871,8 @@ class BermudanSwaption:
         return self.getValues(model)["value"]
 
     def _desc(self):
+        if self.provider is not None:
+            raise ValueError("the fused Bermudan kernels (gradient, portfolio) take the built-in or swap-rate basis")
         return _lib.LmmBermudanDesc(len(self.fixingDates),
                                     self.isPeriodStartDateExerciseDate.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)),
                                     _p(self.fixingDates), _p(self.periodLengths), _p(self.paymentDates),

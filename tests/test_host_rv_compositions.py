@@ -187,3 +187,25 @@ def test_simulation_facade(lmm20_host):
     libors = sim.getLIBORs(4)
     assert len(libors) == 20 and np.array_equal(libors[7].getRealizations(), osim.process_value(4, 7))
     assert sim.getLiborPeriod(3) == 1.5 and sim.getLiborPeriodIndex(1.5) == 3 and sim.getLiborPeriodIndex(1.6) < 0
+
+
+def test_bermudan_with_a_user_basis_provider(lmm20_host):
+    # BermudanSwaption.getValues (BermudanSwaption.java:91-157) with a user
+    # RegressionBasisFunctionsProvider: a provider returning the built-in basis (:215-252)
+    # reprices the oracle's Bermudan with that basis, path by path
+    cfg, m, osim, sim = lmm20_host
+    fix, plen, pay, K = W.bermudan_schedule(cfg)
+    builtin = finmath_gb300.BermudanSwaption(np.ones(len(fix)), fix, plen, pay, 1.0, K, True, None)
+
+    class Provider:
+        def getBasisFunctions(self, fixingDate, model):
+            return builtin.getBasisFunctions(fixingDate, model)
+
+    custom = finmath_gb300.BermudanSwaption(np.ones(len(fix)), fix, plen, pay, 1.0, K, True, Provider())
+    r = custom.getValues(sim, per_path=True)
+    v, e, pp, et = osim.bermudan(fix, plen, pay, K, basis_id=0, per_path=True)  # 0: the built-in basis
+    assert r["value"] == pytest.approx(v, rel=1e-10) and r["error"] == pytest.approx(e, rel=1e-8)
+    assert np.mean(np.abs(r["values"] - pp) <= 1e-10 * np.max(np.abs(pp))) >= 0.999
+    assert custom.getExerciseTimes() == list(fix)
+    with pytest.raises(ValueError):
+        custom._desc()  # the fused gradient and portfolio kernels take the built-in bases only
