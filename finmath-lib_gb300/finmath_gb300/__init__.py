@@ -11,7 +11,7 @@ from .lmm import (TimeDiscretizationFromArray, ForwardCurveInterpolation, Discou
                   LIBORVolatilityModelFromGivenMatrix, LIBORCovarianceModelFromVolatilityAndCorrelation,
                   LIBORMarketModelFromCovarianceModel, BrownianMotionFromMersenneRandomNumbers,
                   EulerSchemeFromProcessModel, LIBORMonteCarloSimulationFromLIBORModel, Swaption, SwaptionSimple,
-                  BermudanSwaption, Portfolio,
+                  SwaptionAnalyticApproximation, BermudanSwaption, Portfolio,
                   mersenne_twister_uniforms, kernel_stats)
 from .randomvariable import RandomVariableGPU, RandomVariableGPUFactory, MonteCarloConditionalExpectationRegression
 from .rvproducts import (Bond, BermudanSwaptionFromSwapSchedules, Caplet, DigitalCaplet, DigitalFloorlet, LIBORBond,

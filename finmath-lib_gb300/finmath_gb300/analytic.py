@@ -77,15 +77,25 @@ def blackScholesOptionImpliedVolatility(forward, optionMaturity, optionStrike, p
     return solver.bestPoint
 
 
-def blackScholesOptionValue(forward, volatility, optionMaturity, optionStrike, payoffUnit) -> float:
-    """The Black value of a call on the forward (for tests and targets)."""
+def blackScholesGeneralizedOptionValue(forward, volatility, optionMaturity, optionStrike, payoffUnit) -> float:
+    """The Black value of a call on the forward (functions/AnalyticFormulas.java:54-78): a
+    negative forward by put-call parity, the intrinsic value when the forward, strike,
+    volatility or maturity leaves nothing to integrate."""
     if optionMaturity < 0:
         return 0.0
-    if volatility == 0.0 or optionMaturity == 0.0 or optionStrike <= 0.0:
+    if forward < 0:
+        return ((forward - optionStrike) * payoffUnit
+                + blackScholesGeneralizedOptionValue(-forward, volatility, optionMaturity, -optionStrike, payoffUnit))
+    if forward == 0 or optionStrike <= 0.0 or volatility <= 0.0 or optionMaturity <= 0.0:
         return max(forward - optionStrike, 0.0) * payoffUnit
-    s = volatility * math.sqrt(optionMaturity)
-    dPlus = (math.log(forward / optionStrike) + 0.5 * s * s) / s
-    return (forward * normal_cdf(dPlus) - optionStrike * normal_cdf(dPlus - s)) * payoffUnit
+    dPlus = ((math.log(forward / optionStrike) + 0.5 * volatility * volatility * optionMaturity)
+             / (volatility * math.sqrt(optionMaturity)))
+    dMinus = dPlus - volatility * math.sqrt(optionMaturity)
+    return (forward * normal_cdf(dPlus) - optionStrike * normal_cdf(dMinus)) * payoffUnit
+
+
+blackScholesOptionValue = blackScholesGeneralizedOptionValue
+blackModelSwaptionValue = blackScholesGeneralizedOptionValue  # AnalyticFormulas.java:985-993
 
 
 def bachelierOptionValue(forward, volatility, optionMaturity, optionStrike, payoffUnit) -> float:

@@ -10,6 +10,7 @@ setup in its C++ part, simulation and valuation in its CUDA kernels.
 from __future__ import annotations
 
 import ctypes
+import math
 
 import numpy as np
 
@@ -324,6 +325,36 @@ class LIBORMarketModelFromCovarianceModel:
 
     def getCovarianceModel(self):
         return self.covarianceModel
+
+    def getIntegratedLIBORCovariance(self, simulationTimeDiscretization):
+        """LIBORMarketModelFromCovarianceModel.getIntegratedLIBORCovariance (:1552-1596):
+        [t][i][j] = the sum over simulation steps up to t of lambda_i . lambda_j dt, each step
+        counting only components not yet fixed (T_i above the step's start); the upper
+        triangle of step 0 and both triangles after it, as the reference fills them."""
+        cov = self.covarianceModel
+        tenor = self.liborPeriodDiscretization
+        n, N = simulationTimeDiscretization.getNumberOfTimeSteps(), tenor.getNumberOfTimeSteps()
+        out = np.zeros((n, N, N))
+        for t in range(n):
+            time = simulationTimeDiscretization.getTime(t)
+            dt = simulationTimeDiscretization.getTime(t + 1) - time
+            ct = cov.timeDiscretization.getTimeIndex(time)
+            ct = ct if ct >= 0 else -ct - 2
+            loadings = cov.factorLoadings[ct]
+            for i in range(N):
+                if tenor.getTime(i) <= time:
+                    continue
+                for j in range(i, N):
+                    v = 0.0
+                    for k in range(loadings.shape[1]):
+                        v += float(loadings[i, k]) * float(loadings[j, k]) * dt
+                    out[t, i, j] = v
+        for t in range(1, n):
+            for i in range(N):
+                for j in range(i, N):
+                    out[t, i, j] = out[t - 1, i, j] + out[t, i, j]
+                    out[t, j, i] = out[t, i, j]
+        return out
 
     def getCloneWithModifiedCovarianceModel(self, covarianceModel):
         """:1646-1650: the same model with another covariance model."""
@@ -769,6 +800,85 @@ class SwaptionSimple:
         else:
             v = A.bachelierOptionImpliedVolatility(parSwaprate, optionMaturity, self.swaprate, annuity, value)
         return v * v * optionMaturity
+
+
+class SwaptionAnalyticApproximation:
+    """net.finmath.montecarlo.interestrate.products.SwaptionAnalyticApproximation (host
+    arithmetic on the model's tables, no simulation): Rebonato's frozen-weight swap-rate
+    variance  sum_ij w_i w_j C_ij(T0)  from the log swap-rate derivatives w (:188-281) and
+    the integrated LIBOR covariance C up to the option maturity, returned as the integrated
+    variance, the Black volatility, or the Black price on the par swap rate and annuity
+    (:125-172)."""
+
+    def __init__(self, swaprate, swapTenor, valueUnit="VALUE"):
+        t = swapTenor.getAsDoubleArray() if isinstance(swapTenor, TimeDiscretizationFromArray) else _f64(swapTenor)
+        self.swapTenor = [float(x) for x in t]
+        self.swaprate = float(swaprate)
+        self.valueUnit = str(valueUnit).upper()
+        if self.valueUnit not in ("VALUE", "VOLATILITY", "VOLATILITYLOGNORMAL", "INTEGRATEDVARIANCE",
+                                  "INTEGRATEDVARIANCELOGNORMAL"):
+            raise ValueError(f"Unknown valueUnit: {valueUnit}")
+
+    def getLogSwaprateDerivative(self, liborPeriodDiscretization, discountCurve, forwardCurve):
+        if discountCurve is None:
+            discountCurve = DiscountCurveFromForwardCurve(forwardCurve)
+        tenor, swapTenor = liborPeriodDiscretization, self.swapTenor
+        start, end = tenor.getTimeIndex(swapTenor[0]), tenor.getTimeIndex(swapTenor[-1])
+        forwardRates = [0.0] * (end - start + 1)
+        discountFactors = [0.0] * (end - start + 1)
+        discountFactors[0] = discountCurve.getDiscountFactor(None, swapTenor[0])
+        for j in range(start, end):
+            forwardRates[j - start] = forwardCurve.getForward(None, tenor.getTime(j))
+            discountFactors[j - start + 1] = discountCurve.getDiscountFactor(None, tenor.getTime(j + 1))
+        swapAnnuities = [0.0] * (len(swapTenor) - 1)
+        swapAnnuity = 0.0
+        for k in range(len(swapTenor) - 2, -1, -1):
+            periodEnd = tenor.getTimeIndex(swapTenor[k + 1])
+            swapAnnuity += discountFactors[periodEnd - start] * (swapTenor[k + 1] - swapTenor[k])
+            swapAnnuities[k] = swapAnnuity
+        valueFloatLeg = 0.0
+        for j in range(start, end):
+            valueFloatLeg += forwardRates[j - start] * discountFactors[j - start + 1] * tenor.getTimeStep(j)
+        weights = [0.0] * (end - start)
+        k, upToStart = 0, 0.0
+        for j in range(start, end):
+            if tenor.getTime(j) >= swapTenor[k + 1]:
+                k += 1
+            libor, length = forwardRates[j - start], tenor.getTimeStep(j)
+            upToStart += forwardRates[j - start] * discountFactors[j - start + 1] * length
+            dfEnd = discountCurve.getDiscountFactor(None, tenor.getTime(j + 1))
+            dFloat = (dfEnd + upToStart - valueFloatLeg) * length / (1.0 + libor * length) / valueFloatLeg
+            dFix = -swapAnnuities[k] / swapAnnuity * length / (1.0 + libor * length)
+            weights[j - start] = (dFloat - dFix) * libor
+        return {"values": weights, "discountFactors": discountFactors, "swapAnnuities": swapAnnuities}
+
+    def getValue(self, model, evaluationTime: float = 0.0):
+        from . import analytic as A
+        if evaluationTime > 0:
+            raise ValueError("Forward start evaluation currently not supported.")
+        m = model.model if hasattr(model, "model") and hasattr(model, "process") else model
+        td = model.getTimeDiscretization() if m is not model else m.covarianceModel.timeDiscretization
+        swapStart, swapEnd = self.swapTenor[0], self.swapTenor[-1]
+        tenor = m.liborPeriodDiscretization
+        start, end = tenor.getTimeIndex(swapStart), tenor.getTimeIndex(swapEnd)
+        maturityIndex = m.covarianceModel.timeDiscretization.getTimeIndex(swapStart) - 1
+        w = self.getLogSwaprateDerivative(tenor, m.discountCurve, m.forwardRateCurve)["values"]
+        C = m.getIntegratedLIBORCovariance(td)[maturityIndex]
+        variance = 0.0
+        for i in range(start, end):
+            for j in range(i + 1, end):
+                variance += 2.0 * w[i - start] * w[j - start] * C[i, j]
+            variance += w[i - start] * w[i - start] * C[i, i]
+        if self.valueUnit in ("INTEGRATEDVARIANCELOGNORMAL", "INTEGRATEDVARIANCE"):
+            return variance
+        volatility = math.sqrt(variance / swapStart)
+        if self.valueUnit in ("VOLATILITYLOGNORMAL", "VOLATILITY"):
+            return volatility
+        dc = m.discountCurve if m.discountCurve is not None else DiscountCurveFromForwardCurve(m.forwardRateCurve)
+        tenorSwap = TimeDiscretizationFromArray(self.swapTenor)
+        par = A.forward_swap_rate(tenorSwap, m.forwardRateCurve, dc)
+        annuity = A.swap_annuity(tenorSwap, dc)
+        return A.blackModelSwaptionValue(par, volatility, swapStart, self.swaprate, annuity)
 
 
 class BermudanSwaption:

@@ -1,6 +1,7 @@
 """Analytic formulas of the calibration products and SwaptionSimple's value units, host only."""
 import math
 
+import numpy as np
 import pytest
 
 import finmath_gb300 as F
@@ -84,3 +85,58 @@ def test_swaption_simple_value_units():
     assert plain.swaption.exerciseDate == 5.0 and list(plain.swaption.fixingDates) == list(tenor.getAsDoubleArray()[:-1])
     with pytest.raises(ValueError):
         F.SwaptionSimple(K, tenor, "PERCENT")
+
+
+def _lmm_model(cfg):
+    td = F.TimeDiscretizationFromArray(0.0, int(round(cfg["T_end"] / cfg["dt"])), cfg["dt"])
+    tenor = F.TimeDiscretizationFromArray(0.0, int(round(cfg["tenor_end"] / cfg["period"])), cfg["period"])
+    curve = F.ForwardCurveInterpolation.createForwardCurveFromForwards("forwardCurve", cfg["curve_nodes"],
+                                                                       cfg["curve_values"], cfg["period"])
+    cov = F.LIBORCovarianceModelFromVolatilityAndCorrelation(
+        td, tenor, F.LIBORVolatilityModelFourParameterExponentialForm(td, tenor, *cfg["abcd"]),
+        F.LIBORCorrelationModelExponentialDecay(td, tenor, cfg["F"], cfg["corr_decay"]))
+    return F.LIBORMarketModelFromCovarianceModel.of(tenor, None, curve, F.DiscountCurveFromForwardCurve(curve), None,
+                                                    cov)
+
+
+def test_integrated_libor_covariance_matches_the_oracle_loadings():
+    # getIntegratedLIBORCovariance (LIBORMarketModelFromCovarianceModel.java:1552-1596)
+    from conftest import oracle_model
+    cfg = W.LMM40
+    model = _lmm_model(cfg)
+    m = oracle_model(cfg)
+    C = model.getIntegratedLIBORCovariance(model.covarianceModel.timeDiscretization)
+    times, tenor = m.times, m.tenor
+    acc = np.zeros((len(tenor) - 1, len(tenor) - 1))
+    for t in (0, 7, 39, 79):
+        acc[:] = 0.0
+        for s in range(t + 1):
+            alive = tenor[:-1] > times[s]
+            lam = m.loadings[s] * alive[:, None]
+            acc += (lam @ lam.T) * (times[s + 1] - times[s])
+        upper = np.triu_indices(len(tenor) - 1)
+        assert np.allclose(C[t][upper], acc[upper], rtol=1e-12, atol=1e-18)
+
+
+def test_swaption_analytic_approximation():
+    # SwaptionAnalyticApproximation (products/SwaptionAnalyticApproximation.java): on a flat curve
+    # its log swap-rate derivatives are Rebonato's frozen weights, so it equals that formula
+    from conftest import oracle_model
+    from test_oracle_lmm import black_swaption_rebonato
+    for cfg, cases, tol in ((W.LMM20, ((5.0, 10.0, 0.05), (2.0, 4.0, 0.045), (1.0, 9.5, 0.055)), 1e-12),
+                            (W.LMM40, ((10.0, 20.0, 0.04), (2.0, 4.0, 0.035)), 5e-3)):
+        model, m = _lmm_model(cfg), oracle_model(cfg)
+        for ex, end, K in cases:
+            fix = np.arange(ex, end - 1e-12, cfg["period"])
+            tenor = list(fix) + [end]
+            value = F.SwaptionAnalyticApproximation(K, tenor).getValue(model)
+            assert value == pytest.approx(black_swaption_rebonato(m, ex, fix, fix + cfg["period"], K), rel=tol)
+            var = F.SwaptionAnalyticApproximation(K, tenor, "INTEGRATEDVARIANCE").getValue(model)
+            vol = F.SwaptionAnalyticApproximation(K, tenor, "VOLATILITY").getValue(model)
+            assert vol == math.sqrt(var / ex)
+            dc = F.DiscountCurveFromForwardCurve(model.forwardRateCurve)
+            td = F.TimeDiscretizationFromArray(tenor)
+            assert value == A.blackModelSwaptionValue(A.forward_swap_rate(td, model.forwardRateCurve, dc), vol, ex, K,
+                                                      A.swap_annuity(td, dc))
+    with pytest.raises(ValueError):
+        F.SwaptionAnalyticApproximation(0.05, [1.0, 2.0], "VOLATILITYNORMAL")
