@@ -10,6 +10,8 @@ time steps / seconds.  Synthetic inputs as the workload defines them; the Browni
 increments (6.7 GB) are larger than L2, so no separate flush is needed.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+  python bench.py --case valuation|greeks|portfolio --precision fp64|mixed --paths P --repeat R
+      (one named valuation case, for profiling single kernels under ncu)
 
 --impl reference times the CPU restatement of the reference's algorithm (the oracle,
 C, all host threads) on a bounded sample of the same workload; under torchrun only
@@ -117,6 +119,60 @@ def cpu_baseline(paths: int, threads: int):
     return paths * m.T / dt, dt, berm, swpt
 
 
+def headline_parity(F, W, cfg, sim, berm, swpt, paths, threads):
+    """The oracle's valuation of the same workload, timed as the CPU baseline and, when it
+    runs at the bench's own path count, compared with the GPU's FP64 valuation of the same
+    paths (outside the timed region): Bermudan and swaption value and standard error,
+    every per-path Bermudan value, and forward rates and numeraires at a few times."""
+    from oracle import pyoracle as po
+    m = po.build_model(**{k: cfg[k] for k in ("dt", "T_end", "period", "tenor_end", "F", "corr_decay", "abcd",
+                                              "curve_nodes", "curve_values")})
+    obs = np.zeros(m.T + 1, np.uint8)
+    tenor_tidx = W.tenor_time_indices(cfg)
+    obs[tenor_tidx] = 1
+    fix, plen, pay, K = W.bermudan_schedule(cfg)
+    ex, sfix, spay, sK = W.swaption_schedule(cfg)
+    t0 = time.perf_counter()
+    dW = po.brownian_increments(m.times, m.F, paths, cfg["seed"])
+    osim = po.Simulation(m, dW, observe=obs, threads=threads)
+    ob = osim.bermudan(fix, plen, pay, K, basis_id=1, per_path=True)
+    os_ = osim.swaption(ex, sfix, spay, sK)
+    dt = time.perf_counter() - t0
+    del dW
+    rate = paths * m.T / dt
+    if sim is None or paths != sim.getNumberOfPaths() or sim.process.brownianMotion.precision != F.PRECISION_FP64:
+        return rate, dt, None
+    gb = berm.getValues(sim, per_path=True)
+    gs = swpt.getValues(sim)
+
+    def rel(a, b):
+        return abs(a - b) / abs(b)
+
+    vg, vo = gb["values"], ob[2]
+    scale = float(np.max(np.abs(vo)))
+    dpath = np.abs(vg - vo)
+    states = []
+    for t, j in ((tenor_tidx[20], 39), (tenor_tidx[-1], 39), (tenor_tidx[2], 10)):
+        g, o = sim.process.getProcessValue(int(t), j), osim.process_value(int(t), j)
+        states.append({"time_index": int(t), "component": j, "max_rel": float(np.max(np.abs(g - o) / np.abs(o)))})
+    nums = []
+    for T_ in (1.0, 10.0, 20.0):
+        g, o = sim.process.getNumeraire(T_), osim.numeraire(T_)
+        nums.append({"time": T_, "max_rel": float(np.max(np.abs(g - o) / np.abs(o)))})
+    parity = {
+        "paths": paths, "oracle": "oracle/lmm_oracle.c (C restatement of the reference, OpenMP)",
+        "bermudan": {"gpu": gb["value"], "oracle": ob[0], "rel": rel(gb["value"], ob[0]),
+                     "error_gpu": gb["error"], "error_oracle": ob[1], "error_rel": rel(gb["error"], ob[1])},
+        "swaption": {"gpu": gs["value"], "oracle": os_[0], "rel": rel(gs["value"], os_[0]),
+                     "error_gpu": gs["error"], "error_oracle": os_[1], "error_rel": rel(gs["error"], os_[1])},
+        "bermudan_per_path": {"paths_compared": int(vg.size), "max_abs_over_max_value": float(np.max(dpath) / scale),
+                              "paths_beyond_1e-12": int(np.count_nonzero(dpath > 1e-12 * scale))},
+        "forward_rates": states, "numeraires": nums,
+    }
+    parity["within_1e-12"] = bool(parity["bermudan"]["rel"] <= 1e-12 and parity["swaption"]["rel"] <= 1e-12)
+    return rate, dt, parity
+
+
 def run_reference(args):
     ws, rank, local = _dist()
     if rank != 0:
@@ -143,17 +199,19 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def _from_profile(key):
-    """A figure of the path kernel's committed ncu summary (DRAM bytes per launch, FP64 pipe
-    share), if present."""
-    path = os.path.join(HERE, "profiles", "lmm_paths_fp64_lmm40.md")
+def _ncu_counters(kernel, paths):
+    """DRAM bytes per launch of a path kernel from the committed ncu counters
+    (profiles/ncu_counters.json: one capture on a smaller case), scaled to `paths` by the
+    path count (the kernel streams increments in and states out per path, so its traffic
+    grows in proportion), with the pipe activity of the same capture; None if absent."""
     try:
-        for ln in open(path):
-            if ln.startswith(key + ":"):
-                return float(ln.split(":", 1)[1].strip())
-    except OSError:
-        pass
-    return None
+        with open(os.path.join(HERE, "profiles", "ncu_counters.json")) as f:
+            rec = json.load(f)[kernel]
+    except (OSError, ValueError, KeyError):
+        return None
+    scale = paths / rec["paths"]
+    return {"traffic": (rec["dram_bytes_read"] + rec["dram_bytes_write"]) * scale,
+            "pipe_active": rec.get("pipe_active"), "captured_paths": rec["paths"], "scale": scale}
 
 
 def _measured_hbm_gbs():
@@ -275,7 +333,8 @@ def run_ours(args):
     L.lmm_probe_fp64_fma_rate(ctypes.byref(fma))
     peak = 2.0 * fma.value / 1e12
     achieved = flops / k_avg_s / 1e12
-    traffic = _from_profile("traffic_bytes_per_launch") if prec == F.PRECISION_FP64 and P == (1 << 20) else None
+    counters = _ncu_counters(kname, P)
+    traffic = counters["traffic"] if counters else None
     roofline = {"bound": "fp64" if prec == F.PRECISION_FP64 else "fp32", "kernel": kname,
                 "achieved": achieved, "peak": peak if prec == F.PRECISION_FP64 else None, "unit": "TFLOP/s",
                 "frac": achieved / peak if prec == F.PRECISION_FP64 else None, "traffic": traffic,
@@ -284,12 +343,13 @@ def run_ours(args):
                                "MEASURED_PEAKS.json holds no FP64 figure",
                 "component_steps_per_path": comp_steps,
                 "transcendentals_per_launch": {"exp_small": P * comp_steps, "rcp_newton": P * comp_steps},
-                "ncu_fp64_pipe_active": _from_profile("fp64_pipe_active") if prec == F.PRECISION_FP64 else None,
+                "ncu_pipe_active": counters["pipe_active"] if counters else None,
+                "traffic_source": (f"ncu DRAM read+write of one launch at {counters['captured_paths']} paths, "
+                                   f"scaled x{counters['scale']:g} by the path count") if counters else None,
                 "note": "algorithmic flops count the reference algorithm's add/mul per component-step (its "
                         "log, exp and division as one each); the FP64 kernel fuses them into FMAs, evaluates "
                         "the log-Euler step as L exp(d) with a table-driven 9-instruction exp and replaces the "
-                        "division by a 4-FMA Newton reciprocal, and is FP64-pipe bound "
-                        "(ncu, profiles/lmm_paths_fp64_lmm40.md)"}
+                        "division by a 4-FMA Newton reciprocal, and is FP64-pipe bound"}
 
     # ---------------- end to end through the C ABI with host buffers (tables in, prices out)
     e2e_times = []
@@ -345,9 +405,11 @@ def run_ours(args):
             line["forms"]["portfolio"] = portfolio_form(args, F, W, cfg, P)
         line["forms"]["random_variable"] = random_variable_form(args, F, W, cfg, P)
     if rank == 0 and not args.no_cpu_baseline:
-        v, dt, _, _ = cpu_baseline(args.cpu_paths, os.cpu_count() or 1)
+        v, dt, parity = headline_parity(F, W, cfg, sim, berm, swpt, args.cpu_paths, os.cpu_count() or 1)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                                 "sample": f"{args.cpu_paths} paths of lmm40, one pass ({dt:.1f} s)"}
+        if parity is not None:
+            line["parity"] = parity
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:
@@ -594,6 +656,43 @@ def portfolio_form(args, F, W, cfg, P):
     return res
 
 
+def run_case(args):
+    """A named valuation case for profiling single kernels under ncu (no JSON bench line):
+    each repetition regenerates the increments (seed + repetition) and values the
+    workload's Bermudan swaption; 'greeks' adds its adjoint deltas and vegas; 'portfolio'
+    runs a 16-product portfolio with Greeks through one graph launch.  Kernel counts and
+    (with --timing) CUDA-event times exclude the first repetition."""
+    import finmath_gb300 as F
+    from finmath_gb300 import workloads as W
+    L = F.load()
+    if args.timing:
+        L.lmm_stats_enable_timing(1)
+    cfg = W.WORKLOADS[args.workload]
+    prec = F.PRECISION_MIXED if args.precision == "mixed" else F.PRECISION_FP64
+    sim = W.build(cfg, paths=args.paths, precision=prec)
+    fix, plen, pay, K = W.bermudan_schedule(cfg)
+    berm = F.BermudanSwaption(np.ones(len(fix)), fix, plen, pay, 1.0, K, True, "swaprate")
+    out = None
+    if args.case == "portfolio":
+        pf = F.Portfolio(sim, W.portfolio_products(cfg, n=16, seed=20261203), True, args.stride, 4, 128, 0)
+        for r in range(args.repeat):
+            out = pf.run()["total_ms"]
+            if r == 0:
+                L.lmm_stats_reset()
+        pf.close()
+    else:
+        for r in range(args.repeat):
+            sim.process.brownianMotion.setSeed(cfg["seed"] + r)
+            if args.case == "greeks":
+                out = berm.getGradient(sim, checkpointStride=args.stride)["value"]
+            else:
+                out = berm.getValue(sim)
+            if r == 0:
+                L.lmm_stats_reset()
+    print(json.dumps({"case": args.case, "precision": args.precision, "paths": args.paths, "last": out,
+                      "kernels": F.kernel_stats()}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -602,15 +701,28 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--paths", type=int, default=1 << 20)
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
-    ap.add_argument("--cpu-paths", type=int, default=0, help="CPU sample paths (default 2^19 for the baseline leg, 2^18 per reference step)")
+    ap.add_argument("--cpu-paths", type=int, default=0,
+                    help="CPU sample paths (default: the bench's own path count for the baseline and parity leg, "
+                         "2^18 per reference step)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true")
     ap.add_argument("--no-portfolio", action="store_true")
+    ap.add_argument("--case", choices=["valuation", "greeks", "portfolio"], default=None,
+                    help="run one named valuation case for profiling instead of the bench")
+    ap.add_argument("--repeat", type=int, default=3, help="--case: repetitions")
+    ap.add_argument("--workload", default="lmm40", help="--case: workload name")
+    ap.add_argument("--stride", type=int, default=1, help="--case: checkpoint stride")
+    ap.add_argument("--timing", action="store_true", help="--case: CUDA-event time per kernel family")
     args = ap.parse_args()
+    if args.case:
+        if args.paths == (1 << 20) and "--paths" not in sys.argv:
+            args.paths = 65536
+        run_case(args)
+        return
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     if args.cpu_paths <= 0:
-        args.cpu_paths = (1 << 18) if args.impl == "reference" else (1 << 19)
+        args.cpu_paths = (1 << 18) if args.impl == "reference" else args.paths
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -1145,6 +1145,21 @@ int lmm_stats_h2d_bytes(int64_t* out)
     return LMM_OK;
 }
 
+int lmm_stats_pool_bytes(int64_t* out_reserved, int64_t* out_used)
+{
+    if (!out_reserved || !out_used) return lmm::fail(LMM_ERR_INVALID, "null argument");
+    int dev = 0;
+    cudaMemPool_t pool;
+    LMM_CUDA(cudaGetDevice(&dev));
+    LMM_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev));
+    uint64_t reserved = 0, used = 0;
+    LMM_CUDA(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &reserved));
+    LMM_CUDA(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used));
+    *out_reserved = (int64_t)reserved;
+    *out_used = (int64_t)used;
+    return LMM_OK;
+}
+
 int lmm_stats_reset(void)
 {
     collect_timings();

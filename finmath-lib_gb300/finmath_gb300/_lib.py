@@ -116,6 +116,7 @@ SIGNATURES = {
     "lmm_stats_enable_timing": (ctypes.c_int, [ctypes.c_int]),
     "lmm_stats_reset": (ctypes.c_int, []),
     "lmm_stats_h2d_bytes": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int64)]),
+    "lmm_stats_pool_bytes": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]),
     "lmm_stats_get": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_char_p), _I64, _D]),
     "lmm_process_stream": (ctypes.c_int, [_VP, ctypes.POINTER(_VP)]),
     "lmm_probe_fp64_fma_rate": (ctypes.c_int, [_D]),

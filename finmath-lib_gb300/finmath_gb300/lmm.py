@@ -340,6 +340,9 @@ class LIBORMarketModelFromCovarianceModel:
             dt = simulationTimeDiscretization.getTime(t + 1) - time
             ct = cov.timeDiscretization.getTimeIndex(time)
             ct = ct if ct >= 0 else -ct - 2
+            if ct < 0 or ct >= cov.factorLoadings.shape[0]:
+                # the reference's factor-loading lookup throws outside the covariance grid
+                raise ValueError(f"simulation time {time} outside the covariance model's time discretization")
             loadings = cov.factorLoadings[ct]
             for i in range(N):
                 if tenor.getTime(i) <= time:
@@ -621,7 +624,7 @@ class LIBORMonteCarloSimulationFromLIBORModel:
             ct = cov.timeDiscretization.getTimeIndex(td.getTime(sumTimeIndex))
             if ct < 0:
                 ct = -ct - 2
-            if ct >= cov.factorLoadings.shape[0]:
+            if ct < 0 or ct >= cov.factorLoadings.shape[0]:
                 raise ValueError("factor loading beyond the covariance model's time discretization")
             squares = 0.0  # getRandomVariableForConstant(0.0).add(oneFactor.squared()) per factor
             for loading in cov.getFactorLoading(ct, liborIndex):

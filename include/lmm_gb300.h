@@ -223,16 +223,18 @@ int lmm_bermudan_get_value(lmm_process* proc, const lmm_bermudan_desc* product, 
 /* Mean and standard error of num_values doubles already in device memory (d_values),
  * computed with the same compensated reduction as the product entry points, without
  * allocating anything.  No counterpart in finmath-lib: it exists for callers that must
- * not allocate device memory on their valuation path -- a service that reserves its
- * whole device budget at start-up and forbids allocator calls afterwards, or code that
- * records its work into a CUDA graph, where an allocation would become part of the
- * graph.  Its scratch is one fixed 8,208-byte array per GPU inside the library (held
- * until the process exits), so:
+ * not allocate device memory on their valuation path -- a pricing service that reserves
+ * its whole device budget at start-up and forbids allocator calls afterwards (a JVM host
+ * sharing one GPU between several engines, each held to a fixed slice), or code running
+ * where an allocator call would stall other work on the device.  Its scratch is one fixed
+ * 8,208-byte array per GPU inside the library (held until the process exits), so:
  *   - num_values must be in [1, 2^30]; larger inputs are rejected with LMM_ERR_INVALID;
  *   - every call shares that array: calls that overlap on the GPU (different streams, or
  *     different host threads on one device) race and must be serialised by the caller;
  *   - the first call on a device looks up the array's device address (which may load the
- *     library's GPU code on that device); make that first call before any stream capture.
+ *     library's GPU code on that device); make that first call before any stream capture;
+ *   - the looked-up address is kept for the life of the process: the library must not be
+ *     used on a device after cudaDeviceReset there.
  * stream is a cudaStream_t (NULL = the legacy default stream); d_values must be ready in
  * stream order.  The call waits for the two results and writes them to host memory. */
 int lmm_values_mean_stderr_noalloc(const double* d_values, int64_t num_values, void* stream, double* out_mean,
@@ -292,6 +294,10 @@ int lmm_stats_get(int max, const char** names, int64_t* launches, double* total_
 /* Bytes this library has copied from host to device since it was loaded (tables, states,
  * parameters): the difference across a call is that call's host-to-device traffic. */
 int lmm_stats_h2d_bytes(int64_t* out);
+/* Bytes reserved from the device and in use in the current device's default stream-ordered
+ * memory pool, the pool every allocation of this library comes from: the difference across
+ * a call is that call's pool traffic. */
+int lmm_stats_pool_bytes(int64_t* out_reserved, int64_t* out_used);
 /* The CUDA stream (as an opaque pointer) on which a process enqueues its work. */
 int lmm_process_stream(lmm_process* proc, void** out_stream);
 /* A FP64 fused-multiply-add throughput probe (DFMA/s), used to report the FP64 roofline. */

@@ -2,8 +2,9 @@
 
 The mixed form has no bit-parity target: its FP32 path state, FP32 basis and FP32 payoffs
 (with the regression sums carried in twice FP32 precision) move prices by amounts far
-below the Monte Carlo error.  The bounds below are stated in standard errors of the FP64
-price (Bermudan) and relative to the price (European swaption)."""
+below the Monte Carlo error.  The Bermudan bound is the form's target, 0.1 bp of the unit
+notional (1e-5 absolute), and a small share of the FP64 standard error; the European
+swaption's is relative to its price."""
 import numpy as np
 import pytest
 
@@ -13,6 +14,7 @@ from finmath_gb300 import workloads as W
 pytestmark = pytest.mark.gpu
 
 P = 65536
+BERMUDAN_TOL_ABS = 1e-5    # |mixed - FP64|: 0.1 bp of the unit notional
 BERMUDAN_TOL_SE = 0.05     # |mixed - FP64| in FP64 standard errors
 SWAPTION_TOL_REL = 2e-5    # |mixed - FP64| / FP64
 FLIP_FRACTION = 2e-3       # share of paths whose exercise date differs
@@ -45,6 +47,7 @@ def test_bermudan_mixed_vs_fp64(sims, basis):
     prod = F.BermudanSwaption(np.ones(len(fix)), fix, plen, pay, 1.0, K, True, basis)
     a = prod.getValues(s64, per_path=True)
     b = prod.getValues(s32, per_path=True)
+    assert abs(b["value"] - a["value"]) <= BERMUDAN_TOL_ABS
     assert abs(b["value"] - a["value"]) <= BERMUDAN_TOL_SE * a["error"]
     assert b["error"] == pytest.approx(a["error"], rel=1e-2)
     # the per-path values agree wherever the exercise decisions agree
@@ -64,4 +67,5 @@ def test_bermudan_variants_mixed_vs_fp64(sims):
         prod = F.BermudanSwaption(ex, fix, plen, pay, notional, strikes, callable_, "swaprate")
         a = prod.getValues(s64)
         b = prod.getValues(s32)
+        assert abs(b["value"] - a["value"]) <= BERMUDAN_TOL_ABS * np.max(notional)
         assert abs(b["value"] - a["value"]) <= BERMUDAN_TOL_SE * a["error"]

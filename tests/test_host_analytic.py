@@ -140,3 +140,53 @@ def test_swaption_analytic_approximation():
                                                       A.swap_annuity(td, dc))
     with pytest.raises(ValueError):
         F.SwaptionAnalyticApproximation(0.05, [1.0, 2.0], "VOLATILITYNORMAL")
+
+
+def test_log_swaprate_derivative_equals_finite_differences():
+    # SwaptionAnalyticApproximation.getLogSwaprateDerivative (products/SwaptionAnalyticApproximation.java:188-281)
+    # gives d log S / d log L_j of the par swap rate S = float leg / annuity, the discount
+    # factors chained from the forward rates; central differences of that S in log L_j,
+    # rebuilt here from the rates alone, pin every weight independently of the formula
+    for cfg, swapTenor in ((W.LMM40, np.arange(10.0, 20.0 + 1e-9, 0.5)), (W.LMM40, np.arange(2.0, 4.0 + 1e-9, 1.0)),
+                           (W.LMM20, np.arange(5.0, 10.0 + 1e-9, 0.5))):
+        model = _lmm_model(cfg)
+        tenor = model.liborPeriodDiscretization
+        w = F.SwaptionAnalyticApproximation(0.04, list(swapTenor)).getLogSwaprateDerivative(
+            tenor, model.discountCurve, model.forwardRateCurve)["values"]
+        start, end = tenor.getTimeIndex(swapTenor[0]), tenor.getTimeIndex(swapTenor[-1])
+        L0 = np.array([model.forwardRateCurve.getForward(None, tenor.getTime(j)) for j in range(start, end)])
+        dt = np.array([tenor.getTimeStep(j) for j in range(start, end)])
+        pay = np.array([tenor.getTime(j + 1) for j in range(start, end)])
+
+        def log_swaprate(L):
+            df = np.cumprod(1.0 / (1.0 + L * dt))  # P(T_{j+1}) / P(T_start)
+            floating = np.sum(L * dt * df)
+            annuity = sum((swapTenor[k + 1] - swapTenor[k]) * df[np.searchsorted(pay, swapTenor[k + 1] - 1e-9)]
+                          for k in range(len(swapTenor) - 1))
+            return math.log(floating / annuity)
+
+        h = 1e-6
+        for j in range(end - start):
+            up, dn = L0.copy(), L0.copy()
+            up[j] *= math.exp(h)
+            dn[j] *= math.exp(-h)
+            fd = (log_swaprate(up) - log_swaprate(dn)) / (2 * h)
+            assert w[j] == pytest.approx(fd, rel=1e-6, abs=1e-10)
+
+
+def test_integrated_libor_covariance_rejects_times_before_the_covariance_grid():
+    # AbstractLIBORCovarianceModel.getFactorLoading throws for a time before its grid; the
+    # covariance grid here starts at 1.0 while the simulation grid starts at 0.0
+    cfg = W.LMM20
+    tenor = F.TimeDiscretizationFromArray(0.0, 20, 0.5)
+    cov_td = F.TimeDiscretizationFromArray(1.0, 18, 0.5)
+    curve = F.ForwardCurveInterpolation.createForwardCurveFromForwards("forwardCurve", cfg["curve_nodes"],
+                                                                       cfg["curve_values"], cfg["period"])
+    cov = F.LIBORCovarianceModelFromVolatilityAndCorrelation(
+        cov_td, tenor, F.LIBORVolatilityModelFourParameterExponentialForm(cov_td, tenor, *cfg["abcd"]),
+        F.LIBORCorrelationModelExponentialDecay(cov_td, tenor, cfg["F"], cfg["corr_decay"]))
+    model = F.LIBORMarketModelFromCovarianceModel.of(tenor, None, curve, F.DiscountCurveFromForwardCurve(curve), None,
+                                                     cov)
+    with pytest.raises(ValueError):
+        model.getIntegratedLIBORCovariance(F.TimeDiscretizationFromArray(0.0, 20, 0.5))
+    assert model.getIntegratedLIBORCovariance(F.TimeDiscretizationFromArray(1.0, 18, 0.5)).shape == (18, 20, 20)
