@@ -189,7 +189,7 @@ struct lmm_process {
     double *d_loadings = nullptr, *d_variance = nullptr, *d_dt = nullptr, *d_delta = nullptr, *d_init = nullptr;
     double* d_exp_tab = nullptr;
     double *d_inv_delta = nullptr, *d_var_half_dt = nullptr;
-    float *d_lam32 = nullptr, *d_var32 = nullptr, *d_inv_delta32 = nullptr, *d_dt32 = nullptr, *d_init_log32 = nullptr;
+    float *d_lam32 = nullptr, *d_var32 = nullptr, *d_inv_delta32 = nullptr, *d_dt32 = nullptr, *d_init32 = nullptr;
     int *d_first = nullptr, *d_obs_slot = nullptr, *d_tenor_tidx = nullptr;
     uint8_t* d_det = nullptr;
     // results
@@ -497,16 +497,18 @@ int lmm_process_create(const lmm_model_desc* m, lmm_brownian* bm, lmm_process** 
         std::vector<float> l32((size_t)T * N * FP, 0.0f), v32((size_t)T * N);
         for (size_t r = 0; r < (size_t)T * N; r++)
             for (int k = 0; k < F; k++) l32[r * FP + k] = (float)m->factor_loadings[r * F + k];
-        for (size_t i = 0; i < v32.size(); i++) v32[i] = (float)m->variance[i];
+        // the drift's deterministic part of a step, (variance * -0.5) * dt_i, rounded once to FP32
+        for (size_t i = 0; i < v32.size(); i++) v32[i] = (float)var_half_dt[i];
         std::vector<float> id32(N), dt32(T), y32(N);
         for (int j = 0; j < N; j++) id32[j] = (float)inv_delta[j];
-        for (int j = 0; j < N; j++) y32[j] = (float)std::log(std::max(m->initial_forwards[j], 0.0));  // getInitialState
+        // the initial forward rates exp(getInitialState) = max(f, 0), rounded once to FP32
+        for (int j = 0; j < N; j++) y32[j] = (float)std::max(m->initial_forwards[j], 0.0);
         for (int i = 0; i < T; i++) dt32[i] = (float)dt[i];
         rc = upload(&pr->d_lam32, l32.data(), l32.size(), s);
         if (!rc) rc = upload(&pr->d_var32, v32.data(), v32.size(), s);
         if (!rc) rc = upload(&pr->d_inv_delta32, id32.data(), id32.size(), s);
         if (!rc) rc = upload(&pr->d_dt32, dt32.data(), dt32.size(), s);
-        if (!rc) rc = upload(&pr->d_init_log32, y32.data(), y32.size(), s);
+        if (!rc) rc = upload(&pr->d_init32, y32.data(), y32.size(), s);
         if (!rc) rc = cudaStreamSynchronize(s) == cudaSuccess ? 0 : fail(LMM_ERR_CUDA, "stream sync");
     }
     if (!rc) rc = cudaStreamSynchronize(s) == cudaSuccess ? 0 : fail(LMM_ERR_CUDA, "stream sync");
@@ -576,7 +578,7 @@ static int process_ensure(lmm_process* pr)
     a.d_var_half_dt = pr->d_var_half_dt;
     a.d_inv_delta32 = pr->d_inv_delta32;
     a.d_dt32 = pr->d_dt32;
-    a.d_init_log32 = pr->d_init_log32;
+    a.d_init32 = pr->d_init32;
     a.d_init = pr->d_init;
     a.d_obs_slot = pr->d_obs_slot;
     a.d_dw = pr->bm->d_dw;
@@ -704,7 +706,7 @@ int lmm_process_destroy(lmm_process* pr)
     dfree(pr->d_var32, s);
     dfree(pr->d_inv_delta32, s);
     dfree(pr->d_dt32, s);
-    dfree(pr->d_init_log32, s);
+    dfree(pr->d_init32, s);
     dfree(pr->d_first, s);
     dfree(pr->d_tenor_tidx, s);
     dfree(pr->d_det, s);

@@ -119,7 +119,7 @@ struct PathLaunch {
     const double* d_var_half_dt; // [T][N] (variance * -0.5) * dt_i, the drift's deterministic part of a step
     const float* d_inv_delta32;// [N] 1/delta in FP32 (mixed form)
     const float* d_dt32;       // [T] time steps in FP32 (mixed form)
-    const float* d_init_log32; // [N] log of the initial forwards in FP32 (mixed form)
+    const float* d_init32;     // [N] initial forwards max(f, 0) in FP32 (mixed form)
     const double* d_exp_tab;   // [2 kExpTableHalf + 1] exp(k/kExpTableHalf) (FP64 form, see fp64math.cuh)
     const double* d_init;      // [N] initial forwards
     const int* d_obs_slot;     // [T+1] observation slot or -1
@@ -133,7 +133,8 @@ struct PathLaunch {
     int ckpt_stride;           // forward rates L every ckpt_stride steps (in the path precision)
 };
 int launch_paths_fp64(const PathLaunch& a, cudaStream_t s, int* blocks_out);
-// lam32: [T][N][paths_fp32_pitch(N, F)] FP32 loadings, zero padded beyond F; var32: [T][N]
+// lam32: [T][N][paths_fp32_pitch(N, F)] FP32 loadings, zero padded beyond F; var32: [T][N] the
+// drift's deterministic part of each step, (variance * -0.5) * dt_i, in FP32
 int paths_fp32_pitch(int N, int F);
 int launch_paths_fp32(const PathLaunch& a, const float* lam32, const float* var32, cudaStream_t s, int* blocks_out);
 int path_blocks(int P);

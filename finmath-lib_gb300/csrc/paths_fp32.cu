@@ -1,19 +1,22 @@
-// paths_fp32.cu -- K2 (mixed-precision form): the fused path kernel in FP32 log space.
+// paths_fp32.cu -- K2 (mixed-precision form): the fused path kernel in FP32.
 //
-// Same recurrence as paths_fp64.cu (EulerSchemeFromProcessModel.java:170-326 with the
-// spot drift of LIBORMarketModelFromCovarianceModel.java:1125-1191), but the path state
-// is kept as Y = log L in FP32 (the EULER form in log coordinates), the drift running
-// sums (carried with dt and the increments, G_k = dW_k + dt S_k) use FP32 FMAs, and exp /
-// the measure-change ratio use the SFU (__expf, __fdividef).  The numeraire accrual and
-// its adjustment sums stay FP64, as do the regression sums and payoff averages downstream.  The error against the FP64 form is
+// Same recurrence as paths_fp64.cu (EulerSchemeFromProcessModel.java:170-326 in its default
+// EULER_FUNCTIONAL form, with the spot drift of LIBORMarketModelFromCovarianceModel.java:
+// 1125-1191): the log-Euler step Y' = log L + d, L' = min(exp(Y'), cap) is carried as
+// L' = min(L exp(d), cap) on the forward rates themselves, so the path state is one FP32
+// register per component.  The drift running sums (carried with dt and the increments,
+// G_k = dW_k + dt S_k) use paired FP32 FMAs, exp and the measure-change ratio use the SFU
+// (__expf, __fdividef).  The numeraire accrual and its adjustment sums stay FP64, as do the
+// regression sums and payoff averages downstream.  The error against the FP64 form is
 // measured and reported, not assumed.
 //
 // GB300 layout: one thread per path, the forward vector in registers for all steps.  Each
-// warp stages the next step's factor rows (zero padded to whole float4 vectors) and
-// variances in shared memory with cp.async while it works on the current step, and each
-// thread prefetches its own path's next increments the same way, so the step loop does
-// not wait on global memory.  The sums over factors run on paired FP32 FMAs (__ffma2_rn,
-// two factors per instruction).
+// warp stages the next step's factor rows (zero padded to whole float4 vectors) and the
+// step's deterministic drift terms (variance * -0.5 * dt, from the host) in shared memory
+// with cp.async while it works on the current step, and each thread prefetches its own
+// path's next increments the same way, so the step loop does not wait on global memory.
+// The sums over factors run on paired FP32 FMAs (__ffma2_rn, two factors per instruction),
+// the drift's dot product in two independent accumulators to halve its dependency chain.
 #include "lmm_internal.h"
 #include "fp64math.cuh"
 #include "reduce.cuh"
@@ -43,18 +46,23 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 template <int NMAX, int FMAX>
 struct Smem32 {
     static constexpr int FP = row_pitch(FMAX);
-    static constexpr int TABLE = NMAX * FP + NMAX;  // loadings rows [NMAX][FP], then variances [NMAX]
+    static constexpr int TABLE = NMAX * FP + NMAX;  // loadings rows [NMAX][FP], then drift terms [NMAX]
     float table[kPathThreads / 32][2][TABLE];       // per warp, two steps
     float dw[2][FMAX][kPathThreads];                // per thread column, two steps
+    float inv_delta[NMAX];                          // 1/delta_j
     double wsum[kPathThreads / 32][NMAX];           // numeraire-adjustment warp sums
 };
+
+// resident blocks per SM: the FP32 state of NMAX components, the factor pairs and the
+// staged row of one component fit the register budget this leaves
+__host__ __device__ constexpr int fp32_min_blocks(int nmax) { return nmax <= 24 ? 8 : nmax <= 40 ? 6 : 3; }
 
 // CAPPED: the model caps the forward rates.  The cap is a compile-time variant: on this GPU
 // the compiler's min/select for `v > cap ? cap : v` issues to the narrow FP64 pipe, once per
 // component and step, which costs the uncapped models several percent if left in.
 template <int NMAX, int FMAX, bool CAPPED>
-__global__ void __launch_bounds__(kPathThreads, NMAX <= 40 ? 4 : 2) paths_fp32_kernel(const PathLaunch a, const float* __restrict__ lam32,
-                                                                  const float* __restrict__ var32)
+__global__ void __launch_bounds__(kPathThreads, fp32_min_blocks(NMAX))
+    paths_fp32_kernel(const PathLaunch a, const float* __restrict__ lam32, const float* __restrict__ vhd32)
 {
     using SM = Smem32<NMAX, FMAX>;
     constexpr int FP = SM::FP;
@@ -69,31 +77,26 @@ __global__ void __launch_bounds__(kPathThreads, NMAX <= 40 ? 4 : 2) paths_fp32_k
     const float* dW = static_cast<const float*>(a.d_dw);
     float* states = static_cast<float*>(a.d_states);
 
-    // step i's loadings (pitch FP) and variances into this warp's buffer i&1, and this
+    // step i's loadings (pitch FP) and drift terms into this warp's buffer i&1, and this
     // thread's increments into dw[i&1]
     auto prefetch = [&](int i) {
         float* tb = sm.table[warp][i & 1];
         const float* ls = lam32 + (size_t)i * N * FP;
         for (int q = lane; q < N * FP / 4; q += 32) cp_async16(tb + 4 * q, ls + 4 * q);
-        for (int j = lane; j < N; j += 32) cp_async4(tb + NMAX * FP + j, var32 + (size_t)i * N + j);
+        for (int j = lane; j < N; j += 32) cp_async4(tb + NMAX * FP + j, vhd32 + (size_t)i * N + j);
         if (active)
             for (int k = 0; k < F; k++) cp_async4(&sm.dw[i & 1][k][tid], dW + ((size_t)i * F + k) * P + p);
         cp_async_commit();
     };
     if (a.T > 0) prefetch(0);
+    for (int j = tid; j < N; j += kPathThreads) sm.inv_delta[j] = __ldg(a.d_inv_delta32 + j);
 
-    float Y[NMAX], L[NMAX];
+    float L[NMAX];
 #pragma unroll
     for (int j = 0; j < NMAX; j++) {
-        if (j < N) {
-            Y[j] = __ldg(a.d_init_log32 + j);
-            float v = __expf(Y[j]);
-            if (CAPPED && v > cap) v = cap;
-            L[j] = v;
-        } else {
-            Y[j] = 0.0f;
-            L[j] = 0.0f;
-        }
+        float v = j < N ? __ldg(a.d_init32 + j) : 0.0f;
+        if (CAPPED && v > cap) v = cap;
+        L[j] = v;
     }
     {
         const int slot = __ldg(a.d_obs_slot + 0);
@@ -109,6 +112,7 @@ __global__ void __launch_bounds__(kPathThreads, NMAX <= 40 ? 4 : 2) paths_fp32_k
                 if (j < N) ck[(size_t)j * P + p] = L[j];
         }
     }
+    __syncthreads();  // sm.inv_delta
     for (int i = 0; i < a.T; i++) {
         const int first = __ldg(a.d_first + i);
         const float dt = __ldg(a.d_dt32 + i);
@@ -138,19 +142,19 @@ __global__ void __launch_bounds__(kPathThreads, NMAX <= 40 ? 4 : 2) paths_fp32_k
                     lr[4 * q + 2] = v.z;
                     lr[4 * q + 3] = v.w;
                 }
-                const float invd = __ldg(a.d_inv_delta32 + j);
-                const float osdt = __fdividef(L[j], L[j] + invd) * dt;
+                const float Lj = L[j];
+                const float osdt = __fdividef(Lj, Lj + sm.inv_delta[j]) * dt;
                 const float2 os2 = make_float2(osdt, osdt);
-                float2 d2 = make_float2(-0.5f * tb[NMAX * FP + j] * dt, 0.0f);
+                float2 da = make_float2(tb[NMAX * FP + j], 0.0f), db = make_float2(0.0f, 0.0f);
 #pragma unroll
                 for (int m = 0; m < FH; m++) {
                     // factors 2m and 2m+1 (the rows are zero padded beyond F)
                     const float2 l2 = make_float2(lr[2 * m], lr[2 * m + 1]);
                     G2[m] = __ffma2_rn(os2, l2, G2[m]);
-                    d2 = __ffma2_rn(G2[m], l2, d2);
+                    if (m & 1) db = __ffma2_rn(G2[m], l2, db);
+                    else da = __ffma2_rn(G2[m], l2, da);
                 }
-                Y[j] = Y[j] + (d2.x + d2.y);
-                float v = __expf(Y[j]);
+                float v = Lj * __expf((da.x + db.x) + (da.y + db.y));
                 if (CAPPED && v > cap) v = cap;
                 L[j] = v;
             }
@@ -203,7 +207,7 @@ __global__ void __launch_bounds__(kPathThreads, NMAX <= 40 ? 4 : 2) paths_fp32_k
 }
 
 template <int NMAX, int FMAX, bool CAPPED>
-int launch_t(const PathLaunch& a, const float* lam32, const float* var32, cudaStream_t s, int blocks)
+int launch_t(const PathLaunch& a, const float* lam32, const float* vhd32, cudaStream_t s, int blocks)
 {
     const size_t smem = sizeof(Smem32<NMAX, FMAX>);
     static bool attr_set = false;  // set once, before any stream capture
@@ -212,7 +216,7 @@ int launch_t(const PathLaunch& a, const float* lam32, const float* var32, cudaSt
                                       (int)smem));
         attr_set = true;
     }
-    paths_fp32_kernel<NMAX, FMAX, CAPPED><<<blocks, kPathThreads, smem, s>>>(a, lam32, var32);
+    paths_fp32_kernel<NMAX, FMAX, CAPPED><<<blocks, kPathThreads, smem, s>>>(a, lam32, vhd32);
     LMM_CUDA(cudaGetLastError());
     return LMM_OK;
 }
