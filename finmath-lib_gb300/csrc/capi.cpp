@@ -189,7 +189,7 @@ struct lmm_process {
     double *d_loadings = nullptr, *d_variance = nullptr, *d_dt = nullptr, *d_delta = nullptr, *d_init = nullptr;
     double* d_exp_tab = nullptr;
     double *d_inv_delta = nullptr, *d_var_half_dt = nullptr;
-    float *d_lam32 = nullptr, *d_var32 = nullptr, *d_inv_delta32 = nullptr, *d_dt32 = nullptr, *d_init32 = nullptr;
+    float *d_lam32 = nullptr, *d_inv_delta32 = nullptr, *d_dt32 = nullptr, *d_init32 = nullptr;
     int *d_first = nullptr, *d_obs_slot = nullptr, *d_tenor_tidx = nullptr;
     uint8_t* d_det = nullptr;
     // results
@@ -493,19 +493,22 @@ int lmm_process_create(const lmm_model_desc* m, lmm_brownian* bm, lmm_process** 
     if (!rc) rc = upload(&pr->d_det, pr->num_det.data(), pr->num_det.size(), s);
     if (!rc) rc = upload(&pr->d_tenor_tidx, pr->tenor_tidx.data(), pr->tenor_tidx.size(), s);
     if (!rc && pr->precision == LMM_PRECISION_MIXED) {
-        const int FP = paths_fp32_pitch(N, F);
-        std::vector<float> l32((size_t)T * N * FP, 0.0f), v32((size_t)T * N);
-        for (size_t r = 0; r < (size_t)T * N; r++)
+        int fmax = 0;
+        const int FP = paths_fp32_rows(N, F, &fmax);
+        std::vector<float> l32((size_t)T * N * FP, 0.0f);
+        for (size_t r = 0; r < (size_t)T * N; r++) {
             for (int k = 0; k < F; k++) l32[r * FP + k] = (float)m->factor_loadings[r * F + k];
-        // the drift's deterministic part of a step, (variance * -0.5) * dt_i, rounded once to FP32
-        for (size_t i = 0; i < v32.size(); i++) v32[i] = (float)var_half_dt[i];
+            // the drift's deterministic part of a step, (variance * -0.5) * dt_i, and 1/delta_j,
+            // each rounded once to FP32
+            l32[r * FP + fmax] = (float)var_half_dt[r];
+            l32[r * FP + fmax + 1] = (float)inv_delta[r % N];
+        }
         std::vector<float> id32(N), dt32(T), y32(N);
         for (int j = 0; j < N; j++) id32[j] = (float)inv_delta[j];
         // the initial forward rates exp(getInitialState) = max(f, 0), rounded once to FP32
         for (int j = 0; j < N; j++) y32[j] = (float)std::max(m->initial_forwards[j], 0.0);
         for (int i = 0; i < T; i++) dt32[i] = (float)dt[i];
         rc = upload(&pr->d_lam32, l32.data(), l32.size(), s);
-        if (!rc) rc = upload(&pr->d_var32, v32.data(), v32.size(), s);
         if (!rc) rc = upload(&pr->d_inv_delta32, id32.data(), id32.size(), s);
         if (!rc) rc = upload(&pr->d_dt32, dt32.data(), dt32.size(), s);
         if (!rc) rc = upload(&pr->d_init32, y32.data(), y32.size(), s);
@@ -607,7 +610,7 @@ static int process_ensure(lmm_process* pr)
     }
     int blocks = 0;
     rc = pr->precision == LMM_PRECISION_FP64 ? launch_paths_fp64(a, s, &blocks)
-                                              : launch_paths_fp32(a, pr->d_lam32, pr->d_var32, s, &blocks);
+                                              : launch_paths_fp32(a, pr->d_lam32, s, &blocks);
     if (rc) return rc;
     rc = launch_numeraire_finish(pr->d_partials, blocks, pr->N, pr->P, pr->d_numeraire, pr->d_det, pr->d_num_adj, s);
     if (rc) return rc;
@@ -689,6 +692,16 @@ int lmm_process_get_numeraire_rv(lmm_process* pr, double time, lmm_rv** out)
                         pr->num_det[l], pr->has_discount ? pr->discount[l] : 1.0, pr->P, pr->stream, out);
 }
 
+int lmm_process_get_numeraire_unadjusted_rv(lmm_process* pr, double time, lmm_rv** out)
+{
+    if (!pr || !out) return fail(LMM_ERR_INVALID, "null argument");
+    const int l = time_index(pr->tenor, time);
+    if (l < 0) return fail(LMM_ERR_INVALID, "numeraire requested off the tenor grid");
+    int rc = process_ensure(pr);
+    if (rc) return rc;
+    return rv_numeraire(time, pr->d_numeraire + (size_t)l * pr->P, nullptr, 0, 0, 1.0, pr->P, pr->stream, out);
+}
+
 int lmm_process_destroy(lmm_process* pr)
 {
     if (!pr) return LMM_OK;
@@ -703,7 +716,6 @@ int lmm_process_destroy(lmm_process* pr)
     dfree(pr->d_var_half_dt, s);
     dfree(pr->d_init, s);
     dfree(pr->d_lam32, s);
-    dfree(pr->d_var32, s);
     dfree(pr->d_inv_delta32, s);
     dfree(pr->d_dt32, s);
     dfree(pr->d_init32, s);

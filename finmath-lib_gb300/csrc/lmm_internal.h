@@ -133,10 +133,11 @@ struct PathLaunch {
     int ckpt_stride;           // forward rates L every ckpt_stride steps (in the path precision)
 };
 int launch_paths_fp64(const PathLaunch& a, cudaStream_t s, int* blocks_out);
-// lam32: [T][N][paths_fp32_pitch(N, F)] FP32 loadings, zero padded beyond F; var32: [T][N] the
-// drift's deterministic part of each step, (variance * -0.5) * dt_i, in FP32
-int paths_fp32_pitch(int N, int F);
-int launch_paths_fp32(const PathLaunch& a, const float* lam32, const float* var32, cudaStream_t s, int* blocks_out);
+// rows32: [T][N][pitch] FP32 component rows of the mixed path kernel, pitch =
+// paths_fp32_rows(N, F, &fmax): the F loadings, zeros up to fmax, then at fmax the drift's
+// deterministic part of the step, (variance * -0.5) * dt_i, and at fmax + 1 the 1/delta_j
+int paths_fp32_rows(int N, int F, int* fmax);
+int launch_paths_fp32(const PathLaunch& a, const float* rows32, cudaStream_t s, int* blocks_out);
 int path_blocks(int P);
 // exp(k/kExpTableHalf) for |k| <= kExpTableHalf, rounded to FP64 from extended precision
 // (the table of exp_small in fp64math.cuh)

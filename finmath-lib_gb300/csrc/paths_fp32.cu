@@ -11,12 +11,15 @@
 // measured and reported, not assumed.
 //
 // GB300 layout: one thread per path, the forward vector in registers for all steps.  Each
-// warp stages the next step's factor rows (zero padded to whole float4 vectors) and the
-// step's deterministic drift terms (variance * -0.5 * dt, from the host) in shared memory
-// with cp.async while it works on the current step, and each thread prefetches its own
-// path's next increments the same way, so the step loop does not wait on global memory.
-// The sums over factors run on paired FP32 FMAs (__ffma2_rn, two factors per instruction),
-// the drift's dot product in two independent accumulators to halve its dependency chain.
+// warp stages the next step's component rows in shared memory with cp.async while it works
+// on the current step -- per component one row of whole float4 vectors: the factor loadings
+// (zero padded to FMAX), the step's deterministic drift term (variance * -0.5 * dt) and
+// 1/delta, so a component-step reads its row with three 16-byte loads -- and each thread
+// prefetches its own path's next increments the same way, so the step loop does not wait on
+// global memory.  The sums over factors run on paired FP32 FMAs (__ffma2_rn, two factors
+// per instruction), the drift's dot product in two independent accumulators to halve its
+// dependency chain.  When the model has exactly NMAX components (EXACT) the component loop
+// carries no run-time bound checks.
 #include "lmm_internal.h"
 #include "fp64math.cuh"
 #include "reduce.cuh"
@@ -27,8 +30,9 @@ namespace {
 
 constexpr int kPathThreads = 128;
 
-// factor-row pitch of the staged loadings: FMAX rounded up to whole float4 vectors
-__host__ __device__ constexpr int row_pitch(int fmax) { return (fmax + 3) / 4 * 4; }
+// row pitch of the staged component rows: FMAX loadings, the drift term and 1/delta,
+// rounded up to whole float4 vectors
+__host__ __device__ constexpr int row_pitch(int fmax) { return (fmax + 2 + 3) / 4 * 4; }
 
 __device__ __forceinline__ void cp_async4(float* dst, const float* src)
 {
@@ -46,10 +50,8 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 template <int NMAX, int FMAX>
 struct Smem32 {
     static constexpr int FP = row_pitch(FMAX);
-    static constexpr int TABLE = NMAX * FP + NMAX;  // loadings rows [NMAX][FP], then drift terms [NMAX]
-    float table[kPathThreads / 32][2][TABLE];       // per warp, two steps
+    float table[kPathThreads / 32][2][NMAX * FP];   // per warp, two steps: rows [NMAX][FP]
     float dw[2][FMAX][kPathThreads];                // per thread column, two steps
-    float inv_delta[NMAX];                          // 1/delta_j
     double wsum[kPathThreads / 32][NMAX];           // numeraire-adjustment warp sums
 };
 
@@ -60,9 +62,9 @@ __host__ __device__ constexpr int fp32_min_blocks(int nmax) { return nmax <= 24 
 // CAPPED: the model caps the forward rates.  The cap is a compile-time variant: on this GPU
 // the compiler's min/select for `v > cap ? cap : v` issues to the narrow FP64 pipe, once per
 // component and step, which costs the uncapped models several percent if left in.
-template <int NMAX, int FMAX, bool CAPPED>
+template <int NMAX, int FMAX, bool CAPPED, bool EXACT>
 __global__ void __launch_bounds__(kPathThreads, fp32_min_blocks(NMAX))
-    paths_fp32_kernel(const PathLaunch a, const float* __restrict__ lam32, const float* __restrict__ vhd32)
+    paths_fp32_kernel(const PathLaunch a, const float* __restrict__ rows32)
 {
     using SM = Smem32<NMAX, FMAX>;
     constexpr int FP = SM::FP;
@@ -72,24 +74,24 @@ __global__ void __launch_bounds__(kPathThreads, fp32_min_blocks(NMAX))
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int p = blockIdx.x * kPathThreads + tid;
     const bool active = p < a.P;
-    const int N = a.N, F = a.F, P = a.P;
+    const int N = EXACT ? NMAX : a.N, F = a.F, P = a.P;
     const float cap = CAPPED ? (float)a.libor_cap : 0.0f;
     const float* dW = static_cast<const float*>(a.d_dw);
     float* states = static_cast<float*>(a.d_states);
 
-    // step i's loadings (pitch FP) and drift terms into this warp's buffer i&1, and this
-    // thread's increments into dw[i&1]
+    // step i's component rows (pitch FP) into this warp's buffer i&1, and this thread's
+    // increments into dw[i&1]
     auto prefetch = [&](int i) {
         float* tb = sm.table[warp][i & 1];
-        const float* ls = lam32 + (size_t)i * N * FP;
+        const float* ls = rows32 + (size_t)i * N * FP;
         for (int q = lane; q < N * FP / 4; q += 32) cp_async16(tb + 4 * q, ls + 4 * q);
-        for (int j = lane; j < N; j += 32) cp_async4(tb + NMAX * FP + j, vhd32 + (size_t)i * N + j);
-        if (active)
-            for (int k = 0; k < F; k++) cp_async4(&sm.dw[i & 1][k][tid], dW + ((size_t)i * F + k) * P + p);
+        if (active) {
+            const float* src = dW + (size_t)i * F * P + p;
+            for (int k = 0; k < F; k++) cp_async4(&sm.dw[i & 1][k][tid], src + (size_t)k * P);
+        }
         cp_async_commit();
     };
     if (a.T > 0) prefetch(0);
-    for (int j = tid; j < N; j += kPathThreads) sm.inv_delta[j] = __ldg(a.d_inv_delta32 + j);
 
     float L[NMAX];
 #pragma unroll
@@ -98,21 +100,21 @@ __global__ void __launch_bounds__(kPathThreads, fp32_min_blocks(NMAX))
         if (CAPPED && v > cap) v = cap;
         L[j] = v;
     }
+    // the forward rates of all components into rows [N][P] starting at dst (a running
+    // pointer: one address increment per component)
+    auto store_rows = [&](float* dst) {
+#pragma unroll
+        for (int j = 0; j < NMAX; j++)
+            if (EXACT || j < N) {
+                *dst = L[j];
+                dst += P;
+            }
+    };
     {
         const int slot = __ldg(a.d_obs_slot + 0);
-        if (slot >= 0 && active) {
-#pragma unroll
-            for (int j = 0; j < NMAX; j++)
-                if (j < N) states[((size_t)slot * N + j) * P + p] = L[j];
-        }
-        if (a.d_ckpt && active) {
-            float* ck = static_cast<float*>(a.d_ckpt);
-#pragma unroll
-            for (int j = 0; j < NMAX; j++)
-                if (j < N) ck[(size_t)j * P + p] = L[j];
-        }
+        if (slot >= 0 && active) store_rows(states + (size_t)slot * N * P + p);
+        if (a.d_ckpt && active) store_rows(static_cast<float*>(a.d_ckpt) + p);
     }
-    __syncthreads();  // sm.inv_delta
     for (int i = 0; i < a.T; i++) {
         const int first = __ldg(a.d_first + i);
         const float dt = __ldg(a.d_dt32 + i);
@@ -132,7 +134,7 @@ __global__ void __launch_bounds__(kPathThreads, fp32_min_blocks(NMAX))
         const float* tb = sm.table[warp][i & 1];
         for_up_from<NMAX>(first, [&](auto jc) {
             constexpr int j = decltype(jc)::value;
-            if (j < N) {
+            if (EXACT || j < N) {
                 float lr[FP];
 #pragma unroll
                 for (int q = 0; q < FP / 4; q++) {
@@ -143,13 +145,14 @@ __global__ void __launch_bounds__(kPathThreads, fp32_min_blocks(NMAX))
                     lr[4 * q + 3] = v.w;
                 }
                 const float Lj = L[j];
-                const float osdt = __fdividef(Lj, Lj + sm.inv_delta[j]) * dt;
+                const float osdt = __fdividef(Lj, Lj + lr[FMAX + 1]) * dt;
                 const float2 os2 = make_float2(osdt, osdt);
-                float2 da = make_float2(tb[NMAX * FP + j], 0.0f), db = make_float2(0.0f, 0.0f);
+                float2 da = make_float2(lr[FMAX], 0.0f), db = make_float2(0.0f, 0.0f);
 #pragma unroll
                 for (int m = 0; m < FH; m++) {
-                    // factors 2m and 2m+1 (the rows are zero padded beyond F)
-                    const float2 l2 = make_float2(lr[2 * m], lr[2 * m + 1]);
+                    // factors 2m and 2m+1 (the rows are zero padded beyond F; for an odd FMAX
+                    // the last pair's second entry is the drift term, multiplied by G = 0)
+                    const float2 l2 = make_float2(lr[2 * m], 2 * m + 1 < FMAX ? lr[2 * m + 1] : 0.0f);
                     G2[m] = __ffma2_rn(os2, l2, G2[m]);
                     if (m & 1) db = __ffma2_rn(G2[m], l2, db);
                     else da = __ffma2_rn(G2[m], l2, da);
@@ -160,40 +163,62 @@ __global__ void __launch_bounds__(kPathThreads, fp32_min_blocks(NMAX))
             }
         });
         const int slot = __ldg(a.d_obs_slot + i + 1);
-        if (slot >= 0 && active) {
-#pragma unroll
-            for (int j = 0; j < NMAX; j++)
-                if (j < N) states[((size_t)slot * N + j) * P + p] = L[j];
-        }
-        if (a.d_ckpt && active && (i + 1) % a.ckpt_stride == 0) {
-            float* ck = static_cast<float*>(a.d_ckpt) + (size_t)((i + 1) / a.ckpt_stride) * N * P;
-#pragma unroll
-            for (int j = 0; j < NMAX; j++)
-                if (j < N) ck[(size_t)j * P + p] = L[j];
-        }
+        if (slot >= 0 && active) store_rows(states + (size_t)slot * N * P + p);
+        if (a.d_ckpt && active && (i + 1) % a.ckpt_stride == 0)
+            store_rows(static_cast<float*>(a.d_ckpt) + (size_t)((i + 1) / a.ckpt_stride) * N * P + p);
     }
     cp_async_wait();
-    // FP64 spot numeraire from the frozen fixings (as paths_fp64.cu), 1/N by a Newton
-    // reciprocal in FP64 (fp64math.cuh), the FP32 fixings widened in integer operations.
-    // The block partial sums of 1/N_l for the numeraire adjustment: plain FP64 within a warp
-    // (lane order), compensated across the block's warps (warp order).
+    // FP64 spot numeraire from the frozen fixings (as paths_fp64.cu), the FP32 fixings
+    // widened in integer operations, and 1/N by the FP32 reciprocal refined by one Newton
+    // step in FP64 (relative error about 2^-46, far below the FP32 path state's).  The warp
+    // sums of 1/N_l for the numeraire adjustment are transposed reductions over chunks of
+    // eight tenor times: three exchange levels that each halve the values a lane holds
+    // (lanes with the level's bit set keep the upper half, the others the lower half, and
+    // add what the partner sends), then two plain levels, so a chunk costs 9 FP64 adds per
+    // warp instead of 40.  The block partials: compensated across the block's warps.
+    static_assert(NMAX % 8 == 0, "the transposed reduction works on chunks of eight tenor times");
     double Nv = 1.0;
     if (active) a.d_numeraire[p] = 1.0;
     if (a.d_inv_numeraire && active) a.d_inv_numeraire[p] = 1.0;
+    const bool u16 = lane & 16, u8 = lane & 8, u4 = lane & 4;
 #pragma unroll
-    for (int l = 0; l < NMAX; l++) {
-        if (l < N) {
-            const double delta = __ldg(a.d_delta + l);
-            const double Ll = f32_to_f64_int(L[l]);
-            if (l < a.num_det_prefix) Nv = Ll * (delta * Nv) + Nv;
-            else Nv = Nv * (1.0 + Ll * delta);
-            if (active) a.d_numeraire[(size_t)(l + 1) * P + p] = Nv;
-            double v = active ? rcp_newton(Nv) : 0.0;
-            if (a.d_inv_numeraire && active) a.d_inv_numeraire[(size_t)(l + 1) * P + p] = v;
+    for (int c = 0; c < NMAX / 8; c++) {
+        double v[8];
 #pragma unroll
-            for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-            if (lane == 0) sm.wsum[warp][l] = v;
+        for (int q = 0; q < 8; q++) {
+            const int l = 8 * c + q;
+            v[q] = 0.0;
+            if (EXACT || l < N) {
+                const double delta = __ldg(a.d_delta + l);
+                const double Ll = f32_to_f64_int(L[l]);
+                if (l < a.num_det_prefix) Nv = Ll * (delta * Nv) + Nv;
+                else Nv = Nv * (1.0 + Ll * delta);
+                if (active) {
+                    a.d_numeraire[(size_t)(l + 1) * P + p] = Nv;
+                    const double r0 = f32_to_f64_int(__frcp_rn(f64_to_f32_int(Nv)));
+                    v[q] = fma(r0, fma(-Nv, r0, 1.0), r0);
+                    if (a.d_inv_numeraire) a.d_inv_numeraire[(size_t)(l + 1) * P + p] = v[q];
+                }
+            }
         }
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const double keep = u16 ? v[q + 4] : v[q], send = u16 ? v[q] : v[q + 4];
+            v[q] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+        }
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+            const double keep = u8 ? v[q + 2] : v[q], send = u8 ? v[q] : v[q + 2];
+            v[q] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+        }
+        {
+            const double keep = u4 ? v[1] : v[0], send = u4 ? v[0] : v[1];
+            v[0] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+        }
+        v[0] += __shfl_xor_sync(0xffffffffu, v[0], 2);
+        v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
+        const int idx = 8 * c + (u16 ? 4 : 0) + (u8 ? 2 : 0) + (u4 ? 1 : 0);
+        if ((lane & 3) == 0 && idx < N) sm.wsum[warp][idx] = v[0];
     }
     __syncthreads();
     if (tid < N) {
@@ -206,45 +231,56 @@ __global__ void __launch_bounds__(kPathThreads, fp32_min_blocks(NMAX))
     }
 }
 
-template <int NMAX, int FMAX, bool CAPPED>
-int launch_t(const PathLaunch& a, const float* lam32, const float* vhd32, cudaStream_t s, int blocks)
+template <int NMAX, int FMAX, bool CAPPED, bool EXACT>
+int launch_t(const PathLaunch& a, const float* rows32, cudaStream_t s, int blocks)
 {
     const size_t smem = sizeof(Smem32<NMAX, FMAX>);
     static bool attr_set = false;  // set once, before any stream capture
     if (!attr_set) {
-        LMM_CUDA(cudaFuncSetAttribute(paths_fp32_kernel<NMAX, FMAX, CAPPED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)smem));
+        LMM_CUDA(cudaFuncSetAttribute(paths_fp32_kernel<NMAX, FMAX, CAPPED, EXACT>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         attr_set = true;
     }
-    paths_fp32_kernel<NMAX, FMAX, CAPPED><<<blocks, kPathThreads, smem, s>>>(a, lam32, vhd32);
+    paths_fp32_kernel<NMAX, FMAX, CAPPED, EXACT><<<blocks, kPathThreads, smem, s>>>(a, rows32);
     LMM_CUDA(cudaGetLastError());
     return LMM_OK;
 }
 
 template <int NMAX, int FMAX>
-int launch_c(const PathLaunch& a, const float* lam32, const float* var32, cudaStream_t s, int blocks)
+int launch_c(const PathLaunch& a, const float* rows32, cudaStream_t s, int blocks)
 {
-    if (isinf(a.libor_cap)) return launch_t<NMAX, FMAX, false>(a, lam32, var32, s, blocks);
-    return launch_t<NMAX, FMAX, true>(a, lam32, var32, s, blocks);
+    const bool capped = !isinf(a.libor_cap);
+    if (a.N == NMAX)
+        return capped ? launch_t<NMAX, FMAX, true, true>(a, rows32, s, blocks)
+                      : launch_t<NMAX, FMAX, false, true>(a, rows32, s, blocks);
+    return capped ? launch_t<NMAX, FMAX, true, false>(a, rows32, s, blocks)
+                  : launch_t<NMAX, FMAX, false, false>(a, rows32, s, blocks);
+}
+
+int fp32_fmax(int N, int F)
+{
+    if (N <= 24 && F <= 4) return 4;
+    if (N <= 40 && F <= 10) return 10;
+    return 16;
 }
 
 }  // namespace
 
-int paths_fp32_pitch(int N, int F)
+int paths_fp32_rows(int N, int F, int* fmax)
 {
-    if (N <= 24 && F <= 4) return row_pitch(4);
-    if (N <= 40 && F <= 10) return row_pitch(10);
-    return row_pitch(16);
+    const int fm = fp32_fmax(N, F);
+    if (fmax) *fmax = fm;
+    return row_pitch(fm);
 }
 
-int launch_paths_fp32(const PathLaunch& a, const float* lam32, const float* var32, cudaStream_t s, int* blocks_out)
+int launch_paths_fp32(const PathLaunch& a, const float* rows32, cudaStream_t s, int* blocks_out)
 {
     const int blocks = path_blocks(a.P);
     if (blocks_out) *blocks_out = blocks;
     KernelTimer kt(K_PATHS_FP32, s);
-    if (a.N <= 24 && a.F <= 4) return launch_c<24, 4>(a, lam32, var32, s, blocks);
-    if (a.N <= 40 && a.F <= 10) return launch_c<40, 10>(a, lam32, var32, s, blocks);
-    if (a.N <= 64 && a.F <= 16) return launch_c<64, 16>(a, lam32, var32, s, blocks);
+    if (a.N <= 24 && a.F <= 4) return launch_c<24, 4>(a, rows32, s, blocks);
+    if (a.N <= 40 && a.F <= 10) return launch_c<40, 10>(a, rows32, s, blocks);
+    if (a.N <= 64 && a.F <= 16) return launch_c<64, 16>(a, rows32, s, blocks);
     return fail(LMM_ERR_INVALID, "mixed path kernel supports at most 64 forward rates and 16 factors");
 }
 

@@ -91,6 +91,7 @@ SIGNATURES = {
     "lmm_process_get_numeraire": (ctypes.c_int, [_VP, ctypes.c_double, _D]),
     "lmm_process_get_value_rv": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_VP)]),
     "lmm_process_get_numeraire_rv": (ctypes.c_int, [_VP, ctypes.c_double, ctypes.POINTER(_VP)]),
+    "lmm_process_get_numeraire_unadjusted_rv": (ctypes.c_int, [_VP, ctypes.c_double, ctypes.POINTER(_VP)]),
     "lmm_rv_create_constant": (ctypes.c_int, [ctypes.c_double, ctypes.c_double, ctypes.POINTER(_VP)]),
     "lmm_rv_create": (ctypes.c_int, [ctypes.c_double, _D, ctypes.c_int64, ctypes.POINTER(_VP)]),
     "lmm_rv_destroy": (ctypes.c_int, [_VP]),

@@ -98,6 +98,25 @@ blackScholesOptionValue = blackScholesGeneralizedOptionValue
 blackModelSwaptionValue = blackScholesGeneralizedOptionValue  # AnalyticFormulas.java:985-993
 
 
+def blackScholesDigitalOptionValue(initialStockValue, riskFreeRate, volatility, optionMaturity, optionStrike) -> float:
+    """The value of a digital call under Black-Scholes (functions/AnalyticFormulas.java:728-750):
+    exp(-r T) N(d-), and 1 for a non-positive strike."""
+    if optionStrike <= 0.0:
+        return 1.0
+    dPlus = ((math.log(initialStockValue / optionStrike) + (riskFreeRate + 0.5 * volatility * volatility) * optionMaturity)
+             / (volatility * math.sqrt(optionMaturity)))
+    dMinus = dPlus - volatility * math.sqrt(optionMaturity)
+    return math.exp(-riskFreeRate * optionMaturity) * normal_cdf(dMinus)
+
+
+def blackModelDigitalCapletValue(forward, volatility, periodLength, discountFactor, optionMaturity,
+                                 optionStrike) -> float:
+    """A digital caplet under Black'76 (functions/AnalyticFormulas.java:916-926): the digital
+    option on the forward with zero rate, times the period length and the discount factor."""
+    return (blackScholesDigitalOptionValue(forward, 0.0, volatility, optionMaturity, optionStrike) * periodLength
+            * discountFactor)
+
+
 def bachelierOptionValue(forward, volatility, optionMaturity, optionStrike, payoffUnit) -> float:
     if optionMaturity < 0:
         return 0.0

@@ -261,6 +261,36 @@ class LIBORCovarianceModelFromVolatilityAndCorrelation:
         return float(self.variance[timeIndex, component1])
 
 
+class LIBORCovarianceModelExponentialForm5Param(LIBORCovarianceModelFromVolatilityAndCorrelation):
+    """covariance/LIBORCovarianceModelExponentialForm5Param.java: the four-parameter
+    exponential volatility (a, b, c, d) on the simulation and tenor grids and the
+    exponential-decay correlation (decay e) on the tenor grid, reduced to numberOfFactors;
+    all five parameters calibrateable (default 0.20, 0.05, 0.10, 0.20, 0.10)."""
+
+    def __init__(self, timeDiscretization, liborPeriodDiscretization, numberOfFactors,
+                 parameters=(0.20, 0.05, 0.10, 0.20, 0.10)):
+        p = [float(x) for x in parameters]
+        if len(p) != 5:
+            raise ValueError("LIBORCovarianceModelExponentialForm5Param takes five parameters")
+        vol = LIBORVolatilityModelFourParameterExponentialForm(timeDiscretization, liborPeriodDiscretization, *p[:4],
+                                                               False)
+        corr = LIBORCorrelationModelExponentialDecay(liborPeriodDiscretization, liborPeriodDiscretization,
+                                                     int(numberOfFactors), p[4], False)
+        super().__init__(timeDiscretization, liborPeriodDiscretization, vol, corr)
+        self.parameter = p
+        self.numberOfFactors = int(numberOfFactors)
+
+    def getParameter(self):
+        return list(self.parameter)
+
+    def getParameterAsDouble(self):
+        return np.asarray(self.parameter, dtype=np.float64)
+
+    def getCloneWithModifiedParameters(self, parameters):
+        return LIBORCovarianceModelExponentialForm5Param(self.timeDiscretization, self.liborPeriodDiscretization,
+                                                         self.numberOfFactors, parameters)
+
+
 # --------------------------------------------------------------------------- model
 class LIBORMarketModelFromCovarianceModel:
     """The model's tables as finmath-lib evaluates them (LIBORMarketModelFromCovarianceModel.java:388-444)."""
@@ -330,10 +360,19 @@ class LIBORMarketModelFromCovarianceModel:
         """LIBORMarketModelFromCovarianceModel.getIntegratedLIBORCovariance (:1552-1596):
         [t][i][j] = the sum over simulation steps up to t of lambda_i . lambda_j dt, each step
         counting only components not yet fixed (T_i above the step's start); the upper
-        triangle of step 0 and both triangles after it, as the reference fills them."""
+        triangle of step 0 and both triangles after it, as the reference fills them.  The
+        reference caches the result in the model; so does this class, per simulation grid.
+        Each step's sums run over the factors in the reference's order ((l_ik l_jk) dt added
+        factor by factor), vectorised over the component pairs."""
+        key = tuple(float(x) for x in simulationTimeDiscretization.getAsDoubleArray())
+        cache = self.__dict__.setdefault("_integratedLIBORCovariance", {})
+        if key in cache:
+            return cache[key]
         cov = self.covarianceModel
         tenor = self.liborPeriodDiscretization
         n, N = simulationTimeDiscretization.getNumberOfTimeSteps(), tenor.getNumberOfTimeSteps()
+        tenorTimes = np.array([tenor.getTime(i) for i in range(N)])
+        upper = np.triu(np.ones((N, N), dtype=bool))
         out = np.zeros((n, N, N))
         for t in range(n):
             time = simulationTimeDiscretization.getTime(t)
@@ -343,20 +382,16 @@ class LIBORMarketModelFromCovarianceModel:
             if ct < 0 or ct >= cov.factorLoadings.shape[0]:
                 # the reference's factor-loading lookup throws outside the covariance grid
                 raise ValueError(f"simulation time {time} outside the covariance model's time discretization")
-            loadings = cov.factorLoadings[ct]
-            for i in range(N):
-                if tenor.getTime(i) <= time:
-                    continue
-                for j in range(i, N):
-                    v = 0.0
-                    for k in range(loadings.shape[1]):
-                        v += float(loadings[i, k]) * float(loadings[j, k]) * dt
-                    out[t, i, j] = v
+            loadings = np.asarray(cov.factorLoadings[ct], dtype=np.float64)
+            acc = np.zeros((N, N))
+            for k in range(loadings.shape[1]):
+                acc = acc + (loadings[:, None, k] * loadings[None, :, k]) * dt
+            alive = (tenorTimes > time)[:, None] & upper
+            out[t] = np.where(alive, acc, 0.0)
         for t in range(1, n):
-            for i in range(N):
-                for j in range(i, N):
-                    out[t, i, j] = out[t - 1, i, j] + out[t, i, j]
-                    out[t, j, i] = out[t, i, j]
+            u = out[t - 1] + out[t]
+            out[t] = np.where(upper, u, u.T)
+        cache[key] = out
         return out
 
     def getCloneWithModifiedCovarianceModel(self, covarianceModel):
@@ -528,10 +563,50 @@ class LIBORMonteCarloSimulationFromLIBORModel:
         return RandomVariableGPU(h)
 
     def getNumeraireRandomVariable(self, time):
-        """getNumeraire as a device random variable (adjusted, as getNumeraire), :153-155."""
+        """getNumeraire as a device random variable (adjusted, as getNumeraire), :153-155.
+
+        At a tenor time the library serves it directly.  Between tenor times it is composed as
+        LIBORMarketModelFromCovarianceModel.getNumeraire does (:860-876, :968-1015): under SPOT
+        the unadjusted numeraire of the next tenor time discounted with the forward rate
+        L(t; t, T_next) over T_next - t; under TERMINAL the product of the discount factors of
+        the periods from T_next on with the rates read at min(t, T_l); then, with a discount
+        curve, times mean(N(0) / N(t)) and divided by the geometrically interpolated
+        discount-curve chain (:883-943).  Before time 0 it is the discount curve's factor."""
+        from .randomvariable import RandomVariableGPU
+        time = float(time)
+        m = self.model
+        tenor = m.liborPeriodDiscretization
+        if time < 0:
+            return RandomVariableGPU.constant(float("-inf"), m.discountCurve.getDiscountFactor(None, time))
+        L = _lib.load()
+        if tenor.getTimeIndex(time) >= 0:
+            h = ctypes.c_void_p()
+            check(L.lmm_process_get_numeraire_rv(self.process._h, time, ctypes.byref(h)), "getNumeraire")
+            return RandomVariableGPU(h)
+        upperIndex = -tenor.getTimeIndex(time) - 1
+        if upperIndex - 1 < 0 or upperIndex > tenor.getNumberOfTimeSteps():
+            raise ValueError(f"Numeraire requested for time {time}. Unsupported")
+        upper = tenor.getTime(upperIndex)
+        if m.measure == _lib.MEASURE_TERMINAL:
+            numeraire = RandomVariableGPU.constant(float("-inf"), 1.0)
+            for liborIndex in range(upperIndex, tenor.getNumberOfTimeSteps()):
+                libor = self.getLIBORRandomVariable(self.getTimeIndex(min(time, tenor.getTime(liborIndex))), liborIndex)
+                numeraire = numeraire.discount(libor, tenor.getTimeStep(liborIndex))
+        else:
+            numeraire = self._unadjustedNumeraire(upper)
+        numeraire = numeraire.discount(self.getForwardRate(time, time, upper), upper - time)
+        if m.discountCurve is not None:
+            zeroBond = m.getNumeraireDefaultableZeroBondAsOfTimeZero(time)
+            nonDefaultableZeroBond = numeraire.invert().mult(self._unadjustedNumeraire(0.0)).getAverage()
+            numeraire = numeraire.mult(nonDefaultableZeroBond).div(zeroBond)
+        return numeraire
+
+    def _unadjustedNumeraire(self, tenorTime):
+        """getNumerairetUnAdjusted at a tenor time (:1017-1074), from the simulated paths."""
         from .randomvariable import RandomVariableGPU
         h = ctypes.c_void_p()
-        check(_lib.load().lmm_process_get_numeraire_rv(self.process._h, float(time), ctypes.byref(h)), "getNumeraire")
+        check(_lib.load().lmm_process_get_numeraire_unadjusted_rv(self.process._h, float(tenorTime), ctypes.byref(h)),
+              "getNumerairetUnAdjusted")
         return RandomVariableGPU(h)
 
     def getForwardRate(self, time, periodStart, periodEnd):

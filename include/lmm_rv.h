@@ -94,6 +94,11 @@ int lmm_rv_min_max(const lmm_rv* x, double* out_min, double* out_max);
  * LIBORMarketModelFromCovarianceModel.java:860-876). */
 int lmm_process_get_value_rv(lmm_process* proc, int time_index, int component, lmm_rv** out);
 int lmm_process_get_numeraire_rv(lmm_process* proc, double time, lmm_rv** out);
+/* The numeraire before the discount-curve adjustment at a tenor time,
+ * getNumerairetUnAdjusted (LIBORMarketModelFromCovarianceModel.java:968-1015): the building
+ * block of getNumeraire between tenor times, where the reference discounts the next tenor
+ * time's unadjusted numeraire with the short forward rate and re-applies the adjustment. */
+int lmm_process_get_numeraire_unadjusted_rv(lmm_process* proc, double time, lmm_rv** out);
 
 #ifdef __cplusplus
 }

@@ -824,6 +824,17 @@ double orc_standard_error(const double* x, int64_t n)
 static double orc_numeraire_at_zero(const orc_sim* s);
 
 /* getNumeraire(time) at a tenor time (:860-876, :915-944). out[P]; returns 1 if deterministic. */
+/* getNumerairetUnAdjusted at a tenor time (LIBORMarketModelFromCovarianceModel.java:1017-1074) */
+int orc_sim_numeraire_unadjusted(const orc_sim* s, double time, double* out)
+{
+    const int P = s->P, N = s->m.N;
+    int l = orc_time_index(s->m.tenor, N + 1, time);
+    if (l < 0) return -1;
+    const double* Nu = s->numeraire + (size_t)l * P;
+    for (int p = 0; p < P; p++) out[p] = s->num_det[l] ? Nu[0] : Nu[p];
+    return s->num_det[l];
+}
+
 int orc_sim_numeraire(const orc_sim* s, double time, double* out)
 {
     const int P = s->P, N = s->m.N;

@@ -111,6 +111,7 @@ void     orc_sim_free(orc_sim* s);
 int orc_sim_process_value(const orc_sim* s, int time_index, int component, double* out);
 /* getNumeraire(time) (adjusted) at a tenor time; returns 1 if deterministic. */
 int orc_sim_numeraire(const orc_sim* s, double time, double* out);
+int orc_sim_numeraire_unadjusted(const orc_sim* s, double time, double* out);
 /* Kahan average (RandomVariableFromDoubleArray.getAverage). */
 double orc_kahan_average(const double* x, int64_t n);
 double orc_standard_error(const double* x, int64_t n);

@@ -78,6 +78,7 @@ def lib():
         L.orc_sim_free.argtypes = [ctypes.c_void_p]
         L.orc_sim_process_value.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _D]
         L.orc_sim_numeraire.argtypes = [ctypes.c_void_p, ctypes.c_double, _D]
+        L.orc_sim_numeraire_unadjusted.argtypes = [ctypes.c_void_p, ctypes.c_double, _D]
         L.orc_kahan_average.argtypes = [_D, ctypes.c_int64]
         L.orc_kahan_average.restype = ctypes.c_double
         L.orc_standard_error.argtypes = [_D, ctypes.c_int64]
@@ -255,6 +256,12 @@ class Simulation:
         out = np.empty(self.P)
         rc = lib().orc_sim_numeraire(self._h, time, _p(out))
         if rc < 0:
+            raise ValueError("numeraire off the tenor grid")
+        return out
+
+    def numeraire_unadjusted(self, time: float) -> np.ndarray:
+        out = np.empty(self.P)
+        if lib().orc_sim_numeraire_unadjusted(self._h, time, _p(out)) < 0:
             raise ValueError("numeraire off the tenor grid")
         return out
 

@@ -65,6 +65,10 @@ class NumpyRV:
     def exp(self): return NumpyRV(self.t, np.exp(self.v))
     def invert(self): return NumpyRV(self.t, 1.0 / np.asarray(self.v))
 
+    def discount(self, rate, periodLength):
+        t, v = self._operand(rate)
+        return NumpyRV(max(self.t, t), self.v / (1 + v * periodLength))
+
     def accrue(self, rate, periodLength):
         t, v = self._operand(rate)
         return NumpyRV(max(self.t, t), self.v * (1 + v * periodLength))
@@ -209,3 +213,26 @@ def test_bermudan_with_a_user_basis_provider(lmm20_host):
     assert custom.getExerciseTimes() == list(fix)
     with pytest.raises(ValueError):
         custom._desc()  # the fused gradient and portfolio kernels take the built-in bases only
+
+
+def test_numeraire_between_tenor_times(lmm20_host):
+    # getNumeraire off the tenor grid (LIBORMarketModelFromCovarianceModel.java:860-876,
+    # :883-943, :968-1015) over the oracle's paths: the next tenor time's unadjusted numeraire
+    # discounted with L(t; t, T_next) over T_next - t, times mean(N(0) / N(t)) and divided by
+    # the geometric interpolation of the discount-curve chain
+    cfg, m, osim, sim = lmm20_host
+    sim._unadjustedNumeraire = lambda T: NumpyRV(T, osim.numeraire_unadjusted(T))
+    base = LM.LIBORMonteCarloSimulationFromLIBORModel.getNumeraireRandomVariable
+    tenor = sim.model.liborPeriodDiscretization
+    for t in (0.125, 1.3, 4.75, 9.9):
+        got = base(sim, t).getRealizations()
+        up = tenor.getTime(-tenor.getTimeIndex(t) - 1)
+        lo = up - cfg["period"]
+        fwd = sim.getForwardRate(t, t, up).getRealizations()
+        nu = osim.numeraire_unadjusted(up) / (1.0 + fwd * (up - t))
+        a0, a1 = m.discount_chain[int(round(lo / cfg["period"]))], m.discount_chain[int(round(up / cfg["period"]))]
+        pd = a0 * (a1 / a0) ** ((t - lo) / (up - lo))
+        expected = nu * po.kahan_average(osim.numeraire_unadjusted(0.0) / nu) / pd
+        assert np.allclose(got, expected, rtol=1e-13, atol=0.0)
+    with pytest.raises(ValueError):
+        base(sim, 10.25)  # beyond the last tenor time
