@@ -9,6 +9,7 @@ from ._lib import (CalculationException, PRECISION_FP64, PRECISION_MIXED, SCHEME
 from .lmm import (TimeDiscretizationFromArray, ForwardCurveInterpolation, DiscountCurveFromForwardCurve,
                   LIBORCorrelationModelExponentialDecay, LIBORVolatilityModelFourParameterExponentialForm,
                   LIBORVolatilityModelFromGivenMatrix, LIBORCovarianceModelFromVolatilityAndCorrelation,
+                  LIBORCovarianceModelExponentialForm5Param,
                   LIBORMarketModelFromCovarianceModel, BrownianMotionFromMersenneRandomNumbers,
                   EulerSchemeFromProcessModel, LIBORMonteCarloSimulationFromLIBORModel, Swaption, SwaptionSimple,
                   SwaptionAnalyticApproximation, BermudanSwaption, Portfolio,

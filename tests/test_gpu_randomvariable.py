@@ -225,8 +225,15 @@ def test_process_values_as_random_variables_match_host_copies():
         t = W.tenor_time_indices(cfg)[5]
         assert np.array_equal(sim.getLIBORRandomVariable(t, 7).getRealizations(), sim.getLIBOR(t, 7))
         assert np.array_equal(sim.getNumeraireRandomVariable(3.0).getRealizations(), sim.getNumeraire(3.0))
+        # between tenor times the numeraire is composed from the next tenor time's unadjusted
+        # numeraire and the short forward rate (LIBORMarketModelFromCovarianceModel.java:968-1015)
+        n = sim.getNumeraireRandomVariable(0.25).getRealizations()
+        nu = sim._unadjustedNumeraire(0.5).getRealizations() / (
+            1.0 + sim.getForwardRate(0.25, 0.25, 0.5).getRealizations() * 0.25)
+        a = po.kahan_average(sim._unadjustedNumeraire(0.0).getRealizations() / nu)
+        assert np.allclose(n, nu * a / sim.model.getNumeraireDefaultableZeroBondAsOfTimeZero(0.25), rtol=1e-13, atol=0)
         with pytest.raises(ValueError):
-            sim.getNumeraireRandomVariable(0.25)  # off the tenor grid
+            sim.getNumeraireRandomVariable(10.25)  # beyond the last tenor time
         sim.process.close()
         sim.process.brownianMotion.close()
 

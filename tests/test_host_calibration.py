@@ -146,3 +146,50 @@ def test_calibration_loop_recovers_a_consistent_surface(monkeypatch):
     m2 = F.LIBORMarketModelFromCovarianceModel.of(tenor, None, curve, F.DiscountCurveFromForwardCurve(curve), None,
                                                   start, items, {"calibrationParameters": params2})
     assert m2.getCovarianceModel().getParameter() == pytest.approx(calibrated.getParameter(), rel=1e-12)
+
+
+def test_reference_swaption_calibration_on_the_host(monkeypatch):
+    # testSwaptionCalibration (LIBORMarketModelValuationTest.java:685-807) with its analytic
+    # calibration products: the 5-parameter covariance model calibrated to 36 swaption
+    # volatilities, RMS below the reference's 0.025.  The products need no simulation, so
+    # a process test double stands in for the GPU process the calibration loop builds.
+    import test_gpu_reference_acceptance as RA
+
+    class Process:
+        def __init__(self, model, brownianMotion, *args, **kwargs):
+            self.model, self.brownianMotion, self.numberOfPaths = model, brownianMotion, RA.PATHS
+
+        def getTimeDiscretization(self):
+            return self.brownianMotion.timeDiscretization
+
+        def close(self):
+            pass
+
+    class BrownianMotion:
+        def __init__(self, timeDiscretization, *args):
+            self.timeDiscretization = timeDiscretization
+
+        def close(self):
+            pass
+
+    monkeypatch.setattr(LM, "EulerSchemeFromProcessModel", Process)
+    monkeypatch.setattr(LM, "BrownianMotionFromMersenneRandomNumbers", BrownianMotion)
+    td = F.TimeDiscretizationFromArray(0.0, 40, 0.5)
+    tenor = F.TimeDiscretizationFromArray(0.0, 40, 0.5)
+    curve = F.ForwardCurveInterpolation.createForwardCurveFromForwards(
+        "forwardCurve", [0.5, 1.0, 2.0, 5.0, 40.0], [0.05] * 5, 0.5)
+    model = F.LIBORMarketModelFromCovarianceModel.of(tenor, None, curve, F.DiscountCurveFromForwardCurve(curve), None,
+                                                     F.LIBORCovarianceModelExponentialForm5Param(td, tenor, 6), [], {})
+    sim = F.LIBORMonteCarloSimulationFromLIBORModel(Process(model, BrownianMotion(td)))
+    products = RA.calibration_products(sim)
+    assert len(products) == 36
+    params = {"accuracy": 1e-6, "numberOfPaths": RA.PATHS}
+    calibrated = F.LIBORMarketModelFromCovarianceModel.of(tenor, None, curve, None, None,
+                                                          F.LIBORCovarianceModelExponentialForm5Param(td, tenor, 6),
+                                                          products, {"calibrationParameters": params})
+    simulation = F.LIBORMonteCarloSimulationFromLIBORModel(Process(calibrated, BrownianMotion(td)))
+    deviations = [p.getProduct().getValue(simulation) - p.getTargetValue() for p in products]
+    rms = math.sqrt(sum(d * d for d in deviations) / len(deviations))
+    assert rms < 0.025
+    assert params["optimizer"].getIterations() > 1  # the parameters moved
+    assert list(calibrated.covarianceModel.getParameterAsDouble()) != [0.20, 0.05, 0.10, 0.20, 0.10]
