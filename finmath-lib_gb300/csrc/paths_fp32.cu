@@ -5,8 +5,8 @@
 // 1125-1191): the log-Euler step Y' = log L + d, L' = min(exp(Y'), cap) is carried as
 // L' = min(L exp(d), cap) on the forward rates themselves, so the path state is one FP32
 // register per component.  The drift running sums (carried with dt and the increments,
-// G_k = dW_k + dt S_k) use paired FP32 FMAs, exp and the measure-change ratio use the SFU
-// (__expf, __fdividef).  The numeraire accrual and its adjustment sums stay FP64, as do the
+// G_k = dW_k + dt S_k) use paired FP32 FMAs, exp and the measure-change ratio one SFU
+// instruction each (ex2.approx, rcp.approx).  The numeraire accrual and its adjustment sums stay FP64, as do the
 // regression sums and payoff averages downstream.  The error against the FP64 form is
 // measured and reported, not assumed.
 //
@@ -44,6 +44,23 @@ __device__ __forceinline__ void cp_async16(float* dst, const float* src)
     const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
 }
+// The SFU's approximate reciprocal and base-2 exponential with flush-to-zero, one MUFU
+// instruction each: the arguments here (L + 1/delta in (0, 1e5 + 2], and the step
+// increment times log2 e) are normal numbers far from the range edges that __fdividef and
+// __expf guard with extra compares, selects and scalings.
+__device__ __forceinline__ float rcp_approx(float x)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float exp2_approx(float x)
+{
+    float r;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
@@ -59,9 +76,8 @@ struct Smem32 {
 // staged row of one component fit the register budget this leaves
 __host__ __device__ constexpr int fp32_min_blocks(int nmax) { return nmax <= 24 ? 8 : nmax <= 40 ? 6 : 3; }
 
-// CAPPED: the model caps the forward rates.  The cap is a compile-time variant: on this GPU
-// the compiler's min/select for `v > cap ? cap : v` issues to the narrow FP64 pipe, once per
-// component and step, which costs the uncapped models several percent if left in.
+// CAPPED: the model caps the forward rates (one FMNMX per component-step, a compile-time
+// variant so that uncapped models pay nothing).
 template <int NMAX, int FMAX, bool CAPPED, bool EXACT>
 __global__ void __launch_bounds__(kPathThreads, fp32_min_blocks(NMAX))
     paths_fp32_kernel(const PathLaunch a, const float* __restrict__ rows32)
@@ -97,7 +113,7 @@ __global__ void __launch_bounds__(kPathThreads, fp32_min_blocks(NMAX))
 #pragma unroll
     for (int j = 0; j < NMAX; j++) {
         float v = j < N ? __ldg(a.d_init32 + j) : 0.0f;
-        if (CAPPED && v > cap) v = cap;
+        if (CAPPED) v = fminf(v, cap);
         L[j] = v;
     }
     // the forward rates of all components into rows [N][P] starting at dst (a running
@@ -145,7 +161,7 @@ __global__ void __launch_bounds__(kPathThreads, fp32_min_blocks(NMAX))
                     lr[4 * q + 3] = v.w;
                 }
                 const float Lj = L[j];
-                const float osdt = __fdividef(Lj, Lj + lr[FMAX + 1]) * dt;
+                const float osdt = (Lj * dt) * rcp_approx(Lj + lr[FMAX + 1]);
                 const float2 os2 = make_float2(osdt, osdt);
                 float2 da = make_float2(lr[FMAX], 0.0f), db = make_float2(0.0f, 0.0f);
 #pragma unroll
@@ -157,8 +173,9 @@ __global__ void __launch_bounds__(kPathThreads, fp32_min_blocks(NMAX))
                     if (m & 1) db = __ffma2_rn(G2[m], l2, db);
                     else da = __ffma2_rn(G2[m], l2, da);
                 }
-                float v = Lj * __expf((da.x + db.x) + (da.y + db.y));
-                if (CAPPED && v > cap) v = cap;
+                // exp(d) = 2^(d log2 e)
+                float v = Lj * exp2_approx(((da.x + db.x) + (da.y + db.y)) * 1.4426950408889634f);
+                if (CAPPED) v = fminf(v, cap);
                 L[j] = v;
             }
         });

@@ -925,6 +925,7 @@ int orc_swaption(const orc_sim* s, double exercise, int nper, const double* fixi
 }
 
 #define MAXB 6
+#define MAXPER 128
 
 /* MonteCarloConditionalExpectationRegression (M:montecarlo/conditionalexpectation/
  * MonteCarloConditionalExpectationRegression.java:98-150).  basis[b] NULL = the constant 1. */
@@ -960,10 +961,24 @@ static void regression_ce(int P, int nb, double** basis, const double* y, double
     free(tmp);
 }
 
-int orc_bermudan(const orc_sim* s, int nper, const uint8_t* exercisable, const double* fixing,
-                 const double* period_length, const double* payment, const double* notional,
-                 const double* strike, int callable, int basis_id,
-                 double* value, double* stderr_out, double* per_path, double* exercise_time)
+/* What the AAD reverse sweep needs of the forward valuation, per exercise date (in the
+ * order the backward induction visits them): the period, the conditional expectation X of
+ * the trigger, the continuation values Y and underlying Z the choice picks from, and the
+ * five non-constant basis functions. */
+typedef struct {
+    int ne;
+    int per[MAXPER];
+    double* X;   /* [ne][P] */
+    double* Y;   /* [ne][P] */
+    double* Z;   /* [ne][P] */
+    double* B;   /* [ne][MAXB - 1][P] */
+} berm_record;
+
+static int bermudan_core(const orc_sim* s, int nper, const uint8_t* exercisable, const double* fixing,
+                         const double* period_length, const double* payment, const double* notional,
+                         const double* strike, int callable, int basis_id,
+                         double* value, double* stderr_out, double* per_path, double* exercise_time,
+                         berm_record* rec)
 {
     const int P = s->P, N = s->m.N;
     const double w = 1.0 / (double)P;
@@ -1062,6 +1077,15 @@ int orc_bermudan(const orc_sim* s, int nper, const uint8_t* exercisable, const d
             basis[1] = b[0]; basis[2] = b[1]; basis[3] = b[2]; basis[4] = b[3]; basis[5] = b[4];
         }
         regression_ce(P, 6, basis, trig, ce);
+        if (rec) {
+            const int r = rec->ne++;
+            const size_t P_ = (size_t)P;
+            rec->per[r] = per;
+            memcpy(rec->X + r * P_, ce, sizeof(double) * P_);
+            memcpy(rec->Y + r * P_, values, sizeof(double) * P_);
+            memcpy(rec->Z + r * P_, under, sizeof(double) * P_);
+            for (int i = 1; i < MAXB; i++) memcpy(rec->B + ((size_t)r * (MAXB - 1) + i - 1) * P_, basis[i], sizeof(double) * P_);
+        }
         for (int p = 0; p < P; p++) {
             int cont = ce[p] >= 0.0;
             values[p] = cont ? values[p] : under[p];
@@ -1079,6 +1103,112 @@ int orc_bermudan(const orc_sim* s, int nper, const uint8_t* exercisable, const d
 done:
     free(values); free(under); free(ex); free(num); free(trig); free(ce);
     for (int i = 0; i < MAXB; i++) free(b[i]);
+    return rc;
+}
+
+int orc_bermudan(const orc_sim* s, int nper, const uint8_t* exercisable, const double* fixing,
+                 const double* period_length, const double* payment, const double* notional,
+                 const double* strike, int callable, int basis_id,
+                 double* value, double* stderr_out, double* per_path, double* exercise_time)
+{
+    return bermudan_core(s, nper, exercisable, fixing, period_length, payment, notional, strike, callable, basis_id,
+                         value, stderr_out, per_path, exercise_time, NULL);
+}
+
+/* getStandardDeviation (RandomVariableFromDoubleArray.java:395-404 with getVariance :333-355) */
+static double orc_standard_deviation(const double* x, int64_t n)
+{
+    if (n <= 1) return 0.0;
+    double avg = orc_kahan_average(x, n);
+    double sum = 0.0, err = 0.0;
+    for (int64_t i = 0; i < n; i++) {
+        double v = (x[i] - avg) * (x[i] - avg) - err;
+        double ns = sum + v;
+        err = (ns - sum) - v;
+        sum = ns;
+    }
+    return sqrt(sum / (double)n);
+}
+
+/* The adjoint weights that the reference's RandomVariableDifferentiableAAD gives the
+ * Bermudan's discounted cash flows.  The value is F = mean(values * N(0) / w) with
+ * values built by BermudanSwaption.getValues (BermudanSwaption.java:91-157) from the cash
+ * flows c[k][p] = ((L_k - K_k) d_k) n_k / N(T_pay) times the weight w = 1/P; the reverse
+ * sweep of that operator graph follows RandomVariableDifferentiableAAD.java:
+ *   CHOOSE  values = X.choose(Y, Z): Y gets the adjoint where X >= 0, Z where X < 0
+ *           (:171-208 with the partial derivatives of :396-444); X gets
+ *           ZERO (method 0): nothing;
+ *           DISCRETE_DELTA (method 1): (Y - Z) 1{-eps/2 <= X < eps/2} / eps with
+ *           eps = width * X.getStandardDeviation() (:409-429; the factory's default width
+ *           is 0.05, RandomVariableDifferentiableAADFactory.java:67-68);
+ *   CONDITIONAL_EXPECTATION  the trigger X = E[values - under | basis]: its argument gets
+ *           the conditional expectation of the adjoint, with the same basis (:188-192);
+ *   AVERAGE  getAverage returns a double, so the numeraire adjustment is a constant (:771).
+ * omega[k][p] = dF/dc[k][p] / w: the gradient of F is then the path mean of
+ * sum_k omega[k][p] dc[k][p]/dtheta, the cash flows differentiated with the adjustment held. */
+int orc_bermudan_aad(const orc_sim* s, int nper, const uint8_t* exercisable, const double* fixing,
+                     const double* period_length, const double* payment, const double* notional,
+                     const double* strike, int callable, int basis_id, int method, double width,
+                     double* value, double* omega)
+{
+    const int P = s->P;
+    const size_t P_ = (size_t)P;
+    if (nper > MAXPER) return -10;
+    int ne = 0;
+    for (int k = 0; k < nper; k++) ne += exercisable[k] ? 1 : 0;
+    berm_record rec;
+    rec.ne = 0;
+    rec.X = (double*)malloc(sizeof(double) * P_ * (size_t)(ne > 0 ? ne : 1));
+    rec.Y = (double*)malloc(sizeof(double) * P_ * (size_t)(ne > 0 ? ne : 1));
+    rec.Z = (double*)malloc(sizeof(double) * P_ * (size_t)(ne > 0 ? ne : 1));
+    rec.B = (double*)malloc(sizeof(double) * P_ * (MAXB - 1) * (size_t)(ne > 0 ? ne : 1));
+    double* vbar = (double*)malloc(sizeof(double) * P_);
+    double* ubar = (double*)malloc(sizeof(double) * P_);
+    double* xbar = (double*)malloc(sizeof(double) * P_);
+    double* dbar = (double*)malloc(sizeof(double) * P_);
+    int rc = bermudan_core(s, nper, exercisable, fixing, period_length, payment, notional, strike, callable, basis_id,
+                           value, NULL, NULL, NULL, &rec);
+    if (rc == 0) {
+        const double num0 = orc_numeraire_at_zero(s);
+        for (int p = 0; p < P; p++) { vbar[p] = num0; ubar[p] = 0.0; }
+        /* the backward induction recorded its dates from the last period down: replay them upward */
+        int r = rec.ne - 1;
+        for (int k = 0; k < nper; k++) {
+            if (exercisable[k]) {
+                const double* X = rec.X + (size_t)r * P_;
+                const double* Y = rec.Y + (size_t)r * P_;
+                const double* Z = rec.Z + (size_t)r * P_;
+                double eps = 0.0;
+                if (method == 1) eps = width * orc_standard_deviation(X, P);
+                for (int p = 0; p < P; p++) {
+                    double xb = 0.0;
+                    if (method == 1) {
+                        if (isinf(eps)) xb = vbar[p] * (Y[p] - Z[p]);
+                        else if (eps > 0.0)
+                            xb = (X[p] + eps / 2 >= 0.0 && X[p] - eps / 2 < 0.0) ? vbar[p] * (Y[p] - Z[p]) / eps : 0.0;
+                    }
+                    xbar[p] = xb;
+                    const int cont = X[p] >= 0.0;
+                    ubar[p] = ubar[p] + (cont ? 0.0 : vbar[p]);
+                    vbar[p] = cont ? vbar[p] : 0.0;
+                }
+                if (method == 1) {
+                    double* basis[MAXB];
+                    basis[0] = NULL;
+                    for (int i = 1; i < MAXB; i++) basis[i] = rec.B + ((size_t)r * (MAXB - 1) + i - 1) * P_;
+                    regression_ce(P, 6, basis, xbar, dbar);
+                    for (int p = 0; p < P; p++) {
+                        vbar[p] = vbar[p] + dbar[p];
+                        ubar[p] = ubar[p] - dbar[p];
+                    }
+                }
+                r--;
+            }
+            for (int p = 0; p < P; p++) omega[(size_t)k * P_ + p] = callable ? ubar[p] : vbar[p];
+        }
+    }
+    free(rec.X); free(rec.Y); free(rec.Z); free(rec.B);
+    free(vbar); free(ubar); free(xbar); free(dbar);
     return rc;
 }
 

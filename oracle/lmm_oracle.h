@@ -128,6 +128,13 @@ int orc_bermudan(const orc_sim* s, int nper, const uint8_t* exercisable, const d
                  const double* strike, int callable, int basis_id,
                  double* value, double* stderr_out, double* per_path /* or NULL */,
                  double* exercise_time /* or NULL */);
+/* The reference AAD's adjoint weights of the Bermudan's discounted cash flows (method 0:
+ * diracDeltaApproximationMethod ZERO, 1: DISCRETE_DELTA with the given width per standard
+ * deviation); omega [nper][P]. */
+int orc_bermudan_aad(const orc_sim* s, int nper, const uint8_t* exercisable, const double* fixing,
+                     const double* period_length, const double* payment, const double* notional,
+                     const double* strike, int callable, int basis_id, int method, double width,
+                     double* value, double* omega);
 
 /* Bermudan value with frozen per-path exercise times (for finite differences of the
  * pathwise derivative). */

@@ -88,6 +88,8 @@ def lib():
         L.orc_bermudan.argtypes = [ctypes.c_void_p, ctypes.c_int, _U8, _D, _D, _D, _D, _D, ctypes.c_int,
                                    ctypes.c_int, _D, _D, _D, _D]
         L.orc_bermudan_frozen.argtypes = [ctypes.c_void_p, ctypes.c_int, _D, _D, _D, _D, _D, ctypes.c_int, _D, _D]
+        L.orc_bermudan_aad.argtypes = [ctypes.c_void_p, ctypes.c_int, _U8, _D, _D, _D, _D, _D, ctypes.c_int,
+                                       ctypes.c_int, ctypes.c_int, ctypes.c_double, _D, _D]
         _lib = L
     return _lib
 
@@ -292,6 +294,28 @@ class Simulation:
         if rc != 0:
             raise ValueError(f"bermudan failed rc={rc}")
         return (v.value, e.value, pp, et) if per_path else (v.value, e.value)
+
+
+def _bermudan_aad(self, fixing, period_length, payment, strike, method="ZERO", width=0.05, exercisable=None,
+                  notional=None, callable_=True, basis_id=1):
+    """The reference AAD's adjoint weights omega[k][p] of the discounted cash flows (see
+    orc_bermudan_aad) and the forward value."""
+    fixing, period_length, payment = f64(fixing), f64(period_length), f64(payment)
+    n = len(fixing)
+    strike = f64(np.broadcast_to(strike, (n,)))
+    notional = f64(np.ones(n) if notional is None else np.broadcast_to(notional, (n,)))
+    ex = np.ascontiguousarray(np.ones(n) if exercisable is None else exercisable, dtype=np.uint8)
+    v = ctypes.c_double()
+    omega = np.empty((n, self.P))
+    m = {"ZERO": 0, "DISCRETE_DELTA": 1}[method]
+    rc = lib().orc_bermudan_aad(self._h, n, _p(ex, _U8), _p(fixing), _p(period_length), _p(payment), _p(notional),
+                                _p(strike), int(callable_), basis_id, m, float(width), ctypes.byref(v), _p(omega))
+    if rc != 0:
+        raise ValueError(f"bermudan aad failed rc={rc}")
+    return v.value, omega
+
+
+Simulation.bermudan_aad = _bermudan_aad
 
 
 def _bermudan_frozen(self, fixing, period_length, payment, strike, exercise_time, notional=None, callable_=True):

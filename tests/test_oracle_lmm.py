@@ -147,3 +147,28 @@ def test_oracle_euler_and_functional_agree_to_rounding():
     a = po.Simulation(m1, dW).process_value(m1.T, m1.N - 1)
     b = po.Simulation(m0, dW).process_value(m0.T, m0.N - 1)
     np.testing.assert_allclose(a, b, rtol=1e-12)
+
+
+def test_reference_aad_weights_of_the_bermudan():
+    # orc_bermudan_aad (the reverse sweep of RandomVariableDifferentiableAAD over
+    # BermudanSwaption.getValues): under ZERO the weights are the frozen exercise decisions,
+    # so the weighted discounted cash flows rebuild the value; DISCRETE_DELTA with an empty
+    # window reduces to ZERO; with the default window the boundary term, projected through
+    # the regression, moves the weights of every path
+    cfg = W.LMM20
+    P = 2000
+    m = oracle_model(cfg)
+    sim = po.Simulation(m, po.brownian_increments(m.times, m.F, P, cfg["seed"]))
+    fix, plen, pay, K = W.bermudan_schedule(cfg)
+    v, e, pp, et = sim.bermudan(fix, plen, pay, K, basis_id=1, per_path=True)
+    v0, w0 = sim.bermudan_aad(fix, plen, pay, K, method="ZERO")
+    assert v0 == v
+    paid = (np.asarray(fix)[:, None] >= et[None, :]).astype(float)
+    assert np.array_equal(w0, paid)
+    cash = np.array([((sim.process_value(int(round(f / cfg["dt"])), int(round(f / cfg["period"]))) - K) * d)
+                     / sim.numeraire(t) for f, d, t in zip(fix, plen, pay)])
+    assert np.allclose(np.sum(w0 * cash, axis=0), pp, rtol=1e-12, atol=1e-15)
+    _, we = sim.bermudan_aad(fix, plen, pay, K, method="DISCRETE_DELTA", width=0.0)
+    assert np.array_equal(we, w0)
+    _, wd = sim.bermudan_aad(fix, plen, pay, K, method="DISCRETE_DELTA")
+    assert np.all(np.isfinite(wd)) and np.any(wd != w0)
