@@ -188,8 +188,9 @@ struct lmm_process {
     // device tables
     double *d_loadings = nullptr, *d_variance = nullptr, *d_dt = nullptr, *d_delta = nullptr, *d_init = nullptr;
     double* d_exp_tab = nullptr;
-    double *d_inv_delta = nullptr, *d_var_half_dt = nullptr;
+    double *d_inv_delta = nullptr, *d_var_half_dt = nullptr, *d_init_state = nullptr;
     float *d_lam32 = nullptr, *d_inv_delta32 = nullptr, *d_dt32 = nullptr, *d_init32 = nullptr;
+    float *d_rows_df = nullptr, *d_dt_df = nullptr;  // FP64 fast kernel: double-float rows and time steps
     int *d_first = nullptr, *d_obs_slot = nullptr, *d_tenor_tidx = nullptr;
     uint8_t* d_det = nullptr;
     // results
@@ -489,9 +490,35 @@ int lmm_process_create(const lmm_model_desc* m, lmm_brownian* bm, lmm_process** 
     if (!rc) rc = upload(&pr->d_inv_delta, inv_delta.data(), inv_delta.size(), s);
     if (!rc) rc = upload(&pr->d_var_half_dt, var_half_dt.data(), var_half_dt.size(), s);
     if (!rc) rc = upload(&pr->d_init, m->initial_forwards, (size_t)N, s);
+    // getInitialState (log(max(f, 0)), LIBORMarketModelFromCovarianceModel.java:1081-1093) and
+    // applyStateSpaceTransform (exp, :1200-1212): the same deterministic value on every path
+    std::vector<double> init_state(N);  // lives until the stream synchronisation below
+    for (int j = 0; j < N; j++) init_state[j] = std::exp(std::log(std::max(m->initial_forwards[j], 0.0)));
+    if (!rc) rc = upload(&pr->d_init_state, init_state.data(), init_state.size(), s);
     if (!rc) rc = upload(&pr->d_first, pr->first.data(), pr->first.size(), s);
     if (!rc) rc = upload(&pr->d_det, pr->num_det.data(), pr->num_det.size(), s);
     if (!rc) rc = upload(&pr->d_tenor_tidx, pr->tenor_tidx.data(), pr->tenor_tidx.size(), s);
+    if (!rc && pr->precision == LMM_PRECISION_FP64) {
+        // the FP64 fast kernel's rows as double-float pairs (hi = x rounded to FP32, lo = the
+        // rounded remainder): loadings, the drift term (variance * -0.5) * dt_i and 1/delta_j
+        const int fmax = paths_fp64_fmax(N, F);
+        const int FPD = fp64_df_pitch(fmax);
+        auto split = [](double x, float* hi, float* lo) {
+            *hi = (float)x;
+            *lo = (float)(x - (double)*hi);
+        };
+        std::vector<float> rows((size_t)T * N * FPD, 0.0f), dtdf((size_t)T * 2);
+        for (size_t r = 0; r < (size_t)T * N; r++) {
+            float* row = rows.data() + r * FPD;
+            for (int k = 0; k < F; k++) split(m->factor_loadings[r * F + k], row + k, row + fmax + k);
+            split(var_half_dt[r], row + 2 * fmax, row + 2 * fmax + 1);
+            split(inv_delta[r % N], row + 2 * fmax + 2, row + 2 * fmax + 3);
+        }
+        for (int i = 0; i < T; i++) split(dt[i], &dtdf[2 * i], &dtdf[2 * i + 1]);
+        rc = upload(&pr->d_rows_df, rows.data(), rows.size(), s);
+        if (!rc) rc = upload(&pr->d_dt_df, dtdf.data(), dtdf.size(), s);
+        if (!rc) rc = cudaStreamSynchronize(s) == cudaSuccess ? 0 : fail(LMM_ERR_CUDA, "stream sync");
+    }
     if (!rc && pr->precision == LMM_PRECISION_MIXED) {
         int fmax = 0;
         const int FP = paths_fp32_rows(N, F, &fmax);
@@ -577,6 +604,9 @@ static int process_ensure(lmm_process* pr)
     a.d_first = pr->d_first;
     a.d_delta = pr->d_delta;
     a.d_exp_tab = pr->d_exp_tab;
+    a.d_init_state = pr->d_init_state;
+    a.d_rows_df = pr->d_rows_df;
+    a.d_dt_df = pr->d_dt_df;
     a.d_inv_delta = pr->d_inv_delta;
     a.d_var_half_dt = pr->d_var_half_dt;
     a.d_inv_delta32 = pr->d_inv_delta32;
@@ -712,6 +742,9 @@ int lmm_process_destroy(lmm_process* pr)
     dfree(pr->d_dt, s);
     dfree(pr->d_delta, s);
     dfree(pr->d_exp_tab, s);
+    dfree(pr->d_init_state, s);
+    dfree(pr->d_rows_df, s);
+    dfree(pr->d_dt_df, s);
     dfree(pr->d_inv_delta, s);
     dfree(pr->d_var_half_dt, s);
     dfree(pr->d_init, s);

@@ -99,4 +99,32 @@ __device__ __forceinline__ double f32_to_f64_int(float f)
     return __hiloint2double((int)hi, (int)(b << 29));
 }
 
+// ---------------------------------------------------------------- double-float sums for the FP64 path kernel
+// A value carried as an unevaluated pair p + s of floats (p the running FP32 value, s the
+// FP32 sum of the exact errors): Dot2 accumulation, about 2^-48 relative per accumulated term.
+
+// p + s += (ah + al) (bh + bl), the al bl term dropped; the product's rounding error is exact
+// (one fused multiply-add) and the two cross terms ride in the same error accumulator
+__device__ __forceinline__ void df_dot_acc(float& p, float& s, float ah, float al, float bh, float bl)
+{
+    const float h = __fmul_rn(ah, bh);
+    float r = fmaf(ah, bh, -h);
+    r = fmaf(ah, bl, r);
+    r = fmaf(al, bh, r);
+    float x, q;
+    two_sum(p, h, x, q);
+    p = x;
+    s = s + (q + r);
+}
+
+// a double as hi + lo floats (hi = x rounded to FP32 in integer operations, lo = the rounded
+// remainder: one FP64 subtraction, which is exact), about 2^-48 relative
+__device__ __forceinline__ void df_split(double x, float& hi, float& lo)
+{
+    hi = f64_to_f32_int(x);
+    lo = f64_to_f32_int(x - f32_to_f64_int(hi));
+}
+
+__device__ __forceinline__ double df_to_double(float hi, float lo) { return f32_to_f64_int(hi) + f32_to_f64_int(lo); }
+
 }  // namespace lmm

@@ -121,7 +121,11 @@ struct PathLaunch {
     const float* d_dt32;       // [T] time steps in FP32 (mixed form)
     const float* d_init32;     // [N] initial forwards max(f, 0) in FP32 (mixed form)
     const double* d_exp_tab;   // [2 kExpTableHalf + 1] exp(k/kExpTableHalf) (FP64 form, see fp64math.cuh)
+    const float* d_rows_df;    // [T][N][fp64_df_pitch(FMAX)] FP64 fast kernel rows as double-float pairs:
+                               // loadings hi [FMAX], lo [FMAX], drift term (hi, lo), 1/delta (hi, lo)
+    const float* d_dt_df;      // [T][2] time steps as double-float pairs
     const double* d_init;      // [N] initial forwards
+    const double* d_init_state;// [N] exp(log(max(f, 0))): the transformed initial state of the lognormal model
     const int* d_obs_slot;     // [T+1] observation slot or -1
     const void* d_dw;          // [T][F][P] fp64 or fp32
     void* d_states;            // [nobs][N][P] fp64 or fp32
@@ -133,6 +137,10 @@ struct PathLaunch {
     int ckpt_stride;           // forward rates L every ckpt_stride steps (in the path precision)
 };
 int launch_paths_fp64(const PathLaunch& a, cudaStream_t s, int* blocks_out);
+// row pitch (floats) of the FP64 fast kernel's double-float rows, and the FMAX the launcher
+// instantiates for N forward rates and F factors
+__host__ __device__ constexpr int fp64_df_pitch(int fmax) { return (2 * fmax + 4 + 3) / 4 * 4; }
+int paths_fp64_fmax(int N, int F);
 // rows32: [T][N][pitch] FP32 component rows of the mixed path kernel, pitch =
 // paths_fp32_rows(N, F, &fmax): the F loadings, zeros up to fmax, then at fmax the drift's
 // deterministic part of the step, (variance * -0.5) * dt_i, and at fmax + 1 the 1/delta_j

@@ -197,7 +197,6 @@ __global__ void __launch_bounds__(kPathThreads, fp32_min_blocks(NMAX))
     double Nv = 1.0;
     if (active) a.d_numeraire[p] = 1.0;
     if (a.d_inv_numeraire && active) a.d_inv_numeraire[p] = 1.0;
-    const bool u16 = lane & 16, u8 = lane & 8, u4 = lane & 4;
 #pragma unroll
     for (int c = 0; c < NMAX / 8; c++) {
         double v[8];
@@ -218,24 +217,9 @@ __global__ void __launch_bounds__(kPathThreads, fp32_min_blocks(NMAX))
                 }
             }
         }
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            const double keep = u16 ? v[q + 4] : v[q], send = u16 ? v[q] : v[q + 4];
-            v[q] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
-        }
-#pragma unroll
-        for (int q = 0; q < 2; q++) {
-            const double keep = u8 ? v[q + 2] : v[q], send = u8 ? v[q] : v[q + 2];
-            v[q] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
-        }
-        {
-            const double keep = u4 ? v[1] : v[0], send = u4 ? v[0] : v[1];
-            v[0] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
-        }
-        v[0] += __shfl_xor_sync(0xffffffffu, v[0], 2);
-        v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
-        const int idx = 8 * c + (u16 ? 4 : 0) + (u8 ? 2 : 0) + (u4 ? 1 : 0);
-        if ((lane & 3) == 0 && idx < N) sm.wsum[warp][idx] = v[0];
+        const double sum = warp_sum8_transposed(v, lane);
+        const int idx = 8 * c + ((lane >> 2) & 7);
+        if ((lane & 3) == 0 && idx < N) sm.wsum[warp][idx] = sum;
     }
     __syncthreads();
     if (tid < N) {

@@ -8,6 +8,13 @@ int launch_paths_fp64_n64(const PathLaunch& a, cudaStream_t s, int blocks);
 
 int path_blocks(int P) { return (P + kPathThreads - 1) / kPathThreads; }
 
+int paths_fp64_fmax(int N, int F)
+{
+    if (N <= 24 && F <= 4) return 4;
+    if (N <= 40 && F <= 10) return 10;
+    return 16;
+}
+
 int launch_paths_fp64(const PathLaunch& a, cudaStream_t s, int* blocks_out)
 {
     const int blocks = path_blocks(a.P);

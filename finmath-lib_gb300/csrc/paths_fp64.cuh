@@ -13,20 +13,26 @@
 // at the end from the frozen fixings, and each block writes compensated partial sums
 // of 1/N(T_l) for the numeraire adjustment.
 //
-// Compiled with -fmad=false.  The GPU's narrow FP64 pipe bounds the fast kernel, so it
-// spends fewer FP64 instructions than the reference's literal arithmetic, all in FP64:
-//  * the drift's and the Euler step's multiply-adds are fused FP64 FMAs (each rounds once
-//    instead of twice), and the drift's running sums S_k carry dt and the increments dW_k
-//    along (G_k = dW_k + dt S_k), so that a component costs 2F FMAs instead of 3F;
+// Compiled with -fmad=false.  On this GPU an FP64 instruction costs as much pipe time as
+// 64 FP32 ones, so the fast kernel keeps in FP64 only what needs FP64's range and
+// accuracy -- the forward rates, the exponential of the step and the numeraire -- and moves
+// the rest to the FP32 pipe in double-float arithmetic (pairs of floats, about 2^-48
+// relative, dfloat.cuh):
+//  * the drift's running sums S_k carry dt and the increments dW_k along (G_k = dW_k +
+//    dt S_k), as double-float pairs, so that a component costs 2F double-float multiply-adds
+//    (Dot2 steps: 12 FP32 instructions each) and no FP64 multiply-add;
+//  * L / (L + 1/delta) is the FP32 reciprocal refined by one double-float Newton step;
 //  * the Euler-log step exp(log L + d) (EULER_FUNCTIONAL) is evaluated as L exp(d), and the
 //    EULER step exp(Y + d) as exp(Y) exp(d) with exp(Y) carried instead of Y, where exp(d)
-//    of the small step increment d is exp_small (fp64math.cuh) -- no log, and a 9-instruction exp;
-//  * the drift's L / (L + 1/delta) takes a Newton reciprocal (rcp_newton) for the division.
-// The states agree with the reference's order to about 1e-14 relative, inside the 1e-12
-// parity bound.  The general kernel keeps the reference's literal order throughout
-// (CUDA's exp/log, correctly rounded division, unfused).
+//    is the table method of exp_small (fp64math.cuh) with its argument reduction done in
+//    FP32 on the double-float d: nine FP64 instructions per component-step in all.
+// The increment d has an absolute error of a few 1e-16, so the states agree with the
+// reference's order to about 1e-14 relative, inside the 1e-12 parity bound.  The general
+// kernel keeps the reference's literal order throughout (CUDA's exp/log, correctly rounded
+// division, unfused).
 #pragma once
 
+#include "dfloat.cuh"
 #include "fp64math.cuh"
 #include "lmm_internal.h"
 #include "reduce.cuh"
@@ -45,9 +51,18 @@ __device__ __forceinline__ double cap_positive(double v, long long capbits)
     return (b > capbits && b <= 0x7ff0000000000000LL) ? __longlong_as_double(capbits) : v;
 }
 
+// the SFU's approximate reciprocal (flush-to-zero; the argument here is L + 1/delta > 0)
+__device__ __forceinline__ float rcp_approx_f32(float x)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 template <int NMAX, int FMAX, bool FUNCTIONAL>
 __global__ void __launch_bounds__(kPathThreads) paths_fp64_kernel(const PathLaunch a)
 {
+    constexpr int FPD = fp64_df_pitch(FMAX);
     const int p = blockIdx.x * kPathThreads + threadIdx.x;
     const bool active = p < a.P;
     const int N = a.N, F = a.F, P = a.P;
@@ -61,9 +76,9 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp64_kernel(const PathLaun
 #pragma unroll
     for (int j = 0; j < NMAX; j++) {
         if (j < N) {
-            // getInitialState (:1081-1093): log(max(f,0)); applyStateSpaceTransform (:1200-1212)
-            const double f = __ldg(a.d_init + j);
-            const double e0 = exp(log(f > 0.0 ? f : 0.0));
+            // getInitialState (:1081-1093) and applyStateSpaceTransform (:1200-1212):
+            // exp(log(max(f,0))), the same for every path, from the host
+            const double e0 = __ldg(a.d_init_state + j);
             L[j] = cap_positive(e0, capbits);
             if (!FUNCTIONAL) E[FUNCTIONAL ? 0 : j] = e0;
         } else {
@@ -87,43 +102,89 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp64_kernel(const PathLaun
 
     for (int i = 0; i < a.T; i++) {
         const int first = __ldg(a.d_first + i);
-        const double dt = __ldg(a.d_dt + i);
-        const double* lam = a.d_loadings + (size_t)i * N * F;
-        const double* var_half_dt = a.d_var_half_dt + (size_t)i * N;
-        double dw[FMAX];
-#pragma unroll
-        for (int k = 0; k < FMAX; k++) dw[k] = (k < F && active) ? dW[((size_t)i * F + k) * P + p] : 0.0;
+        const float dth = __ldg(a.d_dt_df + 2 * i), dtl = __ldg(a.d_dt_df + 2 * i + 1);
+        const float4* rows = reinterpret_cast<const float4*>(a.d_rows_df + (size_t)i * N * FPD);
         // G_k = dW_k + dt S_k with the drift's running sum S_k = sum_{l<=j} os_l lambda_lk
-        // (:1156-1158): the step increment of component j is then
-        //   d_j = mu_j dt + sum_k dW_k lambda_jk = sum_k G_k lambda_jk - dt variance_j / 2,
-        // two fused multiply-adds per factor instead of three
-        double G[FMAX];
+        // (:1156-1158), carried as double-float pairs (Gp + Gs): the step increment of
+        // component j is then  d_j = mu_j dt + sum_k dW_k lambda_jk = sum_k G_k lambda_jk
+        // - dt variance_j / 2, two double-float multiply-adds per factor on the FP32 pipe
+        float Gp[FMAX], Gs[FMAX];
 #pragma unroll
-        for (int k = 0; k < FMAX; k++) G[k] = dw[k];
+        for (int k = 0; k < FMAX; k++) {
+            Gp[k] = 0.0f;
+            Gs[k] = 0.0f;
+            if (k < F && active) df_split(dW[((size_t)i * F + k) * P + p], Gp[k], Gs[k]);
+        }
 #pragma unroll
         for (int j = 0; j < NMAX; j++) {
             if (j < N && j >= first) {
+                // the component's row: loadings (hi, lo), the drift term (variance * -0.5) * dt
+                // and 1/delta, each as a double-float pair
+                float r[FPD];
+#pragma unroll
+                for (int q = 0; q < FPD / 4; q++) {
+                    const float4 v = __ldg(rows + j * (FPD / 4) + q);
+                    r[4 * q] = v.x;
+                    r[4 * q + 1] = v.y;
+                    r[4 * q + 2] = v.z;
+                    r[4 * q + 3] = v.w;
+                }
                 const double Lj = L[j];
-                // Scalar(delta).discount(L, delta) = 1/(L*(delta/delta) + 1/delta) (stochastic/Scalar.java:321-328),
-                // times L (:1149-1153); delta/delta is exactly 1.0 and 1/delta is precomputed.
-                const double os = rcp_newton(Lj + __ldg(a.d_inv_delta + j)) * Lj;
-                const double osdt = os * dt;
-                double lj[FMAX];
+                // os = L / (L + 1/delta) (Scalar(delta).discount(L, delta) times L, :1149-1153):
+                // the FP32 reciprocal of L + 1/delta refined by one double-float Newton step
+                // (about 2^-44 relative; os enters only the drift, a small part of d)
+                float Lh, Ll;
+                df_split(Lj, Lh, Ll);
+                float xh, xl;
+                two_sum(Lh, r[2 * FMAX + 2], xh, xl);
+                xl = xl + (Ll + r[2 * FMAX + 3]);
+                const float r0 = rcp_approx_f32(xh);
+                const float ph = __fmul_rn(xh, r0);
+                float pe = fmaf(xh, r0, -ph);
+                pe = fmaf(xl, r0, pe);
+                const float er = (1.0f - ph) - pe;
+                const float r1 = __fmul_rn(r0, er);
+                const float oh = __fmul_rn(Lh, r0);
+                float oe = fmaf(Lh, r0, -oh);
+                oe = fmaf(Lh, r1, oe);
+                oe = fmaf(Ll, r0, oe);
+                // os dt
+                const float qh = __fmul_rn(oh, dth);
+                float qe = fmaf(oh, dth, -qh);
+                qe = fmaf(oh, dtl, qe);
+                qe = fmaf(oe, dth, qe);
+                // Euler step (EulerSchemeFromProcessModel.java:235-255) with the drift of
+                // :1159 and :1183-1189: the increment d of the log state
+                float dp = r[2 * FMAX], ds = r[2 * FMAX + 1];
 #pragma unroll
                 for (int k = 0; k < FMAX; k++) {
                     if (k < F) {
-                        lj[k] = __ldg(lam + j * F + k);
-                        G[k] = fma(osdt, lj[k], G[k]);
+                        df_dot_acc(Gp[k], Gs[k], qh, qe, r[k], r[FMAX + k]);
+                        df_dot_acc(dp, ds, Gp[k], Gs[k], r[k], r[FMAX + k]);
                     }
                 }
-                // Euler step (EulerSchemeFromProcessModel.java:235-255) with the drift of
-                // :1159 and :1183-1189 (variance * -0.5): the increment d of the log state,
+                // exp(d) by the table method of exp_small (fp64math.cuh): k = rint(256 d) and
+                // the exact remainder dh - k/256 formed in FP32, the reduced argument and its
+                // degree-5 polynomial in FP64
+                float dh, dl;
+                two_sum(dp, ds, dh, dl);
+                double g;
+                if (fabsf(dh) <= 1.0f) {
+                    const float t = fmaf(dh, (float)kExpTableHalf, 12582912.0f);  // 1.5 2^23 + rint(256 dh)
+                    const int kk = __float_as_int(t) - 0x4b400000;
+                    const float rh = fmaf(-(t - 12582912.0f), 1.0f / kExpTableHalf, dh);  // exact
+                    const double rr = df_to_double(rh, dl);
+                    double pp = 1.0 / 120.0;
+                    pp = fma(pp, rr, 1.0 / 24.0);
+                    pp = fma(pp, rr, 1.0 / 6.0);
+                    pp = fma(pp, rr, 0.5);
+                    pp = fma(pp, rr, 1.0);
+                    pp = fma(pp, rr, 1.0);
+                    g = __ldg(etab + kExpTableHalf + kk) * pp;
+                } else {
+                    g = exp(df_to_double(dh, dl));
+                }
                 // then L exp(d) (FUNCTIONAL: log L is the state) or exp(Y) exp(d) (EULER)
-                double d = __ldg(var_half_dt + j);  // (variance * -0.5) * dt, from the host
-#pragma unroll
-                for (int k = 0; k < FMAX; k++)
-                    if (k < F) d = fma(G[k], lj[k], d);
-                const double g = exp_small(d, etab);
                 if (FUNCTIONAL) {
                     L[j] = cap_positive(Lj * g, capbits);
                 } else {
@@ -148,22 +209,46 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp64_kernel(const PathLaun
     }
 
     // Spot numeraire from the frozen fixings L_l(T_l) (:1050-1066): Scalar.accrue while
-    // the numeraire is deterministic, RandomVariableFromDoubleArray.accrue afterwards.
+    // the numeraire is deterministic, RandomVariableFromDoubleArray.accrue afterwards.  The
+    // numeraire adjustment's input, mean of N(T)^-1 * N(0) (:869-874), from 1/N by a Newton
+    // reciprocal (within an ulp of the division) summed in plain FP64 within each warp
+    // (transposed reductions over chunks of eight tenor times) and compensated across warps.
+    static_assert(NMAX % 8 == 0, "the transposed reduction works on chunks of eight tenor times");
+    __shared__ double wsum[kPathThreads / 32][NMAX];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     double Nv = 1.0;
     if (active) a.d_numeraire[p] = 1.0;
     if (a.d_inv_numeraire && active) a.d_inv_numeraire[p] = 1.0;
 #pragma unroll
-    for (int l = 0; l < NMAX; l++) {
-        if (l < N) {
-            const double delta = __ldg(a.d_delta + l);
-            if (l < a.num_det_prefix) Nv = L[l] * (delta * Nv) + Nv;
-            else Nv = Nv * (1.0 + L[l] * delta);
-            if (active) a.d_numeraire[(size_t)(l + 1) * P + p] = Nv;
-            // numeraire adjustment input: mean of N(T)^-1 * N(0) (:869-874)
-            const double inv = (1.0 / Nv) * 1.0;
-            if (a.d_inv_numeraire && active) a.d_inv_numeraire[(size_t)(l + 1) * P + p] = inv;
-            block_dd_partial(active ? inv : 0.0, a.d_inv_num_partials + ((size_t)blockIdx.x * N + l) * 2);
+    for (int c = 0; c < NMAX / 8; c++) {
+        double v[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            const int l = 8 * c + q;
+            v[q] = 0.0;
+            if (l < N) {
+                const double delta = __ldg(a.d_delta + l);
+                if (l < a.num_det_prefix) Nv = L[l] * (delta * Nv) + Nv;
+                else Nv = Nv * (1.0 + L[l] * delta);
+                if (active) {
+                    a.d_numeraire[(size_t)(l + 1) * P + p] = Nv;
+                    v[q] = rcp_newton(Nv);
+                    if (a.d_inv_numeraire) a.d_inv_numeraire[(size_t)(l + 1) * P + p] = v[q];
+                }
+            }
         }
+        const double sum = warp_sum8_transposed(v, lane);
+        const int idx = 8 * c + ((lane >> 2) & 7);
+        if ((lane & 3) == 0 && idx < N) wsum[warp][idx] = sum;
+    }
+    __syncthreads();
+    if ((int)threadIdx.x < N) {
+        dd acc{0.0, 0.0};
+#pragma unroll
+        for (int w = 0; w < kPathThreads / 32; w++) acc = dd_add_d(acc, wsum[w][threadIdx.x]);
+        double* o = a.d_inv_num_partials + ((size_t)blockIdx.x * N + threadIdx.x) * 2;
+        o[0] = acc.hi;
+        o[1] = acc.lo;
     }
 }
 

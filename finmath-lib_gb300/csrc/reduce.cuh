@@ -81,6 +81,33 @@ __device__ __forceinline__ void block_dd_partial(double x, double* out)
     }
 }
 
+// Warp sums of eight doubles per lane as a transposed reduction: three exchange levels each
+// halve the values a lane holds (lanes with the level's bit set keep the upper half, the
+// others the lower half, and add what the partner sends), then two plain levels -- 9 FP64
+// additions per warp for the eight sums instead of 40.  Returns, in the lanes with
+// (lane & 3) == 0, the sum of value index (lane >> 2) & 7; all lanes must call it.
+__device__ __forceinline__ double warp_sum8_transposed(double (&v)[8], int lane)
+{
+    const bool u16 = lane & 16, u8 = lane & 8, u4 = lane & 4;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const double keep = u16 ? v[q + 4] : v[q], send = u16 ? v[q] : v[q + 4];
+        v[q] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+    }
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+        const double keep = u8 ? v[q + 2] : v[q], send = u8 ? v[q] : v[q + 2];
+        v[q] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+    }
+    {
+        const double keep = u4 ? v[1] : v[0], send = u4 ? v[0] : v[1];
+        v[0] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+    }
+    v[0] += __shfl_xor_sync(0xffffffffu, v[0], 2);
+    v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
+    return v[0];
+}
+
 // Block sums of NV doubles per thread, for the mixed-precision form: plain FP64 within each
 // warp (lane order), compensated across the warps (warp order).  Thread i < NV writes the
 // (hi, lo) pair of sum i to out + 2 (i * stride).  All threads must call it.
