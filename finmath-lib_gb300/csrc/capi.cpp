@@ -6,6 +6,7 @@
 // reuse HBM instead of returning it to the CUDA driver.
 #include <algorithm>
 #include <atomic>
+#include <cstdlib>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -107,14 +108,40 @@ static int ensure_pool()
     return rc;
 }
 
+static std::atomic<int64_t> g_allocations{0};
+
+static int64_t injected_alloc_limit()
+{
+    static const int64_t limit = [] {
+        const char* e = std::getenv("LMM_FAULT_INJECT_ALLOC");
+        return (e && *e) ? (int64_t)std::atoll(e) : (int64_t)-1;
+    }();
+    return limit;
+}
+
+int device_alloc(void** p, size_t bytes, cudaStream_t s, const char* what)
+{
+    *p = nullptr;
+    const int64_t limit = injected_alloc_limit();
+    if (limit >= 0 && g_allocations.fetch_add(1) >= limit)
+        return fail(LMM_ERR_NOMEM, std::string("out of device memory in ") + what +
+                                       " (injected by LMM_FAULT_INJECT_ALLOC)");
+    const cudaError_t e = cudaMallocAsync(p, bytes, s);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return cuda_fail(e, what);
+    }
+    return LMM_OK;
+}
+
 template <typename T>
 static int dalloc(T** p, size_t count, cudaStream_t s)
 {
     *p = nullptr;
     if (count == 0) return LMM_OK;
     void* v = nullptr;
-    cudaError_t e = cudaMallocAsync(&v, count * sizeof(T), s);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaMallocAsync");
+    int rc = device_alloc(&v, count * sizeof(T), s, "cudaMallocAsync");
+    if (rc) return rc;
     *p = static_cast<T*>(v);
     return LMM_OK;
 }

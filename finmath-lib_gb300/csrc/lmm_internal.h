@@ -53,6 +53,11 @@ struct KernelTimer {
 bool timing_enabled();
 // host-to-device bytes copied by the library (every table and parameter upload)
 void count_h2d(size_t bytes);
+// Every device allocation of the library: cudaMallocAsync on stream s, failures mapped to
+// LMM_ERR_NOMEM / LMM_ERR_CUDA with a message.  With LMM_FAULT_INJECT_ALLOC=n in the
+// environment (read once), every allocation after the first n fails as an out-of-memory
+// would, without calling the allocator: the host-side fault injection the tests use.
+int device_alloc(void** p, size_t bytes, cudaStream_t s, const char* what);
 
 // ---------------------------------------------------------------- MT19937 (host side)
 constexpr int kMtN = 624;

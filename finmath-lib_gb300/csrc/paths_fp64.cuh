@@ -36,6 +36,7 @@
 #include "fp64math.cuh"
 #include "lmm_internal.h"
 #include "reduce.cuh"
+#include "unroll_range.cuh"
 
 namespace lmm {
 namespace {
@@ -59,13 +60,17 @@ __device__ __forceinline__ float rcp_approx_f32(float x)
     return r;
 }
 
-template <int NMAX, int FMAX, bool FUNCTIONAL>
+// EXACT: the model has exactly NMAX components, so the component loop carries no bound
+// checks; the loop enters its unrolled sequence at the first alive component through a jump
+// table (unroll_range.cuh), so the compiler sees one straight-line block per step and can
+// overlap the components' independent work (the os_j and the increments' dot products).
+template <int NMAX, int FMAX, bool FUNCTIONAL, bool EXACT>
 __global__ void __launch_bounds__(kPathThreads) paths_fp64_kernel(const PathLaunch a)
 {
     constexpr int FPD = fp64_df_pitch(FMAX);
     const int p = blockIdx.x * kPathThreads + threadIdx.x;
     const bool active = p < a.P;
-    const int N = a.N, F = a.F, P = a.P;
+    const int N = EXACT ? NMAX : a.N, F = a.F, P = a.P;
     const long long capbits = __double_as_longlong(a.libor_cap);  // +infinity when uncapped: never caps
     const double* dW = static_cast<const double*>(a.d_dw);
     double* states = static_cast<double*>(a.d_states);
@@ -115,9 +120,9 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp64_kernel(const PathLaun
             Gs[k] = 0.0f;
             if (k < F && active) df_split(dW[((size_t)i * F + k) * P + p], Gp[k], Gs[k]);
         }
-#pragma unroll
-        for (int j = 0; j < NMAX; j++) {
-            if (j < N && j >= first) {
+        for_up_from<NMAX>(first, [&](auto jc) {
+            constexpr int j = decltype(jc)::value;
+            if (EXACT || j < N) {
                 // the component's row: loadings (hi, lo), the drift term (variance * -0.5) * dt
                 // and 1/delta, each as a double-float pair
                 float r[FPD];
@@ -155,19 +160,24 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp64_kernel(const PathLaun
                 qe = fmaf(oe, dth, qe);
                 // Euler step (EulerSchemeFromProcessModel.java:235-255) with the drift of
                 // :1159 and :1183-1189: the increment d of the log state
-                float dp = r[2 * FMAX], ds = r[2 * FMAX + 1];
+                // two independent accumulators (even and odd factors) halve the dependency
+                // chain of the dot product; the rows are zero beyond F, so padded factors add 0
+                float dp = r[2 * FMAX], ds = r[2 * FMAX + 1], ep = 0.0f, es = 0.0f;
 #pragma unroll
                 for (int k = 0; k < FMAX; k++) {
-                    if (k < F) {
-                        df_dot_acc(Gp[k], Gs[k], qh, qe, r[k], r[FMAX + k]);
-                        df_dot_acc(dp, ds, Gp[k], Gs[k], r[k], r[FMAX + k]);
-                    }
+                    df_dot_acc(Gp[k], Gs[k], qh, qe, r[k], r[FMAX + k]);
+                    if (k & 1) df_dot_acc(ep, es, Gp[k], Gs[k], r[k], r[FMAX + k]);
+                    else df_dot_acc(dp, ds, Gp[k], Gs[k], r[k], r[FMAX + k]);
                 }
                 // exp(d) by the table method of exp_small (fp64math.cuh): k = rint(256 d) and
                 // the exact remainder dh - k/256 formed in FP32, the reduced argument and its
                 // degree-5 polynomial in FP64
                 float dh, dl;
-                two_sum(dp, ds, dh, dl);
+                {
+                    float x, q;
+                    two_sum(dp, ep, x, q);
+                    two_sum(x, (ds + es) + q, dh, dl);
+                }
                 double g;
                 if (fabsf(dh) <= 1.0f) {
                     const float t = fmaf(dh, (float)kExpTableHalf, 12582912.0f);  // 1.5 2^23 + rint(256 dh)
@@ -193,7 +203,7 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp64_kernel(const PathLaun
                     L[j] = cap_positive(e, capbits);
                 }
             }
-        }
+        });
         const int slot = __ldg(a.d_obs_slot + i + 1);
         if (slot >= 0 && active) {
 #pragma unroll
@@ -420,10 +430,12 @@ int launch_t(const PathLaunch& a, cudaStream_t s, int blocks)
 {
     if (a.scheme > 1 || a.measure != 0 || a.state_space != 0)
         paths_fp64_general_kernel<NMAX, FMAX><<<blocks, kPathThreads, 0, s>>>(a);
+    else if (a.scheme == 1 && a.N == NMAX)
+        paths_fp64_kernel<NMAX, FMAX, true, true><<<blocks, kPathThreads, 0, s>>>(a);
     else if (a.scheme == 1)
-        paths_fp64_kernel<NMAX, FMAX, true><<<blocks, kPathThreads, 0, s>>>(a);
+        paths_fp64_kernel<NMAX, FMAX, true, false><<<blocks, kPathThreads, 0, s>>>(a);
     else
-        paths_fp64_kernel<NMAX, FMAX, false><<<blocks, kPathThreads, 0, s>>>(a);
+        paths_fp64_kernel<NMAX, FMAX, false, false><<<blocks, kPathThreads, 0, s>>>(a);
     LMM_CUDA(cudaGetLastError());
     return LMM_OK;
 }

@@ -277,10 +277,11 @@ int rv_alloc(double time, int64_t n, lmm_rv** out)
     r->time = time;
     r->n = n;
     if (n > 0) {
-        const cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&r->d), sizeof(double) * (size_t)n, rv_stream());
-        if (e != cudaSuccess) {
+        const int rc = device_alloc(reinterpret_cast<void**>(&r->d), sizeof(double) * (size_t)n, rv_stream(),
+                                    "cudaMallocAsync (random variable)");
+        if (rc) {
             delete r;
-            return cuda_fail(e, "cudaMallocAsync (random variable)");
+            return rc;
         }
     }
     *out = r;
@@ -486,7 +487,9 @@ static int reduce_sum(const lmm_rv* x, bool centered, double center, double* out
 {
     const int blocks = (int)std::min<int64_t>((x->n + kRvThreads - 1) / kRvThreads, 1024);
     double* scratch = nullptr;
-    LMM_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&scratch), sizeof(double) * (2 * (size_t)blocks + 1), rv_stream()));
+    int arc = device_alloc(reinterpret_cast<void**>(&scratch), sizeof(double) * (2 * (size_t)blocks + 1), rv_stream(),
+                           "cudaMallocAsync (reduction scratch)");
+    if (arc) return arc;
     rv_sum_kernel<<<blocks, kRvThreads, 0, rv_stream()>>>(x->d, x->n, centered ? 1 : 0, center, scratch);
     rv_finish_kernel<<<1, kRvThreads, 0, rv_stream()>>>(scratch, blocks, x->n, scratch + 2 * blocks);
     cudaError_t e = cudaGetLastError();
@@ -542,7 +545,9 @@ int lmm_rv_min_max(const lmm_rv* x, double* out_min, double* out_max)
     }
     const int blocks = (int)std::min<int64_t>((x->n + kRvThreads - 1) / kRvThreads, 1024);
     double* scratch = nullptr;
-    LMM_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&scratch), sizeof(double) * 2 * (size_t)blocks, rv_stream()));
+    int arc = device_alloc(reinterpret_cast<void**>(&scratch), sizeof(double) * 2 * (size_t)blocks, rv_stream(),
+                           "cudaMallocAsync (min/max scratch)");
+    if (arc) return arc;
     rv_minmax_kernel<<<blocks, kRvThreads, 0, rv_stream()>>>(x->d, x->n, scratch);
     std::vector<double> h(2 * (size_t)blocks);
     cudaError_t e = cudaGetLastError();

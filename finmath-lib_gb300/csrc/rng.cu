@@ -612,7 +612,9 @@ int launch_mt_generate(const RngLaunch& a, cudaStream_t s, int* num_launches)
     {
         KernelTimer kt(K_MT_JUMP_GENERATE, s, 2);
         uint32_t* states = nullptr;  // [chunks][624] chunk start states
-        LMM_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&states), sizeof(uint32_t) * kMtN * (size_t)a.plan->chunks, s));
+        const int arc = device_alloc(reinterpret_cast<void**>(&states), sizeof(uint32_t) * kMtN * (size_t)a.plan->chunks, s,
+                                     "cudaMallocAsync (generator chunk states)");
+        if (arc) return arc;
         mt_jump_kernel<<<(unsigned)a.plan->chunks, kRngThreads, (size_t)kJumpWindow * 4, s>>>(prm, states);
         mt_generate_kernel<<<(unsigned)a.plan->chunks, kRngThreads, (size_t)a.plan->smem_bytes, s>>>(prm, states);
         const cudaError_t e = cudaGetLastError();
