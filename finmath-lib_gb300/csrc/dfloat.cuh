@@ -117,12 +117,28 @@ __device__ __forceinline__ void df_dot_acc(float& p, float& s, float ah, float a
     s = s + (q + r);
 }
 
+// binary64 -> binary32 for values whose magnitude lies in FP32's normal range or below it
+// (the forward rates, increments and their remainders): round to nearest even in integer
+// operations only -- magnitudes below FP32's normal range become a signed zero, and nothing
+// falls back to the hardware conversion, whose FP64-pipe instruction a compiler would
+// otherwise execute predicated on every call.  Not for magnitudes of 2^128 and above.
+__device__ __forceinline__ float f64_to_f32_small(double x)
+{
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
+    const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);
+    const unsigned rest = lo & 0x1fffffffu;
+    unsigned bits = (hi & 0x80000000u) | ((unsigned)(e > 0 ? e : 0) << 23) | m;
+    if (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) bits += 1u;
+    return __uint_as_float(e > 0 ? bits : (hi & 0x80000000u));
+}
+
 // a double as hi + lo floats (hi = x rounded to FP32 in integer operations, lo = the rounded
-// remainder: one FP64 subtraction, which is exact), about 2^-48 relative
+// remainder: one FP64 subtraction, which is exact), about 2^-48 relative; |x| < 2^128
 __device__ __forceinline__ void df_split(double x, float& hi, float& lo)
 {
-    hi = f64_to_f32_int(x);
-    lo = f64_to_f32_int(x - f32_to_f64_int(hi));
+    hi = f64_to_f32_small(x);
+    lo = f64_to_f32_small(x - f32_to_f64_int(hi));
 }
 
 __device__ __forceinline__ double df_to_double(float hi, float lo) { return f32_to_f64_int(hi) + f32_to_f64_int(lo); }

@@ -60,14 +60,38 @@ __device__ __forceinline__ float rcp_approx_f32(float x)
     return r;
 }
 
+// The forward vector of a path: in registers, or (SMEM) in the thread's own column of a
+// shared-memory array [NMAX][threads], which frees NMAX * 2 registers a thread so that more
+// warps share an SM and hide the latency of the double-float chains.
+template <int NMAX, bool SMEM>
+struct PathState;
+template <int NMAX>
+struct PathState<NMAX, false> {
+    double v[NMAX];
+    __device__ __forceinline__ double& operator[](int j) { return v[j]; }
+};
+template <int NMAX>
+struct PathState<NMAX, true> {
+    double* col;
+    __device__ __forceinline__ double& operator[](int j) { return col[j * kPathThreads]; }
+};
+
+// the shared-memory state for up to 40 components (40 KB a block, five blocks an SM)
+__host__ __device__ constexpr bool fp64_state_in_smem(int nmax, bool functional) { return functional && nmax <= 40; }
+__host__ __device__ constexpr int fp64_min_blocks(int nmax, bool functional)
+{
+    return fp64_state_in_smem(nmax, functional) ? 5 : 1;
+}
+
 // EXACT: the model has exactly NMAX components, so the component loop carries no bound
 // checks; the loop enters its unrolled sequence at the first alive component through a jump
 // table (unroll_range.cuh), so the compiler sees one straight-line block per step and can
 // overlap the components' independent work (the os_j and the increments' dot products).
 template <int NMAX, int FMAX, bool FUNCTIONAL, bool EXACT>
-__global__ void __launch_bounds__(kPathThreads) paths_fp64_kernel(const PathLaunch a)
+__global__ void __launch_bounds__(kPathThreads, fp64_min_blocks(NMAX, FUNCTIONAL)) paths_fp64_kernel(const PathLaunch a)
 {
     constexpr int FPD = fp64_df_pitch(FMAX);
+    constexpr bool SMEM = fp64_state_in_smem(NMAX, FUNCTIONAL);
     const int p = blockIdx.x * kPathThreads + threadIdx.x;
     const bool active = p < a.P;
     const int N = EXACT ? NMAX : a.N, F = a.F, P = a.P;
@@ -76,7 +100,9 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp64_kernel(const PathLaun
     double* states = static_cast<double*>(a.d_states);
 
     const double* etab = a.d_exp_tab;
-    double L[NMAX];
+    __shared__ double state_smem[SMEM ? NMAX : 1][kPathThreads];
+    PathState<NMAX, SMEM> L;
+    if constexpr (SMEM) L.col = &state_smem[0][threadIdx.x];
     double E[FUNCTIONAL ? 1 : NMAX];  // EULER: exp of the uncapped log state Y
 #pragma unroll
     for (int j = 0; j < NMAX; j++) {
