@@ -94,6 +94,17 @@ SIGNATURES = {
     "lmm_process_get_numeraire_unadjusted_rv": (ctypes.c_int, [_VP, ctypes.c_double, ctypes.POINTER(_VP)]),
     "lmm_rv_create_constant": (ctypes.c_int, [ctypes.c_double, ctypes.c_double, ctypes.POINTER(_VP)]),
     "lmm_rv_create": (ctypes.c_int, [ctypes.c_double, _D, ctypes.c_int64, ctypes.POINTER(_VP)]),
+    "lmm_rv_create_float": (ctypes.c_int, [ctypes.c_double, ctypes.POINTER(ctypes.c_float), ctypes.c_int64,
+                                           ctypes.POINTER(_VP)]),
+    "lmm_rv_create_constant_float": (ctypes.c_int, [ctypes.c_double, ctypes.c_double, ctypes.POINTER(_VP)]),
+    "lmm_rv_to_float": (ctypes.c_int, [_VP, ctypes.POINTER(_VP)]),
+    "lmm_rv_is_float": (ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_int)]),
+    "lmm_rv_get_float": (ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_float)]),
+    "lmm_rv_quantile": (ctypes.c_int, [_VP, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]),
+    "lmm_rv_quantile_expectation": (ctypes.c_int, [_VP, ctypes.c_double, ctypes.c_double,
+                                                   ctypes.POINTER(ctypes.c_double)]),
+    "lmm_rv_histogram": (ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_double), ctypes.c_int,
+                                        ctypes.POINTER(ctypes.c_double)]),
     "lmm_rv_destroy": (ctypes.c_int, [_VP]),
     "lmm_rv_stream": (ctypes.c_int, [ctypes.POINTER(_VP)]),
     "lmm_rv_describe": (ctypes.c_int, [_VP, _D, _I64, ctypes.POINTER(ctypes.c_int), _D]),

@@ -43,6 +43,40 @@ class RandomVariableGPU:
                                    ctypes.byref(h)), "createRandomVariable")
         return cls(h)
 
+    @classmethod
+    def from_float_array(cls, time: float, values) -> "RandomVariableGPU":
+        """RandomVariableFromFloatArray(time, float[]): FP32 realizations of the float class."""
+        a = np.ascontiguousarray(values, dtype=np.float32)
+        h = ctypes.c_void_p()
+        check(load().lmm_rv_create_float(float(time), a.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), a.size,
+                                         ctypes.byref(h)), "createRandomVariable")
+        return cls(h)
+
+    @classmethod
+    def constant_float(cls, time: float, value: float) -> "RandomVariableGPU":
+        """RandomVariableFromFloatArray(time, value): a deterministic value of the float class."""
+        h = ctypes.c_void_p()
+        check(load().lmm_rv_create_constant_float(float(time), float(value), ctypes.byref(h)), "createRandomVariable")
+        return cls(h)
+
+    def toFloat(self) -> "RandomVariableGPU":
+        """RandomVariableFromFloatArray(RandomVariable): the realizations rounded to FP32."""
+        h = ctypes.c_void_p()
+        check(self._L.lmm_rv_to_float(self._h, ctypes.byref(h)), "RandomVariableFromFloatArray")
+        return RandomVariableGPU(h)
+
+    def isFloat(self) -> bool:
+        out = ctypes.c_int()
+        check(self._L.lmm_rv_is_float(self._h, ctypes.byref(out)), "isFloat")
+        return bool(out.value)
+
+    def getFloatRealizations(self) -> np.ndarray:
+        t, n, det, v = self._describe()
+        out = np.empty(n, dtype=np.float32)
+        check(self._L.lmm_rv_get_float(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_float))),
+              "getRealizations")
+        return out
+
     def close(self):
         if getattr(self, "_h", None):
             self._L.lmm_rv_destroy(self._h)
@@ -124,13 +158,41 @@ class RandomVariableGPU:
         (RandomVariableTest.java:233-272 accept UnsupportedOperationException)."""
         raise NotImplementedError("apply(operator) is not supported on device random variables")
 
-    def getQuantile(self, quantile, *args):
-        """getQuantile / getQuantileExpectation / getHistogram need a device sort; not part of
-        this layer."""
-        raise NotImplementedError("quantiles are not supported on device random variables")
+    def getQuantile(self, quantile, probabilities=None) -> float:
+        """getQuantile (RandomVariableFromDoubleArray.java:446-460): the sorted realizations'
+        element at (int) Math.round((n + 1) quantile - 1), clamped; sorted on the device.
+        The weighted form is not implemented in the reference either (:463-472)."""
+        if probabilities is not None:
+            raise NotImplementedError("Method not implemented.")
+        return self._reduce(lambda h, out: self._L.lmm_rv_quantile(h, float(quantile), out))
 
-    getQuantileExpectation = getQuantile
-    getHistogram = getQuantile
+    def getQuantileExpectation(self, quantileStart, quantileEnd) -> float:
+        """getQuantileExpectation (:475-499): the mean of the sorted realizations between the
+        two quantiles' indices."""
+        return self._reduce(lambda h, out: self._L.lmm_rv_quantile_expectation(h, float(quantileStart),
+                                                                                float(quantileEnd), out))
+
+    def getHistogram(self, intervalPoints, standardDeviations=None):
+        """getHistogram(double[] intervalPoints) (:502-553): the share of realizations in each
+        interval, numberOfPoints + 1 entries; getHistogram(int numberOfPoints, double
+        standardDeviations) (:556-575): interval points spread standardDeviations standard
+        deviations around the mean, returned with their anchor points as [anchors, histogram]."""
+        if standardDeviations is not None:
+            numberOfPoints = int(intervalPoints)
+            center, radius = self.getAverage(), standardDeviations * self.getStandardDeviation()
+            stepSize = (numberOfPoints - 1) / 2.0
+            points, anchors = np.empty(numberOfPoints), np.empty(numberOfPoints + 1)
+            for i in range(numberOfPoints):
+                alpha = (-float(numberOfPoints - 1) / 2.0 + i) / stepSize
+                points[i] = center + alpha * radius
+                anchors[i] = center + alpha * radius - radius / (2 * stepSize)
+            anchors[numberOfPoints] = center + 1 * radius + radius / (2 * stepSize)
+            return [anchors, self.getHistogram(points)]
+        p = np.ascontiguousarray(intervalPoints, dtype=np.float64)
+        out = np.empty(p.size + 1)
+        dp = ctypes.POINTER(ctypes.c_double)
+        check(self._L.lmm_rv_histogram(self._h, p.ctypes.data_as(dp), p.size, out.ctypes.data_as(dp)), "getHistogram")
+        return out
 
     def getConditionalExpectation(self, conditionalExpectationOperator):
         """RandomVariableFromDoubleArray.getConditionalExpectation: the estimator's estimate of this."""
@@ -207,15 +269,23 @@ def _as_rv(x) -> RandomVariableGPU:
 
 
 class RandomVariableGPUFactory:
-    """RandomVariableFactory.createRandomVariable (RandomVariableFactory.java:56-94) on the GPU."""
+    """RandomVariableFactory.createRandomVariable (RandomVariableFactory.java:56-94) on the GPU;
+    like RandomVariableFromArrayFactory(isUseDoublePrecisionFloatingPointImplementation)
+    (RandomVariableFromArrayFactory.java:37-60) it makes double-class random variables, or
+    float-class ones (RandomVariableFromFloatArray) when that flag is False."""
+
+    def __init__(self, isUseDoublePrecisionFloatingPointImplementation: bool = True):
+        self.isUseDoublePrecisionFloatingPointImplementation = bool(isUseDoublePrecisionFloatingPointImplementation)
 
     def createRandomVariable(self, *args) -> RandomVariableGPU:
         if len(args) == 1:  # AbstractRandomVariableFactory.java:22-24: measurable at -infinity
-            return RandomVariableGPU.constant(float("-inf"), args[0])
-        time, value = args
+            time, value = float("-inf"), args[0]
+        else:
+            time, value = args
+        double = self.isUseDoublePrecisionFloatingPointImplementation
         if np.ndim(value) == 0:
-            return RandomVariableGPU.constant(time, value)
-        return RandomVariableGPU.from_array(time, value)
+            return RandomVariableGPU.constant(time, value) if double else RandomVariableGPU.constant_float(time, value)
+        return RandomVariableGPU.from_array(time, value) if double else RandomVariableGPU.from_float_array(time, value)
 
 
 class MonteCarloConditionalExpectationRegression:

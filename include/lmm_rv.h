@@ -81,6 +81,32 @@ int lmm_rv_apply(const lmm_rv* x, int op, const lmm_rv* y, lmm_rv** out);
 /* the three-argument operations LMM_RV_ACCRUE .. LMM_RV_SUB_RATIO */
 int lmm_rv_apply3(const lmm_rv* x, int op, const lmm_rv* a, const lmm_rv* b, double c, lmm_rv** out);
 
+/* The float class, RandomVariableFromFloatArray (montecarlo/RandomVariableFromFloatArray.java):
+ * FP32 realizations; + - * / in FP32 arithmetic, square root and the transcendental functions
+ * in FP64 rounded to FP32, the deterministic forms in FP64, as the reference computes them
+ * (:755-1486).  The receiver of an operation decides the class of its result; a
+ * deterministic double-class receiver (a Scalar, type priority 0) hands the operation to a
+ * float-class operand.  Reductions read the floats as doubles (:311-430).
+ * lmm_rv_create_float: n FP32 realizations; lmm_rv_create_constant_float: a deterministic
+ * value of the float class; lmm_rv_to_float: RandomVariableFromFloatArray(RandomVariable),
+ * the realizations rounded to FP32 (:38-45, :214-220); lmm_rv_is_float: 1 for the float
+ * class; lmm_rv_get_float: the FP32 realizations (lmm_rv_get widens them, :222-228). */
+int lmm_rv_create_float(double time, const float* host, int64_t n, lmm_rv** out);
+int lmm_rv_create_constant_float(double time, double value, lmm_rv** out);
+int lmm_rv_to_float(const lmm_rv* x, lmm_rv** out);
+int lmm_rv_is_float(const lmm_rv* x, int* out);
+int lmm_rv_get_float(const lmm_rv* x, float* out_host);
+
+/* getQuantile, getQuantileExpectation and getHistogram(intervalPoints)
+ * (stochastic/RandomVariable.java:219-269; RandomVariableFromDoubleArray.java:446-553 and the
+ * float class's :470-520): the realizations sorted on the device as java.util.Arrays.sort
+ * orders them, the element at (int) Math.round((n + 1) q - 1) clamped to [0, n - 1], the
+ * plain mean of the sorted range between two such indices, and the share of realizations in
+ * each interval (out has num_points + 1 entries; the reference's deterministic case kept). */
+int lmm_rv_quantile(const lmm_rv* x, double quantile, double* out);
+int lmm_rv_quantile_expectation(const lmm_rv* x, double quantile_start, double quantile_end, double* out);
+int lmm_rv_histogram(const lmm_rv* x, const double* interval_points, int num_points, double* out);
+
 /* getAverage, getVariance, getStandardError, getMin / getMax (:257-283) */
 int lmm_rv_average(const lmm_rv* x, double* out);
 int lmm_rv_variance(const lmm_rv* x, double* out);

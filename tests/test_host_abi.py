@@ -203,9 +203,23 @@ def test_swaption_constructors_follow_the_reference_overloads():
 
 
 def test_unsupported_random_variable_operations_raise():
-    # apply(operator) and quantiles: UnsupportedOperationException in the reference's terms
+    # apply(operator) and the weighted quantile: UnsupportedOperationException / "Method not
+    # implemented." in the reference's terms
     from finmath_gb300.randomvariable import RandomVariableGPU as RV
     r = RV.constant(0.0, 1.0)
-    for call in (lambda: r.apply(abs), lambda: r.getQuantile(0.5), lambda: r.getHistogram([0.0])):
+    for call in (lambda: r.apply(abs), lambda: r.getQuantile(0.5, r)):
         with pytest.raises(NotImplementedError):
             call()
+
+
+def test_deterministic_quantiles_and_histogram():
+    # RandomVariableFromDoubleArray.java:446-553 for a deterministic value: the value itself,
+    # and the reference's histogram of a 1 at the first interval point the value exceeds and a
+    # 1 in the last entry (no device work)
+    from finmath_gb300.randomvariable import RandomVariableGPU as RV
+    r = RV.constant(0.0, 1.0)
+    assert r.getQuantile(0.3) == 1.0 and r.getQuantileExpectation(0.9, 0.1) == 1.0
+    assert list(r.getHistogram([2.0, 0.5, 0.0])) == [0.0, 1.0, 0.0, 1.0]
+    assert list(r.getHistogram([])) == [1.0]
+    f = RV.constant_float(0.0, 2.5)
+    assert f.isFloat() and f.isDeterministic() and f.getQuantile(0.5) == 2.5
