@@ -461,6 +461,7 @@ struct SeedParams {
     double* seeds;                 // [N][P]: pass 1 the payoff part, pass 2 final (divided by P)
     double* nb;                    // [N+1][P] adjoints of the adjusted numeraires (pass 1 -> 2)
     double* value_partials;        // [blocks] (pass 1): sum of the frozen-decision values
+    const double* omega;           // nullptr, or [nper][P]: the cash flows' AAD weights (FP64 form)
 };
 
 constexpr int kSeedThreads = 256;
@@ -502,17 +503,21 @@ __global__ void __launch_bounds__(kSeedThreads) seed_kernel(const SeedParams a)
             // receives the periods before its exercise date
             const bool paid = active && (a.callable ? (c.fixing >= tau) : (c.fixing < tau));
             const int l = c.pay_num_index;
-            double cf = 0.0;
-            if (paid) {
+            // the cash flow's adjoint weight: the frozen decision, or the AAD sweep's weight
+            const double wgt = a.omega ? (active ? a.omega[(size_t)q * P + p] : 0.0) : (paid ? 1.0 : 0.0);
+            double cf = 0.0, wcf = 0.0;
+            if (paid || wgt != 0.0) {
                 const double L = st<TS>(a, c.libor_slot, c.libor_index, p);
                 const double invN = a.inv_numeraire[(size_t)l * P + p] * r_adj[l];
                 const double A = ((L - c.strike) * c.period_length) * c.notional;
-                cf = A * invN;
-                a.seeds[(size_t)c.libor_index * P + p] += (c.period_length * c.notional) * invN;
-                if (!a.det[l]) a.nb[(size_t)l * P + p] -= cf * invN;
+                cf = paid ? A * invN : 0.0;
+                wcf = a.omega ? wgt * (A * invN) : cf;
+                a.seeds[(size_t)c.libor_index * P + p] += a.omega ? wgt * ((c.period_length * c.notional) * invN)
+                                                                  : (c.period_length * c.notional) * invN;
+                if (!a.det[l]) a.nb[(size_t)l * P + p] -= wcf * invN;
             }
             x += cf;
-            double v = cf;
+            double v = wcf;
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
             if (lane == 0) wsum[warp][l] += v;
@@ -869,6 +874,8 @@ int launch_adjoint(const AdjointLaunch& L, cudaStream_t s)
     sp.value_partials = L.d_value_partials;
     sp.nb = L.d_nb;
     sp.inv_numeraire = L.d_inv_numeraire;
+    sp.omega = L.d_omega;
+    if (L.d_omega && L.fp32) return fail(LMM_ERR_INVALID, "the cash-flow weights of the AAD sweep are an FP64-form input");
     if (!L.d_inv_numeraire || !L.d_nb) return fail(LMM_ERR_STATE, "adjoint: the simulation kept no reciprocal numeraire");
     if (L.nper > 0 && L.N > 64) return fail(LMM_ERR_INVALID, "adjoint: at most 64 forward rates");
     const int sb = (L.P + kSeedThreads - 1) / kSeedThreads;

@@ -249,6 +249,9 @@ struct lmm_process {
     unsigned char *d_adj_seg = nullptr, *d_adj_ybar = nullptr;  // stride > 1 segment buffers
     double* d_adj_nb = nullptr;                                 // seed scratch [N+1][P]
     size_t adj_seg_bytes = 0, adj_ybar_bytes = 0;
+    double* d_dd_rec = nullptr;      // DISCRETE_DELTA: the forward valuation's triggers and Y - Z
+    double* d_dd_scratch = nullptr;  // DISCRETE_DELTA: weights, sweep state, moments, coefficients
+    size_t dd_rec_doubles = 0, dd_scratch_doubles = 0;
 };
 
 extern "C" {
@@ -769,6 +772,8 @@ int lmm_process_destroy(lmm_process* pr)
     dfree(pr->d_dt, s);
     dfree(pr->d_delta, s);
     dfree(pr->d_exp_tab, s);
+    dfree(pr->d_dd_rec, s);
+    dfree(pr->d_dd_scratch, s);
     dfree(pr->d_init_state, s);
     dfree(pr->d_rows_df, s);
     dfree(pr->d_dt_df, s);
@@ -968,7 +973,7 @@ static int build_bermudan(lmm_process* pr, const lmm_bermudan_desc* d, BermudanL
 }
 
 static int bermudan_run(lmm_process* pr, const lmm_bermudan_desc* d, double* value, double* error, double* values_host,
-                        BermudanLaunch* launch_out)
+                        BermudanLaunch* launch_out, double* d_rec = nullptr)
 {
     if (!pr || !d || !value) return fail(LMM_ERR_INVALID, "null argument");
     BermudanLaunch a;
@@ -1031,6 +1036,7 @@ static int bermudan_run(lmm_process* pr, const lmm_bermudan_desc* d, double* val
     sc.d_tenor_delta = pr->d_tenor_delta;
     sc.d_period_index = pr->d_period_index;
     sc.d_period_length = pr->d_period_length;
+    sc.d_rec = d_rec;
     ProductView v = product_view(pr);
     rc = launch_bermudan(v, a, sc, s, nullptr);
     if (rc) return rc;
@@ -1105,15 +1111,39 @@ extern "C" {
 int lmm_bermudan_get_gradient(lmm_process* pr, const lmm_bermudan_desc* d, int stride, int freeze, double* value,
                               double* error, double* deltas, double* vegas)
 {
+    return lmm_bermudan_get_gradient_aad(pr, d, stride, freeze, LMM_DIRAC_ZERO, 0.0, value, error, deltas, vegas);
+}
+
+int lmm_bermudan_get_gradient_aad(lmm_process* pr, const lmm_bermudan_desc* d, int stride, int freeze, int dirac_method,
+                                  double dirac_width, double* value, double* error, double* deltas, double* vegas)
+{
     if (!pr || !d || !value || !deltas || !vegas) return fail(LMM_ERR_INVALID, "null argument");
     if (stride < 1 || stride > 16) return fail(LMM_ERR_INVALID, "checkpoint stride must be in [1, 16]");
+    if (dirac_method != LMM_DIRAC_ZERO && dirac_method != LMM_DIRAC_DISCRETE_DELTA)
+        return fail(LMM_ERR_INVALID, "diracDeltaApproximationMethod must be ZERO or DISCRETE_DELTA");
+    const bool dd = dirac_method == LMM_DIRAC_DISCRETE_DELTA;
+    if (dd && pr->precision != LMM_PRECISION_FP64)
+        return fail(LMM_ERR_INVALID, "the DISCRETE_DELTA sweep runs on FP64 processes");
+    if (dd && !(dirac_width >= 0.0)) return fail(LMM_ERR_INVALID, "the Dirac delta width must be >= 0");
     if (pr->N > 40 || pr->F > 10) return fail(LMM_ERR_INVALID, "the adjoint supports at most 40 forward rates and 10 factors");
     if (pr->measure != LMM_MEASURE_SPOT || pr->state_space != LMM_STATE_SPACE_LOGNORMAL || pr->scheme > LMM_SCHEME_EULER_FUNCTIONAL)
         return fail(LMM_ERR_INVALID, "the adjoint takes the SPOT measure, LOGNORMAL state space and Euler schemes");
     if (pr->obs_slot[pr->T] < 0) return fail(LMM_ERR_STATE, "the adjoint needs the last simulation time observed");
     pr->want_ckpt = stride;
     BermudanLaunch bl;
-    int rc = bermudan_run(pr, d, value, error, nullptr, &bl);
+    int rc = 0;
+    int ne_dd = 0;
+    if (dd) {
+        // the forward valuation records each date's trigger and Y - Z for the sweep
+        for (int q = 0; q < d->num_periods; q++) ne_dd += d->is_exercise_date[q] ? 1 : 0;
+        const size_t need = (size_t)std::max(ne_dd, 1) * 2 * (size_t)pr->P;
+        if (need > pr->dd_rec_doubles) {
+            dfree(pr->d_dd_rec, pr->stream);
+            if ((rc = dalloc(&pr->d_dd_rec, need, pr->stream))) return rc;
+            pr->dd_rec_doubles = need;
+        }
+    }
+    rc = bermudan_run(pr, d, value, error, nullptr, &bl, dd ? pr->d_dd_rec : nullptr);
     if (rc) return rc;
     if ((rc = adjoint_tables(pr))) return rc;
     cudaStream_t s = pr->stream;
@@ -1198,6 +1228,35 @@ int lmm_bermudan_get_gradient(lmm_process* pr, const lmm_bermudan_desc* d, int s
     L.d_delta_partials = pr->d_delta_partials;
     L.d_vegas = pr->d_vegas;
     L.d_deltas = pr->d_deltas;
+    if (dd) {
+        // the cash flows' weights from the AAD sweep over the backward induction
+        const size_t om = (size_t)bl.nper * pr->P, mom = (size_t)std::max(ne_dd, 1) * 64 * 2;
+        const size_t need = om + 2 * (size_t)pr->P + mom + 3 * 64 + 64 * 6 + (size_t)bermudan_blocks(pr->P) * 12 + 2;
+        if (need > pr->dd_scratch_doubles) {
+            dfree(pr->d_dd_scratch, s);
+            if ((rc = dalloc(&pr->d_dd_scratch, need, s))) return rc;
+            pr->dd_scratch_doubles = need;
+        }
+        double* z0 = pr->d_dd_scratch;
+        BermudanDdScratch ds;
+        ds.d_rec = pr->d_dd_rec;
+        ds.d_basis = pr->d_basis;
+        ds.d_svd = pr->d_svd;
+        ds.d_omega = z0;
+        ds.d_vbar = z0 + om;
+        ds.d_ubar = ds.d_vbar + pr->P;
+        ds.d_moments = ds.d_ubar + pr->P;
+        ds.d_mean = ds.d_moments + mom;
+        ds.d_eps = ds.d_mean + 64;
+        ds.d_betap = ds.d_eps + 64;
+        ds.d_partials = ds.d_betap + 64 * 6 + 64;
+        const size_t pbytes = sizeof(double) * ((size_t)bermudan_blocks(pr->P) * 12 + 2);
+        LMM_CUDA(cudaMemsetAsync(ds.d_partials, 0, pbytes, s));  // the completion counter starts at zero
+        // the value's adjoint seed: the numeraire at time 0 (exactly 1 under SPOT)
+        const double num0 = 1.0;
+        if ((rc = launch_bermudan_dd_weights(bl, ds, pr->P, num0, dirac_width, s))) return rc;
+        L.d_omega = ds.d_omega;
+    }
     if ((rc = launch_adjoint(L, s))) return rc;
     LMM_CUDA(cudaMemcpyAsync(deltas, pr->d_deltas, sizeof(double) * N, cudaMemcpyDeviceToHost, s));
     LMM_CUDA(cudaMemcpyAsync(vegas, pr->d_vegas, sizeof(double) * (size_t)T * N, cudaMemcpyDeviceToHost, s));

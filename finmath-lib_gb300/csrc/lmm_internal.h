@@ -231,7 +231,24 @@ struct BermudanScratch {
     const double* d_period_length;  // [nper]
     int tables_on_device = 0;       // d_per / d_ex_period already hold this product's tables
     int gram_blocks = 0;            // Gram blocks per exercise date (0: automatic)
+    double* d_rec = nullptr;        // FP64 form, optional: [2][ne][P] trigger X and Y - Z per date
 };
+// scratch of the discrete-delta AAD weights of a Bermudan's cash flows (launch_bermudan_dd_weights)
+struct BermudanDdScratch {
+    const double* d_rec;      // [2][ne][P] from the forward valuation
+    const double* d_basis;    // [ne][5][P]
+    const double* d_svd;      // [ne][80]
+    double* d_moments;        // [ne][64][2]
+    double* d_mean;           // [ne]
+    double* d_eps;            // [ne]
+    double* d_betap;          // [ne][6]
+    double* d_vbar;           // [P]
+    double* d_ubar;           // [P]
+    double* d_omega;          // [nper][P] the weights
+    double* d_partials;       // [blocks][6][2] + completion counter (zero on entry)
+};
+int launch_bermudan_dd_weights(const BermudanLaunch& a, const BermudanDdScratch& sc, int P, double num0, double width,
+                               cudaStream_t s);
 int reduce_mean_var_device(const double* d_values, int P, double* d_scratch, double* d_out2, cudaStream_t s);
 int launch_timestamp(unsigned long long* d_out, cudaStream_t s);
 int bermudan_blocks(int P);
@@ -263,6 +280,7 @@ struct AdjointLaunch {
     double *d_abar, *d_abar_partials, *d_seeds, *d_value_partials, *d_value_out;
     double* d_nb;                  // [N+1][P] adjoints of the adjusted numeraires (scratch)
     double *d_vega_partials, *d_delta_partials, *d_vegas, *d_deltas;
+    const double* d_omega;         // nullptr, or [nper][P] the cash flows' AAD weights (FP64 form)
 };
 int adjoint_blocks(int P, int threads, int fp32);
 // scratch of one adjoint evaluation: per-warp partial rows and the segment buffers of stride > 1

@@ -507,6 +507,8 @@ struct BermStepParams {
     const double* svd_cur;     // SVD factors of the date cur_ex (when it regresses)
     double* beta_cur;          // its coefficients, written by the launch's last block
     int init;
+    double* rec;               // nullptr, or [2][ne][P]: per exercise date the trigger X and Y - Z
+                               // (continuation minus underlying) the choice is made on
 };
 
 // The last block of a step launch to finish reduces every block's X^T y partials (in block
@@ -562,6 +564,10 @@ __global__ void __launch_bounds__(kProdThreads) bermudan_step_kernel(const BermS
 #pragma unroll
             for (int i = 1; i < 6; i++) ce = ce + bprev[(size_t)(i - 1) * sh.P + p] * beta[i];
             const bool cont = ce >= 0.0;
+            if (a.rec) {
+                a.rec[(size_t)a.pending_ex * sh.P + p] = ce;
+                a.rec[((size_t)sh.ne + a.pending_ex) * sh.P + p] = v - u;
+            }
             v = cont ? v : u;
             if (!cont) a.ex[p] = a.pending_fixing;
         }
@@ -883,6 +889,7 @@ int launch_bermudan(const ProductView& v, const BermudanLaunch& a, const Bermuda
     prm.under = sc.d_under;
     prm.ex = sc.d_ex;
     prm.partials = sc.d_partials;
+    prm.rec = v.state_fp32 ? nullptr : sc.d_rec;
     int pending = -1;  // exercise index whose choose is pending
     for (int per = a.nper - 1; per >= -1; per--) {
         prm.cur = per;
@@ -901,6 +908,185 @@ int launch_bermudan(const ProductView& v, const BermudanLaunch& a, const Bermuda
         if (launches) (*launches)++;
         pending = -1;
         if (per >= 0 && prm.cur_ex >= 0) pending = prm.cur_ex;  // its coefficients come from the step's last block
+    }
+    return LMM_OK;
+}
+
+// ------------------------------------------------------------------ AAD weights of the cash flows
+// The reverse sweep that finmath-lib's RandomVariableDifferentiableAAD runs over
+// BermudanSwaption.getValues (BermudanSwaption.java:91-157) with
+// diracDeltaApproximationMethod DISCRETE_DELTA (RandomVariableDifferentiableAAD.java:409-429):
+// per path, the adjoint weight omega[q][p] of each period's discounted cash flow.  The choice
+// values = X.choose(Y, Z) passes its adjoint to Y where X >= 0 and to Z where X < 0, and to
+// the trigger X the term (Y - Z) 1{-eps/2 <= X < eps/2} / eps, eps = width * stdev(X); the
+// trigger is the conditional expectation of Y - Z, whose argument receives the conditional
+// expectation of the adjoint (:188-192) -- the regression of the trigger's adjoint on the
+// date's basis, solved with the date's stored SVD -- so consecutive dates depend on one
+// another through a reduction over all paths: one launch per date, whose last block solves
+// for the projection coefficients the next launch applies.
+namespace {
+
+struct DdSweepParams {
+    int P, nper, callable;
+    int prev_e, cur_e;           // exercise index applied / processed (-1: none)
+    int q_lo, q_hi;              // periods whose weights this launch writes
+    double num0;                 // numeraire at time 0: the value's adjoint seed
+    const double* rec;           // [2][ne][P]
+    const double* basis;         // [ne][5][P]
+    const double* eps;           // [ne]
+    const double* svd_cur;       // SVD of the date cur_e
+    double* betap;               // [ne][6] projection coefficients
+    double* vbar;                // [P] adjoint of the continuation values
+    double* ubar;                // [P] adjoint of the underlying
+    double* omega;               // [nper][P]
+    double* partials;            // [blocks][6][2], then the completion counter
+    int ne;
+};
+
+__global__ void __launch_bounds__(kProdThreads) dd_sweep_kernel(const DdSweepParams a)
+{
+    double acc[kRhs];
+#pragma unroll
+    for (int i = 0; i < kRhs; i++) acc[i] = 0.0;
+    double bp[6];
+    const double* bprev = nullptr;
+    if (a.prev_e >= 0) {
+#pragma unroll
+        for (int i = 0; i < 6; i++) bp[i] = a.betap[a.prev_e * 6 + i];
+        bprev = a.basis + (size_t)a.prev_e * 5 * a.P;
+    }
+    const double* bcur = a.cur_e >= 0 ? a.basis + (size_t)a.cur_e * 5 * a.P : nullptr;
+    const double eps = a.cur_e >= 0 ? a.eps[a.cur_e] : 0.0;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.P; p += gridDim.x * blockDim.x) {
+        double vb = a.prev_e < 0 && a.q_lo == 0 ? a.num0 : a.vbar[p];
+        double ub = a.prev_e < 0 && a.q_lo == 0 ? 0.0 : a.ubar[p];
+        if (bprev) {
+            // the projection of the previous date's trigger adjoint, as the estimator forms it
+            double d = 1.0 * bp[0];
+#pragma unroll
+            for (int i = 1; i < 6; i++) d = d + bprev[(size_t)(i - 1) * a.P + p] * bp[i];
+            vb = vb + d;
+            ub = ub - d;
+        }
+        for (int q = a.q_lo; q < a.q_hi; q++) a.omega[(size_t)q * a.P + p] = a.callable ? ub : vb;
+        if (bcur) {
+            const double X = a.rec[(size_t)a.cur_e * a.P + p];
+            const double D = a.rec[((size_t)a.ne + a.cur_e) * a.P + p];
+            double xb = 0.0;
+            if (isinf(eps)) xb = vb * D;
+            else if (eps > 0.0 && X + eps / 2 >= 0.0 && X - eps / 2 < 0.0) xb = vb * D / eps;
+            const bool cont = X >= 0.0;
+            ub = ub + (cont ? 0.0 : vb);
+            vb = cont ? vb : 0.0;
+            acc[0] = acc[0] + xb * 1.0;
+#pragma unroll
+            for (int i = 0; i < 5; i++) acc[1 + i] = acc[1 + i] + xb * bcur[(size_t)i * a.P + p];
+        }
+        a.vbar[p] = vb;
+        a.ubar[p] = ub;
+    }
+    if (bcur) {
+#pragma unroll
+        for (int i = 0; i < kRhs; i++) {
+            const dd s = block_dd_sum(dd{acc[i], 0.0});
+            if (threadIdx.x == 0) {
+                a.partials[((size_t)blockIdx.x * kRhs + i) * 2] = s.hi;
+                a.partials[((size_t)blockIdx.x * kRhs + i) * 2 + 1] = s.lo;
+            }
+        }
+        __shared__ bool last;
+        __threadfence();
+        __syncthreads();
+        unsigned int* done = reinterpret_cast<unsigned int*>(a.partials + (size_t)gridDim.x * kRhs * 2);
+        if (threadIdx.x == 0) last = atomicAdd(done, 1u) == gridDim.x - 1;
+        __syncthreads();
+        if (last) {
+            __threadfence();
+            regression_solve(a.partials, gridDim.x, a.P, a.svd_cur, a.betap + a.cur_e * 6);
+            if (threadIdx.x == 0) *done = 0u;
+        }
+    }
+}
+
+// block partial sums per exercise date of X (pass 0) or of (X - mean)^2 (pass 1)
+__global__ void __launch_bounds__(kProdThreads) dd_moment_kernel(const double* rec, int P, const double* mean,
+                                                                 double* partials)
+{
+    const int e = blockIdx.y;
+    const double* x = rec + (size_t)e * P;
+    const double m = mean ? mean[e] : 0.0;
+    double sum = 0.0, err = 0.0;  // the Kahan loop of getAverage / getVariance, per thread
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x) {
+        const double v = (mean ? (x[p] - m) * (x[p] - m) : x[p]) - err;
+        const double t = sum + v;
+        err = (t - sum) - v;
+        sum = t;
+    }
+    const dd s = block_dd_sum(dd{sum, -err});
+    if (threadIdx.x == 0) {
+        partials[((size_t)e * gridDim.x + blockIdx.x) * 2] = s.hi;
+        partials[((size_t)e * gridDim.x + blockIdx.x) * 2 + 1] = s.lo;
+    }
+}
+
+// mean (pass 0) or eps = width * sqrt(variance) (pass 1) of every date
+__global__ void __launch_bounds__(kProdThreads) dd_moment_finish_kernel(const double* partials, int blocks, int P,
+                                                                        int pass, double width, double* out)
+{
+    const int e = blockIdx.x;
+    dd acc{0.0, 0.0};
+    for (int b = threadIdx.x; b < blocks; b += blockDim.x)
+        acc = dd_add(acc, dd{partials[((size_t)e * blocks + b) * 2], partials[((size_t)e * blocks + b) * 2 + 1]});
+    acc = block_dd_sum(acc);
+    if (threadIdx.x == 0) {
+        const double v = (acc.hi + acc.lo) / (double)P;
+        out[e] = pass == 0 ? v : width * sqrt(v);
+    }
+}
+
+}  // namespace
+
+int launch_bermudan_dd_weights(const BermudanLaunch& a, const BermudanDdScratch& sc, int P, double num0, double width,
+                               cudaStream_t s)
+{
+    std::vector<int> ex_period;
+    for (int q = 0; q < a.nper; q++)
+        if (a.per[q].exercisable) ex_period.push_back(q);
+    const int ne = (int)ex_period.size();
+    const int blocks = bermudan_blocks(P);
+    KernelTimer kt(K_ADJOINT, s, 2 * (ne > 0 ? 2 : 0) + ne + 1);
+    if (ne > 0) {
+        const int mb = std::min(64, std::max(1, (P + kProdThreads - 1) / kProdThreads));
+        const dim3 grid(mb, ne);
+        dd_moment_kernel<<<grid, kProdThreads, 0, s>>>(sc.d_rec, P, nullptr, sc.d_moments);
+        dd_moment_finish_kernel<<<ne, kProdThreads, 0, s>>>(sc.d_moments, mb, P, 0, width, sc.d_mean);
+        dd_moment_kernel<<<grid, kProdThreads, 0, s>>>(sc.d_rec, P, sc.d_mean, sc.d_moments);
+        dd_moment_finish_kernel<<<ne, kProdThreads, 0, s>>>(sc.d_moments, mb, P, 1, width, sc.d_eps);
+        LMM_CUDA(cudaGetLastError());
+    }
+    DdSweepParams prm;
+    std::memset(&prm, 0, sizeof(prm));
+    prm.P = P;
+    prm.nper = a.nper;
+    prm.callable = a.callable;
+    prm.num0 = num0;
+    prm.rec = sc.d_rec;
+    prm.basis = sc.d_basis;
+    prm.eps = sc.d_eps;
+    prm.betap = sc.d_betap;
+    prm.vbar = sc.d_vbar;
+    prm.ubar = sc.d_ubar;
+    prm.omega = sc.d_omega;
+    prm.partials = sc.d_partials;
+    prm.ne = ne;
+    for (int k = 0; k <= ne; k++) {
+        prm.prev_e = k - 1;
+        prm.cur_e = k < ne ? k : -1;
+        prm.q_lo = k == 0 ? 0 : ex_period[k - 1];
+        prm.q_hi = k < ne ? ex_period[k] : a.nper;
+        prm.svd_cur = k < ne ? sc.d_svd + (size_t)k * kSvdStride : nullptr;
+        dd_sweep_kernel<<<blocks, kProdThreads, 0, s>>>(prm);
+        LMM_CUDA(cudaGetLastError());
     }
     return LMM_OK;
 }

@@ -149,7 +149,7 @@ __host__ __device__ __forceinline__ float java_maxf(float a, float b)
 // 755-1486): x the receiver as a float, a and b the operands as (float) get(i), c the double
 // argument; xd the receiver's double value when it is deterministic (xdet), which floor reads
 // unrounded (:1249).  + - * / in FP32, square root and the transcendentals in FP64 rounded to
-// FP32 ((float) Math.f), pow with its exponent first rounded to FP32.
+// FP32 ((float) Math.f), pow with its exponent (the operand a) first rounded to FP32.
 template <int OP>
 __device__ __forceinline__ float rv_op_f32(float x, float a, float b, double c, bool has_b, double xd, bool xdet)
 {
@@ -162,7 +162,7 @@ __device__ __forceinline__ float rv_op_f32(float x, float a, float b, double c, 
         case LMM_RV_VID: return a / x;
         case LMM_RV_CAP: return java_minf(x, a);
         case LMM_RV_FLOOR: return xdet ? (float)java_max(xd, (double)a) : java_maxf(x, a);
-        case LMM_RV_POW: return (float)java_pow((double)x, (double)(float)c);
+        case LMM_RV_POW: return (float)java_pow((double)x, (double)a);  // a: the exponent as (float) exponent
         case LMM_RV_SQUARED: return x * x;
         case LMM_RV_SQRT: return (float)sqrt((double)x);
         case LMM_RV_EXP: return (float)exp((double)x);

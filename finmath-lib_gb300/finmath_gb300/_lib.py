@@ -33,6 +33,8 @@ STATE_SPACE_LOGNORMAL = 0
 STATE_SPACE_NORMAL = 1
 BASIS_REFERENCE = 0
 BASIS_SWAPRATE = 1
+LMM_DIRAC_ZERO = 0
+LMM_DIRAC_DISCRETE_DELTA = 1
 
 
 class LmmModelDesc(ctypes.Structure):
@@ -121,6 +123,8 @@ SIGNATURES = {
     "lmm_bermudan_get_value": (ctypes.c_int, [_VP, ctypes.POINTER(LmmBermudanDesc), _D, _D, _D]),
     "lmm_bermudan_get_gradient": (ctypes.c_int, [_VP, ctypes.POINTER(LmmBermudanDesc), ctypes.c_int, ctypes.c_int,
                                                  _D, _D, _D, _D]),
+    "lmm_bermudan_get_gradient_aad": (ctypes.c_int, [_VP, ctypes.POINTER(LmmBermudanDesc), ctypes.c_int, ctypes.c_int,
+                                                     ctypes.c_int, ctypes.c_double, _D, _D, _D, _D]),
     "lmm_portfolio_create": (ctypes.c_int, [_VP, ctypes.POINTER(LmmPortfolioDesc), ctypes.POINTER(_VP)]),
     "lmm_portfolio_run": (ctypes.c_int, [_VP, _D, _D, _D, _D, _D, _D]),
     "lmm_portfolio_destroy": (ctypes.c_int, [_VP]),

@@ -1067,18 +1067,28 @@ class BermudanSwaption:
                                     _p(self.periodNotionals), _p(self.swaprates), int(self.isCallable), self.basis)
 
     def getGradient(self, model: LIBORMonteCarloSimulationFromLIBORModel, checkpointStride: int = 1,
-                    freezeNumeraireAdjustment: bool = False):
+                    freezeNumeraireAdjustment: bool = False, diracDeltaApproximationMethod: str = "ZERO",
+                    diracDeltaApproximationWidthPerStdDev: float = 0.05):
         """Value, deltas d V / d L_j(0) and vegas d V / d sigma_{i,j} by the adjoint kernel
-        (the role of RandomVariableDifferentiable.getGradient with these leaves)."""
+        (the role of RandomVariableDifferentiable.getGradient with these leaves).  The
+        exercise decisions are frozen (diracDeltaApproximationMethod "ZERO"), or the reference
+        AAD's default "DISCRETE_DELTA" sweep weights the cash flows (FP64 processes;
+        RandomVariableDifferentiableAADFactory.java:60-72)."""
         proc = model.process
         T = len(proc._keep["times"]) - 1
         N = len(proc._keep["tenor"]) - 1
         d = self._desc()
         v, e = ctypes.c_double(), ctypes.c_double()
         deltas, vegas = np.empty(N), np.empty((T, N))
-        check(_lib.load().lmm_bermudan_get_gradient(proc._h, ctypes.byref(d), int(checkpointStride),
-                                                    int(freezeNumeraireAdjustment), ctypes.byref(v), ctypes.byref(e),
-                                                    _p(deltas), _p(vegas)), "BermudanSwaption.getGradient")
+        methods = {"ZERO": _lib.LMM_DIRAC_ZERO, "DISCRETE_DELTA": _lib.LMM_DIRAC_DISCRETE_DELTA}
+        if diracDeltaApproximationMethod not in methods:
+            raise ValueError(f"diracDeltaApproximationMethod {diracDeltaApproximationMethod} is not supported")
+        check(_lib.load().lmm_bermudan_get_gradient_aad(proc._h, ctypes.byref(d), int(checkpointStride),
+                                                        int(freezeNumeraireAdjustment),
+                                                        methods[diracDeltaApproximationMethod],
+                                                        float(diracDeltaApproximationWidthPerStdDev),
+                                                        ctypes.byref(v), ctypes.byref(e), _p(deltas), _p(vegas)),
+              "BermudanSwaption.getGradient")
         return {"value": v.value, "error": e.value, "deltas": deltas, "vegas": vegas}
 
 

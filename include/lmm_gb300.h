@@ -256,6 +256,21 @@ int lmm_bermudan_get_gradient(lmm_process* proc, const lmm_bermudan_desc* produc
                               int freeze_numeraire_adjustment, double* out_value, double* out_error,
                               double* out_deltas, double* out_vegas);
 
+/* The same gradient with RandomVariableDifferentiableAADFactory's diracDeltaApproximationMethod
+ * (montecarlo/automaticdifferentiation/backward/RandomVariableDifferentiableAADFactory.java:
+ * 60-72): LMM_DIRAC_ZERO is lmm_bermudan_get_gradient (exercise decisions frozen);
+ * LMM_DIRAC_DISCRETE_DELTA (the reference's default, width 0.05) runs the reference AAD's
+ * reverse sweep over the backward induction (RandomVariableDifferentiableAAD.java:171-208,
+ * 396-429): each choice passes (Y - Z) 1{-eps/2 <= X < eps/2} / eps, eps = dirac_width x the
+ * trigger's standard deviation, to its trigger, and the trigger's conditional expectation
+ * hands that adjoint to its argument through the same regression; the resulting weights of
+ * the cash flows seed the adjoint of the Euler scheme.  FP64 processes only. */
+#define LMM_DIRAC_ZERO 0
+#define LMM_DIRAC_DISCRETE_DELTA 1
+int lmm_bermudan_get_gradient_aad(lmm_process* proc, const lmm_bermudan_desc* product, int checkpoint_stride,
+                                  int freeze_numeraire_adjustment, int dirac_method, double dirac_width,
+                                  double* out_value, double* out_error, double* out_deltas, double* out_vegas);
+
 /* ---------------------------------------------------------------- portfolio batch
  * A portfolio of Bermudan swaptions valued, with their deltas and vegas, on one shared
  * simulation: the per-product work (regression, backward induction, adjoint) is recorded

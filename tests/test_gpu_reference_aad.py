@@ -11,11 +11,10 @@ Euler scheme's by central differences of the weighted cash flows, per path).
 
 * ZERO: the GPU adjoint with the numeraire adjustment frozen is the same pathwise
   derivative, so every delta and vega agrees to 1e-6 of the largest Greek.
-* DISCRETE_DELTA (the reference's default): the boundary term is a Monte Carlo quantity
-  of its own; the GPU's frozen-exercise Greeks differ from it by the restated term, which
-  the test measures in standard errors of the per-path gradient and reports; it asserts
-  only that the GPU's Greeks and the restated ZERO Greeks agree, and that the DISCRETE_DELTA
-  ones reduce to them when the window is empty (width 0).
+* DISCRETE_DELTA (the reference's default): the GPU runs the same sweep over its backward
+  induction (lmm_bermudan_get_gradient_aad) and its Greeks agree with the restatement's to
+  1e-6 of the largest Greek; the boundary term itself, measured in standard errors of the
+  per-path gradient, is reported; with an empty window (width 0) both reduce to ZERO.
 """
 import numpy as np
 import pytest
@@ -47,7 +46,11 @@ def setup():
             for meth in ("ZERO", "DISCRETE_DELTA")}
     empty = AR.bermudan_gradient(m, dW, fix, plen, pay, K, method="DISCRETE_DELTA", width=0.0, deltas=DELTAS[:2],
                                  build_model=build)
-    yield dict(g=g, refs=refs, empty=empty)
+    gdd = berm.getGradient(sim, checkpointStride=4, freezeNumeraireAdjustment=True,
+                           diracDeltaApproximationMethod="DISCRETE_DELTA")
+    gdd0 = berm.getGradient(sim, checkpointStride=4, freezeNumeraireAdjustment=True,
+                            diracDeltaApproximationMethod="DISCRETE_DELTA", diracDeltaApproximationWidthPerStdDev=0.0)
+    yield dict(g=g, refs=refs, empty=empty, gdd=gdd, gdd0=gdd0)
     sim.process.close()
     sim.process.brownianMotion.close()
 
@@ -86,3 +89,18 @@ def test_discrete_delta_term(setup, record_property):
     _, empty = setup["empty"]
     for j, (mean, se) in empty["deltas"].items():
         assert mean == pytest.approx(zero["deltas"][j][0], rel=1e-12, abs=1e-15)
+
+
+def test_discrete_delta_method_equals_the_restated_reference(setup):
+    g, gdd = setup["g"], setup["gdd"]
+    _, ref = setup["refs"]["DISCRETE_DELTA"]
+    assert gdd["value"] == g["value"]  # the AAD valuation's value is the plain value
+    scale_d, scale_v = np.max(np.abs(gdd["deltas"])), np.max(np.abs(gdd["vegas"]))
+    for j, (mean, se) in ref["deltas"].items():
+        assert gdd["deltas"][j] == pytest.approx(mean, abs=1e-6 * scale_d)
+    for (i, j), (mean, se) in ref["vegas"].items():
+        assert gdd["vegas"][i, j] == pytest.approx(mean, abs=1e-6 * scale_v)
+    # the boundary term is present, and an empty window gives back the frozen-exercise Greeks
+    assert np.max(np.abs(gdd["deltas"] - g["deltas"])) > 1e-4 * scale_d
+    assert np.allclose(setup["gdd0"]["deltas"], g["deltas"], rtol=1e-12, atol=1e-15)
+    assert np.allclose(setup["gdd0"]["vegas"], g["vegas"], rtol=1e-12, atol=1e-15)
