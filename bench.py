@@ -427,6 +427,7 @@ def run_ours(args):
         if not args.no_portfolio:
             line["forms"]["portfolio"] = portfolio_form(args, F, W, cfg, P)
         line["forms"]["random_variable"] = random_variable_form(args, F, W, cfg, P)
+        line["forms"]["calibration"] = calibration_form(args, F, W)
     if rank == 0 and not args.no_cpu_baseline:
         v, dt, parity = headline_parity(F, W, cfg, sim, berm, swpt, args.cpu_paths, os.cpu_count() or 1)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
@@ -643,6 +644,62 @@ def random_variable_form(args, F, W, cfg, P, n=1 << 26):
     sim.process.close()
     sim.process.brownianMotion.close()
     return out
+
+
+def calibration_form(args, F, W, paths=20000, iterations=20):
+    """Monte Carlo calibration form: the abcd volatility of the lmm20 model fitted by
+    Levenberg-Marquardt to seven swaption prices of another surface (moved by up to 3 %, so no
+    exact fit exists), every objective evaluation a new Euler process on one resident
+    Brownian motion of `paths` paths and the fused swaption kernel; objective evaluations per
+    second (one evaluation prices every calibration product)."""
+    import torch
+    cfg = W.LMM20
+    td = F.TimeDiscretizationFromArray(0.0, int(round(cfg["T_end"] / cfg["dt"])), cfg["dt"])
+    tenor = F.TimeDiscretizationFromArray(0.0, int(round(cfg["tenor_end"] / cfg["period"])), cfg["period"])
+    curve = F.ForwardCurveInterpolation.createForwardCurveFromForwards("forwardCurve", cfg["curve_nodes"],
+                                                                       cfg["curve_values"], cfg["period"])
+
+    def covariance(abcd):
+        vol = F.LIBORVolatilityModelFourParameterExponentialForm(td, tenor, *abcd, True)
+        corr = F.LIBORCorrelationModelExponentialDecay(td, tenor, cfg["F"], cfg["corr_decay"], False)
+        return F.LIBORCovarianceModelFromVolatilityAndCorrelation(td, tenor, vol, corr)
+
+    model = F.LIBORMarketModelFromCovarianceModel.of(tenor, None, curve, F.DiscountCurveFromForwardCurve(curve), None,
+                                                     covariance(cfg["abcd"]), None, {})
+    bm = F.BrownianMotionFromMersenneRandomNumbers(td, cfg["F"], paths, 31415)
+    specs = []
+    for ex, n in ((1.0, 4), (2.0, 6), (3.0, 4), (5.0, 8), (7.0, 4), (2.0, 12), (4.0, 10)):
+        fix = [ex + 0.5 * i for i in range(n)]
+        specs.append((ex, fix, [x + 0.5 for x in fix], 0.05))
+    proc = F.EulerSchemeFromProcessModel(model, bm)
+    targets = [F.Swaption(*sp).getValue(F.LIBORMonteCarloSimulationFromLIBORModel(proc)) * (1.0 + 0.03 * np.sin(3.0 * i))
+               for i, sp in enumerate(specs)]
+    proc.close()
+    count = [0]
+
+    class Counted:
+        def __init__(self, sp, first):
+            self.swaption, self.first = F.Swaption(*sp), first
+
+        def getValue(self, sim):
+            if self.first:
+                count[0] += 1
+            return self.swaption.getValue(sim)
+
+    items = [F.CalibrationProduct(f"s{i}", Counted(sp, i == 0), t) for i, (sp, t) in enumerate(zip(specs, targets))]
+    params = {"brownianMotion": bm, "maxIterations": iterations, "accuracy": 0.0}
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    calibrated = covariance((0.25, 0.15, 0.2, 0.12)).getCloneCalibrated(model, items, params)
+    torch.cuda.synchronize()
+    sec = time.perf_counter() - t0
+    opt = params["optimizer"]
+    bm.close()
+    return {"paths": paths, "products": len(specs), "parameters": 4, "objective_evaluations": count[0],
+            "seconds": sec, "evaluations_per_second": count[0] / sec, "iterations": opt.getIterations(),
+            "rms_error": opt.getRootMeanSquaredError(), "parameters_calibrated": list(calibrated.getParameter()),
+            "note": "each evaluation builds the trial covariance model and Euler process on the host and prices "
+                    "the products with one fused launch each; the Jacobian's columns run one after another"}
 
 
 def portfolio_form(args, F, W, cfg, P):

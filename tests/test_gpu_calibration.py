@@ -42,3 +42,50 @@ def test_calibration_recovers_the_generating_volatility_parameters():
     assert opt.getRootMeanSquaredError() <= 1e-10 * max(targets)
     assert np.allclose(calibrated.getCovarianceModel().getParameter(), cfg["abcd"], rtol=1e-7)
     bm.close()
+
+
+def test_calibration_matches_the_oracle_calibration():
+    # the same Levenberg-Marquardt calibration to targets no parameter set fits exactly (the
+    # prices of another volatility surface, moved by up to 3 %), once with the GPU process and
+    # fused swaption kernel and once with the oracle pricing the same paths: the iterations see
+    # the same objective values to rounding, so they end at the same parameters and error
+    import test_host_calibration as HC
+    from finmath_gb300 import lmm as LM
+    cfg = W.LMM20
+    td, tenor, truth = HC._covariance(cfg, corr_cal=False)
+    curve = F.ForwardCurveInterpolation.createForwardCurveFromForwards("forwardCurve", cfg["curve_nodes"],
+                                                                       cfg["curve_values"], cfg["period"])
+    model = F.LIBORMarketModelFromCovarianceModel.of(tenor, None, curve, F.DiscountCurveFromForwardCurve(curve), None,
+                                                     truth, None, {})
+    P, seed = 2000, 31415
+    specs = []
+    for ex, n in ((1.0, 4), (2.0, 6), (3.0, 4), (5.0, 8), (7.0, 4), (2.0, 12), (4.0, 10)):
+        fix = [ex + 0.5 * i for i in range(n)]
+        specs.append((ex, fix, [x + 0.5 for x in fix], 0.05))
+    bm = F.BrownianMotionFromMersenneRandomNumbers(td, cfg["F"], P, seed)
+    process = F.EulerSchemeFromProcessModel(model, bm)
+    sim = F.LIBORMonteCarloSimulationFromLIBORModel(process)
+    targets = [F.Swaption(*sp).getValue(sim) * (1.0 + 0.03 * np.sin(3.0 * i)) for i, sp in enumerate(specs)]
+    process.close()
+    _, _, start = HC._covariance(cfg, corr_cal=False, abcd=(0.25, 0.15, 0.2, 0.12))
+
+    gpu_items = [F.CalibrationProduct(f"s{i}", F.Swaption(*sp), t) for i, (sp, t) in enumerate(zip(specs, targets))]
+    gp = {"brownianMotion": bm, "maxIterations": 40, "accuracy": 0.0}
+    gpu = start.getCloneCalibrated(model, gpu_items, gp)
+
+    saved = (LM.EulerSchemeFromProcessModel, LM.LIBORMonteCarloSimulationFromLIBORModel)
+    LM.EulerSchemeFromProcessModel, LM.LIBORMonteCarloSimulationFromLIBORModel = HC._HostProcess, HC._HostSimulation
+    try:
+        hbm = HC._HostBrownian(td.getAsDoubleArray(), cfg["F"], P, seed)
+        host_items = [F.CalibrationProduct(f"s{i}", HC._OracleSwaption(*sp), t)
+                      for i, (sp, t) in enumerate(zip(specs, targets))]
+        hp = {"brownianMotion": hbm, "maxIterations": 40, "accuracy": 0.0}
+        host = start.getCloneCalibrated(model, host_items, hp)
+    finally:
+        LM.EulerSchemeFromProcessModel, LM.LIBORMonteCarloSimulationFromLIBORModel = saved
+    bm.close()
+    assert gp["optimizer"].getRootMeanSquaredError() > 1e-4 * max(targets)  # no exact fit exists
+    assert gpu.getParameter() == pytest.approx(host.getParameter(), rel=1e-6)
+    assert gp["optimizer"].getRootMeanSquaredError() == pytest.approx(hp["optimizer"].getRootMeanSquaredError(),
+                                                                      rel=1e-6)
+    assert gp["optimizer"].getIterations() == hp["optimizer"].getIterations()
