@@ -16,10 +16,10 @@
 // (increments_loop) so that each [t][f] row is written in 64-byte segments although the
 // stream runs path-major.
 //
-// This translation unit is compiled with -fmad=false.  The FP64 inverse normal, which the
-// GPU's narrow FP64 pipe bounds, evaluates the reference's rational functions with fused
-// Horner steps and a Newton quotient (within a few ulp of the reference's normals; the
-// uniforms stay bit-exact).
+// This translation unit is compiled with -fmad=false (the error-free transforms below rely
+// on every add and multiply rounding separately).  The FP64 inverse normal evaluates the
+// reference's rational functions in double-float arithmetic on the FP32 pipe (within 5e-14
+// relative of the reference's normals; the uniforms stay bit-exact).
 #include "fp64math.cuh"
 #include "lmm_internal.h"
 
@@ -80,15 +80,90 @@ __device__ __forceinline__ uint32_t mt_next(uint32_t x_m, uint32_t x_0, uint32_t
 }
 
 // NormalDistribution.inverseCumulativeNormalDistributionWichura (functions/NormalDistribution.java:67-162),
-// AS241 (Wichura 1988): the reference's coefficients and branches, evaluated with fused
-// Horner steps.  The central branch (|p - 0.5| <= 0.425, ~85 % of draws) and the tails are
-// separate functions so that the generator can run each on a compacted set of lanes.
+// AS241 (Wichura 1988): the reference's coefficients and branches.  The central branch
+// (|p - 0.5| <= 0.425, ~85 % of draws) and the tails are separate functions so that the
+// generator runs each on a compacted set of lanes.
+//
+// The FP64 form evaluates the rational functions in double-float arithmetic on the FP32
+// pipe (on this GPU FP64 issues at 1/64 of the FP32 rate, and the FP64 Horner steps were
+// most of the generator's time): the argument r is formed in FP64 and split into a pair
+// of floats hi + lo, each Horner step v <- v r + c runs on float pairs (the product's
+// rounding error by fused multiply-adds, the sum by TwoSum, a renormalisation), and the
+// quotient is the rounded FP32 quotient plus the residual's quotient.  Every term of the
+// polynomials is positive on its branch (no cancellation), so the pair carries about
+// 2^-47 relative per step: the normals stay within 5e-14 relative of the reference's FP64
+// evaluation, four FP64 instructions per central draw instead of 24.
+
+// a coefficient c as hi + lo floats: hi = c rounded to FP32, lo = the rounded remainder
+struct DfCoef {
+    float h, l;
+};
+__host__ __device__ constexpr DfCoef dfc(double c) { return DfCoef{(float)c, (float)(c - (double)(float)c)}; }
+
+// c[0] r^7 + ... + c[7] for r = rh + rl, by Horner steps on float pairs
+__device__ __forceinline__ void df_horner8(float rh, float rl, const DfCoef (&c)[8], float& vh, float& vl)
+{
+    vh = c[0].h;
+    vl = c[0].l;
+#pragma unroll
+    for (int i = 1; i < 8; i++) {
+        const float p = __fmul_rn(vh, rh);
+        float e = fmaf(vh, rh, -p);  // the product's rounding error, exactly
+        e = fmaf(vh, rl, e);
+        e = fmaf(vl, rh, e);
+        float s, t;
+        two_sum(p, c[i].h, s, t);
+        t = (e + c[i].l) + t;
+        vh = s + t;  // |t| is far below |s|: the renormalised pair, exactly
+        vl = t - (vh - s);
+    }
+}
+
+// binary32 -> binary64 in integer operations for normal floats and zero (subnormals become
+// zero; no infinity or NaN reaches it)
+__device__ __forceinline__ double f32_to_f64_nz(float f)
+{
+    const unsigned b = __float_as_uint(f);
+    const unsigned e = (b >> 23) & 0xffu;
+    const unsigned hi = (b & 0x80000000u) | (e ? (((e + (1023u - 127u)) << 20) | ((b & 0x7fffffu) >> 3)) : 0u);
+    return __hiloint2double((int)hi, e ? (int)(b << 29) : 0);
+}
+
+// a double as hi + lo floats (hi rounded in integer operations, lo the rounded remainder of
+// one exact FP64 subtraction)
+__device__ __forceinline__ void df_split_nz(double x, float& hi, float& lo)
+{
+    hi = f64_to_f32_small(x);
+    lo = f64_to_f32_small(x - f32_to_f64_nz(hi));
+}
+
+// (nh + nl) / (dh + dl) for positive pairs: the rounded FP32 quotient yh plus the quotient
+// of the residual nh + nl - yh (dh + dl), formed exactly up to its last rounding
+__device__ __forceinline__ double df_quotient(float nh, float nl, float dh, float dl)
+{
+    const float yh = __fdiv_rn(nh, dh);
+    const float p = __fmul_rn(yh, dh);
+    const float e = fmaf(yh, dh, -p);
+    float res = (nh - p) - e;  // nh - p is exact: p lies within a few ulp of nh
+    res = res + nl;
+    res = fmaf(-yh, dl, res);
+    const float yl = __fmul_rn(res, __frcp_rn(dh));
+    return f32_to_f64_nz(yh) + f32_to_f64_nz(yl);
+}
+
 // The central branch for q = dq 2^-52 (|q| <= 0.425): q converted in integer operations,
-// the two degree-7 polynomials by fused Horner steps, and q num / den as the Newton
-// reciprocal of den (den >= 1 on the branch) times q num, corrected once by the residual
-// q num - den y.  About 23 FP64 instructions instead of 43.
+// r = 0.180625 - q^2 by one FP64 fused multiply-add, the two degree-7 polynomials and their
+// quotient on float pairs, and q times the quotient in FP64.
 __device__ __forceinline__ double icdf_central(int64_t dq)
 {
+    constexpr DfCoef a[8] = {dfc(2.5090809287301226727e+03), dfc(3.3430575583588128105e+04),
+                             dfc(6.7265770927008700853e+04), dfc(4.5921953931549871457e+04),
+                             dfc(1.3731693765509461125e+04), dfc(1.9715909503065514427e+03),
+                             dfc(1.3314166789178437745e+02), dfc(3.3871328727963666080e+00)};
+    constexpr DfCoef b[8] = {dfc(5.2264952788528545610e+03), dfc(2.8729085735721942674e+04),
+                             dfc(3.9307895800092710610e+04), dfc(2.1213794301586595867e+04),
+                             dfc(5.3941960214247511077e+03), dfc(6.8718700749205790830e+02),
+                             dfc(4.2313330701600911252e+01), dfc(1.0)};
     double q = 0.0;
     if (dq != 0) {
         // |dq| < 2^51: exact as a double; exponent from the leading bit, scaled by 2^-52
@@ -99,72 +174,50 @@ __device__ __forceinline__ double icdf_central(int64_t dq)
                                         ((unsigned long long)(1023 + lead - 52) << 52) | frac;
         q = __longlong_as_double((long long)bits);
     }
-    const double r = fma(-q, q, 0.180625);
-    double num = 2.5090809287301226727e+03;
-    num = fma(num, r, 3.3430575583588128105e+04);
-    num = fma(num, r, 6.7265770927008700853e+04);
-    num = fma(num, r, 4.5921953931549871457e+04);
-    num = fma(num, r, 1.3731693765509461125e+04);
-    num = fma(num, r, 1.9715909503065514427e+03);
-    num = fma(num, r, 1.3314166789178437745e+02);
-    num = fma(num, r, 3.3871328727963666080e+00);
-    double den = 5.2264952788528545610e+03;
-    den = fma(den, r, 2.8729085735721942674e+04);
-    den = fma(den, r, 3.9307895800092710610e+04);
-    den = fma(den, r, 2.1213794301586595867e+04);
-    den = fma(den, r, 5.3941960214247511077e+03);
-    den = fma(den, r, 6.8718700749205790830e+02);
-    den = fma(den, r, 4.2313330701600911252e+01);
-    den = fma(den, r, 1.0);
-    const double n = q * num;
-    const double rd = rcp_newton(den);
-    const double y = n * rd;
-    return fma(rd, fma(-den, y, n), y);
-}
-
-// c[0] r^7 + ... + c[7] by fused Horner steps
-__device__ __forceinline__ double horner8d(double r, const double (&c)[8])
-{
-    double v = c[0];
-#pragma unroll
-    for (int i = 1; i < 8; i++) v = fma(v, r, c[i]);
-    return v;
+    const double r = fma(-q, q, 0.180625);  // > 0 on the branch
+    float rh, rl, nh, nl, dh, dl;
+    df_split_nz(r, rh, rl);
+    df_horner8(rh, rl, a, nh, nl);
+    df_horner8(rh, rl, b, dh, dl);
+    return q * df_quotient(nh, nl, dh, dl);
 }
 
 // The tail branch (|p - 1/2| > 0.425, the draws the central test rejected) of the same
-// transform: CUDA's log and sqrt, the rational functions by fused Horner steps and a
-// Newton quotient (the denominators are >= 1 on their branches).
+// transform: CUDA's log and sqrt in FP64, the rational functions and their quotient on
+// float pairs (the shifted argument is >= 0 and every coefficient positive).
 __device__ double icdf_tail(double p)
 {
-    constexpr double c[8] = {7.74545014278341407640e-04, 2.27238449892691845833e-02, 2.41780725177450611770e-01,
-                             1.27045825245236838258e+00, 3.64784832476320460504e+00, 5.76949722146069140550e+00,
-                             4.63033784615654529590e+00, 1.42343711074968357734e+00};
-    constexpr double d[8] = {1.05075007164441684324e-09, 5.47593808499534494600e-04, 1.51986665636164571966e-02,
-                             1.48103976427480074590e-01, 6.89767334985100004550e-01, 1.67638483018380384940e+00,
-                             2.05319162663775882187e+00, 1.0};
-    constexpr double e[8] = {2.01033439929228813265e-07, 2.71155556874348757815e-05, 1.24266094738807843860e-03,
-                             2.65321895265761230930e-02, 2.96560571828504891230e-01, 1.78482653991729133580e+00,
-                             5.46378491116411436990e+00, 6.65790464350110377720e+00};
-    constexpr double f[8] = {2.04426310338993978564e-15, 1.42151175831644588870e-07, 1.84631831751005468180e-05,
-                             7.86869131145613259100e-04, 1.48753612908506148525e-02, 1.36929880922735805310e-01,
-                             5.99832206555887937690e-01, 1.0};
+    constexpr DfCoef c[8] = {dfc(7.74545014278341407640e-04), dfc(2.27238449892691845833e-02),
+                             dfc(2.41780725177450611770e-01), dfc(1.27045825245236838258e+00),
+                             dfc(3.64784832476320460504e+00), dfc(5.76949722146069140550e+00),
+                             dfc(4.63033784615654529590e+00), dfc(1.42343711074968357734e+00)};
+    constexpr DfCoef d[8] = {dfc(1.05075007164441684324e-09), dfc(5.47593808499534494600e-04),
+                             dfc(1.51986665636164571966e-02), dfc(1.48103976427480074590e-01),
+                             dfc(6.89767334985100004550e-01), dfc(1.67638483018380384940e+00),
+                             dfc(2.05319162663775882187e+00), dfc(1.0)};
+    constexpr DfCoef e[8] = {dfc(2.01033439929228813265e-07), dfc(2.71155556874348757815e-05),
+                             dfc(1.24266094738807843860e-03), dfc(2.65321895265761230930e-02),
+                             dfc(2.96560571828504891230e-01), dfc(1.78482653991729133580e+00),
+                             dfc(5.46378491116411436990e+00), dfc(6.65790464350110377720e+00)};
+    constexpr DfCoef f[8] = {dfc(2.04426310338993978564e-15), dfc(1.42151175831644588870e-07),
+                             dfc(1.84631831751005468180e-05), dfc(7.86869131145613259100e-04),
+                             dfc(1.48753612908506148525e-02), dfc(1.36929880922735805310e-01),
+                             dfc(5.99832206555887937690e-01), dfc(1.0)};
     const double q = p - 0.5;
     double r = (q < 0.0) ? p : 1.0 - p;
     if (r <= 0.0) return 0.0;
     r = sqrt(-log(r));
-    double num, den;
+    float rh, rl, nh, nl, dh, dl;
     if (r <= 5.0) {
-        r -= 1.6;
-        num = horner8d(r, c);
-        den = horner8d(r, d);
+        df_split_nz(r - 1.6, rh, rl);
+        df_horner8(rh, rl, c, nh, nl);
+        df_horner8(rh, rl, d, dh, dl);
     } else {
-        r -= 5.0;
-        num = horner8d(r, e);
-        den = horner8d(r, f);
+        df_split_nz(r - 5.0, rh, rl);
+        df_horner8(rh, rl, e, nh, nl);
+        df_horner8(rh, rl, f, dh, dl);
     }
-    const double rd = rcp_newton(den);
-    const double y = num * rd;
-    const double v = fma(rd, fma(-den, y, num), y);
+    const double v = df_quotient(nh, nl, dh, dl);
     return (q < 0.0) ? -v : v;
 }
 
@@ -273,7 +326,7 @@ template <typename OutT>
 __device__ __forceinline__ void increments_loop(const RngParams& prm, uint32_t* x, int tid, int64_t v0, int64_t v1,
                                                 unsigned long long* tail_w, int2* tail_pos, int* tail_n)
 {
-    constexpr bool kExact = sizeof(OutT) == 8;  // FP64: the reference's arithmetic, bit for bit
+    constexpr bool kExact = sizeof(OutT) == 8;  // FP64 increments (the parity form)
     constexpr int kRound = kMtN / 2;
     const int TF = prm.values_per_path, F = prm.num_factors, P = prm.num_paths, K = prm.tile_k;
     const int T = TF / F;
