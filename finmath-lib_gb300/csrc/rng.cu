@@ -92,7 +92,9 @@ __device__ __forceinline__ uint32_t mt_next(uint32_t x_m, uint32_t x_0, uint32_t
 // quotient is the rounded FP32 quotient plus the residual's quotient.  Every term of the
 // polynomials is positive on its branch (no cancellation), so the pair carries about
 // 2^-47 relative per step: the normals stay within 5e-14 relative of the reference's FP64
-// evaluation, four FP64 instructions per central draw instead of 24.
+// evaluation, four FP64 instructions per central draw instead of 24.  The tails take
+// their logarithm and square root on float pairs as well (restated from the mathematics
+// below; CUDA's FP64 log and sqrt were most of the tail's FP64 instructions).
 
 // a coefficient c as hi + lo floats: hi = c rounded to FP32, lo = the rounded remainder
 struct DfCoef {
@@ -100,22 +102,35 @@ struct DfCoef {
 };
 __host__ __device__ constexpr DfCoef dfc(double c) { return DfCoef{(float)c, (float)(c - (double)(float)c)}; }
 
-// c[0] r^7 + ... + c[7] for r = rh + rl, by Horner steps on float pairs
-__device__ __forceinline__ void df_horner8(float rh, float rl, const DfCoef (&c)[8], float& vh, float& vl)
+// Numerator (lane x) and denominator (lane y) polynomials c[0] r^7 + ... + c[7] for
+// r = rh + rl, by Horner steps on float pairs, both at once on the paired FP32 pipe: each
+// step forms -p = -(v_h r_h) and the product's exact error v_h r_h - p by fused multiply-
+// adds (plus the cross terms v_h r_l, v_l r_h), adds the coefficient by TwoSum
+// (subtractions as fused multiply-adds with -1, which round once like a subtraction) and
+// renormalises the pair.
+__device__ __forceinline__ void df_horner8x2(float rh, float rl, const DfCoef (&a)[8], const DfCoef (&b)[8],
+                                             float2& vh, float2& vl)
 {
-    vh = c[0].h;
-    vl = c[0].l;
+    const float2 R = make_float2(rh, rh), Rn = make_float2(-rh, -rh), Rl = make_float2(rl, rl);
+    const float2 M1 = make_float2(-1.0f, -1.0f);
+    vh = make_float2(a[0].h, b[0].h);
+    vl = make_float2(a[0].l, b[0].l);
 #pragma unroll
     for (int i = 1; i < 8; i++) {
-        const float p = __fmul_rn(vh, rh);
-        float e = fmaf(vh, rh, -p);  // the product's rounding error, exactly
-        e = fmaf(vh, rl, e);
-        e = fmaf(vl, rh, e);
-        float s, t;
-        two_sum(p, c[i].h, s, t);
-        t = (e + c[i].l) + t;
-        vh = s + t;  // |t| is far below |s|: the renormalised pair, exactly
-        vl = t - (vh - s);
+        const float2 C = make_float2(a[i].h, b[i].h), CL = make_float2(a[i].l, b[i].l);
+        const float2 pn = __fmul2_rn(vh, Rn);      // -p, p = v_h r_h rounded
+        float2 e = __ffma2_rn(vh, R, pn);          // v_h r_h - p, exactly
+        e = __ffma2_rn(vh, Rl, e);
+        e = __ffma2_rn(vl, R, e);
+        const float2 s = __ffma2_rn(pn, M1, C);    // C + p
+        const float2 z = __ffma2_rn(C, M1, s);     // s - C
+        const float2 u = __ffma2_rn(z, M1, s);     // s - z
+        const float2 v = __ffma2_rn(u, M1, C);     // C - u
+        const float2 w = __fadd2_rn(pn, z);        // -(p - z)
+        const float2 err = __ffma2_rn(w, M1, v);   // (C - (s - z)) + (p - z): the TwoSum error
+        const float2 t = __fadd2_rn(__fadd2_rn(e, CL), err);
+        vh = __fadd2_rn(s, t);
+        vl = __ffma2_rn(__ffma2_rn(s, M1, vh), M1, t);  // t - (vh - s)
     }
 }
 
@@ -175,17 +190,106 @@ __device__ __forceinline__ double icdf_central(int64_t dq)
         q = __longlong_as_double((long long)bits);
     }
     const double r = fma(-q, q, 0.180625);  // > 0 on the branch
-    float rh, rl, nh, nl, dh, dl;
+    float rh, rl;
+    float2 vh, vl;
     df_split_nz(r, rh, rl);
-    df_horner8(rh, rl, a, nh, nl);
-    df_horner8(rh, rl, b, dh, dl);
-    return q * df_quotient(nh, nl, dh, dl);
+    df_horner8x2(rh, rl, a, b, vh, vl);
+    return q * df_quotient(vh.x, vl.x, vh.y, vl.y);
+}
+
+// ---- float-pair arithmetic of the tail branch
+__device__ __forceinline__ void df_fast_two_sum(float a, float b, float& s, float& e)
+{
+    s = a + b;  // |a| >= |b|
+    e = b - (s - a);
+}
+
+__device__ __forceinline__ void df_add(float ah, float al, float bh, float bl, float& sh, float& sl)
+{
+    float s, e;
+    two_sum(ah, bh, s, e);
+    df_fast_two_sum(s, (al + bl) + e, sh, sl);
+}
+
+__device__ __forceinline__ void df_mul(float ah, float al, float bh, float bl, float& ph, float& pl)
+{
+    const float p = __fmul_rn(ah, bh);
+    float e = fmaf(ah, bh, -p);
+    e = fmaf(ah, bl, e);
+    e = fmaf(al, bh, e);
+    df_fast_two_sum(p, e, ph, pl);
+}
+
+__device__ __forceinline__ void df_div(float nh, float nl, float dh, float dl, float& yh, float& yl)
+{
+    const float q = __fdiv_rn(nh, dh);
+    const float p = __fmul_rn(q, dh);
+    const float e = fmaf(q, dh, -p);
+    float res = (nh - p) - e;
+    res = res + nl;
+    res = fmaf(-q, dl, res);
+    df_fast_two_sum(q, __fmul_rn(res, __frcp_rn(dh)), yh, yl);
+}
+
+// sqrt(-log t) for t = M 2^-52, 1 <= M < 2^50, as a float pair (about 2^-46 relative), from
+// the mathematics of the logarithm: t = x 2^k with x in [1/sqrt 2, sqrt 2), read exactly
+// from the integer; log x = 2 atanh(s) = 2 s (1 + s^2/3 + s^4/5 + ...) with
+// s = (x - 1)/(x + 1), |s| <= 0.172 (terms beyond s^10/11 are below 2^-50 and run in FP32,
+// the leading five on float pairs); log t = k log 2 + log x; the square root as the rounded
+// FP32 root plus the residual's correction.
+__device__ __forceinline__ void df_sqrt_neg_log(int64_t M, float& rh, float& rl)
+{
+    constexpr DfCoef ln2 = dfc(0.693147180559945309417232121458176568);
+    constexpr DfCoef inv[4] = {dfc(1.0 / 9.0), dfc(1.0 / 7.0), dfc(1.0 / 5.0), dfc(1.0 / 3.0)};
+    const unsigned long long um = (unsigned long long)M;
+    int lead = 63 - __clzll((long long)um);              // M in [2^lead, 2^(lead+1))
+    const unsigned long long norm = um << (63 - lead);  // the leading one at bit 63
+    float xh = __uint2float_rn((unsigned)(norm >> 40)) * 0x1.0p-23f;  // 24 bits: exact, in [1, 2)
+    const unsigned rest = (unsigned)((norm >> 16) & 0xffffffull), rest2 = (unsigned)(norm & 0xffffull);
+    float xl = __fmaf_rn(__uint2float_rn(rest2), 0x1.0p-63f, __uint2float_rn(rest) * 0x1.0p-47f);
+    if (xh >= 1.4142135f) {  // x / 2 in [0.707, 1)
+        xh *= 0.5f;
+        xl *= 0.5f;
+        lead++;
+    }
+    float nh, nl, dh, dl, sh, sl, wh, wl;
+    df_add(xh - 1.0f, 0.0f, xl, 0.0f, nh, nl);  // xh - 1 is exact
+    df_add(xh, xl, 1.0f, 0.0f, dh, dl);
+    df_div(nh, nl, dh, dl, sh, sl);
+    df_mul(sh, sl, sh, sl, wh, wl);
+    float q = 1.0f / 21.0f;
+    q = fmaf(q, wh, 1.0f / 19.0f);
+    q = fmaf(q, wh, 1.0f / 17.0f);
+    q = fmaf(q, wh, 1.0f / 15.0f);
+    q = fmaf(q, wh, 1.0f / 13.0f);
+    q = fmaf(q, wh, 1.0f / 11.0f);
+    float vh = q, vl = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        df_mul(vh, vl, wh, wl, vh, vl);
+        df_add(vh, vl, inv[i].h, inv[i].l, vh, vl);
+    }
+    df_mul(vh, vl, wh, wl, vh, vl);
+    df_add(vh, vl, 1.0f, 0.0f, vh, vl);
+    float lh, ll;
+    df_mul(sh, sl, vh, vl, lh, ll);  // log x / 2
+    const float K = (float)(lead - 52);
+    const float p = __fmul_rn(K, ln2.h);
+    float e = fmaf(K, ln2.h, -p);
+    e = fmaf(K, ln2.l, e);
+    float Lh, Ll;
+    df_add(p, e, 2.0f * lh, 2.0f * ll, Lh, Ll);  // log t < -2.59
+    const float ah = -Lh, al = -Ll;
+    const float r = __fsqrt_rn(ah);
+    const float res = fmaf(-r, r, ah) + al;
+    df_fast_two_sum(r, __fmul_rn(res, __frcp_rn(r + r)), rh, rl);
 }
 
 // The tail branch (|p - 1/2| > 0.425, the draws the central test rejected) of the same
-// transform: CUDA's log and sqrt in FP64, the rational functions and their quotient on
-// float pairs (the shifted argument is >= 0 and every coefficient positive).
-__device__ double icdf_tail(double p)
+// transform for the tail probability t = M 2^-52 = min(u, 1 - u) > 0, without its sign:
+// r = sqrt(-log t), then the rational functions of r - 1.6 (r <= 5) or r - 5 and their
+// quotient, all on float pairs (the shifted argument is >= 0 and every coefficient positive).
+__device__ double icdf_tail(int64_t M)
 {
     constexpr DfCoef c[8] = {dfc(7.74545014278341407640e-04), dfc(2.27238449892691845833e-02),
                              dfc(2.41780725177450611770e-01), dfc(1.27045825245236838258e+00),
@@ -203,22 +307,18 @@ __device__ double icdf_tail(double p)
                              dfc(1.84631831751005468180e-05), dfc(7.86869131145613259100e-04),
                              dfc(1.48753612908506148525e-02), dfc(1.36929880922735805310e-01),
                              dfc(5.99832206555887937690e-01), dfc(1.0)};
-    const double q = p - 0.5;
-    double r = (q < 0.0) ? p : 1.0 - p;
-    if (r <= 0.0) return 0.0;
-    r = sqrt(-log(r));
-    float rh, rl, nh, nl, dh, dl;
-    if (r <= 5.0) {
-        df_split_nz(r - 1.6, rh, rl);
-        df_horner8(rh, rl, c, nh, nl);
-        df_horner8(rh, rl, d, dh, dl);
+    constexpr DfCoef c16 = dfc(1.6);
+    float rh, rl, xh, xl;
+    df_sqrt_neg_log(M, rh, rl);
+    float2 vh, vl;
+    if (rh < 5.0f || (rh == 5.0f && rl <= 0.0f)) {
+        df_add(rh, rl, -c16.h, -c16.l, xh, xl);
+        df_horner8x2(xh, xl, c, d, vh, vl);
     } else {
-        df_split_nz(r - 5.0, rh, rl);
-        df_horner8(rh, rl, e, nh, nl);
-        df_horner8(rh, rl, f, dh, dl);
+        df_add(rh, rl, -5.0f, 0.0f, xh, xl);
+        df_horner8x2(xh, xl, e, f, vh, vl);
     }
-    const double v = df_quotient(nh, nl, dh, dl);
-    return (q < 0.0) ? -v : v;
+    return df_quotient(vh.x, vl.x, vh.y, vl.y);
 }
 
 // FP32 evaluation of the same rational approximations (mixed-precision form).  The draw
@@ -411,7 +511,15 @@ __device__ __forceinline__ void increments_loop(const RngParams& prm, uint32_t* 
             divmod_u32((uint32_t)pos.y, (uint32_t)F, prm.magic_f, t, k);
             OutT val;
             if constexpr (kExact) {
-                val = icdf_tail((double)(int64_t)w * 0x1.0p-52) * __ldg(prm.sqrt_dt + t);
+                // the tail probability min(u, 1 - u) = M 2^-52 exactly; u = 0 gives 0 as in the reference
+                const int64_t m = (int64_t)w;
+                const bool lower = m < ((int64_t)1 << 51);
+                const int64_t M = lower ? m : ((int64_t)1 << 52) - m;
+                val = 0.0;
+                if (M > 0) {
+                    const double v = icdf_tail(M);
+                    val = (lower ? -v : v) * __ldg(prm.sqrt_dt + t);
+                }
             } else {
                 const uint32_t hi = (uint32_t)(w >> 32), lo = (uint32_t)w;
                 const bool lower = hi < (1u << 25);
