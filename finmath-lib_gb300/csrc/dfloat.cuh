@@ -143,4 +143,36 @@ __device__ __forceinline__ void df_split(double x, float& hi, float& lo)
 
 __device__ __forceinline__ double df_to_double(float hi, float lo) { return f32_to_f64_int(hi) + f32_to_f64_int(lo); }
 
+// binary32 -> binary64 in integer operations for normal floats and zero (subnormals become
+// zero; no infinity or NaN may reach it): no branch to the hardware conversion
+__device__ __forceinline__ double f32_to_f64_nz(float f)
+{
+    const unsigned b = __float_as_uint(f);
+    const unsigned e = (b >> 23) & 0xffu;
+    const unsigned hi = (b & 0x80000000u) | (e ? (((e + (1023u - 127u)) << 20) | ((b & 0x7fffffu) >> 3)) : 0u);
+    return __hiloint2double((int)hi, e ? (int)(b << 29) : 0);
+}
+
+// a double as hi + lo floats without an FP64 instruction: hi = x rounded to FP32 (as
+// f64_to_f32_small), lo = x - hi rounded to FP32, where x - hi is the signed integer D of
+// the 29 fraction bits rounded away (|D| <= 2^28) times x's last place 2^(e - 1075).  For
+// |x| in FP32's normal range; lo becomes zero where x's last place is below 2^-126.
+__device__ __forceinline__ void df_split_int(double x, float& hi, float& lo)
+{
+    const unsigned xh = (unsigned)__double2hiint(x), xl = (unsigned)__double2loint(x);
+    const int ex = (int)((xh >> 20) & 0x7ffu);
+    const int e = ex - 1023 + 127;
+    const unsigned m = ((xh & 0xfffffu) << 3) | (xl >> 29);
+    const unsigned rest = xl & 0x1fffffffu;
+    const bool up = rest > 0x10000000u || (rest == 0x10000000u && (m & 1u));
+    unsigned bits = (xh & 0x80000000u) | ((unsigned)(e > 0 ? e : 0) << 23) | m;
+    if (up) bits += 1u;
+    hi = __uint_as_float(e > 0 ? bits : (xh & 0x80000000u));
+    const int D = up ? (int)rest - (1 << 29) : (int)rest;           // |x| - |hi| in last places
+    const int se = ex - 1075 + 127;                                  // biased FP32 exponent of the last place
+    const float ulp = __uint_as_float(se > 0 ? (unsigned)se << 23 : 0u);
+    const float l = __int2float_rn(D) * ulp;                        // exact scaling by a power of two
+    lo = (xh & 0x80000000u) ? -l : l;
+}
+
 }  // namespace lmm

@@ -24,10 +24,13 @@
 //  * L / (L + 1/delta) is the FP32 reciprocal refined by one double-float Newton step;
 //  * the Euler-log step exp(log L + d) (EULER_FUNCTIONAL) is evaluated as L exp(d), and the
 //    EULER step exp(Y + d) as exp(Y) exp(d) with exp(Y) carried instead of Y, where exp(d)
-//    is the table method of exp_small (fp64math.cuh) with its argument reduction done in
-//    FP32 on the double-float d: nine FP64 instructions per component-step in all.
-// The increment d has an absolute error of a few 1e-16, so the states agree with the
-// reference's order to about 1e-14 relative, inside the 1e-12 parity bound.  The general
+//    is the table method of exp_small (fp64math.cuh) with its argument reduction and the
+//    polynomial of the reduced argument on float pairs (about 2^-48 relative): three FP64
+//    instructions per component-step in all (L times the table entry, times the pair);
+//  * L and the increments are split into float pairs in integer operations.
+// The increment d has an absolute error of a few 1e-16 and exp(r) about 2^-48 relative per
+// step, so the states agree with the reference's order to about 1e-13 relative, inside the
+// 1e-12 parity bound.  The general
 // kernel keeps the reference's literal order throughout (CUDA's exp/log, correctly rounded
 // division, unfused).
 #pragma once
@@ -144,7 +147,7 @@ __global__ void __launch_bounds__(kPathThreads, fp64_min_blocks(NMAX, FUNCTIONAL
         for (int k = 0; k < FMAX; k++) {
             Gp[k] = 0.0f;
             Gs[k] = 0.0f;
-            if (k < F && active) df_split(dW[((size_t)i * F + k) * P + p], Gp[k], Gs[k]);
+            if (k < F && active) df_split_int(dW[((size_t)i * F + k) * P + p], Gp[k], Gs[k]);
         }
         for_up_from<NMAX>(first, [&](auto jc) {
             constexpr int j = decltype(jc)::value;
@@ -165,7 +168,7 @@ __global__ void __launch_bounds__(kPathThreads, fp64_min_blocks(NMAX, FUNCTIONAL
                 // the FP32 reciprocal of L + 1/delta refined by one double-float Newton step
                 // (about 2^-44 relative; os enters only the drift, a small part of d)
                 float Lh, Ll;
-                df_split(Lj, Lh, Ll);
+                df_split_int(Lj, Lh, Ll);
                 float xh, xl;
                 two_sum(Lh, r[2 * FMAX + 2], xh, xl);
                 xl = xl + (Ll + r[2 * FMAX + 3]);
@@ -195,39 +198,41 @@ __global__ void __launch_bounds__(kPathThreads, fp64_min_blocks(NMAX, FUNCTIONAL
                     if (k & 1) df_dot_acc(ep, es, Gp[k], Gs[k], r[k], r[FMAX + k]);
                     else df_dot_acc(dp, ds, Gp[k], Gs[k], r[k], r[FMAX + k]);
                 }
-                // exp(d) by the table method of exp_small (fp64math.cuh): k = rint(256 d) and
-                // the exact remainder dh - k/256 formed in FP32, the reduced argument and its
-                // degree-5 polynomial in FP64
+                // exp(d) by the table method of exp_small (fp64math.cuh), k = rint(256 d): the
+                // remainder r = (dh - k/256) + dl (|r| <= 1/512, its high part exact in FP32)
+                // and exp(r) = 1 + r + r^2 B(r), B = 1/2 + r/6 + r^2/24 + r^3/120, as a float
+                // pair s + low (B - 1/2 in FP32: it enters times r^2 <= 2^-18); then
+                // L exp(k/256) (s + low) in three FP64 instructions
                 float dh, dl;
                 {
                     float x, q;
                     two_sum(dp, ep, x, q);
                     two_sum(x, (ds + es) + q, dh, dl);
                 }
-                double g;
+                const double base = FUNCTIONAL ? Lj : E[FUNCTIONAL ? 0 : j];
+                double nv;
                 if (fabsf(dh) <= 1.0f) {
                     const float t = fmaf(dh, (float)kExpTableHalf, 12582912.0f);  // 1.5 2^23 + rint(256 dh)
                     const int kk = __float_as_int(t) - 0x4b400000;
                     const float rh = fmaf(-(t - 12582912.0f), 1.0f / kExpTableHalf, dh);  // exact
-                    const double rr = df_to_double(rh, dl);
-                    double pp = 1.0 / 120.0;
-                    pp = fma(pp, rr, 1.0 / 24.0);
-                    pp = fma(pp, rr, 1.0 / 6.0);
-                    pp = fma(pp, rr, 0.5);
-                    pp = fma(pp, rr, 1.0);
-                    pp = fma(pp, rr, 1.0);
-                    g = __ldg(etab + kExpTableHalf + kk) * pp;
+                    const float r2h = __fmul_rn(rh, rh);
+                    const float r2e = fmaf(rh, rh, -r2h) + (rh + rh) * dl;  // r^2 - r2h
+                    const float bt = rh * fmaf(rh, fmaf(rh, 1.0f / 120.0f, 1.0f / 24.0f), 1.0f / 6.0f);
+                    const float th = 0.5f * r2h;                      // exact
+                    const float tl = fmaf(r2h, bt, 0.5f * r2e);
+                    const float s1 = 1.0f + rh;                       // |1| >= |rh|: fast TwoSum
+                    const float e1 = rh - (s1 - 1.0f);
+                    const float s2 = s1 + th;
+                    const float e2 = th - (s2 - s1);
+                    const float low = (e1 + e2) + (dl + tl);
+                    const double scaled = base * __ldg(etab + kExpTableHalf + kk);  // L exp(k/256)
+                    nv = fma(scaled, f32_to_f64_nz(low), scaled * f32_to_f64_nz(s2));
                 } else {
-                    g = exp(df_to_double(dh, dl));
+                    nv = base * exp(df_to_double(dh, dl));
                 }
                 // then L exp(d) (FUNCTIONAL: log L is the state) or exp(Y) exp(d) (EULER)
-                if (FUNCTIONAL) {
-                    L[j] = cap_positive(Lj * g, capbits);
-                } else {
-                    const double e = E[FUNCTIONAL ? 0 : j] * g;
-                    E[FUNCTIONAL ? 0 : j] = e;
-                    L[j] = cap_positive(e, capbits);
-                }
+                if (!FUNCTIONAL) E[FUNCTIONAL ? 0 : j] = nv;
+                L[j] = cap_positive(nv, capbits);
             }
         });
         const int slot = __ldg(a.d_obs_slot + i + 1);

@@ -134,16 +134,6 @@ __device__ __forceinline__ void df_horner8x2(float rh, float rl, const DfCoef (&
     }
 }
 
-// binary32 -> binary64 in integer operations for normal floats and zero (subnormals become
-// zero; no infinity or NaN reaches it)
-__device__ __forceinline__ double f32_to_f64_nz(float f)
-{
-    const unsigned b = __float_as_uint(f);
-    const unsigned e = (b >> 23) & 0xffu;
-    const unsigned hi = (b & 0x80000000u) | (e ? (((e + (1023u - 127u)) << 20) | ((b & 0x7fffffu) >> 3)) : 0u);
-    return __hiloint2double((int)hi, e ? (int)(b << 29) : 0);
-}
-
 // a double as hi + lo floats (hi rounded in integer operations, lo the rounded remainder of
 // one exact FP64 subtraction)
 __device__ __forceinline__ void df_split_nz(double x, float& hi, float& lo)
