@@ -117,6 +117,26 @@ __device__ __forceinline__ void df_dot_acc(float& p, float& s, float ah, float a
     s = s + (q + r);
 }
 
+// df_dot_acc for two lanes at once on the paired FP32 pipe (the same operations, lane by
+// lane): bn = -bh; subtractions as fused multiply-adds with -1, which round once like the
+// subtraction itself, so every lane's result equals df_dot_acc's bit for bit
+__device__ __forceinline__ void df_dot_acc2(float2& p, float2& s, float2 ah, float2 al, float2 bh, float2 bl, float2 bn)
+{
+    const float2 M1 = make_float2(-1.0f, -1.0f);
+    const float2 hn = __fmul2_rn(ah, bn);   // -h, h = ah bh rounded
+    float2 r = __ffma2_rn(ah, bh, hn);      // ah bh - h, exactly
+    r = __ffma2_rn(ah, bl, r);
+    r = __ffma2_rn(al, bh, r);
+    const float2 x = __ffma2_rn(hn, M1, p); // p + h
+    const float2 z = __ffma2_rn(p, M1, x);  // x - p
+    const float2 t = __ffma2_rn(z, M1, x);  // x - z
+    const float2 u = __ffma2_rn(t, M1, p);  // p - (x - z)
+    const float2 v = __fadd2_rn(hn, z);     // z - h
+    const float2 q = __ffma2_rn(v, M1, u);  // (p - (x - z)) + (h - z): TwoSum's error
+    p = x;
+    s = __fadd2_rn(s, __fadd2_rn(q, r));
+}
+
 // binary64 -> binary32 for values whose magnitude lies in FP32's normal range or below it
 // (the forward rates, increments and their remainders): round to nearest even in integer
 // operations only -- magnitudes below FP32's normal range become a signed zero, and nothing

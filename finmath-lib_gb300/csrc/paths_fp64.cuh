@@ -20,7 +20,8 @@
 // relative, dfloat.cuh):
 //  * the drift's running sums S_k carry dt and the increments dW_k along (G_k = dW_k +
 //    dt S_k), as double-float pairs, so that a component costs 2F double-float multiply-adds
-//    (Dot2 steps: 12 FP32 instructions each) and no FP64 multiply-add;
+//    (Dot2 steps: 12 FP32 instructions each, two factors at once on paired FP32
+//    instructions) and no FP64 multiply-add;
 //  * L / (L + 1/delta) is the FP32 reciprocal refined by one double-float Newton step;
 //  * the Euler-log step exp(log L + d) (EULER_FUNCTIONAL) is evaluated as L exp(d), and the
 //    EULER step exp(Y + d) as exp(Y) exp(d) with exp(Y) carried instead of Y, where exp(d)
@@ -45,6 +46,11 @@ namespace lmm {
 namespace {
 
 constexpr int kPathThreads = 128;
+
+// a component index known only at run time, for the rolled component loop
+struct RuntimeIndex {
+    int value;
+};
 
 // v capped at the bit pattern capbits of a positive cap: for v >= 0 (exp's range) the IEEE
 // order is the integer order of the bit patterns, so the comparison needs no FP64
@@ -87,12 +93,13 @@ __host__ __device__ constexpr int fp64_min_blocks(int nmax, bool functional)
 }
 
 // EXACT: the model has exactly NMAX components, so the component loop carries no bound
-// checks; the loop enters its unrolled sequence at the first alive component through a jump
-// table (unroll_range.cuh), so the compiler sees one straight-line block per step and can
-// overlap the components' independent work (the os_j and the increments' dot products).
+// checks.  With the state in registers the loop enters its unrolled sequence at the first
+// alive component through a jump table (unroll_range.cuh); with the state in shared memory
+// it is a rolled loop.
 template <int NMAX, int FMAX, bool FUNCTIONAL, bool EXACT>
 __global__ void __launch_bounds__(kPathThreads, fp64_min_blocks(NMAX, FUNCTIONAL)) paths_fp64_kernel(const PathLaunch a)
 {
+    static_assert(FMAX % 2 == 0, "factors run in pairs");
     constexpr int FPD = fp64_df_pitch(FMAX);
     constexpr bool SMEM = fp64_state_in_smem(NMAX, FUNCTIONAL);
     const int p = blockIdx.x * kPathThreads + threadIdx.x;
@@ -142,15 +149,18 @@ __global__ void __launch_bounds__(kPathThreads, fp64_min_blocks(NMAX, FUNCTIONAL
         // (:1156-1158), carried as double-float pairs (Gp + Gs): the step increment of
         // component j is then  d_j = mu_j dt + sum_k dW_k lambda_jk = sum_k G_k lambda_jk
         // - dt variance_j / 2, two double-float multiply-adds per factor on the FP32 pipe
-        float Gp[FMAX], Gs[FMAX];
+        // factor pairs (2m, 2m+1) side by side in the lanes of float2 registers
+        float2 Gh[FMAX / 2], Gl[FMAX / 2];
 #pragma unroll
-        for (int k = 0; k < FMAX; k++) {
-            Gp[k] = 0.0f;
-            Gs[k] = 0.0f;
-            if (k < F && active) df_split_int(dW[((size_t)i * F + k) * P + p], Gp[k], Gs[k]);
+        for (int m = 0; m < FMAX / 2; m++) {
+            float h0 = 0.0f, l0 = 0.0f, h1 = 0.0f, l1 = 0.0f;
+            if (2 * m < F && active) df_split_int(dW[((size_t)i * F + 2 * m) * P + p], h0, l0);
+            if (2 * m + 1 < F && active) df_split_int(dW[((size_t)i * F + 2 * m + 1) * P + p], h1, l1);
+            Gh[m] = make_float2(h0, h1);
+            Gl[m] = make_float2(l0, l1);
         }
-        for_up_from<NMAX>(first, [&](auto jc) {
-            constexpr int j = decltype(jc)::value;
+        auto component_step = [&](auto jc) {
+            const int j = jc.value;
             if (EXACT || j < N) {
                 // the component's row: loadings (hi, lo), the drift term (variance * -0.5) * dt
                 // and 1/delta, each as a double-float pair
@@ -188,16 +198,20 @@ __global__ void __launch_bounds__(kPathThreads, fp64_min_blocks(NMAX, FUNCTIONAL
                 qe = fmaf(oh, dtl, qe);
                 qe = fmaf(oe, dth, qe);
                 // Euler step (EulerSchemeFromProcessModel.java:235-255) with the drift of
-                // :1159 and :1183-1189: the increment d of the log state
-                // two independent accumulators (even and odd factors) halve the dependency
-                // chain of the dot product; the rows are zero beyond F, so padded factors add 0
-                float dp = r[2 * FMAX], ds = r[2 * FMAX + 1], ep = 0.0f, es = 0.0f;
+                // :1159 and :1183-1189: the increment d of the log state.  Two accumulators,
+                // even factors in lane x (started at the drift term) and odd ones in lane y, on
+                // paired instructions; the rows are zero beyond F, so padded factors add 0
+                float2 acc_h = make_float2(r[2 * FMAX], 0.0f), acc_l = make_float2(r[2 * FMAX + 1], 0.0f);
+                const float2 q2h = make_float2(qh, qh), q2l = make_float2(qe, qe);
 #pragma unroll
-                for (int k = 0; k < FMAX; k++) {
-                    df_dot_acc(Gp[k], Gs[k], qh, qe, r[k], r[FMAX + k]);
-                    if (k & 1) df_dot_acc(ep, es, Gp[k], Gs[k], r[k], r[FMAX + k]);
-                    else df_dot_acc(dp, ds, Gp[k], Gs[k], r[k], r[FMAX + k]);
+                for (int m = 0; m < FMAX / 2; m++) {
+                    const float2 bh = make_float2(r[2 * m], r[2 * m + 1]);
+                    const float2 bl = make_float2(r[FMAX + 2 * m], r[FMAX + 2 * m + 1]);
+                    const float2 bn = __fmul2_rn(bh, make_float2(-1.0f, -1.0f));
+                    df_dot_acc2(Gh[m], Gl[m], q2h, q2l, bh, bl, bn);      // G_k += os dt lambda_k
+                    df_dot_acc2(acc_h, acc_l, Gh[m], Gl[m], bh, bl, bn);  // d += G_k lambda_k
                 }
+                const float dp = acc_h.x, ep = acc_h.y, ds = acc_l.x, es = acc_l.y;
                 // exp(d) by the table method of exp_small (fp64math.cuh), k = rint(256 d): the
                 // remainder r = (dh - k/256) + dl (|r| <= 1/512, its high part exact in FP32)
                 // and exp(r) = 1 + r + r^2 B(r), B = 1/2 + r/6 + r^2/24 + r^3/120, as a float
@@ -234,7 +248,16 @@ __global__ void __launch_bounds__(kPathThreads, fp64_min_blocks(NMAX, FUNCTIONAL
                 if (!FUNCTIONAL) E[FUNCTIONAL ? 0 : j] = nv;
                 L[j] = cap_positive(nv, capbits);
             }
-        });
+        };
+        if constexpr (SMEM) {
+            // the state lives in shared memory: a rolled loop keeps the step's code inside the
+            // instruction cache (the unrolled sequence of 40 components did not fit, and its
+            // instruction-fetch stalls cost a third of the kernel's time)
+#pragma unroll 1
+            for (int j = first; j < N; j++) component_step(RuntimeIndex{j});
+        } else {
+            for_up_from<NMAX>(first, component_step);
+        }
         const int slot = __ldg(a.d_obs_slot + i + 1);
         if (slot >= 0 && active) {
 #pragma unroll
