@@ -223,7 +223,7 @@ struct lmm_process {
     // results
     void* d_states = nullptr;
     double *d_numeraire = nullptr, *d_partials = nullptr, *d_num_adj = nullptr;
-    double* d_inv_numeraire = nullptr;  // kept for the adjoint (allocated with the checkpoints)
+    double* d_inv_numeraire = nullptr;  // [N+1][P] 1/N per path, written by the path kernels
     int path_blocks = 0;
     bool simulated = false;
     uint64_t bm_generation = 0;  // Brownian generation the results were simulated from
@@ -663,11 +663,10 @@ static int process_ensure(lmm_process* pr)
         a.d_ckpt = pr->d_ckpt;
         a.ckpt_stride = pr->want_ckpt;
     }
-    // 1/N per path: read by the adjoint seeds, and by the mixed form's products (no divisions)
-    if (pr->want_ckpt > 0 || pr->precision == LMM_PRECISION_MIXED) {
-        if (!pr->d_inv_numeraire && (rc = dalloc(&pr->d_inv_numeraire, (size_t)(pr->N + 1) * pr->P, s))) return rc;
-        a.d_inv_numeraire = pr->d_inv_numeraire;
-    }
+    // 1/N per path: read by the adjoint seeds and by the Bermudan's backward induction
+    // (no division per path)
+    if (!pr->d_inv_numeraire && (rc = dalloc(&pr->d_inv_numeraire, (size_t)(pr->N + 1) * pr->P, s))) return rc;
+    a.d_inv_numeraire = pr->d_inv_numeraire;
     int blocks = 0;
     rc = pr->precision == LMM_PRECISION_FP64 ? launch_paths_fp64(a, s, &blocks)
                                               : launch_paths_fp32(a, pr->d_lam32, s, &blocks);
@@ -835,7 +834,7 @@ static ProductView product_view(lmm_process* pr)
     v.d_states = pr->d_states;
     v.h_obs_slot = pr->obs_slot.data();
     v.d_numeraire = pr->d_numeraire;
-    v.d_inv_numeraire = pr->precision == LMM_PRECISION_MIXED ? pr->d_inv_numeraire : nullptr;
+    v.d_inv_numeraire = pr->d_inv_numeraire;
     v.d_num_adj = pr->d_num_adj;
     v.h_discount = pr->has_discount ? pr->discount.data() : nullptr;
     v.h_num_det = pr->num_det.data();

@@ -470,12 +470,15 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp64_general_kernel(const 
     } else if (active && __ldg(a.d_tenor_tidx + N) > a.T) {
         a.d_numeraire[(size_t)N * P + p] = 1.0;
     }
-    // block partials of N(T_l)^-1 * N(0) for the numeraire adjustment (:869-874)
+    // block partials of N(T_l)^-1 * N(0) for the numeraire adjustment (:869-874), and 1/N
+    // per path for the products
     const double N0 = active ? a.d_numeraire[p] : 1.0;
+    if (a.d_inv_numeraire && active) a.d_inv_numeraire[p] = 1.0 / N0;
 #pragma unroll 1
     for (int l = 1; l <= N; l++) {
-        const double inv = active ? (1.0 / a.d_numeraire[(size_t)l * P + p]) * N0 : 0.0;
-        block_dd_partial(inv, a.d_inv_num_partials + ((size_t)blockIdx.x * N + (l - 1)) * 2);
+        const double r = active ? 1.0 / a.d_numeraire[(size_t)l * P + p] : 0.0;
+        if (a.d_inv_numeraire && active) a.d_inv_numeraire[(size_t)l * P + p] = r;
+        block_dd_partial(active ? r * N0 : 0.0, a.d_inv_num_partials + ((size_t)blockIdx.x * N + (l - 1)) * 2);
     }
 }
 

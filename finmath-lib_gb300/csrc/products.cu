@@ -27,7 +27,7 @@ struct NumeraireInfo {
     int has_discount;
     const double* numeraire;   // [N+1][P] unadjusted
     const double* adj;         // [N+1] mean of 1/N (device)
-    const double* inv_numeraire;  // [N+1][P] 1/N (mixed form; else nullptr)
+    const double* inv_numeraire;  // [N+1][P] 1/N from the path kernel (or nullptr)
     double pd[kMaxN + 1];      // P^d(T_l)
     double inv_pd[kMaxN + 1];  // 1 / P^d(T_l)
     unsigned char det[kMaxN + 1];
@@ -267,6 +267,94 @@ __device__ __forceinline__ void bermudan_basis32(const BermShared& a, const Berm
     }
 }
 
+// FP64 form, swap-rate basis: the par rate S = (prod g_q - 1) / H of the remaining periods
+// by the same forward recursion on float pairs (FP32 pipe): the forwards split into pairs in
+// integer operations, the period lengths staged as pairs; g = 1 + L d, prod <- prod g,
+// H <- H g + d as double-float products and sums (about 2^-47 relative a step).  The basis
+// enters only the regression that estimates the continuation value, so its error moves
+// the exercise decisions of paths within ~1e-13 of the boundary only; the adjusted
+// numeraire is N times the date's uniform factor adjustment / P^d.
+struct SwapRowsDf {
+    int idx[kMaxN];
+    float len_h[kMaxN], len_l[kMaxN];
+};
+
+__device__ __forceinline__ void df_mul_pair(float ah, float al, float bh, float bl, float& ph, float& pl)
+{
+    const float p = __fmul_rn(ah, bh);
+    float e = fmaf(ah, bh, -p);
+    e = fmaf(ah, bl, e);
+    e = fmaf(al, bh, e);
+    ph = p + e;  // |e| is far below |p|: the renormalised pair
+    pl = e - (ph - p);
+}
+
+__device__ __forceinline__ void df_add_pair(float ah, float al, float bh, float bl, float& sh, float& sl)
+{
+    float s, e;
+    two_sum(ah, bh, s, e);
+    const float t = (al + bl) + e;
+    sh = s + t;
+    sl = t - (sh - s);
+}
+
+__device__ __forceinline__ void bermudan_basis_swaprate_df(const BermShared& a, const BermudanPeriod& c, int p,
+                                                           const SwapRowsDf* rows, double nfac, double B[5])
+{
+    const double* st = static_cast<const double*>(a.states) + (size_t)c.ex_slot * a.N * a.P + p;
+    const int nq = c.swap_last - c.swap_first;
+    float ph = 1.0f, pl = 0.0f, hh = 0.0f, hl = 0.0f;
+    for (int q0 = 0; q0 < nq; q0 += 8) {
+        double Lb[8];  // eight independent loads in flight per thread
+#pragma unroll
+        for (int k = 0; k < 8; k++) Lb[k] = q0 + k < nq ? st[(size_t)rows->idx[q0 + k] * a.P] : 0.0;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const int q = q0 + k;
+            if (q < nq) {
+                float Lh, Ll;
+                df_split_int(Lb[k], Lh, Ll);
+                const float dh = rows->len_h[q], dl = rows->len_l[q];
+                // g = 1 + L d: the product's exact error, then 1 + x with |x| < 1
+                const float x = __fmul_rn(Lh, dh);
+                float xe = fmaf(Lh, dh, -x);
+                xe = fmaf(Lh, dl, xe);
+                xe = fmaf(Ll, dh, xe);
+                const float gh0 = 1.0f + x;
+                const float gl0 = (x - (gh0 - 1.0f)) + xe;
+                if (q == 0) {
+                    ph = gh0;
+                    pl = gl0;
+                    hh = dh;
+                    hl = dl;
+                } else {
+                    df_mul_pair(ph, pl, gh0, gl0, ph, pl);
+                    float th, tl;
+                    df_mul_pair(hh, hl, gh0, gl0, th, tl);
+                    df_add_pair(th, tl, dh, dl, hh, hl);
+                }
+            }
+        }
+    }
+    // S = (prod - 1) / H
+    float nh, nl;
+    df_add_pair(ph, pl, -1.0f, 0.0f, nh, nl);
+    const float yh = __fdiv_rn(nh, hh);
+    const float pr = __fmul_rn(yh, hh);
+    const float pe = fmaf(yh, hh, -pr);
+    float res = (nh - pr) - pe;
+    res = res + nl;
+    res = fmaf(-yh, hl, res);
+    const float yl = __fmul_rn(res, __frcp_rn(hh));
+    const double S = f32_to_f64_nz(yh) + f32_to_f64_nz(yl);
+    const double Nn = a.num.numeraire[(size_t)c.ex_num_index * a.P + p] * nfac;
+    B[0] = S;
+    B[1] = S * S;
+    B[2] = Nn;
+    B[3] = Nn * Nn;
+    B[4] = S * Nn;
+}
+
 // grid (bx, ne): basis functions of exercise date blockIdx.y and their Gram partial sums
 template <typename TS>
 __global__ void __launch_bounds__(kProdThreads, sizeof(TS) == 4 ? 3 : 1) bermudan_gram_kernel(const BermShared a, double* partials)
@@ -313,35 +401,42 @@ __global__ void __launch_bounds__(kProdThreads, sizeof(TS) == 4 ? 3 : 1) bermuda
         block_sums_warp_plain<kGram>(acc, partials + ((size_t)e * gridDim.x + blockIdx.x) * kGram * 2, 1);
         return;
     }
+    // FP64 form: the swap-rate basis on float pairs (above), the reference basis in FP64;
+    // the Gram sums by fused multiply-adds, plain within a thread and a warp, compensated
+    // across warps and blocks
+    __shared__ SwapRowsDf rows;
+    __shared__ double nfac_d;
+    if (a.basis == 1) {
+        for (int q = threadIdx.x; q < c.swap_last - c.swap_first; q += blockDim.x) {
+            const double d = a.period_length[c.swap_first + q];
+            rows.idx[q] = a.period_index[c.swap_first + q];
+            rows.len_h[q] = (float)d;
+            rows.len_l[q] = (float)(d - (double)rows.len_h[q]);
+        }
+        if (threadIdx.x == 0) {
+            const int l = c.ex_num_index;
+            nfac_d = a.num.has_discount ? a.num.adj[l] / a.num.pd[l] : 1.0;
+        }
+        __syncthreads();
+    }
 #pragma unroll
     for (int k = 0; k < kGram; k++) acc[k] = 0.0;
     double* bb = a.basis_buf + (size_t)e * 5 * a.P;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.P; p += gridDim.x * blockDim.x) {
         double B[5];
-        bermudan_basis<TS>(a, c, p, B);
+        if (a.basis == 1) bermudan_basis_swaprate_df(a, c, p, &rows, nfac_d, B);
+        else bermudan_basis<TS>(a, c, p, B);
 #pragma unroll
         for (int i = 0; i < 5; i++) bb[(size_t)i * a.P + p] = B[i];
-        int k = 0;
 #pragma unroll
-        for (int i = 0; i < 5; i++) acc[k + i] = acc[k + i] + B[i];  // mean(1 * B_i)
-        k += 5;
+        for (int i = 0; i < 5; i++) acc[i] = acc[i] + B[i];  // mean(1 * B_i)
+        int k = 5;
 #pragma unroll
         for (int i = 0; i < 5; i++)
 #pragma unroll
-            for (int j = i; j < 5; j++) {
-                acc[k] = acc[k] + B[i] * B[j];  // the product rounds first, as the reference's
-                k++;
-            }
+            for (int j = i; j < 5; j++, k++) acc[k] = fma(B[i], B[j], acc[k]);
     }
-#pragma unroll
-    for (int k = 0; k < kGram; k++) {
-        const dd s = block_dd_sum(dd{acc[k], 0.0});
-        if (threadIdx.x == 0) {
-            double* q = partials + (((size_t)e * gridDim.x + blockIdx.x) * kGram + k) * 2;
-            q[0] = s.hi;
-            q[1] = s.lo;
-        }
-    }
+    block_sums_warp_plain<kGram>(acc, partials + ((size_t)e * gridDim.x + blockIdx.x) * kGram * 2, 1);
 }
 
 __device__ void svd6(const double G[36], double U[36], double s[6], double V[36])
@@ -530,11 +625,22 @@ __device__ void finish_date_last_block(const BermStepParams& a, bool mixed)
     }
 }
 
-// FP64 form: the reference's arithmetic and order (BermudanSwaption.java:91-157).
+// FP64 form: the reference's backward induction (BermudanSwaption.java:91-157) with fused
+// multiply-adds for X beta and X^T y, and the payoff times the path's reciprocal numeraire
+// (from the path kernel) and the date's uniform factor P^d / adjustment instead of a
+// division per path.
 __global__ void __launch_bounds__(kProdThreads) bermudan_step_kernel(const BermStepParams a)
 {
     const BermShared& sh = a.sh;
     const double w = 1.0 / (double)sh.P;
+    __shared__ double pay_fac;  // (P^d / adjustment) w of the payment date, once per block
+    if (a.cur >= 0 && sh.num.inv_numeraire) {
+        if (threadIdx.x == 0) {
+            const int l = sh.per[a.cur].pay_num_index;
+            pay_fac = sh.num.has_discount ? (sh.num.pd[l] / sh.num.adj[l]) * w : w;
+        }
+        __syncthreads();
+    }
     double acc[kRhs];
 #pragma unroll
     for (int i = 0; i < kRhs; i++) acc[i] = 0.0;
@@ -560,9 +666,9 @@ __global__ void __launch_bounds__(kProdThreads) bermudan_step_kernel(const BermS
         }
         if (bprev) {
             // conditional expectation X beta (:104-107), then choose (:139, :141)
-            double ce = 1.0 * beta[0];
+            double ce = beta[0];
 #pragma unroll
-            for (int i = 1; i < 6; i++) ce = ce + bprev[(size_t)(i - 1) * sh.P + p] * beta[i];
+            for (int i = 1; i < 6; i++) ce = fma(bprev[(size_t)(i - 1) * sh.P + p], beta[i], ce);
             const bool cont = ce >= 0.0;
             if (a.rec) {
                 a.rec[(size_t)a.pending_ex * sh.P + p] = ce;
@@ -574,15 +680,19 @@ __global__ void __launch_bounds__(kProdThreads) bermudan_step_kernel(const BermS
         if (a.cur >= 0) {
             const double L = state_at<double>(sh.states, c.libor_slot, sh.N, sh.P, c.libor_index, p);
             double payoff = ((L - c.strike) * c.period_length) * c.notional;
-            payoff = payoff / numeraire_adj(sh.num, c.pay_num_index, p);
-            payoff = payoff * w;
+            if (sh.num.inv_numeraire) {
+                payoff = payoff * (sh.num.inv_numeraire[(size_t)c.pay_num_index * sh.P + p] * pay_fac);
+            } else {
+                payoff = payoff / numeraire_adj(sh.num, c.pay_num_index, p);
+                payoff = payoff * w;
+            }
             if (sh.callable) u = u + payoff;
             else v = v + payoff;
             if (bcur) {
                 const double y = v - u;
-                acc[0] = acc[0] + y * 1.0;
+                acc[0] = acc[0] + y;
 #pragma unroll
-                for (int i = 0; i < 5; i++) acc[1 + i] = acc[1 + i] + y * bcur[(size_t)i * sh.P + p];
+                for (int i = 0; i < 5; i++) acc[1 + i] = fma(y, bcur[(size_t)i * sh.P + p], acc[1 + i]);
             }
         } else {
             v = (v * numeraire_adj(sh.num, 0, 0)) / w;  // numeraire at time 0 (exactly 1 under SPOT)
