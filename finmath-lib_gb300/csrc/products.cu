@@ -43,22 +43,6 @@ __device__ __forceinline__ double numeraire_adj(const NumeraireInfo& n, int l, i
     return (Nu * a) / n.pd[l];
 }
 
-// Mixed form only: N_adj = N (a / P^d) and 1/N_adj = (1/N) (P^d / a) with the per-date
-// factor uniform across paths, so no division per path.
-__device__ __forceinline__ double numeraire_adj_mixed(const NumeraireInfo& n, int l, int p)
-{
-    const double Nu = n.numeraire[(size_t)l * n.P + p];
-    if (!n.has_discount) return Nu;
-    return Nu * (n.adj[l] * n.inv_pd[l]);
-}
-__device__ __forceinline__ double inv_numeraire_adj_mixed(const NumeraireInfo& n, int l, int p)
-{
-    if (!n.inv_numeraire) return 1.0 / numeraire_adj_mixed(n, l, p);
-    const double iN = n.inv_numeraire[(size_t)l * n.P + p];
-    if (!n.has_discount) return iN;
-    return iN * (n.pd[l] / n.adj[l]);
-}
-
 template <typename TS>
 __device__ __forceinline__ double state_at(const void* states, int slot, int N, int P, int j, int p)
 {
@@ -701,14 +685,8 @@ __global__ void __launch_bounds__(kProdThreads) bermudan_step_kernel(const BermS
         a.under[p] = u;
     }
     if (bcur) {
-#pragma unroll
-        for (int i = 0; i < kRhs; i++) {
-            const dd s = block_dd_sum(dd{acc[i], 0.0});
-            if (threadIdx.x == 0) {
-                a.partials[((size_t)blockIdx.x * kRhs + i) * 2] = s.hi;
-                a.partials[((size_t)blockIdx.x * kRhs + i) * 2 + 1] = s.lo;
-            }
-        }
+        // plain within a warp (a thread holds a few paths' sums), compensated across warps
+        block_sums_warp_plain<kRhs>(acc, a.partials + (size_t)blockIdx.x * kRhs * 2, 1);
         finish_date_last_block(a, false);
     }
 }
@@ -1096,14 +1074,7 @@ __global__ void __launch_bounds__(kProdThreads) dd_sweep_kernel(const DdSweepPar
         a.ubar[p] = ub;
     }
     if (bcur) {
-#pragma unroll
-        for (int i = 0; i < kRhs; i++) {
-            const dd s = block_dd_sum(dd{acc[i], 0.0});
-            if (threadIdx.x == 0) {
-                a.partials[((size_t)blockIdx.x * kRhs + i) * 2] = s.hi;
-                a.partials[((size_t)blockIdx.x * kRhs + i) * 2 + 1] = s.lo;
-            }
-        }
+        block_sums_warp_plain<kRhs>(acc, a.partials + (size_t)blockIdx.x * kRhs * 2, 1);
         __shared__ bool last;
         __threadfence();
         __syncthreads();
