@@ -47,10 +47,16 @@ void eigen_symmetric(int n, const double* Ain, std::vector<double>& ev, std::vec
                 else diag += a * a;
             }
         if (off <= 1e-300 || off <= 1e-34 * diag) break;
+        // an element below 2^-53 of the diagonal norm is rounding noise: rotating it changes
+        // nothing the factor matrix keeps, and a sweep without a rotation ends the iteration
+        // (rank-deficient and clustered spectra otherwise never meet the relative criterion)
+        const double tiny = 0x1.0p-53 * std::sqrt(diag);
+        bool rotated = false;
         for (int p = 0; p < n - 1; p++)
             for (int q = p + 1; q < n; q++) {
                 const double apq = A[(size_t)p * n + q];
-                if (apq == 0.0) continue;
+                if (apq == 0.0 || std::fabs(apq) <= tiny) continue;
+                rotated = true;
                 const double theta = (A[(size_t)q * n + q] - A[(size_t)p * n + p]) / (2.0 * apq);
                 const double t = (theta >= 0.0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
                 const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
@@ -70,6 +76,7 @@ void eigen_symmetric(int n, const double* Ain, std::vector<double>& ev, std::vec
                     V[(size_t)k * n + q] = s * vkp + c * vkq;
                 }
             }
+        if (!rotated) break;
     }
     for (int i = 0; i < n; i++) ev[i] = A[(size_t)i * n + i];
 }

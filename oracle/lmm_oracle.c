@@ -246,10 +246,17 @@ int orc_eigen_symmetric(int n, const double* Ain, double* evals, double* V)
                 else diag += A[i * n + i] * A[i * n + i];
             }
         if (off <= 1e-300 || off <= 1e-34 * diag) break;
+        /* an element below 2^-53 of the matrix's diagonal norm is rounding noise: rotating
+         * it changes nothing the factor matrix keeps, and a sweep without a rotation ends
+         * the iteration (rank-deficient and clustered spectra otherwise never meet the
+         * relative criterion above) */
+        const double tiny = 0x1.0p-53 * sqrt(diag);
+        int rotated = 0;
         for (int p = 0; p < n - 1; p++)
             for (int q = p + 1; q < n; q++) {
                 double apq = A[p * n + q];
-                if (apq == 0.0) continue;
+                if (apq == 0.0 || fabs(apq) <= tiny) continue;
+                rotated = 1;
                 double app = A[p * n + p], aqq = A[q * n + q];
                 double theta = (aqq - app) / (2.0 * apq);
                 double t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
@@ -270,6 +277,7 @@ int orc_eigen_symmetric(int n, const double* Ain, double* evals, double* V)
                     V[k * n + q] = s * vkp + c * vkq;
                 }
             }
+        if (!rotated) break;
     }
     for (int i = 0; i < n; i++) evals[i] = A[i * n + i];
     free(A);
