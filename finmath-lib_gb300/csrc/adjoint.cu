@@ -114,6 +114,7 @@ struct RevParams {
     int base_step;       // states[] holds the steps base_step, base_step+1, ...
     int seed;            // 1: start from the seeds at t_end, else from ybar
     int capped;
+    int normal;          // NORMAL state space: the state is L itself (else log L)
     double cap;
     const int* first;     // [T]
     const double* init;   // [N]
@@ -255,8 +256,13 @@ __global__ void __launch_bounds__(TH, rev_min_blocks<R, TH>()) reverse_kernel(co
             for (int j = 0; j < NMAX; j++) {
                 R yb = R(0);
                 if (j < NE && active) {
-                    const R L = Ls[(size_t)j * a.P + p];
-                    if (!(a.capped && L >= cap)) yb = static_cast<const R*>(a.seeds)[(size_t)j * a.P + p] * L;
+                    const R sd = static_cast<const R*>(a.seeds)[(size_t)j * a.P + p];
+                    if (a.normal) {
+                        yb = sd;  // the state is L: its adjoint is the seed
+                    } else {
+                        const R L = Ls[(size_t)j * a.P + p];
+                        if (!(a.capped && L >= cap)) yb = sd * L;
+                    }
                 }
                 Ybar[j] = yb;
             }
@@ -293,7 +299,8 @@ __global__ void __launch_bounds__(TH, rev_min_blocks<R, TH>()) reverse_kernel(co
                 if (j < NE && j >= first) {
                     const R L = active ? sbuf[j * TH] : R(0);
                     if (a.capped && L >= cap) capmask |= 1ull << j;
-                    const R o = fdiv<R>(L, L + tb.inv_delta[j]);
+                    // os_j = L/(L + 1/d) (LOGNORMAL) or d/(1 + d L) = 1/(L + 1/d) (NORMAL)
+                    const R o = fdiv<R>(a.normal ? R(1) : L, L + tb.inv_delta[j]);
                     if (kKeepOs) os[kKeepOs ? j : 0] = o;
                     const R oss = o * sig[j];
                     R fr[FP];
@@ -316,7 +323,7 @@ __global__ void __launch_bounds__(TH, rev_min_blocks<R, TH>()) reverse_kernel(co
                         o = os[kKeepOs ? j : 0];
                     } else {
                         const R L = active ? sbuf[j * TH] : R(0);
-                        o = fdiv<R>(L, L + tb.inv_delta[j]);
+                        o = fdiv<R>(a.normal ? R(1) : L, L + tb.inv_delta[j]);
                     }
                     const R sg = sig[j];
                     const R yb = Ybar[j];
@@ -340,9 +347,12 @@ __global__ void __launch_bounds__(TH, rev_min_blocks<R, TH>()) reverse_kernel(co
                     const R A = A2.x + A2.y, B = B2.x + B2.y, D = D2.x + D2.y;
                     // sigmabar_ij = sum_k lambar_jk f_jk - mubar_j sigma_ij with
                     // lambar_jk = mubar_j S_k + os_j R_k + Ybar'_j dW_k
-                    red[j * RS + lane] = active ? (mub * B + o * A + yb * D - mubs) : R(0);
-                    // osbar_j = sigma_j A;  d os_j / d Y_j = os_j (1 - os_j) (zero where capped)
-                    if (!(a.capped && ((capmask >> j) & 1ull))) Ybar[j] = yb + (sg * A) * (o * (R(1) - o));
+                    // (NORMAL: no -variance/2 drift term, so no -mubar_j sigma_ij)
+                    red[j * RS + lane] = active ? (mub * B + o * A + yb * D - (a.normal ? R(0) : mubs)) : R(0);
+                    // osbar_j = sigma_j A;  d os_j / d Y_j = os_j (1 - os_j) (LOGNORMAL, zero where
+                    // capped), d os_j / d L_j = -os_j^2 (NORMAL)
+                    if (a.normal) Ybar[j] = yb - (sg * A) * (o * o);
+                    else if (!(a.capped && ((capmask >> j) & 1ull))) Ybar[j] = yb + (sg * A) * (o * (R(1) - o));
                 }
             }
             if (!kKeepOs && n - 1 >= a.n_lo) prefetch(n - 1);
@@ -362,7 +372,8 @@ __global__ void __launch_bounds__(TH, rev_min_blocks<R, TH>()) reverse_kernel(co
                 if (j < NE && active) yb[(size_t)j * a.P + p] = Ybar[j];
         } else {
             // deltas: Y_0 = log(L_0(0)) -> d value / d L_0 = Ybar / L_0, the uniform division
-            // applied to the warp's sum (one division per component and warp, not per path)
+            // applied to the warp's sum (one division per component and warp, not per path);
+            // NORMAL: the state is L_0 itself
 #pragma unroll
             for (int j = 0; j < NMAX; j++)
                 if (j < NE) red[j * RS + lane] = active ? Ybar[j] : R(0);
@@ -370,7 +381,7 @@ __global__ void __launch_bounds__(TH, rev_min_blocks<R, TH>()) reverse_kernel(co
 #pragma unroll
             for (int h = 0; h < (NMAX + 31) / 32; h++) {
                 const int r = lane + 32 * h;
-                if (r < NE) atomicAdd(a.delta_partials + gw * N + r, row_sum<R>(red, r) / a.init[r]);
+                if (r < NE) atomicAdd(a.delta_partials + gw * N + r, a.normal ? row_sum<R>(red, r) : row_sum<R>(red, r) / a.init[r]);
             }
             __syncwarp();
         }
@@ -381,7 +392,7 @@ __global__ void __launch_bounds__(TH, rev_min_blocks<R, TH>()) reverse_kernel(co
 // Replays the Euler-log steps [n0, n_stop) of every path from the checkpoint at n0 (forward
 // rates) and stores the forward rates of the steps n0..n_stop in seg[0..n_stop-n0].
 struct ReplayParams {
-    int T, N, F, P, n0, n_stop, n_eff, capped;
+    int T, N, F, P, n0, n_stop, n_eff, capped, normal;
     double cap;
     const int* first;
     const void* ckpt_slot;  // [N][P] forward rates at n0
@@ -402,7 +413,7 @@ __global__ void __launch_bounds__(128) replay_kernel(const ReplayParams a, const
 #pragma unroll
     for (int j = 0; j < NMAX; j++) {
         L[j] = (j < NE) ? ck[(size_t)j * P + p] : R(0);
-        Y[j] = (j < NE) ? flog<R>(L[j]) : R(0);
+        Y[j] = (j < NE) ? (a.normal ? L[j] : flog<R>(L[j])) : R(0);
         if (j < NE) seg[(size_t)j * P + p] = L[j];
     }
     for (int n = a.n0; n < a.n_stop; n++) {
@@ -418,8 +429,8 @@ __global__ void __launch_bounds__(128) replay_kernel(const ReplayParams a, const
 #pragma unroll
         for (int j = 0; j < NMAX; j++) {
             if (j < NE && j >= first) {
-                const R os = fdiv<R>(L[j], L[j] + tb.inv_delta[j]);
-                R mu = tb.var_half[(size_t)n * N + j], diff = R(0);
+                const R os = fdiv<R>(a.normal ? R(1) : L[j], L[j] + tb.inv_delta[j]);
+                R mu = a.normal ? R(0) : tb.var_half[(size_t)n * N + j], diff = R(0);
 #pragma unroll
                 for (int k = 0; k < FMAX; k++) {
                     if (k < F) {
@@ -430,7 +441,7 @@ __global__ void __launch_bounds__(128) replay_kernel(const ReplayParams a, const
                     }
                 }
                 Y[j] = Y[j] + (mu * dt + diff);
-                R v = fexp<R>(Y[j]);
+                R v = a.normal ? Y[j] : fexp<R>(Y[j]);
                 if (a.capped && v > cap) v = cap;
                 L[j] = v;
             }
@@ -453,9 +464,9 @@ struct SeedParams {
     const double* inv_numeraire;   // [N+1][P] 1/N
     const double* adj;             // [N+1]
     const double* abar;            // [N+1] (pass 2)
-    double inv_pd[65];             // 1 / P^d(T_l)
-    unsigned char det[65];
-    double delta[64];              // tenor period lengths
+    double inv_pd[kMaxForwardRates + 1];  // 1 / P^d(T_l)
+    unsigned char det[kMaxForwardRates + 1];
+    double delta[kMaxForwardRates];       // tenor period lengths
     const double* ex_time;         // [P]
     double* abar_partials;         // [blocks][N+1] (pass 1)
     double* seeds;                 // [N][P]: pass 1 the payoff part, pass 2 final (divided by P)
@@ -483,8 +494,9 @@ __device__ __forceinline__ double st(const SeedParams& a, int slot, int j, int p
 template <typename TS>
 __global__ void __launch_bounds__(kSeedThreads) seed_kernel(const SeedParams a)
 {
-    __shared__ double r_adj[65];                      // P^d_l / a_l: 1/N_adj = (1/N) r_adj
-    __shared__ double wsum[kSeedThreads / 32][66];    // per warp: cash-flow sums by date, then the value
+    constexpr int VC = kMaxForwardRates + 1;                // the value's column of wsum
+    __shared__ double r_adj[kMaxForwardRates + 1];          // P^d_l / a_l: 1/N_adj = (1/N) r_adj
+    __shared__ double wsum[kSeedThreads / 32][VC + 1];      // per warp: cash-flow sums by date, then the value
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int p = blockIdx.x * kSeedThreads + tid;
     const bool active = p < a.P;
@@ -524,11 +536,11 @@ __global__ void __launch_bounds__(kSeedThreads) seed_kernel(const SeedParams a)
         }
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
-        if (lane == 0) wsum[warp][65] = x;
+        if (lane == 0) wsum[warp][VC] = x;
         __syncthreads();
         // block partials, compensated across the warps (warp order)
         for (int l = tid; l <= N + 1; l += kSeedThreads) {
-            const int col = (l <= N) ? l : 65;
+            const int col = (l <= N) ? l : VC;
             dd acc{0.0, 0.0};
             for (int w = 0; w < kSeedThreads / 32; w++) acc = dd_add_d(acc, wsum[w][col]);
             const double sum = acc.hi + acc.lo;
@@ -575,19 +587,20 @@ __global__ void __launch_bounds__(kSeedThreads) seed_kernel(const SeedParams a)
 // block: on this GPU an FP64 instruction per path would cost more than the pass itself.
 // Exercise times are compared as the bit patterns of non-negative doubles (the IEEE order).
 struct SeedSmem32 {
-    float r_adj[65];    // P^d_l / a_l
-    float adj_pd[65];   // a_l / P^d_l
-    float abar[65];     // pass 2
-    float delta[64];
-    float strike[64], lennot[64];
-    long long fixbits[64];
-    int libor_slot[64], libor_index[64], pay[64];
+    float r_adj[kMaxForwardRates + 1];    // P^d_l / a_l
+    float adj_pd[kMaxForwardRates + 1];   // a_l / P^d_l
+    float abar[kMaxForwardRates + 1];     // pass 2
+    float delta[kMaxForwardRates];
+    float strike[kMaxForwardRates], lennot[kMaxForwardRates];
+    long long fixbits[kMaxForwardRates];
+    int libor_slot[kMaxForwardRates], libor_index[kMaxForwardRates], pay[kMaxForwardRates];
 };
 
 __global__ void __launch_bounds__(kSeedThreads) seed_mixed_kernel(const SeedParams a)
 {
+    constexpr int VC = kMaxForwardRates + 1;          // the value's column of wsum
     __shared__ SeedSmem32 c;
-    __shared__ Sum2 wsum[kSeedThreads / 32][66];  // per warp: cash-flow sums by date, then the value
+    __shared__ Sum2 wsum[kSeedThreads / 32][VC + 1];  // per warp: cash-flow sums by date, then the value
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int p = blockIdx.x * kSeedThreads + tid;
     const bool active = p < a.P;
@@ -611,7 +624,7 @@ __global__ void __launch_bounds__(kSeedThreads) seed_mixed_kernel(const SeedPara
         c.libor_index[q] = pq.libor_index;
         c.pay[q] = pq.pay_num_index;
     }
-    if (tid < kSeedThreads / 32) wsum[tid][65] = Sum2{0.0f, 0.0f};
+    if (tid < kSeedThreads / 32) wsum[tid][VC] = Sum2{0.0f, 0.0f};
     __syncthreads();
     const float* states = static_cast<const float*>(a.states);
     if (a.pass == 1) {
@@ -644,11 +657,11 @@ __global__ void __launch_bounds__(kSeedThreads) seed_mixed_kernel(const SeedPara
             const Sum2 y{__shfl_down_sync(0xffffffffu, x.p, off), __shfl_down_sync(0xffffffffu, x.s, off)};
             x = sum2_merge(x, y);
         }
-        if (lane == 0) wsum[warp][65] = x;
+        if (lane == 0) wsum[warp][VC] = x;
         __syncthreads();
         // block partials, the warps merged in warp order
         for (int l = tid; l <= N + 1; l += kSeedThreads) {
-            const int col = (l <= N) ? l : 65;
+            const int col = (l <= N) ? l : VC;
             Sum2 acc = wsum[0][col];
             for (int w = 1; w < kSeedThreads / 32; w++) acc = sum2_merge(acc, wsum[w][col]);
             const double sum = sum2_value(acc);
@@ -741,7 +754,12 @@ int launch_rev_dispatch(const RevParams& a, const AdjTables<R>& tb, int threads,
         }
         return launch_rev_threads<R, 40, 10>(a, tb, threads, blocks, s);
     }
-    return fail(LMM_ERR_INVALID, "adjoint supports at most 40 forward rates and 10 factors");
+    if constexpr (sizeof(R) == 8) {
+        // the FP64 form with up to 80 forward rates and two factors (the reference's own
+        // sensitivity test: 80 forwards, one factor)
+        if (a.N <= kMaxForwardRates && a.F <= 2) return launch_rev<R, 80, 2, 64>(a, tb, blocks, s);
+    }
+    return fail(LMM_ERR_INVALID, "adjoint supports at most 40 forward rates and 10 factors (FP64: or 80 and 2)");
 }
 
 template <typename R>
@@ -750,7 +768,8 @@ int launch_replay_dispatch(const ReplayParams& a, const AdjTables<R>& tb, cudaSt
     const int blocks = (a.P + 127) / 128;
     if (a.N <= 24 && a.F <= 4) replay_kernel<R, 24, 4><<<blocks, 128, 0, s>>>(a, tb);
     else if (a.N <= 40 && a.F <= 10) replay_kernel<R, 40, 10><<<blocks, 128, 0, s>>>(a, tb);
-    else return fail(LMM_ERR_INVALID, "adjoint supports at most 40 forward rates and 10 factors");
+    else if (sizeof(R) == 8 && a.N <= kMaxForwardRates && a.F <= 2) replay_kernel<R, 80, 2><<<blocks, 128, 0, s>>>(a, tb);
+    else return fail(LMM_ERR_INVALID, "adjoint supports at most 40 forward rates and 10 factors (FP64: or 80 and 2)");
     LMM_CUDA(cudaGetLastError());
     return LMM_OK;
 }
@@ -767,6 +786,7 @@ int reverse_sweeps(const AdjointLaunch& L, const AdjTables<R>& tb, cudaStream_t 
     rp.t_end = L.t_end;
     rp.n_eff = L.n_eff;
     rp.capped = !std::isinf(L.cap);
+    rp.normal = L.normal;
     rp.cap = L.cap;
     rp.first = L.d_first;
     rp.init = L.d_init;
@@ -791,6 +811,7 @@ int reverse_sweeps(const AdjointLaunch& L, const AdjTables<R>& tb, cudaStream_t 
     q.P = L.P;
     q.n_eff = L.n_eff;
     q.capped = rp.capped;
+    q.normal = L.normal;
     q.cap = L.cap;
     q.first = L.d_first;
     q.seg = L.d_seg;
@@ -818,6 +839,7 @@ int adjoint_f_pitch(int N, int F, int fp32)
 {
     const bool small = N <= 24 && F <= 4;  // the (forward rates, factors) templates of the reverse kernel
     if (fp32) return small ? f_pitch<float, 4>() : f_pitch<float, 10>();
+    if (!small && !(N <= 40 && F <= 10)) return f_pitch<double, 2>();  // 41..80 forward rates, <= 2 factors
     return small ? f_pitch<double, 4>() : f_pitch<double, 10>();
 }
 
@@ -863,11 +885,11 @@ int launch_adjoint(const AdjointLaunch& L, cudaStream_t s)
     sp.numeraire = L.d_numeraire;
     sp.adj = L.d_num_adj;
     sp.abar = L.d_abar;
-    for (int l = 0; l <= L.N && l < 65; l++) {
+    for (int l = 0; l <= L.N && l <= kMaxForwardRates; l++) {
         sp.inv_pd[l] = L.h_discount ? 1.0 / L.h_discount[l] : 1.0;
         sp.det[l] = L.h_num_det[l];
     }
-    for (int j = 0; j < L.N && j < 64; j++) sp.delta[j] = L.h_delta[j];
+    for (int j = 0; j < L.N && j < kMaxForwardRates; j++) sp.delta[j] = L.h_delta[j];
     sp.ex_time = L.d_ex;
     sp.abar_partials = L.d_abar_partials;
     sp.seeds = L.d_seeds;
@@ -877,7 +899,7 @@ int launch_adjoint(const AdjointLaunch& L, cudaStream_t s)
     sp.omega = L.d_omega;
     if (L.d_omega && L.fp32) return fail(LMM_ERR_INVALID, "the cash-flow weights of the AAD sweep are an FP64-form input");
     if (!L.d_inv_numeraire || !L.d_nb) return fail(LMM_ERR_STATE, "adjoint: the simulation kept no reciprocal numeraire");
-    if (L.nper > 0 && L.N > 64) return fail(LMM_ERR_INVALID, "adjoint: at most 64 forward rates");
+    if (L.nper > 0 && L.N > kMaxForwardRates) return fail(LMM_ERR_INVALID, "adjoint: at most 80 forward rates");
     const int sb = (L.P + kSeedThreads - 1) / kSeedThreads;
     {
         KernelTimer kt(K_ADJOINT, s, 4);

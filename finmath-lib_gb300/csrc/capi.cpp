@@ -435,7 +435,10 @@ int lmm_process_create(const lmm_model_desc* m, lmm_brownian* bm, lmm_process** 
     for (int i = 0; i <= T; i++)
         if (m->times[i] != bm->times[i]) return fail(LMM_ERR_INVALID, "model time discretization must be the Brownian motion's");
     if (F != bm->F) return fail(LMM_ERR_INVALID, "number of factors differs from the Brownian motion's");
-    if (N <= 0 || N > 64 || F > 16) return fail(LMM_ERR_INVALID, "supported sizes: 1 <= forward rates <= 64, factors <= 16");
+    if (N <= 0 || N > kMaxForwardRates || F > 16)
+        return fail(LMM_ERR_INVALID, "supported sizes: 1 <= forward rates <= 80, factors <= 16");
+    if (bm->precision == LMM_PRECISION_MIXED && N > 64)
+        return fail(LMM_ERR_INVALID, "the mixed-precision form takes at most 64 forward rates");
     if (!m->tenor || !m->factor_loadings || !m->variance || !m->initial_forwards) return fail(LMM_ERR_INVALID, "model tables missing");
     if (m->measure != LMM_MEASURE_SPOT && m->measure != LMM_MEASURE_TERMINAL) return fail(LMM_ERR_INVALID, "unknown measure");
     if (m->state_space != LMM_STATE_SPACE_LOGNORMAL && m->state_space != LMM_STATE_SPACE_NORMAL)
@@ -867,8 +870,8 @@ static int ensure_values(lmm_process* pr)
 int lmm_swaption_get_value(lmm_process* pr, const lmm_swaption_desc* d, double* value, double* error)
 {
     if (!pr || !d || !value) return fail(LMM_ERR_INVALID, "null argument");
-    if (d->num_periods <= 0 || d->num_periods > 64 || !d->fixing_dates || !d->payment_dates || !d->swaprates)
-        return fail(LMM_ERR_INVALID, "swaption needs 1..64 periods with fixing, payment dates and swap rates");
+    if (d->num_periods <= 0 || d->num_periods > kMaxForwardRates || !d->fixing_dates || !d->payment_dates || !d->swaprates)
+        return fail(LMM_ERR_INVALID, "swaption needs 1..80 periods with fixing, payment dates and swap rates");
     SwaptionLaunch a;
     std::memset(&a, 0, sizeof(a));
     a.notional = d->notional;
@@ -910,9 +913,9 @@ static int build_bermudan(lmm_process* pr, const lmm_bermudan_desc* d, BermudanL
 {
     if (!pr || !d) return fail(LMM_ERR_INVALID, "null argument");
     const int n = d->num_periods;
-    if (n <= 0 || n > 64 || !d->is_exercise_date || !d->fixing_dates || !d->period_lengths || !d->payment_dates ||
+    if (n <= 0 || n > kMaxForwardRates || !d->is_exercise_date || !d->fixing_dates || !d->period_lengths || !d->payment_dates ||
         !d->notionals || !d->swaprates)
-        return fail(LMM_ERR_INVALID, "Bermudan needs 1..64 periods and all per-period arrays");
+        return fail(LMM_ERR_INVALID, "Bermudan needs 1..80 periods and all per-period arrays");
     if (d->basis != LMM_BASIS_REFERENCE && d->basis != LMM_BASIS_SWAPRATE) return fail(LMM_ERR_INVALID, "unknown regression basis");
     BermudanLaunch& a = *out;
     a.nper = n;
@@ -1000,11 +1003,11 @@ static int bermudan_run(lmm_process* pr, const lmm_bermudan_desc* d, double* val
                           ? LMM_OK : fail(LMM_ERR_CUDA, "memset");
         if (!rc) rc = dalloc(&pr->d_beta, (size_t)64 * 6, s);
         if (!rc) rc = dalloc(&pr->d_svd, (size_t)64 * 80, s);
-        if (!rc) rc = dalloc(&pr->d_period_length, (size_t)64, s);
-        if (!rc) rc = dalloc(&pr->d_period_index, (size_t)64, s);
-        if (!rc) rc = dalloc(&pr->d_ex_period, (size_t)64, s);
-        if (!rc) rc = dalloc(&pr->d_tenor_delta, (size_t)64, s);
-        if (!rc) rc = dalloc(&pr->d_per, (size_t)64, s);
+        if (!rc) rc = dalloc(&pr->d_period_length, (size_t)kMaxForwardRates, s);
+        if (!rc) rc = dalloc(&pr->d_period_index, (size_t)kMaxForwardRates, s);
+        if (!rc) rc = dalloc(&pr->d_ex_period, (size_t)kMaxForwardRates, s);
+        if (!rc) rc = dalloc(&pr->d_tenor_delta, (size_t)kMaxForwardRates, s);
+        if (!rc) rc = dalloc(&pr->d_per, (size_t)kMaxForwardRates, s);
         if (rc) return rc;
     }
     if (!pr->d_gram) {
@@ -1124,9 +1127,14 @@ int lmm_bermudan_get_gradient_aad(lmm_process* pr, const lmm_bermudan_desc* d, i
     if (dd && pr->precision != LMM_PRECISION_FP64)
         return fail(LMM_ERR_INVALID, "the DISCRETE_DELTA sweep runs on FP64 processes");
     if (dd && !(dirac_width >= 0.0)) return fail(LMM_ERR_INVALID, "the Dirac delta width must be >= 0");
-    if (pr->N > 40 || pr->F > 10) return fail(LMM_ERR_INVALID, "the adjoint supports at most 40 forward rates and 10 factors");
-    if (pr->measure != LMM_MEASURE_SPOT || pr->state_space != LMM_STATE_SPACE_LOGNORMAL || pr->scheme > LMM_SCHEME_EULER_FUNCTIONAL)
-        return fail(LMM_ERR_INVALID, "the adjoint takes the SPOT measure, LOGNORMAL state space and Euler schemes");
+    const bool fp64 = pr->precision == LMM_PRECISION_FP64;
+    const bool normal = pr->state_space == LMM_STATE_SPACE_NORMAL;
+    if (!((pr->N <= 40 && pr->F <= 10) || (fp64 && pr->N <= kMaxForwardRates && pr->F <= 2)))
+        return fail(LMM_ERR_INVALID, "the adjoint supports at most 40 forward rates and 10 factors (FP64: or 80 and 2)");
+    if (pr->measure != LMM_MEASURE_SPOT || pr->scheme > LMM_SCHEME_EULER_FUNCTIONAL)
+        return fail(LMM_ERR_INVALID, "the adjoint takes the SPOT measure and Euler schemes");
+    if (normal && (!fp64 || !std::isinf(pr->cap)))
+        return fail(LMM_ERR_INVALID, "the NORMAL state space's adjoint runs on uncapped FP64 processes");
     if (pr->obs_slot[pr->T] < 0) return fail(LMM_ERR_STATE, "the adjoint needs the last simulation time observed");
     pr->want_ckpt = stride;
     BermudanLaunch bl;
@@ -1195,6 +1203,7 @@ int lmm_bermudan_get_gradient_aad(lmm_process* pr, const lmm_bermudan_desc* d, i
     for (int q = 0; q < bl.nper; q++) m_end = std::max(m_end, bl.per[q].libor_index);
     L.n_eff = m_end + 1;
     L.t_end = std::max(1, pr->tenor_tidx[m_end]);
+    L.normal = normal ? 1 : 0;
     L.cap = pr->cap;
     L.h_discount = pr->has_discount ? pr->discount.data() : nullptr;
     L.h_num_det = pr->num_det.data();
@@ -1229,8 +1238,9 @@ int lmm_bermudan_get_gradient_aad(lmm_process* pr, const lmm_bermudan_desc* d, i
     L.d_deltas = pr->d_deltas;
     if (dd) {
         // the cash flows' weights from the AAD sweep over the backward induction
-        const size_t om = (size_t)bl.nper * pr->P, mom = (size_t)std::max(ne_dd, 1) * 64 * 2;
-        const size_t need = om + 2 * (size_t)pr->P + mom + 3 * 64 + 64 * 6 + (size_t)bermudan_blocks(pr->P) * 12 + 2;
+        constexpr size_t K = kMaxForwardRates;
+        const size_t om = (size_t)bl.nper * pr->P, mom = (size_t)std::max(ne_dd, 1) * K * 2;
+        const size_t need = om + 2 * (size_t)pr->P + mom + 3 * K + K * 6 + (size_t)bermudan_blocks(pr->P) * 12 + 2;
         if (need > pr->dd_scratch_doubles) {
             dfree(pr->d_dd_scratch, s);
             if ((rc = dalloc(&pr->d_dd_scratch, need, s))) return rc;
@@ -1246,9 +1256,9 @@ int lmm_bermudan_get_gradient_aad(lmm_process* pr, const lmm_bermudan_desc* d, i
         ds.d_ubar = ds.d_vbar + pr->P;
         ds.d_moments = ds.d_ubar + pr->P;
         ds.d_mean = ds.d_moments + mom;
-        ds.d_eps = ds.d_mean + 64;
-        ds.d_betap = ds.d_eps + 64;
-        ds.d_partials = ds.d_betap + 64 * 6 + 64;
+        ds.d_eps = ds.d_mean + K;
+        ds.d_betap = ds.d_eps + K;
+        ds.d_partials = ds.d_betap + K * 6 + K;
         const size_t pbytes = sizeof(double) * ((size_t)bermudan_blocks(pr->P) * 12 + 2);
         LMM_CUDA(cudaMemsetAsync(ds.d_partials, 0, pbytes, s));  // the completion counter starts at zero
         // the value's adjoint seed: the numeraire at time 0 (exactly 1 under SPOT)

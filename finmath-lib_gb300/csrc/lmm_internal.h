@@ -155,6 +155,9 @@ int path_blocks(int P);
 // exp(k/kExpTableHalf) for |k| <= kExpTableHalf, rounded to FP64 from extended precision
 // (the table of exp_small in fp64math.cuh)
 constexpr int kExpTableHalf = 256;
+// forward rates of a model: the FP64 form takes up to 80 (the fast path kernels and the mixed
+// form up to 64, the general FP64 path kernel beyond)
+constexpr int kMaxForwardRates = 80;
 void fp64_exp_table(double out[2 * kExpTableHalf + 1]);
 
 // device random variables (randomvariable.cu) from process buffers: a copy (FP32 states
@@ -260,6 +263,7 @@ struct AdjointLaunch {
     int T, N, F, P, nper, stride, callable, freeze_adjustment, fp32, T_slot, blocks;
     int threads;        // adjoint threads per block (64, 128, 256)
     int t_end, n_eff;   // reverse sweep from time index t_end over components 0..n_eff-1
+    int normal;         // NORMAL state space (FP64 form): the state is L itself
     double cap;
     const double* h_discount;      // [N+1] or nullptr
     const uint8_t* h_num_det;      // [N+1]

@@ -5,6 +5,7 @@
 namespace lmm {
 
 int launch_paths_fp64_n64(const PathLaunch& a, cudaStream_t s, int blocks);
+int launch_paths_fp64_n80(const PathLaunch& a, cudaStream_t s, int blocks);
 
 int path_blocks(int P) { return (P + kPathThreads - 1) / kPathThreads; }
 
@@ -23,7 +24,8 @@ int launch_paths_fp64(const PathLaunch& a, cudaStream_t s, int* blocks_out)
     if (a.N <= 24 && a.F <= 4) return launch_t<24, 4>(a, s, blocks);
     if (a.N <= 40 && a.F <= 10) return launch_t<40, 10>(a, s, blocks);
     if (a.N <= 64 && a.F <= 16) return launch_paths_fp64_n64(a, s, blocks);
-    return fail(LMM_ERR_INVALID, "FP64 path kernel supports at most 64 forward rates and 16 factors");
+    if (a.N <= kMaxForwardRates && a.F <= 16) return launch_paths_fp64_n80(a, s, blocks);
+    return fail(LMM_ERR_INVALID, "FP64 path kernel supports at most 80 forward rates and 16 factors");
 }
 
 }  // namespace lmm

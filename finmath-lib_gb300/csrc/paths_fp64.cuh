@@ -413,6 +413,8 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp64_general_kernel(const 
         const int slot = __ldg(a.d_obs_slot + 0);
         if (slot >= 0 && active)
             for (int j = 0; j < N; j++) states[((size_t)slot * N + j) * P + p] = L[j];
+        if (a.d_ckpt && active)
+            for (int j = 0; j < N; j++) static_cast<double*>(a.d_ckpt)[(size_t)j * P + p] = L[j];
         if (terminal && active)
             for (int l = 0; l <= N; l++)
                 if (__ldg(a.d_tenor_tidx + l) == 0) a.d_numeraire[(size_t)l * P + p] = terminal_numeraire(a, l, L, true);
@@ -452,6 +454,10 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp64_general_kernel(const 
         const int slot = __ldg(a.d_obs_slot + i + 1);
         if (slot >= 0 && active)
             for (int j = 0; j < N; j++) states[((size_t)slot * N + j) * P + p] = L[j];
+        if (a.d_ckpt && active && (i + 1) % a.ckpt_stride == 0) {
+            double* ck = static_cast<double*>(a.d_ckpt) + (size_t)((i + 1) / a.ckpt_stride) * N * P;
+            for (int j = 0; j < N; j++) ck[(size_t)j * P + p] = L[j];
+        }
         if (terminal && active)
             for (int l = 0; l <= N; l++)
                 if (__ldg(a.d_tenor_tidx + l) == i + 1) a.d_numeraire[(size_t)l * P + p] = terminal_numeraire(a, l, L, false);
@@ -480,6 +486,14 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp64_general_kernel(const 
         if (a.d_inv_numeraire && active) a.d_inv_numeraire[(size_t)l * P + p] = r;
         block_dd_partial(active ? r * N0 : 0.0, a.d_inv_num_partials + ((size_t)blockIdx.x * N + (l - 1)) * 2);
     }
+}
+
+template <int NMAX, int FMAX>
+int launch_general(const PathLaunch& a, cudaStream_t s, int blocks)
+{
+    paths_fp64_general_kernel<NMAX, FMAX><<<blocks, kPathThreads, 0, s>>>(a);
+    LMM_CUDA(cudaGetLastError());
+    return LMM_OK;
 }
 
 template <int NMAX, int FMAX>

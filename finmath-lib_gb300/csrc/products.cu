@@ -20,7 +20,7 @@ namespace lmm {
 namespace {
 
 constexpr int kProdThreads = 256;
-constexpr int kMaxN = 64;
+constexpr int kMaxN = kMaxForwardRates;
 
 struct NumeraireInfo {
     int P;

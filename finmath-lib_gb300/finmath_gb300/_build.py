@@ -22,7 +22,7 @@ LIB = os.path.join(BUILD, "liblmm_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # translation units whose FP64 arithmetic must not be contracted into FMAs
-NO_FMAD = {"rng.cu", "paths_fp64.cu", "paths_fp64_n64.cu", "products.cu", "randomvariable.cu"}
+NO_FMAD = {"rng.cu", "paths_fp64.cu", "paths_fp64_n64.cu", "paths_fp64_n80.cu", "products.cu", "randomvariable.cu"}
 
 
 def _nvcc() -> str:

@@ -481,6 +481,38 @@ def mersenne_twister_uniforms(seed: int, count: int, offset: int = 0) -> np.ndar
 
 
 # --------------------------------------------------------------------------- process
+def _covariance_on_process_grid(cov, times, tenor, state_space):
+    """The covariance model's factor loadings, variances and volatilities at the process's
+    simulation times t_i and forward rates j.  A model on its own (coarser) time and tenor
+    grids is read as the reference reads it: the loading of (t_i, j) is the model's loading
+    at the floor indices of t_i and of T_j in its grids
+    (AbstractLIBORCovarianceModel.java:45-60, called from
+    LIBORMarketModelFromCovarianceModel.java:1198); the LOGNORMAL drift's variance term is
+    getCovariance(time, j, j) (:1188), whose component j is the model's own index, not mapped
+    (AbstractLIBORCovarianceModel.java:69-75)."""
+    lam = _f64(cov.factorLoadings)
+    T, N = len(times) - 1, len(tenor) - 1
+    vol = getattr(cov, "volatility", None)
+    if lam.shape[:2] == (T, N):
+        return lam, _f64(cov.variance), None if vol is None else _f64(vol)
+    ct = np.asarray(cov.timeDiscretization.getAsDoubleArray(), dtype=np.float64)
+    cc = np.asarray(cov.liborPeriodDiscretization.getAsDoubleArray(), dtype=np.float64)
+    ti = np.searchsorted(ct, times[:-1], side="right") - 1
+    tj = np.searchsorted(cc, tenor[:-1], side="right") - 1
+    if ti.min() < 0 or tj.min() < 0 or ti.max() >= lam.shape[0] or tj.max() >= lam.shape[1]:
+        raise ValueError("the covariance model's grids do not cover the process's times and forward rates")
+    mapped = np.ascontiguousarray(lam[ti][:, tj, :])
+    if state_space == _lib.STATE_SPACE_LOGNORMAL:
+        if N > lam.shape[1]:
+            raise ValueError("LOGNORMAL drift: getCovariance(time, j, j) reads the covariance model's component j, "
+                             "which this model does not have")
+        var = np.ascontiguousarray(np.einsum("ijk,ijk->ij", lam[ti][:, :N, :], lam[ti][:, :N, :]))
+    else:
+        var = np.ascontiguousarray(np.einsum("ijk,ijk->ij", mapped, mapped))  # not read by the NORMAL drift
+    vm = None if vol is None else np.ascontiguousarray(_f64(vol)[ti][:, tj])
+    return mapped, var, vm
+
+
 class EulerSchemeFromProcessModel:
     EULER = _lib.SCHEME_EULER
     EULER_FUNCTIONAL = _lib.SCHEME_EULER_FUNCTIONAL
@@ -494,14 +526,14 @@ class EulerSchemeFromProcessModel:
         self.brownianMotion = brownianMotion
         self.scheme = _lib.SCHEME_EULER_FUNCTIONAL if scheme is None else scheme
         cov = model.covarianceModel
-        self._keep = dict(times=_f64(brownianMotion._times), tenor=_f64(model.liborPeriodDiscretization.getAsDoubleArray()),
-                          lam=_f64(cov.factorLoadings), var=_f64(cov.variance), init=_f64(model.initialForwards),
-                          chain=None if model.discountChain is None else _f64(model.discountChain))
+        times = _f64(brownianMotion._times)
+        tenor = _f64(model.liborPeriodDiscretization.getAsDoubleArray())
+        lam, var, vol = _covariance_on_process_grid(cov, times, tenor, model.stateSpace)
+        self._keep = dict(times=times, tenor=tenor, lam=lam, var=var, init=_f64(model.initialForwards),
+                          chain=None if model.discountChain is None else _f64(model.discountChain), vol=vol)
         k = self._keep
         T = len(k["times"]) - 1
         N = len(k["tenor"]) - 1
-        vol = getattr(cov, "volatility", None)
-        k["vol"] = None if vol is None else _f64(vol)
         desc = _lib.LmmModelDesc(T, _p(k["times"]), N, _p(k["tenor"]), cov.getNumberOfFactors(), _p(k["lam"]),
                                  _p(k["var"]), _p(k["init"]), _p(k["chain"]), model.liborCap, int(self.scheme),
                                  int(model.measure), int(model.stateSpace), _p(k["vol"]))
