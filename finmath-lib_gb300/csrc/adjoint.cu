@@ -916,6 +916,12 @@ int launch_adjoint(const AdjointLaunch& L, cudaStream_t s)
         else seed_kernel<double><<<sb, kSeedThreads, 0, s>>>(sp);
         LMM_CUDA(cudaGetLastError());
     }
+    return launch_adjoint_sweeps(L, s);
+}
+
+int launch_adjoint_sweeps(const AdjointLaunch& L, cudaStream_t s)
+{
+    if (L.stride < 1 || L.stride > kMaxStride) return fail(LMM_ERR_INVALID, "checkpoint stride must be in [1, 16]");
     // ---- reverse sweeps over the paths (per-warp partials, then fixed-order column sums)
     const int warps = L.blocks * (L.threads / 32);
     LMM_CUDA(cudaMemsetAsync(L.d_vega_partials, 0, sizeof(double) * (size_t)warps * L.T * L.N, s));

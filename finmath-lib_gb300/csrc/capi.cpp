@@ -867,12 +867,12 @@ static int ensure_values(lmm_process* pr)
     return rc;
 }
 
-int lmm_swaption_get_value(lmm_process* pr, const lmm_swaption_desc* d, double* value, double* error)
+// Validate a Swaption description against the process and build its launch table.
+static int build_swaption(lmm_process* pr, const lmm_swaption_desc* d, SwaptionLaunch& a)
 {
-    if (!pr || !d || !value) return fail(LMM_ERR_INVALID, "null argument");
+    if (!pr || !d) return fail(LMM_ERR_INVALID, "null argument");
     if (d->num_periods <= 0 || d->num_periods > kMaxForwardRates || !d->fixing_dates || !d->payment_dates || !d->swaprates)
         return fail(LMM_ERR_INVALID, "swaption needs 1..80 periods with fixing, payment dates and swap rates");
-    SwaptionLaunch a;
     std::memset(&a, 0, sizeof(a));
     a.notional = d->notional;
     a.num_index = time_index(pr->tenor, d->exercise_date);
@@ -898,7 +898,15 @@ int lmm_swaption_get_value(lmm_process* pr, const lmm_swaption_desc* d, double* 
         n++;
     }
     a.nper = n;
-    int rc = process_ensure(pr);
+    return LMM_OK;
+}
+
+int lmm_swaption_get_value(lmm_process* pr, const lmm_swaption_desc* d, double* value, double* error)
+{
+    if (!pr || !d || !value) return fail(LMM_ERR_INVALID, "null argument");
+    SwaptionLaunch a;
+    int rc = build_swaption(pr, d, a);
+    if (!rc) rc = process_ensure(pr);
     if (!rc) rc = ensure_values(pr);
     if (rc) return rc;
     ProductView v = product_view(pr);
@@ -1108,55 +1116,13 @@ static int adjoint_tables(lmm_process* pr)
     return rc;
 }
 
-extern "C" {
-
-int lmm_bermudan_get_gradient(lmm_process* pr, const lmm_bermudan_desc* d, int stride, int freeze, double* value,
-                              double* error, double* deltas, double* vegas)
+// the adjoint's per-process scratch (seeds, partial sums, Greeks, segment buffers)
+static int adjoint_alloc(lmm_process* pr, int stride, int threads, AdjointScratch* zout)
 {
-    return lmm_bermudan_get_gradient_aad(pr, d, stride, freeze, LMM_DIRAC_ZERO, 0.0, value, error, deltas, vegas);
-}
-
-int lmm_bermudan_get_gradient_aad(lmm_process* pr, const lmm_bermudan_desc* d, int stride, int freeze, int dirac_method,
-                                  double dirac_width, double* value, double* error, double* deltas, double* vegas)
-{
-    if (!pr || !d || !value || !deltas || !vegas) return fail(LMM_ERR_INVALID, "null argument");
-    if (stride < 1 || stride > 16) return fail(LMM_ERR_INVALID, "checkpoint stride must be in [1, 16]");
-    if (dirac_method != LMM_DIRAC_ZERO && dirac_method != LMM_DIRAC_DISCRETE_DELTA)
-        return fail(LMM_ERR_INVALID, "diracDeltaApproximationMethod must be ZERO or DISCRETE_DELTA");
-    const bool dd = dirac_method == LMM_DIRAC_DISCRETE_DELTA;
-    if (dd && pr->precision != LMM_PRECISION_FP64)
-        return fail(LMM_ERR_INVALID, "the DISCRETE_DELTA sweep runs on FP64 processes");
-    if (dd && !(dirac_width >= 0.0)) return fail(LMM_ERR_INVALID, "the Dirac delta width must be >= 0");
-    const bool fp64 = pr->precision == LMM_PRECISION_FP64;
-    const bool normal = pr->state_space == LMM_STATE_SPACE_NORMAL;
-    if (!((pr->N <= 40 && pr->F <= 10) || (fp64 && pr->N <= kMaxForwardRates && pr->F <= 2)))
-        return fail(LMM_ERR_INVALID, "the adjoint supports at most 40 forward rates and 10 factors (FP64: or 80 and 2)");
-    if (pr->measure != LMM_MEASURE_SPOT || pr->scheme > LMM_SCHEME_EULER_FUNCTIONAL)
-        return fail(LMM_ERR_INVALID, "the adjoint takes the SPOT measure and Euler schemes");
-    if (normal && (!fp64 || !std::isinf(pr->cap)))
-        return fail(LMM_ERR_INVALID, "the NORMAL state space's adjoint runs on uncapped FP64 processes");
-    if (pr->obs_slot[pr->T] < 0) return fail(LMM_ERR_STATE, "the adjoint needs the last simulation time observed");
-    pr->want_ckpt = stride;
-    BermudanLaunch bl;
-    int rc = 0;
-    int ne_dd = 0;
-    if (dd) {
-        // the forward valuation records each date's trigger and Y - Z for the sweep
-        for (int q = 0; q < d->num_periods; q++) ne_dd += d->is_exercise_date[q] ? 1 : 0;
-        const size_t need = (size_t)std::max(ne_dd, 1) * 2 * (size_t)pr->P;
-        if (need > pr->dd_rec_doubles) {
-            dfree(pr->d_dd_rec, pr->stream);
-            if ((rc = dalloc(&pr->d_dd_rec, need, pr->stream))) return rc;
-            pr->dd_rec_doubles = need;
-        }
-    }
-    rc = bermudan_run(pr, d, value, error, nullptr, &bl, dd ? pr->d_dd_rec : nullptr);
-    if (rc) return rc;
-    if ((rc = adjoint_tables(pr))) return rc;
-    cudaStream_t s = pr->stream;
     const int T = pr->T, N = pr->N, P = pr->P;
     const int sb = (P + 255) / 256;
-    const int threads = 128;
+    cudaStream_t s = pr->stream;
+    int rc = LMM_OK;
     const AdjointScratch z = adjoint_scratch(T, N, P, threads, stride, pr->precision == LMM_PRECISION_MIXED);
     if (!pr->d_seeds) {
         if (!rc) rc = dalloc(&pr->d_abar, (size_t)N + 1, s);
@@ -1181,6 +1147,169 @@ int lmm_bermudan_get_gradient_aad(lmm_process* pr, const lmm_bermudan_desc* d, i
         if ((rc = dalloc(&pr->d_adj_ybar, z.ybar_bytes, s))) return rc;
         pr->adj_ybar_bytes = z.ybar_bytes;
     }
+    *zout = z;
+    return LMM_OK;
+}
+
+// the model restrictions every adjoint shares
+static int adjoint_check(lmm_process* pr)
+{
+    const bool fp64 = pr->precision == LMM_PRECISION_FP64;
+    if (!((pr->N <= 40 && pr->F <= 10) || (fp64 && pr->N <= kMaxForwardRates && pr->F <= 2)))
+        return fail(LMM_ERR_INVALID, "the adjoint supports at most 40 forward rates and 10 factors (FP64: or 80 and 2)");
+    if (pr->measure != LMM_MEASURE_SPOT || pr->scheme > LMM_SCHEME_EULER_FUNCTIONAL)
+        return fail(LMM_ERR_INVALID, "the adjoint takes the SPOT measure and Euler schemes");
+    if (pr->state_space == LMM_STATE_SPACE_NORMAL && (!fp64 || !std::isinf(pr->cap)))
+        return fail(LMM_ERR_INVALID, "the NORMAL state space's adjoint runs on uncapped FP64 processes");
+    return LMM_OK;
+}
+
+// deltas and vegas of a European product from its seeds at the process time index t_index
+// (components 0..n_eff-1): simulate with checkpoints, fill pr->d_seeds by `seeds`, sweep back
+template <typename Seeds>
+static int european_gradient(lmm_process* pr, int t_index, int n_eff, int stride, Seeds&& seeds, double* deltas,
+                             double* vegas)
+{
+    if (pr->precision != LMM_PRECISION_FP64) return fail(LMM_ERR_INVALID, "the European products' adjoint runs on FP64 processes");
+    if (stride < 1 || stride > 16) return fail(LMM_ERR_INVALID, "checkpoint stride must be in [1, 16]");
+    int rc = adjoint_check(pr);
+    if (rc) return rc;
+    pr->want_ckpt = stride;
+    if ((rc = process_ensure(pr))) return rc;
+    if ((rc = adjoint_tables(pr))) return rc;
+    const int threads = 128;
+    AdjointScratch z;
+    if ((rc = adjoint_alloc(pr, stride, threads, &z))) return rc;
+    const int T = pr->T, N = pr->N, P = pr->P;
+    std::vector<double> delta(N);
+    for (int j = 0; j < N; j++) delta[j] = pr->tenor[j + 1] - pr->tenor[j];
+    ProductView v = product_view(pr);
+    if ((rc = seeds(v, delta.data()))) return rc;
+    AdjointLaunch L;
+    std::memset(&L, 0, sizeof(L));
+    L.T = T;
+    L.N = N;
+    L.F = pr->F;
+    L.P = P;
+    L.stride = stride;
+    L.blocks = z.blocks;
+    L.threads = threads;
+    L.t_end = std::max(1, t_index);
+    L.n_eff = n_eff;
+    L.normal = pr->state_space == LMM_STATE_SPACE_NORMAL ? 1 : 0;
+    L.cap = pr->cap;
+    L.d_first = pr->d_first;
+    L.d_init = pr->d_init;
+    L.d_dw = pr->bm->d_dw;
+    L.d_ckpt = pr->d_ckpt;
+    L.d_seg = pr->d_adj_seg;
+    L.d_ybar = pr->d_adj_ybar;
+    L.d_lam = pr->d_adj_lam;
+    L.d_f = pr->d_adj_f;
+    L.d_sigma = pr->d_adj_sigma;
+    L.d_var_half = pr->d_adj_var_half;
+    L.d_inv_delta = pr->d_adj_inv_delta;
+    L.d_dt = pr->d_adj_dt;
+    L.d_seeds = pr->d_seeds;
+    L.d_vega_partials = pr->d_vega_partials;
+    L.d_delta_partials = pr->d_delta_partials;
+    L.d_vegas = pr->d_vegas;
+    L.d_deltas = pr->d_deltas;
+    cudaStream_t s = pr->stream;
+    if ((rc = launch_adjoint_sweeps(L, s))) return rc;
+    LMM_CUDA(cudaMemcpyAsync(deltas, pr->d_deltas, sizeof(double) * N, cudaMemcpyDeviceToHost, s));
+    LMM_CUDA(cudaMemcpyAsync(vegas, pr->d_vegas, sizeof(double) * (size_t)T * N, cudaMemcpyDeviceToHost, s));
+    LMM_CUDA(cudaStreamSynchronize(s));
+    return LMM_OK;
+}
+
+extern "C" {
+
+int lmm_swaption_get_gradient(lmm_process* pr, const lmm_swaption_desc* d, int stride, double* value, double* error,
+                              double* deltas, double* vegas)
+{
+    if (!pr || !d || !value || !deltas || !vegas) return fail(LMM_ERR_INVALID, "null argument");
+    SwaptionLaunch a;
+    int rc = build_swaption(pr, d, a);
+    if (rc) return rc;
+    const int ti = process_index_nearest(pr, d->exercise_date);
+    if (ti < 0 || pr->obs_slot[ti] < 0) return fail(LMM_ERR_STATE, "the swaption's adjoint needs the exercise time observed");
+    int m_end = 0;
+    for (int q = 0; q < a.nper; q++) m_end = std::max(m_end, a.period_index[q]);
+    auto seeds = [&](const ProductView& v, const double* delta) {
+        return launch_swaption_seeds(v, a, pr->obs_slot[ti], delta, pr->d_seeds, pr->stream);
+    };
+    if ((rc = european_gradient(pr, ti, std::max(m_end, a.num_index) + 1, stride, seeds, deltas, vegas))) return rc;
+    // the value: the plain valuation's kernel and reduction on the same simulation
+    if ((rc = ensure_values(pr))) return rc;
+    ProductView v = product_view(pr);
+    if ((rc = launch_swaption(v, a, pr->d_values, pr->stream))) return rc;
+    return reduce_mean_stderr(pr->d_values, pr->P, pr->d_reduce, pr->reduce_bytes, value, error, pr->stream);
+}
+
+int lmm_caplet_get_gradient(lmm_process* pr, double maturity, double period_length, double strike, double daycount,
+                            int stride, double* deltas, double* vegas)
+{
+    if (!pr || !deltas || !vegas) return fail(LMM_ERR_INVALID, "null argument");
+    const int m = time_index(pr->tenor, maturity);
+    if (m < 0 || m >= pr->N || time_index(pr->tenor, maturity + period_length) != m + 1)
+        return fail(LMM_ERR_INVALID, "the caplet's period must be a tenor period");
+    const int ti = process_index_nearest(pr, maturity);
+    if (ti < 0 || pr->obs_slot[ti] < 0) return fail(LMM_ERR_STATE, "the caplet's adjoint needs its fixing time observed");
+    CapletSeed c;
+    c.slot = pr->obs_slot[ti];
+    c.index = m;
+    c.strike = strike;
+    c.daycount = daycount;
+    auto seeds = [&](const ProductView& v, const double* delta) {
+        return launch_caplet_seeds(v, c, delta, pr->d_seeds, pr->stream);
+    };
+    return european_gradient(pr, ti, m + 1, stride, seeds, deltas, vegas);
+}
+
+int lmm_bermudan_get_gradient(lmm_process* pr, const lmm_bermudan_desc* d, int stride, int freeze, double* value,
+                              double* error, double* deltas, double* vegas)
+{
+    return lmm_bermudan_get_gradient_aad(pr, d, stride, freeze, LMM_DIRAC_ZERO, 0.0, value, error, deltas, vegas);
+}
+
+int lmm_bermudan_get_gradient_aad(lmm_process* pr, const lmm_bermudan_desc* d, int stride, int freeze, int dirac_method,
+                                  double dirac_width, double* value, double* error, double* deltas, double* vegas)
+{
+    if (!pr || !d || !value || !deltas || !vegas) return fail(LMM_ERR_INVALID, "null argument");
+    if (stride < 1 || stride > 16) return fail(LMM_ERR_INVALID, "checkpoint stride must be in [1, 16]");
+    if (dirac_method != LMM_DIRAC_ZERO && dirac_method != LMM_DIRAC_DISCRETE_DELTA)
+        return fail(LMM_ERR_INVALID, "diracDeltaApproximationMethod must be ZERO or DISCRETE_DELTA");
+    const bool dd = dirac_method == LMM_DIRAC_DISCRETE_DELTA;
+    if (dd && pr->precision != LMM_PRECISION_FP64)
+        return fail(LMM_ERR_INVALID, "the DISCRETE_DELTA sweep runs on FP64 processes");
+    if (dd && !(dirac_width >= 0.0)) return fail(LMM_ERR_INVALID, "the Dirac delta width must be >= 0");
+    const bool normal = pr->state_space == LMM_STATE_SPACE_NORMAL;
+    if (int rc0 = adjoint_check(pr)) return rc0;
+    if (pr->obs_slot[pr->T] < 0) return fail(LMM_ERR_STATE, "the adjoint needs the last simulation time observed");
+    pr->want_ckpt = stride;
+    BermudanLaunch bl;
+    int rc = 0;
+    int ne_dd = 0;
+    if (dd) {
+        // the forward valuation records each date's trigger and Y - Z for the sweep
+        for (int q = 0; q < d->num_periods; q++) ne_dd += d->is_exercise_date[q] ? 1 : 0;
+        const size_t need = (size_t)std::max(ne_dd, 1) * 2 * (size_t)pr->P;
+        if (need > pr->dd_rec_doubles) {
+            dfree(pr->d_dd_rec, pr->stream);
+            if ((rc = dalloc(&pr->d_dd_rec, need, pr->stream))) return rc;
+            pr->dd_rec_doubles = need;
+        }
+    }
+    rc = bermudan_run(pr, d, value, error, nullptr, &bl, dd ? pr->d_dd_rec : nullptr);
+    if (rc) return rc;
+    if ((rc = adjoint_tables(pr))) return rc;
+    cudaStream_t s = pr->stream;
+    const int T = pr->T, N = pr->N, P = pr->P;
+    const int sb = (P + 255) / 256;
+    const int threads = 128;
+    AdjointScratch z;
+    if ((rc = adjoint_alloc(pr, stride, threads, &z))) return rc;
     LMM_CUDA(cudaMemsetAsync(pr->d_abar_partials, 0, sizeof(double) * (size_t)sb * (N + 1), s));
     std::vector<double> delta(N);
     for (int j = 0; j < N; j++) delta[j] = pr->tenor[j + 1] - pr->tenor[j];

@@ -184,15 +184,30 @@ struct ProductView {
 
 struct SwaptionLaunch {
     int nper;
-    int period_slot[64];         // observation slot of min(exercise, fixing) per period
-    int num_index;               // tenor index of the exercise date
-    int period_index[64];        // tenor index of each period
-    double period_length[64];
-    double disc_dt[64];          // payment - max(fixing, exercise)
-    double strike[64];
+    int period_slot[kMaxForwardRates];   // observation slot of min(exercise, fixing) per period
+    int num_index;                       // tenor index of the exercise date
+    int period_index[kMaxForwardRates];  // tenor index of each period
+    double period_length[kMaxForwardRates];
+    double disc_dt[kMaxForwardRates];    // payment - max(fixing, exercise)
+    double strike[kMaxForwardRates];
     double notional;
 };
 int launch_swaption(const ProductView& v, const SwaptionLaunch& a, double* d_values, cudaStream_t s);
+// Adjoint seeds of a European product (FP64 states): d value_p / d L_j(t) / P for every
+// component j at the product's observation slot (the fixings of frozen components and the
+// forwards of alive ones), the cross-path numeraire adjustment held constant (the reference
+// AAD's getAverage).  Swaption.getValue (Swaption.java:137-199) and Caplet.getValue
+// (Caplet.java:100-147) have pathwise derivatives: floor(0) differentiates to 1 where its
+// argument is >= 0 (RandomVariableDifferentiableAAD.java:324-331).
+struct CapletSeed {
+    int slot;           // observation slot of the maturity (fixing) time
+    int index;          // tenor index m of the period; paid at T_{m+1}
+    double strike, daycount;
+};
+int launch_swaption_seeds(const ProductView& v, const SwaptionLaunch& a, int exercise_slot, const double* h_delta,
+                          double* d_seeds, cudaStream_t s);
+int launch_caplet_seeds(const ProductView& v, const CapletSeed& c, const double* h_delta, double* d_seeds,
+                        cudaStream_t s);
 
 // mean and standard error of d_values[P] (Kahan-equivalent compensated sums)
 int reduce_mean_stderr(const double* d_values, int P, double* d_scratch, size_t scratch_bytes, double* h_mean,
@@ -298,6 +313,8 @@ AdjointScratch adjoint_scratch(int T, int N, int P, int threads, int stride, int
 // row pitch (elements) of the factor table f[T][N][pitch] the reverse kernel reads
 int adjoint_f_pitch(int N, int F, int fp32);
 int launch_adjoint(const AdjointLaunch& a, cudaStream_t s);
+// the reverse sweeps and Greek sums alone, from seeds already in d_seeds (d value / d L_j at t_end)
+int launch_adjoint_sweeps(const AdjointLaunch& a, cudaStream_t s);
 int launch_bermudan(const ProductView& v, const BermudanLaunch& a, const BermudanScratch& sc, cudaStream_t s,
                     int* launches);
 

@@ -124,6 +124,70 @@ __global__ void __launch_bounds__(kProdThreads) swaption_kernel(const SwaptionPa
     a.values[p] = x;
 }
 
+// ------------------------------------------------------------------ European products' adjoint seeds
+// Per path the value V = payoff N(0) / N_adj(T_l) of a swaption (kind 0: Swaption.getValue's
+// backward recursion U <- (U + A_q) / (1 + L_q tau_q) over the forwards read at the exercise
+// slot, floored at 0) or a caplet (kind 1: max(L_m(T_m) - K, 0) times the day count fraction,
+// paid at T_{m+1}), and its derivative to every state of the observation slot: through the
+// payoff, and through the numeraire N(T_l) = prod_{k<l} (1 + d_k L_k(T_k)) whose adjustment
+// factor a_l / P^d_l is held constant.  The recursion's adjoint runs forward over the
+// periods: with D_q = 1 + L_q tau_q and U_q the value after period q,
+//   dU_q / dL_q = (len_q notional - U_q tau_q) / D_q,   Ubar_{q+1} = Ubar_q / D_q.
+struct EuroSeedParams {
+    SwaptionLaunch s;
+    CapletSeed c;
+    int kind, N, P, num_index, state_slot;
+    NumeraireInfo num;
+    const double* states;
+    double delta[kMaxN];
+    double* seeds;  // [N][P]: d V_p / d L_j / P
+};
+
+__global__ void __launch_bounds__(kProdThreads) european_seed_kernel(const EuroSeedParams a)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= a.P) return;
+    double g[kMaxN];
+#pragma unroll 1
+    for (int j = 0; j < a.N; j++) g[j] = 0.0;
+    const double scale = numeraire_adj(a.num, 0, 0) / numeraire_adj(a.num, a.num_index, p);  // N(0) / N_adj(T_l)
+    double V;
+    if (a.kind == 0) {
+        double vout[kMaxN];
+        double v = 0.0;
+#pragma unroll 1
+        for (int per = a.s.nper - 1; per >= 0; per--) {
+            const double L = state_at<double>(a.states, a.s.period_slot[per], a.N, a.P, a.s.period_index[per], p);
+            const double payoff = ((L - a.s.strike[per]) * a.s.period_length[per]) * a.s.notional;
+            v = v + payoff;
+            v = v / (1.0 + L * a.s.disc_dt[per]);
+            vout[per] = v;
+        }
+        V = (v > 0.0 ? v : 0.0) * scale;
+        double ub = (v >= 0.0 ? 1.0 : 0.0) * scale;
+#pragma unroll 1
+        for (int per = 0; per < a.s.nper; per++) {
+            const double L = state_at<double>(a.states, a.s.period_slot[per], a.N, a.P, a.s.period_index[per], p);
+            const double D = 1.0 + L * a.s.disc_dt[per];
+            g[a.s.period_index[per]] += ub * (a.s.period_length[per] * a.s.notional - vout[per] * a.s.disc_dt[per]) / D;
+            ub = ub / D;
+        }
+    } else {
+        const double L = state_at<double>(a.states, a.c.slot, a.N, a.P, a.c.index, p);
+        const double x = L - a.c.strike;
+        V = (x > 0.0 ? x : 0.0) * a.c.daycount * scale;
+        g[a.c.index] += (x >= 0.0 ? a.c.daycount : 0.0) * scale;
+    }
+#pragma unroll 1
+    for (int k = 0; k < a.num_index; k++) {
+        const double Lk = state_at<double>(a.states, a.state_slot, a.N, a.P, k, p);  // L_k(T_k)
+        g[k] -= V * a.delta[k] / (1.0 + a.delta[k] * Lk);
+    }
+    const double invP = 1.0 / (double)a.P;
+#pragma unroll 1
+    for (int j = 0; j < a.N; j++) a.seeds[(size_t)j * a.P + p] = g[j] * invP;
+}
+
 // ------------------------------------------------------------------ Bermudan
 // The regression's Gram matrix X^T X at an exercise date depends only on the basis
 // functions, not on the backward induction, so (as the reference caches its solver,
@@ -820,6 +884,46 @@ int grid_for(int P, int threads, int max_blocks)
 }
 
 }  // namespace
+
+static int launch_european_seeds(const ProductView& v, EuroSeedParams& e, const double* h_delta, double* d_seeds,
+                                 cudaStream_t s)
+{
+    if (v.state_fp32) return fail(LMM_ERR_INVALID, "the European products' adjoint runs on FP64 processes");
+    e.N = v.N;
+    e.P = v.P;
+    e.num = make_numeraire_info(v);
+    e.states = static_cast<const double*>(v.d_states);
+    for (int k = 0; k < v.N && k < kMaxN; k++) e.delta[k] = h_delta[k];
+    e.seeds = d_seeds;
+    KernelTimer kt(K_ADJOINT, s);
+    european_seed_kernel<<<(v.P + kProdThreads - 1) / kProdThreads, kProdThreads, 0, s>>>(e);
+    LMM_CUDA(cudaGetLastError());
+    return LMM_OK;
+}
+
+int launch_swaption_seeds(const ProductView& v, const SwaptionLaunch& a, int exercise_slot, const double* h_delta,
+                          double* d_seeds, cudaStream_t s)
+{
+    EuroSeedParams e;
+    std::memset(&e, 0, sizeof(e));
+    e.s = a;
+    e.kind = 0;
+    e.num_index = a.num_index;
+    e.state_slot = exercise_slot;  // the fixings L_k(T_k), k < the exercise index, as of the exercise date
+    return launch_european_seeds(v, e, h_delta, d_seeds, s);
+}
+
+int launch_caplet_seeds(const ProductView& v, const CapletSeed& c, const double* h_delta, double* d_seeds,
+                        cudaStream_t s)
+{
+    EuroSeedParams e;
+    std::memset(&e, 0, sizeof(e));
+    e.c = c;
+    e.kind = 1;
+    e.num_index = c.index + 1;
+    e.state_slot = c.slot;
+    return launch_european_seeds(v, e, h_delta, d_seeds, s);
+}
 
 int launch_numeraire_finish(const double* d_partials, int blocks, int N, int P, const double* d_numeraire,
                             const uint8_t* d_det, double* d_adj, cudaStream_t s)

@@ -869,6 +869,22 @@ class Swaption:
     def getValue(self, model):
         return self.getValues(model)["value"]
 
+    def getGradient(self, model: LIBORMonteCarloSimulationFromLIBORModel, checkpointStride: int = 1):
+        """Value, deltas d V / d L_j(0) and vegas d V / d sigma_{i,j}: the payoff's pathwise
+        derivative (floor(0) differentiates to 1 where its argument is >= 0, as the reference's
+        AAD does; RandomVariableDifferentiableAAD.java:324-331) swept back through the Euler
+        scheme by the adjoint kernel.  FP64 processes; the value is the plain valuation's."""
+        proc = model.process
+        T = len(proc._keep["times"]) - 1
+        N = len(proc._keep["tenor"]) - 1
+        d = _lib.LmmSwaptionDesc(self.exerciseDate, len(self.fixingDates), _p(self.fixingDates), _p(self.paymentDates),
+                                 _p(self.periodLengths), _p(self.swaprates), self.notional)
+        v, e = ctypes.c_double(), ctypes.c_double()
+        deltas, vegas = np.empty(N), np.empty((T, N))
+        check(_lib.load().lmm_swaption_get_gradient(proc._h, ctypes.byref(d), int(checkpointStride), ctypes.byref(v),
+                                                     ctypes.byref(e), _p(deltas), _p(vegas)), "Swaption.getGradient")
+        return {"value": v.value, "error": e.value, "deltas": deltas, "vegas": vegas}
+
 
 class SwaptionSimple:
     """net.finmath.montecarlo.interestrate.products.SwaptionSimple (SwaptionSimple.java): the

@@ -7,6 +7,8 @@ LMM hot path (Swaption, BermudanSwaption) the fused kernels of lmm.py are the fa
 """
 from __future__ import annotations
 
+import numpy as np
+
 from .randomvariable import RandomVariableGPU
 
 
@@ -55,6 +57,26 @@ class Caplet:
 
     def getValue(self, model, evaluationTime: float = 0.0) -> float:
         return self.getValueRandomVariable(evaluationTime, model).getAverage()
+
+    def getGradient(self, model, checkpointStride: int = 1):
+        """Value (this product's own valuation), deltas d V / d L_j(0) and vegas
+        d V / d sigma_{i,j} of the caplet by the adjoint kernel: the payoff's pathwise
+        derivative (floor(0) differentiates to 1 where its argument is >= 0,
+        RandomVariableDifferentiableAAD.java:324-331) through the fixing and the payment
+        numeraire, swept back through the Euler scheme.  FP64 processes, caplets only."""
+        import ctypes
+        from . import _lib
+        if self.isFloorlet:
+            raise NotImplementedError("the adjoint covers caplets")
+        proc = model.process
+        T = len(proc._keep["times"]) - 1
+        N = len(proc._keep["tenor"]) - 1
+        deltas, vegas = np.empty(N), np.empty((T, N))
+        dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))  # noqa: E731
+        _lib.check(_lib.load().lmm_caplet_get_gradient(proc._h, self.maturity, self.periodLength, self.strike,
+                                                        self.daycountFraction, int(checkpointStride), dp(deltas),
+                                                        dp(vegas)), "Caplet.getGradient")
+        return {"value": self.getValue(model), "deltas": deltas, "vegas": vegas}
 
 
 class SimpleSwap:

@@ -244,7 +244,8 @@ int lmm_values_mean_stderr_noalloc(const double* d_values, int64_t num_values, v
  * (montecarlo/automaticdifferentiation/RandomVariableDifferentiable.java:56-75) gives it for
  * the initial forwards and the volatility-matrix entries as leaves
  * (LIBORMarketModelNormalAADSensitivitiesTest.java:343-355, 431-434).  A hand-written adjoint
- * of the Euler-log step replays each path backward from checkpoints written every
+ * of the Euler step (LOGNORMAL: in log coordinates; NORMAL, FP64 processes, uncapped: on the
+ * forwards themselves) replays each path backward from checkpoints written every
  * checkpoint_stride steps (1..16); exercise decisions are frozen from the forward
  * valuation.  freeze_numeraire_adjustment = 1 treats the numeraire adjustment's path
  * average as a constant, as the reference's AAD does (RandomVariableDifferentiableAAD
@@ -270,6 +271,24 @@ int lmm_bermudan_get_gradient(lmm_process* proc, const lmm_bermudan_desc* produc
 int lmm_bermudan_get_gradient_aad(lmm_process* proc, const lmm_bermudan_desc* product, int checkpoint_stride,
                                   int freeze_numeraire_adjustment, int dirac_method, double dirac_width,
                                   double* out_value, double* out_error, double* out_deltas, double* out_vegas);
+
+/* Gradients of the European products the reference's sensitivity test differentiates
+ * (LIBORMarketModelNormalAADSensitivitiesTest.java:127-165): Swaption.getValue
+ * (montecarlo/interestrate/products/Swaption.java:137-199) and Caplet.getValue
+ * (montecarlo/interestrate/products/Caplet.java:100-147).  Their payoffs are floored at 0,
+ * whose AAD derivative is 1 where the argument is >= 0 (RandomVariableDifferentiableAAD.java:
+ * 324-331), so the gradient is pathwise: per path the derivative of the value to every
+ * state of the product's observation date (the swaption's forwards at the exercise date and
+ * the fixings of its numeraire; the caplet's fixing L_m(T_m) and the fixings of N(T_{m+1})),
+ * the numeraire adjustment held constant, then the adjoint of the Euler scheme back to the
+ * initial forwards and the volatility matrix (as lmm_bermudan_get_gradient).  FP64
+ * processes; the LOGNORMAL or NORMAL state space.  The swaption's value and error are the
+ * plain valuation's (the same kernel and reduction).  The caplet's period [maturity,
+ * maturity + period_length] must be a tenor period; daycount is its day count fraction. */
+int lmm_swaption_get_gradient(lmm_process* proc, const lmm_swaption_desc* product, int checkpoint_stride,
+                              double* out_value, double* out_error, double* out_deltas, double* out_vegas);
+int lmm_caplet_get_gradient(lmm_process* proc, double maturity, double period_length, double strike,
+                            double daycount_fraction, int checkpoint_stride, double* out_deltas, double* out_vegas);
 
 /* ---------------------------------------------------------------- portfolio batch
  * A portfolio of Bermudan swaptions valued, with their deltas and vegas, on one shared

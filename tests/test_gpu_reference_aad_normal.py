@@ -6,18 +6,22 @@ LIBORMarketModelNormalAADSensitivitiesTest.java:288-401) builds 80 semi-annual f
 d = 0.3 / 20 / 2 on the grid {0, 10, 20, 30, 40} for both times and forwards (read at the
 floor indices of t_i and T_j), one factor with correlation decay 0, the SPOT measure, the
 NORMAL state space, no LIBOR cap, no discount curve, 5,000 paths of MersenneTwister seed
-1352 and the EULER scheme.  Its Bermudan case exercises every six months from 30y into a swap
-to 40y at the par swap rate (:98-165).  The checks, with the reference's tolerances:
+1352 and the EULER scheme.  Its five cases (:127-165, the bucket of each delta in brackets):
+caplets at 5y [10], 10y [20] and 30y [60] struck at the par rate of the 30y-into-10y swap,
+that swaption [60], and the Bermudan exercisable every six months from 30y into the same
+swap [60].  The checks, with the reference's tolerances:
 
   testVega  (:411-553)  the AAD vega to the matrix entry (2, 2) against central differences
                         with a 1e-8 shift of that entry, |FD - AD| <= 1.3e-2;
-  testDelta (:563-711)  the AAD delta to L_60(0) (DISCRETE_DELTA, width 0.05) against central
-                        differences with a 1e-2 bump of that forward, |FD - AD| <= 1.3e-2;
+  testDelta (:563-711)  the AAD delta to the bucket's initial forward (the Bermudan:
+                        DISCRETE_DELTA, width 0.05) against central differences with a 1e-2
+                        bump of that forward, |FD - AD| <= 1.3e-2;
   both                  the AAD run's value equals the plain valuation's exactly.
 
-Tighter than the reference: the GPU paths and Bermudan value equal the oracle's on the same
-tables, and the frozen-exercise (ZERO) adjoint equals central differences of the oracle's
-frozen-exercise value to 1e-6 for deltas and for vegas of the simulation grid.
+Tighter than the reference: the GPU paths and the Bermudan and swaption values equal the
+oracle's on the same tables; the frozen-exercise (ZERO) Bermudan adjoint and the swaption's
+adjoint equal central differences of the oracle's values to 1e-6 for deltas and for vegas of
+the simulation grid; the caplets' deltas equal small-bump GPU differences to 1e-6.
 """
 import math
 
@@ -26,6 +30,7 @@ import pytest
 
 import finmath_gb300 as F
 from finmath_gb300 import analytic as A
+from finmath_gb300 import rvproducts as RP
 from oracle import pyoracle as po
 
 pytestmark = pytest.mark.gpu
@@ -85,24 +90,50 @@ def bermudan(K):
                               np.full(PERIODS, K))
 
 
-def _value(product, **bumps):
-    sim = create_libor_market_model(**bumps)
-    v = product.getValue(sim)
-    _close(sim)
-    return v
+def swaption(K):
+    fixing, payment, _ = _swaption_schedule()
+    return F.Swaption(EXERCISE, fixing, payment, np.full(PERIODS, 0.5), np.full(PERIODS, K))
+
+
+def products(K):
+    """data() (:127-165): name -> (product, delta bucket, its AAD gradient on a simulation)"""
+    def dd(p):
+        return lambda sim: p.getGradient(sim, diracDeltaApproximationMethod="DISCRETE_DELTA",
+                                         diracDeltaApproximationWidthPerStdDev=0.05)
+    out = {}
+    for T in (5.0, 10.0, EXERCISE):
+        c = RP.Caplet(T, 0.5, K)
+        out[f"caplet{T:g}"] = (c, int(round(T * 2)), c.getGradient)
+    sw = swaption(K)
+    out["swaption"] = (sw, int(round(EXERCISE * 2)), sw.getGradient)
+    b = bermudan(K)
+    out["bermudan"] = (b, int(round(EXERCISE * 2)), dd(b))
+    return out
+
+
+BUMPS = {"delta10+": dict(delta_bucket=10, delta_shift=1e-2), "delta10-": dict(delta_bucket=10, delta_shift=-1e-2),
+         "delta20+": dict(delta_bucket=20, delta_shift=1e-2), "delta20-": dict(delta_bucket=20, delta_shift=-1e-2),
+         "delta60+": dict(delta_bucket=60, delta_shift=1e-2), "delta60-": dict(delta_bucket=60, delta_shift=-1e-2),
+         "vega+": dict(vol_bucket=(2, 2), vol_shift=1e-8), "vega-": dict(vol_bucket=(2, 2), vol_shift=-1e-8)}
 
 
 @pytest.fixture(scope="module")
 def case():
     K = par_swaprate()
-    berm = bermudan(K)
+    prods = products(K)
     sim = create_libor_market_model()
-    plain = berm.getValue(sim)
-    g_dd = berm.getGradient(sim, diracDeltaApproximationMethod="DISCRETE_DELTA",
-                            diracDeltaApproximationWidthPerStdDev=0.05)
-    g_zero = berm.getGradient(sim, checkpointStride=1)
-    g_zero8 = berm.getGradient(sim, checkpointStride=8)
-    yield dict(K=K, berm=berm, sim=sim, plain=plain, g_dd=g_dd, g_zero=g_zero, g_zero8=g_zero8)
+    plain = {name: p.getValue(sim) for name, (p, _, _) in prods.items()}
+    grads = {name: grad(sim) for name, (_, _, grad) in prods.items()}
+    g_zero = prods["bermudan"][0].getGradient(sim, checkpointStride=1)
+    g_zero8 = prods["bermudan"][0].getGradient(sim, checkpointStride=8)
+    g_sw8 = prods["swaption"][0].getGradient(sim, checkpointStride=8)
+    bumped = {}
+    for key, kw in BUMPS.items():
+        b = create_libor_market_model(**kw)
+        bumped[key] = {name: p.getValue(b) for name, (p, _, _) in prods.items()}
+        _close(b)
+    yield dict(K=K, prods=prods, sim=sim, plain=plain, grads=grads, g_zero=g_zero, g_zero8=g_zero8, g_sw8=g_sw8,
+               bumped=bumped, berm=prods["bermudan"][0], g_dd=grads["bermudan"])
     _close(sim)
 
 
@@ -116,26 +147,34 @@ def _coarse_vega(sim, vegas, ic, jc):
     return float(vegas[np.ix_(rows, cols)].sum())
 
 
-def test_aad_value_equals_the_plain_value(case):
+NAMES = ["caplet5", "caplet10", "caplet30", "swaption", "bermudan"]
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_aad_value_equals_the_plain_value(case, name):
     # Assert.assertEquals("Valuation", valueSimulation2, valueSimulation, 0.0) (:552, :710)
-    assert case["g_dd"]["value"] == case["plain"]
-    assert case["g_zero"]["value"] == case["plain"]
+    assert case["grads"][name]["value"] == case["plain"][name]
 
 
-def test_delta(case):
-    bucket, shift = int(round(EXERCISE * 2)), 1e-2
-    fd = (_value(case["berm"], delta_bucket=bucket, delta_shift=shift)
-          - _value(case["berm"], delta_bucket=bucket, delta_shift=-shift)) / shift / 2
-    ad = case["g_dd"]["deltas"][bucket]
+@pytest.mark.parametrize("name", NAMES)
+def test_delta(case, name):
+    bucket, shift = case["prods"][name][1], 1e-2
+    up, dn = case["bumped"][f"delta{bucket}+"][name], case["bumped"][f"delta{bucket}-"][name]
+    fd = (up - dn) / shift / 2
+    ad = case["grads"][name]["deltas"][bucket]
     assert ad == pytest.approx(fd, abs=1.3e-2)
 
 
-def test_vega(case):
+@pytest.mark.parametrize("name", NAMES)
+def test_vega(case, name):
     ic, jc, shift = 2, 2, 1e-8
-    fd = (_value(case["berm"], vol_bucket=(ic, jc), vol_shift=shift)
-          - _value(case["berm"], vol_bucket=(ic, jc), vol_shift=-shift)) / shift / 2
-    ad = _coarse_vega(case["sim"], case["g_dd"]["vegas"], ic, jc)
+    fd = (case["bumped"]["vega+"][name] - case["bumped"]["vega-"][name]) / shift / 2
+    ad = _coarse_vega(case["sim"], case["grads"][name]["vegas"], ic, jc)
     assert ad == pytest.approx(fd, abs=1.3e-2)
+
+
+def test_bermudan_value_equals_zero_method_value(case):
+    assert case["g_zero"]["value"] == case["plain"]["bermudan"]
 
 
 # ---------------------------------------------------------------- against the oracle
@@ -157,7 +196,8 @@ def oracle(case):
     base = po.Simulation(m, dW)
     fixing, payment, _ = _swaption_schedule()
     v, e, pp, et = base.bermudan(fixing, np.full(PERIODS, 0.5), payment, case["K"], basis_id=0, per_path=True)
-    return dict(m=m, dW=dW, base=base, v=v, et=et)
+    sv, _ = base.swaption(EXERCISE, fixing, payment, case["K"])
+    return dict(m=m, dW=dW, base=base, v=v, et=et, sv=sv)
 
 
 def test_paths_and_value_equal_the_oracle(case, oracle):
@@ -168,12 +208,18 @@ def test_paths_and_value_equal_the_oracle(case, oracle):
         assert np.allclose(g, o, rtol=1e-12, atol=1e-15)
     for t in (10.0, 30.0, 40.0):
         assert np.allclose(sim.process.getNumeraire(t), base.numeraire(t), rtol=1e-12)
-    assert case["plain"] == pytest.approx(oracle["v"], rel=1e-12)
+    assert case["plain"]["bermudan"] == pytest.approx(oracle["v"], rel=1e-12)
+    assert case["plain"]["swaption"] == pytest.approx(oracle["sv"], rel=1e-12)
 
 
 def _frozen(oracle, m, K):
     fixing, payment, _ = _swaption_schedule()
     return po.Simulation(m, oracle["dW"]).bermudan_frozen(fixing, np.full(PERIODS, 0.5), payment, K, oracle["et"])
+
+
+def _swaption_value(oracle, m, K):
+    fixing, payment, _ = _swaption_schedule()
+    return po.Simulation(m, oracle["dW"]).swaption(EXERCISE, fixing, payment, K)[0]
 
 
 @pytest.mark.parametrize("j", [0, 30, 60, 70, 79])
@@ -206,3 +252,49 @@ def test_frozen_exercise_vegas_equal_oracle_differences(case, oracle, i, j):
 def test_checkpoint_stride_invariance(case):
     assert np.allclose(case["g_zero8"]["deltas"], case["g_zero"]["deltas"], rtol=1e-12, atol=1e-15)
     assert np.allclose(case["g_zero8"]["vegas"], case["g_zero"]["vegas"], rtol=1e-12, atol=1e-15)
+
+
+@pytest.mark.parametrize("j", [0, 30, 59, 60, 79])
+def test_swaption_deltas_equal_oracle_differences(case, oracle, j):
+    h = 1e-6
+    m = oracle["m"]
+    up, dn = m.initial_forwards.copy(), m.initial_forwards.copy()
+    up[j] += h
+    dn[j] -= h
+    fd = (_swaption_value(oracle, _oracle_model(case["sim"], init=up), case["K"])
+          - _swaption_value(oracle, _oracle_model(case["sim"], init=dn), case["K"])) / (2 * h)
+    g = case["grads"]["swaption"]["deltas"]
+    assert g[j] == pytest.approx(fd, abs=1e-6 * np.max(np.abs(g)))
+
+
+@pytest.mark.parametrize("i,j", [(0, 1), (100, 45), (200, 62), (239, 70)])
+def test_swaption_vegas_equal_oracle_differences(case, oracle, i, j):
+    h = 1e-8
+    lam = case["sim"].process._keep["lam"]
+    sigma = np.sqrt(np.sum(lam[i, j] ** 2))
+    up, dn = lam.copy(), lam.copy()
+    up[i, j] *= (sigma + h) / sigma
+    dn[i, j] *= (sigma - h) / sigma
+    fd = (_swaption_value(oracle, _oracle_model(case["sim"], loadings=up), case["K"])
+          - _swaption_value(oracle, _oracle_model(case["sim"], loadings=dn), case["K"])) / (2 * h)
+    g = case["grads"]["swaption"]["vegas"]
+    assert g[i, j] == pytest.approx(fd, abs=1e-6 * np.max(np.abs(g)))
+
+
+@pytest.mark.parametrize("T,j", [(5.0, 10), (5.0, 3), (30.0, 60), (30.0, 41)])
+def test_caplet_deltas_equal_small_bump_differences(case, T, j):
+    h = 1e-6
+    c = RP.Caplet(T, 0.5, case["K"])
+    up = create_libor_market_model(delta_bucket=j, delta_shift=h)
+    dn = create_libor_market_model(delta_bucket=j, delta_shift=-h)
+    fd = (c.getValue(up) - c.getValue(dn)) / (2 * h)
+    _close(up)
+    _close(dn)
+    g = case["grads"][f"caplet{T:g}"]["deltas"]
+    assert g[j] == pytest.approx(fd, abs=1e-6 * np.max(np.abs(g)))
+
+
+def test_swaption_checkpoint_stride_invariance(case):
+    g1, g8 = case["grads"]["swaption"], case["g_sw8"]
+    assert np.allclose(g8["deltas"], g1["deltas"], rtol=1e-12, atol=1e-15)
+    assert np.allclose(g8["vegas"], g1["vegas"], rtol=1e-12, atol=1e-15)
