@@ -252,8 +252,9 @@ __global__ void __launch_bounds__(kPathThreads, fp64_min_blocks(NMAX, FUNCTIONAL
         if constexpr (SMEM) {
             // the state lives in shared memory: a rolled loop keeps the step's code inside the
             // instruction cache (the unrolled sequence of 40 components did not fit, and its
-            // instruction-fetch stalls cost a third of the kernel's time)
-#pragma unroll 1
+            // instruction-fetch stalls cost a third of the kernel's time); two components per
+            // iteration let the compiler overlap one's exponential with the next one's sums
+#pragma unroll 2
             for (int j = first; j < N; j++) component_step(RuntimeIndex{j});
         } else {
             for_up_from<NMAX>(first, component_step);
