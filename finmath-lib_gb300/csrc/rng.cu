@@ -29,7 +29,14 @@
 namespace lmm {
 namespace {
 
-constexpr int kRngThreads = 320;
+constexpr int kRngThreads = 320;   // the chunk-jump kernel
+// The generator: ten draw warps (one draw per thread of a 312-draw round) and two tail warps,
+// which evaluate the tail draws of the rounds before while the draw warps evaluate the
+// central draws of the current one.
+constexpr int kDrawThreads = 320;
+constexpr int kTailWarpThreads = 64;
+constexpr int kGenThreads = kDrawThreads + kTailWarpThreads;
+constexpr int kTailQueue = 512;    // ring buffer of pending tail draws (a power of two)
 
 struct RngParams {
     int64_t central_max;      // |m - 2^51| <= central_max  <=>  |u - 0.5| <= 0.425 for u = m 2^-52
@@ -362,7 +369,7 @@ __device__ __forceinline__ float icdf_tail_f32(float t)
 constexpr int kStateWords = 2 * kMtN;  // the two state buffers at the start of shared memory
 
 // nxt = one regeneration of the 624-word state cur (three dependent phases of <= 227 words)
-__device__ __forceinline__ void mt_regenerate(const uint32_t* cur, uint32_t* nxt, int tid, int* tail_n)
+__device__ __forceinline__ void mt_regenerate(const uint32_t* cur, uint32_t* nxt, int tid)
 {
     if (tid < 227) nxt[tid] = mt_next(cur[tid + kMtM], cur[tid], cur[tid + 1]);
     __syncthreads();
@@ -370,7 +377,6 @@ __device__ __forceinline__ void mt_regenerate(const uint32_t* cur, uint32_t* nxt
         const int k = 227 + tid;
         nxt[k] = mt_next(nxt[k - 227], cur[k], cur[k + 1]);
     }
-    if (tid == 0) *tail_n = 0;  // every lane finished the previous round's tails before the barrier above
     __syncthreads();
     if (tid < 170) {
         const int k = 454 + tid;
@@ -404,20 +410,77 @@ __device__ __forceinline__ void drain_tile(const OutT* tile, OutT* out, int TF, 
     }
 }
 
+// The pending tail draws: a ring buffer of (draw word, position) entries; an evaluated
+// entry holds its increment's bits in place of the draw.
+struct TailQueue {
+    unsigned long long w[kTailQueue];
+    int2 pos[kTailQueue];  // (path relative to the chunk's first path, step * F + factor); path -1: placed
+    int head;              // oldest entry not yet placed
+    int snap;              // entries appended before the current round
+    int tail;              // next free entry (atomic)
+};
+
+// One tail draw's increment (the draw word as the central test queued it), as the bits of the
+// element type
+template <typename OutT>
+__device__ __forceinline__ unsigned long long tail_increment(const RngParams& prm, unsigned long long w, int row)
+{
+    uint32_t t, k;
+    divmod_u32((uint32_t)row, (uint32_t)prm.num_factors, prm.magic_f, t, k);
+    if constexpr (sizeof(OutT) == 8) {
+        // the tail probability min(u, 1 - u) = M 2^-52 exactly; u = 0 gives 0 as in the reference
+        const int64_t m = (int64_t)w;
+        const bool lower = m < ((int64_t)1 << 51);
+        const int64_t M = lower ? m : ((int64_t)1 << 52) - m;
+        double val = 0.0;
+        if (M > 0) {
+            const double v = icdf_tail(M);
+            val = (lower ? -v : v) * __ldg(prm.sqrt_dt + t);
+        }
+        return (unsigned long long)__double_as_longlong(val);
+    } else {
+        const uint32_t hi = (uint32_t)(w >> 32), lo = (uint32_t)w;
+        const bool lower = hi < (1u << 25);
+        // min(u, 1-u): u itself below 1/2; 1-u = ((2^26-1-hi) 2^26 + (2^26-lo)) 2^-52 above
+        const float tp = lower ? fmaf((float)lo, 0x1.0p-52f, (float)hi * 0x1.0p-26f)
+                               : fmaf((float)((1u << 26) - lo), 0x1.0p-52f, (float)((1u << 26) - 1u - hi) * 0x1.0p-26f);
+        float v = tp > 0.0f ? icdf_tail_f32(tp) : 0.0f;
+        if (lower) v = -v;
+        return (unsigned long long)__float_as_uint(v * __ldg(prm.sqrt_dt32 + t));
+    }
+}
+
+template <typename OutT>
+__device__ __forceinline__ OutT from_bits(unsigned long long b)
+{
+    if constexpr (sizeof(OutT) == 8) return __longlong_as_double((long long)b);
+    else return __uint_as_float((unsigned)b);
+}
+
 // Brownian increments dW[t*F+k][p] of the chunk [v0, v1) of the stream.  The stream runs
 // path-major (path p's T*F draws are consecutive) while the output rows are [t*F+k][P]:
 // the draws go to a shared-memory tile of K consecutive paths x T*F values, and each full
 // tile leaves as row segments of K consecutive paths (K x element size = 128 bytes when the
 // tile fits).  Column k of row r of the tile sits at k ^ (r mod K), so that both the
-// column-wise fill and the row-wise drain are free of bank conflicts.  Thread i owns draw i
-// of every round; its position (path, step, factor) advances by the round's 312 draws
-// without divisions.
+// column-wise fill and the row-wise drain are free of bank conflicts.  Draw thread i owns
+// draw i of every round; its position (path, step, factor) advances by the round's 312 draws
+// without divisions.  A draw in the central region is evaluated at once; a tail draw (about
+// 15 %) joins the queue, whose entries the two tail warps evaluate during the next round
+// (up to 64 a round), so that the slow tail branch runs beside the central draws instead of
+// after them.  Entries still pending when a tile is about to drain (and at the chunk's end,
+// or when the queue fills) are evaluated by every thread in the round's second interval.
 template <typename OutT>
 __device__ __forceinline__ void increments_loop(const RngParams& prm, uint32_t* x, int tid, int64_t v0, int64_t v1,
-                                                unsigned long long* tail_w, int2* tail_pos, int* tail_n)
+                                                TailQueue& q)
 {
     constexpr bool kExact = sizeof(OutT) == 8;  // FP64 increments (the parity form)
+    // The FP64 tail branch costs more than a round's central draws, so the tail warps take it
+    // off the critical path; the FP32 one is cheap enough that the extra queue traffic would
+    // cost more than it saves: the FP32 form evaluates every round's tails in its second
+    // interval, by all threads.
+    constexpr bool kTailWarps = kExact;
     constexpr int kRound = kMtN / 2;
+    constexpr int kMask = kTailQueue - 1;
     const int TF = prm.values_per_path, F = prm.num_factors, P = prm.num_paths, K = prm.tile_k;
     const int T = TF / F;
     OutT* tile = reinterpret_cast<OutT*>(x + kStateWords);
@@ -428,10 +491,10 @@ __device__ __forceinline__ void increments_loop(const RngParams& prm, uint32_t* 
     int rpo = 0, rtf = ts;  // the round's first draw
     int spo, st, sk;        // this thread's draw: path, time step, factor
     {
-        uint32_t q, r, t, k;
-        divmod_u32((uint32_t)(ts + tid), (uint32_t)TF, prm.magic_tf, q, r);
+        uint32_t q0, r, t, k;
+        divmod_u32((uint32_t)(ts + tid), (uint32_t)TF, prm.magic_tf, q0, r);
         divmod_u32(r, (uint32_t)F, prm.magic_f, t, k);
-        spo = (int)q;
+        spo = (int)q0;
         st = (int)t;
         sk = (int)k;
     }
@@ -439,107 +502,112 @@ __device__ __forceinline__ void increments_loop(const RngParams& prm, uint32_t* 
     int pt = 0;  // first path of the tile, relative to ps
     const int lane = tid & 31, warp = tid >> 5;
     const int rpp = 32 / K;  // tile rows drained per warp pass
-    const int dk = lane % K, r0 = warp * rpp + lane / K, rstep = (kRngThreads / 32) * rpp;
+    const int nthreads = blockDim.x;  // the FP32 form runs without the tail warps
+    const int dk = lane % K, r0 = warp * rpp + lane / K, rstep = (nthreads / 32) * rpp;
     const int rounds = (int)((v1 - v0 + kRound - 1) / kRound);
+    if (tid == 0) {
+        q.head = 0;
+        q.snap = 0;
+        q.tail = 0;
+    }
     // Software pipeline: the words of round rd sit in `cur`; while the block turns them into
     // increments it also twists them into round rd+1's words in `nxt` (the three phases of
-    // the twist share the three barrier intervals of the round's draws, tails and placement).
+    // the twist share the three barrier intervals of the round's draws, pending tails and
+    // placement).
     uint32_t* cur = x + kMtN;
     uint32_t* nxt = x;
-    mt_regenerate(x, cur, tid, tail_n);  // round 0 from the jumped state; resets the tail queue
+    mt_regenerate(x, cur, tid);  // round 0 from the jumped state (its barriers also publish the queue)
     for (int rd = 0; rd < rounds; rd++) {
         const bool more = rd + 1 < rounds;
         const int nv = min(kRound, (int)(v1 - v0 - (int64_t)rd * kRound));
-        // ---- interval 1: twist phase 1 of round rd+1; draws of round rd
+        uint32_t dl, rl;
+        divmod_u32((uint32_t)(rtf + nv - 1), (uint32_t)TF, prm.magic_tf, dl, rl);
+        const int plast = rpo + (int)dl;  // path of the round's last draw
+        const int head = q.head, snap = q.snap;
+        const int take = kTailWarps ? min(snap - head, kTailWarpThreads) : 0;  // the tail warps' share
+        // ---- interval 1: twist phase 1 of round rd+1; central draws of round rd; the tail
+        // warps evaluate pending entries [head, head + take)
         if (more && tid < 227) nxt[tid] = mt_next(cur[tid + kMtM], cur[tid], cur[tid + 1]);
-        OutT hv0 = OutT(0), hv1 = OutT(0);
-        int hp0 = -1, hf0 = 0, hp1 = -1, hf1 = 0;  // held draws: path (relative to ps; -1: none), row
+        OutT hv0 = OutT(0);
+        int hp0 = -1, hf0 = 0;  // held draw: path (relative to ps; -1: none), row
         if (tid < nv) {
             const uint2 ww = *reinterpret_cast<const uint2*>(cur + 2 * tid);
             const uint32_t w1 = mt_temper(ww.x), w2 = mt_temper(ww.y);
             bool central;
+            unsigned long long qw;
             if constexpr (kExact) {
                 // |u - 1/2| <= 0.425 tested exactly on the 52-bit grid, u = m 2^-52
                 const int64_t m = (int64_t)(((uint64_t)(w1 >> 6) << 26) | (uint64_t)(w2 >> 6));
                 const int64_t dq = m - ((int64_t)1 << 51);
                 central = (dq < 0 ? -dq : dq) <= prm.central_max;
-                if (central) {
-                    hv0 = icdf_central(dq) * __ldg(prm.sqrt_dt + st);
-                } else {
-                    const int slot = atomicAdd(tail_n, 1);
-                    tail_w[slot] = (unsigned long long)m;
-                    tail_pos[slot] = make_int2(spo, st * F + sk);
-                }
+                if (central) hv0 = icdf_central(dq) * __ldg(prm.sqrt_dt + st);
+                qw = (unsigned long long)m;
             } else {
                 const uint32_t hi = w1 >> 6, lo = w2 >> 6;  // u = (hi 2^26 + lo) 2^-52
-                const float q = fmaf((float)lo, 0x1.0p-52f, (float)((int)hi - (1 << 25)) * 0x1.0p-26f);
-                central = fabsf(q) <= 0.425f;
-                if (central) {
-                    hv0 = icdf_central_f32(q) * __ldg(prm.sqrt_dt32 + st);
-                } else {
-                    const int slot = atomicAdd(tail_n, 1);
-                    tail_w[slot] = ((unsigned long long)hi << 32) | lo;
-                    tail_pos[slot] = make_int2(spo, st * F + sk);
-                }
+                const float qv = fmaf((float)lo, 0x1.0p-52f, (float)((int)hi - (1 << 25)) * 0x1.0p-26f);
+                central = fabsf(qv) <= 0.425f;
+                if (central) hv0 = icdf_central_f32(qv) * __ldg(prm.sqrt_dt32 + st);
+                qw = ((unsigned long long)hi << 32) | lo;
             }
             if (central) {
                 hp0 = spo;
                 hf0 = st * F + sk;
+            } else {
+                const int e = atomicAdd(&q.tail, 1) & kMask;
+                q.w[e] = qw;
+                q.pos[e] = make_int2(spo, st * F + sk);
+            }
+        } else if (tid >= kDrawThreads) {
+            const int i = tid - kDrawThreads;
+            if (i < take) {
+                const int e = (head + i) & kMask;
+                q.w[e] = tail_increment<OutT>(prm, q.w[e], q.pos[e].y);
             }
         }
         __syncthreads();
-        // ---- interval 2: twist phase 2; the round's tail draws on consecutive lanes
+        // ---- interval 2: twist phase 2; before a drain (and at the end, or when the queue is
+        // nearly full) every thread evaluates the remaining pending entries
         if (more && tid < 227) {
             const int k = 227 + tid;
             nxt[k] = mt_next(nxt[k - 227], cur[k], cur[k + 1]);
         }
-        const int n_tail = *tail_n;
-        if (tid < n_tail) {
-            const unsigned long long w = tail_w[tid];
-            const int2 pos = tail_pos[tid];
-            uint32_t t, k;
-            divmod_u32((uint32_t)pos.y, (uint32_t)F, prm.magic_f, t, k);
-            OutT val;
-            if constexpr (kExact) {
-                // the tail probability min(u, 1 - u) = M 2^-52 exactly; u = 0 gives 0 as in the reference
-                const int64_t m = (int64_t)w;
-                const bool lower = m < ((int64_t)1 << 51);
-                const int64_t M = lower ? m : ((int64_t)1 << 52) - m;
-                val = 0.0;
-                if (M > 0) {
-                    const double v = icdf_tail(M);
-                    val = (lower ? -v : v) * __ldg(prm.sqrt_dt + t);
-                }
-            } else {
-                const uint32_t hi = (uint32_t)(w >> 32), lo = (uint32_t)w;
-                const bool lower = hi < (1u << 25);
-                // min(u, 1-u): u itself below 1/2; 1-u = ((2^26-1-hi) 2^26 + (2^26-lo)) 2^-52 above
-                const float tp = lower ? fmaf((float)lo, 0x1.0p-52f, (float)hi * 0x1.0p-26f)
-                                       : fmaf((float)((1u << 26) - lo), 0x1.0p-52f, (float)((1u << 26) - 1u - hi) * 0x1.0p-26f);
-                float v = tp > 0.0f ? icdf_tail_f32(tp) : 0.0f;
-                if (lower) v = -v;
-                val = v * __ldg(prm.sqrt_dt32 + t);
-            }
-            hv1 = val;
-            hp1 = pos.x;
-            hf1 = pos.y;
+        const int qend = q.tail;
+        const bool flush = !kTailWarps || !more || plast >= pt + K ||
+                           qend - (head + take) > kTailQueue - kRound - kTailWarpThreads;
+        const int done = flush ? qend : head + take;  // entries [head, done) are evaluated after this interval
+        OutT hv1 = OutT(0);
+        int hp1 = -1, hf1 = 0;  // FP32: the round's tail draw held by this thread
+        if constexpr (kTailWarps) {
+            if (flush)
+                for (int e = head + take + tid; e < qend; e += nthreads)
+                    q.w[e & kMask] = tail_increment<OutT>(prm, q.w[e & kMask], q.pos[e & kMask].y);
+        } else if (tid < qend - head) {  // at most one round's tails, one per thread
+            const int e = (head + tid) & kMask;
+            hv1 = from_bits<OutT>(tail_increment<OutT>(prm, q.w[e], q.pos[e].y));
+            hp1 = q.pos[e].x;
+            hf1 = q.pos[e].y;
         }
         __syncthreads();
-        // ---- interval 3: twist phase 3; place the held draws, draining the tile when needed
+        // ---- interval 3: twist phase 3; place the held draws and the evaluated entries,
+        // draining the tile when needed
         if (more && tid < 170) {
             const int k = 454 + tid;
             nxt[k] = mt_next(nxt[k - 227], cur[k], (k == kMtN - 1) ? nxt[0] : cur[k + 1]);
         }
-        if (tid == 0) *tail_n = 0;  // every lane read the round's tails before the barrier above
-        uint32_t dl, rl;
-        divmod_u32((uint32_t)(rtf + nv - 1), (uint32_t)TF, prm.magic_tf, dl, rl);
-        const int plast = rpo + (int)dl;  // path of the round's last draw
         while (true) {
             if (hp0 >= 0 && hp0 < pt + K) {
                 tile[hf0 * K + ((hp0 - pt) ^ (hf0 & (K - 1)))] = hv0;
                 hp0 = -1;
             }
-            if (hp1 >= 0 && hp1 < pt + K) {
+            if constexpr (kTailWarps) {
+                for (int e = head + tid; e < done; e += nthreads) {
+                    const int2 ps2 = q.pos[e & kMask];
+                    if (ps2.x >= 0 && ps2.x < pt + K) {
+                        tile[ps2.y * K + ((ps2.x - pt) ^ (ps2.y & (K - 1)))] = from_bits<OutT>(q.w[e & kMask]);
+                        q.pos[e & kMask].x = -1;
+                    }
+                }
+            } else if (hp1 >= 0 && hp1 < pt + K) {
                 tile[hf1 * K + ((hp1 - pt) ^ (hf1 & (K - 1)))] = hv1;
                 hp1 = -1;
             }
@@ -548,6 +616,10 @@ __device__ __forceinline__ void increments_loop(const RngParams& prm, uint32_t* 
             drain_tile<OutT>(tile, out, TF, K, P, ps + pt, ps, ts, pe, te, r0, rstep, dk);
             __syncthreads();
             pt += K;
+        }
+        if (tid == 0) {
+            q.head = done;
+            q.snap = q.tail;  // every append of this round happened before the barriers above
         }
         __syncthreads();  // round rd+1's words complete; `cur` is free for round rd+2
         // advance the round's and this thread's positions by 312 draws
@@ -632,32 +704,30 @@ __global__ void __launch_bounds__(kRngThreads) mt_jump_kernel(const RngParams pr
     for (int i = tid; i < kMtN; i += kRngThreads) states[c * kMtN + i] = x[i];
 }
 
-__global__ void __launch_bounds__(kRngThreads, 3) mt_generate_kernel(const RngParams prm, const uint32_t* states)
+__global__ void __launch_bounds__(kGenThreads, 3) mt_generate_kernel(const RngParams prm, const uint32_t* states)
 {
     // shared memory: the two state buffers (kStateWords words) followed by the increments tile
     extern __shared__ __align__(16) uint32_t x[];
-    __shared__ unsigned long long tail_w[kMtN / 2];  // tail draws of a round, handled by consecutive lanes
-    __shared__ int2 tail_pos[kMtN / 2];               // their positions (path, step * F + factor)
-    __shared__ int tail_n;
+    __shared__ TailQueue tails;
     const int tid = threadIdx.x;
     const int64_t c = blockIdx.x;
     const int64_t v0 = c * prm.chunk_values;
     if (v0 >= prm.num_values) return;
     const int64_t v1 = min(v0 + prm.chunk_values, prm.num_values);
 
-    for (int i = tid; i < kMtN; i += kRngThreads) x[i] = states[c * kMtN + i];  // the chunk's start state
+    for (int i = tid; i < kMtN; i += (int)blockDim.x) x[i] = states[c * kMtN + i];  // the chunk's start state
     __syncthreads();
 
     if (prm.mode == 1) {
-        increments_loop<double>(prm, x, tid, v0, v1, tail_w, tail_pos, &tail_n);
+        increments_loop<double>(prm, x, tid, v0, v1, tails);
     } else if (prm.mode == 2) {
-        increments_loop<float>(prm, x, tid, v0, v1, tail_w, tail_pos, &tail_n);
+        increments_loop<float>(prm, x, tid, v0, v1, tails);
     } else {
         // uniforms in stream order (contiguous stores)
         uint32_t* cur = x;
         uint32_t* nxt = x + kMtN;
         for (int64_t v = v0; v < v1; v += kMtN / 2) {
-            mt_regenerate(cur, nxt, tid, &tail_n);
+            mt_regenerate(cur, nxt, tid);
             if (tid < kMtN / 2 && v + tid < v1) {
                 const uint32_t w1 = mt_temper(nxt[2 * tid]);
                 const uint32_t w2 = mt_temper(nxt[2 * tid + 1]);
@@ -680,7 +750,7 @@ int plan_mt_generate(int64_t num_values, int values_per_path, int elem_bytes, Rn
     LMM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     // the increments tile: K paths x values_per_path, K x element = 128 bytes when it fits
     int kbytes = 128;
-    const size_t budget = 72 * 1024;  // three generator CTAs per SM
+    const size_t budget = 66 * 1024;  // three generator CTAs per SM beside the static tail queue (8 KB)
     if (values_per_path > 1) {
         while (kbytes > elem_bytes && (size_t)values_per_path * kbytes + kStateWords * 4 > budget) kbytes /= 2;
         if ((size_t)values_per_path * kbytes + kStateWords * 4 > budget)
@@ -691,7 +761,8 @@ int plan_mt_generate(int64_t num_values, int values_per_path, int elem_bytes, Rn
     plan->smem_bytes = (int)((size_t)kStateWords * 4 + tile_bytes);
     LMM_CUDA(cudaFuncSetAttribute(mt_generate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 210 * 1024));
     LMM_CUDA(cudaFuncSetAttribute(mt_jump_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kJumpWindow * 4));
-    LMM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mt_generate_kernel, kRngThreads, plan->smem_bytes));
+    LMM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mt_generate_kernel, elem_bytes == 8 ? kGenThreads : kDrawThreads,
+                                                           plan->smem_bytes));
     const int resident = sms * (per_sm > 0 ? per_sm : 1);
     // one chunk per resident CTA, at least 4096 values per chunk
     int64_t chunks = resident;
@@ -767,7 +838,9 @@ int launch_mt_generate(const RngLaunch& a, cudaStream_t s, int* num_launches)
                                      "cudaMallocAsync (generator chunk states)");
         if (arc) return arc;
         mt_jump_kernel<<<(unsigned)a.plan->chunks, kRngThreads, (size_t)kJumpWindow * 4, s>>>(prm, states);
-        mt_generate_kernel<<<(unsigned)a.plan->chunks, kRngThreads, (size_t)a.plan->smem_bytes, s>>>(prm, states);
+        // the FP64 form with its two tail warps, the FP32 form and the uniforms with the draw warps
+        const int threads = prm.mode == 1 ? kGenThreads : kDrawThreads;
+        mt_generate_kernel<<<(unsigned)a.plan->chunks, threads, (size_t)a.plan->smem_bytes, s>>>(prm, states);
         const cudaError_t e = cudaGetLastError();
         cudaFreeAsync(states, s);
         if (e != cudaSuccess) return cuda_fail(e, "generator launch");
