@@ -228,65 +228,77 @@ __device__ __forceinline__ void df_div(float nh, float nl, float dh, float dl, f
     df_fast_two_sum(q, __fmul_rn(res, __frcp_rn(dh)), yh, yl);
 }
 
+// The logarithm's table: for j = 0..127, r_j = 1/c_j rounded to FP32 with c_j = 1 + (j + 1/2)/128,
+// and -log(r_j) as a float pair (FP64 log, split), built by each generator block in shared
+// memory (FP64 form only).
+struct LogTable {
+    float r[128], lh[128], ll[128];
+};
+
+__device__ __forceinline__ void build_log_table(LogTable& t, int tid)
+{
+    if (tid < 128) {
+        const float r = (float)(1.0 / (1.0 + ((double)tid + 0.5) / 128.0));
+        const double lg = -log((double)r);
+        t.r[tid] = r;
+        t.lh[tid] = (float)lg;
+        t.ll[tid] = (float)(lg - (double)t.lh[tid]);
+    }
+}
+
 // sqrt(-log t) for t = M 2^-52, 1 <= M < 2^50, as a float pair (about 2^-46 relative), from
-// the mathematics of the logarithm: t = x 2^k with x in [1/sqrt 2, sqrt 2), read exactly
-// from the integer; log x = 2 atanh(s) = 2 s (1 + s^2/3 + s^4/5 + ...) with
-// s = (x - 1)/(x + 1), |s| <= 0.172 (terms beyond s^10/11 are below 2^-50 and run in FP32,
-// the leading five on float pairs); log t = k log 2 + log x; the square root as the rounded
-// FP32 root plus the residual's correction.
-__device__ __forceinline__ void df_sqrt_neg_log(int64_t M, float& rh, float& rl)
+// the mathematics of the logarithm (Tang's table-driven reduction): t = x 2^k with x in [1, 2)
+// read exactly from the integer; with j the leading seven fraction bits of x,
+// y = x r_j - 1 (|y| <= 1/256, x r_j formed exactly), log x = -log(r_j) + log(1 + y) and
+// log(1 + y) = y - y^2/2 + y^3 (1/3 - y/4 + y^2/5) (the truncated terms are below 2^-50; the
+// cubic part in FP32, since it enters below 2^-24); log t = k log 2 + log x; the square
+// root as the rounded FP32 root plus the residual's correction.
+__device__ __forceinline__ void df_sqrt_neg_log(int64_t M, const LogTable& tab, float& rh, float& rl)
 {
     constexpr DfCoef ln2 = dfc(0.693147180559945309417232121458176568);
-    constexpr DfCoef inv[4] = {dfc(1.0 / 9.0), dfc(1.0 / 7.0), dfc(1.0 / 5.0), dfc(1.0 / 3.0)};
     const unsigned long long um = (unsigned long long)M;
-    int lead = 63 - __clzll((long long)um);              // M in [2^lead, 2^(lead+1))
+    const int lead = 63 - __clzll((long long)um);        // M in [2^lead, 2^(lead+1))
     const unsigned long long norm = um << (63 - lead);  // the leading one at bit 63
-    float xh = __uint2float_rn((unsigned)(norm >> 40)) * 0x1.0p-23f;  // 24 bits: exact, in [1, 2)
+    const unsigned top = (unsigned)(norm >> 40);         // 24 bits: x's leading bits
+    const float xh = __uint2float_rn(top) * 0x1.0p-23f;  // exact, in [1, 2)
     const unsigned rest = (unsigned)((norm >> 16) & 0xffffffull), rest2 = (unsigned)(norm & 0xffffull);
-    float xl = __fmaf_rn(__uint2float_rn(rest2), 0x1.0p-63f, __uint2float_rn(rest) * 0x1.0p-47f);
-    if (xh >= 1.4142135f) {  // x / 2 in [0.707, 1)
-        xh *= 0.5f;
-        xl *= 0.5f;
-        lead++;
-    }
-    float nh, nl, dh, dl, sh, sl, wh, wl;
-    df_add(xh - 1.0f, 0.0f, xl, 0.0f, nh, nl);  // xh - 1 is exact
-    df_add(xh, xl, 1.0f, 0.0f, dh, dl);
-    df_div(nh, nl, dh, dl, sh, sl);
-    df_mul(sh, sl, sh, sl, wh, wl);
-    float q = 1.0f / 21.0f;
-    q = fmaf(q, wh, 1.0f / 19.0f);
-    q = fmaf(q, wh, 1.0f / 17.0f);
-    q = fmaf(q, wh, 1.0f / 15.0f);
-    q = fmaf(q, wh, 1.0f / 13.0f);
-    q = fmaf(q, wh, 1.0f / 11.0f);
-    float vh = q, vl = 0.0f;
-#pragma unroll
-    for (int i = 0; i < 4; i++) {
-        df_mul(vh, vl, wh, wl, vh, vl);
-        df_add(vh, vl, inv[i].h, inv[i].l, vh, vl);
-    }
-    df_mul(vh, vl, wh, wl, vh, vl);
-    df_add(vh, vl, 1.0f, 0.0f, vh, vl);
-    float lh, ll;
-    df_mul(sh, sl, vh, vl, lh, ll);  // log x / 2
+    const float xl = __fmaf_rn(__uint2float_rn(rest2), 0x1.0p-63f, __uint2float_rn(rest) * 0x1.0p-47f);
+    const int j = (int)((top >> 16) & 127u);
+    const float r = tab.r[j];
+    // y = x r - 1: xh r as the exact pair (p, pe), p - 1 exact (p within 1/256 of 1)
+    const float p = __fmul_rn(xh, r);
+    const float pe = fmaf(xh, r, -p);
+    float s, e;
+    two_sum(p - 1.0f, pe, s, e);
+    float yh, yl;
+    df_fast_two_sum(s, fmaf(xl, r, e), yh, yl);
+    // y^2 / 2 as a pair, the cubic part in FP32
+    const float h2 = __fmul_rn(yh, yh);
+    float e2 = fmaf(yh, yh, -h2);
+    e2 = fmaf(yh + yh, yl, e2);
+    const float B = fmaf(fmaf(yh, 0.2f, -0.25f), yh, 1.0f / 3.0f);
+    const float y3B = __fmul_rn(__fmul_rn(__fmul_rn(yh, yh), yh), B);
+    float ah, al;
+    df_add(yh, yl, -0.5f * h2, -0.5f * e2, ah, al);
+    df_add(ah, al, y3B, 0.0f, ah, al);
+    df_add(ah, al, tab.lh[j], tab.ll[j], ah, al);  // log x
     const float K = (float)(lead - 52);
-    const float p = __fmul_rn(K, ln2.h);
-    float e = fmaf(K, ln2.h, -p);
-    e = fmaf(K, ln2.l, e);
+    const float pk = __fmul_rn(K, ln2.h);
+    float ek = fmaf(K, ln2.h, -pk);
+    ek = fmaf(K, ln2.l, ek);
     float Lh, Ll;
-    df_add(p, e, 2.0f * lh, 2.0f * ll, Lh, Ll);  // log t < -2.59
-    const float ah = -Lh, al = -Ll;
-    const float r = __fsqrt_rn(ah);
-    const float res = fmaf(-r, r, ah) + al;
-    df_fast_two_sum(r, __fmul_rn(res, __frcp_rn(r + r)), rh, rl);
+    df_add(pk, ek, ah, al, Lh, Ll);  // log t < -2.59
+    const float nh = -Lh, nl = -Ll;
+    const float q = __fsqrt_rn(nh);
+    const float res = fmaf(-q, q, nh) + nl;
+    df_fast_two_sum(q, __fmul_rn(res, __frcp_rn(q + q)), rh, rl);
 }
 
 // The tail branch (|p - 1/2| > 0.425, the draws the central test rejected) of the same
 // transform for the tail probability t = M 2^-52 = min(u, 1 - u) > 0, without its sign:
 // r = sqrt(-log t), then the rational functions of r - 1.6 (r <= 5) or r - 5 and their
 // quotient, all on float pairs (the shifted argument is >= 0 and every coefficient positive).
-__device__ double icdf_tail(int64_t M)
+__device__ double icdf_tail(int64_t M, const LogTable& tab)
 {
     constexpr DfCoef c[8] = {dfc(7.74545014278341407640e-04), dfc(2.27238449892691845833e-02),
                              dfc(2.41780725177450611770e-01), dfc(1.27045825245236838258e+00),
@@ -306,7 +318,7 @@ __device__ double icdf_tail(int64_t M)
                              dfc(5.99832206555887937690e-01), dfc(1.0)};
     constexpr DfCoef c16 = dfc(1.6);
     float rh, rl, xh, xl;
-    df_sqrt_neg_log(M, rh, rl);
+    df_sqrt_neg_log(M, tab, rh, rl);
     float2 vh, vl;
     if (rh < 5.0f || (rh == 5.0f && rl <= 0.0f)) {
         df_add(rh, rl, -c16.h, -c16.l, xh, xl);
@@ -423,7 +435,8 @@ struct TailQueue {
 // One tail draw's increment (the draw word as the central test queued it), as the bits of the
 // element type
 template <typename OutT>
-__device__ __forceinline__ unsigned long long tail_increment(const RngParams& prm, unsigned long long w, int row)
+__device__ __forceinline__ unsigned long long tail_increment(const RngParams& prm, const LogTable& tab,
+                                                             unsigned long long w, int row)
 {
     uint32_t t, k;
     divmod_u32((uint32_t)row, (uint32_t)prm.num_factors, prm.magic_f, t, k);
@@ -434,7 +447,7 @@ __device__ __forceinline__ unsigned long long tail_increment(const RngParams& pr
         const int64_t M = lower ? m : ((int64_t)1 << 52) - m;
         double val = 0.0;
         if (M > 0) {
-            const double v = icdf_tail(M);
+            const double v = icdf_tail(M, tab);
             val = (lower ? -v : v) * __ldg(prm.sqrt_dt + t);
         }
         return (unsigned long long)__double_as_longlong(val);
@@ -471,7 +484,7 @@ __device__ __forceinline__ OutT from_bits(unsigned long long b)
 // or when the queue fills) are evaluated by every thread in the round's second interval.
 template <typename OutT>
 __device__ __forceinline__ void increments_loop(const RngParams& prm, uint32_t* x, int tid, int64_t v0, int64_t v1,
-                                                TailQueue& q)
+                                                TailQueue& q, const LogTable& tab)
 {
     constexpr bool kExact = sizeof(OutT) == 8;  // FP64 increments (the parity form)
     // The FP64 tail branch costs more than a round's central draws, so the tail warps take it
@@ -561,7 +574,7 @@ __device__ __forceinline__ void increments_loop(const RngParams& prm, uint32_t* 
             const int i = tid - kDrawThreads;
             if (i < take) {
                 const int e = (head + i) & kMask;
-                q.w[e] = tail_increment<OutT>(prm, q.w[e], q.pos[e].y);
+                q.w[e] = tail_increment<OutT>(prm, tab, q.w[e], q.pos[e].y);
             }
         }
         __syncthreads();
@@ -580,10 +593,10 @@ __device__ __forceinline__ void increments_loop(const RngParams& prm, uint32_t* 
         if constexpr (kTailWarps) {
             if (flush)
                 for (int e = head + take + tid; e < qend; e += nthreads)
-                    q.w[e & kMask] = tail_increment<OutT>(prm, q.w[e & kMask], q.pos[e & kMask].y);
+                    q.w[e & kMask] = tail_increment<OutT>(prm, tab, q.w[e & kMask], q.pos[e & kMask].y);
         } else if (tid < qend - head) {  // at most one round's tails, one per thread
             const int e = (head + tid) & kMask;
-            hv1 = from_bits<OutT>(tail_increment<OutT>(prm, q.w[e], q.pos[e].y));
+            hv1 = from_bits<OutT>(tail_increment<OutT>(prm, tab, q.w[e], q.pos[e].y));
             hp1 = q.pos[e].x;
             hf1 = q.pos[e].y;
         }
@@ -709,6 +722,7 @@ __global__ void __launch_bounds__(kGenThreads, 3) mt_generate_kernel(const RngPa
     // shared memory: the two state buffers (kStateWords words) followed by the increments tile
     extern __shared__ __align__(16) uint32_t x[];
     __shared__ TailQueue tails;
+    __shared__ LogTable logtab;
     const int tid = threadIdx.x;
     const int64_t c = blockIdx.x;
     const int64_t v0 = c * prm.chunk_values;
@@ -716,12 +730,13 @@ __global__ void __launch_bounds__(kGenThreads, 3) mt_generate_kernel(const RngPa
     const int64_t v1 = min(v0 + prm.chunk_values, prm.num_values);
 
     for (int i = tid; i < kMtN; i += (int)blockDim.x) x[i] = states[c * kMtN + i];  // the chunk's start state
+    if (prm.mode == 1) build_log_table(logtab, tid);
     __syncthreads();
 
     if (prm.mode == 1) {
-        increments_loop<double>(prm, x, tid, v0, v1, tails);
+        increments_loop<double>(prm, x, tid, v0, v1, tails, logtab);
     } else if (prm.mode == 2) {
-        increments_loop<float>(prm, x, tid, v0, v1, tails);
+        increments_loop<float>(prm, x, tid, v0, v1, tails, logtab);
     } else {
         // uniforms in stream order (contiguous stores)
         uint32_t* cur = x;
@@ -750,7 +765,7 @@ int plan_mt_generate(int64_t num_values, int values_per_path, int elem_bytes, Rn
     LMM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     // the increments tile: K paths x values_per_path, K x element = 128 bytes when it fits
     int kbytes = 128;
-    const size_t budget = 66 * 1024;  // three generator CTAs per SM beside the static tail queue (8 KB)
+    const size_t budget = 64 * 1024;  // three generator CTAs per SM beside the static tail queue and log table (10 KB)
     if (values_per_path > 1) {
         while (kbytes > elem_bytes && (size_t)values_per_path * kbytes + kStateWords * 4 > budget) kbytes /= 2;
         if ((size_t)values_per_path * kbytes + kStateWords * 4 > budget)
