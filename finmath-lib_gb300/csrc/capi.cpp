@@ -230,6 +230,8 @@ struct lmm_process {
     // product scratch
     double* d_values = nullptr;
     double* d_reduce = nullptr;
+    double* d_batch = nullptr;  // [2 x batch_cap] device means and variances of a product batch
+    int batch_cap = 0;
     size_t reduce_bytes = 0;
     double *d_under = nullptr, *d_ex = nullptr, *d_basis = nullptr, *d_gram = nullptr, *d_beta = nullptr;
     double *d_svd = nullptr, *d_rhs = nullptr;
@@ -791,6 +793,7 @@ int lmm_process_destroy(lmm_process* pr)
     dfree(pr->d_det, s);
     dfree(pr->d_values, s);
     dfree(pr->d_reduce, s);
+    dfree(pr->d_batch, s);
     dfree(pr->d_under, s);
     dfree(pr->d_ex, s);
     dfree(pr->d_basis, s);
@@ -898,6 +901,48 @@ static int build_swaption(lmm_process* pr, const lmm_swaption_desc* d, SwaptionL
         n++;
     }
     a.nper = n;
+    return LMM_OK;
+}
+
+int lmm_swaption_values_batch(int n_processes, lmm_process* const* processes, int n_products,
+                              const lmm_swaption_desc* products, double* values, double* errors)
+{
+    if (n_processes <= 0 || n_products <= 0 || !processes || !products || !values)
+        return fail(LMM_ERR_INVALID, "empty batch or null argument");
+    std::vector<SwaptionLaunch> tables((size_t)n_products);
+    int rc = LMM_OK;
+    // every process simulates and prices on its stream, means and variances kept on the device
+    for (int i = 0; i < n_processes && !rc; i++) {
+        lmm_process* pr = processes[i];
+        if (!pr) return fail(LMM_ERR_INVALID, "null process in the batch");
+        for (int k = 0; k < n_products && !rc; k++) rc = build_swaption(pr, &products[k], tables[k]);
+        if (!rc) rc = process_ensure(pr);
+        if (!rc) rc = ensure_values(pr);
+        if (!rc && pr->batch_cap < n_products) {
+            dfree(pr->d_batch, pr->stream);
+            rc = dalloc(&pr->d_batch, 2 * (size_t)n_products, pr->stream);
+            pr->batch_cap = rc ? 0 : n_products;
+        }
+        if (rc) break;
+        ProductView v = product_view(pr);
+        for (int k = 0; k < n_products && !rc; k++) {
+            rc = launch_swaption(v, tables[k], pr->d_values, pr->stream);
+            if (!rc) rc = reduce_mean_var_device(pr->d_values, pr->P, pr->d_reduce, pr->d_batch + 2 * k, pr->stream);
+        }
+    }
+    if (rc) return rc;
+    // then one copy back per process
+    std::vector<double> mv(2 * (size_t)n_products);
+    for (int i = 0; i < n_processes; i++) {
+        lmm_process* pr = processes[i];
+        LMM_CUDA(cudaMemcpyAsync(mv.data(), pr->d_batch, sizeof(double) * mv.size(), cudaMemcpyDeviceToHost, pr->stream));
+        LMM_CUDA(cudaStreamSynchronize(pr->stream));
+        for (int k = 0; k < n_products; k++) {
+            values[(size_t)i * n_products + k] = mv[2 * k];
+            if (errors)
+                errors[(size_t)i * n_products + k] = pr->P > 1 ? std::sqrt(mv[2 * k + 1]) / std::sqrt((double)pr->P) : 0.0;
+        }
+    }
     return LMM_OK;
 }
 

@@ -12,6 +12,7 @@ from .lmm import (TimeDiscretizationFromArray, ForwardCurveInterpolation, Discou
                   LIBORCovarianceModelExponentialForm5Param,
                   LIBORMarketModelFromCovarianceModel, BrownianMotionFromMersenneRandomNumbers,
                   EulerSchemeFromProcessModel, LIBORMonteCarloSimulationFromLIBORModel, Swaption, SwaptionSimple,
+                  swaptionValuesBatch,
                   SwaptionAnalyticApproximation, BermudanSwaption, Portfolio,
                   mersenne_twister_uniforms, kernel_stats)
 from .randomvariable import RandomVariableGPU, RandomVariableGPUFactory, MonteCarloConditionalExpectationRegression

@@ -125,6 +125,8 @@ SIGNATURES = {
                                                  _D, _D, _D, _D]),
     "lmm_bermudan_get_gradient_aad": (ctypes.c_int, [_VP, ctypes.POINTER(LmmBermudanDesc), ctypes.c_int, ctypes.c_int,
                                                      ctypes.c_int, ctypes.c_double, _D, _D, _D, _D]),
+    "lmm_swaption_values_batch": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(_VP), ctypes.c_int,
+                                                 ctypes.POINTER(LmmSwaptionDesc), _D, _D]),
     "lmm_swaption_get_gradient": (ctypes.c_int, [_VP, ctypes.POINTER(LmmSwaptionDesc), ctypes.c_int, _D, _D, _D, _D]),
     "lmm_caplet_get_gradient": (ctypes.c_int, [_VP, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                                ctypes.c_int, _D, _D]),

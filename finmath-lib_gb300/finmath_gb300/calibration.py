@@ -39,6 +39,8 @@ class LevenbergMarquardt:
         self.lambdaDivisor, self.lambdaMultiplicator = 3.0, 2.0
         self.errorRootMeanSquaredTolerance = 0.0
         self._objective = objective
+        self._batch_objective = None  # f over several parameter vectors at once (the Jacobian's columns)
+        self.evaluations = 0          # parameter vectors evaluated
         self.iteration = 0
         self.parameterCurrent = None
         self.errorMeanSquaredCurrent = math.inf
@@ -66,6 +68,7 @@ class LevenbergMarquardt:
         if self._objective is None:
             raise NotImplementedError("setValues must be overridden or an objective given")
         out = self._objective(list(parameters))
+        self.evaluations += 1
         for k in range(len(values)):
             values[k] = float(out[k])
 
@@ -76,17 +79,39 @@ class LevenbergMarquardt:
             error += self.weights[k] * deviation * deviation
         return error / len(value)
 
+    def setBatchObjective(self, batchObjective):
+        """f over a list of parameter vectors at once: the derivative's columns are then
+        evaluated together, as the reference evaluates them in parallel threads
+        (LevenbergMarquardt.java's executor; AbstractLIBORCovarianceModelParametric.java:177-178)."""
+        self._batch_objective = batchObjective
+        return self
+
     def setDerivatives(self, parameters, derivatives):
         # forward differences, one parameter at a time; a failed or NaN valuation gives 0
+        steps, columns = [], []
         for i in range(len(parameters)):
             shifted = list(parameters)
             h = self.parameterSteps[i] if self.parameterSteps is not None else (abs(shifted[i]) + 1) * 1e-8
             shifted[i] += h
-            d = [0.0] * len(self.valueCurrent)
+            steps.append(h)
+            columns.append(shifted)
+        batch = None
+        if self._batch_objective is not None:
             try:
-                self.setValues(shifted, d)
+                batch = [[float(x) for x in out] for out in self._batch_objective(columns)]
+                self.evaluations += len(columns)
             except Exception:
-                d = [math.nan] * len(self.valueCurrent)
+                batch = None
+        for i in range(len(parameters)):
+            h = steps[i]
+            if batch is not None:
+                d = list(batch[i])
+            else:
+                d = [0.0] * len(self.valueCurrent)
+                try:
+                    self.setValues(columns[i], d)
+                except Exception:
+                    d = [math.nan] * len(self.valueCurrent)
             for k in range(len(d)):
                 d[k] -= self.valueCurrent[k]
                 d[k] /= h
@@ -240,7 +265,7 @@ def calibrate_covariance_model(covarianceModel, calibrationModel, calibrationPro
     The optimizer is kept in calibrationParameters["optimizer"] after the run when the caller
     passes a dict, for its iteration count and error."""
     from .lmm import BrownianMotionFromMersenneRandomNumbers, EulerSchemeFromProcessModel, \
-        LIBORMonteCarloSimulationFromLIBORModel
+        LIBORMonteCarloSimulationFromLIBORModel, Swaption, swaptionValuesBatch
     params = {} if calibrationParameters is None else calibrationParameters
     numberOfPaths = int(params.get("numberOfPaths", 2000))
     seed = int(params.get("seed", 31415))
@@ -257,7 +282,31 @@ def calibrate_covariance_model(covarianceModel, calibrationModel, calibrationPro
         raise ValueError("the covariance model has no calibrateable parameters")
     products = list(calibrationProducts)
 
+    def batch_objective(parameter_list):
+        # every calibration product a fused swaption: the trial models' processes are simulated
+        # and priced in one batch (lmm_swaption_values_batch)
+        processes = []
+        try:
+            for parameters in parameter_list:
+                cov = covarianceModel.getCloneWithModifiedParameters(parameters)
+                model = calibrationModel.getCloneWithModifiedCovarianceModel(cov)
+                processes.append(EulerSchemeFromProcessModel(model, bm))
+            sims = [LIBORMonteCarloSimulationFromLIBORModel(pr) for pr in processes]
+            values, _ = swaptionValuesBatch(sims, [p.getProduct() for p in products])
+            return [[(float(values[i, k]) - p.getTargetValue()) * p.getWeight() for k, p in enumerate(products)]
+                    for i in range(len(parameter_list))]
+        finally:
+            for pr in processes:
+                pr.close()
+
+    batched = all(isinstance(p.getProduct(), Swaption) for p in products)
+
     def objective(parameters):
+        if batched:
+            try:
+                return batch_objective([parameters])[0]
+            except Exception:
+                pass  # a failing batch falls back to the product-by-product valuation
         cov = covarianceModel.getCloneWithModifiedParameters(parameters)
         model = calibrationModel.getCloneWithModifiedCovarianceModel(cov)
         process = EulerSchemeFromProcessModel(model, bm)
@@ -270,6 +319,8 @@ def calibrate_covariance_model(covarianceModel, calibrationModel, calibrationPro
     factory = params.get("optimizerFactory") or OptimizerFactoryLevenbergMarquardt(maxIterations, accuracy)
     optimizer = factory.getOptimizer(objective, initial, [-math.inf] * len(initial), [math.inf] * len(initial),
                                      [step] * len(initial), [0.0] * len(products))
+    if batched and hasattr(optimizer, "setBatchObjective"):
+        optimizer.setBatchObjective(batch_objective)
     try:
         optimizer.run()
     finally:

@@ -886,6 +886,22 @@ class Swaption:
         return {"value": v.value, "error": e.value, "deltas": deltas, "vegas": vegas}
 
 
+def swaptionValuesBatch(simulations, swaptions):
+    """Values and standard errors of every swaption on every simulation (a calibration's trial
+    models on one Brownian motion): the simulations, the fused swaption kernels and the
+    reductions are queued without a host round trip, one copy back per simulation
+    (lmm_swaption_values_batch).  Returns (values, errors), arrays [simulations][swaptions]."""
+    sims, prods = list(simulations), list(swaptions)
+    descs = (_lib.LmmSwaptionDesc * len(prods))(*[
+        _lib.LmmSwaptionDesc(s.exerciseDate, len(s.fixingDates), _p(s.fixingDates), _p(s.paymentDates),
+                             _p(s.periodLengths), _p(s.swaprates), s.notional) for s in prods])
+    handles = (ctypes.c_void_p * len(sims))(*[m.process._h for m in sims])
+    values, errors = np.empty((len(sims), len(prods))), np.empty((len(sims), len(prods)))
+    check(_lib.load().lmm_swaption_values_batch(len(sims), handles, len(prods), descs, _p(values), _p(errors)),
+          "swaptionValuesBatch")
+    return values, errors
+
+
 class SwaptionSimple:
     """net.finmath.montecarlo.interestrate.products.SwaptionSimple (SwaptionSimple.java): the
     swaption on a swap tenor, exercised at its first date, valued by the fused swaption

@@ -202,6 +202,14 @@ typedef struct {
 int lmm_swaption_get_value(lmm_process* proc, const lmm_swaption_desc* product, double* out_value,
                            double* out_error);
 
+/* The same values for n_products swaptions on each of n_processes processes (a calibration's
+ * trial models, which share one Brownian motion): the simulations, the fused swaption kernels and
+ * the mean / variance reductions are queued on the processes' streams without a host round
+ * trip, then each process's results come back in one copy.  out_values[n_processes][n_products];
+ * out_errors likewise, or NULL. */
+int lmm_swaption_values_batch(int n_processes, lmm_process* const* processes, int n_products,
+                              const lmm_swaption_desc* products, double* out_values, double* out_errors);
+
 typedef struct {
     int num_periods;
     const uint8_t* is_exercise_date;  /* [n] isPeriodStartDateExerciseDate */

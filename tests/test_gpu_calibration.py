@@ -89,3 +89,20 @@ def test_calibration_matches_the_oracle_calibration():
     assert gp["optimizer"].getRootMeanSquaredError() == pytest.approx(hp["optimizer"].getRootMeanSquaredError(),
                                                                       rel=1e-6)
     assert gp["optimizer"].getIterations() == hp["optimizer"].getIterations()
+
+
+def test_batched_swaption_values_equal_single_valuations():
+    """lmm_swaption_values_batch: the same kernels and reductions as Swaption.getValues, queued
+    for several trial models at once: equal values and errors."""
+    cfg = W.LMM20
+    sims = [W.build(cfg, paths=3000, seed=11) for _ in range(3)]
+    fix = [2.0 + 0.5 * i for i in range(6)]
+    swaptions = [F.Swaption(2.0, fix, [x + 0.5 for x in fix], K) for K in (0.04, 0.05, 0.06)]
+    values, errors = F.swaptionValuesBatch(sims, swaptions)
+    for i, sim in enumerate(sims):
+        for k, s in enumerate(swaptions):
+            r = s.getValues(sim)
+            assert values[i, k] == r["value"] and errors[i, k] == r["error"]
+    for sim in sims:
+        sim.process.close()
+        sim.process.brownianMotion.close()

@@ -39,6 +39,27 @@ def test_levenberg_marquardt_matches_scipy_least_squares():
     assert opt.getRootMeanSquaredError() == pytest.approx(math.sqrt(np.mean(ref.fun ** 2)), rel=1e-6)
 
 
+def test_levenberg_marquardt_batch_objective_gives_the_same_fit():
+    # the Jacobian's columns evaluated together take the same path as one at a time
+    rng = np.random.default_rng(5)
+    x = np.linspace(0.0, 4.0, 25)
+    y = 2.0 * np.exp(-1.3 * x) + 0.5 + rng.normal(0.0, 0.01, x.size)
+    f = lambda p: list(p[0] * np.exp(-p[1] * x) + p[2])  # noqa: E731
+    calls = []
+
+    def batch(ps):
+        calls.append(len(ps))
+        return [f(p) for p in ps]
+
+    a = F.OptimizerFactoryLevenbergMarquardt(100, 0.0).getOptimizer(f, [1.0, 1.0, 0.0], None, None, None, list(y))
+    a.run()
+    b = F.OptimizerFactoryLevenbergMarquardt(100, 0.0).getOptimizer(f, [1.0, 1.0, 0.0], None, None, None, list(y))
+    b.setBatchObjective(batch).run()
+    assert b.getBestFitParameters() == a.getBestFitParameters()
+    assert b.getIterations() == a.getIterations() and b.evaluations == a.evaluations
+    assert calls and all(n == 3 for n in calls)
+
+
 def test_levenberg_marquardt_rejects_nan_points():
     # a NaN error compares false: the point is rejected and lambda grows (:662-676)
     def f(p):
