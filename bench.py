@@ -508,7 +508,7 @@ def fd_check(F, W, cfg, P, berm, grads, h=1e-4):
     Greek |adjoint - FD| within 2 % of FD or 3 standard errors of the FD (the per-path
     differences' standard error).  The re-run regression moves exercise decisions: the FD
     carries the exercise boundary's response, which frozen decisions leave out and the
-    DISCRETE_DELTA sweep approximates."""
+    DISCRETE_DELTA sweep approximates (mixed and FP64 forms)."""
     base = W.build(cfg, paths=P)
     bm = base.process.brownianMotion
     model = base.process.model
@@ -566,6 +566,8 @@ def fd_check(F, W, cfg, P, berm, grads, h=1e-4):
     relse = [se / abs(fd) for kind, arg, fd, se in rows if fd != 0.0]
     res = {"bump": h, "greeks_checked": len(rows), "median_rel_fd_se": float(np.median(relse)) if relse else None,
            "mixed_adjoint_frozen_exercise": compare(grads["mixed"])}
+    if "mixed_dd" in grads:
+        res["mixed_adjoint_discrete_delta"] = compare(grads["mixed_dd"])
     if "fp64_dd" in grads:
         res["fp64_adjoint_discrete_delta"] = compare(grads["fp64_dd"])
     return res
@@ -595,6 +597,17 @@ def greeks_form(args, F, W, cfg, P, T, berm, fp64_valuation_ms):
             res[stride] = (1e3 * (time.perf_counter() - t0) / reps, g)
         ms, g = res[8]
         grads[name] = g
+        if name == "mixed":
+            # the reference AAD's default boundary treatment on the mixed form, timed as above
+            g_dd = berm.getGradient(sim, checkpointStride=8, diracDeltaApproximationMethod="DISCRETE_DELTA")
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                bm.setSeed(cfg["seed"])
+                g_dd = berm.getGradient(sim, checkpointStride=8, diracDeltaApproximationMethod="DISCRETE_DELTA")
+            torch.cuda.synchronize()
+            out["mixed_discrete_delta_ms"] = 1e3 * (time.perf_counter() - t0) / reps
+            grads["mixed_dd"] = g_dd
         if name == "fp64":
             # the reference AAD's default treatment of the exercise boundary (DISCRETE_DELTA,
             # width 0.05 standard deviations): the FP64 form's sweep over the backward induction
@@ -621,6 +634,14 @@ def greeks_form(args, F, W, cfg, P, T, berm, fp64_valuation_ms):
         "max_abs_vega_diff_bp_per_vol_pt": float(1e4 * 1e-2 * np.max(np.abs(g32["vegas"] - g64["vegas"]))),
         "max_rel_delta_diff": float(np.max(np.abs(g32["deltas"] - g64["deltas"])) / np.max(np.abs(g64["deltas"]))),
         "max_rel_vega_diff": float(np.max(np.abs(g32["vegas"] - g64["vegas"])) / np.max(np.abs(g64["vegas"]))),
+    }
+    d32, d64 = grads["mixed_dd"], grads["fp64_dd"]
+    out["mixed_vs_fp64_discrete_delta"] = {
+        "value_bp": 1e4 * (d32["value"] - d64["value"]),
+        "max_abs_delta_diff_bp_per_bp": float(np.max(np.abs(d32["deltas"] - d64["deltas"]))),
+        "max_abs_vega_diff_bp_per_vol_pt": float(1e4 * 1e-2 * np.max(np.abs(d32["vegas"] - d64["vegas"]))),
+        "max_rel_delta_diff": float(np.max(np.abs(d32["deltas"] - d64["deltas"])) / np.max(np.abs(d64["deltas"]))),
+        "max_rel_vega_diff": float(np.max(np.abs(d32["vegas"] - d64["vegas"])) / np.max(np.abs(d64["vegas"]))),
     }
     out["fd_check"] = fd_check(F, W, cfg, P, berm, grads)
     out["note"] = ("bump-and-revalue estimate = (2 x (deltas + nonzero vegas) + 1) x the measured FP64 valuation; "

@@ -635,16 +635,20 @@ __global__ void __launch_bounds__(kSeedThreads) seed_mixed_kernel(const SeedPara
             // receives the periods before its exercise date (times >= 0: bit order = value order)
             const bool paid = active && (a.callable ? (c.fixbits[q] >= taubits) : (c.fixbits[q] < taubits));
             const int l = c.pay[q];
-            float cf = 0.0f;
-            if (paid) {
+            // the cash flow's adjoint weight: the frozen decision, or the AAD sweep's weight
+            const float wgt = a.omega ? (active ? (float)a.omega[(size_t)q * P + p] : 0.0f) : (paid ? 1.0f : 0.0f);
+            float cf = 0.0f, wcf = 0.0f;
+            if (paid || wgt != 0.0f) {
                 const float L = states[((size_t)c.libor_slot[q] * N + c.libor_index[q]) * P + p];
                 const float invN = f64_to_f32_int(a.inv_numeraire[(size_t)l * P + p]) * c.r_adj[l];
-                cf = __fmul_rn((L - c.strike[q]) * c.lennot[q], invN);  // exact input of the Sum2 below
-                seeds[(size_t)c.libor_index[q] * P + p] += c.lennot[q] * invN;
-                if (!a.det[l]) nb[(size_t)l * P + p] -= cf * invN;
+                const float A = __fmul_rn((L - c.strike[q]) * c.lennot[q], invN);  // exact input of the Sum2 below
+                cf = paid ? A : 0.0f;
+                wcf = a.omega ? wgt * A : cf;
+                seeds[(size_t)c.libor_index[q] * P + p] += wgt * (c.lennot[q] * invN);
+                if (!a.det[l]) nb[(size_t)l * P + p] -= wcf * invN;
             }
             sum2_add(x, cf);
-            Sum2 v{cf, 0.0f};
+            Sum2 v{wcf, 0.0f};
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) {
                 const Sum2 y{__shfl_down_sync(0xffffffffu, v.p, off), __shfl_down_sync(0xffffffffu, v.s, off)};
@@ -897,7 +901,6 @@ int launch_adjoint(const AdjointLaunch& L, cudaStream_t s)
     sp.nb = L.d_nb;
     sp.inv_numeraire = L.d_inv_numeraire;
     sp.omega = L.d_omega;
-    if (L.d_omega && L.fp32) return fail(LMM_ERR_INVALID, "the cash-flow weights of the AAD sweep are an FP64-form input");
     if (!L.d_inv_numeraire || !L.d_nb) return fail(LMM_ERR_STATE, "adjoint: the simulation kept no reciprocal numeraire");
     if (L.nper > 0 && L.N > kMaxForwardRates) return fail(LMM_ERR_INVALID, "adjoint: at most 80 forward rates");
     const int sb = (L.P + kSeedThreads - 1) / kSeedThreads;

@@ -1326,8 +1326,6 @@ int lmm_bermudan_get_gradient_aad(lmm_process* pr, const lmm_bermudan_desc* d, i
     if (dirac_method != LMM_DIRAC_ZERO && dirac_method != LMM_DIRAC_DISCRETE_DELTA)
         return fail(LMM_ERR_INVALID, "diracDeltaApproximationMethod must be ZERO or DISCRETE_DELTA");
     const bool dd = dirac_method == LMM_DIRAC_DISCRETE_DELTA;
-    if (dd && pr->precision != LMM_PRECISION_FP64)
-        return fail(LMM_ERR_INVALID, "the DISCRETE_DELTA sweep runs on FP64 processes");
     if (dd && !(dirac_width >= 0.0)) return fail(LMM_ERR_INVALID, "the Dirac delta width must be >= 0");
     const bool normal = pr->state_space == LMM_STATE_SPACE_NORMAL;
     if (int rc0 = adjoint_check(pr)) return rc0;
@@ -1424,6 +1422,7 @@ int lmm_bermudan_get_gradient_aad(lmm_process* pr, const lmm_bermudan_desc* d, i
         BermudanDdScratch ds;
         ds.d_rec = pr->d_dd_rec;
         ds.d_basis = pr->d_basis;
+        ds.basis_fp32 = pr->precision == LMM_PRECISION_MIXED ? 1 : 0;
         ds.d_svd = pr->d_svd;
         ds.d_omega = z0;
         ds.d_vbar = z0 + om;

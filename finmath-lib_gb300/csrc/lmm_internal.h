@@ -254,7 +254,8 @@ struct BermudanScratch {
 // scratch of the discrete-delta AAD weights of a Bermudan's cash flows (launch_bermudan_dd_weights)
 struct BermudanDdScratch {
     const double* d_rec;      // [2][ne][P] from the forward valuation
-    const double* d_basis;    // [ne][5][P]
+    const void* d_basis;      // [ne][5][P]: doubles (FP64 form) or floats (mixed form)
+    int basis_fp32;
     const double* d_svd;      // [ne][80]
     double* d_moments;        // [ne][64][2]
     double* d_mean;           // [ne]

@@ -833,6 +833,10 @@ __global__ void __launch_bounds__(kProdThreads) bermudan_step_mixed_kernel(const
                 dot2_add(ce, bh[i], x);
                 ce.s = fmaf(bl[i], x, ce.s);
             }
+            if (a.rec) {
+                a.rec[(size_t)a.pending_ex * P + p] = sum2_value(ce);
+                a.rec[((size_t)sh.ne + a.pending_ex) * P + p] = f32_to_f64_int(v - u);
+            }
             if (!(ce.p + ce.s >= 0.0f)) {
                 v = u;
                 a.ex[p] = a.pending_fixing;
@@ -1081,7 +1085,7 @@ int launch_bermudan(const ProductView& v, const BermudanLaunch& a, const Bermuda
     prm.under = sc.d_under;
     prm.ex = sc.d_ex;
     prm.partials = sc.d_partials;
-    prm.rec = v.state_fp32 ? nullptr : sc.d_rec;
+    prm.rec = sc.d_rec;
     int pending = -1;  // exercise index whose choose is pending
     for (int per = a.nper - 1; per >= -1; per--) {
         prm.cur = per;
@@ -1124,7 +1128,7 @@ struct DdSweepParams {
     int q_lo, q_hi;              // periods whose weights this launch writes
     double num0;                 // numeraire at time 0: the value's adjoint seed
     const double* rec;           // [2][ne][P]
-    const double* basis;         // [ne][5][P]
+    const void* basis;           // [ne][5][P] of type TB
     const double* eps;           // [ne]
     const double* svd_cur;       // SVD of the date cur_e
     double* betap;               // [ne][6] projection coefficients
@@ -1135,19 +1139,23 @@ struct DdSweepParams {
     int ne;
 };
 
+// TB: the basis as the forward valuation stored it (double in the FP64 form, float in the mixed
+// form); the sweep itself runs in FP64 in both
+template <typename TB>
 __global__ void __launch_bounds__(kProdThreads) dd_sweep_kernel(const DdSweepParams a)
 {
     double acc[kRhs];
 #pragma unroll
     for (int i = 0; i < kRhs; i++) acc[i] = 0.0;
     double bp[6];
-    const double* bprev = nullptr;
+    const TB* basis = static_cast<const TB*>(a.basis);
+    const TB* bprev = nullptr;
     if (a.prev_e >= 0) {
 #pragma unroll
         for (int i = 0; i < 6; i++) bp[i] = a.betap[a.prev_e * 6 + i];
-        bprev = a.basis + (size_t)a.prev_e * 5 * a.P;
+        bprev = basis + (size_t)a.prev_e * 5 * a.P;
     }
-    const double* bcur = a.cur_e >= 0 ? a.basis + (size_t)a.cur_e * 5 * a.P : nullptr;
+    const TB* bcur = a.cur_e >= 0 ? basis + (size_t)a.cur_e * 5 * a.P : nullptr;
     const double eps = a.cur_e >= 0 ? a.eps[a.cur_e] : 0.0;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.P; p += gridDim.x * blockDim.x) {
         double vb = a.prev_e < 0 && a.q_lo == 0 ? a.num0 : a.vbar[p];
@@ -1156,7 +1164,7 @@ __global__ void __launch_bounds__(kProdThreads) dd_sweep_kernel(const DdSweepPar
             // the projection of the previous date's trigger adjoint, as the estimator forms it
             double d = 1.0 * bp[0];
 #pragma unroll
-            for (int i = 1; i < 6; i++) d = d + bprev[(size_t)(i - 1) * a.P + p] * bp[i];
+            for (int i = 1; i < 6; i++) d = d + (double)bprev[(size_t)(i - 1) * a.P + p] * bp[i];
             vb = vb + d;
             ub = ub - d;
         }
@@ -1172,7 +1180,7 @@ __global__ void __launch_bounds__(kProdThreads) dd_sweep_kernel(const DdSweepPar
             vb = cont ? vb : 0.0;
             acc[0] = acc[0] + xb * 1.0;
 #pragma unroll
-            for (int i = 0; i < 5; i++) acc[1 + i] = acc[1 + i] + xb * bcur[(size_t)i * a.P + p];
+            for (int i = 0; i < 5; i++) acc[1 + i] = acc[1 + i] + xb * (double)bcur[(size_t)i * a.P + p];
         }
         a.vbar[p] = vb;
         a.ubar[p] = ub;
@@ -1270,7 +1278,8 @@ int launch_bermudan_dd_weights(const BermudanLaunch& a, const BermudanDdScratch&
         prm.q_lo = k == 0 ? 0 : ex_period[k - 1];
         prm.q_hi = k < ne ? ex_period[k] : a.nper;
         prm.svd_cur = k < ne ? sc.d_svd + (size_t)k * kSvdStride : nullptr;
-        dd_sweep_kernel<<<blocks, kProdThreads, 0, s>>>(prm);
+        if (sc.basis_fp32) dd_sweep_kernel<float><<<blocks, kProdThreads, 0, s>>>(prm);
+        else dd_sweep_kernel<double><<<blocks, kProdThreads, 0, s>>>(prm);
         LMM_CUDA(cudaGetLastError());
     }
     return LMM_OK;

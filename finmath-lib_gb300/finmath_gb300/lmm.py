@@ -1136,8 +1136,9 @@ class BermudanSwaption:
         """Value, deltas d V / d L_j(0) and vegas d V / d sigma_{i,j} by the adjoint kernel
         (the role of RandomVariableDifferentiable.getGradient with these leaves).  The
         exercise decisions are frozen (diracDeltaApproximationMethod "ZERO"), or the reference
-        AAD's default "DISCRETE_DELTA" sweep weights the cash flows (FP64 processes;
-        RandomVariableDifferentiableAADFactory.java:60-72)."""
+        AAD's default "DISCRETE_DELTA" sweep weights the cash flows
+        (RandomVariableDifferentiableAADFactory.java:60-72; an FP64 sweep in both precision
+        forms)."""
         proc = model.process
         T = len(proc._keep["times"]) - 1
         N = len(proc._keep["tenor"]) - 1

@@ -104,3 +104,24 @@ def test_discrete_delta_method_equals_the_restated_reference(setup):
     assert np.max(np.abs(gdd["deltas"] - g["deltas"])) > 1e-4 * scale_d
     assert np.allclose(setup["gdd0"]["deltas"], g["deltas"], rtol=1e-12, atol=1e-15)
     assert np.allclose(setup["gdd0"]["vegas"], g["vegas"], rtol=1e-12, atol=1e-15)
+
+
+def test_mixed_precision_discrete_delta_close_to_fp64(setup):
+    """The mixed form runs the same DISCRETE_DELTA sweep (FP64 sweep over its FP32 backward
+    induction): its Greeks agree with the FP64 form's to 2e-3 of the largest Greek (paths whose
+    trigger sits at the window's edge may fall on either side in FP32)."""
+    cfg = W.LMM20
+    fix, plen, pay, K = W.bermudan_schedule(cfg)
+    sim32 = W.build(cfg, paths=P, precision=F.PRECISION_MIXED)
+    berm = F.BermudanSwaption(np.ones(len(fix)), fix, plen, pay, 1.0, K, True, "swaprate")
+    g32 = berm.getGradient(sim32, checkpointStride=4, freezeNumeraireAdjustment=True,
+                           diracDeltaApproximationMethod="DISCRETE_DELTA")
+    g64 = setup["gdd"]
+    assert abs(g32["value"] - g64["value"]) <= 1e-5
+    assert np.max(np.abs(g32["deltas"] - g64["deltas"])) <= 2e-3 * np.max(np.abs(g64["deltas"]))
+    assert np.max(np.abs(g32["vegas"] - g64["vegas"])) <= 2e-3 * np.max(np.abs(g64["vegas"]))
+    # and the boundary term is there: it moves the deltas away from the frozen-exercise ones
+    g32z = berm.getGradient(sim32, checkpointStride=4, freezeNumeraireAdjustment=True)
+    assert np.max(np.abs(g32["deltas"] - g32z["deltas"])) > 1e-4 * np.max(np.abs(g64["deltas"]))
+    sim32.process.close()
+    sim32.process.brownianMotion.close()
