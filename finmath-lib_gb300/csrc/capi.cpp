@@ -560,9 +560,9 @@ int lmm_process_create(const lmm_model_desc* m, lmm_brownian* bm, lmm_process** 
         std::vector<float> l32((size_t)T * N * FP, 0.0f);
         for (size_t r = 0; r < (size_t)T * N; r++) {
             for (int k = 0; k < F; k++) l32[r * FP + k] = (float)m->factor_loadings[r * F + k];
-            // the drift's deterministic part of a step, (variance * -0.5) * dt_i, and 1/delta_j,
-            // each rounded once to FP32
-            l32[r * FP + fmax] = (float)var_half_dt[r];
+            // the drift's deterministic part of a step in base-2 units, (variance * -0.5) * dt_i
+            // * log2(e) (the kernel exponentiates with exp2), and 1/delta_j, each rounded once to FP32
+            l32[r * FP + fmax] = (float)(var_half_dt[r] * 1.4426950408889634074);
             l32[r * FP + fmax + 1] = (float)inv_delta[r % N];
         }
         std::vector<float> id32(N), dt32(T), y32(N);

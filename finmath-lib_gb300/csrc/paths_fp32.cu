@@ -133,7 +133,8 @@ __global__ void __launch_bounds__(kPathThreads, fp32_min_blocks(NMAX))
     }
     for (int i = 0; i < a.T; i++) {
         const int first = __ldg(a.d_first + i);
-        const float dt = __ldg(a.d_dt32 + i);
+        // the step's sums in base-2 units: G and dt carry log2(e), so that exp(d) = exp2(d')
+        const float dt = __ldg(a.d_dt32 + i) * 1.4426950408889634f;
         cp_async_wait();
         __syncwarp();  // the warp's staged table of step i is visible to every lane
         // G_k = dW_k + dt S_k, the drift's running sum S_k = sum_{l<=j} os_l lambda_lk carried
@@ -145,6 +146,7 @@ __global__ void __launch_bounds__(kPathThreads, fp32_min_blocks(NMAX))
             const int k0 = 2 * m, k1 = 2 * m + 1;
             G2[m].x = (k0 < F && active) ? sm.dw[i & 1][k0][tid] : 0.0f;
             G2[m].y = (k1 < F && k1 < FMAX && active) ? sm.dw[i & 1][k1 < FMAX ? k1 : 0][tid] : 0.0f;
+            G2[m] = __fmul2_rn(G2[m], make_float2(1.4426950408889634f, 1.4426950408889634f));
         }
         if (i + 1 < a.T) prefetch(i + 1);  // buffers (i+1)&1 were last read in step i-1
         const float* tb = sm.table[warp][i & 1];
@@ -163,18 +165,21 @@ __global__ void __launch_bounds__(kPathThreads, fp32_min_blocks(NMAX))
                 const float Lj = L[j];
                 const float osdt = (Lj * dt) * rcp_approx(Lj + lr[FMAX + 1]);
                 const float2 os2 = make_float2(osdt, osdt);
-                float2 da = make_float2(lr[FMAX], 0.0f), db = make_float2(0.0f, 0.0f);
+                float2 da, db = make_float2(0.0f, 0.0f);
 #pragma unroll
                 for (int m = 0; m < FH; m++) {
                     // factors 2m and 2m+1 (the rows are zero padded beyond F; for an odd FMAX
                     // the last pair's second entry is the drift term, multiplied by G = 0)
                     const float2 l2 = make_float2(lr[2 * m], 2 * m + 1 < FMAX ? lr[2 * m + 1] : 0.0f);
                     G2[m] = __ffma2_rn(os2, l2, G2[m]);
-                    if (m & 1) db = __ffma2_rn(G2[m], l2, db);
+                    if (m == 0) da = __fmul2_rn(G2[m], l2);
+                    else if (m == 1) db = __fmul2_rn(G2[m], l2);
+                    else if (m & 1) db = __ffma2_rn(G2[m], l2, db);
                     else da = __ffma2_rn(G2[m], l2, da);
                 }
-                // exp(d) = 2^(d log2 e)
-                float v = Lj * exp2_approx(((da.x + db.x) + (da.y + db.y)) * 1.4426950408889634f);
+                // exp(d) = 2^d' with d' = d log2(e) (G, dt and the drift term carry the factor)
+                const float2 s2 = __fadd2_rn(da, db);
+                float v = Lj * exp2_approx((s2.x + s2.y) + lr[FMAX]);
                 if (CAPPED) v = fminf(v, cap);
                 L[j] = v;
             }
