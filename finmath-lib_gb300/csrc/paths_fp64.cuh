@@ -109,7 +109,15 @@ __global__ void __launch_bounds__(kPathThreads, fp64_min_blocks(NMAX, FUNCTIONAL
     const double* dW = static_cast<const double*>(a.d_dw);
     double* states = static_cast<double*>(a.d_states);
 
-    const double* etab = a.d_exp_tab;
+    // exp(k/128), |k| <= 128, in shared memory: every 2nd entry of the exp(k/256) table.  The
+    // lanes of a warp gather about twenty distinct entries a component-step; from the L1,
+    // beside the shared-memory state, those gathers kept missing
+    constexpr int kExpHalf = 128;
+    static_assert(kExpTableHalf % kExpHalf == 0, "the shared table takes every n-th entry");
+    __shared__ double etab_s[2 * kExpHalf + 1];
+    for (int q = threadIdx.x; q <= 2 * kExpHalf; q += kPathThreads)
+        etab_s[q] = __ldg(a.d_exp_tab + kExpTableHalf + (q - kExpHalf) * (kExpTableHalf / kExpHalf));
+    __syncthreads();
     __shared__ double state_smem[SMEM ? NMAX : 1][kPathThreads];
     PathState<NMAX, SMEM> L;
     if constexpr (SMEM) L.col = &state_smem[0][threadIdx.x];
@@ -150,14 +158,27 @@ __global__ void __launch_bounds__(kPathThreads, fp64_min_blocks(NMAX, FUNCTIONAL
         // component j is then  d_j = mu_j dt + sum_k dW_k lambda_jk = sum_k G_k lambda_jk
         // - dt variance_j / 2, two double-float multiply-adds per factor on the FP32 pipe
         // factor pairs (2m, 2m+1) side by side in the lanes of float2 registers
+        // (the increments, read once, bypass the L1, which keeps the component rows)
         float2 Gh[FMAX / 2], Gl[FMAX / 2];
 #pragma unroll
         for (int m = 0; m < FMAX / 2; m++) {
             float h0 = 0.0f, l0 = 0.0f, h1 = 0.0f, l1 = 0.0f;
-            if (2 * m < F && active) df_split_int(dW[((size_t)i * F + 2 * m) * P + p], h0, l0);
-            if (2 * m + 1 < F && active) df_split_int(dW[((size_t)i * F + 2 * m + 1) * P + p], h1, l1);
+            if (2 * m < F && active) df_split_int(__ldcg(dW + ((size_t)i * F + 2 * m) * P + p), h0, l0);
+            if (2 * m + 1 < F && active) df_split_int(__ldcg(dW + ((size_t)i * F + 2 * m + 1) * P + p), h1, l1);
             Gh[m] = make_float2(h0, h1);
             Gl[m] = make_float2(l0, l1);
+        }
+        // the next step's component rows into this SM's L1 (one 128-byte line per thread; the
+        // first warp of every SM to reach a step would otherwise wait on their L2 round trips)
+        // and this path's next increments into L2
+        if (i + 1 < a.T) {
+            const int row_lines = (N * FPD * (int)sizeof(float) + 127) / 128;
+            const char* nrows = reinterpret_cast<const char*>(a.d_rows_df + (size_t)(i + 1) * N * FPD);
+            for (int q = threadIdx.x; q < row_lines; q += kPathThreads)
+                asm volatile("prefetch.global.L1 [%0];" ::"l"(nrows + 128 * q));
+            if (active)
+                for (int k = 0; k < F; k++)
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(dW + ((size_t)(i + 1) * F + k) * P + p));
         }
         auto component_step = [&](auto jc) {
             const int j = jc.value;
@@ -212,11 +233,12 @@ __global__ void __launch_bounds__(kPathThreads, fp64_min_blocks(NMAX, FUNCTIONAL
                     df_dot_acc2(acc_h, acc_l, Gh[m], Gl[m], bh, bl, bn);  // d += G_k lambda_k
                 }
                 const float dp = acc_h.x, ep = acc_h.y, ds = acc_l.x, es = acc_l.y;
-                // exp(d) by the table method of exp_small (fp64math.cuh), k = rint(256 d): the
-                // remainder r = (dh - k/256) + dl (|r| <= 1/512, its high part exact in FP32)
-                // and exp(r) = 1 + r + r^2 B(r), B = 1/2 + r/6 + r^2/24 + r^3/120, as a float
-                // pair s + low (B - 1/2 in FP32: it enters times r^2 <= 2^-18); then
-                // L exp(k/256) (s + low) in three FP64 instructions
+                // exp(d) by the table method of exp_small (fp64math.cuh) with k = rint(128 d):
+                // the remainder r = (dh - k/128) + dl (|r| <= 1/256, its high part exact in
+                // FP32) and exp(r) = 1 + r + r^2 B(r), B = 1/2 + r/6 + r^2/24 + r^3/120
+                // (truncation below 2^-57), as a float pair s + low (B - 1/2 in FP32: it
+                // enters times r^2 <= 2^-16); then L exp(k/128) (s + low) in three FP64
+                // instructions
                 float dh, dl;
                 {
                     float x, q;
@@ -226,9 +248,9 @@ __global__ void __launch_bounds__(kPathThreads, fp64_min_blocks(NMAX, FUNCTIONAL
                 const double base = FUNCTIONAL ? Lj : E[FUNCTIONAL ? 0 : j];
                 double nv;
                 if (fabsf(dh) <= 1.0f) {
-                    const float t = fmaf(dh, (float)kExpTableHalf, 12582912.0f);  // 1.5 2^23 + rint(256 dh)
+                    const float t = fmaf(dh, (float)kExpHalf, 12582912.0f);  // 1.5 2^23 + rint(128 dh)
                     const int kk = __float_as_int(t) - 0x4b400000;
-                    const float rh = fmaf(-(t - 12582912.0f), 1.0f / kExpTableHalf, dh);  // exact
+                    const float rh = fmaf(-(t - 12582912.0f), 1.0f / kExpHalf, dh);  // exact
                     const float r2h = __fmul_rn(rh, rh);
                     const float r2e = fmaf(rh, rh, -r2h) + (rh + rh) * dl;  // r^2 - r2h
                     const float bt = rh * fmaf(rh, fmaf(rh, 1.0f / 120.0f, 1.0f / 24.0f), 1.0f / 6.0f);
@@ -239,7 +261,7 @@ __global__ void __launch_bounds__(kPathThreads, fp64_min_blocks(NMAX, FUNCTIONAL
                     const float s2 = s1 + th;
                     const float e2 = th - (s2 - s1);
                     const float low = (e1 + e2) + (dl + tl);
-                    const double scaled = base * __ldg(etab + kExpTableHalf + kk);  // L exp(k/256)
+                    const double scaled = base * etab_s[kExpHalf + kk];  // L exp(k/128)
                     nv = fma(scaled, f32_to_f64_nz(low), scaled * f32_to_f64_nz(s2));
                 } else {
                     nv = base * exp(df_to_double(dh, dl));
