@@ -11,6 +11,7 @@
 // Compiled with -fmad=false (unfused FP64, as the reference's Java).
 #include "lmm_internal.h"
 #include "reduce.cuh"
+#include "exact_sum.cuh"
 
 #include <math_constants.h>
 #include <cstring>
@@ -574,12 +575,8 @@ __device__ void regression_solve(const double* partials, int blocks, int P, cons
     __shared__ double b[kRhs];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (warp < kRhs) {
-        dd acc{0.0, 0.0};
-        for (int k = lane; k < blocks; k += 32) {
-            const double* q = partials + ((size_t)k * kRhs + warp) * 2;
-            acc = dd_add(acc, dd{q[0], q[1]});
-        }
-        acc = warp_dd_sum(acc);
+        // the blocks' double-double partials of column `warp`, summed exactly
+        const dd acc = warp_exact_pair_sum(partials + (size_t)warp * 2, blocks, kRhs * 2);
         if (lane == 0) b[warp] = (acc.hi + acc.lo) / (double)P;
     }
     __syncthreads();
@@ -607,12 +604,8 @@ __device__ void regression_solve_mixed(const double* partials, int blocks, int P
     __shared__ double b[kRhs];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (warp < kRhs) {
-        dd acc{0.0, 0.0};
-        for (int k = lane; k < blocks; k += 32) {
-            const double* q = partials + ((size_t)k * kRhs + warp) * 2;
-            acc = dd_add(acc, dd{q[0], q[1]});
-        }
-        acc = warp_dd_sum(acc);
+        // the blocks' double-double partials of column `warp`, summed exactly
+        const dd acc = warp_exact_pair_sum(partials + (size_t)warp * 2, blocks, kRhs * 2);
         if (lane == 0) b[warp] = (acc.hi + acc.lo) / (double)P;
     }
     __syncthreads();
