@@ -234,9 +234,10 @@ __global__ void __launch_bounds__(kPathThreads, fp64_min_blocks(NMAX, FUNCTIONAL
                 }
                 const float dp = acc_h.x, ep = acc_h.y, ds = acc_l.x, es = acc_l.y;
                 // exp(d) by the table method of exp_small (fp64math.cuh) with k = rint(128 d):
-                // the remainder r = (dh - k/128) + dl (|r| <= 1/256, its high part exact in
-                // FP32) and exp(r) = 1 + r + r^2 B(r), B = 1/2 + r/6 + r^2/24 + r^3/120
-                // (truncation below 2^-57), as a float pair s + low (B - 1/2 in FP32: it
+                // the remainder r = rh + dl, rh = dh - k/128 (|rh| <= 1/256, exact in FP32),
+                // and exp(r) = 1 + r + r^2 B, B = 1/2 + rh/6 + rh^2/24 + rh^3/120 + dl/2
+                // (dl/2: the low part's first-order share of r^3/6, up to 2^-44 with this
+                // table; truncation below 2^-57), as a float pair s + low (B - 1/2 in FP32: it
                 // enters times r^2 <= 2^-16); then L exp(k/128) (s + low) in three FP64
                 // instructions
                 float dh, dl;
@@ -253,7 +254,7 @@ __global__ void __launch_bounds__(kPathThreads, fp64_min_blocks(NMAX, FUNCTIONAL
                     const float rh = fmaf(-(t - 12582912.0f), 1.0f / kExpHalf, dh);  // exact
                     const float r2h = __fmul_rn(rh, rh);
                     const float r2e = fmaf(rh, rh, -r2h) + (rh + rh) * dl;  // r^2 - r2h
-                    const float bt = rh * fmaf(rh, fmaf(rh, 1.0f / 120.0f, 1.0f / 24.0f), 1.0f / 6.0f);
+                    const float bt = fmaf(dl, 0.5f, rh * fmaf(rh, fmaf(rh, 1.0f / 120.0f, 1.0f / 24.0f), 1.0f / 6.0f));
                     const float th = 0.5f * r2h;                      // exact
                     const float tl = fmaf(r2h, bt, 0.5f * r2e);
                     const float s1 = 1.0f + rh;                       // |1| >= |rh|: fast TwoSum
