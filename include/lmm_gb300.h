@@ -239,8 +239,11 @@ int lmm_bermudan_get_value(lmm_process* proc, const lmm_bermudan_desc* product, 
  *   - num_values must be in [1, 2^30]; larger inputs are rejected with LMM_ERR_INVALID;
  *   - every call shares that array: calls that overlap on the GPU (different streams, or
  *     different host threads on one device) race and must be serialised by the caller;
+ *   - the call copies its two results to the host and waits for them, so it must not be
+ *     made while any stream is being captured into a graph (the capture would be
+ *     invalidated); graph users call it between graph launches;
  *   - the first call on a device looks up the array's device address (which may load the
- *     library's GPU code on that device); make that first call before any stream capture;
+ *     library's GPU code on that device);
  *   - the looked-up address is kept for the life of the process: the library must not be
  *     used on a device after cudaDeviceReset there.
  * stream is a cudaStream_t (NULL = the legacy default stream); d_values must be ready in
