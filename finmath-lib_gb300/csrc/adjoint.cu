@@ -92,10 +92,6 @@ struct Pair<double> {
 template <typename R, int FMAX>
 __host__ __device__ constexpr int f_pitch() { return (FMAX + Vec<R>::W - 1) / Vec<R>::W * Vec<R>::W; }
 
-// row pitch (elements) of a warp's transpose buffer: 16-byte rows, conflict-free vector reads
-template <typename R>
-__host__ __device__ constexpr int red_pitch() { return sizeof(R) == 4 ? 36 : 34; }
-
 template <typename R>
 struct AdjTables {
     const R* lam;       // [T][N][F] factor loadings (replay)
@@ -125,21 +121,44 @@ struct RevParams {
     double* delta_partials;  // [warps][N]
 };
 
-// sum of row r of a warp's transpose buffer over the 32 lanes, in fixed order
+// Sums over the warp's 32 lanes of eight values a lane holds (v[0..7], overwritten): three
+// transposed exchange levels (offsets 16, 8, 4), at each of which a lane keeps half of what it
+// holds and adds its partner's copy of that half, then two plain levels (offsets 2, 1).
+// Every lane returns the total of value (lane >> 2) & 7; the order of the additions is fixed.
+// All 32 lanes must call it.  It takes 7 exchanges and 2 plain shuffles for eight sums, and
+// no shared memory (a transpose buffer of the warp's per-component values would hold
+// NMAX x 32 values per warp).
 template <typename R>
-__device__ __forceinline__ double row_sum(const R* red, int r)
+__device__ __forceinline__ R warp_sum8_transposed(R (&v)[8], int lane)
 {
-    using V = Vec<R>;
-    const typename V::T* row = reinterpret_cast<const typename V::T*>(red + r * red_pitch<R>());
-    R acc = R(0);
+    {
+        const bool up = (lane & 16) != 0;
 #pragma unroll
-    for (int q = 0; q < 32 / V::W; q++) {
-        R e[V::W];
-        V::unpack(row[q], e);
-#pragma unroll
-        for (int w = 0; w < V::W; w++) acc += e[w];
+        for (int i = 0; i < 4; i++) {
+            const R send = up ? v[i] : v[i + 4];
+            const R keep = up ? v[i + 4] : v[i];
+            v[i] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+        }
     }
-    return (double)acc;
+    {
+        const bool up = (lane & 8) != 0;
+#pragma unroll
+        for (int i = 0; i < 2; i++) {
+            const R send = up ? v[i] : v[i + 2];
+            const R keep = up ? v[i + 2] : v[i];
+            v[i] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+        }
+    }
+    {
+        const bool up = (lane & 4) != 0;
+        const R send = up ? v[0] : v[1];
+        const R keep = up ? v[1] : v[0];
+        v[0] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+    }
+    R t = v[0];
+    t += __shfl_xor_sync(0xffffffffu, t, 2);
+    t += __shfl_xor_sync(0xffffffffu, t, 1);
+    return t;
 }
 
 // FP32 sweeps stage each step's factor table in shared memory; FP64 ones read it from L1/L2
@@ -171,50 +190,53 @@ __device__ __forceinline__ void cp_async16(void* dst, const void* src)
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
-// resident warps per SM the register budget is sized for: 12 in FP32, 8 in FP64 (whose
-// arrays are twice as wide and whose FP64 pipe, not latency, bounds the sweep)
+// resident warps per SM the grid is sized for (the shared memory of 40 components holds it
+// there): 12 in FP32, 8 in FP64
+template <typename R>
+__host__ __device__ constexpr int rev_warps_per_sm() { return sizeof(R) == 4 ? 12 : 8; }
 template <typename R, int TH>
-__host__ __device__ constexpr int rev_min_blocks() { return (sizeof(R) == 4 ? 384 : 256) / TH > 0 ? (sizeof(R) == 4 ? 384 : 256) / TH : 1; }
+__host__ __device__ constexpr int rev_min_blocks() { return rev_warps_per_sm<R>() * 32 / TH > 0 ? rev_warps_per_sm<R>() * 32 / TH : 1; }
 
-// shared memory of the reverse kernel: the warps' transpose buffers, the step buffer
-// [NMAX][TH] of one step's forward rates, two increment buffers [2][FMAX][TH], and (FP32)
-// per warp two copies of a step's factor rows and volatilities [2][NMAX*pitch + NMAX]
+// shared memory of the reverse kernel: the step buffer [NMAX][TH] of one step's forward
+// rates, the adjoint buffer [NMAX][TH], two increment buffers [2][FMAX][TH], and (FP32) per
+// warp two copies of a step's factor rows and volatilities [2][NMAX*pitch + NMAX]
 template <typename R, int NMAX, int FMAX>
 __host__ __device__ constexpr int rev_table_elems() { return NMAX * f_pitch<R, FMAX>() + NMAX; }
 template <typename R, int NMAX, int FMAX, int TH>
-__host__ __device__ constexpr size_t rev_red_bytes() { return (size_t)(TH / 32) * NMAX * red_pitch<R>() * sizeof(R); }
-template <typename R, int NMAX, int FMAX, int TH>
 __host__ __device__ constexpr size_t rev_smem_bytes()
 {
-    return rev_red_bytes<R, NMAX, FMAX, TH>() + (size_t)(NMAX + 2 * FMAX) * TH * sizeof(R) +
+    return (size_t)(2 * NMAX + 2 * FMAX) * TH * sizeof(R) +
            (rev_stage_tables<R>() ? (size_t)(TH / 32) * 2 * rev_table_elems<R, NMAX, FMAX>() * sizeof(R) : 0);
 }
 
 // Reverse sweep over the steps [n_lo, n_hi) of every path, from stored forward rates.
 // One thread per path (grid-stride over path batches; the partition is fixed by the grid, so
-// the per-warp partial sums and their order do not depend on the checkpoint stride).  Each
-// thread prefetches its own path's forward rates and increments of the next step into shared
-// memory (cp.async) while it works on the current step.  The copy into the rate buffer is
-// issued only after every rate of the current step has been consumed (FP32: by the forward
-// pass; FP64: by the reverse pass); the increments alternate between two buffers.  In FP32
-// each warp also stages the next step's factor rows and volatilities (16-byte copies by its
-// lanes, two buffers), read back as broadcast shared-memory vectors.  The per-warp partial
-// sums are fire-and-forget reductions (one lane per entry, so their order is program order).
+// the per-warp partial sums and their order do not depend on the checkpoint stride).  The
+// path's forward rates of the step and its adjoint vector Ybar live in the thread's own
+// columns of shared memory, so that both component passes are rolled loops over the live
+// components [first, NE): fully unrolled over 40 components the sweep overflowed the
+// instruction cache (a fifth of the fetches missed).  The reverse pass runs over chunks of
+// eight components, unrolled within a chunk, and takes the per-warp vega sums of each chunk
+// by a transposed shuffle reduction.  Each thread prefetches its path's forward rates and
+// increments of the next step (cp.async) once the current step's rates are consumed; the
+// increments alternate between two buffers.  In FP32 each warp also stages the next step's
+// factor rows and volatilities (16-byte copies by its lanes, two buffers), read back as
+// broadcast shared-memory vectors.  The per-warp partial sums are fire-and-forget
+// reductions (one lane per entry, so their order is program order).
 template <typename R, int NMAX, int FMAX, int TH>
 __global__ void __launch_bounds__(TH, rev_min_blocks<R, TH>()) reverse_kernel(const RevParams a, const AdjTables<R> tb)
 {
     constexpr int FP = f_pitch<R, FMAX>();
-    constexpr int RS = red_pitch<R>();
-    constexpr bool kKeepOs = sizeof(R) == 4;  // FP64 recomputes os_j in the reverse pass (registers)
+    static_assert(NMAX % 8 == 0, "the per-warp sums work on chunks of eight components");
     using V = Vec<R>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    R* red = reinterpret_cast<R*>(smem_raw) + (size_t)warp * NMAX * RS;  // [NMAX][RS] of this warp
-    R* sbuf = reinterpret_cast<R*>(smem_raw + rev_red_bytes<R, NMAX, FMAX, TH>()) + tid;  // [NMAX][TH], own column
-    R* wbuf = sbuf + NMAX * TH;                                                            // [2][FMAX][TH], own column
+    R* sbuf = reinterpret_cast<R*>(smem_raw) + tid;  // [NMAX][TH]: the step's forward rates, own column
+    R* ybuf = sbuf + NMAX * TH;                       // [NMAX][TH]: Ybar, own column
+    R* wbuf = ybuf + NMAX * TH;                       // [2][FMAX][TH]: increments, own column
     constexpr int TE_ = rev_table_elems<R, NMAX, FMAX>();
-    R* tbuf = reinterpret_cast<R*>(smem_raw + rev_red_bytes<R, NMAX, FMAX, TH>()) + (NMAX + 2 * FMAX) * TH +
-              (size_t)warp * 2 * TE_;                                                      // [2][NMAX*FP + NMAX] of this warp
+    R* tbuf = reinterpret_cast<R*>(smem_raw) + (2 * NMAX + 2 * FMAX) * TH +
+              (size_t)warp * 2 * TE_;                 // [2][NMAX*FP + NMAX] of this warp
     const int N = a.N, F = a.F, NE = a.n_eff;
     const size_t gw = (size_t)blockIdx.x * (TH / 32) + warp;
     double* vp = a.vega_partials + gw * a.T * N;
@@ -238,9 +260,7 @@ __global__ void __launch_bounds__(TH, rev_min_blocks<R, TH>()) reverse_kernel(co
             if (active) {
                 const int fst = __ldg(a.first + n);
                 const R* Ls = states + (size_t)(n - a.base_step) * N * a.P + p;
-#pragma unroll
-                for (int j = 0; j < NMAX; j++)
-                    if (j < NE && j >= fst) cp_async(sbuf + j * TH, Ls + (size_t)j * a.P);
+                for (int j = fst; j < NE; j++) cp_async(sbuf + j * TH, Ls + (size_t)j * a.P);
                 R* wb = wbuf + (n & 1) * FMAX * TH;
 #pragma unroll
                 for (int k = 0; k < FMAX; k++)
@@ -249,13 +269,11 @@ __global__ void __launch_bounds__(TH, rev_min_blocks<R, TH>()) reverse_kernel(co
             cp_async_commit();
         };
         prefetch(a.n_hi - 1);
-        R Ybar[NMAX];
         if (a.seed) {
             const R* Ls = states + (size_t)(a.t_end - a.base_step) * N * a.P;
-#pragma unroll
-            for (int j = 0; j < NMAX; j++) {
+            for (int j = 0; j < NE; j++) {
                 R yb = R(0);
-                if (j < NE && active) {
+                if (active) {
                     const R sd = static_cast<const R*>(a.seeds)[(size_t)j * a.P + p];
                     if (a.normal) {
                         yb = sd;  // the state is L: its adjoint is the seed
@@ -264,12 +282,11 @@ __global__ void __launch_bounds__(TH, rev_min_blocks<R, TH>()) reverse_kernel(co
                         if (!(a.capped && L >= cap)) yb = sd * L;
                     }
                 }
-                Ybar[j] = yb;
+                ybuf[j * TH] = yb;
             }
         } else {
             const R* yb = static_cast<const R*>(a.ybar);
-#pragma unroll
-            for (int j = 0; j < NMAX; j++) Ybar[j] = (j < NE && active) ? yb[(size_t)j * a.P + p] : R(0);
+            for (int j = 0; j < NE; j++) ybuf[j * TH] = active ? yb[(size_t)j * a.P + p] : R(0);
         }
 
         for (int n = a.n_hi - 1; n >= a.n_lo; n--) {
@@ -291,99 +308,87 @@ __global__ void __launch_bounds__(TH, rev_min_blocks<R, TH>()) reverse_kernel(co
                 S[m] = Pair<R>::mk(R(0), R(0));
                 Rk[m] = Pair<R>::mk(R(0), R(0));
             }
+            // os_j = L/(L + 1/d) (LOGNORMAL) or d/(1 + d L) = 1/(L + 1/d) (NORMAL)
+            auto os_of = [&](int j, R L) { return fdiv<R>(a.normal ? R(1) : L, L + tb.inv_delta[j]); };
             // forward pass of the step: S_k = sum_j os_j sigma_j f_jk
-            R os[kKeepOs ? NMAX : 1];
-            unsigned long long capmask = 0ull;
+            unsigned long long capmask = 0ull;  // capped models have at most 64 components
+#pragma unroll 2
+            for (int j = first; j < NE; j++) {
+                const R L = active ? sbuf[j * TH] : R(0);
+                if (a.capped && L >= cap && j < 64) capmask |= 1ull << j;
+                const R oss2s = os_of(j, L) * sig[j];
+                R fr[FP];
 #pragma unroll
-            for (int j = 0; j < NMAX; j++) {
-                if (j < NE && j >= first) {
-                    const R L = active ? sbuf[j * TH] : R(0);
-                    if (a.capped && L >= cap) capmask |= 1ull << j;
-                    // os_j = L/(L + 1/d) (LOGNORMAL) or d/(1 + d L) = 1/(L + 1/d) (NORMAL)
-                    const R o = fdiv<R>(a.normal ? R(1) : L, L + tb.inv_delta[j]);
-                    if (kKeepOs) os[kKeepOs ? j : 0] = o;
-                    const R oss = o * sig[j];
-                    R fr[FP];
+                for (int q = 0; q < FP / V::W; q++) V::unpack(load_row<R>(frow + j * FP, q), fr + q * V::W);
+                const PT oss2 = Pair<R>::mk(oss2s, oss2s);
 #pragma unroll
-                    for (int q = 0; q < FP / V::W; q++) V::unpack(load_row<R>(frow + j * FP, q), fr + q * V::W);
-                    const PT oss2 = Pair<R>::mk(oss, oss);
-#pragma unroll
-                    for (int m = 0; m < FH; m++) S[m] = Pair<R>::fma(oss2, Pair<R>::mk(fr[2 * m], fr[2 * m + 1]), S[m]);
-                }
+                for (int m = 0; m < FH; m++) S[m] = Pair<R>::fma(oss2, Pair<R>::mk(fr[2 * m], fr[2 * m + 1]), S[m]);
             }
-            // the step buffer is free once the forward pass consumed it (FP32) -- fetch the next step
-            if (kKeepOs && n - 1 >= a.n_lo) prefetch(n - 1);
-            // reverse pass over the components
+            // reverse pass over the components, by chunks of eight from the chunk of NE-1 down
+            // to the chunk of first; each chunk's per-warp vega sums as it completes
+            for (int c = (NE - 1) >> 3; c >= (first >> 3); c--) {
+                R vch[8];
 #pragma unroll
-            for (int jj = NMAX - 1; jj >= 0; jj--) {
-                const int j = jj;
-                if (j < NE && j >= first) {
-                    R o;
-                    if (kKeepOs) {
-                        o = os[kKeepOs ? j : 0];
-                    } else {
+                for (int i = 7; i >= 0; i--) {
+                    const int j = 8 * c + i;
+                    vch[i] = R(0);
+                    if (j < NE && j >= first) {
                         const R L = active ? sbuf[j * TH] : R(0);
-                        o = fdiv<R>(a.normal ? R(1) : L, L + tb.inv_delta[j]);
-                    }
-                    const R sg = sig[j];
-                    const R yb = Ybar[j];
-                    const R mub = yb * dt;
-                    const R mubs = mub * sg;
-                    const R oss = o * sg;
-                    R fr[FP];
+                        const R o = os_of(j, L);
+                        const R sg = sig[j];
+                        const R yb = ybuf[j * TH];
+                        const R mub = yb * dt;
+                        const R mubs = mub * sg;
+                        const R oss = o * sg;
+                        R fr[FP];
 #pragma unroll
-                    for (int q = 0; q < FP / V::W; q++) V::unpack(load_row<R>(frow + j * FP, q), fr + q * V::W);
-                    const PT mubs2 = Pair<R>::mk(mubs, mubs), noss2 = Pair<R>::mk(-oss, -oss);
-                    PT A2 = Pair<R>::mk(R(0), R(0)), B2 = A2, D2 = A2;
+                        for (int q = 0; q < FP / V::W; q++) V::unpack(load_row<R>(frow + j * FP, q), fr + q * V::W);
+                        const PT mubs2 = Pair<R>::mk(mubs, mubs), noss2 = Pair<R>::mk(-oss, -oss);
+                        PT A2 = Pair<R>::mk(R(0), R(0)), B2 = A2, D2 = A2;
 #pragma unroll
-                    for (int m = 0; m < FH; m++) {
-                        const PT f2 = Pair<R>::mk(fr[2 * m], fr[2 * m + 1]);
-                        Rk[m] = Pair<R>::fma(mubs2, f2, Rk[m]);  // R_k = sum_{l>=j} mubar_l lam_lk
-                        A2 = Pair<R>::fma(Rk[m], f2, A2);
-                        B2 = Pair<R>::fma(S[m], f2, B2);         // S^(j)
-                        D2 = Pair<R>::fma(dw[m], f2, D2);
-                        S[m] = Pair<R>::fma(noss2, f2, S[m]);    // S^(j-1)
+                        for (int m = 0; m < FH; m++) {
+                            const PT f2 = Pair<R>::mk(fr[2 * m], fr[2 * m + 1]);
+                            Rk[m] = Pair<R>::fma(mubs2, f2, Rk[m]);  // R_k = sum_{l>=j} mubar_l lam_lk
+                            A2 = Pair<R>::fma(Rk[m], f2, A2);
+                            B2 = Pair<R>::fma(S[m], f2, B2);         // S^(j)
+                            D2 = Pair<R>::fma(dw[m], f2, D2);
+                            S[m] = Pair<R>::fma(noss2, f2, S[m]);    // S^(j-1)
+                        }
+                        const R A = A2.x + A2.y, B = B2.x + B2.y, D = D2.x + D2.y;
+                        // sigmabar_ij = sum_k lambar_jk f_jk - mubar_j sigma_ij with
+                        // lambar_jk = mubar_j S_k + os_j R_k + Ybar'_j dW_k
+                        // (NORMAL: no -variance/2 drift term, so no -mubar_j sigma_ij)
+                        vch[i] = active ? (mub * B + o * A + yb * D - (a.normal ? R(0) : mubs)) : R(0);
+                        // osbar_j = sigma_j A;  d os_j / d Y_j = os_j (1 - os_j) (LOGNORMAL, zero
+                        // where capped), d os_j / d L_j = -os_j^2 (NORMAL)
+                        if (a.normal) ybuf[j * TH] = yb - (sg * A) * (o * o);
+                        else if (!(a.capped && j < 64 && ((capmask >> j) & 1ull))) ybuf[j * TH] = yb + (sg * A) * (o * (R(1) - o));
                     }
-                    const R A = A2.x + A2.y, B = B2.x + B2.y, D = D2.x + D2.y;
-                    // sigmabar_ij = sum_k lambar_jk f_jk - mubar_j sigma_ij with
-                    // lambar_jk = mubar_j S_k + os_j R_k + Ybar'_j dW_k
-                    // (NORMAL: no -variance/2 drift term, so no -mubar_j sigma_ij)
-                    red[j * RS + lane] = active ? (mub * B + o * A + yb * D - (a.normal ? R(0) : mubs)) : R(0);
-                    // osbar_j = sigma_j A;  d os_j / d Y_j = os_j (1 - os_j) (LOGNORMAL, zero where
-                    // capped), d os_j / d L_j = -os_j^2 (NORMAL)
-                    if (a.normal) Ybar[j] = yb - (sg * A) * (o * o);
-                    else if (!(a.capped && ((capmask >> j) & 1ull))) Ybar[j] = yb + (sg * A) * (o * (R(1) - o));
                 }
+                const R sum = warp_sum8_transposed<R>(vch, lane);
+                const int r = 8 * c + ((lane >> 2) & 7);
+                if ((lane & 3) == 0 && r < NE && r >= first) atomicAdd(vp + (size_t)n * N + r, (double)sum);
             }
-            if (!kKeepOs && n - 1 >= a.n_lo) prefetch(n - 1);
-            __syncwarp();
-#pragma unroll
-            for (int h = 0; h < (NMAX + 31) / 32; h++) {
-                const int r = lane + 32 * h;
-                if (r < NE && r >= first) atomicAdd(vp + (size_t)n * N + r, row_sum<R>(red, r));
-            }
-            __syncwarp();
+            // the step's rates are consumed -- fetch the next step
+            if (n - 1 >= a.n_lo) prefetch(n - 1);
         }
 
         if (a.n_lo > 0) {
             R* yb = static_cast<R*>(a.ybar);
-#pragma unroll
-            for (int j = 0; j < NMAX; j++)
-                if (j < NE && active) yb[(size_t)j * a.P + p] = Ybar[j];
+            if (active)
+                for (int j = 0; j < NE; j++) yb[(size_t)j * a.P + p] = ybuf[j * TH];
         } else {
             // deltas: Y_0 = log(L_0(0)) -> d value / d L_0 = Ybar / L_0, the uniform division
             // applied to the warp's sum (one division per component and warp, not per path);
             // NORMAL: the state is L_0 itself
+            for (int c = 0; 8 * c < NE; c++) {
+                R v8[8];
 #pragma unroll
-            for (int j = 0; j < NMAX; j++)
-                if (j < NE) red[j * RS + lane] = active ? Ybar[j] : R(0);
-            __syncwarp();
-#pragma unroll
-            for (int h = 0; h < (NMAX + 31) / 32; h++) {
-                const int r = lane + 32 * h;
-                if (r < NE) atomicAdd(a.delta_partials + gw * N + r, a.normal ? row_sum<R>(red, r) : row_sum<R>(red, r) / a.init[r]);
+                for (int i = 0; i < 8; i++) v8[i] = (8 * c + i < NE && active) ? ybuf[(8 * c + i) * TH] : R(0);
+                const R sum = warp_sum8_transposed<R>(v8, lane);
+                const int r = 8 * c + ((lane >> 2) & 7);
+                if ((lane & 3) == 0 && r < NE) atomicAdd(a.delta_partials + gw * N + r, a.normal ? (double)sum : (double)sum / a.init[r]);
             }
-            __syncwarp();
         }
     }
     cp_async_wait();
@@ -851,7 +856,7 @@ int adjoint_blocks(int P, int threads, int fp32)
 {
     int dev = 0, sms = 152;
     if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int want = sms * std::max(1, (fp32 ? 384 : 256) / threads);  // the resident blocks of rev_min_blocks
+    const int want = sms * std::max(1, (fp32 ? rev_warps_per_sm<float>() : rev_warps_per_sm<double>()) * 32 / threads);  // the resident blocks of rev_min_blocks
     const int need = (P + threads - 1) / threads;
     return need < want ? need : want;
 }
