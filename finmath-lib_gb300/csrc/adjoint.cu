@@ -31,6 +31,8 @@
 
 #include "lmm_internal.h"
 #include "reduce.cuh"
+#include "euler_fp32.cuh"
+#include "unroll_range.cuh"
 
 namespace lmm {
 namespace {
@@ -458,6 +460,70 @@ __global__ void __launch_bounds__(128) replay_kernel(const ReplayParams a, const
     }
 }
 
+// The mixed form's replay: the steps [n0, n_stop) of every path from the checkpoint at n0 by
+// the FP32 path kernel's own component step (euler_fp32.cuh), on its own rows and time
+// steps, so that every replayed forward rate is bit for bit the one the path kernel computed
+// (components at or beyond n_eff do not enter components below it).  The state lives in
+// registers and the component loop enters its unrolled sequence at the step's first live
+// component, as in the path kernel.
+struct Replay32Params {
+    int N, F, P, n0, n_stop, n_eff;
+    float cap;
+    const int* first;
+    const float* ckpt_slot;  // [N][P] forward rates at n0
+    const float* rows32;     // [T][N][pitch]
+    const float* dt32;       // [T]
+    const float* dw;         // [T][F][P]
+    float* seg;              // [n_stop-n0+1][N][P]
+};
+
+template <int NMAX, int FMAX, bool CAPPED>
+__global__ void __launch_bounds__(128) replay32_kernel(const Replay32Params a)
+{
+    constexpr int FP = euler32::row_pitch(FMAX);
+    constexpr int FH = (FMAX + 1) / 2;
+    const int p = blockIdx.x * 128 + threadIdx.x;
+    if (p >= a.P) return;
+    const int N = a.N, F = a.F, NE = a.n_eff, P = a.P;
+    float L[NMAX];
+#pragma unroll
+    for (int j = 0; j < NMAX; j++) {
+        L[j] = j < NE ? a.ckpt_slot[(size_t)j * P + p] : 0.0f;
+        if (j < NE) a.seg[(size_t)j * P + p] = L[j];
+    }
+    for (int n = a.n0; n < a.n_stop; n++) {
+        const int first = __ldg(a.first + n);
+        const float dt = euler32::step_dt(a.dt32, n);
+        float2 G2[FH];
+#pragma unroll
+        for (int m = 0; m < FH; m++) {
+            const int k0 = 2 * m, k1 = 2 * m + 1;
+            G2[m] = euler32::start_sum(k0 < F ? a.dw[((size_t)n * F + k0) * P + p] : 0.0f,
+                                       (k1 < F && k1 < FMAX) ? a.dw[((size_t)n * F + (k1 < FMAX ? k1 : 0)) * P + p] : 0.0f);
+        }
+        const float4* rows = reinterpret_cast<const float4*>(a.rows32 + (size_t)n * N * FP);
+        for_up_from<NMAX>(first, [&](auto jc) {
+            constexpr int j = decltype(jc)::value;
+            if (j < NE) {
+                float lr[FP];
+#pragma unroll
+                for (int q = 0; q < FP / 4; q++) {
+                    const float4 v = __ldg(rows + j * (FP / 4) + q);
+                    lr[4 * q] = v.x;
+                    lr[4 * q + 1] = v.y;
+                    lr[4 * q + 2] = v.z;
+                    lr[4 * q + 3] = v.w;
+                }
+                L[j] = euler32::component_step<FMAX, CAPPED>(L[j], lr, dt, G2, a.cap);
+            }
+        });
+        float* out = a.seg + (size_t)(n + 1 - a.n0) * N * P;
+#pragma unroll
+        for (int j = 0; j < NMAX; j++)
+            if (j < NE) out[(size_t)j * P + p] = L[j];
+    }
+}
+
 // ------------------------------------------------------------------ seeds from the Bermudan cash flows
 struct SeedParams {
     int nper, N, P, T_slot, callable, freeze_adjustment, pass;
@@ -783,6 +849,25 @@ int launch_replay_dispatch(const ReplayParams& a, const AdjTables<R>& tb, cudaSt
     return LMM_OK;
 }
 
+template <int NMAX, int FMAX>
+void launch_replay32_t(const Replay32Params& q, bool capped, cudaStream_t s)
+{
+    const int blocks = (q.P + 127) / 128;
+    if (capped) replay32_kernel<NMAX, FMAX, true><<<blocks, 128, 0, s>>>(q);
+    else replay32_kernel<NMAX, FMAX, false><<<blocks, 128, 0, s>>>(q);
+}
+
+// the row table's pitch follows the path kernel's (forward rates, factors) template, which the
+// same bounds select
+int launch_replay32(const Replay32Params& q, bool capped, cudaStream_t s)
+{
+    if (q.N <= 24 && q.F <= 4) launch_replay32_t<24, 4>(q, capped, s);
+    else if (q.N <= 40 && q.F <= 10) launch_replay32_t<40, 10>(q, capped, s);
+    else return fail(LMM_ERR_INVALID, "adjoint supports at most 40 forward rates and 10 factors");
+    LMM_CUDA(cudaGetLastError());
+    return LMM_OK;
+}
+
 template <typename R>
 int reverse_sweeps(const AdjointLaunch& L, const AdjTables<R>& tb, cudaStream_t s)
 {
@@ -830,7 +915,26 @@ int reverse_sweeps(const AdjointLaunch& L, const AdjTables<R>& tb, cudaStream_t 
         q.n0 = n0;
         q.n_stop = (sgi == nseg - 1) ? n1 : n1 - 1;  // the last segment also needs the state at t_end
         q.ckpt_slot = static_cast<const R*>(L.d_ckpt) + (size_t)sgi * L.N * L.P;
-        int rc = launch_replay_dispatch<R>(q, tb, s);
+        int rc;
+        if (sizeof(R) == 4 && L.d_rows32 && !L.normal) {
+            Replay32Params q32;
+            q32.N = L.N;
+            q32.F = L.F;
+            q32.P = L.P;
+            q32.n0 = q.n0;
+            q32.n_stop = q.n_stop;
+            q32.n_eff = L.n_eff;
+            q32.cap = (float)L.cap;
+            q32.first = L.d_first;
+            q32.ckpt_slot = static_cast<const float*>(q.ckpt_slot);
+            q32.rows32 = L.d_rows32;
+            q32.dt32 = L.d_dt32;
+            q32.dw = static_cast<const float*>(L.d_dw);
+            q32.seg = static_cast<float*>(L.d_seg);
+            rc = launch_replay32(q32, rp.capped != 0, s);
+        } else {
+            rc = launch_replay_dispatch<R>(q, tb, s);
+        }
         if (rc) return rc;
         rp.n_lo = n0;
         rp.n_hi = n1;

@@ -1255,6 +1255,8 @@ static int european_gradient(lmm_process* pr, int t_index, int n_eff, int stride
     L.d_var_half = pr->d_adj_var_half;
     L.d_inv_delta = pr->d_adj_inv_delta;
     L.d_dt = pr->d_adj_dt;
+    L.d_rows32 = pr->d_lam32;  // FP32 processes: the path kernel's rows and steps (replay)
+    L.d_dt32 = pr->d_dt32;
     L.d_seeds = pr->d_seeds;
     L.d_vega_partials = pr->d_vega_partials;
     L.d_delta_partials = pr->d_delta_partials;
@@ -1399,6 +1401,8 @@ int lmm_bermudan_get_gradient_aad(lmm_process* pr, const lmm_bermudan_desc* d, i
     L.d_var_half = pr->d_adj_var_half;
     L.d_inv_delta = pr->d_adj_inv_delta;
     L.d_dt = pr->d_adj_dt;
+    L.d_rows32 = pr->d_lam32;  // FP32 processes: the path kernel's rows and steps (replay)
+    L.d_dt32 = pr->d_dt32;
     L.d_abar = pr->d_abar;
     L.d_abar_partials = pr->d_abar_partials;
     L.d_seeds = pr->d_seeds;
@@ -1641,6 +1645,8 @@ static int portfolio_enqueue(lmm_portfolio* pf, int q, PortfolioBranch& b)
         L.d_var_half = pr->d_adj_var_half;
         L.d_inv_delta = pr->d_adj_inv_delta;
         L.d_dt = pr->d_adj_dt;
+        L.d_rows32 = pr->d_lam32;  // FP32 processes: the path kernel's rows and steps (replay)
+        L.d_dt32 = pr->d_dt32;
         L.d_abar = b.abar;
         L.d_abar_partials = b.abar_partials;
         L.d_seeds = b.seeds;

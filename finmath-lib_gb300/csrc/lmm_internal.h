@@ -297,6 +297,8 @@ struct AdjointLaunch {
     void* d_seg;                   // stride > 1: [stride+1][N][P] replayed forward rates of a segment
     void* d_ybar;                  // stride > 1: [N][P] adjoint of log L between segments
     const void *d_lam, *d_f, *d_sigma, *d_var_half, *d_inv_delta, *d_dt;  // tables in the path precision
+    const float* d_rows32;         // FP32 processes: the mixed path kernel's component rows [T][N][pitch]
+    const float* d_dt32;           // and its time steps [T] (the replay runs the path kernel's own step)
     double *d_abar, *d_abar_partials, *d_seeds, *d_value_partials, *d_value_out;
     double* d_nb;                  // [N+1][P] adjoints of the adjusted numeraires (scratch)
     double *d_vega_partials, *d_delta_partials, *d_vegas, *d_deltas;

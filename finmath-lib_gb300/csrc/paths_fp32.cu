@@ -24,15 +24,14 @@
 #include "fp64math.cuh"
 #include "reduce.cuh"
 #include "unroll_range.cuh"
+#include "euler_fp32.cuh"
 
 namespace lmm {
 namespace {
 
 constexpr int kPathThreads = 128;
 
-// row pitch of the staged component rows: FMAX loadings, the drift term and 1/delta,
-// rounded up to whole float4 vectors
-__host__ __device__ constexpr int row_pitch(int fmax) { return (fmax + 2 + 3) / 4 * 4; }
+using euler32::row_pitch;
 
 __device__ __forceinline__ void cp_async4(float* dst, const float* src)
 {
@@ -44,23 +43,6 @@ __device__ __forceinline__ void cp_async16(float* dst, const float* src)
     const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
 }
-// The SFU's approximate reciprocal and base-2 exponential with flush-to-zero, one MUFU
-// instruction each: the arguments here (L + 1/delta in (0, 1e5 + 2], and the step
-// increment times log2 e) are normal numbers far from the range edges that __fdividef and
-// __expf guard with extra compares, selects and scalings.
-__device__ __forceinline__ float rcp_approx(float x)
-{
-    float r;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-    return r;
-}
-__device__ __forceinline__ float exp2_approx(float x)
-{
-    float r;
-    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-    return r;
-}
-
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
@@ -134,7 +116,7 @@ __global__ void __launch_bounds__(kPathThreads, fp32_min_blocks(NMAX))
     for (int i = 0; i < a.T; i++) {
         const int first = __ldg(a.d_first + i);
         // the step's sums in base-2 units: G and dt carry log2(e), so that exp(d) = exp2(d')
-        const float dt = __ldg(a.d_dt32 + i) * 1.4426950408889634f;
+        const float dt = euler32::step_dt(a.d_dt32, i);
         cp_async_wait();
         __syncwarp();  // the warp's staged table of step i is visible to every lane
         // G_k = dW_k + dt S_k, the drift's running sum S_k = sum_{l<=j} os_l lambda_lk carried
@@ -144,9 +126,8 @@ __global__ void __launch_bounds__(kPathThreads, fp32_min_blocks(NMAX))
 #pragma unroll
         for (int m = 0; m < FH; m++) {
             const int k0 = 2 * m, k1 = 2 * m + 1;
-            G2[m].x = (k0 < F && active) ? sm.dw[i & 1][k0][tid] : 0.0f;
-            G2[m].y = (k1 < F && k1 < FMAX && active) ? sm.dw[i & 1][k1 < FMAX ? k1 : 0][tid] : 0.0f;
-            G2[m] = __fmul2_rn(G2[m], make_float2(1.4426950408889634f, 1.4426950408889634f));
+            G2[m] = euler32::start_sum((k0 < F && active) ? sm.dw[i & 1][k0][tid] : 0.0f,
+                                       (k1 < F && k1 < FMAX && active) ? sm.dw[i & 1][k1 < FMAX ? k1 : 0][tid] : 0.0f);
         }
         if (i + 1 < a.T) prefetch(i + 1);  // buffers (i+1)&1 were last read in step i-1
         const float* tb = sm.table[warp][i & 1];
@@ -162,26 +143,7 @@ __global__ void __launch_bounds__(kPathThreads, fp32_min_blocks(NMAX))
                     lr[4 * q + 2] = v.z;
                     lr[4 * q + 3] = v.w;
                 }
-                const float Lj = L[j];
-                const float osdt = (Lj * dt) * rcp_approx(Lj + lr[FMAX + 1]);
-                const float2 os2 = make_float2(osdt, osdt);
-                float2 da, db = make_float2(0.0f, 0.0f);
-#pragma unroll
-                for (int m = 0; m < FH; m++) {
-                    // factors 2m and 2m+1 (the rows are zero padded beyond F; for an odd FMAX
-                    // the last pair's second entry is the drift term, multiplied by G = 0)
-                    const float2 l2 = make_float2(lr[2 * m], 2 * m + 1 < FMAX ? lr[2 * m + 1] : 0.0f);
-                    G2[m] = __ffma2_rn(os2, l2, G2[m]);
-                    if (m == 0) da = __fmul2_rn(G2[m], l2);
-                    else if (m == 1) db = __fmul2_rn(G2[m], l2);
-                    else if (m & 1) db = __ffma2_rn(G2[m], l2, db);
-                    else da = __ffma2_rn(G2[m], l2, da);
-                }
-                // exp(d) = 2^d' with d' = d log2(e) (G, dt and the drift term carry the factor)
-                const float2 s2 = __fadd2_rn(da, db);
-                float v = Lj * exp2_approx((s2.x + s2.y) + lr[FMAX]);
-                if (CAPPED) v = fminf(v, cap);
-                L[j] = v;
+                L[j] = euler32::component_step<FMAX, CAPPED>(L[j], lr, dt, G2, cap);
             }
         });
         const int slot = __ldg(a.d_obs_slot + i + 1);

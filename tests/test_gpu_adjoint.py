@@ -4,7 +4,7 @@ Bermudan swaption against finite differences.
 1. Exact check: the FP64 adjoint equals central finite differences (bump 1e-5, common
    random numbers) of the oracle's frozen-exercise Bermudan value -- the pathwise
    derivative the adjoint computes -- to 1e-6.
-2. The checkpoint stride does not change the result.
+2. The checkpoint stride does not change the result (in the mixed form, not by one bit).
 3. The mixed-precision adjoint agrees with the FP64 adjoint.
 4. Statistical check: full central finite differences on the GPU (regression re-run in
    every bumped valuation, common random numbers) agree with the adjoint within 2 % or
@@ -89,6 +89,22 @@ def test_checkpoint_stride_invariance(lmm20):
         g = lmm20["berm"].getGradient(lmm20["sim"], checkpointStride=stride)
         assert np.allclose(g["deltas"], lmm20["g"]["deltas"], rtol=1e-12, atol=1e-15)
         assert np.allclose(g["vegas"], lmm20["g"]["vegas"], rtol=1e-12, atol=1e-15)
+
+
+def test_mixed_precision_checkpoint_stride_is_exact(lmm20):
+    """The mixed form replays the steps between checkpoints with the FP32 path kernel's own
+    component step on its own tables, so the replayed forward rates are the stored ones bit
+    for bit; the reverse sweep's partition and order of sums do not depend on the stride, so
+    the Greeks at strides 3 and 8 equal those at stride 1 exactly."""
+    sim = W.build(lmm20["cfg"], paths=lmm20["P"], precision=F.PRECISION_MIXED)
+    g1 = lmm20["berm"].getGradient(sim, checkpointStride=1)
+    for stride in (3, 8):
+        g = lmm20["berm"].getGradient(sim, checkpointStride=stride)
+        assert g["value"] == g1["value"]
+        assert np.array_equal(g["deltas"], g1["deltas"])
+        assert np.array_equal(g["vegas"], g1["vegas"])
+    sim.process.close()
+    sim.process.brownianMotion.close()
 
 
 def test_mixed_precision_adjoint_close_to_fp64(lmm20):
