@@ -245,6 +245,10 @@ __global__ void __launch_bounds__(TH, rev_min_blocks<R, TH>()) reverse_kernel(co
     const R* states = static_cast<const R*>(a.states);
     const R* dW = static_cast<const R*>(tb.dw);
     const R cap = (R)a.cap;
+    // 1/delta_j, read in every iteration of both component passes
+    __shared__ R inv_delta_s[NMAX];
+    for (int j = tid; j < NMAX; j += TH) inv_delta_s[j] = j < NE ? tb.inv_delta[j] : R(1);
+    __syncthreads();
 
     for (int base = blockIdx.x * TH; base < a.P; base += gridDim.x * TH) {
         const int p = base + tid;
@@ -311,7 +315,7 @@ __global__ void __launch_bounds__(TH, rev_min_blocks<R, TH>()) reverse_kernel(co
                 Rk[m] = Pair<R>::mk(R(0), R(0));
             }
             // os_j = L/(L + 1/d) (LOGNORMAL) or d/(1 + d L) = 1/(L + 1/d) (NORMAL)
-            auto os_of = [&](int j, R L) { return fdiv<R>(a.normal ? R(1) : L, L + tb.inv_delta[j]); };
+            auto os_of = [&](int j, R L) { return fdiv<R>(a.normal ? R(1) : L, L + inv_delta_s[j]); };
             // forward pass of the step: S_k = sum_j os_j sigma_j f_jk
             unsigned long long capmask = 0ull;  // capped models have at most 64 components
 #pragma unroll 2
@@ -491,15 +495,25 @@ __global__ void __launch_bounds__(128) replay32_kernel(const Replay32Params a)
         L[j] = j < NE ? a.ckpt_slot[(size_t)j * P + p] : 0.0f;
         if (j < NE) a.seg[(size_t)j * P + p] = L[j];
     }
+    // the increments of step n, loaded one step ahead
+    float wn[FMAX];
+    auto load_dw = [&](int n) {
+#pragma unroll
+        for (int k = 0; k < FMAX; k++) wn[k] = k < F ? a.dw[((size_t)n * F + k) * P + p] : 0.0f;
+    };
+    if (a.n0 < a.n_stop) load_dw(a.n0);
     for (int n = a.n0; n < a.n_stop; n++) {
         const int first = __ldg(a.first + n);
         const float dt = euler32::step_dt(a.dt32, n);
         float2 G2[FH];
 #pragma unroll
-        for (int m = 0; m < FH; m++) {
-            const int k0 = 2 * m, k1 = 2 * m + 1;
-            G2[m] = euler32::start_sum(k0 < F ? a.dw[((size_t)n * F + k0) * P + p] : 0.0f,
-                                       (k1 < F && k1 < FMAX) ? a.dw[((size_t)n * F + (k1 < FMAX ? k1 : 0)) * P + p] : 0.0f);
+        for (int m = 0; m < FH; m++) G2[m] = euler32::start_sum(wn[2 * m], 2 * m + 1 < FMAX ? wn[2 * m + 1] : 0.0f);
+        if (n + 1 < a.n_stop) {
+            load_dw(n + 1);
+            // the next step's rows into L1 (one 128-byte line per lane of the first warp)
+            const char* nrows = reinterpret_cast<const char*>(a.rows32 + (size_t)(n + 1) * N * FP);
+            for (int q = threadIdx.x; q < (N * FP * (int)sizeof(float) + 127) / 128; q += 128)
+                asm volatile("prefetch.global.L1 [%0];" ::"l"(nrows + 128 * q));
         }
         const float4* rows = reinterpret_cast<const float4*>(a.rows32 + (size_t)n * N * FP);
         for_up_from<NMAX>(first, [&](auto jc) {
