@@ -947,7 +947,17 @@ int reverse_sweeps(const AdjointLaunch& L, const AdjTables<R>& tb, cudaStream_t 
             q32.seg = static_cast<float*>(L.d_seg);
             rc = launch_replay32(q32, rp.capped != 0, s);
         } else {
-            rc = launch_replay_dispatch<R>(q, tb, s);
+            rc = kReplayNotFast;
+            if (sizeof(R) == 8 && L.path64) {
+                ReplaySegment seg;
+                seg.n0 = q.n0;
+                seg.n_stop = q.n_stop;
+                seg.n_eff = L.n_eff;
+                seg.ckpt = static_cast<const double*>(q.ckpt_slot);
+                seg.seg = static_cast<double*>(L.d_seg);
+                rc = launch_replay_fp64(*L.path64, seg, s);
+            }
+            if (rc == kReplayNotFast) rc = launch_replay_dispatch<R>(q, tb, s);
         }
         if (rc) return rc;
         rp.n_lo = n0;

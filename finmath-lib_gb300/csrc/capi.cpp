@@ -605,25 +605,11 @@ int lmm_process_set_observed_times(lmm_process* pr, const uint8_t* mask)
     return LMM_OK;
 }
 
-static int process_ensure(lmm_process* pr)
+// the path kernels' launch parameters of a process (checkpoints and 1/N set by the caller)
+static PathLaunch path_launch_of(lmm_process* pr)
 {
-    if (pr->simulated && pr->bm->generated && pr->bm_generation == pr->bm->generation &&
-        pr->ckpt_stride == pr->want_ckpt)
-        return LMM_OK;
-    int rc = brownian_ensure(pr->bm);
-    if (rc) return rc;
-    cudaStream_t s = pr->stream;
-    const size_t esz = pr->precision == LMM_PRECISION_FP64 ? sizeof(double) : sizeof(float);
-    pr->path_blocks = path_blocks(pr->P);
-    if (!pr->d_obs_slot) {
-        if (!rc) rc = upload(&pr->d_obs_slot, pr->obs_slot.data(), pr->obs_slot.size(), s);
-        if (!rc) rc = dalloc((unsigned char**)&pr->d_states, (size_t)pr->nobs * pr->N * (size_t)pr->P * esz, s);
-        if (!rc) rc = dalloc(&pr->d_numeraire, (size_t)(pr->N + 1) * pr->P, s);
-        if (!rc) rc = dalloc(&pr->d_partials, (size_t)pr->path_blocks * pr->N * 2, s);
-        if (!rc) rc = dalloc(&pr->d_num_adj, (size_t)(pr->N + 1), s);
-        if (rc) return rc;
-    }
     PathLaunch a;
+    std::memset(&a, 0, sizeof(a));
     a.T = pr->T;
     a.N = pr->N;
     a.F = pr->F;
@@ -655,6 +641,28 @@ static int process_ensure(lmm_process* pr)
     a.d_inv_numeraire = nullptr;
     a.d_inv_num_partials = pr->d_partials;
     a.num_det_prefix = pr->num_det_prefix;
+    return a;
+}
+
+static int process_ensure(lmm_process* pr)
+{
+    if (pr->simulated && pr->bm->generated && pr->bm_generation == pr->bm->generation &&
+        pr->ckpt_stride == pr->want_ckpt)
+        return LMM_OK;
+    int rc = brownian_ensure(pr->bm);
+    if (rc) return rc;
+    cudaStream_t s = pr->stream;
+    const size_t esz = pr->precision == LMM_PRECISION_FP64 ? sizeof(double) : sizeof(float);
+    pr->path_blocks = path_blocks(pr->P);
+    if (!pr->d_obs_slot) {
+        if (!rc) rc = upload(&pr->d_obs_slot, pr->obs_slot.data(), pr->obs_slot.size(), s);
+        if (!rc) rc = dalloc((unsigned char**)&pr->d_states, (size_t)pr->nobs * pr->N * (size_t)pr->P * esz, s);
+        if (!rc) rc = dalloc(&pr->d_numeraire, (size_t)(pr->N + 1) * pr->P, s);
+        if (!rc) rc = dalloc(&pr->d_partials, (size_t)pr->path_blocks * pr->N * 2, s);
+        if (!rc) rc = dalloc(&pr->d_num_adj, (size_t)(pr->N + 1), s);
+        if (rc) return rc;
+    }
+    PathLaunch a = path_launch_of(pr);
     a.d_ckpt = nullptr;
     a.ckpt_stride = 0;
     if (pr->want_ckpt > 0) {
@@ -1232,6 +1240,8 @@ static int european_gradient(lmm_process* pr, int t_index, int n_eff, int stride
     if ((rc = seeds(v, delta.data()))) return rc;
     AdjointLaunch L;
     std::memset(&L, 0, sizeof(L));
+    const PathLaunch path64 = path_launch_of(pr);  // FP64: the replay runs the path kernel's own step
+    if (pr->precision == LMM_PRECISION_FP64) L.path64 = &path64;
     L.T = T;
     L.N = N;
     L.F = pr->F;
@@ -1360,6 +1370,8 @@ int lmm_bermudan_get_gradient_aad(lmm_process* pr, const lmm_bermudan_desc* d, i
     for (int j = 0; j < N; j++) delta[j] = pr->tenor[j + 1] - pr->tenor[j];
     AdjointLaunch L;
     std::memset(&L, 0, sizeof(L));
+    const PathLaunch path64 = path_launch_of(pr);  // FP64: the replay runs the path kernel's own step
+    if (pr->precision == LMM_PRECISION_FP64) L.path64 = &path64;
     L.T = T;
     L.N = N;
     L.F = pr->F;
@@ -1607,6 +1619,8 @@ static int portfolio_enqueue(lmm_portfolio* pf, int q, PortfolioBranch& b)
         for (int j = 0; j < N; j++) delta[j] = pr->tenor[j + 1] - pr->tenor[j];
         AdjointLaunch L;
         std::memset(&L, 0, sizeof(L));
+        const PathLaunch path64 = path_launch_of(pr);  // FP64: the replay runs the path kernel's own step
+        if (pr->precision == LMM_PRECISION_FP64) L.path64 = &path64;
         L.T = T;
         L.N = N;
         L.F = pr->F;

@@ -140,8 +140,24 @@ struct PathLaunch {
     int num_det_prefix;        // numeraire deterministic for l < num_det_prefix
     void* d_ckpt;              // [T/stride+1][N][P] path state every ckpt_stride steps (nullptr: none)
     int ckpt_stride;           // forward rates L every ckpt_stride steps (in the path precision)
+    // the adjoint's replay (FP64 fast kernel): steps [rp_n0, rp_n_stop) from rp_ckpt [N][P],
+    // the rates of components below rp_n_eff into rp_seg [rp_n_stop - rp_n0 + 1][N][P]
+    int rp_n0, rp_n_stop, rp_n_eff;
+    const double* rp_ckpt;
+    double* rp_seg;
 };
 int launch_paths_fp64(const PathLaunch& a, cudaStream_t s, int* blocks_out);
+// The adjoint's replay of the steps [n0, n_stop) of an FP64 process from its checkpoint at
+// n0 with the fast path kernel's own step (bit for bit the stored rates): seg[n - n0][j][p]
+// for the components j < n_eff.  Returns kReplayNotFast where the simulation did not run the
+// fast kernel (another scheme, measure or state space, or EULER with a cap).
+struct ReplaySegment {
+    int n0, n_stop, n_eff;
+    const double* ckpt;  // [N][P]
+    double* seg;         // [n_stop - n0 + 1][N][P]
+};
+constexpr int kReplayNotFast = -1000;
+int launch_replay_fp64(const PathLaunch& a, const ReplaySegment& r, cudaStream_t s);
 // row pitch (floats) of the FP64 fast kernel's double-float rows, and the FMAX the launcher
 // instantiates for N forward rates and F factors
 __host__ __device__ constexpr int fp64_df_pitch(int fmax) { return (2 * fmax + 4 + 3) / 4 * 4; }
@@ -297,6 +313,7 @@ struct AdjointLaunch {
     void* d_seg;                   // stride > 1: [stride+1][N][P] replayed forward rates of a segment
     void* d_ybar;                  // stride > 1: [N][P] adjoint of log L between segments
     const void *d_lam, *d_f, *d_sigma, *d_var_half, *d_inv_delta, *d_dt;  // tables in the path precision
+    const PathLaunch* path64;      // FP64 processes: the path kernel's launch (the replay runs its own step)
     const float* d_rows32;         // FP32 processes: the mixed path kernel's component rows [T][N][pitch]
     const float* d_dt32;           // and its time steps [T] (the replay runs the path kernel's own step)
     double *d_abar, *d_abar_partials, *d_seeds, *d_value_partials, *d_value_out;

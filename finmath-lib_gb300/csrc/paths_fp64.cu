@@ -28,4 +28,18 @@ int launch_paths_fp64(const PathLaunch& a, cudaStream_t s, int* blocks_out)
     return fail(LMM_ERR_INVALID, "FP64 path kernel supports at most 80 forward rates and 16 factors");
 }
 
+int launch_replay_fp64(const PathLaunch& path, const ReplaySegment& r, cudaStream_t s)
+{
+    PathLaunch a = path;
+    a.rp_n0 = r.n0;
+    a.rp_n_stop = r.n_stop;
+    a.rp_n_eff = r.n_eff;
+    a.rp_ckpt = r.ckpt;
+    a.rp_seg = r.seg;
+    const int blocks = path_blocks(a.P);
+    if (a.N <= 24 && a.F <= 4) return replay_t<24, 4>(a, s, blocks);
+    if (a.N <= 40 && a.F <= 10) return replay_t<40, 10>(a, s, blocks);
+    return kReplayNotFast;
+}
+
 }  // namespace lmm

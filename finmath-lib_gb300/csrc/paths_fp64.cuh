@@ -37,6 +37,8 @@
 #pragma once
 
 #include "dfloat.cuh"
+#include <cmath>
+
 #include "fp64math.cuh"
 #include "lmm_internal.h"
 #include "reduce.cuh"
@@ -96,7 +98,12 @@ __host__ __device__ constexpr int fp64_min_blocks(int nmax, bool functional)
 // checks.  With the state in registers the loop enters its unrolled sequence at the first
 // alive component through a jump table (unroll_range.cuh); with the state in shared memory
 // it is a rolled loop.
-template <int NMAX, int FMAX, bool FUNCTIONAL, bool EXACT>
+// REPLAY: the adjoint's replay of the steps [rp_n0, rp_n_stop) from the checkpoint rp_ckpt,
+// with the same step code, so that the replayed forward rates equal the stored ones bit for
+// bit; it writes the rates of every step of the segment (components below rp_n_eff) and no
+// numeraire.  EULER (not FUNCTIONAL) restarts exp(Y) from the stored rate: exact when
+// uncapped only.
+template <int NMAX, int FMAX, bool FUNCTIONAL, bool EXACT, bool REPLAY = false>
 __global__ void __launch_bounds__(kPathThreads, fp64_min_blocks(NMAX, FUNCTIONAL)) paths_fp64_kernel(const PathLaunch a)
 {
     static_assert(FMAX % 2 == 0, "factors run in pairs");
@@ -122,8 +129,18 @@ __global__ void __launch_bounds__(kPathThreads, fp64_min_blocks(NMAX, FUNCTIONAL
     PathState<NMAX, SMEM> L;
     if constexpr (SMEM) L.col = &state_smem[0][threadIdx.x];
     double E[FUNCTIONAL ? 1 : NMAX];  // EULER: exp of the uncapped log state Y
+    if constexpr (REPLAY) {
+#pragma unroll
+        for (int j = 0; j < NMAX; j++) {
+            const double v = (j < N && active) ? a.rp_ckpt[(size_t)j * P + p] : 0.0;
+            L[j] = v;
+            if (!FUNCTIONAL) E[FUNCTIONAL ? 0 : j] = v;
+            if (j < a.rp_n_eff && active) a.rp_seg[(size_t)j * P + p] = v;
+        }
+    }
 #pragma unroll
     for (int j = 0; j < NMAX; j++) {
+        if (REPLAY) break;
         if (j < N) {
             // getInitialState (:1081-1093) and applyStateSpaceTransform (:1200-1212):
             // exp(log(max(f,0))), the same for every path, from the host
@@ -134,7 +151,7 @@ __global__ void __launch_bounds__(kPathThreads, fp64_min_blocks(NMAX, FUNCTIONAL
             L[j] = 0.0;
         }
     }
-    {
+    if (!REPLAY) {
         const int slot = __ldg(a.d_obs_slot + 0);
         if (slot >= 0 && active) {
 #pragma unroll
@@ -149,7 +166,8 @@ __global__ void __launch_bounds__(kPathThreads, fp64_min_blocks(NMAX, FUNCTIONAL
         }
     }
 
-    for (int i = 0; i < a.T; i++) {
+    const int i_end = REPLAY ? a.rp_n_stop : a.T;
+    for (int i = REPLAY ? a.rp_n0 : 0; i < i_end; i++) {
         const int first = __ldg(a.d_first + i);
         const float dth = __ldg(a.d_dt_df + 2 * i), dtl = __ldg(a.d_dt_df + 2 * i + 1);
         const float4* rows = reinterpret_cast<const float4*>(a.d_rows_df + (size_t)i * N * FPD);
@@ -171,7 +189,7 @@ __global__ void __launch_bounds__(kPathThreads, fp64_min_blocks(NMAX, FUNCTIONAL
         // the next step's component rows into this SM's L1 (one 128-byte line per thread; the
         // first warp of every SM to reach a step would otherwise wait on their L2 round trips)
         // and this path's next increments into L2
-        if (i + 1 < a.T) {
+        if (i + 1 < i_end) {
             const int row_lines = (N * FPD * (int)sizeof(float) + 127) / 128;
             const char* nrows = reinterpret_cast<const char*>(a.d_rows_df + (size_t)(i + 1) * N * FPD);
             for (int q = threadIdx.x; q < row_lines; q += kPathThreads)
@@ -282,6 +300,15 @@ __global__ void __launch_bounds__(kPathThreads, fp64_min_blocks(NMAX, FUNCTIONAL
         } else {
             for_up_from<NMAX>(first, component_step);
         }
+        if constexpr (REPLAY) {
+            if (active) {
+                double* out = a.rp_seg + (size_t)(i + 1 - a.rp_n0) * N * P + p;
+#pragma unroll
+                for (int j = 0; j < NMAX; j++)
+                    if (j < a.rp_n_eff) out[(size_t)j * P] = L[j];
+            }
+            continue;
+        }
         const int slot = __ldg(a.d_obs_slot + i + 1);
         if (slot >= 0 && active) {
 #pragma unroll
@@ -295,6 +322,7 @@ __global__ void __launch_bounds__(kPathThreads, fp64_min_blocks(NMAX, FUNCTIONAL
                 if (j < N) ck[(size_t)j * P + p] = L[j];
         }
     }
+    if constexpr (REPLAY) return;
 
     // Spot numeraire from the frozen fixings L_l(T_l) (:1050-1066): Scalar.accrue while
     // the numeraire is deterministic, RandomVariableFromDoubleArray.accrue afterwards.  The
@@ -510,6 +538,24 @@ __global__ void __launch_bounds__(kPathThreads) paths_fp64_general_kernel(const 
         if (a.d_inv_numeraire && active) a.d_inv_numeraire[(size_t)l * P + p] = r;
         block_dd_partial(active ? r * N0 : 0.0, a.d_inv_num_partials + ((size_t)blockIdx.x * N + (l - 1)) * 2);
     }
+}
+
+// the fast kernel's template choice of launch_t, as a replay; kReplayNotFast where the
+// forward simulation ran another kernel (or EULER with a cap)
+template <int NMAX, int FMAX>
+int replay_t(const PathLaunch& a, cudaStream_t s, int blocks)
+{
+    if (a.scheme > 1 || a.measure != 0 || a.state_space != 0) return kReplayNotFast;
+    if (a.scheme == 1 && a.N == NMAX)
+        paths_fp64_kernel<NMAX, FMAX, true, true, true><<<blocks, kPathThreads, 0, s>>>(a);
+    else if (a.scheme == 1)
+        paths_fp64_kernel<NMAX, FMAX, true, false, true><<<blocks, kPathThreads, 0, s>>>(a);
+    else if (std::isinf(a.libor_cap) && a.libor_cap > 0.0)
+        paths_fp64_kernel<NMAX, FMAX, false, false, true><<<blocks, kPathThreads, 0, s>>>(a);
+    else
+        return kReplayNotFast;
+    LMM_CUDA(cudaGetLastError());
+    return LMM_OK;
 }
 
 template <int NMAX, int FMAX>
