@@ -257,8 +257,10 @@ int lmm_values_mean_stderr_noalloc(const double* d_values, int64_t num_values, v
  * (LIBORMarketModelNormalAADSensitivitiesTest.java:343-355, 431-434).  A hand-written adjoint
  * of the Euler step (LOGNORMAL: in log coordinates; NORMAL, FP64 processes, uncapped: on the
  * forwards themselves) replays each path backward from checkpoints written every
- * checkpoint_stride steps (1..16); exercise decisions are frozen from the forward
- * valuation.  freeze_numeraire_adjustment = 1 treats the numeraire adjustment's path
+ * checkpoint_stride steps (1..16); the steps between checkpoints are recomputed by the
+ * path kernel's own step, so the stride trades memory for time without changing a bit of
+ * the result (LOGNORMAL SPOT Euler processes; other FP64 forms replay in plain FP64);
+ * exercise decisions are frozen from the forward valuation.  freeze_numeraire_adjustment = 1 treats the numeraire adjustment's path
  * average as a constant, as the reference's AAD does (RandomVariableDifferentiableAAD
  * getAverage returns a double); 0 differentiates through it (the derivative that central
  * finite differences of the value measure).
