@@ -17,8 +17,11 @@
 //
 // so a reverse step costs O(N F) like the forward one.  The forward rates come from the
 // path kernel's checkpoints: with stride 1 (the default: HBM holds every state) one sweep
-// reads them directly; with a larger stride a replay kernel regenerates each segment from
-// its checkpoint into a global buffer before that segment's sweep.  The Bermudan's exercise
+// reads them directly; with a larger stride each segment is regenerated from its
+// checkpoint into a global buffer before that segment's sweep, by the path kernels' own
+// step (the FP32 component step of euler_fp32.cuh; the FP64 fast kernel's REPLAY
+// instantiation), so the regenerated rates are the stored ones bit for bit and the Greeks
+// do not depend on the stride.  The Bermudan's exercise
 // decisions are frozen from the forward valuation (regression coefficients fixed); the seed
 // kernel turns each path's realised cash flows into adjoints of the fixings L_m(T_m),
 // through the payment numeraires, their cross-path adjustment a_l = mean(1/N_l)
