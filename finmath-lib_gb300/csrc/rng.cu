@@ -208,26 +208,6 @@ __device__ __forceinline__ void df_add(float ah, float al, float bh, float bl, f
     df_fast_two_sum(s, (al + bl) + e, sh, sl);
 }
 
-__device__ __forceinline__ void df_mul(float ah, float al, float bh, float bl, float& ph, float& pl)
-{
-    const float p = __fmul_rn(ah, bh);
-    float e = fmaf(ah, bh, -p);
-    e = fmaf(ah, bl, e);
-    e = fmaf(al, bh, e);
-    df_fast_two_sum(p, e, ph, pl);
-}
-
-__device__ __forceinline__ void df_div(float nh, float nl, float dh, float dl, float& yh, float& yl)
-{
-    const float q = __fdiv_rn(nh, dh);
-    const float p = __fmul_rn(q, dh);
-    const float e = fmaf(q, dh, -p);
-    float res = (nh - p) - e;
-    res = res + nl;
-    res = fmaf(-q, dl, res);
-    df_fast_two_sum(q, __fmul_rn(res, __frcp_rn(dh)), yh, yl);
-}
-
 // The logarithm's table: for j = 0..127, r_j = 1/c_j rounded to FP32 with c_j = 1 + (j + 1/2)/128,
 // and -log(r_j) as a float pair (FP64 log, split), built by each generator block in shared
 // memory (FP64 form only).
@@ -665,18 +645,26 @@ __device__ __forceinline__ void increments_loop(const RngParams& prm, uint32_t* 
 // jump per nonzero base-8 digit of the chunk index c, written to states[c][624].  Its own
 // kernel: the jump window (kJumpWindow words of shared memory) would otherwise cap the
 // generator at two blocks per SM.
-__global__ void __launch_bounds__(kRngThreads) mt_jump_kernel(const RngParams prm, uint32_t* states)
+// Block b starts from src[b >> src_shift] (the seeded state when src is null) and applies the
+// digits j_lo..j_hi-1 of the chunk index c = b << idx_shift, writing dst[b].  One launch
+// with all digits moves every chunk by up to three jumps; two levels (the groups of eight
+// chunks by their upper digits, then each chunk from its group by its lowest digit) take at
+// most two jumps per group and one per chunk.
+__global__ void __launch_bounds__(kRngThreads) mt_jump_kernel(const RngParams prm, const uint32_t* src, int src_shift,
+                                                              int idx_shift, int j_lo, int j_hi, uint32_t* dst)
 {
     extern __shared__ __align__(16) uint32_t x[];  // the jump window
     const int tid = threadIdx.x;
-    const int64_t c = blockIdx.x;
+    const int64_t b = blockIdx.x;
+    const int64_t c = b << idx_shift;
     if (c * prm.chunk_values >= prm.num_values) return;
-    for (int i = tid; i < kMtN; i += kRngThreads) x[i] = prm.seeded[i];
+    const uint32_t* s0 = src ? src + (size_t)(b >> src_shift) * kMtN : prm.seeded;
+    for (int i = tid; i < kMtN; i += kRngThreads) x[i] = s0[i];
     __syncthreads();
 
     // jump to word offset 2*v0 = c * stride: apply x^(d 8^j stride) for every nonzero
-    // base-8 digit d of c (position j)
-    for (int j = 0; j < prm.ndigits; j++) {
+    // base-8 digit d of c (position j) in [j_lo, j_hi)
+    for (int j = j_lo; j < j_hi; j++) {
         const int d = (int)((c >> (kJumpDigitBits * j)) & (kJumpBase - 1));
         if (d == 0) continue;
         const int list = j * (kJumpBase - 1) + d - 1;
@@ -714,7 +702,7 @@ __global__ void __launch_bounds__(kRngThreads) mt_jump_kernel(const RngParams pr
         __syncthreads();
     }
 
-    for (int i = tid; i < kMtN; i += kRngThreads) states[c * kMtN + i] = x[i];
+    for (int i = tid; i < kMtN; i += kRngThreads) dst[b * kMtN + i] = x[i];
 }
 
 __global__ void __launch_bounds__(kGenThreads, 3) mt_generate_kernel(const RngParams prm, const uint32_t* states)
@@ -846,13 +834,25 @@ int launch_mt_generate(const RngLaunch& a, cudaStream_t s, int* num_launches)
             (size_t)a.plan->smem_bytes < kStateWords * sizeof(uint32_t) + (size_t)a.values_per_path * K * elem)
             return fail(LMM_ERR_INVALID, "generator plan does not match the increments layout");
     }
+    const bool two_level = prm.ndigits > 1;
     {
-        KernelTimer kt(K_MT_JUMP_GENERATE, s, 2);
-        uint32_t* states = nullptr;  // [chunks][624] chunk start states
-        const int arc = device_alloc(reinterpret_cast<void**>(&states), sizeof(uint32_t) * kMtN * (size_t)a.plan->chunks, s,
+        KernelTimer kt(K_MT_JUMP_GENERATE, s, two_level ? 3 : 2);
+        const int64_t groups = (a.plan->chunks + kJumpBase - 1) >> kJumpDigitBits;
+        uint32_t* states = nullptr;  // [chunks][624] chunk start states, then [groups][624] group states
+        const int arc = device_alloc(reinterpret_cast<void**>(&states),
+                                     sizeof(uint32_t) * kMtN * (size_t)(a.plan->chunks + (two_level ? groups : 0)), s,
                                      "cudaMallocAsync (generator chunk states)");
         if (arc) return arc;
-        mt_jump_kernel<<<(unsigned)a.plan->chunks, kRngThreads, (size_t)kJumpWindow * 4, s>>>(prm, states);
+        if (two_level) {
+            uint32_t* gstates = states + (size_t)a.plan->chunks * kMtN;
+            mt_jump_kernel<<<(unsigned)groups, kRngThreads, (size_t)kJumpWindow * 4, s>>>(prm, nullptr, 0, kJumpDigitBits, 1,
+                                                                                          prm.ndigits, gstates);
+            mt_jump_kernel<<<(unsigned)a.plan->chunks, kRngThreads, (size_t)kJumpWindow * 4, s>>>(prm, gstates, kJumpDigitBits,
+                                                                                                   0, 0, 1, states);
+        } else {
+            mt_jump_kernel<<<(unsigned)a.plan->chunks, kRngThreads, (size_t)kJumpWindow * 4, s>>>(prm, nullptr, 0, 0, 0,
+                                                                                                   prm.ndigits, states);
+        }
         // the FP64 form with its two tail warps, the FP32 form and the uniforms with the draw warps
         const int threads = prm.mode == 1 ? kGenThreads : kDrawThreads;
         mt_generate_kernel<<<(unsigned)a.plan->chunks, threads, (size_t)a.plan->smem_bytes, s>>>(prm, states);
@@ -861,7 +861,7 @@ int launch_mt_generate(const RngLaunch& a, cudaStream_t s, int* num_launches)
         if (e != cudaSuccess) return cuda_fail(e, "generator launch");
         LMM_CUDA(cudaGetLastError());
     }
-    if (num_launches) (*num_launches) += 2;
+    if (num_launches) (*num_launches) += two_level ? 3 : 2;
     return LMM_OK;
 }
 
