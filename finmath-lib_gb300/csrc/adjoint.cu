@@ -34,6 +34,7 @@
 
 #include "lmm_internal.h"
 #include "reduce.cuh"
+#include "dfloat.cuh"
 #include "euler_fp32.cuh"
 #include "unroll_range.cuh"
 
@@ -467,6 +468,236 @@ __global__ void __launch_bounds__(128) replay_kernel(const ReplayParams a, const
     }
 }
 
+// ------------------------------------------------------------------ FP64 sweep on float pairs
+// The FP64 form's reverse sweep with its arithmetic in double-float pairs on the FP32 pipe
+// (about 2^-44 relative per operation; the FP64 adjoint is checked to 1e-6): the FP64 sweep
+// ran about 60 FP64 fused multiply-adds per component-step on a pipe that issues at 1/64 of
+// the FP32 rate.  Rates, adjoints and increments stay FP64 in memory (split into pairs in
+// integer operations as they are read, rebuilt by one FP64 addition as they are written);
+// the factor pairs' running sums use the path kernel's paired Dot2 step (df_dot_acc2).  The
+// products are explicit __fmul_rn / __fmaf_rn so that FMA contraction cannot break the
+// error-free transforms.
+struct DF {
+    float h, l;
+};
+__device__ __forceinline__ DF df_of(double x)
+{
+    DF r;
+    df_split_int(x, r.h, r.l);
+    return r;
+}
+__device__ __forceinline__ double df_val(DF a) { return f32_to_f64_int(a.h) + f32_to_f64_int(a.l); }
+__device__ __forceinline__ DF df_norm(float s, float e)
+{
+    DF r;
+    r.h = __fadd_rn(s, e);
+    r.l = __fsub_rn(e, __fsub_rn(r.h, s));
+    return r;
+}
+__device__ __forceinline__ DF df_mul(DF a, DF b)
+{
+    const float p = __fmul_rn(a.h, b.h);
+    float e = __fmaf_rn(a.h, b.h, -p);
+    e = __fmaf_rn(a.h, b.l, e);
+    e = __fmaf_rn(a.l, b.h, e);
+    return df_norm(p, e);
+}
+__device__ __forceinline__ DF df_add(DF a, DF b)
+{
+    const float s = __fadd_rn(a.h, b.h);
+    const float z = __fsub_rn(s, a.h);
+    float e = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, z)), __fsub_rn(b.h, z));
+    e = __fadd_rn(e, __fadd_rn(a.l, b.l));
+    return df_norm(s, e);
+}
+__device__ __forceinline__ DF df_neg(DF a) { return DF{-a.h, -a.l}; }
+// n / d for d > 0: the approximate FP32 reciprocal, then the residual's quotient
+__device__ __forceinline__ DF df_div(DF n, DF d)
+{
+    const float r0 = euler32::rcp_approx(d.h);
+    const float q0 = __fmul_rn(n.h, r0);
+    const float p = __fmul_rn(q0, d.h);
+    const float e = __fmaf_rn(q0, d.h, -p);
+    float res = __fsub_rn(__fsub_rn(n.h, p), e);
+    res = __fadd_rn(res, n.l);
+    res = __fmaf_rn(-q0, d.l, res);
+    return df_norm(q0, __fmul_rn(res, r0));
+}
+
+template <int NMAX, int FMAX, int TH>
+__global__ void __launch_bounds__(TH, rev_min_blocks<double, TH>()) reverse_df_kernel(const RevParams a, const AdjTables<double> tb)
+{
+    using R = double;
+    constexpr int FP = f_pitch<R, FMAX>();
+    static_assert(NMAX % 8 == 0 && FMAX % 2 == 0, "chunks of eight components, factor pairs");
+    using V = Vec<R>;
+    constexpr int FH = FMAX / 2;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    R* sbuf = reinterpret_cast<R*>(smem_raw) + tid;  // [NMAX][TH]: the step's forward rates, own column
+    R* ybuf = sbuf + NMAX * TH;                       // [NMAX][TH]: Ybar, own column
+    R* wbuf = ybuf + NMAX * TH;                       // [2][FMAX][TH]: increments, own column
+    const int N = a.N, F = a.F, NE = a.n_eff;
+    const size_t gw = (size_t)blockIdx.x * (TH / 32) + warp;
+    double* vp = a.vega_partials + gw * a.T * N;
+    const R* states = static_cast<const R*>(a.states);
+    const R* dW = static_cast<const R*>(tb.dw);
+    const R cap = a.cap;
+    __shared__ float invd_h[NMAX], invd_l[NMAX];
+    for (int j = tid; j < NMAX; j += TH) {
+        const DF v = df_of(j < NE ? tb.inv_delta[j] : 1.0);
+        invd_h[j] = v.h;
+        invd_l[j] = v.l;
+    }
+    __syncthreads();
+
+    for (int base = blockIdx.x * TH; base < a.P; base += gridDim.x * TH) {
+        const int p = base + tid;
+        const bool active = p < a.P;
+        auto prefetch = [&](int n) {
+            if (active) {
+                const int fst = __ldg(a.first + n);
+                const R* Ls = states + (size_t)(n - a.base_step) * N * a.P + p;
+                for (int j = fst; j < NE; j++) cp_async(sbuf + j * TH, Ls + (size_t)j * a.P);
+                R* wb = wbuf + (n & 1) * FMAX * TH;
+#pragma unroll
+                for (int k = 0; k < FMAX; k++)
+                    if (k < F) cp_async(wb + k * TH, dW + ((size_t)n * F + k) * a.P + p);
+            }
+            cp_async_commit();
+        };
+        prefetch(a.n_hi - 1);
+        if (a.seed) {
+            const R* Ls = states + (size_t)(a.t_end - a.base_step) * N * a.P;
+            for (int j = 0; j < NE; j++) {
+                R yb = R(0);
+                if (active) {
+                    const R sd = static_cast<const R*>(a.seeds)[(size_t)j * a.P + p];
+                    if (a.normal) {
+                        yb = sd;
+                    } else {
+                        const R L = Ls[(size_t)j * a.P + p];
+                        if (!(a.capped && L >= cap)) yb = sd * L;
+                    }
+                }
+                ybuf[j * TH] = yb;
+            }
+        } else {
+            const R* yb = static_cast<const R*>(a.ybar);
+            for (int j = 0; j < NE; j++) ybuf[j * TH] = active ? yb[(size_t)j * a.P + p] : R(0);
+        }
+
+        for (int n = a.n_hi - 1; n >= a.n_lo; n--) {
+            const int first = __ldg(a.first + n);
+            const DF dt = df_of(tb.dt[n]);
+            cp_async_wait();
+            const R* sig = tb.sigma + (size_t)n * N;
+            const R* frow = tb.f + (size_t)n * N * FP;
+            // factor pairs (2m, 2m+1) as float pairs: high parts (lanes x, y) and low parts
+            float2 dwh[FH], dwl[FH], Sh[FH], Sl[FH], Rh[FH], Rl[FH];
+#pragma unroll
+            for (int m = 0; m < FH; m++) {
+                const int k0 = 2 * m, k1 = 2 * m + 1;
+                const DF w0 = df_of((k0 < F && active) ? wbuf[((n & 1) * FMAX + k0) * TH] : R(0));
+                const DF w1 = df_of((k1 < F && active) ? wbuf[((n & 1) * FMAX + k1) * TH] : R(0));
+                dwh[m] = make_float2(w0.h, w1.h);
+                dwl[m] = make_float2(w0.l, w1.l);
+                Sh[m] = Sl[m] = Rh[m] = Rl[m] = make_float2(0.0f, 0.0f);
+            }
+            // os_j = L/(L + 1/d) (LOGNORMAL) or 1/(L + 1/d) (NORMAL)
+            auto os_of = [&](int j, DF L) {
+                const DF den = df_add(L, DF{invd_h[j], invd_l[j]});
+                return df_div(a.normal ? DF{1.0f, 0.0f} : L, den);
+            };
+            // the factor row of component j as pairs (hi, lo, -hi)
+            auto row_of = [&](int j, float2 (&fh)[FH], float2 (&fl)[FH], float2 (&fn)[FH]) {
+                R fr[FP];
+#pragma unroll
+                for (int q = 0; q < FP / V::W; q++) V::unpack(load_row<R>(frow + j * FP, q), fr + q * V::W);
+#pragma unroll
+                for (int m = 0; m < FH; m++) {
+                    const DF f0 = df_of(fr[2 * m]), f1 = df_of(fr[2 * m + 1]);
+                    fh[m] = make_float2(f0.h, f1.h);
+                    fl[m] = make_float2(f0.l, f1.l);
+                    fn[m] = make_float2(-f0.h, -f1.h);
+                }
+            };
+            unsigned long long capmask = 0ull;
+#pragma unroll 2
+            for (int j = first; j < NE; j++) {
+                const R Lr = active ? sbuf[j * TH] : R(0);
+                if (a.capped && Lr >= cap && j < 64) capmask |= 1ull << j;
+                const DF oss = df_mul(os_of(j, df_of(Lr)), df_of(sig[j]));
+                const float2 oh = make_float2(oss.h, oss.h), ol = make_float2(oss.l, oss.l);
+                float2 fh[FH], fl[FH], fn[FH];
+                row_of(j, fh, fl, fn);
+#pragma unroll
+                for (int m = 0; m < FH; m++) df_dot_acc2(Sh[m], Sl[m], oh, ol, fh[m], fl[m], fn[m]);  // S_k += os sigma f_k
+            }
+            for (int c = (NE - 1) >> 3; c >= (first >> 3); c--) {
+                R vch[8];
+#pragma unroll
+                for (int i = 7; i >= 0; i--) {
+                    const int j = 8 * c + i;
+                    vch[i] = R(0);
+                    if (j < NE && j >= first) {
+                        const DF L = df_of(active ? sbuf[j * TH] : R(0));
+                        const DF o = os_of(j, L);
+                        const DF sg = df_of(sig[j]);
+                        const DF yb = df_of(ybuf[j * TH]);
+                        const DF mub = df_mul(yb, dt);
+                        const DF mubs = df_mul(mub, sg);
+                        const DF oss = df_mul(o, sg);
+                        float2 fh[FH], fl[FH], fn[FH];
+                        row_of(j, fh, fl, fn);
+                        const float2 mh = make_float2(mubs.h, mubs.h), ml = make_float2(mubs.l, mubs.l);
+                        const float2 nh = make_float2(-oss.h, -oss.h), nl = make_float2(-oss.l, -oss.l);
+                        float2 Ah = make_float2(0.0f, 0.0f), Al = Ah, Bh = Ah, Bl = Ah, Dh = Ah, Dl = Ah;
+#pragma unroll
+                        for (int m = 0; m < FH; m++) {
+                            df_dot_acc2(Rh[m], Rl[m], mh, ml, fh[m], fl[m], fn[m]);       // R_k += mubar lam_k
+                            df_dot_acc2(Ah, Al, Rh[m], Rl[m], fh[m], fl[m], fn[m]);       // A += R_k f_k
+                            df_dot_acc2(Bh, Bl, Sh[m], Sl[m], fh[m], fl[m], fn[m]);       // B += S^(j)_k f_k
+                            df_dot_acc2(Dh, Dl, dwh[m], dwl[m], fh[m], fl[m], fn[m]);     // D += dW_k f_k
+                            df_dot_acc2(Sh[m], Sl[m], nh, nl, fh[m], fl[m], fn[m]);       // S^(j-1)_k
+                        }
+                        const DF A = df_add(DF{Ah.x, Al.x}, DF{Ah.y, Al.y});
+                        const DF B = df_add(DF{Bh.x, Bl.x}, DF{Bh.y, Bl.y});
+                        const DF D = df_add(DF{Dh.x, Dl.x}, DF{Dh.y, Dl.y});
+                        DF v = df_add(df_add(df_mul(mub, B), df_mul(o, A)), df_mul(yb, D));
+                        if (!a.normal) v = df_add(v, df_neg(mubs));
+                        vch[i] = active ? df_val(v) : R(0);
+                        const DF sa = df_mul(sg, A);
+                        if (a.normal) ybuf[j * TH] = df_val(df_add(yb, df_neg(df_mul(sa, df_mul(o, o)))));
+                        else if (!(a.capped && j < 64 && ((capmask >> j) & 1ull)))
+                            ybuf[j * TH] = df_val(df_add(yb, df_mul(sa, df_mul(o, df_add(DF{1.0f, 0.0f}, df_neg(o))))));
+                    }
+                }
+                const R sum = warp_sum8_transposed<R>(vch, lane);
+                const int r = 8 * c + ((lane >> 2) & 7);
+                if ((lane & 3) == 0 && r < NE && r >= first) atomicAdd(vp + (size_t)n * N + r, sum);
+            }
+            if (n - 1 >= a.n_lo) prefetch(n - 1);
+        }
+
+        if (a.n_lo > 0) {
+            R* yb = static_cast<R*>(a.ybar);
+            if (active)
+                for (int j = 0; j < NE; j++) yb[(size_t)j * a.P + p] = ybuf[j * TH];
+        } else {
+            for (int c = 0; 8 * c < NE; c++) {
+                R v8[8];
+#pragma unroll
+                for (int i = 0; i < 8; i++) v8[i] = (8 * c + i < NE && active) ? ybuf[(8 * c + i) * TH] : R(0);
+                const R sum = warp_sum8_transposed<R>(v8, lane);
+                const int r = 8 * c + ((lane >> 2) & 7);
+                if ((lane & 3) == 0 && r < NE) atomicAdd(a.delta_partials + gw * N + r, a.normal ? sum : sum / a.init[r]);
+            }
+        }
+    }
+    cp_async_wait();
+}
+
 // The mixed form's replay: the steps [n0, n_stop) of every path from the checkpoint at n0 by
 // the FP32 path kernel's own component step (euler_fp32.cuh), on its own rows and time
 // steps, so that every replayed forward rate is bit for bit the one the path kernel computed
@@ -812,12 +1043,20 @@ int launch_rev(const RevParams& a, const AdjTables<R>& tb, int blocks, cudaStrea
 {
     const size_t smem = rev_smem_bytes<R, NMAX, FMAX, TH>();
     static bool attr_set = false;  // set once, before any stream capture
+    // the FP64 form up to 40 forward rates sweeps on float pairs (the 80-rate, two-factor
+    // form keeps the FP64 sweep)
+    constexpr bool kDf = sizeof(R) == 8 && NMAX <= 40;
     if (!attr_set) {
-        LMM_CUDA(cudaFuncSetAttribute(reverse_kernel<R, NMAX, FMAX, TH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)smem));
+        if constexpr (kDf)
+            LMM_CUDA(cudaFuncSetAttribute(reverse_df_kernel<NMAX, FMAX, TH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem));
+        else
+            LMM_CUDA(cudaFuncSetAttribute(reverse_kernel<R, NMAX, FMAX, TH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem));
         attr_set = true;
     }
-    reverse_kernel<R, NMAX, FMAX, TH><<<blocks, TH, smem, s>>>(a, tb);
+    if constexpr (kDf) reverse_df_kernel<NMAX, FMAX, TH><<<blocks, TH, smem, s>>>(a, tb);
+    else reverse_kernel<R, NMAX, FMAX, TH><<<blocks, TH, smem, s>>>(a, tb);
     LMM_CUDA(cudaGetLastError());
     return LMM_OK;
 }
